@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the Feel++ assembly hot path on GB300.
+
+Workload (one "step"): plain FP64 assembly of the P2 Lagrange Laplacian +
+mass matrix, kappa*inner(gradt(u),grad(v)) + idt(u)*id(v), on the 64^3-hex
+Kuhn cube (1 572 864 tets, interior vertices perturbed +-0.15h, lognormal(0,1)
+per-element kappa, quadrature degree 4), into the device CSR with the Feel++
+GraphCSR pattern (2 146 689 rows, 60 859 905 nonzeros). The pattern is built
+once before timing, as Feel++ builds and caches it in form2(). Synthetic
+inputs stand in for the reference's gmsh meshes (seeded generator, same shape).
+
+value  : nnz x steps / device time (CUDA events on the launch stream), Mnnz/s
+e2e    : same metric through the C-ABI with host buffers: per step the vertex
+         coordinates and kappa are copied from pinned host memory, the matrix is
+         assembled, and the assembled CSR values are read back into pinned host
+         memory; wall clock around the steps.
+Also reported: FP32 assembly, and the CG time-to-1e-10 (FP64 PCG vs FP32 inner
+CG + FP64 refinement) on the same system with homogeneous Dirichlet rows.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle; Feel++ itself cannot be built here) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "P2 Laplacian assembly Mnnz/s & CG time-to-1e-10, FP32+refine vs FP64, 1 GB300"
+UNIT = "Mnnz/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=64)
+    p.add_argument("--order", type=int, default=2)
+    p.add_argument("--no-solve", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-n", type=int, default=24)
+    return p.parse_args()
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM traffic of the gather kernel from the committed ncu summary (bytes per nnz)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "assemble_gather_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def build_workload(n, order, env):
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    xyz, tets = meshgen.kuhn_box(n, perturb=0.15, seed=1234)
+    kappa = meshgen.lognormal_kappa(len(tets), seed=5678)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, order)
+    return fpp, xyz, tets, kappa, M, V
+
+
+def cpu_sample(args, nthreads):
+    """The oracle (CPU restatement) timed on a bounded sample: P2 on the cpu_n^3 Kuhn cube."""
+    from feelpp_gb300 import meshgen
+    from oracle import pyoracle as orc
+    xyz, tets = meshgen.kuhn_box(args.cpu_n, perturb=0.15, seed=1234)
+    kappa = meshgen.lognormal_kappa(len(tets), seed=5678)
+    N, l2g = orc.dof_table(tets, args.order)
+    ia, ja = orc.pattern(N, l2g)
+    val = np.zeros(len(ja))
+    t0 = time.perf_counter()
+    orc.assemble(args.order, xyz, tets, l2g, ia, ja, kappa=kappa, mass=1.0, nthreads=nthreads, val=val)
+    dt = time.perf_counter() - t0
+    return len(ja), dt, len(tets)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import pyoracle as orc
+    threads = orc.num_threads()
+    for _ in range(args.warmup):
+        cpu_sample(args, threads)
+    total_nnz, total_t = 0, 0.0
+    for _ in range(args.steps):
+        nnz, dt, nt = cpu_sample(args, threads)
+        total_nnz += nnz
+        total_t += dt
+    v = total_nnz / total_t / 1e6
+    sample = "P2 Laplacian+mass FP64 assembly (quadrature form, PETSc-style sorted-row scatter) of the %d^3 Kuhn cube (%d tets, nnz %d), element colours in parallel" % (args.cpu_n, nt, nnz)
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": total_t / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "P2 Laplacian+mass assembly, Kuhn cube %d^3 (bounded CPU sample of the 64^3 workload)" % args.cpu_n,
+                      "order": args.order},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_gb300(args, rank, world, local):
+    import ctypes as C
+
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import _ffi
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    env = fpp.Environment(device=local, stream=C.c_void_p(stream.cuda_stream), profile=True)
+    fpp_, xyz, tets, kappa, M, V = build_workload(args.n, args.order, env)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    nnz, N, T = a.nnz, V.ndof, len(tets)
+    d_kappa = torch.from_numpy(kappa).to("cuda")
+    lib = env.lib
+    desc = _ffi.FormDesc()
+    desc.kind = _ffi.FORM_LAPLACE_MASS
+    desc.kappa, desc.mass, desc.quad_degree, desc.algo = 0.0, 1.0, 0, _ffi.ALGO_AUTO
+    desc.kappa_elem = None
+    kp = C.c_void_p(d_kappa.data_ptr())
+
+    def step(h):
+        env.check(lib.fgpu_assemble_matrix_dev(env.h, h, C.byref(desc), kp, 0))
+
+    # ---- device-resident throughput (value) ----
+    for _ in range(max(args.warmup, 3)):
+        step(a.h)
+    torch.cuda.synchronize()
+    env.prof_reset()
+    launches0 = env.launches()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(a.h)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms_max = reduce_max(ms, world)
+    launches = env.launches() - launches0
+    g_cnt, g_ms = env.prof("assemble_gather")
+    geo_cnt, geo_ms = env.prof("geometry")
+    value = nnz * args.steps * world / (ms_max / 1e3) / 1e6
+
+    # roofline of the dominant kernel (gather assembly)
+    hbm_peak, peak_kind = load_peaks()
+    n_loc = (args.order + 1) * (args.order + 2) * (args.order + 3) // 6
+    alg_bytes = nnz * (8 + 4) + (N + 1) * 8 * 2 + T * (n_loc * 4 * 2 + 64)
+    per_launch_ms = g_ms / max(g_cnt, 1)
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    tr = load_traffic()
+    traffic = None
+    if tr and tr.get("order") == args.order:
+        traffic = tr["bytes_per_nnz"] * nnz
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "assemble_gather", "kernel_ms": per_launch_ms, "algorithmic_bytes": alg_bytes,
+                "flops_per_launch": T * n_loc * n_loc * 7 * 2,
+                "geometry_ms": geo_ms / max(geo_cnt, 1)}
+
+    # ---- FP32 assembly ----
+    a32 = fpp.form2(test=V, trial=V, precision="f32")
+    for _ in range(3):
+        step(a32.h)
+    torch.cuda.synchronize()
+    env.prof_reset()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(a32.h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1)
+    g32_cnt, g32_ms = env.prof("assemble_gather")
+    fp32 = {"value": nnz * args.steps / (ms32 / 1e3) / 1e6, "unit": UNIT,
+            "kernel_ms": g32_ms / max(g32_cnt, 1)}
+    vals64 = a.values()
+    vals32 = a32.values()
+    fp32["max_rel_err_vs_fp64"] = float(np.abs(vals32 - vals64).max() / np.abs(vals64).max())
+    del a32
+
+    # ---- e2e through the C-ABI with host buffers ----
+    h_xyz = torch.from_numpy(np.ascontiguousarray(xyz)).pin_memory()
+    h_kappa = torch.from_numpy(kappa).pin_memory()
+    h_vals = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    desc_h = _ffi.FormDesc()
+    desc_h.kind, desc_h.kappa, desc_h.mass, desc_h.quad_degree, desc_h.algo = _ffi.FORM_LAPLACE_MASS, 0.0, 1.0, 0, 0
+    desc_h.kappa_elem = C.c_void_p(h_kappa.data_ptr())
+
+    def e2e_step():
+        env.check(lib.fgpu_mesh_set_coords(M.h, C.c_void_p(h_xyz.data_ptr())))
+        env.check(lib.fgpu_assemble_matrix(env.h, a.h, C.byref(desc_h), 0))
+        env.check(lib.fgpu_matrix_get_csr(a.h, None, None, C.c_void_p(h_vals.data_ptr())))
+
+    for _ in range(2):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = reduce_max(time.perf_counter() - t0, world)
+    e2e = {"value": nnz * args.steps * world / t_e2e / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": int(xyz.nbytes + kappa.nbytes), "d2h_bytes_per_step": int(nnz * 8)}
+    assert np.array_equal(h_vals.numpy(), vals64)
+
+    # ---- CG time-to-1e-10 on the same system (homogeneous Dirichlet) ----
+    solve = None
+    if not args.no_solve:
+        l = fpp.form1(test=V)
+        l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+        a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v)))
+        a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+        s64 = a.solve(rhs=l, solution=u, rtol=1e-10)
+        u2 = V.element()
+        smx = a.solve(rhs=l, solution=u2, rtol=1e-10, mixed=True)
+        x64, xmx = u.to_numpy(), u2.to_numpy()
+        solve = {"fp64": s64, "mixed_fp32_refine": smx,
+                 "solution_rel_diff": float(np.linalg.norm(xmx - x64) / np.linalg.norm(x64)),
+                 "speedup_mixed_vs_fp64": s64["time_ms"] / smx["time_ms"] if smx["time_ms"] else None}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        from oracle import pyoracle as orc
+        threads = orc.num_threads()
+        s_nnz, s_dt, s_nt = cpu_sample(args, threads)
+        cpu = {"value": s_nnz / s_dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "oracle (CPU restatement of the Feel++ algorithm) P2 Laplacian+mass FP64 assembly of the %d^3 Kuhn cube (%d tets, nnz %d), %d threads over element colours" % (args.cpu_n, s_nt, s_nnz, threads)}
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "P2 Lagrange Laplacian+mass FP64 assembly, %d^3-hex Kuhn cube (%d tets, N=%d, nnz=%d), perturb 0.15h, lognormal kappa, quad degree 4" % (args.n, T, N, nnz),
+                      "order": args.order, "mesh_n": args.n, "l2": "inputs larger than L2 (CSR values %.0f MB)" % (nnz * 8 / 1e6),
+                      "parallelism": "replicas" if world > 1 else "single"},
+           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+           "clocks": clk.summary(), "fp32_assembly": fp32, "solve": solve}
+    print(json.dumps(out), flush=True)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

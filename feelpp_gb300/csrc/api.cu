@@ -1,0 +1,629 @@
+// C-ABI entry points (include/fgpu.h). Host orchestration of the device
+// assembly path; every call returns a status code and never throws.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fgpu_core.h"
+
+namespace fgpu {
+int launch_assemble_elasticity(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const double* d_coef, double lam,
+                               double mu, int accumulate);
+int launch_expand_pattern(fgpu_ctx* ctx, const DevPattern& P, int nc, int64_t* d_ia, int32_t* d_ja);
+}  // namespace fgpu
+
+using namespace fgpu;
+
+DevPattern::~DevPattern() {
+    cudaFree(d_ia);
+    cudaFree(d_ja);
+}
+
+namespace {
+
+int set_err(fgpu_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+template <typename T>
+int dev_alloc(fgpu_ctx* ctx, T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_err(ctx, FGPU_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return FGPU_OK;
+}
+
+// Resolve pending profiling events (after a stream sync) and check the status word.
+int finish(fgpu_ctx* ctx, bool sync = true) {
+    if (!sync) return FGPU_OK;
+    int hst = 0;
+    cudaError_t e = cudaMemcpyAsync(&hst, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return set_err(ctx, FGPU_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+    for (auto& ev : ctx->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev.start, ev.stop);
+        auto& a = ctx->prof[ev.name];
+        a.count++;
+        a.total_ms += ms;
+        ctx->event_pool.push_back(ev.start);
+        ctx->event_pool.push_back(ev.stop);
+    }
+    ctx->pending.clear();
+    if (hst) {
+        cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        if (hst & kStatusBadElement) return set_err(ctx, FGPU_ERR_BAD_ELEMENT, "degenerate element: |det K| <= 0 or non-finite");
+        if (hst & kStatusMissingEntry) return set_err(ctx, FGPU_ERR_PATTERN, "element column absent from the pattern");
+        if (hst & kStatusRowOverflow) return set_err(ctx, FGPU_ERR_INVALID, "pattern row longer than the staging buffer");
+        return set_err(ctx, FGPU_ERR_CUDA, "device status " + std::to_string(hst));
+    }
+    return FGPU_OK;
+}
+
+int ensure_pattern(fgpu_space* V) {
+    if (V->pattern) return FGPU_OK;
+    fgpu_ctx* ctx = V->ctx;
+    std::string err;
+    if (!build_node_pattern(V->topo, V->mesh->nt, V->h_pattern, ctx->host_threads, err))
+        return set_err(ctx, FGPU_ERR_ALLOC, err);
+    auto P = std::make_shared<DevPattern>();
+    P->nrows = V->h_pattern.nrows;
+    P->nnz = V->h_pattern.nnz;
+    P->max_row = V->h_pattern.max_row;
+    int rc = dev_alloc(ctx, &P->d_ia, P->nrows + 1);
+    if (!rc) rc = dev_alloc(ctx, &P->d_ja, P->nnz);
+    if (rc) return rc;
+    FGPU_CUDA_CHECK(ctx, cudaMemcpy(P->d_ia, V->h_pattern.ia.data(), (P->nrows + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    FGPU_CUDA_CHECK(ctx, cudaMemcpy(P->d_ja, V->h_pattern.ja.data(), P->nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+    V->pattern = P;
+    // the device copy is authoritative; drop the host ja
+    std::vector<int32_t>().swap(V->h_pattern.ja);
+    return FGPU_OK;
+}
+
+int form_qdeg(const fgpu_space* V, int q) { return q > 0 ? q : 2 * V->order; }
+
+}  // namespace
+
+extern "C" {
+
+int fgpu_create(const fgpu_config* cfg, fgpu_ctx** out) {
+    if (!out) return FGPU_ERR_INVALID;
+    *out = nullptr;
+    fgpu_ctx* ctx = new (std::nothrow) fgpu_ctx();
+    if (!ctx) return FGPU_ERR_ALLOC;
+    ctx->device = cfg ? cfg->device : 0;
+    ctx->profile = cfg ? cfg->profile : 0;
+    int ht = cfg ? cfg->host_threads : 0;
+    if (ht <= 0) ht = (int)std::max(1u, std::thread::hardware_concurrency());
+    ctx->host_threads = ht;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return FGPU_ERR_CUDA;
+    }
+    if (cfg && cfg->stream) {
+        ctx->stream = (cudaStream_t)cfg->stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        ctx->own_stream = true;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        delete ctx;
+        return FGPU_ERR_CUDA;
+    }
+    *out = ctx;
+    return FGPU_OK;
+}
+
+int fgpu_destroy(fgpu_ctx* ctx) {
+    if (!ctx) return FGPU_OK;
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& ev : ctx->pending) {
+        cudaEventDestroy(ev.start);
+        cudaEventDestroy(ev.stop);
+    }
+    for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+    cudaFree(ctx->d_status);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return FGPU_OK;
+}
+
+const char* fgpu_last_error(const fgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fgpu_sync(fgpu_ctx* ctx) {
+    if (!ctx) return FGPU_ERR_INVALID;
+    return finish(ctx, true);
+}
+
+int64_t fgpu_launch_count(const fgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ---------------------------------------------------------------------------
+int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, const int32_t* tets, fgpu_mesh** out) {
+    if (!ctx || !out || !xyz || !tets || nv <= 0 || nt <= 0) return set_err(ctx, FGPU_ERR_INVALID, "mesh_upload: bad arguments");
+    *out = nullptr;
+    for (int64_t k = 0; k < 4 * nt; ++k)
+        if (tets[k] < 0 || tets[k] >= nv) return set_err(ctx, FGPU_ERR_OUT_OF_RANGE, "tetrahedron vertex index out of range");
+    fgpu_mesh* M = new (std::nothrow) fgpu_mesh();
+    if (!M) return set_err(ctx, FGPU_ERR_ALLOC, "host allocation");
+    M->ctx = ctx;
+    M->nv = nv;
+    M->nt = nt;
+    M->h_xyz.assign(xyz, xyz + 3 * nv);
+    M->h_tets.assign(tets, tets + 4 * nt);
+    int rc = dev_alloc(ctx, &M->d_xyz, 3 * nv);
+    if (!rc) rc = dev_alloc(ctx, &M->d_tets, 4 * nt);
+    if (rc) { delete M; return rc; }
+    cudaMemcpyAsync(M->d_xyz, xyz, 3 * nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(M->d_tets, tets, 4 * nt * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(M->d_xyz); cudaFree(M->d_tets); delete M;
+        return set_err(ctx, FGPU_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = M;
+    return FGPU_OK;
+}
+
+int fgpu_mesh_set_coords(fgpu_mesh* M, const double* xyz) {
+    if (!M || !xyz) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = M->ctx;
+    FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(M->d_xyz, xyz, 3 * M->nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    std::memcpy(M->h_xyz.data(), xyz, 3 * M->nv * sizeof(double));
+    return FGPU_OK;
+}
+
+int fgpu_mesh_destroy(fgpu_mesh* M) {
+    if (!M) return FGPU_OK;
+    cudaFree(M->d_xyz);
+    cudaFree(M->d_tets);
+    cudaFree(M->d_colour_perm);
+    delete M;
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* M, int order, int ncomp, fgpu_space** out) {
+    if (!ctx || !M || !out) return set_err(ctx, FGPU_ERR_INVALID, "space_create: bad arguments");
+    if (order < 1 || order > 3) return set_err(ctx, FGPU_ERR_INVALID, "order must be 1, 2 or 3");
+    if (ncomp != 1 && ncomp != 3) return set_err(ctx, FGPU_ERR_INVALID, "ncomp must be 1 or 3");
+    *out = nullptr;
+    fgpu_space* V = new (std::nothrow) fgpu_space();
+    if (!V) return set_err(ctx, FGPU_ERR_ALLOC, "host allocation");
+    V->ctx = ctx;
+    V->mesh = M;
+    V->order = order;
+    V->ncomp = ncomp;
+    V->n = nloc_of(order);
+    std::string err;
+    if (!build_topology(M->nv, M->nt, M->h_tets.data(), order, V->topo, err)) {
+        delete V;
+        return set_err(ctx, FGPU_ERR_INVALID, err);
+    }
+    V->ndof = V->topo.nnodes * ncomp;
+    int rc = dev_alloc(ctx, &V->d_l2n, V->topo.l2n.size());
+    if (!rc) rc = dev_alloc(ctx, &V->d_inc_ptr, V->topo.inc_ptr.size());
+    if (!rc) rc = dev_alloc(ctx, &V->d_inc, V->topo.inc.size());
+    if (rc) { fgpu_space_destroy(V); return rc; }
+    cudaMemcpy(V->d_l2n, V->topo.l2n.data(), V->topo.l2n.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    cudaMemcpy(V->d_inc_ptr, V->topo.inc_ptr.data(), V->topo.inc_ptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(V->d_inc, V->topo.inc.data(), V->topo.inc.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { fgpu_space_destroy(V); return set_err(ctx, FGPU_ERR_CUDA, cudaGetErrorString(e)); }
+    *out = V;
+    return FGPU_OK;
+}
+
+int fgpu_space_ndof(const fgpu_space* V, int64_t* ndof, int* nloc) {
+    if (!V) return FGPU_ERR_INVALID;
+    if (ndof) *ndof = V->ndof;
+    if (nloc) *nloc = V->n * V->ncomp;
+    return FGPU_OK;
+}
+
+int fgpu_space_l2g(const fgpu_space* V, int32_t* out) {
+    if (!V || !out) return FGPU_ERR_INVALID;
+    const int n = V->n, nc = V->ncomp;
+    const int64_t nt = V->mesh->nt;
+    for (int64_t e = 0; e < nt; ++e)
+        for (int c = 0; c < nc; ++c)
+            for (int l = 0; l < n; ++l)
+                out[e * n * nc + (int64_t)n * c + l] = V->topo.l2n[(size_t)e * n + l] * nc + c;
+    return FGPU_OK;
+}
+
+int fgpu_space_boundary_dofs(const fgpu_space* V, int xmax_on, double xmax, int64_t* count, int32_t* dofs) {
+    if (!V || !count) return FGPU_ERR_INVALID;
+    std::vector<int32_t> nodes;
+    boundary_nodes(V->mesh->nt, V->mesh->h_tets.data(), V->mesh->h_xyz.data(), V->topo, xmax_on, xmax, nodes);
+    *count = (int64_t)nodes.size() * V->ncomp;
+    if (dofs)
+        for (size_t k = 0; k < nodes.size(); ++k)
+            for (int c = 0; c < V->ncomp; ++c) dofs[k * V->ncomp + c] = nodes[k] * V->ncomp + c;
+    return FGPU_OK;
+}
+
+int fgpu_space_destroy(fgpu_space* V) {
+    if (!V) return FGPU_OK;
+    cudaFree(V->d_l2n);
+    cudaFree(V->d_inc_ptr);
+    cudaFree(V->d_inc);
+    delete V;
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+int fgpu_matrix_create(fgpu_ctx* ctx, fgpu_space* test, fgpu_space* trial, int precision, fgpu_matrix** out) {
+    if (!ctx || !test || !out) return set_err(ctx, FGPU_ERR_INVALID, "matrix_create: bad arguments");
+    if (trial && trial != test) return set_err(ctx, FGPU_ERR_INVALID, "test and trial spaces must be the same space");
+    if (precision != FGPU_F64 && precision != FGPU_F32) return set_err(ctx, FGPU_ERR_INVALID, "bad precision");
+    *out = nullptr;
+    int rc = ensure_pattern(test);
+    if (rc) return rc;
+    fgpu_matrix* A = new (std::nothrow) fgpu_matrix();
+    if (!A) return set_err(ctx, FGPU_ERR_ALLOC, "host allocation");
+    A->ctx = ctx;
+    A->space = test;
+    A->precision = precision;
+    A->ncomp = test->ncomp;
+    A->pattern = test->pattern;
+    const int nc = test->ncomp;
+    A->nrows = test->pattern->nrows * nc;
+    A->nnz = test->pattern->nnz * nc * nc;
+    if (nc == 1) {
+        A->d_ia = test->pattern->d_ia;
+        A->d_ja = test->pattern->d_ja;
+        A->own_ia_ja = false;
+    } else {
+        rc = dev_alloc(ctx, &A->d_ia, A->nrows + 1);
+        if (!rc) rc = dev_alloc(ctx, &A->d_ja, A->nnz);
+        if (rc) { fgpu_matrix_destroy(A); return rc; }
+        A->own_ia_ja = true;
+        rc = launch_expand_pattern(ctx, *A->pattern, nc, A->d_ia, A->d_ja);
+        if (rc) { fgpu_matrix_destroy(A); return rc; }
+    }
+    rc = dev_alloc(ctx, (char**)&A->d_val, A->nnz * (precision == FGPU_F64 ? 8 : 4));
+    if (rc) { fgpu_matrix_destroy(A); return rc; }
+    cudaMemsetAsync(A->d_val, 0, A->nnz * (precision == FGPU_F64 ? 8 : 4), ctx->stream);
+    rc = finish(ctx);
+    if (rc) { fgpu_matrix_destroy(A); return rc; }
+    *out = A;
+    return FGPU_OK;
+}
+
+int fgpu_matrix_create_like(const fgpu_matrix* S, int precision, fgpu_matrix** out) {
+    if (!S || !out) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = S->ctx;
+    fgpu_matrix* A = new (std::nothrow) fgpu_matrix();
+    if (!A) return FGPU_ERR_ALLOC;
+    A->ctx = ctx;
+    A->space = S->space;
+    A->precision = precision;
+    A->ncomp = S->ncomp;
+    A->pattern = S->pattern;
+    A->nrows = S->nrows;
+    A->nnz = S->nnz;
+    if (S->ncomp == 1) {
+        A->d_ia = S->d_ia;
+        A->d_ja = S->d_ja;
+    } else {
+        int rc = dev_alloc(ctx, &A->d_ia, A->nrows + 1);
+        if (!rc) rc = dev_alloc(ctx, &A->d_ja, A->nnz);
+        if (rc) { fgpu_matrix_destroy(A); return rc; }
+        A->own_ia_ja = true;
+        cudaMemcpyAsync(A->d_ia, S->d_ia, (A->nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, ctx->stream);
+        cudaMemcpyAsync(A->d_ja, S->d_ja, A->nnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, ctx->stream);
+    }
+    int rc = dev_alloc(ctx, (char**)&A->d_val, A->nnz * (precision == FGPU_F64 ? 8 : 4));
+    if (rc) { fgpu_matrix_destroy(A); return rc; }
+    cudaMemsetAsync(A->d_val, 0, A->nnz * (precision == FGPU_F64 ? 8 : 4), ctx->stream);
+    rc = finish(ctx);
+    if (rc) { fgpu_matrix_destroy(A); return rc; }
+    *out = A;
+    return FGPU_OK;
+}
+
+int fgpu_matrix_info(const fgpu_matrix* A, int64_t* nrows, int64_t* nnz, int* precision) {
+    if (!A) return FGPU_ERR_INVALID;
+    if (nrows) *nrows = A->nrows;
+    if (nnz) *nnz = A->nnz;
+    if (precision) *precision = A->precision;
+    return FGPU_OK;
+}
+
+int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* val) {
+    if (!A) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = A->ctx;
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ia) FGPU_CUDA_CHECK(ctx, cudaMemcpy(ia, A->d_ia, (A->nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (ja) FGPU_CUDA_CHECK(ctx, cudaMemcpy(ja, A->d_ja, A->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (val) {
+        if (A->precision == FGPU_F64) {
+            FGPU_CUDA_CHECK(ctx, cudaMemcpy(val, A->d_val, A->nnz * sizeof(double), cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> tmp(A->nnz);
+            FGPU_CUDA_CHECK(ctx, cudaMemcpy(tmp.data(), A->d_val, A->nnz * sizeof(float), cudaMemcpyDeviceToHost));
+            for (int64_t k = 0; k < A->nnz; ++k) val[k] = tmp[k];
+        }
+    }
+    return FGPU_OK;
+}
+
+int fgpu_matrix_values_device(const fgpu_matrix* A, void** dptr) {
+    if (!A || !dptr) return FGPU_ERR_INVALID;
+    *dptr = A->d_val;
+    return FGPU_OK;
+}
+
+int fgpu_matrix_zero(fgpu_matrix* A) {
+    if (!A) return FGPU_ERR_INVALID;
+    FGPU_CUDA_CHECK(A->ctx, cudaMemsetAsync(A->d_val, 0, A->nnz * (A->precision == FGPU_F64 ? 8 : 4), A->ctx->stream));
+    return FGPU_OK;
+}
+
+int fgpu_matrix_convert(const fgpu_matrix* src, fgpu_matrix* dst) {
+    if (!src || !dst || src->nnz != dst->nnz || src->pattern != dst->pattern) return FGPU_ERR_INVALID;
+    int rc = launch_convert_values(src->ctx, src, dst);
+    if (rc) return rc;
+    return finish(src->ctx);
+}
+
+int fgpu_matrix_destroy(fgpu_matrix* A) {
+    if (!A) return FGPU_OK;
+    if (A->own_ia_ja) {
+        cudaFree(A->d_ia);
+        cudaFree(A->d_ja);
+    }
+    cudaFree(A->d_val);
+    cudaFree(A->d_coef);
+    delete A;
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
+    if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
+    fgpu_space* V = A->space;
+    const int qdeg = form_qdeg(V, f->quad_degree);
+    std::string err;
+    DevTables* tab = get_dev_tables(V->order, qdeg, err);
+    if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
+    const int64_t nt = V->mesh->nt;
+    const int rec = f->kind == FGPU_FORM_ELASTICITY ? 16 : 8;
+    if (A->coef_cap < nt * rec) {
+        cudaFree(A->d_coef);
+        A->d_coef = nullptr;
+        A->coef_cap = 0;
+        int rc = dev_alloc(ctx, &A->d_coef, nt * rec);
+        if (rc) return rc;
+        A->coef_cap = nt * rec;
+    }
+    int rc = launch_geometry(ctx, V->mesh, f->kind, d_kappa, f->kappa, f->mass, f->lambda, f->mu, A->d_coef);
+    if (rc) return rc;
+    if (f->kind == FGPU_FORM_LAPLACE_MASS) {
+        rc = launch_assemble_gather(ctx, A, tab, f->kind, A->d_coef, accumulate);
+    } else if (f->kind == FGPU_FORM_ELASTICITY) {
+        rc = launch_assemble_elasticity(ctx, A, tab, A->d_coef, f->lambda, f->mu, accumulate);
+    } else {
+        return set_err(ctx, FGPU_ERR_INVALID, "unknown form kind");
+    }
+    if (rc) return rc;
+    return finish(ctx);
+}
+
+int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, int accumulate) {
+    if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
+    if (!f->kappa_elem) return assemble_impl(ctx, A, f, nullptr, accumulate);
+    const int64_t nt = A->space->mesh->nt;
+    double* dk = nullptr;
+    int rc = dev_alloc(ctx, &dk, nt);
+    if (rc) return rc;
+    cudaMemcpyAsync(dk, f->kappa_elem, nt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    rc = assemble_impl(ctx, A, f, dk, accumulate);
+    cudaFree(dk);
+    return rc;
+}
+
+int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
+    return assemble_impl(ctx, A, f, d_kappa, accumulate);
+}
+
+// ---------------------------------------------------------------------------
+int fgpu_vector_create(fgpu_ctx* ctx, int64_t n, fgpu_vector** out) {
+    if (!ctx || !out || n < 0) return set_err(ctx, FGPU_ERR_INVALID, "vector_create: bad arguments");
+    fgpu_vector* v = new (std::nothrow) fgpu_vector();
+    if (!v) return FGPU_ERR_ALLOC;
+    v->ctx = ctx;
+    v->n = n;
+    int rc = dev_alloc(ctx, &v->d, n);
+    if (rc) { delete v; return rc; }
+    cudaMemsetAsync(v->d, 0, n * sizeof(double), ctx->stream);
+    *out = v;
+    return FGPU_OK;
+}
+int fgpu_vector_upload(fgpu_vector* v, const double* host) {
+    if (!v || !host) return FGPU_ERR_INVALID;
+    FGPU_CUDA_CHECK(v->ctx, cudaMemcpyAsync(v->d, host, v->n * sizeof(double), cudaMemcpyHostToDevice, v->ctx->stream));
+    return FGPU_OK;
+}
+int fgpu_vector_download(const fgpu_vector* v, double* host) {
+    if (!v || !host) return FGPU_ERR_INVALID;
+    FGPU_CUDA_CHECK(v->ctx, cudaMemcpyAsync(host, v->d, v->n * sizeof(double), cudaMemcpyDeviceToHost, v->ctx->stream));
+    FGPU_CUDA_CHECK(v->ctx, cudaStreamSynchronize(v->ctx->stream));
+    return FGPU_OK;
+}
+int fgpu_vector_zero(fgpu_vector* v) {
+    if (!v) return FGPU_ERR_INVALID;
+    FGPU_CUDA_CHECK(v->ctx, cudaMemsetAsync(v->d, 0, v->n * sizeof(double), v->ctx->stream));
+    return FGPU_OK;
+}
+int fgpu_vector_device(const fgpu_vector* v, double** dptr) {
+    if (!v || !dptr) return FGPU_ERR_INVALID;
+    *dptr = v->d;
+    return FGPU_OK;
+}
+int fgpu_vector_destroy(fgpu_vector* v) {
+    if (!v) return FGPU_OK;
+    cudaFree(v->d);
+    delete v;
+    return FGPU_OK;
+}
+
+int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, fgpu_vector* out, int accumulate) {
+    if (!ctx || !V || !rhs || !out || out->n != V->ndof) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad arguments");
+    const int qdeg = form_qdeg(V, rhs->quad_degree);
+    std::string err;
+    DevTables* tab = get_dev_tables(V->order, qdeg, err);
+    if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
+    double* work = nullptr;
+    int rc = dev_alloc(ctx, &work, (size_t)V->mesh->nt * V->n * V->ncomp);
+    if (rc) return rc;
+    rc = launch_rhs(ctx, V, tab, rhs->kind, rhs->c, out->d, accumulate, work);
+    int rc2 = finish(ctx);
+    cudaFree(work);
+    return rc ? rc : rc2;
+}
+
+int fgpu_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, fgpu_vector* rhs, int64_t ndofs, const int32_t* dofs,
+                   const double* values, int mode, double diag) {
+    if (!ctx || !A || (ndofs > 0 && !dofs)) return set_err(ctx, FGPU_ERR_INVALID, "dirichlet: bad arguments");
+    if (mode < 0 || mode > 2) return set_err(ctx, FGPU_ERR_INVALID, "dirichlet: bad mode");
+    if (rhs && rhs->n != A->nrows) return set_err(ctx, FGPU_ERR_INVALID, "dirichlet: rhs size");
+    std::vector<uint8_t> mask(A->nrows, 0);
+    std::vector<double> g;
+    if (values) g.assign(A->nrows, 0.0);
+    for (int64_t k = 0; k < ndofs; ++k) {
+        if (dofs[k] < 0 || dofs[k] >= A->nrows) return set_err(ctx, FGPU_ERR_OUT_OF_RANGE, "dirichlet: dof out of range");
+        mask[dofs[k]] = 1;
+        if (values) g[dofs[k]] = values[k];
+    }
+    uint8_t* dm = nullptr;
+    double* dg = nullptr;
+    int rc = dev_alloc(ctx, &dm, A->nrows);
+    if (!rc && values) rc = dev_alloc(ctx, &dg, A->nrows);
+    if (rc) { cudaFree(dm); return rc; }
+    cudaMemcpyAsync(dm, mask.data(), A->nrows, cudaMemcpyHostToDevice, ctx->stream);
+    if (values) cudaMemcpyAsync(dg, g.data(), A->nrows * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    rc = launch_dirichlet(ctx, A, rhs ? rhs->d : nullptr, dm, dg, mode, diag);
+    int rc2 = finish(ctx);
+    cudaFree(dm);
+    cudaFree(dg);
+    return rc ? rc : rc2;
+}
+
+int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, fgpu_vector* y) {
+    if (!ctx || !A || !x || !y || x->n != A->nrows || y->n != A->nrows) return set_err(ctx, FGPU_ERR_INVALID, "mult: bad arguments");
+    int rc = launch_spmv(ctx, A, x->d, y->d, 0.0, nullptr);
+    if (rc) return rc;
+    return finish(ctx);
+}
+
+int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
+                  const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
+    if (!ctx || !A || !b || !x || !cfg || b->n != A->nrows || x->n != A->nrows)
+        return set_err(ctx, FGPU_ERR_INVALID, "solve_cg: bad arguments");
+    int rc = finish(ctx);
+    if (rc) return rc;
+    if (!cfg->mixed) return solve_pcg(ctx, A, b->d, x->d, cfg, stats);
+    if (A->precision != FGPU_F64) return set_err(ctx, FGPU_ERR_INVALID, "mixed solve needs an FP64 matrix");
+    fgpu_matrix* tmp = nullptr;
+    const fgpu_matrix* a32 = A32;
+    if (!a32) {
+        rc = fgpu_matrix_create_like(A, FGPU_F32, &tmp);
+        if (rc) return rc;
+        rc = launch_convert_values(ctx, A, tmp);
+        if (rc) { fgpu_matrix_destroy(tmp); return rc; }
+        a32 = tmp;
+    }
+    rc = solve_pcg_mixed(ctx, A, a32, b->d, x->d, cfg, stats);
+    if (tmp) fgpu_matrix_destroy(tmp);
+    int rc2 = finish(ctx);
+    return rc ? rc : rc2;
+}
+
+int fgpu_host_dof_table(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int32_t* l2g,
+                        int64_t* ndof) {
+    if (!tets || nv <= 0 || nt <= 0 || (ncomp != 1 && ncomp != 3)) return FGPU_ERR_INVALID;
+    Topology topo;
+    std::string err;
+    if (!build_topology(nv, nt, tets, order, topo, err)) return FGPU_ERR_INVALID;
+    if (ndof) *ndof = topo.nnodes * ncomp;
+    if (l2g) {
+        const int n = topo.n;
+        for (int64_t e = 0; e < nt; ++e)
+            for (int c = 0; c < ncomp; ++c)
+                for (int l = 0; l < n; ++l)
+                    l2g[e * n * ncomp + (int64_t)n * c + l] = topo.l2n[(size_t)e * n + l] * ncomp + c;
+    }
+    return FGPU_OK;
+}
+
+int fgpu_host_pattern(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int64_t* ia, int32_t* ja,
+                      int64_t* nnz) {
+    if (!tets || !ia || nv <= 0 || nt <= 0 || (ncomp != 1 && ncomp != 3)) return FGPU_ERR_INVALID;
+    Topology topo;
+    NodePattern P;
+    std::string err;
+    if (!build_topology(nv, nt, tets, order, topo, err)) return FGPU_ERR_INVALID;
+    if (!build_node_pattern(topo, nt, P, (int)std::max(1u, std::thread::hardware_concurrency()), err)) return FGPU_ERR_ALLOC;
+    const int nc = ncomp;
+    for (int64_t m = 0; m < P.nrows; ++m) {
+        int64_t len = P.ia[m + 1] - P.ia[m];
+        for (int c = 0; c < nc; ++c) ia[m * nc + c] = (int64_t)nc * nc * P.ia[m] + c * nc * len;
+    }
+    ia[P.nrows * nc] = (int64_t)nc * nc * P.nnz;
+    if (nnz) *nnz = (int64_t)nc * nc * P.nnz;
+    if (ja)
+        for (int64_t m = 0; m < P.nrows; ++m) {
+            int64_t b = P.ia[m], len = P.ia[m + 1] - b;
+            for (int c = 0; c < nc; ++c) {
+                int64_t o = (int64_t)nc * nc * b + c * nc * len;
+                for (int64_t k = 0; k < len; ++k)
+                    for (int d = 0; d < nc; ++d) ja[o + k * nc + d] = P.ja[b + k] * nc + d;
+            }
+        }
+    return FGPU_OK;
+}
+
+int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double* dphi, double* S, double* M,
+                         int* npts) {
+    RefTables R;
+    std::string err;
+    if (!build_ref_tables(order, qdeg, R, err)) return FGPU_ERR_INVALID;
+    if (npts) *npts = R.Q;
+    if (nodes) std::memcpy(nodes, R.nodes.data(), R.nodes.size() * sizeof(double));
+    if (phi) std::memcpy(phi, R.phi.data(), R.phi.size() * sizeof(double));
+    if (dphi) std::memcpy(dphi, R.dphi.data(), R.dphi.size() * sizeof(double));
+    if (S) std::memcpy(S, R.S.data(), R.S.size() * sizeof(double));
+    if (M) std::memcpy(M, R.M.data(), R.M.size() * sizeof(double));
+    return FGPU_OK;
+}
+
+int fgpu_prof_reset(fgpu_ctx* ctx) {
+    if (!ctx) return FGPU_ERR_INVALID;
+    finish(ctx);
+    ctx->prof.clear();
+    return FGPU_OK;
+}
+
+int fgpu_prof_get(fgpu_ctx* ctx, const char* name, int64_t* count, double* total_ms) {
+    if (!ctx || !name) return FGPU_ERR_INVALID;
+    int rc = finish(ctx);
+    if (rc) return rc;
+    auto it = ctx->prof.find(name);
+    if (count) *count = it == ctx->prof.end() ? 0 : it->second.count;
+    if (total_ms) *total_ms = it == ctx->prof.end() ? 0.0 : it->second.total_ms;
+    return FGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,633 @@
+// Device assembly kernels: per-element geometry, row-owner gather assembly of
+// the CSR values (scalar Laplacian/mass and vector elasticity), load vector,
+// strong Dirichlet rows.
+//
+// Formulation. On an affine tetrahedron the geometric map is constant, so the
+// quadrature sum the reference evaluates per entry,
+//     K_e(i,j) = sum_q w_q J (kappa (B ghat_j(q)).(B ghat_i(q)) + mass phi_j(q) phi_i(q))
+// (feelpp/feel/feelvf/bilinearformcontext.hpp:552-590, pointsetquadrature.hpp:403-416),
+// factors into 7 element coefficients times 7 reference tensors computed once
+// with the same quadrature rule:
+//     K_e = sum_k c_k T_k,  c = kappa J (G00, G11, G22, G01, G02, G12) (G = B^T B), c_6 = mass J.
+// The result equals the quadrature form up to rounding.
+//
+// Scatter. Instead of adding element blocks into the CSR (MatSetValues
+// ADD_VALUES, matrixpetsc.cpp:919-935), each CSR row is owned by one group of
+// lanes which walks the elements containing the row's dof in increasing
+// element order and sums the row of each element matrix into a shared-memory
+// copy of the row; the row is then written once, coalesced. Every entry is
+// summed in element insertion order, the order the reference adds into PETSc;
+// no float atomics, deterministic.
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <string>
+
+#include "fgpu_core.h"
+
+namespace fgpu {
+
+// ---------------------------------------------------------------------------
+// Reference tables resident on the device, one copy per (device, order, degree).
+// ---------------------------------------------------------------------------
+static std::mutex g_tab_mutex;
+static std::map<std::tuple<int, int, int>, DevTables*> g_tabs;
+
+template <typename T>
+static cudaError_t upload(const std::vector<T>& h, T** d) {
+    cudaError_t e = cudaMalloc((void**)d, h.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+DevTables* get_dev_tables(int order, int qdeg, std::string& err) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_tab_mutex);
+    auto key = std::make_tuple(dev, order, qdeg);
+    auto it = g_tabs.find(key);
+    if (it != g_tabs.end()) return it->second;
+    RefTables R;
+    if (!build_ref_tables(order, qdeg, R, err)) return nullptr;
+    DevTables* D = new DevTables();
+    D->order = order; D->n = R.n; D->Q = R.Q; D->qdeg = qdeg;
+    std::vector<float> T7f(R.T7.begin(), R.T7.end()), Sf(R.S.begin(), R.S.end());
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(R.T7, &D->d_T7);
+    if (e == cudaSuccess) e = upload(R.S, &D->d_S);
+    if (e == cudaSuccess) e = upload(T7f, &D->d_T7f);
+    if (e == cudaSuccess) e = upload(Sf, &D->d_Sf);
+    if (e == cudaSuccess) e = upload(R.phi, &D->d_phi);
+    if (e == cudaSuccess) e = upload(R.dphi, &D->d_dphi);
+    if (e == cudaSuccess) e = upload(R.qx, &D->d_qx);
+    if (e == cudaSuccess) e = upload(R.qw, &D->d_qw);
+    if (e != cudaSuccess) {
+        err = std::string("reference table upload: ") + cudaGetErrorString(e);
+        delete D;
+        return nullptr;
+    }
+    g_tabs[key] = D;
+    return D;
+}
+
+// ---------------------------------------------------------------------------
+// Profiling with CUDA events on the launch stream.
+// ---------------------------------------------------------------------------
+void prof_begin(fgpu_ctx* ctx, const char* name, PendingEvent& ev) {
+    ++ctx->launches;
+    if (!ctx->profile) return;
+    ev.name = name;
+    if (ctx->event_pool.size() >= 2) {
+        ev.start = ctx->event_pool.back(); ctx->event_pool.pop_back();
+        ev.stop = ctx->event_pool.back(); ctx->event_pool.pop_back();
+    } else {
+        cudaEventCreate(&ev.start);
+        cudaEventCreate(&ev.stop);
+    }
+    cudaEventRecord(ev.start, ctx->stream);
+}
+
+void prof_end(fgpu_ctx* ctx, PendingEvent& ev) {
+    if (!ctx->profile) return;
+    cudaEventRecord(ev.stop, ctx->stream);
+    ctx->pending.push_back(ev);
+}
+
+// ---------------------------------------------------------------------------
+// Geometry: one thread per element (geomap.hpp:2310-2350, :1971-1991).
+// Record layout (8 doubles) for the Laplacian/mass form:
+//   [kappa J G00, kappa J G11, kappa J G22, kappa J G01, kappa J G02, kappa J G12, mass J, J]
+// Record layout (16 doubles) for elasticity:
+//   [B (9, row-major), G00, G11, G22, G01, G02, G12, J]
+// ---------------------------------------------------------------------------
+__global__ void geometry_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets, int kind,
+                                const double* __restrict__ kappa, double kappa_c, double mass, double* __restrict__ coef,
+                                int* __restrict__ status) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
+        double x0 = xyz[3 * (int64_t)t.x], y0 = xyz[3 * (int64_t)t.x + 1], z0 = xyz[3 * (int64_t)t.x + 2];
+        // K(r, c) = (X_{c+1} - X_0)[r] / 2
+        double K[9];
+        const int vv[3] = {t.y, t.z, t.w};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double* X = xyz + 3 * (int64_t)vv[c];
+            K[0 * 3 + c] = 0.5 * X[0] - 0.5 * x0;
+            K[1 * 3 + c] = 0.5 * X[1] - 0.5 * y0;
+            K[2 * 3 + c] = 0.5 * X[2] - 0.5 * z0;
+        }
+        double c00 = K[4] * K[8] - K[5] * K[7];
+        double c01 = K[5] * K[6] - K[3] * K[8];
+        double c02 = K[3] * K[7] - K[4] * K[6];
+        double det = K[0] * c00 + K[1] * c01 + K[2] * c02;
+        double J = fabs(det);
+        if (!(J > 0.0) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+        double cof[9] = {c00, c01, c02,
+                         K[2] * K[7] - K[1] * K[8], K[0] * K[8] - K[2] * K[6], K[1] * K[6] - K[0] * K[7],
+                         K[1] * K[5] - K[2] * K[4], K[2] * K[3] - K[0] * K[5], K[0] * K[4] - K[1] * K[3]};
+        double B[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) B[i] = cof[i] / det;
+        // G = B^T B
+        double G[6];
+        const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            G[k] = B[0 * 3 + pa[k]] * B[0 * 3 + pb[k]] + B[1 * 3 + pa[k]] * B[1 * 3 + pb[k]] + B[2 * 3 + pa[k]] * B[2 * 3 + pb[k]];
+        if (kind == FGPU_FORM_LAPLACE_MASS) {
+            double kJ = (kappa ? kappa[e] : kappa_c) * J;
+            double* o = coef + 8 * e;
+            double2* o2 = reinterpret_cast<double2*>(o);
+            o2[0] = make_double2(kJ * G[0], kJ * G[1]);
+            o2[1] = make_double2(kJ * G[2], kJ * G[3]);
+            o2[2] = make_double2(kJ * G[4], kJ * G[5]);
+            o2[3] = make_double2(mass * J, J);
+        } else {
+            double* o = coef + 16 * e;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) o[i] = B[i];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) o[9 + k] = G[k];
+            o[15] = J;
+        }
+    }
+}
+
+int launch_geometry(fgpu_ctx* ctx, const fgpu_mesh* mesh, int kind, const double* d_kappa, double kappa,
+                    double mass, double lam, double mu, double* d_coef) {
+    (void)lam; (void)mu;
+    int threads = 256;
+    int64_t blocks = (mesh->nt + threads - 1) / threads;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "geometry", ev);
+    geometry_kernel<<<(int)blocks, threads, 0, ctx->stream>>>(mesh->nt, mesh->d_xyz, mesh->d_tets, kind, d_kappa, kappa,
+                                                            mass, d_coef, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Row-owner gather assembly, scalar forms.
+// One group of G lanes owns one row (dof node) at a time. Shared memory holds
+// the reference tensors (7 n n, compute type CT) and, per group, the row's
+// column ids and accumulators.
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+    if (G >= 32) return 0xffffffffu;
+    unsigned lane = threadIdx.x & 31u;
+    return ((1u << (G & 31)) - 1u) << (lane / G * G);
+}
+
+__device__ __forceinline__ int lower_bound_s(const int32_t* a, int len, int32_t key) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+template <typename CT>
+__device__ __forceinline__ CT to_ct(double v) { return (CT)v; }
+
+template <typename VT, typename CT, int N, int G>
+__global__ void __launch_bounds__(256) gather_scalar_kernel(
+    int64_t nrows, const int64_t* __restrict__ sia, const int32_t* __restrict__ sja,
+    const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const int32_t* __restrict__ l2n,
+    const double* __restrict__ coef, const CT* __restrict__ T7g, int maxrow, VT* __restrict__ val, int accumulate,
+    int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    CT* T7 = reinterpret_cast<CT*>(smem);
+    constexpr int NT = 7 * N * N;
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) T7[k] = T7g[k];
+    const int gpb = blockDim.x / G;
+    const int g = threadIdx.x / G, lane = threadIdx.x % G;
+    size_t t7bytes = ((size_t)NT * sizeof(CT) + 15) & ~(size_t)15;
+    CT* acc = reinterpret_cast<CT*>(smem + t7bytes) + (size_t)g * maxrow;
+    int32_t* cols = reinterpret_cast<int32_t*>(smem + t7bytes + (size_t)gpb * maxrow * sizeof(CT)) + (size_t)g * maxrow;
+    __syncthreads();
+    const unsigned mask = group_mask<G>();
+    for (int64_t r = (int64_t)blockIdx.x * gpb + g; r < nrows; r += (int64_t)gridDim.x * gpb) {
+        const int64_t start = sia[r];
+        const int len = (int)(sia[r + 1] - start);
+        if (len > maxrow) {
+            if (lane == 0) atomicOr(status, kStatusRowOverflow);
+            continue;
+        }
+        for (int k = lane; k < len; k += G) {
+            cols[k] = sja[start + k];
+            acc[k] = accumulate ? (CT)val[start + k] : (CT)0;
+        }
+        __syncwarp(mask);
+        const int64_t tb = inc_ptr[r], te = inc_ptr[r + 1];
+        for (int64_t t = tb; t < te; ++t) {
+            const int32_t code = inc[t];
+            const int64_t e = code >> 5;
+            const int li = code & 31;
+            if (lane < N) {
+                const double2* cp = reinterpret_cast<const double2*>(coef + 8 * e);
+                const double2 ca = __ldg(cp), cb = __ldg(cp + 1), cc = __ldg(cp + 2), cd = __ldg(cp + 3);
+                const int32_t col = l2n[e * N + lane];
+                const CT* tk = T7 + li * N + lane;
+                CT v = to_ct<CT>(ca.x) * tk[0 * N * N];
+                v += to_ct<CT>(ca.y) * tk[1 * N * N];
+                v += to_ct<CT>(cb.x) * tk[2 * N * N];
+                v += to_ct<CT>(cb.y) * tk[3 * N * N];
+                v += to_ct<CT>(cc.x) * tk[4 * N * N];
+                v += to_ct<CT>(cc.y) * tk[5 * N * N];
+                v += to_ct<CT>(cd.x) * tk[6 * N * N];
+                const int pos = lower_bound_s(cols, len, col);
+                if (pos < len && cols[pos] == col) acc[pos] += v;
+                else atomicOr(status, kStatusMissingEntry);
+            }
+            __syncwarp(mask);
+        }
+        for (int k = lane; k < len; k += G) val[start + k] = (VT)acc[k];
+        __syncwarp(mask);
+    }
+}
+
+// Vector elasticity (Pchv, ncomp = 3). A group owns the 3 component rows of a
+// dof node. For element e (local index li of the node) and lane j, the 3x3
+// block K[(c,li),(d,j)] = J (lambda Y_cd + mu Y_dc + mu delta_cd tr(G X)),
+// X_ab = S_ab(li, j), Y = B X B^T, is the quadrature sum of
+// lambda div u div v + 2 mu eps(u):eps(v) (qs_elasticity.cpp:46-63) written
+// with the reference tensors S_ab = sum_q w_q d_a phi_i d_b phi_j.
+template <typename VT, typename CT, int N, int G>
+__global__ void __launch_bounds__(256) gather_elasticity_kernel(
+    int64_t nnodes, const int64_t* __restrict__ sia, const int32_t* __restrict__ sja,
+    const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const int32_t* __restrict__ l2n,
+    const double* __restrict__ coef, const CT* __restrict__ Sg, double lam, double mu, int maxrow,
+    VT* __restrict__ val, int accumulate, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    CT* S = reinterpret_cast<CT*>(smem);
+    constexpr int NS = 9 * N * N;
+    for (int k = threadIdx.x; k < NS; k += blockDim.x) S[k] = Sg[k];
+    const int gpb = blockDim.x / G;
+    const int g = threadIdx.x / G, lane = threadIdx.x % G;
+    size_t sbytes = ((size_t)NS * sizeof(CT) + 15) & ~(size_t)15;
+    CT* acc = reinterpret_cast<CT*>(smem + sbytes) + (size_t)g * 9 * maxrow;   // [3][3*maxrow]
+    int32_t* cols = reinterpret_cast<int32_t*>(smem + sbytes + (size_t)gpb * 9 * maxrow * sizeof(CT)) + (size_t)g * maxrow;
+    __syncthreads();
+    const unsigned mask = group_mask<G>();
+    for (int64_t m = (int64_t)blockIdx.x * gpb + g; m < nnodes; m += (int64_t)gridDim.x * gpb) {
+        const int64_t sstart = sia[m];
+        const int len = (int)(sia[m + 1] - sstart);
+        if (len > maxrow) {
+            if (lane == 0) atomicOr(status, kStatusRowOverflow);
+            continue;
+        }
+        const int64_t row0 = 9 * sstart;  // start of row 3m: 9 * sia[m]; row 3m+c starts at row0 + c*3*len
+        for (int k = lane; k < len; k += G) cols[k] = sja[sstart + k];
+        for (int k = lane; k < 9 * len; k += G) acc[k] = accumulate ? (CT)val[row0 + k] : (CT)0;
+        __syncwarp(mask);
+        for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
+            const int32_t code = inc[t];
+            const int64_t e = code >> 5;
+            const int li = code & 31;
+            if (lane < N) {
+                const double* cr = coef + 16 * e;
+                CT B[9], Gm[6];
+#pragma unroll
+                for (int i = 0; i < 9; ++i) B[i] = (CT)__ldg(cr + i);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) Gm[i] = (CT)__ldg(cr + 9 + i);
+                const CT J = (CT)__ldg(cr + 15);
+                CT X[9];
+#pragma unroll
+                for (int ab = 0; ab < 9; ++ab) X[ab] = S[(ab * N + li) * N + lane];
+                // Z = X B^T : Z_ad = sum_b X_ab B_db ; Y = B Z : Y_cd = sum_a B_ca Z_ad
+                CT Z[9], Y[9];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) Z[a * 3 + d] = X[a * 3 + 0] * B[d * 3 + 0] + X[a * 3 + 1] * B[d * 3 + 1] + X[a * 3 + 2] * B[d * 3 + 2];
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) Y[c * 3 + d] = B[c * 3 + 0] * Z[0 * 3 + d] + B[c * 3 + 1] * Z[1 * 3 + d] + B[c * 3 + 2] * Z[2 * 3 + d];
+                CT tr = Gm[0] * X[0] + Gm[1] * X[4] + Gm[2] * X[8] + Gm[3] * (X[1] + X[3]) + Gm[4] * (X[2] + X[6]) + Gm[5] * (X[5] + X[7]);
+                const CT lJ = (CT)lam * J, mJ = (CT)mu * J;
+                const int32_t col = l2n[e * N + lane];
+                const int pos = lower_bound_s(cols, len, col);
+                if (pos < len && cols[pos] == col) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            CT v = lJ * Y[c * 3 + d] + mJ * Y[d * 3 + c];
+                            if (c == d) v += mJ * tr;
+                            acc[c * 3 * len + 3 * pos + d] += v;
+                        }
+                } else {
+                    atomicOr(status, kStatusMissingEntry);
+                }
+            }
+            __syncwarp(mask);
+        }
+        for (int k = lane; k < 9 * len; k += G) val[row0 + k] = (VT)acc[k];
+        __syncwarp(mask);
+    }
+}
+
+template <typename VT, typename CT, int N, int G>
+static int run_gather_scalar(fgpu_ctx* ctx, fgpu_matrix* A, const CT* T7, const double* d_coef, int accumulate) {
+    const DevPattern& P = *A->pattern;
+    const fgpu_space* V = A->space;
+    const int threads = 256, gpb = threads / G;
+    size_t t7bytes = ((size_t)7 * N * N * sizeof(CT) + 15) & ~(size_t)15;
+    size_t smem = t7bytes + (size_t)gpb * P.max_row * (sizeof(CT) + sizeof(int32_t));
+    auto kern = gather_scalar_kernel<VT, CT, N, G>;
+    if (smem > 48 * 1024) FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > 227 * 1024) { ctx->err = "pattern rows too long for the gather kernel"; return FGPU_ERR_INVALID; }
+    int per_sm = 0;
+    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    int64_t need = (P.nrows + gpb - 1) / gpb;
+    int64_t blocks = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * sms);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather", ev);
+    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, P.d_ja, V->d_inc_ptr, V->d_inc, V->d_l2n, d_coef,
+                                                      T7, P.max_row, reinterpret_cast<VT*>(A->d_val), accumulate,
+                                                      ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+template <typename VT, typename CT, int N, int G>
+static int run_gather_elasticity(fgpu_ctx* ctx, fgpu_matrix* A, const CT* S, const double* d_coef, double lam,
+                                 double mu, int accumulate) {
+    const DevPattern& P = *A->pattern;
+    const fgpu_space* V = A->space;
+    const int threads = 256, gpb = threads / G;
+    size_t sbytes = ((size_t)9 * N * N * sizeof(CT) + 15) & ~(size_t)15;
+    size_t smem = sbytes + (size_t)gpb * P.max_row * (9 * sizeof(CT) + sizeof(int32_t));
+    auto kern = gather_elasticity_kernel<VT, CT, N, G>;
+    if (smem > 227 * 1024) { ctx->err = "pattern rows too long for the elasticity gather kernel"; return FGPU_ERR_INVALID; }
+    if (smem > 48 * 1024) FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    int64_t need = (P.nrows + gpb - 1) / gpb;
+    int64_t blocks = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * sms);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather_elasticity", ev);
+    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, P.d_ja, V->d_inc_ptr, V->d_inc, V->d_l2n, d_coef, S,
+                                                      lam, mu, P.max_row, reinterpret_cast<VT*>(A->d_val), accumulate,
+                                                      ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+int launch_assemble_gather(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, int kind, const double* d_coef,
+                           int accumulate) {
+    const int order = A->space->order;
+    const bool f32 = A->precision == FGPU_F32;
+    if (kind == FGPU_FORM_LAPLACE_MASS) {
+        if (A->ncomp != 1) { ctx->err = "Laplace/mass form needs a scalar space"; return FGPU_ERR_INVALID; }
+        if (order == 1) return f32 ? run_gather_scalar<float, float, 4, 8>(ctx, A, tab->d_T7f, d_coef, accumulate)
+                                   : run_gather_scalar<double, double, 4, 8>(ctx, A, tab->d_T7, d_coef, accumulate);
+        if (order == 2) return f32 ? run_gather_scalar<float, float, 10, 16>(ctx, A, tab->d_T7f, d_coef, accumulate)
+                                   : run_gather_scalar<double, double, 10, 16>(ctx, A, tab->d_T7, d_coef, accumulate);
+        if (order == 3) return f32 ? run_gather_scalar<float, float, 20, 32>(ctx, A, tab->d_T7f, d_coef, accumulate)
+                                   : run_gather_scalar<double, double, 20, 32>(ctx, A, tab->d_T7, d_coef, accumulate);
+    }
+    ctx->err = "unsupported form/order";
+    return FGPU_ERR_INVALID;
+}
+
+int launch_assemble_elasticity(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const double* d_coef, double lam,
+                               double mu, int accumulate) {
+    const int order = A->space->order;
+    const bool f32 = A->precision == FGPU_F32;
+    if (A->ncomp != 3) { ctx->err = "elasticity needs a 3-component space"; return FGPU_ERR_INVALID; }
+    if (order == 1) return f32 ? run_gather_elasticity<float, float, 4, 8>(ctx, A, tab->d_Sf, d_coef, lam, mu, accumulate)
+                               : run_gather_elasticity<double, double, 4, 8>(ctx, A, tab->d_S, d_coef, lam, mu, accumulate);
+    if (order == 2) return f32 ? run_gather_elasticity<float, float, 10, 16>(ctx, A, tab->d_Sf, d_coef, lam, mu, accumulate)
+                               : run_gather_elasticity<double, double, 10, 16>(ctx, A, tab->d_S, d_coef, lam, mu, accumulate);
+    ctx->err = "elasticity supports P1 and P2";
+    return FGPU_ERR_INVALID;
+}
+
+// ---------------------------------------------------------------------------
+// Load vector (linearformcontext.hpp:305, 395-410): element values into a
+// work buffer, then a per-node gather in element order (no float atomics).
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void rhs_element_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets, int ncomp,
+                                   int Q, const double* __restrict__ qx, const double* __restrict__ qw,
+                                   const double* __restrict__ phi, int fkind, double f0, double f1, double f2,
+                                   double* __restrict__ work) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
+        double X[4][3];
+        const int vv[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) X[v][d] = xyz[3 * (int64_t)vv[v] + d];
+        double K[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) K[r * 3 + c] = 0.5 * X[c + 1][r] - 0.5 * X[0][r];
+        double det = K[0] * (K[4] * K[8] - K[5] * K[7]) + K[1] * (K[5] * K[6] - K[3] * K[8]) + K[2] * (K[3] * K[7] - K[4] * K[6]);
+        double J = fabs(det);
+        double F[3][N];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int i = 0; i < N; ++i) F[c][i] = 0.0;
+        for (int q = 0; q < Q; ++q) {
+            double xh = qx[3 * q], yh = qx[3 * q + 1], zh = qx[3 * q + 2];
+            double g0 = -0.5 * (1 + xh + yh + zh), g1 = 0.5 * (1 + xh), g2 = 0.5 * (1 + yh), g3 = 0.5 * (1 + zh);
+            double p[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) p[d] = X[0][d] * g0 + X[1][d] * g1 + X[2][d] * g2 + X[3][d] * g3;
+            double wJ = qw[q] * J;
+            double fv[3];
+            if (fkind == FGPU_RHS_SINE) {
+                const double pi = 3.141592653589793;
+                fv[0] = 3.0 * pi * pi * sin(pi * p[0]) * sin(pi * p[1]) * sin(pi * p[2]);
+                fv[1] = fv[2] = 0.0;
+            } else if (fkind == FGPU_RHS_CONST_VEC) {
+                fv[0] = f0; fv[1] = f1; fv[2] = f2;
+            } else {
+                fv[0] = f0; fv[1] = fv[2] = 0.0;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (c >= ncomp) break;
+                double s = wJ * fv[c];
+#pragma unroll
+                for (int i = 0; i < N; ++i) F[c][i] += s * phi[q * N + i];
+            }
+        }
+        for (int c = 0; c < ncomp; ++c)
+#pragma unroll
+            for (int i = 0; i < N; ++i) work[(e * ncomp + c) * N + i] = F[c][i];
+    }
+}
+
+__global__ void rhs_gather_kernel(int64_t nnodes, int N, int ncomp, const int64_t* __restrict__ inc_ptr,
+                                  const int32_t* __restrict__ inc, const double* __restrict__ work,
+                                  double* __restrict__ out, int accumulate) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        for (int c = 0; c < ncomp; ++c) {
+            double s = accumulate ? out[m * ncomp + c] : 0.0;
+            for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
+                int32_t code = inc[t];
+                int64_t e = code >> 5;
+                int li = code & 31;
+                s += work[(e * ncomp + c) * N + li];
+            }
+            out[m * ncomp + c] = s;
+        }
+    }
+}
+
+int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fkind, const double* fc, double* d_out,
+               int accumulate, double* d_work) {
+    const fgpu_mesh* M = V->mesh;
+    int threads = 128;
+    int64_t blocks = std::min<int64_t>((M->nt + threads - 1) / threads, 152 * 32);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "rhs_element", ev);
+    switch (V->n) {
+        case 4: rhs_element_kernel<4><<<(int)blocks, threads, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, tab->Q, tab->d_qx, tab->d_qw, tab->d_phi, fkind, fc[0], fc[1], fc[2], d_work); break;
+        case 10: rhs_element_kernel<10><<<(int)blocks, threads, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, tab->Q, tab->d_qx, tab->d_qw, tab->d_phi, fkind, fc[0], fc[1], fc[2], d_work); break;
+        case 20: rhs_element_kernel<20><<<(int)blocks, threads, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, tab->Q, tab->d_qx, tab->d_qw, tab->d_phi, fkind, fc[0], fc[1], fc[2], d_work); break;
+        default: ctx->err = "unsupported order"; return FGPU_ERR_INVALID;
+    }
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    int64_t nn = V->topo.nnodes;
+    int64_t gb = std::min<int64_t>((nn + 255) / 256, 152 * 16);
+    if (gb < 1) gb = 1;
+    PendingEvent ev2;
+    prof_begin(ctx, "rhs_gather", ev2);
+    rhs_gather_kernel<<<(int)gb, 256, 0, ctx->stream>>>(nn, V->n, V->ncomp, V->d_inc_ptr, V->d_inc, d_work, d_out, accumulate);
+    prof_end(ctx, ev2);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Strong Dirichlet (MatrixPetsc::zeroRows, matrixpetsc.cpp:1762-1860), one
+// thread per row; the pattern is kept (MAT_KEEP_NONZERO_PATTERN).
+// ---------------------------------------------------------------------------
+template <typename VT>
+__global__ void dirichlet_kernel(int64_t nrows, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja,
+                                 VT* __restrict__ val, double* __restrict__ rhs, const uint8_t* __restrict__ mask,
+                                 const double* __restrict__ g, int mode, double diag) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = ia[r], e = ia[r + 1];
+        if (!mask[r]) {
+            if (mode == FGPU_ON_ELIMINATION_SYMMETRIC) {
+                double s = rhs ? rhs[r] : 0.0;
+                for (int64_t p = b; p < e; ++p) {
+                    int32_t c = ja[p];
+                    if (mask[c]) {
+                        s -= (double)val[p] * (g ? g[c] : 0.0);
+                        val[p] = (VT)0;
+                    }
+                }
+                if (rhs) rhs[r] = s;
+            }
+            continue;
+        }
+        double dkeep = 0.0;
+        for (int64_t p = b; p < e; ++p) {
+            if (ja[p] == r) dkeep = (double)val[p];
+        }
+        double d = mode == FGPU_ON_ELIMINATION_KEEP_DIAGONAL ? dkeep : diag;
+        for (int64_t p = b; p < e; ++p) val[p] = ja[p] == r ? (VT)d : (VT)0;
+        if (rhs) rhs[r] = d * (g ? g[r] : 0.0);
+    }
+}
+
+int launch_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, double* d_rhs, const uint8_t* d_mask, const double* d_g, int mode,
+                     double diag) {
+    int64_t blocks = std::min<int64_t>((A->nrows + 255) / 256, 152 * 16);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "dirichlet", ev);
+    if (A->precision == FGPU_F32)
+        dirichlet_kernel<float><<<(int)blocks, 256, 0, ctx->stream>>>(A->nrows, A->d_ia, A->d_ja, (float*)A->d_val, d_rhs,
+                                                                      d_mask, d_g, mode, diag);
+    else
+        dirichlet_kernel<double><<<(int)blocks, 256, 0, ctx->stream>>>(A->nrows, A->d_ia, A->d_ja, (double*)A->d_val, d_rhs,
+                                                                       d_mask, d_g, mode, diag);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Expanded (component) CSR of a vector space from its node pattern: row 3m+c
+// holds columns 3n+d for the neighbours n of m (ascending), d = 0..2.
+// ---------------------------------------------------------------------------
+__global__ void expand_ia_kernel(int64_t nnodes, int nc, const int64_t* __restrict__ sia, int64_t* __restrict__ ia) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m <= nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        if (m == nnodes) { ia[nnodes * nc] = (int64_t)nc * nc * sia[nnodes]; continue; }
+        int64_t len = sia[m + 1] - sia[m];
+        for (int c = 0; c < nc; ++c) ia[m * nc + c] = (int64_t)nc * nc * sia[m] + c * nc * len;
+    }
+}
+__global__ void expand_ja_kernel(int64_t nnodes, int nc, const int64_t* __restrict__ sia, const int32_t* __restrict__ sja,
+                                 int32_t* __restrict__ ja) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        int64_t b = sia[m], len = sia[m + 1] - b;
+        for (int c = 0; c < nc; ++c) {
+            int64_t o = (int64_t)nc * nc * b + c * nc * len;
+            for (int64_t k = 0; k < len; ++k)
+                for (int d = 0; d < nc; ++d) ja[o + k * nc + d] = sja[b + k] * nc + d;
+        }
+    }
+}
+
+int launch_expand_pattern(fgpu_ctx* ctx, const DevPattern& P, int nc, int64_t* d_ia, int32_t* d_ja) {
+    int64_t blocks = std::min<int64_t>((P.nrows + 256) / 256, 152 * 16);
+    expand_ia_kernel<<<(int)blocks, 256, 0, ctx->stream>>>(P.nrows, nc, P.d_ia, d_ia);
+    expand_ja_kernel<<<(int)blocks, 256, 0, ctx->stream>>>(P.nrows, nc, P.d_ia, P.d_ja, d_ja);
+    ctx->launches += 2;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+template <typename A, typename B>
+__global__ void convert_kernel(int64_t n, const A* __restrict__ a, B* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (B)a[i];
+}
+
+int launch_convert_values(fgpu_ctx* ctx, const fgpu_matrix* src, fgpu_matrix* dst) {
+    int64_t n = src->nnz;
+    int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "convert_values", ev);
+    if (src->precision == FGPU_F64 && dst->precision == FGPU_F32)
+        convert_kernel<double, float><<<(int)blocks, 256, 0, ctx->stream>>>(n, (const double*)src->d_val, (float*)dst->d_val);
+    else if (src->precision == FGPU_F32 && dst->precision == FGPU_F64)
+        convert_kernel<float, double><<<(int)blocks, 256, 0, ctx->stream>>>(n, (const float*)src->d_val, (double*)dst->d_val);
+    else
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(dst->d_val, src->d_val, n * (src->precision == FGPU_F32 ? 4 : 8),
+                                             cudaMemcpyDeviceToDevice, ctx->stream));
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+}  // namespace fgpu

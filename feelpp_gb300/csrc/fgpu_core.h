@@ -1,0 +1,209 @@
+// Internal declarations of the GB300 assembly backend (not part of the C-ABI).
+#pragma once
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fgpu.h"
+
+namespace fgpu {
+
+// ---------------------------------------------------------------------------
+// Reference tetrahedron conventions (Feel++: feelpp/feel/feelmesh/refsimplex.hpp:151-165,
+// feelpp/feel/feelmesh/simplexordering.hpp:284-293 edges, :341-347 faces).
+// ---------------------------------------------------------------------------
+extern const int kEdgeVerts[6][2];
+extern const int kFaceVerts[4][3];
+
+inline int nloc_of(int order) { return (order + 1) * (order + 2) * (order + 3) / 6; }
+inline int dofs_per_edge(int order) { return order - 1; }
+inline int dofs_per_face(int order) { return order >= 3 ? (order - 1) * (order - 2) / 2 : 0; }
+
+// Tabulated Lagrange basis of order p on a quadrature rule, and the reference
+// tensors of the affine Laplacian / mass / elasticity forms.
+struct RefTables {
+    int order = 0, n = 0, qdeg = 0, Q = 0;
+    std::vector<double> nodes;  // n x 3
+    std::vector<double> qx, qw; // Q x 3, Q
+    std::vector<double> phi;    // Q x n
+    std::vector<double> dphi;   // Q x n x 3 (reference gradients)
+    std::vector<double> S;      // 9 x n x n : S[ab][i][j] = sum_q w_q d_a phi_i d_b phi_j
+    std::vector<double> M;      // n x n     : sum_q w_q phi_i phi_j
+    std::vector<double> T7;     // 7 x n x n : symmetric Laplacian/mass tensors (S00,S11,S22,S01+S10,S02+S20,S12+S21,M)
+};
+bool lagrange_nodes(int order, std::vector<double>& xyz);
+bool build_ref_tables(int order, int qdeg, RefTables& out, std::string& err);
+
+// ---------------------------------------------------------------------------
+// Host topology: entities, DOF numbering, colouring, sparsity pattern.
+// ---------------------------------------------------------------------------
+struct Topology {
+    int order = 0;
+    int n = 0;                       // scalar local dofs per element
+    int64_t nnodes = 0;              // scalar dof nodes
+    std::vector<int32_t> l2n;        // T x n : element -> dof node (first-encounter numbering)
+    std::vector<int64_t> inc_ptr;    // nnodes + 1
+    std::vector<int32_t> inc;        // (element << 5) | local index, sorted by element per node
+    std::vector<uint8_t> edge_rev;   // T x 6 (1 when the element's edge is REVERSE-permuted)
+};
+bool build_topology(int64_t nv, int64_t nt, const int32_t* tets, int order, Topology& topo, std::string& err);
+
+struct NodePattern {                 // scalar node-to-node pattern (COUPLED + diagonal)
+    int64_t nrows = 0, nnz = 0;
+    int max_row = 0;
+    std::vector<int64_t> ia;
+    std::vector<int32_t> ja;
+};
+bool build_node_pattern(const Topology& topo, int64_t nt, NodePattern& pat, int nthreads, std::string& err);
+
+int colour_elements(int64_t nv, int64_t nt, const int32_t* tets, std::vector<int32_t>& perm,
+                    std::vector<int64_t>& colour_ptr);
+
+// Boundary dof nodes: the nodes carried by faces owned by one element; when
+// `xmax_on` only the faces whose three vertices satisfy x <= xmax (+1e-12).
+bool boundary_nodes(int64_t nt, const int32_t* tets, const double* xyz, const Topology& topo, int xmax_on,
+                    double xmax, std::vector<int32_t>& nodes);
+
+}  // namespace fgpu
+
+// ---------------------------------------------------------------------------
+// Opaque handle definitions.
+// ---------------------------------------------------------------------------
+struct ProfAcc {
+    int64_t count = 0;
+    double total_ms = 0;
+};
+struct PendingEvent {
+    std::string name;
+    cudaEvent_t start, stop;
+};
+
+struct fgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int profile = 0;
+    std::map<std::string, ProfAcc> prof;
+    std::vector<PendingEvent> pending;
+    std::vector<cudaEvent_t> event_pool;
+    int* d_status = nullptr;       // device status word written by kernels (bit flags)
+    int64_t launches = 0;          // kernels launched by this context
+    int host_threads = 1;
+};
+
+struct fgpu_mesh {
+    fgpu_ctx* ctx = nullptr;
+    int64_t nv = 0, nt = 0;
+    std::vector<double> h_xyz;
+    std::vector<int32_t> h_tets;
+    double* d_xyz = nullptr;
+    int32_t* d_tets = nullptr;
+    // element colouring (lazily built): elements sorted by colour
+    int ncolours = 0;
+    std::vector<int64_t> colour_ptr;
+    int32_t* d_colour_perm = nullptr;
+};
+
+struct DevPattern {                  // device copy of a scalar node pattern
+    int64_t nrows = 0, nnz = 0;
+    int max_row = 0;
+    int64_t* d_ia = nullptr;
+    int32_t* d_ja = nullptr;
+    ~DevPattern();
+};
+
+struct fgpu_space {
+    fgpu_ctx* ctx = nullptr;
+    fgpu_mesh* mesh = nullptr;
+    int order = 0, ncomp = 1, n = 0;
+    int64_t ndof = 0;
+    fgpu::Topology topo;
+    int32_t* d_l2n = nullptr;        // T x n
+    int64_t* d_inc_ptr = nullptr;
+    int32_t* d_inc = nullptr;
+    std::shared_ptr<DevPattern> pattern;   // scalar node pattern, built on demand
+    fgpu::NodePattern h_pattern;
+};
+
+struct fgpu_matrix {
+    fgpu_ctx* ctx = nullptr;
+    fgpu_space* space = nullptr;     // test == trial space
+    int precision = FGPU_F64;
+    int ncomp = 1;
+    int64_t nrows = 0, nnz = 0;
+    std::shared_ptr<DevPattern> pattern;   // scalar node pattern
+    int64_t* d_ia = nullptr;         // expanded (component) CSR row pointers
+    int32_t* d_ja = nullptr;         // expanded column indices (== pattern->d_ja when ncomp == 1)
+    bool own_ia_ja = false;
+    void* d_val = nullptr;           // nnz values (double or float)
+    double* d_coef = nullptr;        // per-element coefficient records of the last assembly
+    int64_t coef_cap = 0;
+};
+
+struct fgpu_vector {
+    fgpu_ctx* ctx = nullptr;
+    int64_t n = 0;
+    double* d = nullptr;
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (assemble.cu / solve.cu)
+// ---------------------------------------------------------------------------
+namespace fgpu {
+
+enum StatusBits : int {
+    kStatusBadElement = 1,     // |det K| <= 0 or non-finite
+    kStatusRowOverflow = 2,    // a pattern row longer than the kernel's staging buffer
+    kStatusMissingEntry = 4,   // an element column absent from its row (pattern mismatch)
+    kStatusBreakdown = 8,      // CG breakdown (p.Ap <= 0)
+};
+
+struct DevTables {                     // device copies of the reference tables
+    int order = 0, n = 0, Q = 0, qdeg = 0;
+    double* d_T7 = nullptr;            // 7 n n
+    double* d_S = nullptr;             // 9 n n
+    float* d_T7f = nullptr;
+    float* d_Sf = nullptr;
+    double* d_phi = nullptr;           // Q n
+    double* d_dphi = nullptr;          // Q n 3
+    double* d_qx = nullptr;            // Q 3
+    double* d_qw = nullptr;            // Q
+};
+DevTables* get_dev_tables(int order, int qdeg, std::string& err);
+
+void prof_begin(fgpu_ctx* ctx, const char* name, PendingEvent& ev);
+void prof_end(fgpu_ctx* ctx, PendingEvent& ev);
+
+int launch_geometry(fgpu_ctx* ctx, const fgpu_mesh* mesh, int kind, const double* d_kappa, double kappa,
+                    double mass, double lam, double mu, double* d_coef);
+int launch_assemble_gather(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, int kind, const double* d_coef,
+                           int accumulate);
+int launch_assemble_colour(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, int kind, const double* d_coef,
+                           int accumulate);
+int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fkind, const double* fc,
+               double* d_out, int accumulate, double* d_work);
+int launch_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, double* d_rhs, const uint8_t* d_mask, const double* d_g,
+                     int mode, double diag);
+int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y, double alpha_b, const double* b);
+int launch_convert_values(fgpu_ctx* ctx, const fgpu_matrix* src, fgpu_matrix* dst);
+
+int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_x, const fgpu_solver_cfg* cfg,
+              fgpu_solve_stats* st);
+int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A32, const double* d_b, double* d_x,
+                    const fgpu_solver_cfg* cfg, fgpu_solve_stats* st);
+
+}  // namespace fgpu
+
+#define FGPU_CUDA_CHECK(ctx, call)                                                        \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);              \
+            return FGPU_ERR_CUDA;                                                         \
+        }                                                                                 \
+    } while (0)

@@ -1,0 +1,220 @@
+/*
+ * fgpu.h — C-ABI of the GB300-native assembly + solve backend for the Feel++
+ * variational-form hot path:
+ *
+ *   auto a = form2(_test=Xh,_trial=Xh);
+ *   a  = integrate(_range=elements(mesh), _expr=kappa*inner(gradt(u),grad(v)) + idt(u)*id(v));
+ *   auto l = form1(_test=Xh);
+ *   l  = integrate(_range=elements(mesh), _expr=f*id(v));
+ *   a += on(_range=boundaryfaces(mesh), _rhs=l, _element=u, _expr=cst(0.));
+ *   a.solve(_rhs=l, _solution=u);
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns
+ * an int status (FGPU_OK == 0) and never aborts or throws; the message of the
+ * last failure is available from fgpu_last_error(). Objects are opaque
+ * handles owned by the library; host arrays passed in are copied.
+ *
+ * Each declaration names the Feel++ interface it replaces (paths relative to
+ * the Feel++ source tree).
+ */
+#ifndef FGPU_H
+#define FGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference aborts via CHKERRABORT / LOG(FATAL)) ---- */
+#define FGPU_OK 0
+#define FGPU_ERR_INVALID 1        /* bad argument / unsupported combination */
+#define FGPU_ERR_CUDA 2           /* CUDA runtime error */
+#define FGPU_ERR_BAD_ELEMENT 3    /* degenerate element: |det K| <= 0 or non-finite */
+#define FGPU_ERR_OUT_OF_RANGE 4   /* vertex / dof index out of range */
+#define FGPU_ERR_NOT_CONVERGED 5  /* solver reached maxit */
+#define FGPU_ERR_BREAKDOWN 6      /* CG breakdown (p.Ap <= 0: matrix not SPD) */
+#define FGPU_ERR_PATTERN 7        /* assembly met a column absent from the pattern */
+#define FGPU_ERR_ALLOC 8          /* device allocation failed */
+
+/* ---- precision / form kinds / options ---- */
+#define FGPU_F64 0
+#define FGPU_F32 1
+
+#define FGPU_FORM_LAPLACE_MASS 0  /* kappa*inner(gradt(u),grad(v)) + mass*idt(u)*id(v)          */
+#define FGPU_FORM_ELASTICITY 1    /* inner(lambda tr(eps(u)) I + 2 mu eps(u), grad(v)), Pchv    */
+
+#define FGPU_ALGO_AUTO 0          /* autotuned choice between the two below */
+#define FGPU_ALGO_GATHER 1        /* row-owner gather: each CSR row summed by one thread group */
+#define FGPU_ALGO_COLOUR 2        /* element-coloured scatter-add, colours in fixed order */
+
+#define FGPU_RHS_SINE 0           /* f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */
+#define FGPU_RHS_CONST_VEC 1      /* f = (c0, c1, c2) (Pchv) */
+#define FGPU_RHS_CONST 2          /* f = c0 */
+
+#define FGPU_ON_ELIMINATION 0     /* MatZeroRows: row zeroed, diag set, b_i = diag*g_i (default) */
+#define FGPU_ON_ELIMINATION_SYMMETRIC 1 /* MatZeroRowsColumns: also b_j -= A_ji g_i, column zeroed */
+#define FGPU_ON_ELIMINATION_KEEP_DIAGONAL 2 /* row zeroed except the diagonal, b_i = A_ii g_i */
+
+#define FGPU_PC_NONE 0
+#define FGPU_PC_JACOBI 1
+
+typedef struct fgpu_ctx fgpu_ctx;
+typedef struct fgpu_mesh fgpu_mesh;
+typedef struct fgpu_space fgpu_space;
+typedef struct fgpu_matrix fgpu_matrix;
+typedef struct fgpu_vector fgpu_vector;
+
+typedef struct {
+    int device;        /* CUDA device ordinal */
+    void* stream;      /* cudaStream_t to launch on, or NULL for a library-owned stream */
+    int profile;       /* 1: time every kernel launch with CUDA events (fgpu_prof_get) */
+    int host_threads;  /* host threads for setup work (pattern build); 0 = all cores */
+} fgpu_config;
+
+typedef struct {
+    int kind;                 /* FGPU_FORM_* */
+    double kappa;             /* constant diffusion coefficient when kappa_elem == NULL */
+    const double* kappa_elem; /* per-element coefficient (host array, T values) or NULL */
+    double mass;              /* coefficient of idt(u)*id(v) (0: pure Laplacian) */
+    double lambda, mu;        /* Lame coefficients (FGPU_FORM_ELASTICITY) */
+    int quad_degree;          /* exact quadrature degree; 0 = 2*order (feelvf default im(2p)) */
+    int algo;                 /* FGPU_ALGO_* */
+} fgpu_form_desc;
+
+typedef struct {
+    int kind;                 /* FGPU_RHS_* */
+    double c[3];
+    int quad_degree;          /* 0 = 2*order */
+} fgpu_rhs_desc;
+
+typedef struct {
+    double rtol;              /* stop when ||b - A x||_2 <= rtol ||b||_2 (ksp-rtol) */
+    int maxit;                /* ksp-max-it */
+    int pc;                   /* FGPU_PC_* (pc-type) */
+    int mixed;                /* 1: FP32 inner CG + FP64 residual refinement */
+    double inner_rtol;        /* inner relative tolerance of the mixed solver (0 = 1e-4) */
+    int check_every;          /* iterations per convergence poll (0 = 16) */
+} fgpu_solver_cfg;
+
+typedef struct {
+    int iterations;           /* total (inner) CG iterations */
+    int outer;                /* refinement steps (mixed) */
+    double rel_residual;      /* final ||b - A x||_2 / ||b||_2 recomputed in FP64 */
+    double time_ms;           /* solve wall time on the device stream */
+} fgpu_solve_stats;
+
+/* ---- context (replaces Feel::Environment + Backend<double>::build(kind),
+ *      feelpp/feel/feelalg/backend.cpp:218-250) ---- */
+int fgpu_create(const fgpu_config* cfg, fgpu_ctx** out);
+int fgpu_destroy(fgpu_ctx* ctx);
+const char* fgpu_last_error(const fgpu_ctx* ctx);
+int fgpu_sync(fgpu_ctx* ctx);
+/* number of kernels this context has launched so far */
+int64_t fgpu_launch_count(const fgpu_ctx* ctx);
+
+/* ---- mesh (replaces Mesh<Simplex<3>> element storage, feelpp/feel/feelmesh/
+ *      elements.hpp:780-809; vertex coordinates and tetrahedra in insertion order) ---- */
+int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, const int32_t* tets,
+                     fgpu_mesh** out);
+/* replace the vertex coordinates (host array, nv x 3): a moved mesh keeps its topology */
+int fgpu_mesh_set_coords(fgpu_mesh* mesh, const double* xyz);
+int fgpu_mesh_destroy(fgpu_mesh* mesh);
+
+/* ---- function space Pch<order> (ncomp = 1) / Pchv<order> (ncomp = 3)
+ *      (replaces FunctionSpace::init + DofTable::build, feelpp/feel/feeldiscr/
+ *      functionspace.hpp:1314-1440, doftable.hpp:1802-1970, 2364-2455) ---- */
+int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* mesh, int order, int ncomp, fgpu_space** out);
+int fgpu_space_ndof(const fgpu_space* V, int64_t* ndof, int* nloc);
+/* local-to-global table, T x (nloc*ncomp), local index nloc*c + l
+ * (DofTable::localToGlobalIndices, feelpp/feel/feeldiscr/doftable.hpp:742) */
+int fgpu_space_l2g(const fgpu_space* V, int32_t* out);
+/* dofs of the faces owned by one element (boundaryfaces(mesh)); with xmax_on only
+ * faces whose vertices all have x <= xmax (a marked face range). Call with dofs
+ * == NULL to get the count. (IntegratorOnExpr::onFaces, feelpp/feel/feelvf/on.hpp:457-701) */
+int fgpu_space_boundary_dofs(const fgpu_space* V, int xmax_on, double xmax, int64_t* count, int32_t* dofs);
+int fgpu_space_destroy(fgpu_space* V);
+
+/* ---- matrix (replaces Backend::newMatrix -> stencil() -> GraphCSR::close ->
+ *      MatrixPetsc::init, feelpp/feel/feelalg/backend.hpp:349-452,
+ *      feelpp/feel/feeldiscr/stencil.hpp:1500-1692, feelpp/feel/feelalg/graphcsr.cpp:634-660,
+ *      990-1020, matrixpetsc.cpp:316-415). The pattern is COUPLED with a nonzero diagonal. ---- */
+int fgpu_matrix_create(fgpu_ctx* ctx, fgpu_space* test, fgpu_space* trial, int precision, fgpu_matrix** out);
+/* a matrix with the same pattern and another value precision (values not copied) */
+int fgpu_matrix_create_like(const fgpu_matrix* A, int precision, fgpu_matrix** out);
+int fgpu_matrix_info(const fgpu_matrix* A, int64_t* nrows, int64_t* nnz, int* precision);
+/* host copies of the CSR arrays; any pointer may be NULL (values as double) */
+int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* val);
+/* device pointer of the value array (double or float per precision) */
+int fgpu_matrix_values_device(const fgpu_matrix* A, void** dptr);
+/* MatrixPetsc::zero (MatZeroEntries, matrixpetsc.cpp:617-627) */
+int fgpu_matrix_zero(fgpu_matrix* A);
+/* dst = (precision of dst) src values, same pattern */
+int fgpu_matrix_convert(const fgpu_matrix* src, fgpu_matrix* dst);
+int fgpu_matrix_destroy(fgpu_matrix* A);
+
+/* ---- a = integrate(elements(mesh), expr) / a += ... (BilinearForm::operator= / +=
+ *      -> Integrator::assemble -> BilinearForm::Context::integrate/assemble ->
+ *      MatrixPetsc::addMatrix; feelpp/feel/feelvf/bilinearform.hpp:1440-1456,
+ *      integrator.hpp:975-1238, bilinearformcontext.hpp:458-628, 784-847,
+ *      feelpp/feel/feelalg/matrixpetsc.cpp:919-935). accumulate = 0 for '=', 1 for '+='. ---- */
+int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, int accumulate);
+/* same, with the per-element coefficient already on the device (T doubles) */
+int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, const double* d_kappa,
+                             int accumulate);
+
+/* ---- vectors (replaces VectorPetsc, feelpp/feel/feelalg/vectorpetsc.cpp) ---- */
+int fgpu_vector_create(fgpu_ctx* ctx, int64_t n, fgpu_vector** out);
+int fgpu_vector_upload(fgpu_vector* v, const double* host);
+int fgpu_vector_download(const fgpu_vector* v, double* host);
+int fgpu_vector_zero(fgpu_vector* v);
+int fgpu_vector_device(const fgpu_vector* v, double** dptr);
+int fgpu_vector_destroy(fgpu_vector* v);
+
+/* ---- l = integrate(elements(mesh), f*id(v)) (LinearForm::operator= / +=,
+ *      feelpp/feel/feelvf/linearform.hpp:1209-1230, linearformcontext.hpp:305, 395-410) ---- */
+int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, fgpu_vector* out,
+                         int accumulate);
+
+/* ---- a += on(range, rhs=l, element=u, expr=g) (feelpp/feel/feelvf/on.hpp:1140-1190 ->
+ *      MatrixPetsc::zeroRows, feelpp/feel/feelalg/matrixpetsc.cpp:1762-1860).
+ *      dofs: host array of ndofs global dof indices; values: g at those dofs (NULL = 0). ---- */
+int fgpu_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, fgpu_vector* rhs, int64_t ndofs, const int32_t* dofs,
+                   const double* values, int mode, double diag);
+
+/* ---- y = A x (MatrixSparse::multVector / MatMult) ---- */
+int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, fgpu_vector* y);
+
+/* ---- a.solve(_rhs=l, _solution=u) with --ksp-type=cg --pc-type=jacobi
+ *      (BilinearFormBase::solve -> Backend::solve -> SolverLinearPetsc::solve,
+ *      feelpp/feel/feelvf/bilinearformbase.hpp:447-466, feelpp/feel/feelalg/
+ *      solverlinearpetsc.cpp:490-570). A32 is used by the mixed solver (may be
+ *      NULL: then it is made from A). x is the initial guess and the solution. ---- */
+int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
+                  const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+
+/* ---- host-only queries (no device needed): the dof numbering, the sparsity
+ *      pattern and the reference tables the device kernels use ---- */
+/* dof table of Pch/Pchv<order> on a mesh: l2g (T x nloc*ncomp) as fgpu_space_l2g;
+ * returns the number of dofs in *ndof (DofTable::build, doftable.hpp:1802-1970) */
+int fgpu_host_dof_table(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int32_t* l2g,
+                        int64_t* ndof);
+/* CSR pattern of Pch/Pchv<order> (Stencil::computeGraph + GraphCSR::close). Call with
+ * ja == NULL to fill ia (ndof + 1) and get *nnz, then again with ja (nnz). */
+int fgpu_host_pattern(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int64_t* ia, int32_t* ja,
+                      int64_t* nnz);
+/* Lagrange node set (nloc x 3), basis values (Q x nloc) and reference gradients
+ * (Q x nloc x 3) at the degree-qdeg rule, and the reference tensors
+ * S (9 x nloc x nloc) and M (nloc x nloc); any output may be NULL. Returns Q in *npts. */
+int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double* dphi, double* S, double* M,
+                         int* npts);
+
+/* ---- per-kernel device timings (CUDA events), enabled by fgpu_config.profile ---- */
+int fgpu_prof_reset(fgpu_ctx* ctx);
+/* total device time and launch count of the kernels tagged `name` */
+int fgpu_prof_get(fgpu_ctx* ctx, const char* name, int64_t* count, double* total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FGPU_H */

@@ -1,0 +1,188 @@
+"""ctypes bindings of the oracle library (test infrastructure only).
+
+Every function mirrors one ``orc_*`` entry point of ``oracle/oracle.cpp``;
+arrays are numpy arrays (float64 / int32 / int64, C-contiguous).
+"""
+import ctypes as C
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        i64, i32, f64 = C.c_int64, C.c_int, C.c_double
+        sig = {
+            "orc_version": (i32, []),
+            "orc_quad": (i32, [i32, P]),
+            "orc_nodes": (i32, [i32, P]),
+            "orc_gll": (i32, [i32, P]),
+            "orc_tabulate": (i32, [i32, i32, P, P, P]),
+            "orc_dof_table": (i64, [i64, P, i32, i32, P]),
+            "orc_pattern": (i32, [i64, i64, i32, P, P, P]),
+            "orc_geometry": (i32, [P, i64, P, P, P, P]),
+            "orc_assemble": (i32, [i32, i32, i32, P, i64, P, P, i32, P, f64, f64, f64, f64, i64, P, P, P, i32, i64]),
+            "orc_rhs": (i32, [i32, i32, i32, P, i64, P, P, i32, P, P]),
+            "orc_boundary_mask": (i32, [i32, i32, P, i64, P, P, i32, f64, i64, P]),
+            "orc_dirichlet": (i32, [i64, P, P, P, P, P, P, i32, f64]),
+            "orc_spmv": (i32, [i64, P, P, P, P, P]),
+            "orc_pcg": (i32, [i64, P, P, P, P, P, f64, i32, P, i32]),
+            "orc_errors": (i32, [i32, i32, P, i64, P, P, P, P, P]),
+            "orc_num_threads": (i32, []),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def nloc(order):
+    return (order + 1) * (order + 2) * (order + 3) // 6
+
+
+def quad(deg):
+    n = lib().orc_quad(deg, None)
+    out = np.zeros((n, 4))
+    lib().orc_quad(deg, _p(out))
+    return out
+
+
+def nodes(order):
+    out = np.zeros((nloc(order), 3))
+    lib().orc_nodes(order, _p(out))
+    return out
+
+
+def gll(n):
+    out = np.zeros(n)
+    lib().orc_gll(n, _p(out))
+    return out
+
+
+def tabulate(order, pts):
+    pts = _c(pts, np.float64)
+    n = nloc(order)
+    phi = np.zeros((len(pts), n))
+    dphi = np.zeros((len(pts), n, 3))
+    lib().orc_tabulate(order, len(pts), _p(pts), _p(phi), _p(dphi))
+    return phi, dphi
+
+
+def dof_table(tets, order, ncomp=1):
+    tets = _c(tets, np.int32)
+    T = len(tets)
+    l2g = np.zeros((T, nloc(order) * ncomp), dtype=np.int32)
+    N = lib().orc_dof_table(T, _p(tets), order, ncomp, _p(l2g))
+    return int(N), l2g
+
+
+def pattern(N, l2g):
+    l2g = _c(l2g, np.int32)
+    ia = np.zeros(N + 1, dtype=np.int64)
+    lib().orc_pattern(N, l2g.shape[0], l2g.shape[1], _p(l2g), _p(ia), None)
+    ja = np.zeros(int(ia[-1]), dtype=np.int32)
+    lib().orc_pattern(N, l2g.shape[0], l2g.shape[1], _p(l2g), _p(ia), _p(ja))
+    return ia, ja
+
+
+def geometry(xyz, tets):
+    xyz = _c(xyz, np.float64)
+    tets = _c(tets, np.int32)
+    T = len(tets)
+    J = np.zeros(T)
+    B = np.zeros((T, 3, 3))
+    d = np.zeros(T)
+    lib().orc_geometry(_p(xyz), T, _p(tets), _p(J), _p(B), _p(d))
+    return J, B, d
+
+
+def assemble(order, xyz, tets, l2g, ia, ja, kind=0, kappa=None, kappa_const=1.0, mass=0.0,
+             lam=1.0, mu=0.5, qdeg=None, ncomp=1, nthreads=1, val=None):
+    xyz = _c(xyz, np.float64)
+    tets = _c(tets, np.int32)
+    l2g = _c(l2g, np.int32)
+    if qdeg is None:
+        qdeg = 2 * order
+    N = len(ia) - 1
+    if val is None:
+        val = np.zeros(len(ja))
+    kap = None if kappa is None else _c(kappa, np.float64)
+    rc = lib().orc_assemble(order, ncomp, qdeg, _p(xyz), len(tets), _p(tets), _p(l2g), kind, _p(kap),
+                            kappa_const, mass, lam, mu, N, _p(ia), _p(ja), _p(val), nthreads, len(xyz))
+    if rc != 0:
+        raise RuntimeError("orc_assemble failed: %d" % rc)
+    return val
+
+
+def rhs(order, xyz, tets, l2g, N, fkind=0, fc=(0.0, 0.0, 0.0), qdeg=None, ncomp=1):
+    xyz = _c(xyz, np.float64)
+    tets = _c(tets, np.int32)
+    l2g = _c(l2g, np.int32)
+    if qdeg is None:
+        qdeg = 2 * order
+    F = np.zeros(N)
+    fcv = np.array(fc, dtype=np.float64)
+    rc = lib().orc_rhs(order, ncomp, qdeg, _p(xyz), len(tets), _p(tets), _p(l2g), fkind, _p(fcv), _p(F))
+    if rc != 0:
+        raise RuntimeError("orc_rhs failed: %d" % rc)
+    return F
+
+
+def boundary_mask(order, xyz, tets, l2g, N, ncomp=1, xplane=None):
+    xyz = _c(xyz, np.float64)
+    tets = _c(tets, np.int32)
+    l2g = _c(l2g, np.int32)
+    mask = np.zeros(N, dtype=np.uint8)
+    lib().orc_boundary_mask(order, ncomp, _p(xyz), len(tets), _p(tets), _p(l2g),
+                            0 if xplane is None else 1, 0.0 if xplane is None else xplane, N, _p(mask))
+    return mask
+
+
+def dirichlet(ia, ja, val, b, mask, g=None, mode=0, diag=1.0):
+    N = len(ia) - 1
+    gg = None if g is None else _c(g, np.float64)
+    lib().orc_dirichlet(N, _p(ia), _p(ja), _p(val), _p(b), _p(mask), _p(gg), mode, diag)
+
+
+def spmv(ia, ja, val, x):
+    y = np.zeros(len(ia) - 1)
+    lib().orc_spmv(len(ia) - 1, _p(ia), _p(ja), _p(val), _p(_c(x, np.float64)), _p(y))
+    return y
+
+
+def pcg(ia, ja, val, b, rtol=1e-10, maxit=10000, nthreads=1):
+    N = len(ia) - 1
+    x = np.zeros(N)
+    res = np.zeros(1)
+    it = lib().orc_pcg(N, _p(ia), _p(ja), _p(val), _p(_c(b, np.float64)), _p(x), rtol, maxit, _p(res), nthreads)
+    return x, int(it), float(res[0])
+
+
+def errors(order, xyz, tets, l2g, u, qdeg):
+    l2 = np.zeros(1)
+    h1 = np.zeros(1)
+    rc = lib().orc_errors(order, qdeg, _p(_c(xyz, np.float64)), len(tets), _p(_c(tets, np.int32)),
+                          _p(_c(l2g, np.int32)), _p(_c(u, np.float64)), _p(l2), _p(h1))
+    if rc != 0:
+        raise RuntimeError("orc_errors failed")
+    return float(l2[0]), float(h1[0])
+
+
+def num_threads():
+    return lib().orc_num_threads()

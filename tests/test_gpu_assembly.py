@@ -1,0 +1,186 @@
+"""Device assembly parity against the oracle (run on a GB300).
+
+Tolerances: the plain FP64 path must match per entry within
+|a - b| <= 1e-12 |b| + 1e-14 max|A| (helpers.RTOL_F64 / ATOL_F64); the FP32 path
+is reported against the FP64 oracle and must stay within 2e-5 relative to the
+largest entry of its row block."""
+import numpy as np
+import pytest
+
+import feelpp_gb300 as fpp
+from feelpp_gb300 import meshgen
+from tests.helpers import assert_values_close, mesh, oracle_system
+
+pytestmark = pytest.mark.gpu
+
+
+def device_matrix(env, xyz, tets, order, kappa=1.0, mass=1.0, ncomp=1, elasticity=None, precision="f64"):
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.FunctionSpace(M, order, ncomp)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V, precision=precision)
+    if elasticity is not None:
+        a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, *elasticity), fpp.grad(v))))
+    else:
+        expr = kappa * fpp.inner(fpp.gradt(u), fpp.grad(v))
+        if mass:
+            expr = expr + mass * (fpp.idt(u) * fpp.id(v))
+        a.assign(fpp.integrate(fpp.elements(M), expr))
+    return M, V, a
+
+
+def test_p1_unit_cube_16_plain_fp64(env, oracle):
+    """P1 Laplacian stiffness + mass on the 16^3 Kuhn cube (24 576 tets), perturbed 0.2h."""
+    xyz, tets = mesh(16, perturb=0.2)
+    M, V, a = device_matrix(env, xyz, tets, 1)
+    assert V.ndof == 4913 and a.nnz == 66961
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 1, mass=1.0)
+    assert np.array_equal(V.dof_l2g(), l2g)
+    dia, dja, dval = a.csr()
+    assert np.array_equal(dia, ia) and np.array_equal(dja, ja)
+    assert_values_close(dval, val)
+
+
+@pytest.mark.parametrize("order,n", [(1, 6), (2, 6), (3, 4)])
+def test_lognormal_kappa_parity(env, oracle, order, n):
+    xyz, tets = mesh(n, perturb=0.15)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M, V, a = device_matrix(env, xyz, tets, order, kappa=kappa, mass=1.0)
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, order, kappa=kappa, mass=1.0)
+    dia, dja, dval = a.csr()
+    assert np.array_equal(dia, ia) and np.array_equal(dja, ja)
+    assert_values_close(dval, val)
+
+
+@pytest.mark.parametrize("order,n", [(2, 6), (3, 4)])
+def test_fp32_assembly_error_vs_fp64_oracle(env, oracle, order, n):
+    xyz, tets = mesh(n, perturb=0.15)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M, V, a = device_matrix(env, xyz, tets, order, kappa=kappa, mass=1.0, precision="f32")
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, order, kappa=kappa, mass=1.0)
+    dval = a.values()
+    scale = np.abs(val).max()
+    err = np.abs(dval - val) / scale
+    assert err.max() < 2e-5, err.max()
+
+
+def test_elasticity_p2_parity(env, oracle):
+    xyz, tets = mesh(3, perturb=0.1, lengths=(4.0, 1.0, 1.0))
+    M, V, a = device_matrix(env, xyz, tets, 2, ncomp=3, elasticity=(1.0, 0.5))
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 2, ncomp=3, kind=1, lam=1.0, mu=0.5)
+    assert np.array_equal(V.dof_l2g(), l2g)
+    dia, dja, dval = a.csr()
+    assert np.array_equal(dia, ia) and np.array_equal(dja, ja)
+    assert_values_close(dval, val)
+
+
+def test_elasticity_p1_parity(env, oracle):
+    xyz, tets = mesh(4, perturb=0.2)
+    M, V, a = device_matrix(env, xyz, tets, 1, ncomp=3, elasticity=(2.0, 0.3))
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 1, ncomp=3, kind=1, lam=2.0, mu=0.3)
+    dia, dja, dval = a.csr()
+    assert np.array_equal(dja, ja)
+    assert_values_close(dval, val)
+
+
+def test_accumulate_and_reassign(env, oracle):
+    xyz, tets = mesh(4, perturb=0.2)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a += fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v)))
+    a += fpp.integrate(fpp.elements(M), fpp.idt(u) * fpp.id(v))
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 2, mass=1.0)
+    assert_values_close(a.values(), val)
+    a.assign(fpp.integrate(fpp.elements(M), 2.0 * fpp.inner(fpp.gradt(u), fpp.grad(v))))
+    N, l2g, ia, ja, val2 = oracle_system(oracle, xyz, tets, 2, kappa=np.full(len(tets), 2.0), mass=0.0)
+    assert_values_close(a.values(), val2)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_load_vector_parity(env, oracle, order):
+    xyz, tets = mesh(4, perturb=0.2)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, order)
+    v = V.element()
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    N, l2g = oracle.dof_table(tets, order)
+    F = oracle.rhs(order, xyz, tets, l2g, N, fkind=0)
+    assert_values_close(l.to_numpy(), F, what="load vector")
+
+
+def test_vector_load_parity(env, oracle):
+    xyz, tets = mesh(3, perturb=0.1, lengths=(4.0, 1.0, 1.0))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, 2)
+    v = V.element()
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.cst_vec(0, 0, -1), fpp.id(v))))
+    N, l2g = oracle.dof_table(tets, 2, 3)
+    F = oracle.rhs(2, xyz, tets, l2g, N, fkind=1, fc=(0.0, 0.0, -1.0), ncomp=3)
+    assert_values_close(l.to_numpy(), F, what="vector load")
+
+
+@pytest.mark.parametrize("mode_name,mode", [("elimination", 0), ("elimination_symmetric", 1),
+                                            ("elimination_keep_diagonal", 2)])
+def test_dirichlet_modes(env, oracle, mode_name, mode):
+    xyz, tets = mesh(4, perturb=0.2)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v))))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.25, type=mode_name)
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 2, mass=0.0)
+    b = oracle.rhs(2, xyz, tets, l2g, N, fkind=0)
+    mask = oracle.boundary_mask(2, xyz, tets, l2g, N)
+    assert np.array_equal(np.sort(V.boundary_dofs()), np.nonzero(mask)[0])
+    oracle.dirichlet(ia, ja, val, b, mask, g=np.full(N, 0.25), mode=mode)
+    assert_values_close(a.values(), val, what="matrix after on()")
+    assert_values_close(l.to_numpy(), b, what="rhs after on()")
+
+
+def test_bad_element_reported(env):
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [0, 0, 1]], dtype=float)
+    tets = np.array([[0, 1, 2, 3], [0, 1, 2, 4]], dtype=np.int32)   # first tet is flat (det K = 0)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 1)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    with pytest.raises(fpp.FgpuError) as ei:
+        a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v))))
+    assert ei.value.code == 3
+    # the context stays usable
+    xyz2, tets2 = mesh(2)
+    M2, V2, a2 = device_matrix(env, xyz2, tets2, 1)
+    assert a2.nnz > 0
+
+
+def test_p2_large_properties(env):
+    """P2 on 40^3 (384 000 tets, nnz 15.0 M): size-independent checks on the full matrix."""
+    import scipy.sparse as sp
+    n = 40
+    xyz, tets = mesh(n, perturb=0.15)
+    M, V, a = device_matrix(env, xyz, tets, 2, kappa=1.0, mass=0.0)
+    assert V.ndof == (2 * n + 1) ** 3 and a.nnz == 230 * n ** 3 + 138 * n ** 2 + 24 * n + 1
+    ia, ja, val = a.csr()
+    A = sp.csr_matrix((val, ja, ia), shape=(V.ndof, V.ndof))
+    scale = np.abs(val).max()
+    assert np.abs(A @ np.ones(V.ndof)).max() < 1e-11 * scale            # constants in the kernel
+    assert abs(A - A.T).max() < 1e-14 * scale                           # symmetric
+    Mm, Vm, m = device_matrix(env, xyz, tets, 2, kappa=0.0, mass=1.0)
+    assert abs(m.values().sum() - 1.0) < 1e-11                          # 1^T M 1 = |Omega|
+
+
+def test_deterministic_repeat(env):
+    xyz, tets = mesh(8, perturb=0.2)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M, V, a = device_matrix(env, xyz, tets, 3, kappa=kappa)
+    v1 = a.values()
+    u, v = V.element(), V.element()
+    a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v)))
+    assert np.array_equal(v1, a.values())

@@ -1,0 +1,96 @@
+"""Device CG / Jacobi solves against the oracle (run on a GB300)."""
+import numpy as np
+import pytest
+
+import feelpp_gb300 as fpp
+from tests.helpers import mesh, oracle_system
+
+pytestmark = pytest.mark.gpu
+
+
+def poisson(env, n, order, perturb=0.2, mode="elimination_symmetric"):
+    xyz, tets = mesh(n, perturb=perturb)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, order)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v))))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type=mode)
+    return xyz, tets, M, V, u, a, l
+
+
+@pytest.mark.parametrize("order,n", [(1, 16), (2, 8), (3, 5)])
+def test_pcg_matches_oracle(env, oracle, order, n):
+    xyz, tets, M, V, u, a, l = poisson(env, n, order)
+    st = a.solve(rhs=l, solution=u, rtol=1e-10)
+    assert st["rel_residual"] <= 1e-10
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, order, mass=0.0)
+    b = oracle.rhs(order, xyz, tets, l2g, N, fkind=0)
+    mask = oracle.boundary_mask(order, xyz, tets, l2g, N)
+    oracle.dirichlet(ia, ja, val, b, mask, mode=1)
+    x, it, res = oracle.pcg(ia, ja, val, b, rtol=1e-10)
+    ud = u.to_numpy()
+    assert np.linalg.norm(ud - x) <= 1e-8 * np.linalg.norm(x)
+    # same Krylov method and preconditioner: iteration counts agree closely
+    assert abs(st["iterations"] - it) <= max(2, 0.02 * it)
+
+
+@pytest.mark.parametrize("order,n", [(2, 12), (3, 8)])
+def test_mixed_precision_refinement_reaches_1e10(env, oracle, order, n):
+    xyz, tets, M, V, u, a, l = poisson(env, n, order)
+    st = a.solve(rhs=l, solution=u, rtol=1e-10, mixed=True)
+    assert st["rel_residual"] <= 1e-10 and st["outer"] >= 2
+    u64 = V.element()
+    st64 = a.solve(rhs=l, solution=u64, rtol=1e-10)
+    x32, x64 = u.to_numpy(), u64.to_numpy()
+    assert np.linalg.norm(x32 - x64) <= 1e-8 * np.linalg.norm(x64)
+    # discretisation error within 1% of the FP64 solve's
+    N, l2g = oracle.dof_table(tets, order)
+    e32 = oracle.errors(order, xyz, tets, l2g, x32, 2 * order + 2 if 2 * order + 2 <= 8 else 8)
+    e64 = oracle.errors(order, xyz, tets, l2g, x64, 2 * order + 2 if 2 * order + 2 <= 8 else 8)
+    assert abs(e32[0] - e64[0]) <= 0.01 * e64[0]
+
+
+def test_manufactured_solution_rates(env, oracle):
+    errs = []
+    for n in (8, 16):
+        xyz, tets, M, V, u, a, l = poisson(env, n, 2, perturb=0.0)
+        a.solve(rhs=l, solution=u, rtol=1e-12)
+        N, l2g = oracle.dof_table(tets, 2)
+        errs.append(oracle.errors(2, xyz, tets, l2g, u.to_numpy(), 8))
+    assert np.log2(errs[0][0] / errs[1][0]) > 2.7   # L2 ~ h^3
+    assert np.log2(errs[0][1] / errs[1][1]) > 1.8   # H1 ~ h^2
+
+
+def test_elasticity_solve(env, oracle):
+    xyz, tets = mesh(4, perturb=0.0, lengths=(4.0, 1.0, 1.0))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, 2)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, 1.0, 0.5), fpp.grad(v))))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.cst_vec(0, 0, -1), fpp.id(v))))
+    a += fpp.on(fpp.markedfaces(M, 0.0), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    st = a.solve(rhs=l, solution=u, rtol=1e-10, mixed=True)
+    assert st["rel_residual"] <= 1e-10
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 2, ncomp=3, kind=1, lam=1.0, mu=0.5)
+    b = oracle.rhs(2, xyz, tets, l2g, N, fkind=1, fc=(0, 0, -1), ncomp=3)
+    mask = oracle.boundary_mask(2, xyz, tets, l2g, N, ncomp=3, xplane=0.0)
+    oracle.dirichlet(ia, ja, val, b, mask, mode=1)
+    x, it, res = oracle.pcg(ia, ja, val, b, rtol=1e-12, maxit=100000)
+    assert np.linalg.norm(u.to_numpy() - x) <= 1e-8 * np.linalg.norm(x)
+    assert x.reshape(-1, 3)[:, 2].min() < 0          # the beam sags under (0, 0, -1)
+
+
+def test_matrix_mult(env, oracle):
+    xyz, tets, M, V, u, a, l = poisson(env, 6, 3)
+    x = np.random.default_rng(0).standard_normal(V.ndof)
+    xv, yv = V.element(), V.element()
+    xv.upload(x)
+    a.mult(xv, yv)
+    ia, ja, val = a.csr()
+    y = oracle.spmv(ia, ja, val, x)
+    assert np.abs(yv.to_numpy() - y).max() <= 1e-13 * np.abs(y).max()

@@ -1,0 +1,176 @@
+"""Known-answer tests pinning the oracle (CPU only).
+
+The reference stores no golden matrices; its tests pin the path through
+properties, restated here against the oracle:
+  * quadrature exactness (testsuite/feelpoly/test_qm_pk_3D.cpp,
+    testsuite/feelintegration/test_integration.cpp:860-923, tolerance 10^{-2 Order});
+  * Lagrange Kronecker property at the nodes (testsuite/feelpoly/testlagrange.hpp);
+  * warp-blend P3 edge nodes at the Gauss-Lobatto positions (warpblend.hpp:92-115);
+  * form energies equal to integrals (testsuite/feelvf/test_forms.cpp:131-180, 1e-10);
+  * stiffness rows sum to zero (constants are in the kernel), 1^T M 1 = |Omega|;
+  * P2 Laplacian consistency (testsuite/feelvf/test_laplacian.cpp, 1e-9).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from tests.helpers import mesh, oracle_system
+
+
+@pytest.mark.parametrize("deg", range(1, 9))
+def test_quadrature_exact_on_monomials(oracle, deg):
+    q = oracle.quad(deg)
+    x, y, z, w = (q[:, 0] + 1) / 2, (q[:, 1] + 1) / 2, (q[:, 2] + 1) / 2, q[:, 3] / 8
+    assert abs(q[:, 3].sum() - 4.0 / 3.0) < 1e-13
+    for a in range(deg + 1):
+        for b in range(deg + 1 - a):
+            for c in range(deg + 1 - a - b):
+                exact = math.factorial(a) * math.factorial(b) * math.factorial(c) / math.factorial(a + b + c + 3)
+                got = (w * x ** a * y ** b * z ** c).sum()
+                assert abs(got - exact) <= 1e-13 * exact + 1e-16
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_lagrange_kronecker(oracle, order):
+    P = oracle.nodes(order)
+    phi, dphi = oracle.tabulate(order, P)
+    assert np.abs(phi - np.eye(len(P))).max() < 1e-13
+    assert np.abs(dphi.sum(axis=1)).max() < 1e-12   # partition of unity -> gradients sum to 0
+
+
+def test_p3_edge_nodes_are_gll(oracle):
+    g = oracle.gll(4)
+    assert np.allclose(g, [-1, -1 / math.sqrt(5), 1 / math.sqrt(5), 1], atol=1e-15)
+    P = oracle.nodes(3)
+    V = np.array([[-1, -1, -1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=float)
+    e2p = [(1, 2), (2, 0), (0, 1), (0, 3), (1, 3), (2, 3)]
+    for e, (a, b) in enumerate(e2p):
+        for l, t in enumerate([(1 - 1 / math.sqrt(5)) / 2, (1 + 1 / math.sqrt(5)) / 2]):
+            assert np.abs(P[4 + 2 * e + l] - (V[a] + t * (V[b] - V[a]))).max() < 1e-15
+    f2p = [(1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)]
+    for f, vs in enumerate(f2p):
+        assert np.abs(P[16 + f] - V[list(vs)].mean(axis=0)).max() < 1e-15
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_dof_counts_and_pattern_sizes(oracle, order):
+    n = 3
+    xyz, tets = mesh(n)
+    N, l2g = oracle.dof_table(tets, order)
+    assert N == (order * n + 1) ** 3
+    ia, ja = oracle.pattern(N, l2g)
+    nnz = {1: 15 * n ** 3 + 21 * n ** 2 + 9 * n + 1, 2: 230 * n ** 3 + 138 * n ** 2 + 24 * n + 1,
+           3: 1311 * n ** 3 + 459 * n ** 2 + 45 * n + 1}[order]
+    assert ia[-1] == nnz
+    for r in range(N):
+        row = ja[ia[r]:ia[r + 1]]
+        assert np.all(np.diff(row) > 0) and r in row
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_stiffness_properties(oracle, order):
+    xyz, tets = mesh(3, perturb=0.2)
+    N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, order, mass=0.0)
+    ones = np.ones(N)
+    assert np.abs(oracle.spmv(ia, ja, K, ones)).max() < 1e-12 * np.abs(K).max()
+    # u = linear function: u^T K u = int |grad u|^2 = |Omega| |a|^2 (interpolation of a linear field is exact)
+    P = oracle.nodes(order)
+    X = np.zeros((N, 3))
+    for e in range(len(tets)):
+        v = xyz[tets[e]]
+        lam = np.stack([-(1 + P[:, 0] + P[:, 1] + P[:, 2]) / 2, (1 + P[:, 0]) / 2, (1 + P[:, 1]) / 2, (1 + P[:, 2]) / 2], 1)
+        X[l2g[e]] = lam @ v
+    a = np.array([0.3, -1.2, 0.7])
+    u = X @ a
+    energy = u @ oracle.spmv(ia, ja, K, u)
+    assert abs(energy - (a @ a) * 1.0) < 1e-10
+    # symmetry
+    import scipy.sparse as sp
+    A = sp.csr_matrix((K, ja, ia), shape=(N, N))
+    assert abs(A - A.T).max() < 1e-14 * np.abs(K).max()
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_mass_total_is_volume(oracle, order):
+    xyz, tets = mesh(3, perturb=0.15)
+    N, l2g, ia, ja, M = oracle_system(oracle, xyz, tets, order, kappa=np.zeros(len(tets)), mass=1.0)
+    assert abs(M.sum() - 1.0) < 1e-13
+
+
+def test_p2_laplacian_consistency(oracle):
+    # test_laplacian.cpp: for u quadratic, (K u)_i = int grad u . grad phi_i = -int lap(u) phi_i + boundary terms;
+    # restated as u^T K w = int grad u . grad w for two quadratic interpolants.
+    xyz, tets = mesh(2, perturb=0.0)
+    N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, 2, mass=0.0)
+    P = oracle.nodes(2)
+    X = np.zeros((N, 3))
+    for e in range(len(tets)):
+        v = xyz[tets[e]]
+        lam = np.stack([-(1 + P[:, 0] + P[:, 1] + P[:, 2]) / 2, (1 + P[:, 0]) / 2, (1 + P[:, 1]) / 2, (1 + P[:, 2]) / 2], 1)
+        X[l2g[e]] = lam @ v
+    u = X[:, 0] ** 2          # grad u = (2x, 0, 0)
+    w = X[:, 0] * X[:, 1]     # grad w = (y, x, 0)
+    got = u @ oracle.spmv(ia, ja, K, w)
+    exact = 0.5               # int_[0,1]^3 (2x)(y) = 2 * 1/2 * 1/2
+    assert abs(got - exact) < 1e-9
+
+
+def test_elasticity_rigid_modes(oracle):
+    xyz, tets = mesh(2, perturb=0.2)
+    N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, 2, ncomp=3, kind=1, lam=1.0, mu=0.5)
+    P = oracle.nodes(2)
+    nn = N // 3
+    X = np.zeros((nn, 3))
+    for e in range(len(tets)):
+        v = xyz[tets[e]]
+        lam = np.stack([-(1 + P[:, 0] + P[:, 1] + P[:, 2]) / 2, (1 + P[:, 0]) / 2, (1 + P[:, 1]) / 2, (1 + P[:, 2]) / 2], 1)
+        X[l2g[e][:10] // 3] = lam @ v
+    scale = np.abs(K).max()
+    for mode in range(6):
+        u = np.zeros((nn, 3))
+        if mode < 3:
+            u[:, mode] = 1.0
+        else:
+            a, b = [(0, 1), (1, 2), (0, 2)][mode - 3]
+            u[:, a] = -X[:, b]
+            u[:, b] = X[:, a]
+        r = oracle.spmv(ia, ja, K, u.reshape(-1))
+        assert np.abs(r).max() < 1e-12 * scale
+
+
+def test_rhs_integrates_source(oracle):
+    xyz, tets = mesh(4, perturb=0.1)
+    N, l2g = oracle.dof_table(tets, 2)
+    F = oracle.rhs(2, xyz, tets, l2g, N, fkind=0, qdeg=6)
+    # sum_i F_i = int f = 3 pi^2 * (2/pi)^3 ; mesh is a perturbed cube: volume stays 1 but f is not
+    # integrated exactly -> loose check
+    assert abs(F.sum() - 3 * math.pi ** 2 * (2 / math.pi) ** 3) < 5e-2
+
+
+def test_oracle_pcg_solves(oracle):
+    xyz, tets = mesh(4, perturb=0.2)
+    N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, 1, mass=0.0)
+    b = oracle.rhs(1, xyz, tets, l2g, N, fkind=0)
+    mask = oracle.boundary_mask(1, xyz, tets, l2g, N)
+    oracle.dirichlet(ia, ja, K, b, mask, mode=1)
+    x, it, res = oracle.pcg(ia, ja, K, b, rtol=1e-10)
+    assert it > 0 and res <= 1e-10
+    r = b - oracle.spmv(ia, ja, K, x)
+    assert np.linalg.norm(r) <= 1.1e-10 * np.linalg.norm(b)
+
+
+def test_manufactured_convergence_rates(oracle):
+    # quickstart laplacian checker: L2 error O(h^{p+1}), H1 O(h^p)
+    errs = []
+    for n in (4, 8):
+        xyz, tets = mesh(n, perturb=0.0)
+        N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, 1, mass=0.0)
+        b = oracle.rhs(1, xyz, tets, l2g, N, fkind=0, qdeg=4)
+        mask = oracle.boundary_mask(1, xyz, tets, l2g, N)
+        oracle.dirichlet(ia, ja, K, b, mask, mode=1)
+        x, it, res = oracle.pcg(ia, ja, K, b, rtol=1e-12)
+        errs.append(oracle.errors(1, xyz, tets, l2g, x, 6))
+    rl2 = math.log2(errs[0][0] / errs[1][0])
+    rh1 = math.log2(errs[0][1] / errs[1][1])
+    assert rl2 > 1.7 and rh1 > 0.85
