@@ -195,7 +195,10 @@ def run_gb300(args, rank, world, local):
     from feelpp_gb300 import _ffi
 
     torch.cuda.set_device(local)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the library launches on it and the CUDA
+    # events below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     env = fpp.Environment(device=local, stream=C.c_void_p(stream.cuda_stream), profile=True)
     fpp_, xyz, tets, kappa, M, V = build_workload(args.n, args.order, env)
     u, v = V.element(), V.element()
