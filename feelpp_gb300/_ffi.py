@@ -93,6 +93,7 @@ SIGNATURES = {
     "fgpu_host_dof_table": (i32, [i64, i64, P, i32, i32, P, I64P]),
     "fgpu_host_pattern": (i32, [i64, i64, P, i32, i32, P, P, I64P]),
     "fgpu_host_ref_tables": (i32, [i32, i32, P, P, P, P, P, IP]),
+    "fgpu_assemble_vector_noalloc": (i32, [P, C.POINTER(RhsDesc), P, i32, P]),
     "fgpu_prof_reset": (i32, [P]),
     "fgpu_prof_get": (i32, [P, C.c_char_p, I64P, DP]),
 }

@@ -523,6 +523,27 @@ int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fki
     return FGPU_OK;
 }
 
+// Same two load-vector kernels launched on an explicit stream with caller-given
+// tables and work buffer (used by the allocation-free entry point).
+int launch_rhs_raw(cudaStream_t stream, const fgpu_space* V, int Q, const double* qx, const double* qw,
+                   const double* phi, int fkind, const double* fc, double* d_out, int accumulate, double* d_work) {
+    const fgpu_mesh* M = V->mesh;
+    int threads = 128;
+    int64_t blocks = std::min<int64_t>((M->nt + threads - 1) / threads, 152 * 32);
+    if (blocks < 1) blocks = 1;
+    switch (V->n) {
+        case 4: rhs_element_kernel<4><<<(int)blocks, threads, 0, stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, Q, qx, qw, phi, fkind, fc[0], fc[1], fc[2], d_work); break;
+        case 10: rhs_element_kernel<10><<<(int)blocks, threads, 0, stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, Q, qx, qw, phi, fkind, fc[0], fc[1], fc[2], d_work); break;
+        case 20: rhs_element_kernel<20><<<(int)blocks, threads, 0, stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, Q, qx, qw, phi, fkind, fc[0], fc[1], fc[2], d_work); break;
+        default: return FGPU_ERR_INVALID;
+    }
+    int64_t nn = V->topo.nnodes;
+    int64_t gb = std::min<int64_t>((nn + 255) / 256, 152 * 16);
+    if (gb < 1) gb = 1;
+    rhs_gather_kernel<<<(int)gb, 256, 0, stream>>>(nn, V->n, V->ncomp, V->d_inc_ptr, V->d_inc, d_work, d_out, accumulate);
+    return cudaGetLastError() == cudaSuccess ? FGPU_OK : FGPU_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------------------
 // Strong Dirichlet (MatrixPetsc::zeroRows, matrixpetsc.cpp:1762-1860), one
 // thread per row; the pattern is kept (MAT_KEEP_NONZERO_PATTERN).

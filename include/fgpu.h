@@ -209,6 +209,21 @@ int fgpu_host_pattern(int64_t nv, int64_t nt, const int32_t* tets, int order, in
 int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double* dphi, double* S, double* M,
                          int* npts);
 
+/* ---- load vector without device allocation (no counterpart in the reference).
+ *      For callers that cannot call cudaMalloc when they assemble: the device memory
+ *      belongs to the host application's pool allocator, or allocation is forbidden
+ *      after set-up (fixed-latency stepping, code later captured into graphs).
+ *      Same result as fgpu_assemble_vector; the per-element scratch lives in a
+ *      static device array of FGPU_NOALLOC_MAX_ELEMENT_VALUES doubles (16 MiB, held
+ *      by every GPU that loads the library until exit), so T*nloc*ncomp must not
+ *      exceed it (else FGPU_ERR_INVALID). The first call on a device sets it up
+ *      (symbol lookup + table copy) and must come before any stream capture. All
+ *      calls share the scratch: calls that overlap on the GPU race. d_out is a
+ *      device array of ndof doubles; stream is a cudaStream_t (NULL = default). ---- */
+#define FGPU_NOALLOC_MAX_ELEMENT_VALUES (1 << 21)
+int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate,
+                                 void* stream);
+
 /* ---- per-kernel device timings (CUDA events), enabled by fgpu_config.profile ---- */
 int fgpu_prof_reset(fgpu_ctx* ctx);
 /* total device time and launch count of the kernels tagged `name` */
