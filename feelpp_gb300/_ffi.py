@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libfgpu.so")
 FGPU_OK = 0
 F64, F32 = 0, 1
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
-ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR = 0, 1, 2
+ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64 = 0, 1, 2, 3
 RHS_SINE, RHS_CONST_VEC, RHS_CONST = 0, 1, 2
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
 PC_NONE, PC_JACOBI = 0, 1
@@ -94,6 +94,7 @@ SIGNATURES = {
     "fgpu_host_pattern": (i32, [i64, i64, P, i32, i32, P, P, I64P]),
     "fgpu_host_ref_tables": (i32, [i32, i32, P, P, P, P, P, IP]),
     "fgpu_assemble_vector_noalloc": (i32, [P, C.POINTER(RhsDesc), P, i32, P]),
+    "fgpu_host_df64_ops": (i32, [i32, i64, P, P, P]),
     "fgpu_prof_reset": (i32, [P]),
     "fgpu_prof_get": (i32, [P, C.c_char_p, I64P, DP]),
 }

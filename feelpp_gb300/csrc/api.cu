@@ -7,6 +7,7 @@
 #include <thread>
 #include <vector>
 
+#include "df64.h"
 #include "fgpu_core.h"
 
 namespace fgpu {
@@ -408,7 +409,16 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
         if (rc) return rc;
         A->coef_cap = nt * rec;
     }
-    int rc = launch_geometry(ctx, V->mesh, f->kind, d_kappa, f->kappa, f->mass, f->lambda, f->mu, A->d_coef);
+    int rc = FGPU_OK;
+    if (f->kind == FGPU_FORM_LAPLACE_MASS && !(f->algo == FGPU_ALGO_GATHER_NATIVE_F64 && A->precision == FGPU_F64)) {
+        // FP64 matrices: df64 arithmetic on the FP32 pipes; FP32 matrices: binary32
+        rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef));
+        if (rc) return rc;
+        rc = launch_assemble_gather_df(ctx, A, tab, reinterpret_cast<const float4*>(A->d_coef), accumulate);
+        if (rc) return rc;
+        return finish(ctx);
+    }
+    rc = launch_geometry(ctx, V->mesh, f->kind, d_kappa, f->kappa, f->mass, f->lambda, f->mu, A->d_coef);
     if (rc) return rc;
     if (f->kind == FGPU_FORM_LAPLACE_MASS) {
         rc = launch_assemble_gather(ctx, A, tab, f->kind, A->d_coef, accumulate);
@@ -606,6 +616,25 @@ int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double
     if (dphi) std::memcpy(dphi, R.dphi.data(), R.dphi.size() * sizeof(double));
     if (S) std::memcpy(S, R.S.data(), R.S.size() * sizeof(double));
     if (M) std::memcpy(M, R.M.data(), R.M.size() * sizeof(double));
+    return FGPU_OK;
+}
+
+int fgpu_host_df64_ops(int op, int64_t n, const double* a, const double* b, double* out) {
+    if (!a || !out || n < 0) return FGPU_ERR_INVALID;
+    for (int64_t i = 0; i < n; ++i) {
+        df x = d2df(a[i]);
+        df y = b ? d2df(b[i]) : df{0.0f, 0.0f};
+        df r;
+        switch (op) {
+            case 0: r = x; break;
+            case 1: r = df_add(x, y); break;
+            case 2: r = df_mul(x, y); break;
+            case 3: r = df_recip(x); break;
+            case 4: r = df_sub(x, y); break;
+            default: return FGPU_ERR_INVALID;
+        }
+        out[i] = df2d(r);
+    }
     return FGPU_OK;
 }
 

@@ -23,6 +23,7 @@
 #include <mutex>
 #include <string>
 
+#include "df64.h"
 #include "fgpu_core.h"
 
 namespace fgpu {
@@ -52,7 +53,14 @@ DevTables* get_dev_tables(int order, int qdeg, std::string& err) {
     DevTables* D = new DevTables();
     D->order = order; D->n = R.n; D->Q = R.Q; D->qdeg = qdeg;
     std::vector<float> T7f(R.T7.begin(), R.T7.end()), Sf(R.S.begin(), R.S.end());
+    std::vector<float> T7h(R.T7.size()), T7l(R.T7.size());
+    for (size_t k = 0; k < R.T7.size(); ++k) {
+        T7h[k] = (float)R.T7[k];
+        T7l[k] = (float)(R.T7[k] - (double)T7h[k]);
+    }
     cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(T7h, &D->d_T7h);
+    if (e == cudaSuccess) e = upload(T7l, &D->d_T7l);
     if (e == cudaSuccess) e = upload(R.T7, &D->d_T7);
     if (e == cudaSuccess) e = upload(R.S, &D->d_S);
     if (e == cudaSuccess) e = upload(T7f, &D->d_T7f);
@@ -649,6 +657,249 @@ int launch_convert_values(fgpu_ctx* ctx, const fgpu_matrix* src, fgpu_matrix* ds
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
+}
+
+}  // namespace fgpu
+
+// ===========================================================================
+// FP64-accurate assembly on the FP32 pipes (df64) and the pure FP32 path.
+// ===========================================================================
+namespace fgpu {
+
+// Element coefficient record, 16 floats (64 B):
+//   [c0 c1 c2 c3 | c4 c5 c6 J]  high parts,  [c0 c1 c2 c3 | c4 c5 c6 J]  low parts
+// with c_0..5 = kappa * (C^T C)_{00,11,22,01,02,12} / |det K| (= kappa J B^T B, C the
+// cofactor matrix of K, B = C / det K), c_6 = mass * |det K|, J = |det K|.
+// K's entries are formed in FP64 (9 subtractions of vertex coordinates), the rest
+// in df64 (geomap.hpp:1971-1991, 2310-2350).
+__global__ void geometry_df_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                   const double* __restrict__ kappa, double kappa_c, double mass,
+                                   float4* __restrict__ rec, int* __restrict__ status) {
+    const df kc = d2df(kappa_c), mc = d2df(mass);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
+        const double* X0 = xyz + 3 * (int64_t)t.x;
+        const double* Xv[3] = {xyz + 3 * (int64_t)t.y, xyz + 3 * (int64_t)t.z, xyz + 3 * (int64_t)t.w};
+        df K[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) K[r * 3 + c] = df_scale(d2df(Xv[c][r] - X0[r]), 0.5f);
+        df C[9];
+        C[0] = df_sub(df_mul(K[4], K[8]), df_mul(K[5], K[7]));
+        C[1] = df_sub(df_mul(K[5], K[6]), df_mul(K[3], K[8]));
+        C[2] = df_sub(df_mul(K[3], K[7]), df_mul(K[4], K[6]));
+        C[3] = df_sub(df_mul(K[2], K[7]), df_mul(K[1], K[8]));
+        C[4] = df_sub(df_mul(K[0], K[8]), df_mul(K[2], K[6]));
+        C[5] = df_sub(df_mul(K[1], K[6]), df_mul(K[0], K[7]));
+        C[6] = df_sub(df_mul(K[1], K[5]), df_mul(K[2], K[4]));
+        C[7] = df_sub(df_mul(K[2], K[3]), df_mul(K[0], K[5]));
+        C[8] = df_sub(df_mul(K[0], K[4]), df_mul(K[1], K[3]));
+        df det = df_add(df_add(df_mul(K[0], C[0]), df_mul(K[1], C[1])), df_mul(K[2], C[2]));
+        df J = det.hi < 0.0f ? df_neg(det) : det;
+        if (!(J.hi > 0.0f) || !isfinite(J.hi)) atomicOr(status, kStatusBadElement);
+        df inv = df_recip(J);
+        df s = df_mul(kappa ? d2df(kappa[e]) : kc, inv);
+        const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+        df c[8];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            df g = df_add(df_add(df_mul(C[pa[k]], C[pb[k]]), df_mul(C[3 + pa[k]], C[3 + pb[k]])), df_mul(C[6 + pa[k]], C[6 + pb[k]]));
+            c[k] = df_mul(s, g);
+        }
+        c[6] = df_mul(mc, J);
+        c[7] = J;
+        float4* o = rec + 4 * e;
+        o[0] = make_float4(c[0].hi, c[1].hi, c[2].hi, c[3].hi);
+        o[1] = make_float4(c[4].hi, c[5].hi, c[6].hi, c[7].hi);
+        o[2] = make_float4(c[0].lo, c[1].lo, c[2].lo, c[3].lo);
+        o[3] = make_float4(c[4].lo, c[5].lo, c[6].lo, c[7].lo);
+    }
+}
+
+int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
+                       float4* d_rec) {
+    int threads = 256;
+    int64_t blocks = std::min<int64_t>((mesh->nt + threads - 1) / threads, 152 * 16);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "geometry", ev);
+    geometry_df_kernel<<<(int)blocks, threads, 0, ctx->stream>>>(mesh->nt, mesh->d_xyz, mesh->d_tets, d_kappa, kappa, mass,
+                                                               d_rec, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+enum GatherMode { kModeF32 = 0, kModeDF64 = 1 };
+
+// Warp-per-row gather. A warp owns one CSR row (dof node) at a time; each pass
+// evaluates the rows of EPB incident elements at once (lane = slot * N + column),
+// then adds them into the shared-memory row in increasing element order.
+//   DF64: value = sum_k c_k T_k[li][j] as a compensated dot product (TwoProduct +
+//         TwoSum on binary32), accumulation in df64, output converted to binary64
+//         with integer operations.
+//   F32 : binary32 coefficients, tables and accumulation.
+template <int MODE, int N, int EPB>
+__global__ void __launch_bounds__(256) gather_row_kernel(
+    int64_t nrows, const int64_t* __restrict__ sia, const int32_t* __restrict__ sja,
+    const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const int32_t* __restrict__ l2n,
+    const float4* __restrict__ rec, const float* __restrict__ Thg, const float* __restrict__ Tlg, int maxrow,
+    void* __restrict__ valv, int accumulate, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int NT = 7 * N * N;
+    float* Th = reinterpret_cast<float*>(smem);
+    float* Tl = Th + NT;
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) {
+        Th[k] = Thg[k];
+        if (MODE == kModeDF64) Tl[k] = Tlg[k];
+    }
+    const int tbytes = ((MODE == kModeDF64 ? 2 : 1) * NT * 4 + 15) & ~15;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;   // floats per accumulator entry
+    float* acc = reinterpret_cast<float*>(smem + tbytes) + (size_t)warp * maxrow * ACCW;
+    int32_t* cols = reinterpret_cast<int32_t*>(smem + tbytes + (size_t)wpb * maxrow * ACCW * 4) + (size_t)warp * maxrow;
+    __syncthreads();
+    const int slot = lane / N, j = lane - slot * N;
+    const bool lane_used = lane < EPB * N;
+    for (int64_t r = (int64_t)blockIdx.x * wpb + warp; r < nrows; r += (int64_t)gridDim.x * wpb) {
+        const int64_t start = sia[r];
+        const int len = (int)(sia[r + 1] - start);
+        if (len > maxrow) {
+            if (lane == 0) atomicOr(status, kStatusRowOverflow);
+            continue;
+        }
+        for (int k = lane; k < len; k += 32) {
+            cols[k] = sja[start + k];
+            if (MODE == kModeDF64) {
+                df a = accumulate ? d2df(reinterpret_cast<const double*>(valv)[start + k]) : df{0.0f, 0.0f};
+                acc[2 * k] = a.hi;
+                acc[2 * k + 1] = a.lo;
+            } else {
+                acc[k] = accumulate ? reinterpret_cast<const float*>(valv)[start + k] : 0.0f;
+            }
+        }
+        __syncwarp();
+        const int64_t tb = inc_ptr[r], te = inc_ptr[r + 1];
+        for (int64_t c0 = tb; c0 < te; c0 += 32) {
+            const int nin = (int)min((int64_t)32, te - c0);
+            const int32_t mycode = lane < nin ? inc[c0 + lane] : 0;
+            for (int b = 0; b < nin; b += EPB) {
+                const int idx = b + slot;
+                const int32_t code = __shfl_sync(0xffffffffu, mycode, idx < 32 ? idx : 31);
+                const bool active = lane_used && idx < nin;
+                float vh = 0.0f, vl = 0.0f;
+                int pos = 0;
+                if (active) {
+                    const int64_t e = code >> 5;
+                    const int li = code & 31;
+                    const float4* rp = rec + 4 * e;
+                    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1);
+                    const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+                    const int tix = li * N + j;
+                    if (MODE == kModeDF64) {
+                        const float4 l0 = __ldg(rp + 2), l1 = __ldg(rp + 3);
+                        const float cl[7] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z};
+                        float s = 0.0f, err = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) {
+                            const float th = Th[k * N * N + tix], tl = Tl[k * N * N + tix];
+                            const float p = f_mul(ch[k], th);
+                            const float pe = f_fma(ch[k], th, -p);
+                            err = f_fma(ch[k], tl, err);
+                            err = f_fma(cl[k], th, err);
+                            err = f_add(err, pe);
+                            if (k == 0) {
+                                s = p;
+                            } else {
+                                df t = two_sum(s, p);
+                                s = t.hi;
+                                err = f_add(err, t.lo);
+                            }
+                        }
+                        df v = quick_two_sum(s, err);
+                        vh = v.hi;
+                        vl = v.lo;
+                    } else {
+                        float v = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) v = fmaf(ch[k], Th[k * N * N + tix], v);
+                        vh = v;
+                    }
+                    const int32_t col = l2n[e * N + j];
+                    pos = lower_bound_s(cols, len, col);
+                    if (!(pos < len && cols[pos] == col)) {
+                        atomicOr(status, kStatusMissingEntry);
+                        pos = -1;
+                    }
+                }
+                // add in increasing element order (slot order == incidence order)
+#pragma unroll
+                for (int ss = 0; ss < EPB; ++ss) {
+                    if (active && slot == ss && pos >= 0) {
+                        if (MODE == kModeDF64) {
+                            df a = df_add(df{acc[2 * pos], acc[2 * pos + 1]}, df{vh, vl});
+                            acc[2 * pos] = a.hi;
+                            acc[2 * pos + 1] = a.lo;
+                        } else {
+                            acc[pos] = f_add(acc[pos], vh);
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        for (int k = lane; k < len; k += 32) {
+            if (MODE == kModeDF64)
+                reinterpret_cast<double*>(valv)[start + k] = df2d(df{acc[2 * k], acc[2 * k + 1]});
+            else
+                reinterpret_cast<float*>(valv)[start + k] = acc[k];
+        }
+        __syncwarp();
+    }
+}
+
+template <int MODE, int N, int EPB>
+static int run_gather_row(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+    const DevPattern& P = *A->pattern;
+    const fgpu_space* V = A->space;
+    const int threads = 256, wpb = threads / 32;
+    const int NT = 7 * N * N;
+    size_t tbytes = ((MODE == kModeDF64 ? 2 : 1) * NT * 4 + 15) & ~15;
+    size_t smem = tbytes + (size_t)wpb * P.max_row * ((MODE == kModeDF64 ? 8 : 4) + 4);
+    auto kern = gather_row_kernel<MODE, N, EPB>;
+    if (smem > 227 * 1024) { ctx->err = "pattern rows too long for the gather kernel"; return FGPU_ERR_INVALID; }
+    if (smem > 48 * 1024) FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    int64_t need = (P.nrows + wpb - 1) / wpb;
+    int64_t blocks = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * sms);
+    if (blocks < 1) blocks = 1;
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather", ev);
+    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, P.d_ja, V->d_inc_ptr, V->d_inc, V->d_l2n, rec,
+                                                      MODE == kModeDF64 ? tab->d_T7h : tab->d_T7f, tab->d_T7l, P.max_row,
+                                                      A->d_val, accumulate, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+    const int order = A->space->order;
+    const bool f32 = A->precision == FGPU_F32;
+    if (A->ncomp != 1) { ctx->err = "Laplace/mass form needs a scalar space"; return FGPU_ERR_INVALID; }
+    if (order == 1) return f32 ? run_gather_row<kModeF32, 4, 8>(ctx, A, tab, rec, accumulate)
+                               : run_gather_row<kModeDF64, 4, 8>(ctx, A, tab, rec, accumulate);
+    if (order == 2) return f32 ? run_gather_row<kModeF32, 10, 3>(ctx, A, tab, rec, accumulate)
+                               : run_gather_row<kModeDF64, 10, 3>(ctx, A, tab, rec, accumulate);
+    if (order == 3) return f32 ? run_gather_row<kModeF32, 20, 1>(ctx, A, tab, rec, accumulate)
+                               : run_gather_row<kModeDF64, 20, 1>(ctx, A, tab, rec, accumulate);
+    ctx->err = "unsupported order";
+    return FGPU_ERR_INVALID;
 }
 
 }  // namespace fgpu

@@ -169,6 +169,8 @@ struct DevTables {                     // device copies of the reference tables
     double* d_S = nullptr;             // 9 n n
     float* d_T7f = nullptr;
     float* d_Sf = nullptr;
+    float* d_T7h = nullptr;            // df64 split of T7: hi = fl32(T), lo = fl32(T - hi)
+    float* d_T7l = nullptr;
     double* d_phi = nullptr;           // Q n
     double* d_dphi = nullptr;          // Q n 3
     double* d_qx = nullptr;            // Q 3
@@ -185,6 +187,9 @@ int launch_assemble_gather(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, 
                            int accumulate);
 int launch_assemble_colour(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, int kind, const double* d_coef,
                            int accumulate);
+int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
+                       float4* d_rec);
+int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fkind, const double* fc,
                double* d_out, int accumulate, double* d_work);
 int launch_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, double* d_rhs, const uint8_t* d_mask, const double* d_g,

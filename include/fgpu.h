@@ -44,9 +44,11 @@ extern "C" {
 #define FGPU_FORM_LAPLACE_MASS 0  /* kappa*inner(gradt(u),grad(v)) + mass*idt(u)*id(v)          */
 #define FGPU_FORM_ELASTICITY 1    /* inner(lambda tr(eps(u)) I + 2 mu eps(u), grad(v)), Pchv    */
 
-#define FGPU_ALGO_AUTO 0          /* autotuned choice between the two below */
-#define FGPU_ALGO_GATHER 1        /* row-owner gather: each CSR row summed by one thread group */
+#define FGPU_ALGO_AUTO 0          /* best available algorithm for the form */
+#define FGPU_ALGO_GATHER 1        /* row-owner gather: each CSR row summed by one warp, element order */
 #define FGPU_ALGO_COLOUR 2        /* element-coloured scatter-add, colours in fixed order */
+#define FGPU_ALGO_GATHER_NATIVE_F64 3 /* row-owner gather in native FP64 arithmetic (FP64 matrices; the
+                                     default FP64 path computes in double-float on the FP32 pipes) */
 
 #define FGPU_RHS_SINE 0           /* f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */
 #define FGPU_RHS_CONST_VEC 1      /* f = (c0, c1, c2) (Pchv) */
@@ -223,6 +225,10 @@ int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double
 #define FGPU_NOALLOC_MAX_ELEMENT_VALUES (1 << 21)
 int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate,
                                  void* stream);
+
+/* df64 (double-float) arithmetic self-check on the host: op 0 round trip double->df64->double,
+ * 1 a+b, 2 a*b, 3 1/a, 4 a-b, all through df64; writes n results */
+int fgpu_host_df64_ops(int op, int64_t n, const double* a, const double* b, double* out);
 
 /* ---- per-kernel device timings (CUDA events), enabled by fgpu_config.profile ---- */
 int fgpu_prof_reset(fgpu_ctx* ctx);
