@@ -87,6 +87,12 @@ int ensure_pattern(fgpu_space* V) {
     V->pattern = P;
     // the device copy is authoritative; drop the host ja
     std::vector<int32_t>().swap(V->h_pattern.ja);
+    if (P->max_row <= 256) {
+        rc = launch_build_positions(ctx, V);
+        if (rc) return rc;
+        rc = finish(ctx);
+        if (rc) return rc;
+    }
     return FGPU_OK;
 }
 
@@ -259,6 +265,7 @@ int fgpu_space_destroy(fgpu_space* V) {
     cudaFree(V->d_l2n);
     cudaFree(V->d_inc_ptr);
     cudaFree(V->d_inc);
+    cudaFree(V->d_pos);
     delete V;
     return FGPU_OK;
 }

@@ -733,19 +733,61 @@ int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kap
 
 enum GatherMode { kModeF32 = 0, kModeDF64 = 1 };
 
+// Position table: pos[(e n + i) n + j] = offset of node l2n[e][j] inside the
+// pattern row of node l2n[e][i] (rows are at most 255 long). Built once per pattern.
+__global__ void positions_kernel(int64_t nt, int n, const int32_t* __restrict__ l2n, const int64_t* __restrict__ ia,
+                                 const int32_t* __restrict__ ja, uint8_t* __restrict__ pos, int* __restrict__ status) {
+    const int64_t total = nt * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t / (n * n);
+        const int ij = (int)(t - e * n * n);
+        const int i = ij / n, j = ij - i * n;
+        const int32_t row = l2n[e * n + i], col = l2n[e * n + j];
+        const int64_t b = ia[row];
+        int lo = 0, hi = (int)(ia[row + 1] - b);
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (ja[b + mid] < col) lo = mid + 1; else hi = mid;
+        }
+        if (lo >= (int)(ia[row + 1] - b) || ja[b + lo] != col || lo > 255) {
+            atomicOr(status, kStatusMissingEntry);
+            lo = 0;
+        }
+        pos[t] = (uint8_t)lo;
+    }
+}
+
+int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V) {
+    if (V->d_pos) return FGPU_OK;
+    const int64_t total = V->mesh->nt * (int64_t)V->n * V->n;
+    cudaError_t e = cudaMalloc(&V->d_pos, total);
+    if (e != cudaSuccess) { ctx->err = "position table allocation failed"; V->d_pos = nullptr; return FGPU_ERR_ALLOC; }
+    int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 64);
+    PendingEvent ev;
+    prof_begin(ctx, "positions", ev);
+    positions_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(V->mesh->nt, V->n, V->d_l2n, V->pattern->d_ia,
+                                                                              V->pattern->d_ja, V->d_pos, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
 // Warp-per-row gather. A warp owns one CSR row (dof node) at a time; each pass
-// evaluates the rows of EPB incident elements at once (lane = slot * N + column),
-// then adds them into the shared-memory row in increasing element order.
+// evaluates the rows of EPB incident elements at once (lane = slot * N + column).
+// Each slot adds into its own shared-memory copy of the row (no two lanes of a
+// slot share a column), and the EPB copies are summed in slot order when the row
+// is written: the summation order is fixed, hence reproducible, without float
+// atomics.
 //   DF64: value = sum_k c_k T_k[li][j] as a compensated dot product (TwoProduct +
 //         TwoSum on binary32), accumulation in df64, output converted to binary64
 //         with integer operations.
 //   F32 : binary32 coefficients, tables and accumulation.
 template <int MODE, int N, int EPB>
 __global__ void __launch_bounds__(256) gather_row_kernel(
-    int64_t nrows, const int64_t* __restrict__ sia, const int32_t* __restrict__ sja,
-    const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const int32_t* __restrict__ l2n,
-    const float4* __restrict__ rec, const float* __restrict__ Thg, const float* __restrict__ Tlg, int maxrow,
-    void* __restrict__ valv, int accumulate, int* __restrict__ status) {
+    int64_t nrows, const int64_t* __restrict__ sia, const int64_t* __restrict__ inc_ptr,
+    const int32_t* __restrict__ inc, const uint8_t* __restrict__ posg, const float4* __restrict__ rec,
+    const float* __restrict__ Thg, const float* __restrict__ Tlg, int maxrow, void* __restrict__ valv,
+    int accumulate, int* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int NT = 7 * N * N;
     float* Th = reinterpret_cast<float*>(smem);
@@ -758,46 +800,36 @@ __global__ void __launch_bounds__(256) gather_row_kernel(
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
     constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;   // floats per accumulator entry
-    float* acc = reinterpret_cast<float*>(smem + tbytes) + (size_t)warp * maxrow * ACCW;
-    int32_t* cols = reinterpret_cast<int32_t*>(smem + tbytes + (size_t)wpb * maxrow * ACCW * 4) + (size_t)warp * maxrow;
+    float* acc = reinterpret_cast<float*>(smem + tbytes) + (size_t)warp * EPB * maxrow * ACCW;
     __syncthreads();
     const int slot = lane / N, j = lane - slot * N;
     const bool lane_used = lane < EPB * N;
+    float* myacc = acc + (size_t)(slot < EPB ? slot : 0) * maxrow * ACCW;
+    // accumulators start at zero once; the write loop of each row resets what it read
+    for (int k = lane; k < EPB * maxrow * ACCW; k += 32) acc[k] = 0.0f;
+    __syncwarp();
     for (int64_t r = (int64_t)blockIdx.x * wpb + warp; r < nrows; r += (int64_t)gridDim.x * wpb) {
         const int64_t start = sia[r];
         const int len = (int)(sia[r + 1] - start);
+        const int64_t tb = inc_ptr[r], te = inc_ptr[r + 1];
         if (len > maxrow) {
             if (lane == 0) atomicOr(status, kStatusRowOverflow);
             continue;
         }
-        for (int k = lane; k < len; k += 32) {
-            cols[k] = sja[start + k];
-            if (MODE == kModeDF64) {
-                df a = accumulate ? d2df(reinterpret_cast<const double*>(valv)[start + k]) : df{0.0f, 0.0f};
-                acc[2 * k] = a.hi;
-                acc[2 * k + 1] = a.lo;
-            } else {
-                acc[k] = accumulate ? reinterpret_cast<const float*>(valv)[start + k] : 0.0f;
-            }
-        }
-        __syncwarp();
-        const int64_t tb = inc_ptr[r], te = inc_ptr[r + 1];
         for (int64_t c0 = tb; c0 < te; c0 += 32) {
             const int nin = (int)min((int64_t)32, te - c0);
             const int32_t mycode = lane < nin ? inc[c0 + lane] : 0;
             for (int b = 0; b < nin; b += EPB) {
                 const int idx = b + slot;
                 const int32_t code = __shfl_sync(0xffffffffu, mycode, idx < 32 ? idx : 31);
-                const bool active = lane_used && idx < nin;
-                float vh = 0.0f, vl = 0.0f;
-                int pos = 0;
-                if (active) {
+                if (lane_used && idx < nin) {
                     const int64_t e = code >> 5;
                     const int li = code & 31;
                     const float4* rp = rec + 4 * e;
                     const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1);
                     const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
                     const int tix = li * N + j;
+                    const int pos = posg[e * (N * N) + tix];
                     if (MODE == kModeDF64) {
                         const float4 l0 = __ldg(rp + 2), l1 = __ldg(rp + 3);
                         const float cl[7] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z};
@@ -818,43 +850,46 @@ __global__ void __launch_bounds__(256) gather_row_kernel(
                                 err = f_add(err, t.lo);
                             }
                         }
-                        df v = quick_two_sum(s, err);
-                        vh = v.hi;
-                        vl = v.lo;
+                        df a = df_add(df{myacc[2 * pos], myacc[2 * pos + 1]}, quick_two_sum(s, err));
+                        myacc[2 * pos] = a.hi;
+                        myacc[2 * pos + 1] = a.lo;
                     } else {
                         float v = 0.0f;
 #pragma unroll
                         for (int k = 0; k < 7; ++k) v = fmaf(ch[k], Th[k * N * N + tix], v);
-                        vh = v;
-                    }
-                    const int32_t col = l2n[e * N + j];
-                    pos = lower_bound_s(cols, len, col);
-                    if (!(pos < len && cols[pos] == col)) {
-                        atomicOr(status, kStatusMissingEntry);
-                        pos = -1;
+                        myacc[pos] = f_add(myacc[pos], v);
                     }
                 }
-                // add in increasing element order (slot order == incidence order)
-#pragma unroll
-                for (int ss = 0; ss < EPB; ++ss) {
-                    if (active && slot == ss && pos >= 0) {
-                        if (MODE == kModeDF64) {
-                            df a = df_add(df{acc[2 * pos], acc[2 * pos + 1]}, df{vh, vl});
-                            acc[2 * pos] = a.hi;
-                            acc[2 * pos + 1] = a.lo;
-                        } else {
-                            acc[pos] = f_add(acc[pos], vh);
-                        }
-                    }
-                    __syncwarp();
-                }
+                __syncwarp();
             }
         }
+        // write the row: sum the slot copies in slot order (+ the old value for '+='), reset them
         for (int k = lane; k < len; k += 32) {
-            if (MODE == kModeDF64)
-                reinterpret_cast<double*>(valv)[start + k] = df2d(df{acc[2 * k], acc[2 * k + 1]});
-            else
-                reinterpret_cast<float*>(valv)[start + k] = acc[k];
+            if (MODE == kModeDF64) {
+                df a{acc[2 * k], acc[2 * k + 1]};
+                acc[2 * k] = 0.0f;
+                acc[2 * k + 1] = 0.0f;
+#pragma unroll
+                for (int s = 1; s < EPB; ++s) {
+                    float* q = acc + (size_t)s * maxrow * 2 + 2 * k;
+                    a = df_add(a, df{q[0], q[1]});
+                    q[0] = 0.0f;
+                    q[1] = 0.0f;
+                }
+                double* out = reinterpret_cast<double*>(valv) + start + k;
+                if (accumulate) a = df_add(d2df(*out), a);
+                *out = df2d(a);
+            } else {
+                float a = acc[k];
+                acc[k] = 0.0f;
+#pragma unroll
+                for (int s = 1; s < EPB; ++s) {
+                    a = f_add(a, acc[(size_t)s * maxrow + k]);
+                    acc[(size_t)s * maxrow + k] = 0.0f;
+                }
+                float* out = reinterpret_cast<float*>(valv) + start + k;
+                *out = accumulate ? f_add(*out, a) : a;
+            }
         }
         __syncwarp();
     }
@@ -867,8 +902,9 @@ static int run_gather_row(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, c
     const int threads = 256, wpb = threads / 32;
     const int NT = 7 * N * N;
     size_t tbytes = ((MODE == kModeDF64 ? 2 : 1) * NT * 4 + 15) & ~15;
-    size_t smem = tbytes + (size_t)wpb * P.max_row * ((MODE == kModeDF64 ? 8 : 4) + 4);
+    size_t smem = tbytes + (size_t)wpb * EPB * P.max_row * (MODE == kModeDF64 ? 8 : 4);
     auto kern = gather_row_kernel<MODE, N, EPB>;
+    if (P.max_row > 256) { ctx->err = "pattern rows longer than 256 entries"; return FGPU_ERR_INVALID; }
     if (smem > 227 * 1024) { ctx->err = "pattern rows too long for the gather kernel"; return FGPU_ERR_INVALID; }
     if (smem > 48 * 1024) FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -880,7 +916,7 @@ static int run_gather_row(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, c
     if (blocks < 1) blocks = 1;
     PendingEvent ev;
     prof_begin(ctx, "assemble_gather", ev);
-    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, P.d_ja, V->d_inc_ptr, V->d_inc, V->d_l2n, rec,
+    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, V->d_inc_ptr, V->d_inc, V->d_pos, rec,
                                                       MODE == kModeDF64 ? tab->d_T7h : tab->d_T7f, tab->d_T7l, P.max_row,
                                                       A->d_val, accumulate, ctx->d_status);
     prof_end(ctx, ev);

@@ -128,6 +128,7 @@ struct fgpu_space {
     int32_t* d_inc = nullptr;
     std::shared_ptr<DevPattern> pattern;   // scalar node pattern, built on demand
     fgpu::NodePattern h_pattern;
+    uint8_t* d_pos = nullptr;        // T x n x n: position of node l2n[e][j] in row l2n[e][i] (rows <= 255)
 };
 
 struct fgpu_matrix {
@@ -190,6 +191,7 @@ int launch_assemble_colour(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, 
 int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
                        float4* d_rec);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V);
 int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fkind, const double* fc,
                double* d_out, int accumulate, double* d_work);
 int launch_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, double* d_rhs, const uint8_t* d_mask, const double* d_g,
