@@ -16,6 +16,7 @@ ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64 = 0, 1, 2, 3
 RHS_SINE, RHS_CONST_VEC, RHS_CONST = 0, 1, 2
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
 PC_NONE, PC_JACOBI = 0, 1
+ARITH_F64, ARITH_DF64 = 0, 1
 
 ERROR_NAMES = {1: "FGPU_ERR_INVALID", 2: "FGPU_ERR_CUDA", 3: "FGPU_ERR_BAD_ELEMENT", 4: "FGPU_ERR_OUT_OF_RANGE",
                5: "FGPU_ERR_NOT_CONVERGED", 6: "FGPU_ERR_BREAKDOWN", 7: "FGPU_ERR_PATTERN", 8: "FGPU_ERR_ALLOC"}
@@ -42,7 +43,7 @@ class RhsDesc(C.Structure):
 
 class SolverCfg(C.Structure):
     _fields_ = [("rtol", C.c_double), ("maxit", C.c_int), ("pc", C.c_int), ("mixed", C.c_int),
-                ("inner_rtol", C.c_double), ("check_every", C.c_int)]
+                ("inner_rtol", C.c_double), ("check_every", C.c_int), ("arith", C.c_int)]
 
 
 class SolveStats(C.Structure):

@@ -131,6 +131,16 @@ struct fgpu_space {
     uint8_t* d_pos = nullptr;        // T x n x n: position of node l2n[e][j] in row l2n[e][i] (rows <= 255)
 };
 
+struct SellLayout {                  // SELL-C-sigma (C = 32, sigma = 256) copy of a CSR pattern
+    int64_t nrows = 0, nslices = 0, nstored = 0;
+    int32_t* d_perm = nullptr;       // sorted position -> row
+    int64_t* d_slice_ptr = nullptr;  // nslices + 1, start of each slice (in entries)
+    int32_t* d_slice_len = nullptr;  // max row length in the slice
+    int32_t* d_col = nullptr;        // nstored column ids (padding: the row itself)
+    int32_t* d_src = nullptr;        // nstored CSR positions of the entries (-1: padding)
+    ~SellLayout();
+};
+
 struct fgpu_matrix {
     fgpu_ctx* ctx = nullptr;
     fgpu_space* space = nullptr;     // test == trial space
@@ -144,6 +154,7 @@ struct fgpu_matrix {
     void* d_val = nullptr;           // nnz values (double or float)
     double* d_coef = nullptr;        // per-element coefficient records of the last assembly
     int64_t coef_cap = 0;
+    mutable std::shared_ptr<SellLayout> sell; // solver layout, built on first solve
 };
 
 struct fgpu_vector {

@@ -486,9 +486,11 @@ class Form2:
         self.env.check(self.env.lib.fgpu_matrix_mult(self.env.h, self.h, x.h, y.h))
 
     def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False, inner_rtol=1e-4,
-              check_every=16):
+              check_every=16, arith="f64"):
+        """CG + Jacobi (ksp-type=cg, pc-type=jacobi). mixed=True: binary32 inner CG refined with
+        the binary64 residual; arith="df64": double-float arithmetic for the plain solve."""
         cfg = _ffi.SolverCfg(rtol, maxit, _ffi.PC_JACOBI if pc == "jacobi" else _ffi.PC_NONE, 1 if mixed else 0,
-                             inner_rtol, check_every)
+                             inner_rtol, check_every, _ffi.ARITH_DF64 if arith == "df64" else _ffi.ARITH_F64)
         st = _ffi.SolveStats()
         self.env.check(self.env.lib.fgpu_solve_cg(self.env.h, self.h, None, rhs.vec.h, solution.h, C.byref(cfg),
                                                   C.byref(st)))

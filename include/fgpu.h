@@ -61,6 +61,9 @@ extern "C" {
 #define FGPU_PC_NONE 0
 #define FGPU_PC_JACOBI 1
 
+#define FGPU_ARITH_F64 0          /* solver arithmetic: native FP64 (default) */
+#define FGPU_ARITH_DF64 1         /* double-float on the FP32 pipes (~48 bits; moderately conditioned systems) */
+
 typedef struct fgpu_ctx fgpu_ctx;
 typedef struct fgpu_mesh fgpu_mesh;
 typedef struct fgpu_space fgpu_space;
@@ -97,6 +100,7 @@ typedef struct {
     int mixed;                /* 1: FP32 inner CG + FP64 residual refinement */
     double inner_rtol;        /* inner relative tolerance of the mixed solver (0 = 1e-4) */
     int check_every;          /* iterations per convergence poll (0 = 16) */
+    int arith;                /* FGPU_ARITH_* of the non-mixed solve */
 } fgpu_solver_cfg;
 
 typedef struct {

@@ -53,6 +53,17 @@ def test_mixed_precision_refinement_reaches_1e10(env, oracle, order, n):
     assert abs(e32[0] - e64[0]) <= 0.01 * e64[0]
 
 
+@pytest.mark.parametrize("order,n", [(1, 16), (2, 8)])
+def test_df64_solve_matches_f64(env, oracle, order, n):
+    xyz, tets, M, V, u, a, l = poisson(env, n, order)
+    st = a.solve(rhs=l, solution=u, rtol=1e-10, arith="df64")
+    assert st["rel_residual"] <= 1e-9
+    u64 = V.element()
+    a.solve(rhs=l, solution=u64, rtol=1e-10)
+    x, x64 = u.to_numpy(), u64.to_numpy()
+    assert np.linalg.norm(x - x64) <= 1e-8 * np.linalg.norm(x64)
+
+
 def test_manufactured_solution_rates(env, oracle):
     errs = []
     for n in (8, 16):
