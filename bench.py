@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-n", type=int, default=24)
+    p.add_argument("--probe", default=None, choices=[None, "cg"],
+                   help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed)")
     return p.parse_args()
 
 
@@ -371,8 +373,30 @@ def reduce_max(x, world):
     return float(t.item())
 
 
+def run_probe_cg(args):
+    """Short FP64 and mixed CG runs (maxit 48) on the bench system, for kernel profiling."""
+    import feelpp_gb300 as fpp
+    env = fpp.Environment()
+    _, xyz, tets, kappa, M, V = build_workload(args.n, args.order, env)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v)))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    for mixed in (False, True):
+        w = V.element()
+        try:
+            a.solve(rhs=l, solution=w, rtol=1e-10, maxit=48, mixed=mixed)
+        except fpp.FgpuError as e:
+            print("stopped:", e)
+
+
 def main():
     args = parse()
+    if args.probe == "cg":
+        run_probe_cg(args)
+        return
     rank, world, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
