@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libfgpu.so")
 
 FGPU_OK = 0
-F64, F32 = 0, 1
+F64, F32, DF64 = 0, 1, 2
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64 = 0, 1, 2, 3
 RHS_SINE, RHS_CONST_VEC, RHS_CONST = 0, 1, 2
@@ -91,6 +91,11 @@ SIGNATURES = {
     "fgpu_dirichlet": (i32, [P, P, P, i64, P, P, i32, f64]),
     "fgpu_matrix_mult": (i32, [P, P, P, P]),
     "fgpu_solve_cg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
+    "fgpu_operator_create": (i32, [P, P, C.POINTER(FormDesc), i32, PP]),
+    "fgpu_operator_set_dirichlet": (i32, [P, i64, P]),
+    "fgpu_operator_apply": (i32, [P, P, P, P]),
+    "fgpu_operator_destroy": (i32, [P]),
+    "fgpu_solve_cg_operator": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
     "fgpu_host_dof_table": (i32, [i64, i64, P, i32, i32, P, I64P]),
     "fgpu_host_pattern": (i32, [i64, i64, P, i32, i32, P, P, I64P]),
     "fgpu_host_ref_tables": (i32, [i32, i32, P, P, P, P, P, IP]),

@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
-SOURCES = ["basis.cpp", "topology.cpp", "assemble.cu", "solve.cu", "api.cu", "noalloc.cu"]
+SOURCES = ["basis.cpp", "topology.cpp", "assemble.cu", "solve.cu", "matfree.cu", "api.cu", "noalloc.cu"]
 
 
 def _digest(paths):
@@ -33,7 +33,7 @@ def _digest(paths):
 
 
 def _headers():
-    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     hs.append(os.path.join(INCLUDE, "fgpu.h"))
     return sorted(hs)
 

@@ -1,0 +1,733 @@
+// Matrix-free operator y = A x for the affine Laplace/mass form, and the CG
+// that uses it.
+//
+// Feel++ has no element-level matrix-free kernel: its "matrix-free" notion
+// applies form-level operators (MatrixShell::multVector, feelpp/feel/feelalg/
+// matrixshell.hpp:49,120; OperatorLinearFree::apply, feelpp/feel/feeldiscr/
+// operatorlinearfree.hpp:116-170). This operator is validated against the
+// assembled CSR product of the same form (after on() with symmetric
+// elimination, which is what its Dirichlet handling reproduces).
+//
+// Two phases per apply, deterministic and without float atomics:
+//  1. element phase: y_e = K_e x_e with K_e = sum_k c_k T_k (the 7 reference
+//     tensors of the assembly kernels), x_e gathered through the dof table with
+//     Dirichlet dofs masked to zero, written to an element buffer (T x n);
+//  2. node phase: y[m] = sum of the element buffer over the elements containing
+//     dof m, in increasing element order (the node -> element incidence); a
+//     Dirichlet row returns y[m] = x[m].
+// Number formats: binary32 (tables and coefficients in binary32, fused
+// multiply-adds on the FP32 pipes), df64 (double-float, ~48 bits) and native
+// binary64 (FP64 pipe; the reference arithmetic).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "df64.h"
+#include "fgpu_core.h"
+
+namespace fgpu {
+
+// ---------------------------------------------------------------------------
+// element phase
+// ---------------------------------------------------------------------------
+// binary32: one thread per element; T (7 n n floats) in shared memory.
+template <int N>
+__global__ void __launch_bounds__(128) mf_element_f32_kernel(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
+                                                            const float* __restrict__ Tg, const float* __restrict__ x,
+                                                            const uint8_t* __restrict__ mask, float* __restrict__ ye) {
+    constexpr int NT = 7 * N * N;
+    __shared__ float T[NT];
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
+    __syncthreads();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        float xe[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const int32_t d = l2n[e * N + j];
+            xe[j] = (mask && mask[d]) ? 0.0f : x[d];
+        }
+        const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
+        const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+#pragma unroll 1
+        for (int i = 0; i < N; ++i) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                const float* Tk = T + (k * N + i) * N;
+                float s = 0.0f;
+#pragma unroll
+                for (int j = 0; j < N; ++j) s = fmaf(Tk[j], xe[j], s);
+                acc = fmaf(c[k], s, acc);
+            }
+            ye[e * N + i] = acc;
+        }
+    }
+}
+
+// native binary64: one thread per element (FP64 pipe), coefficients from the
+// binary64 geometry records (8 doubles).
+template <int N>
+__global__ void __launch_bounds__(128) mf_element_f64_kernel(int64_t nt, const int32_t* __restrict__ l2n, const double* __restrict__ coef,
+                                                            const double* __restrict__ Tg, const double* __restrict__ x,
+                                                            const uint8_t* __restrict__ mask, double* __restrict__ ye) {
+    constexpr int NT = 7 * N * N;
+    extern __shared__ double Td[];
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) Td[k] = Tg[k];
+    __syncthreads();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        double xe[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const int32_t d = l2n[e * N + j];
+            xe[j] = (mask && mask[d]) ? 0.0 : x[d];
+        }
+        const double* c = coef + 8 * e;
+#pragma unroll 1
+        for (int i = 0; i < N; ++i) {
+            double acc = 0.0;
+#pragma unroll 1
+            for (int k = 0; k < 7; ++k) {
+                const double* Tk = Td + (k * N + i) * N;
+                double s = 0.0;
+#pragma unroll
+                for (int j = 0; j < N; ++j) s = fma(Tk[j], xe[j], s);
+                acc = fma(c[k], s, acc);
+            }
+            ye[e * N + i] = acc;
+        }
+    }
+}
+
+// df64: one thread per element; x and y in binary64 memory, converted with integer
+// operations; products and sums as double-float.
+template <int N>
+__global__ void __launch_bounds__(128) mf_element_df_kernel(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
+                                                           const float* __restrict__ Thg, const float* __restrict__ Tlg,
+                                                           const double* __restrict__ x, const uint8_t* __restrict__ mask,
+                                                           double* __restrict__ ye) {
+    constexpr int NT = 7 * N * N;
+    extern __shared__ float Tsh[];
+    float* Th = Tsh;
+    float* Tl = Tsh + NT;
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) {
+        Th[k] = Thg[k];
+        Tl[k] = Tlg[k];
+    }
+    __syncthreads();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        df xe[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const int32_t d = l2n[e * N + j];
+            xe[j] = (mask && mask[d]) ? df{0.0f, 0.0f} : d2df(x[d]);
+        }
+        const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1), l0 = __ldg(rec + 4 * e + 2), l1 = __ldg(rec + 4 * e + 3);
+        const df c[7] = {{h0.x, l0.x}, {h0.y, l0.y}, {h0.z, l0.z}, {h0.w, l0.w}, {h1.x, l1.x}, {h1.y, l1.y}, {h1.z, l1.z}};
+#pragma unroll 1
+        for (int i = 0; i < N; ++i) {
+            df acc{0.0f, 0.0f};
+#pragma unroll 1
+            for (int k = 0; k < 7; ++k) {
+                const int o = (k * N + i) * N;
+                df s{0.0f, 0.0f};
+#pragma unroll
+                for (int j = 0; j < N; ++j) s = df_add(s, df_mul(df{Th[o + j], Tl[o + j]}, xe[j]));
+                acc = df_add(acc, df_mul(c[k], s));
+            }
+            ye[e * N + i] = df2d(acc);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// node phase: y[m] = sum_{(e,li) in inc(m)} ye[e][li] (element order); Dirichlet rows y = x
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void mf_gather_kernel(int64_t nnodes, int N, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                 const T* __restrict__ ye, const T* __restrict__ x, const uint8_t* __restrict__ mask,
+                                 T* __restrict__ y) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        if (mask && mask[m]) {
+            y[m] = x[m];
+            continue;
+        }
+        T s = 0;
+        for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
+            const int32_t code = inc[t];
+            s += ye[(int64_t)(code >> 5) * N + (code & 31)];
+        }
+        y[m] = s;
+    }
+}
+
+// df64 summation of binary64 element values (keeps ~48 bits in the node sum)
+__global__ void mf_gather_df_kernel(int64_t nnodes, int N, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                    const double* __restrict__ ye, const double* __restrict__ x, const uint8_t* __restrict__ mask,
+                                    double* __restrict__ y) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        if (mask && mask[m]) {
+            y[m] = x[m];
+            continue;
+        }
+        df s{0.0f, 0.0f};
+        for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
+            const int32_t code = inc[t];
+            s = df_add(s, d2df(ye[(int64_t)(code >> 5) * N + (code & 31)]));
+        }
+        y[m] = df2d(s);
+    }
+}
+
+// diagonal of the operator (Jacobi): element diagonals then the node gather
+template <typename T>
+__global__ void mf_diag_element_kernel(int64_t nt, int N, const float4* __restrict__ rec, const double* __restrict__ T7,
+                                       T* __restrict__ ye) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        const float4 h0 = rec[4 * e], h1 = rec[4 * e + 1], l0 = rec[4 * e + 2], l1 = rec[4 * e + 3];
+        const double c[7] = {(double)h0.x + l0.x, (double)h0.y + l0.y, (double)h0.z + l0.z, (double)h0.w + l0.w,
+                             (double)h1.x + l1.x, (double)h1.y + l1.y, (double)h1.z + l1.z};
+        for (int i = 0; i < N; ++i) {
+            double s = 0;
+            for (int k = 0; k < 7; ++k) s += c[k] * T7[(k * N + i) * N + i];
+            ye[e * N + i] = (T)s;
+        }
+    }
+}
+
+}  // namespace fgpu
+
+// ---------------------------------------------------------------------------
+// operator object
+// ---------------------------------------------------------------------------
+struct fgpu_operator {
+    fgpu_ctx* ctx = nullptr;
+    fgpu_space* space = nullptr;
+    int precision = FGPU_F32;        // FGPU_F32, FGPU_F64 (native) or FGPU_DF64 (double-float)
+    int qdeg = 0;
+    fgpu::DevTables* tab = nullptr;
+    float4* d_rec = nullptr;         // df64 coefficient records (T x 4 float4)
+    double* d_coef = nullptr;        // binary64 coefficient records (native FP64 path)
+    void* d_ye = nullptr;            // element buffer T x n (float or double)
+    uint8_t* d_mask = nullptr;       // Dirichlet mask (nnodes) or null
+    void* d_diag = nullptr;          // operator diagonal (float or double)
+    float* d_xf = nullptr;           // binary32 work vectors for the F32 solve
+    int64_t nt = 0, nnodes = 0;
+};
+
+namespace fgpu {
+int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass, float4* d_rec);
+int launch_geometry(fgpu_ctx* ctx, const fgpu_mesh* mesh, int kind, const double* d_kappa, double kappa, double mass,
+                    double lam, double mu, double* d_coef);
+
+static int blocks_for(int64_t n, int threads, int cap) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, cap));
+}
+
+// y = A x; x, y device arrays of nnodes entries in the operator's storage type
+// (float for F32, double for F64 / DF64)
+int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y) {
+    const fgpu_space* V = op->space;
+    const int n = V->n;
+    const int64_t nt = op->nt;
+    PendingEvent ev;
+    prof_begin(ctx, "matfree_element", ev);
+    const int eb = blocks_for(nt, 128, 152 * 16);
+    if (op->precision == FGPU_F32) {
+        switch (n) {
+            case 4: mf_element_f32_kernel<4><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
+            case 10: mf_element_f32_kernel<10><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
+            case 20: mf_element_f32_kernel<20><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
+            default: return FGPU_ERR_INVALID;
+        }
+    } else if (op->precision == FGPU_F64) {
+        const size_t sm = 7 * n * n * sizeof(double);
+        switch (n) {
+            case 4: mf_element_f64_kernel<4><<<eb, 128, sm, ctx->stream>>>(nt, V->d_l2n, op->d_coef, op->tab->d_T7, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            case 10: mf_element_f64_kernel<10><<<eb, 128, sm, ctx->stream>>>(nt, V->d_l2n, op->d_coef, op->tab->d_T7, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            case 20: mf_element_f64_kernel<20><<<eb, 128, sm, ctx->stream>>>(nt, V->d_l2n, op->d_coef, op->tab->d_T7, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            default: return FGPU_ERR_INVALID;
+        }
+    } else {
+        const size_t sm = 2 * 7 * n * n * sizeof(float);
+        switch (n) {
+            case 4: mf_element_df_kernel<4><<<eb, 128, sm, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7h, op->tab->d_T7l, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            case 10: mf_element_df_kernel<10><<<eb, 128, sm, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7h, op->tab->d_T7l, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            case 20: mf_element_df_kernel<20><<<eb, 128, sm, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7h, op->tab->d_T7l, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            default: return FGPU_ERR_INVALID;
+        }
+    }
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    PendingEvent ev2;
+    prof_begin(ctx, "matfree_gather", ev2);
+    const int gb = blocks_for(op->nnodes, 256, 152 * 16);
+    if (op->precision == FGPU_F32)
+        mf_gather_kernel<float><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, (const float*)x, op->d_mask, (float*)y);
+    else if (op->precision == FGPU_F64)
+        mf_gather_kernel<double><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)x, op->d_mask, (double*)y);
+    else
+        mf_gather_df_kernel<<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)x, op->d_mask, (double*)y);
+    prof_end(ctx, ev2);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+int operator_diagonal(fgpu_ctx* ctx, fgpu_operator* op) {
+    const fgpu_space* V = op->space;
+    const int n = V->n;
+    const bool f32 = op->precision == FGPU_F32;
+    const size_t es = f32 ? sizeof(float) : sizeof(double);
+    if (!op->d_diag) FGPU_CUDA_CHECK(ctx, cudaMalloc(&op->d_diag, op->nnodes * es));
+    void* ones = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&ones, op->nnodes * es));
+    // Dirichlet rows: diag 1 (x = 1 passes through the mask branch)
+    std::vector<char> h(op->nnodes * es);
+    if (f32) { float* p = (float*)h.data(); for (int64_t i = 0; i < op->nnodes; ++i) p[i] = 1.0f; }
+    else { double* p = (double*)h.data(); for (int64_t i = 0; i < op->nnodes; ++i) p[i] = 1.0; }
+    cudaMemcpyAsync(ones, h.data(), h.size(), cudaMemcpyHostToDevice, ctx->stream);
+    const int eb = blocks_for(op->nt, 256, 152 * 16);
+    if (f32) mf_diag_element_kernel<float><<<eb, 256, 0, ctx->stream>>>(op->nt, n, op->d_rec, op->tab->d_T7, (float*)op->d_ye);
+    else mf_diag_element_kernel<double><<<eb, 256, 0, ctx->stream>>>(op->nt, n, op->d_rec, op->tab->d_T7, (double*)op->d_ye);
+    const int gb = blocks_for(op->nnodes, 256, 152 * 16);
+    if (f32) mf_gather_kernel<float><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, (const float*)ones, op->d_mask, (float*)op->d_diag);
+    else mf_gather_kernel<double><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)ones, op->d_mask, (double*)op->d_diag);
+    ctx->launches += 2;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(ones);
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return FGPU_ERR_CUDA; }
+    return FGPU_OK;
+}
+
+}  // namespace fgpu
+
+// ===========================================================================
+// matrix-free CG
+// ===========================================================================
+#include "cg_kernels.cuh"
+
+namespace fgpu {
+
+// q = A p fused with the p.q partial sums (node phase of the apply)
+template <class PL>
+__global__ void mf_gather_dot_kernel(int64_t nnodes, int N, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                     const typename PL::S* __restrict__ ye, const typename PL::S* __restrict__ x,
+                                     const uint8_t* __restrict__ mask, typename PL::S* __restrict__ y,
+                                     typename PL::D* __restrict__ partial, const CGScalars<PL>* __restrict__ sc) {
+    if (sc && sc->done) return;
+    __shared__ typename PL::D sh[32];
+    typename PL::D dsum = PL::dzero();
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        typename PL::S v;
+        if (mask && mask[m]) {
+            v = x[m];
+        } else {
+            typename PL::A s = PL::zero();
+            for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
+                const int32_t code = inc[t];
+                s = PL::add(s, PL::ld(ye[(int64_t)(code >> 5) * N + (code & 31)]));
+            }
+            v = PL::st(s);
+        }
+        y[m] = v;
+        if (partial) dsum = PL::dmadd(dsum, PL::ld(x[m]), PL::ld(v));
+    }
+    if (partial) {
+        const typename PL::D t = block_sum<PL>(dsum, sh);
+        if (threadIdx.x == 0) partial[blockIdx.x] = t;
+    }
+}
+
+// element phase gated by the CG stop flag (runs inside the captured graph)
+template <int N>
+__global__ void __launch_bounds__(128) mf_element_f32_gated(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
+                                                           const float* __restrict__ Tg, const float* __restrict__ x,
+                                                           const uint8_t* __restrict__ mask, float* __restrict__ ye,
+                                                           const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    constexpr int NT = 7 * N * N;
+    __shared__ float T[NT];
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
+    __syncthreads();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        float xe[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const int32_t d = l2n[e * N + j];
+            xe[j] = (mask && mask[d]) ? 0.0f : x[d];
+        }
+        const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
+        const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+#pragma unroll 1
+        for (int i = 0; i < N; ++i) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                const float* Tk = T + (k * N + i) * N;
+                float s = 0.0f;
+#pragma unroll
+                for (int j = 0; j < N; ++j) s = fmaf(Tk[j], xe[j], s);
+                acc = fmaf(c[k], s, acc);
+            }
+            ye[e * N + i] = acc;
+        }
+    }
+}
+
+template <typename T>
+__global__ void copy_cast_kernel(int64_t n, const double* __restrict__ a, T* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) b[i] = (T)a[i];
+}
+template <typename T>
+__global__ void cast_back_kernel(int64_t n, const T* __restrict__ a, double* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) b[i] = (double)a[i];
+}
+template <class PL>
+__global__ void residual_from_q_kernel(int64_t n, const typename PL::S* __restrict__ b, const typename PL::S* __restrict__ q,
+                                       typename PL::S* __restrict__ r) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = PL::st(PL::sub(PL::ld(b[i]), PL::ld(q[i])));
+}
+template <class PL>
+__global__ void dinv_from_diag_kernel(int64_t n, const typename PL::S* __restrict__ d, typename PL::S* __restrict__ dinv, int use_pc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const typename PL::A v = PL::ld(d[i]);
+        dinv[i] = PL::st((use_pc && PL::nonzero(v)) ? PL::recip(v) : PL::one());
+    }
+}
+
+int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y);
+
+// element phase + fused node phase; F32 uses the gated kernel (graph-safe)
+template <class PL>
+static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* x, typename PL::S* y, typename PL::D* partial,
+                        const CGScalars<PL>* sc, int gblocks) {
+    const fgpu_space* V = op->space;
+    const int n = V->n;
+    const int eb = blocks_for(op->nt, 128, 152 * 16);
+    const int* stop = sc ? &sc->done : nullptr;
+    if (op->precision == FGPU_F32) {
+        switch (n) {
+            case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
+            case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
+            default: mf_element_f32_gated<20><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
+        }
+    } else {
+        // binary64 element phases (native or df64); not gated: the FP64 matrix-free solve polls every iteration
+        const int save = ctx->profile;
+        ctx->profile = 0;
+        const size_t sm64 = 7 * n * n * sizeof(double), smdf = 2 * 7 * n * n * sizeof(float);
+        if (op->precision == FGPU_F64) {
+            switch (n) {
+                case 4: mf_element_f64_kernel<4><<<eb, 128, sm64, ctx->stream>>>(op->nt, V->d_l2n, op->d_coef, op->tab->d_T7, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+                case 10: mf_element_f64_kernel<10><<<eb, 128, sm64, ctx->stream>>>(op->nt, V->d_l2n, op->d_coef, op->tab->d_T7, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+                default: mf_element_f64_kernel<20><<<eb, 128, sm64, ctx->stream>>>(op->nt, V->d_l2n, op->d_coef, op->tab->d_T7, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            }
+        } else {
+            switch (n) {
+                case 4: mf_element_df_kernel<4><<<eb, 128, smdf, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7h, op->tab->d_T7l, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+                case 10: mf_element_df_kernel<10><<<eb, 128, smdf, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7h, op->tab->d_T7l, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+                default: mf_element_df_kernel<20><<<eb, 128, smdf, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7h, op->tab->d_T7l, (const double*)x, op->d_mask, (double*)op->d_ye); break;
+            }
+        }
+        ctx->profile = save;
+    }
+    mf_gather_dot_kernel<PL><<<gblocks, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc,
+                                                              (const typename PL::S*)op->d_ye, x, op->d_mask, y, partial, sc);
+    ctx->launches += 2;
+}
+
+// Matrix-free PCG with Jacobi (operator diagonal). For the binary32 operator the
+// iterations run from a captured graph like the CSR solver; the binary64 ones
+// launch per iteration (their element phase is long, launch overhead is noise).
+template <class PL>
+static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b, typename PL::S* x, double rtol, int maxit, int pc,
+                       int check_every, int* iters, int* fail, double* rr_out, double* bb_out) {
+    typedef typename PL::S S;
+    typedef typename PL::D D;
+    const int64_t n = op->nnodes;
+    cudaStream_t s = ctx->stream;
+    S *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+    D *partial = nullptr, *pq_partial = nullptr;
+    CGScalars<PL>* sc = nullptr;
+    CGScalars<PL>* hsc = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int vb = vec_blocks(n);
+    const int gb = vb;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dinv); cudaFree(partial); cudaFree(pq_partial); cudaFree(sc);
+        if (hsc) cudaFreeHost(hsc);
+    };
+#define CK(call)                                                             \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) {                                             \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);   \
+            cleanup();                                                       \
+            return FGPU_ERR_CUDA;                                            \
+        }                                                                    \
+    } while (0)
+    if (check_every & 1) ++check_every;
+    CK(cudaMalloc(&r, n * sizeof(S)));
+    CK(cudaMalloc(&z, n * sizeof(S)));
+    CK(cudaMalloc(&p, n * sizeof(S)));
+    CK(cudaMalloc(&q, n * sizeof(S)));
+    CK(cudaMalloc(&dinv, n * sizeof(S)));
+    CK(cudaMalloc(&partial, 3 * vb * sizeof(D)));
+    CK(cudaMalloc(&pq_partial, vb * sizeof(D)));
+    CK(cudaMalloc(&sc, sizeof(CGScalars<PL>)));
+    CK(cudaMallocHost(&hsc, sizeof(CGScalars<PL>)));
+    dinv_from_diag_kernel<PL><<<vb, 256, 0, s>>>(n, (const S*)op->d_diag, dinv, pc == FGPU_PC_JACOBI);
+    mf_apply_cg<PL>(ctx, op, x, q, nullptr, nullptr, gb);
+    residual_from_q_kernel<PL><<<vb, 256, 0, s>>>(n, b, q, r);
+    cg_init_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, b, r, dinv, z, p, partial);
+    cg_init_scalars<PL><<<1, 256, 0, s>>>(partial, vb, PL::host_from_double(rtol * rtol), sc);
+    ctx->launches += 4;
+    CK(cudaGetLastError());
+    const bool use_graph = op->precision == FGPU_F32;
+    if (use_graph) {
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < check_every; ++k) {
+            const int parity = k & 1;
+            mf_apply_cg<PL>(ctx, op, p, q, pq_partial, sc, gb);
+            cg_update_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, x, r, z, p, q, dinv, pq_partial, gb, partial, sc, parity);
+            cg_p_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, p, z, partial, vb, maxit, sc, parity);
+        }
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); cleanup(); return FGPU_ERR_CUDA; }
+        CK(cudaGraphInstantiate(&exec, graph, 0));
+    }
+    CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int guard = 0, parity = 0;
+    while (!hsc->done) {
+        if (use_graph) {
+            CK(cudaGraphLaunch(exec, s));
+            ctx->launches += 4 * check_every;
+        } else {
+            mf_apply_cg<PL>(ctx, op, p, q, pq_partial, sc, gb);
+            cg_update_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, x, r, z, p, q, dinv, pq_partial, gb, partial, sc, parity);
+            cg_p_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, p, z, partial, vb, maxit, sc, parity);
+            parity ^= 1;
+            ctx->launches += 2;
+        }
+        CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (++guard > maxit + 2) break;
+    }
+    *iters = hsc->it;
+    *fail = hsc->fail;
+    *rr_out = PL::host_to_double(hsc->rr);
+    *bb_out = PL::host_to_double(hsc->bb);
+    cleanup();
+#undef CK
+    return FGPU_OK;
+}
+
+static double host_norm(fgpu_ctx* ctx, int64_t n, const double* d) {
+    std::vector<double> h(n);
+    cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    double s = 0;
+    for (double v : h) s += v * v;
+    return std::sqrt(s);
+}
+
+// ||b - A x|| with the binary64 (native or df64) operator
+static int mf_residual64(fgpu_ctx* ctx, fgpu_operator* op, const double* b, const double* x, double* r, double* q, double* out) {
+    mf_apply_cg<PolF64>(ctx, op, x, q, nullptr, nullptr, vec_blocks(op->nnodes));
+    residual_from_q_kernel<PolF64><<<vec_blocks(op->nnodes), 256, 0, ctx->stream>>>(op->nnodes, b, q, r);
+    ctx->launches++;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    *out = host_norm(ctx, op->nnodes, r);
+    return FGPU_OK;
+}
+
+int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const double* d_b, double* d_x,
+                      const fgpu_solver_cfg* cfg, fgpu_solve_stats* st) {
+    const int64_t n = op->nnodes;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    const int ce = cfg->check_every > 0 ? cfg->check_every : 16;
+    int rc = FGPU_OK, iters = 0, fail = 0, outer = 0;
+    double rn = 0, bn = host_norm(ctx, n, d_b);
+    double *r = nullptr, *q = nullptr;
+    if (cudaMalloc(&r, n * sizeof(double)) != cudaSuccess || cudaMalloc(&q, n * sizeof(double)) != cudaSuccess) {
+        cudaFree(r);
+        ctx->err = "matrix-free solve: allocation failed";
+        return FGPU_ERR_ALLOC;
+    }
+    if (!cfg->mixed) {
+        if (op->precision == FGPU_F32) { ctx->err = "the plain matrix-free solve needs a binary64 operator"; rc = FGPU_ERR_INVALID; }
+        else {
+            double rr = 0, bb = 0;
+            rc = mf_pcg_core<PolF64>(ctx, op, d_b, d_x, cfg->rtol, cfg->maxit, cfg->pc, ce, &iters, &fail, &rr, &bb);
+            outer = 1;
+        }
+    } else {
+        if (!op32 || op32->precision != FGPU_F32 || op32->space != op->space) { ctx->err = "mixed matrix-free solve needs a binary32 inner operator on the same space"; rc = FGPU_ERR_INVALID; }
+        float *r32 = nullptr, *d32 = nullptr;
+        if (rc == FGPU_OK && (cudaMalloc(&r32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&d32, n * sizeof(float)) != cudaSuccess)) {
+            ctx->err = "mixed matrix-free solve: allocation failed";
+            rc = FGPU_ERR_ALLOC;
+        }
+        const double inner = cfg->inner_rtol > 0 ? cfg->inner_rtol : 1e-4;
+        while (rc == FGPU_OK) {
+            rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+            if (rc) break;
+            if (bn == 0.0 || rn <= cfg->rtol * bn) break;
+            if (outer >= 50 || iters >= cfg->maxit) { fail = 2; break; }
+            d2f_scaled_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, r, r32, 1.0 / rn);
+            cudaMemsetAsync(d32, 0, n * sizeof(float), ctx->stream);
+            int it = 0, f = 0;
+            double rr = 0, bb = 0;
+            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, inner, cfg->maxit - iters, cfg->pc, ce, &it, &f, &rr, &bb);
+            if (rc) break;
+            iters += it;
+            ++outer;
+            axpy_f_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_x, d32, rn);
+            ctx->launches += 2;
+            if (f == 1) { fail = 1; break; }
+        }
+        cudaFree(r32);
+        cudaFree(d32);
+    }
+    if (rc == FGPU_OK && !cfg->mixed) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+    cudaFree(r);
+    cudaFree(q);
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != FGPU_OK) return rc;
+    if (st) {
+        st->iterations = iters;
+        st->outer = outer;
+        st->rel_residual = bn > 0 ? rn / bn : 0.0;
+        st->time_ms = ms;
+    }
+    if (fail == 1) { ctx->err = "CG breakdown"; return FGPU_ERR_BREAKDOWN; }
+    if (fail == 2) { ctx->err = "matrix-free CG did not reach rtol"; return FGPU_ERR_NOT_CONVERGED; }
+    return FGPU_OK;
+}
+
+}  // namespace fgpu
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+using namespace fgpu;
+
+extern "C" int fgpu_operator_create(fgpu_ctx* ctx, fgpu_space* V, const fgpu_form_desc* f, int precision, fgpu_operator** out) {
+    if (!ctx || !V || !f || !out) return FGPU_ERR_INVALID;
+    if (f->kind != FGPU_FORM_LAPLACE_MASS || V->ncomp != 1) { ctx->err = "matrix-free operators support the scalar Laplace/mass form"; return FGPU_ERR_INVALID; }
+    if (precision != FGPU_F32 && precision != FGPU_F64 && precision != FGPU_DF64) { ctx->err = "bad operator precision"; return FGPU_ERR_INVALID; }
+    *out = nullptr;
+    std::string err;
+    DevTables* tab = get_dev_tables(V->order, f->quad_degree > 0 ? f->quad_degree : 2 * V->order, err);
+    if (!tab) { ctx->err = err; return FGPU_ERR_INVALID; }
+    fgpu_operator* op = new fgpu_operator();
+    op->ctx = ctx;
+    op->space = V;
+    op->precision = precision;
+    op->tab = tab;
+    op->nt = V->mesh->nt;
+    op->nnodes = V->topo.nnodes;
+    double* dk = nullptr;
+    auto fail = [&](int code, const char* msg) {
+        ctx->err = msg;
+        cudaFree(dk);
+        fgpu_operator_destroy(op);
+        return code;
+    };
+    if (f->kappa_elem) {
+        if (cudaMalloc(&dk, op->nt * sizeof(double)) != cudaSuccess) return fail(FGPU_ERR_ALLOC, "operator: allocation failed");
+        cudaMemcpyAsync(dk, f->kappa_elem, op->nt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    }
+    const size_t es = precision == FGPU_F32 ? sizeof(float) : sizeof(double);
+    if (cudaMalloc(&op->d_rec, op->nt * 4 * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&op->d_ye, op->nt * V->n * es) != cudaSuccess)
+        return fail(FGPU_ERR_ALLOC, "operator: allocation failed");
+    int rc = launch_geometry_df(ctx, V->mesh, dk, f->kappa, f->mass, op->d_rec);
+    if (!rc && precision == FGPU_F64) {
+        if (cudaMalloc(&op->d_coef, op->nt * 8 * sizeof(double)) != cudaSuccess) return fail(FGPU_ERR_ALLOC, "operator: allocation failed");
+        rc = launch_geometry(ctx, V->mesh, FGPU_FORM_LAPLACE_MASS, dk, f->kappa, f->mass, 0, 0, op->d_coef);
+    }
+    if (!rc) rc = operator_diagonal(ctx, op);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(dk);
+    dk = nullptr;
+    if (rc) { fgpu_operator_destroy(op); return rc; }
+    *out = op;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_operator_set_dirichlet(fgpu_operator* op, int64_t ndofs, const int32_t* dofs) {
+    if (!op || (ndofs > 0 && !dofs)) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = op->ctx;
+    std::vector<uint8_t> m(op->nnodes, 0);
+    for (int64_t k = 0; k < ndofs; ++k) {
+        if (dofs[k] < 0 || dofs[k] >= op->nnodes) { ctx->err = "dirichlet dof out of range"; return FGPU_ERR_OUT_OF_RANGE; }
+        m[dofs[k]] = 1;
+    }
+    if (!op->d_mask) FGPU_CUDA_CHECK(ctx, cudaMalloc(&op->d_mask, op->nnodes));
+    FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(op->d_mask, m.data(), op->nnodes, cudaMemcpyHostToDevice, ctx->stream));
+    int rc = operator_diagonal(ctx, op);
+    if (rc) return rc;
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_vector* x, fgpu_vector* y) {
+    if (!ctx || !op || !x || !y || x->n != op->nnodes || y->n != op->nnodes) return FGPU_ERR_INVALID;
+    int rc;
+    if (op->precision == FGPU_F32) {
+        float *xf = nullptr, *yf = nullptr;
+        if (cudaMalloc(&xf, op->nnodes * 4) != cudaSuccess || cudaMalloc(&yf, op->nnodes * 4) != cudaSuccess) {
+            cudaFree(xf);
+            ctx->err = "apply: allocation failed";
+            return FGPU_ERR_ALLOC;
+        }
+        const int vb = vec_blocks(op->nnodes);
+        copy_cast_kernel<float><<<vb, 256, 0, ctx->stream>>>(op->nnodes, x->d, xf);
+        rc = operator_apply(ctx, op, xf, yf);
+        cast_back_kernel<float><<<vb, 256, 0, ctx->stream>>>(op->nnodes, yf, y->d);
+        ctx->launches += 2;
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(xf);
+        cudaFree(yf);
+        if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    } else {
+        rc = operator_apply(ctx, op, x->d, y->d);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    }
+    return rc;
+}
+
+extern "C" int fgpu_operator_destroy(fgpu_operator* op) {
+    if (!op) return FGPU_OK;
+    cudaFree(op->d_rec);
+    cudaFree(op->d_coef);
+    cudaFree(op->d_ye);
+    cudaFree(op->d_mask);
+    cudaFree(op->d_diag);
+    cudaFree(op->d_xf);
+    delete op;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const fgpu_vector* b, fgpu_vector* x,
+                                      const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
+    if (!ctx || !op || !b || !x || !cfg || b->n != op->nnodes || x->n != op->nnodes) return FGPU_ERR_INVALID;
+    int rc = solve_cg_operator(ctx, op, op32, b->d, x->d, cfg, stats);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    return rc;
+}

@@ -430,6 +430,10 @@ class Form2:
         self.env.check(self.env.lib.fgpu_matrix_zero(self.h))
 
     def _desc(self, integral):
+        return Form2._desc_of(integral, self.algo)
+
+    @staticmethod
+    def _desc_of(integral, algo):
         d = _ffi.FormDesc()
         d.kind = _ffi.FORM_LAPLACE_MASS
         d.kappa = 0.0
@@ -437,7 +441,7 @@ class Form2:
         d.mass = 0.0
         d.lam, d.mu = 0.0, 0.0
         d.quad_degree = integral.quad
-        d.algo = self.algo
+        d.algo = algo
         kappa_arr = None
         for kind, c in integral.expr.terms:
             if kind == "stiff":
@@ -503,6 +507,57 @@ class Form2:
                 self.env.lib.fgpu_matrix_destroy(self.h)
         except Exception:
             pass
+
+
+class Operator:
+    """Matrix-free operator of a Laplace/mass integral on a scalar space.
+
+    precision: "f32", "f64" (native FP64) or "df64" (double-float). Dirichlet dofs set
+    with set_dirichlet() are eliminated symmetrically, as on(..., type="elimination_symmetric")
+    does on the assembled matrix."""
+
+    PREC = {"f32": _ffi.F32, "f64": _ffi.F64, "df64": _ffi.DF64}
+
+    def __init__(self, space, integral, precision="f32"):
+        self.space = space
+        self.env = space.env
+        d, kappa_arr = Form2._desc_of(integral, _ffi.ALGO_AUTO)
+        self._kappa = kappa_arr
+        if kappa_arr is not None:
+            d.kappa_elem = kappa_arr.ctypes.data_as(C.c_void_p)
+        h = C.c_void_p()
+        self.env.check(self.env.lib.fgpu_operator_create(self.env.h, space.h, C.byref(d), self.PREC[precision], C.byref(h)))
+        self.h = h
+        self.precision = precision
+
+    def set_dirichlet(self, dofs):
+        dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+        self.env.check(self.env.lib.fgpu_operator_set_dirichlet(self.h, len(dofs), _ptr(dofs)))
+
+    def apply(self, x, y):
+        self.env.check(self.env.lib.fgpu_operator_apply(self.env.h, self.h, x.h, y.h))
+
+    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=1e-4, check_every=16):
+        """Matrix-free PCG; with `inner` (a binary32 Operator) the mixed method is used."""
+        cfg = _ffi.SolverCfg(rtol, maxit, _ffi.PC_JACOBI if pc == "jacobi" else _ffi.PC_NONE, 1 if inner else 0,
+                             inner_rtol, check_every, _ffi.ARITH_F64)
+        st = _ffi.SolveStats()
+        vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        self.env.check(self.env.lib.fgpu_solve_cg_operator(self.env.h, self.h, inner.h if inner else None, vec.h,
+                                                           solution.h, C.byref(cfg), C.byref(st)))
+        return {"iterations": st.iterations, "outer": st.outer, "rel_residual": st.rel_residual,
+                "time_ms": st.time_ms}
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.env.lib.fgpu_operator_destroy(self.h)
+        except Exception:
+            pass
+
+
+def operator(test, integral, precision="f32"):
+    return Operator(test, integral, precision)
 
 
 def form1(test):

@@ -40,6 +40,7 @@ extern "C" {
 /* ---- precision / form kinds / options ---- */
 #define FGPU_F64 0
 #define FGPU_F32 1
+#define FGPU_DF64 2               /* matrix-free operators: double-float arithmetic (~48 bits), binary64 interface */
 
 #define FGPU_FORM_LAPLACE_MASS 0  /* kappa*inner(gradt(u),grad(v)) + mass*idt(u)*id(v)          */
 #define FGPU_FORM_ELASTICITY 1    /* inner(lambda tr(eps(u)) I + 2 mu eps(u), grad(v)), Pchv    */
@@ -198,6 +199,22 @@ int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, 
  *      NULL: then it is made from A). x is the initial guess and the solution. ---- */
 int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+
+/* ---- matrix-free operator of a form (the reference applies form-level operators with
+ *      MatrixShell::multVector, feelpp/feel/feelalg/matrixshell.hpp:49,120 and
+ *      OperatorLinearFree::apply, feelpp/feel/feeldiscr/operatorlinearfree.hpp:116-170;
+ *      there is no element-level one). precision: FGPU_F32, FGPU_F64 (native) or FGPU_DF64.
+ *      Dirichlet dofs are eliminated symmetrically (the operator then equals the assembled
+ *      matrix after on(..., elimination_symmetric)). ---- */
+typedef struct fgpu_operator fgpu_operator;
+int fgpu_operator_create(fgpu_ctx* ctx, fgpu_space* V, const fgpu_form_desc* form, int precision, fgpu_operator** out);
+int fgpu_operator_set_dirichlet(fgpu_operator* op, int64_t ndofs, const int32_t* dofs);
+int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_vector* x, fgpu_vector* y);
+int fgpu_operator_destroy(fgpu_operator* op);
+/* matrix-free PCG (Jacobi from the operator diagonal): plain with a binary64 operator, or
+ * mixed (cfg->mixed) with a binary32 inner operator op32 refined by op's residual */
+int fgpu_solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const fgpu_vector* b, fgpu_vector* x,
+                           const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
 
 /* ---- host-only queries (no device needed): the dof numbering, the sparsity
  *      pattern and the reference tables the device kernels use ---- */
