@@ -212,9 +212,12 @@ struct fgpu_operator {
     void* d_diag = nullptr;          // operator diagonal (float or double)
     float* d_xf = nullptr;           // binary32 work vectors for the F32 solve
     int64_t nt = 0, nnodes = 0;
+    int use_tc = 0;                  // binary32 element phase on the tensor cores (tcgen05, P2/P3)
 };
 
 namespace fgpu {
+int launch_mf_element_tc(fgpu_ctx* ctx, int n, int64_t nt, const int32_t* l2n, const float4* rec, const float* T7f, const float* x,
+                         const uint8_t* mask, float* ye, const int* stop);
 int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass, float4* d_rec);
 int launch_geometry(fgpu_ctx* ctx, const fgpu_mesh* mesh, int kind, const double* d_kappa, double kappa, double mass,
                     double lam, double mu, double* d_coef);
@@ -232,7 +235,10 @@ int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y) {
     PendingEvent ev;
     prof_begin(ctx, "matfree_element", ev);
     const int eb = blocks_for(nt, 128, 152 * 16);
-    if (op->precision == FGPU_F32) {
+    if (op->precision == FGPU_F32 && op->use_tc && (n == 10 || n == 20)) {
+        int rc = launch_mf_element_tc(ctx, n, nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, nullptr);
+        if (rc) return rc;
+    } else if (op->precision == FGPU_F32) {
         switch (n) {
             case 4: mf_element_f32_kernel<4><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
             case 10: mf_element_f32_kernel<10><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
@@ -405,7 +411,9 @@ static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* 
     const int n = V->n;
     const int eb = blocks_for(op->nt, 128, 152 * 16);
     const int* stop = sc ? &sc->done : nullptr;
-    if (op->precision == FGPU_F32) {
+    if (op->precision == FGPU_F32 && op->use_tc && (n == 10 || n == 20)) {
+        launch_mf_element_tc(ctx, n, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop);
+    } else if (op->precision == FGPU_F32) {
         switch (n) {
             case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
             case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
@@ -709,6 +717,16 @@ extern "C" int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_
         if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
     }
     return rc;
+}
+
+extern "C" int fgpu_operator_set_tensor_cores(fgpu_operator* op, int on) {
+    if (!op) return FGPU_ERR_INVALID;
+    if (on && (op->precision != FGPU_F32 || (op->space->n != 10 && op->space->n != 20))) {
+        op->ctx->err = "tensor-core element phase: binary32 operators of P2 or P3 only";
+        return FGPU_ERR_INVALID;
+    }
+    op->use_tc = on ? 1 : 0;
+    return FGPU_OK;
 }
 
 extern "C" int fgpu_operator_destroy(fgpu_operator* op) {

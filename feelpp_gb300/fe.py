@@ -530,6 +530,10 @@ class Operator:
         self.h = h
         self.precision = precision
 
+    def use_tensor_cores(self, on=True):
+        """binary32 P2/P3 operators: element phase on the tensor cores (tcgen05, 3xTF32)."""
+        self.env.check(self.env.lib.fgpu_operator_set_tensor_cores(self.h, 1 if on else 0))
+
     def set_dirichlet(self, dofs):
         dofs = np.ascontiguousarray(dofs, dtype=np.int32)
         self.env.check(self.env.lib.fgpu_operator_set_dirichlet(self.h, len(dofs), _ptr(dofs)))

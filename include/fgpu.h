@@ -211,6 +211,12 @@ int fgpu_operator_create(fgpu_ctx* ctx, fgpu_space* V, const fgpu_form_desc* for
 int fgpu_operator_set_dirichlet(fgpu_operator* op, int64_t ndofs, const int32_t* dofs);
 int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_vector* x, fgpu_vector* y);
 int fgpu_operator_destroy(fgpu_operator* op);
+/* run the binary32 element phase on the tensor cores (tcgen05.mma kind::tf32, 3xTF32 split,
+ * accumulator in tensor memory); P2 / P3 binary32 operators */
+int fgpu_operator_set_tensor_cores(fgpu_operator* op, int on);
+/* tensor-core self-check: D = A B^T with A 128 x 24 and B 144 x 24 (row-major binary32, host
+ * arrays) through the same staging / descriptors / MMA / read-back as the operator */
+int fgpu_tc_selftest(fgpu_ctx* ctx, const float* A, const float* B, float* D);
 /* matrix-free PCG (Jacobi from the operator diagonal): plain with a binary64 operator, or
  * mixed (cfg->mixed) with a binary32 inner operator op32 refined by op's residual */
 int fgpu_solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const fgpu_vector* b, fgpu_vector* x,
