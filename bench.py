@@ -48,6 +48,11 @@ def parse():
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-n", type=int, default=24)
+    p.add_argument("--workload", default="assembly", choices=["assembly", "matfree", "elasticity"],
+                   help="assembly: the headline P2 assembly + CG line; matfree: P3 matrix-free operator and CG; "
+                        "elasticity: vector P2 linear elasticity assembly (FP64, FP32) and CG")
+    p.add_argument("--perturb", type=float, default=None)
+    p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--probe", default=None, choices=[None, "cg"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed)")
     return p.parse_args()
@@ -392,10 +397,165 @@ def run_probe_cg(args):
             print("stopped:", e)
 
 
+def run_matfree(args):
+    """Config 5: P3 Poisson, matrix-free operator in FP32 (CUDA cores and tensor cores), df64 and
+    native FP64; mixed CG (FP32 inner, FP64 residual) to 1e-10; L2/H1 errors."""
+    import ctypes as C
+
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    env = fpp.Environment(device=0, stream=C.c_void_p(stream.cuda_stream), profile=True)
+    perturb = 0.1 if args.perturb is None else args.perturb
+    xyz, tets = meshgen.kuhn_box(args.n, perturb=perturb, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, args.order)
+    u, v = V.element(), V.element()
+    integral = fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v)))
+    bd = V.boundary_dofs()
+    ops = {}
+    for name, prec, tc in [("f32_tensor_cores", "f32", True), ("f32_cuda_cores", "f32", False), ("df64", "df64", False),
+                           ("f64", "f64", False)]:
+        op = fpp.operator(V, integral, precision=prec)
+        if tc:
+            op.use_tensor_cores(True)
+        op.set_dirichlet(bd)
+        ops[name] = op
+    x, y = V.element(), V.element()
+    x.upload(np.random.default_rng(0).standard_normal(V.ndof))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    applies = {}
+    with ClockSampler(0) as clk:
+        for name, op in ops.items():
+            reps = 2 if name == "f64" else max(args.steps, 3)
+            for _ in range(2):
+                op.apply(x, y)
+            env.prof_reset()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                op.apply(x, y)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            ne, te = env.prof("matfree_element")
+            ng, tg = env.prof("matfree_gather")
+            applies[name] = {"ms_per_apply": ms, "gdof_per_s": V.ndof / (ms / 1e3) / 1e9,
+                             "element_phase_ms": te / max(ne, 1), "node_phase_ms": tg / max(ng, 1)}
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    lv = l.to_numpy()
+    lv[bd] = 0.0
+    l.vec.upload(lv)
+    sol = V.element()
+    st_mixed = ops["f64"].solve(l, sol, rtol=1e-10, inner=ops["f32_tensor_cores"])
+    err_mixed = sol.errors_sine(8)
+    sol2 = V.element()
+    st_mixed_cc = ops["f64"].solve(l, sol2, rtol=1e-10, inner=ops["f32_cuda_cores"])
+    solve = {"mixed_fp32_tensor_cores": st_mixed, "mixed_fp32_cuda_cores": st_mixed_cc,
+             "l2_error": err_mixed[0], "h1_error": err_mixed[1]}
+    if args.with_plain:
+        sol3 = V.element()
+        st_plain = ops["df64"].solve(l, sol3, rtol=1e-10)
+        e3 = sol3.errors_sine(8)
+        solve["plain_df64"] = st_plain
+        solve["plain_df64_errors"] = e3
+        solve["l2_error_rel_diff_vs_plain"] = abs(err_mixed[0] - e3[0]) / e3[0]
+    out = {"metric": "P3 matrix-free operator apply GDOF/s & CG time-to-1e-10 (FP32 tensor-core inner + FP64 residual)",
+           "value": applies["f32_tensor_cores"]["gdof_per_s"], "unit": "GDOF/s", "n_gpus": 1,
+           "steps": args.steps, "higher_is_better": True, "dtype": "f32 (3xTF32 tensor cores) / f64 residual",
+           "data": "synthetic",
+           "config": {"workload": "P%d Poisson matrix-free, %d^3-hex Kuhn cube (%d tets, N=%d), perturb %.2fh, kappa=1"
+                      % (args.order, args.n, len(tets), V.ndof, perturb)},
+           "applies": applies, "solve": solve, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
+def run_elasticity(args):
+    """Vector P2 linear elasticity (lambda = 1, mu = 0.5) on the 48^3-hex Kuhn mesh of
+    [0,4]x[0,1]x[0,1]: FP64 and FP32 assembly into the device CSR, body force (0,0,-1),
+    clamped at x = 0 (symmetric elimination), PCG to 1e-10 in FP64 and mixed
+    (binary32 CG with binary64 residual replacement); displacement difference vs FP64."""
+    import ctypes as C
+
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    env = fpp.Environment(device=0, stream=C.c_void_p(stream.cuda_stream), profile=True)
+    n = args.n if args.n != 64 else 48
+    perturb = 0.1 if args.perturb is None else args.perturb
+    xyz, tets = meshgen.kuhn_box(n, lengths=(4.0, 1.0, 1.0), perturb=perturb, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, 2)
+    u, v = V.element(), V.element()
+    form = fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, 1.0, 0.5), fpp.grad(v)))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    asm = {}
+    mats = {}
+    with ClockSampler(0) as clk:
+        for prec in ("f64", "f32"):
+            a = fpp.form2(test=V, trial=V, precision=prec)
+            for _ in range(max(args.warmup, 3)):
+                a.assign(form)
+            torch.cuda.synchronize()
+            env.prof_reset()
+            e0.record(stream)
+            for _ in range(args.steps):
+                a.assign(form)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            g_cnt, g_ms = env.prof("assemble_gather_elasticity")
+            asm[prec] = {"ms_per_step": ms, "mnnz_per_s": a.nnz / (ms / 1e3) / 1e6,
+                         "kernel_ms": g_ms / max(g_cnt, 1)}
+            mats[prec] = a
+    v64, v32 = mats["f64"].values(), mats["f32"].values()
+    big = np.abs(v64) > 1e-14 * np.abs(v64).max()
+    rel = np.abs(v32[big] - v64[big]) / np.abs(v64[big])
+    asm["f32"]["max_rel_err_vs_fp64"] = float(rel.max())
+    asm["f32"]["median_rel_err_vs_fp64"] = float(np.median(rel))
+    del mats["f32"]
+    a = mats["f64"]
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.cst_vec(0, 0, -1), fpp.id(v))))
+    a += fpp.on(fpp.markedfaces(M, 0.0), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    solve = None
+    if not args.no_solve:
+        s64 = a.solve(rhs=l, solution=u, rtol=1e-10)
+        u2 = V.element()
+        smx = a.solve(rhs=l, solution=u2, rtol=1e-10, mixed=True)
+        x64, xmx = u.to_numpy(), u2.to_numpy()
+        solve = {"fp64": s64, "mixed_fp32_refine": smx,
+                 "displacement_rel_diff_vs_fp64": float(np.linalg.norm(xmx - x64) / np.linalg.norm(x64)),
+                 "min_uz": float(x64.reshape(-1, 3)[:, 2].min()),
+                 "speedup_mixed_vs_fp64": s64["time_ms"] / smx["time_ms"] if smx["time_ms"] else None}
+    out = {"metric": "vector P2 elasticity assembly Mnnz/s & CG time-to-1e-10", "value": asm["f64"]["mnnz_per_s"],
+           "unit": "Mnnz/s", "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "dtype": "f64",
+           "data": "synthetic",
+           "config": {"workload": "vector P2 elasticity (lambda 1, mu 0.5), %d^3-hex Kuhn mesh of [0,4]x[0,1]^2 (%d tets, N=%d, nnz=%d), perturb %.2fh"
+                      % (n, len(tets), V.ndof, a.nnz, perturb)},
+           "assembly": asm, "solve": solve, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "elasticity":
+        run_elasticity(args)
+        return
     if args.probe == "cg":
         run_probe_cg(args)
+        return
+    if args.workload == "matfree":
+        run_matfree(args)
         return
     rank, world, local = dist_init(args)
     if args.impl == "reference":

@@ -91,6 +91,7 @@ SIGNATURES = {
     "fgpu_dirichlet": (i32, [P, P, P, i64, P, P, i32, f64]),
     "fgpu_matrix_mult": (i32, [P, P, P, P]),
     "fgpu_solve_cg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
+    "fgpu_norms_sine": (i32, [P, P, P, i32, DP, DP]),
     "fgpu_operator_create": (i32, [P, P, C.POINTER(FormDesc), i32, PP]),
     "fgpu_operator_set_dirichlet": (i32, [P, i64, P]),
     "fgpu_operator_apply": (i32, [P, P, P, P]),

@@ -14,6 +14,7 @@ namespace fgpu {
 int launch_assemble_elasticity(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const double* d_coef, double lam,
                                double mu, int accumulate);
 int launch_expand_pattern(fgpu_ctx* ctx, const DevPattern& P, int nc, int64_t* d_ia, int32_t* d_ja);
+int launch_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, const double* d_u, double* l2, double* h1);
 }  // namespace fgpu
 
 using namespace fgpu;
@@ -643,6 +644,16 @@ int fgpu_host_df64_ops(int op, int64_t n, const double* a, const double* b, doub
         out[i] = df2d(r);
     }
     return FGPU_OK;
+}
+
+int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, int quad_degree, double* l2, double* h1) {
+    if (!ctx || !V || !u || !l2 || !h1 || u->n != V->ndof || V->ncomp != 1) return set_err(ctx, FGPU_ERR_INVALID, "norms: bad arguments");
+    std::string err;
+    DevTables* tab = get_dev_tables(V->order, quad_degree > 0 ? quad_degree : 2 * V->order, err);
+    if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
+    int rc = finish(ctx);
+    if (rc) return rc;
+    return launch_norms_sine(ctx, V, tab, u->d, l2, h1);
 }
 
 int fgpu_prof_reset(fgpu_ctx* ctx) {

@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "df64.h"
 #include "fgpu_core.h"
@@ -936,6 +937,112 @@ int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* ta
                                : run_gather_row<kModeDF64, 20, 1>(ctx, A, tab, rec, accumulate);
     ctx->err = "unsupported order";
     return FGPU_ERR_INVALID;
+}
+
+}  // namespace fgpu
+
+// ===========================================================================
+// Error norms against u = sin(pi x) sin(pi y) sin(pi z): normL2 / normH1
+// (feelpp/feel/feelvf/norml2.hpp:37, normh1.hpp = integrate(elements, (u_h - u)^2)).
+// One thread per element in binary64; per-block partial sums, summed on the host.
+// ===========================================================================
+namespace fgpu {
+
+template <int N>
+__global__ void norms_sine_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                  const int32_t* __restrict__ l2n, const double* __restrict__ u, int Q,
+                                  const double* __restrict__ qx, const double* __restrict__ qw, const double* __restrict__ phi,
+                                  const double* __restrict__ dphi, double* __restrict__ partial) {
+    __shared__ double s0[256], s1[256];
+    double a0 = 0.0, a1 = 0.0;
+    const double pi = 3.141592653589793;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        const int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
+        const int vv[4] = {t.x, t.y, t.z, t.w};
+        double X[4][3];
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) X[v][d] = xyz[3 * (int64_t)vv[v] + d];
+        double K[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) K[r * 3 + c] = 0.5 * X[c + 1][r] - 0.5 * X[0][r];
+        const double c00 = K[4] * K[8] - K[5] * K[7], c01 = K[5] * K[6] - K[3] * K[8], c02 = K[3] * K[7] - K[4] * K[6];
+        const double det = K[0] * c00 + K[1] * c01 + K[2] * c02;
+        const double cof[9] = {c00, c01, c02,
+                               K[2] * K[7] - K[1] * K[8], K[0] * K[8] - K[2] * K[6], K[1] * K[6] - K[0] * K[7],
+                               K[1] * K[5] - K[2] * K[4], K[2] * K[3] - K[0] * K[5], K[0] * K[4] - K[1] * K[3]};
+        const double J = fabs(det);
+        double ue[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) ue[i] = u[l2n[e * N + i]];
+        for (int q = 0; q < Q; ++q) {
+            const double xh = qx[3 * q], yh = qx[3 * q + 1], zh = qx[3 * q + 2];
+            const double g[4] = {-0.5 * (1 + xh + yh + zh), 0.5 * (1 + xh), 0.5 * (1 + yh), 0.5 * (1 + zh)};
+            double p[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) p[d] = X[0][d] * g[0] + X[1][d] * g[1] + X[2][d] * g[2] + X[3][d] * g[3];
+            double uh = 0.0, gh[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                uh += ue[i] * phi[q * N + i];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) gh[a] += ue[i] * dphi[(q * N + i) * 3 + a];
+            }
+            // physical gradient B ghat, B = cof / det
+            double gp[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) gp[r] = (cof[3 * r] * gh[0] + cof[3 * r + 1] * gh[1] + cof[3 * r + 2] * gh[2]) / det;
+            const double sx = sin(pi * p[0]), sy = sin(pi * p[1]), sz = sin(pi * p[2]);
+            const double cx = cos(pi * p[0]), cy = cos(pi * p[1]), cz = cos(pi * p[2]);
+            const double ex = uh - sx * sy * sz;
+            const double g0 = gp[0] - pi * cx * sy * sz, g1 = gp[1] - pi * sx * cy * sz, g2 = gp[2] - pi * sx * sy * cz;
+            const double wJ = qw[q] * J;
+            a0 += wJ * ex * ex;
+            a1 += wJ * (g0 * g0 + g1 * g1 + g2 * g2);
+        }
+    }
+    s0[threadIdx.x] = a0;
+    s1[threadIdx.x] = a1;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s0[threadIdx.x] += s0[threadIdx.x + o];
+            s1[threadIdx.x] += s1[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = s0[0];
+        partial[2 * blockIdx.x + 1] = s1[0];
+    }
+}
+
+int launch_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, const double* d_u, double* l2, double* h1) {
+    const fgpu_mesh* M = V->mesh;
+    const int threads = 256;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + threads - 1) / threads, 152 * 8));
+    double* partial = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&partial, 2 * blocks * sizeof(double)));
+    switch (V->n) {
+        case 4: norms_sine_kernel<4><<<blocks, threads, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, V->d_l2n, d_u, tab->Q, tab->d_qx, tab->d_qw, tab->d_phi, tab->d_dphi, partial); break;
+        case 10: norms_sine_kernel<10><<<blocks, threads, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, V->d_l2n, d_u, tab->Q, tab->d_qx, tab->d_qw, tab->d_phi, tab->d_dphi, partial); break;
+        case 20: norms_sine_kernel<20><<<blocks, threads, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, V->d_l2n, d_u, tab->Q, tab->d_qx, tab->d_qw, tab->d_phi, tab->d_dphi, partial); break;
+        default: cudaFree(partial); ctx->err = "unsupported order"; return FGPU_ERR_INVALID;
+    }
+    ctx->launches++;
+    std::vector<double> h(2 * blocks);
+    cudaError_t e = cudaMemcpyAsync(h.data(), partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(partial);
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return FGPU_ERR_CUDA; }
+    double s0 = 0, s1 = 0;
+    for (int b = 0; b < blocks; ++b) { s0 += h[2 * b]; s1 += h[2 * b + 1]; }
+    *l2 = std::sqrt(s0);
+    *h1 = std::sqrt(s1);
+    return FGPU_OK;
 }
 
 }  // namespace fgpu

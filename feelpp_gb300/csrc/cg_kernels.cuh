@@ -330,4 +330,60 @@ static __global__ void axpy_f_kernel(int64_t n, double* __restrict__ x, const fl
         x[i] = fma(scale, (double)d[i], x[i]);
 }
 
+// After a reliable update replaced r: z = dinv r and the partial sums of r.r, r.z
+template <class PL>
+__global__ void cg_refresh_kernel(int64_t n, const typename PL::S* __restrict__ r, const typename PL::S* __restrict__ dinv,
+                                  typename PL::S* __restrict__ z, typename PL::D* __restrict__ partial,
+                                  typename PL::S* __restrict__ p_restart) {
+    __shared__ typename PL::D sh[32];
+    typename PL::D rr = PL::dzero(), rz = PL::dzero();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const typename PL::A ri = PL::ld(r[i]);
+        const typename PL::S zs = PL::st(PL::mul(PL::ld(dinv[i]), ri));
+        z[i] = zs;
+        if (p_restart) p_restart[i] = zs;
+        rr = PL::dmadd(rr, ri, ri);
+        rz = PL::dmadd(rz, ri, PL::ld(zs));
+    }
+    typename PL::D a = block_sum<PL>(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = a;
+    a = block_sum<PL>(rz, sh);
+    if (threadIdx.x == 0) partial[gridDim.x + blockIdx.x] = a;
+}
+
+// New r.r and r.z in both parity slots; iteration count kept. The search
+// direction p is kept unless the refresh restarts it (p = z, passed as
+// p_restart to cg_refresh_kernel): the last iteration before a converged
+// recurrence leaves p without its beta update.
+template <class PL>
+__global__ void cg_refresh_scalars(const typename PL::D* __restrict__ partial, int nb, CGScalars<PL>* sc) {
+    __shared__ typename PL::D sh[32];
+    const typename PL::D a = sum_partials<PL>(partial, nb, sh);
+    const typename PL::D c = sum_partials<PL>(partial + nb, nb, sh);
+    if (threadIdx.x == 0) {
+        sc->rr = a;
+        sc->rz[0] = c;
+        sc->rz[1] = c;
+        sc->done = 0;
+        sc->fail = 0;
+    }
+}
+
+// per-block partial sums of v.v (binary64)
+static __global__ void norm2_partial_kernel(int64_t n, const double* __restrict__ v, double* __restrict__ partial) {
+    __shared__ double sh[32];
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) s = fma(v[i], v[i], s);
+    const double t = block_sum<PolF64>(s, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// x_hi += scale * x_lo (binary64 += binary32), x_lo = 0
+static __global__ void fold_kernel(int64_t n, double* __restrict__ xh, float* __restrict__ xl, double scale) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        xh[i] = fma(scale, (double)xl[i], xh[i]);
+        xl[i] = 0.0f;
+    }
+}
+
 }  // namespace fgpu

@@ -19,6 +19,7 @@
 // multiply-adds on the FP32 pipes), df64 (double-float, ~48 bits) and native
 // binary64 (FP64 pipe; the reference arithmetic).
 #include <cmath>
+#include <functional>
 #include <cstring>
 #include <vector>
 
@@ -447,9 +448,19 @@ static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* 
 // Matrix-free PCG with Jacobi (operator diagonal). For the binary32 operator the
 // iterations run from a captured graph like the CSR solver; the binary64 ones
 // launch per iteration (their element phase is long, launch overhead is noise).
+//
+// Optional reliable updates (mixed precision): at a poll point where the
+// recurrence residual has dropped by delta since the last update, or claims
+// convergence, `refresh` folds x into the binary64 solution, zeroes x and
+// replaces r by the binary64 residual; the search direction is kept.
+template <class PL>
+using MfRefreshFn = std::function<int(typename PL::S* x, typename PL::S* r, bool* converged)>;
+
 template <class PL>
 static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b, typename PL::S* x, double rtol, int maxit, int pc,
-                       int check_every, int* iters, int* fail, double* rr_out, double* bb_out) {
+                       int check_every, int* iters, int* fail, double* rr_out, double* bb_out,
+                       const MfRefreshFn<PL>* refresh = nullptr, double delta = 0.1, int* nrefresh_out = nullptr,
+                       bool* true_conv = nullptr) {
     typedef typename PL::S S;
     typedef typename PL::D D;
     const int64_t n = op->nnodes;
@@ -509,8 +520,31 @@ static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b
     }
     CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    int guard = 0, parity = 0;
-    while (!hsc->done) {
+    int guard = 0, parity = 0, nref = 0;
+    double rr_ref = PL::host_to_double(hsc->rr);
+    while (true) {
+        bool want = false;
+        if (hsc->done) {
+            if (!refresh || hsc->fail != 0) break;
+            want = true;                                   // recurrence converged: verify in binary64
+        } else if (refresh && PL::host_to_double(hsc->rr) <= delta * delta * rr_ref) {
+            want = true;
+        }
+        if (want) {
+            bool conv = false;
+            const int rc2 = (*refresh)(x, r, &conv);
+            if (rc2) { cleanup(); return rc2; }
+            ++nref;
+            if (conv) { if (true_conv) *true_conv = true; break; }
+            if (hsc->it >= maxit) { hsc->fail = 2; break; }
+            cg_refresh_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, r, dinv, z, partial, hsc->done ? p : nullptr);
+            cg_refresh_scalars<PL><<<1, 256, 0, s>>>(partial, vb, sc);
+            ctx->launches += 2;
+            CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            rr_ref = PL::host_to_double(hsc->rr);
+            continue;
+        }
         if (use_graph) {
             CK(cudaGraphLaunch(exec, s));
             ctx->launches += 4 * check_every;
@@ -525,6 +559,7 @@ static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b
         CK(cudaStreamSynchronize(s));
         if (++guard > maxit + 2) break;
     }
+    if (nrefresh_out) *nrefresh_out = nref;
     *iters = hsc->it;
     *fail = hsc->fail;
     *rr_out = PL::host_to_double(hsc->rr);
@@ -535,11 +570,17 @@ static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b
 }
 
 static double host_norm(fgpu_ctx* ctx, int64_t n, const double* d) {
-    std::vector<double> h(n);
-    cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    const int vb = vec_blocks(n);
+    double* partial = nullptr;
+    std::vector<double> h(vb, 0.0);
+    if (cudaMalloc(&partial, vb * sizeof(double)) != cudaSuccess) return NAN;
+    norm2_partial_kernel<<<vb, 256, 0, ctx->stream>>>(n, d, partial);
+    ctx->launches++;
+    cudaMemcpyAsync(h.data(), partial, vb * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
+    cudaFree(partial);
     double s = 0;
-    for (double v : h) s += v * v;
+    for (double v : h) s += v;
     return std::sqrt(s);
 }
 
@@ -583,23 +624,42 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
             ctx->err = "mixed matrix-free solve: allocation failed";
             rc = FGPU_ERR_ALLOC;
         }
-        const double inner = cfg->inner_rtol > 0 ? cfg->inner_rtol : 1e-4;
-        while (rc == FGPU_OK) {
-            rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
-            if (rc) break;
-            if (bn == 0.0 || rn <= cfg->rtol * bn) break;
-            if (outer >= 50 || iters >= cfg->maxit) { fail = 2; break; }
-            d2f_scaled_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, r, r32, 1.0 / rn);
+        // reliable updates: the binary32 CG runs on the residual equation with
+        // its own search direction; every delta reduction of its recurrence
+        // residual (and at its claimed convergence) the correction is folded
+        // into the binary64 solution and the residual replaced by b - A64 x.
+        if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+        if (rc == FGPU_OK && !(bn == 0.0 || rn <= cfg->rtol * bn)) {
+            const double delta = cfg->inner_rtol > 0 ? cfg->inner_rtol : 0.1;
+            const int vb = vec_blocks(n);
+            const double scale = rn;   // binary32 system scaled to a unit initial residual
+            d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, r, r32, 1.0 / scale);
             cudaMemsetAsync(d32, 0, n * sizeof(float), ctx->stream);
-            int it = 0, f = 0;
+            ctx->launches++;
+            MfRefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
+                fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, xl, scale);
+                ctx->launches++;
+                const int r2 = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                if (r2) return r2;
+                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, r, rl, 1.0 / scale);
+                ctx->launches++;
+                *conv = rn <= cfg->rtol * bn;
+                return FGPU_OK;
+            };
+            int f = 0;
             double rr = 0, bb = 0;
-            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, inner, cfg->maxit - iters, cfg->pc, ce, &it, &f, &rr, &bb);
-            if (rc) break;
-            iters += it;
-            ++outer;
-            axpy_f_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_x, d32, rn);
-            ctx->launches += 2;
-            if (f == 1) { fail = 1; break; }
+            bool conv = false;
+            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, cfg->rtol * bn / rn, cfg->maxit, cfg->pc, ce, &iters, &f, &rr, &bb,
+                                     &refresh, delta, &outer, &conv);
+            if (rc == FGPU_OK) {
+                if (f == 1) fail = 1;
+                else if (!conv) {
+                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, d32, scale);
+                    ctx->launches++;
+                    rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                    if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+                }
+            }
         }
         cudaFree(r32);
         cudaFree(d32);

@@ -23,6 +23,7 @@
 // iterations and polls the flag between replays.
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -45,14 +46,6 @@ __global__ void df2d_kernel(int64_t n, const float2* __restrict__ a, double* __r
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         b[i] = df2d(dfun(a[i]));
 }
-__global__ void norm2_partial_kernel(int64_t n, const double* __restrict__ v, double* __restrict__ partial) {
-    __shared__ double sh[32];
-    double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) s = fma(v[i], v[i], s);
-    const double t = block_sum<PolF64>(s, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = t;
-}
-
 // ---------------------------------------------------------------------------
 template <class PL>
 static void launch_spmv_t(cudaStream_t s, const fgpu_matrix* A, const typename PL::V* val, int G, const typename PL::S* x,
@@ -343,10 +336,18 @@ static int plan_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* 
 
 // One PCG solve with policy PL on values `val`, right-hand side b and solution x
 // (initial guess on entry), all in the policy's formats.
+// Optional reliable updates (mixed precision): at a poll point where the
+// recurrence residual has dropped by delta since the last update, or claims
+// convergence, `refresh` folds x into the binary64 solution, zeroes x and
+// replaces r by the binary64 residual; the search direction is kept.
+template <class PL>
+using RefreshFn = std::function<int(typename PL::S* x, typename PL::S* r, bool* converged)>;
+
 template <class PL>
 static int pcg_core(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* val, const typename PL::S* b,
                     typename PL::S* x, double rtol, int maxit, int pc, int check_every, int* iters, int* fail,
-                    double* rr_out, double* bb_out) {
+                    double* rr_out, double* bb_out, const RefreshFn<PL>* refresh = nullptr, double delta = 0.1,
+                    int* nrefresh_out = nullptr, bool* true_conv = nullptr) {
     typedef typename PL::S S;
     typedef typename PL::D D;
     const int64_t n = A->nrows;
@@ -413,14 +414,38 @@ static int pcg_core(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* v
     CK(cudaGraphInstantiate(&exec, graph, 0));
     CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    int guard = 0;
-    while (!hsc->done) {
+    int guard = 0, nref = 0;
+    double rr_ref = PL::host_to_double(hsc->rr);
+    while (true) {
+        bool want = false;
+        if (hsc->done) {
+            if (!refresh || hsc->fail != 0) break;
+            want = true;                                   // recurrence converged: verify in binary64
+        } else if (refresh && PL::host_to_double(hsc->rr) <= delta * delta * rr_ref) {
+            want = true;
+        }
+        if (want) {
+            bool conv = false;
+            const int rc2 = (*refresh)(x, r, &conv);
+            if (rc2) { cleanup(); return rc2; }
+            ++nref;
+            if (conv) { if (true_conv) *true_conv = true; break; }
+            if (hsc->it >= maxit) { hsc->fail = 2; break; }
+            cg_refresh_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, r, dinv, z, partial, hsc->done ? p : nullptr);
+            cg_refresh_scalars<PL><<<1, 256, 0, s>>>(partial, vb, sc);
+            ctx->launches += 2;
+            CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            rr_ref = PL::host_to_double(hsc->rr);
+            continue;
+        }
         CK(cudaGraphLaunch(exec, s));
         ctx->launches += 3 * check_every;
         CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         if (++guard > maxit / std::max(check_every, 1) + 2) break;
     }
+    if (nrefresh_out) *nrefresh_out = nref;
     *iters = hsc->it;
     *fail = hsc->fail;
     *rr_out = PL::host_to_double(hsc->rr);
@@ -518,18 +543,20 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
 
 int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A32, const double* d_b, double* d_x,
                     const fgpu_solver_cfg* cfg, fgpu_solve_stats* st) {
+    // Mixed precision with reliable updates: binary32 CG on A32 for the
+    // correction, binary64 solution and binary64 residual replacement.
     const int64_t n = A64->nrows;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
     int rc = FGPU_OK;
-    int total = 0, outer = 0, fail = 0;
+    int total = 0, nref = 0, fail = 0;
     double rn = 0, bn = 0;
     {
         Scratch64 S;
-        float *r32 = nullptr, *d32 = nullptr;
-        if (!S.alloc(n) || cudaMalloc(&r32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&d32, n * sizeof(float)) != cudaSuccess) {
+        float *r32 = nullptr, *x32 = nullptr;
+        if (!S.alloc(n) || cudaMalloc(&r32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&x32, n * sizeof(float)) != cudaSuccess) {
             ctx->err = "mixed solve: allocation failed";
             rc = FGPU_ERR_ALLOC;
         }
@@ -538,35 +565,46 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
             norm2_partial_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_b, S.partial);
             cudaMemcpyAsync(S.hpart, S.partial, vb * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
             cudaStreamSynchronize(ctx->stream);
-            double s = 0;
-            for (int k = 0; k < vb; ++k) s += S.hpart[k];
-            bn = std::sqrt(s);
-            const double inner = cfg->inner_rtol > 0 ? cfg->inner_rtol : 1e-4;
-            const int ce = cfg->check_every > 0 ? cfg->check_every : 16;
-            while (true) {
-                rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
-                if (rc) break;
-                if (bn == 0.0 || rn <= cfg->rtol * bn) break;
-                if (outer >= 50 || total >= cfg->maxit) { fail = 2; break; }
-                // inner: A32 d = r / ||r|| in binary32
-                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, r32, 1.0 / rn);
-                cudaMemsetAsync(d32, 0, n * sizeof(float), ctx->stream);
-                ctx->launches++;
+            double s2 = 0;
+            for (int k = 0; k < vb; ++k) s2 += S.hpart[k];
+            bn = std::sqrt(s2);
+            rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+            if (rc == FGPU_OK && !(bn == 0.0 || rn <= cfg->rtol * bn)) {
+                const double delta = cfg->inner_rtol > 0 ? cfg->inner_rtol : 0.1;
+                const int ce = cfg->check_every > 0 ? cfg->check_every : 16;
+                const double scale = rn;   // binary32 system scaled to a unit initial residual
+                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, r32, 1.0 / scale);
+                cudaMemsetAsync(x32, 0, n * sizeof(float), ctx->stream);
+                RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
+                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, xl, scale);
+                    int r2 = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+                    if (r2) return r2;
+                    d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, rl, 1.0 / scale);
+                    ctx->launches += 2;
+                    *conv = rn <= cfg->rtol * bn;
+                    return FGPU_OK;
+                };
                 int it = 0, f = 0;
                 double rr = 0, bb = 0;
-                rc = pcg_core<PolF32>(ctx, A32, (const float*)A32->d_val, r32, d32, inner, cfg->maxit - total, cfg->pc, ce,
-                                      &it, &f, &rr, &bb);
-                if (rc) break;
-                total += it;
-                ++outer;
-                axpy_f_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, d32, rn);
-                ctx->launches++;
-                if (f == 1) { fail = 1; break; }
+                bool conv = false;
+                // recurrence tolerance in absolute terms: ||r|| <= rtol ||b|| (relative to the initial ||r|| = rn)
+                rc = pcg_core<PolF32>(ctx, A32, (const float*)A32->d_val, r32, x32, cfg->rtol * bn / rn, cfg->maxit, cfg->pc, ce,
+                                      &it, &f, &rr, &bb, &refresh, delta, &nref, &conv);
+                total = it;
+                if (rc == FGPU_OK) {
+                    if (f == 1) fail = 1;
+                    else if (!conv) {
+                        // fold what is left and measure the final binary64 residual
+                        fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, x32, scale);
+                        rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+                        if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+                    }
+                }
             }
             cudaStreamSynchronize(ctx->stream);
         }
         cudaFree(r32);
-        cudaFree(d32);
+        cudaFree(x32);
     }
     cudaEventRecord(e1, ctx->stream);
     cudaEventSynchronize(e1);
@@ -577,11 +615,11 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
     if (rc != FGPU_OK) return rc;
     if (st) {
         st->iterations = total;
-        st->outer = outer;
+        st->outer = nref;
         st->rel_residual = bn > 0 ? rn / bn : 0.0;
         st->time_ms = ms;
     }
-    if (fail == 1) { ctx->err = "CG breakdown in the inner FP32 solve"; return FGPU_ERR_BREAKDOWN; }
+    if (fail == 1) { ctx->err = "CG breakdown in the binary32 iteration"; return FGPU_ERR_BREAKDOWN; }
     if (fail == 2) { ctx->err = "mixed CG did not reach rtol"; return FGPU_ERR_NOT_CONVERGED; }
     return FGPU_OK;
 }

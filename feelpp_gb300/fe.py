@@ -206,6 +206,12 @@ class Element(DeviceVector):
         self.space = space
         self.name = name
 
+    def errors_sine(self, quad=0):
+        """(normL2, normH1-seminorm) of self - sin(pi x) sin(pi y) sin(pi z)."""
+        l2, h1 = C.c_double(), C.c_double()
+        self.env.check(self.env.lib.fgpu_norms_sine(self.env.h, self.space.h, self.h, quad, C.byref(l2), C.byref(h1)))
+        return float(l2.value), float(h1.value)
+
 
 # ---------------------------------------------------------------------------
 # ranges and expressions
@@ -489,10 +495,12 @@ class Form2:
     def mult(self, x, y):
         self.env.check(self.env.lib.fgpu_matrix_mult(self.env.h, self.h, x.h, y.h))
 
-    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False, inner_rtol=1e-4,
+    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False, inner_rtol=0.1,
               check_every=16, arith="f64"):
-        """CG + Jacobi (ksp-type=cg, pc-type=jacobi). mixed=True: binary32 inner CG refined with
-        the binary64 residual; arith="df64": double-float arithmetic for the plain solve."""
+        """CG + Jacobi (ksp-type=cg, pc-type=jacobi). mixed=True: binary32 CG whose iterate is folded
+        into the binary64 solution, and its residual replaced by the binary64 one, each time the
+        recurrence residual has dropped by `inner_rtol`; arith="df64": double-float arithmetic for
+        the plain solve."""
         cfg = _ffi.SolverCfg(rtol, maxit, _ffi.PC_JACOBI if pc == "jacobi" else _ffi.PC_NONE, 1 if mixed else 0,
                              inner_rtol, check_every, _ffi.ARITH_DF64 if arith == "df64" else _ffi.ARITH_F64)
         st = _ffi.SolveStats()
@@ -541,8 +549,9 @@ class Operator:
     def apply(self, x, y):
         self.env.check(self.env.lib.fgpu_operator_apply(self.env.h, self.h, x.h, y.h))
 
-    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=1e-4, check_every=16):
-        """Matrix-free PCG; with `inner` (a binary32 Operator) the mixed method is used."""
+    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=0.1, check_every=16):
+        """Matrix-free PCG; with `inner` (a binary32 Operator) the mixed method is used
+        (binary32 CG with binary64 residual replacement every `inner_rtol` reduction)."""
         cfg = _ffi.SolverCfg(rtol, maxit, _ffi.PC_JACOBI if pc == "jacobi" else _ffi.PC_NONE, 1 if inner else 0,
                              inner_rtol, check_every, _ffi.ARITH_F64)
         st = _ffi.SolveStats()

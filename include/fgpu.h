@@ -98,15 +98,16 @@ typedef struct {
     double rtol;              /* stop when ||b - A x||_2 <= rtol ||b||_2 (ksp-rtol) */
     int maxit;                /* ksp-max-it */
     int pc;                   /* FGPU_PC_* (pc-type) */
-    int mixed;                /* 1: FP32 inner CG + FP64 residual refinement */
-    double inner_rtol;        /* inner relative tolerance of the mixed solver (0 = 1e-4) */
+    int mixed;                /* 1: binary32 CG with binary64 reliable updates (residual replacement) */
+    double inner_rtol;        /* mixed: reduction of the binary32 recurrence residual between two
+                                 binary64 residual replacements (0 = 0.1) */
     int check_every;          /* iterations per convergence poll (0 = 16) */
     int arith;                /* FGPU_ARITH_* of the non-mixed solve */
 } fgpu_solver_cfg;
 
 typedef struct {
     int iterations;           /* total (inner) CG iterations */
-    int outer;                /* refinement steps (mixed) */
+    int outer;                /* binary64 residual replacements (mixed) */
     double rel_residual;      /* final ||b - A x||_2 / ||b||_2 recomputed in FP64 */
     double time_ms;           /* solve wall time on the device stream */
 } fgpu_solve_stats;
@@ -199,6 +200,10 @@ int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, 
  *      NULL: then it is made from A). x is the initial guess and the solution. ---- */
 int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+
+/* ---- error norms of a scalar field against u = sin(pi x) sin(pi y) sin(pi z):
+ *      normL2(u_h - u) and the H1 seminorm (feelpp/feel/feelvf/norml2.hpp:37, normh1.hpp) ---- */
+int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, int quad_degree, double* l2, double* h1);
 
 /* ---- matrix-free operator of a form (the reference applies form-level operators with
  *      MatrixShell::multVector, feelpp/feel/feelalg/matrixshell.hpp:49,120 and

@@ -65,6 +65,8 @@ def test_mixed_matfree_solve(env, order, n):
     st = op64.solve(l, u, rtol=1e-10, inner=op32)
     assert st["rel_residual"] <= 1e-10 and st["outer"] >= 2
     w = V.element()
+    st64 = a.solve(rhs=l, solution=w, rtol=1e-10)
+    assert st["iterations"] <= 1.25 * st64["iterations"] + 16
     a.solve(rhs=l, solution=w, rtol=1e-11)
     x, xr = u.to_numpy(), w.to_numpy()
     assert np.linalg.norm(x - xr) <= 1e-8 * np.linalg.norm(xr)
