@@ -48,9 +48,13 @@ def parse():
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-n", type=int, default=24)
-    p.add_argument("--workload", default="assembly", choices=["assembly", "matfree", "elasticity"],
+    p.add_argument("--nprob", type=int, default=512, help="batch: number of independent problems")
+    p.add_argument("--nmax", type=int, default=40, help="batch: largest cube resolution")
+    p.add_argument("--heat-steps", type=int, default=100, help="heat: backward-Euler steps")
+    p.add_argument("--workload", default="assembly", choices=["assembly", "matfree", "elasticity", "batch", "heat"],
                    help="assembly: the headline P2 assembly + CG line; matfree: P3 matrix-free operator and CG; "
-                        "elasticity: vector P2 linear elasticity assembly (FP64, FP32) and CG")
+                        "elasticity: vector P2 linear elasticity assembly (FP64, FP32) and CG; batch: many independent "
+                        "problems in one persistent launch; heat: graph-replayed reassembly for backward Euler")
     p.add_argument("--perturb", type=float, default=None)
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--probe", default=None, choices=[None, "cg"],
@@ -546,8 +550,198 @@ def run_elasticity(args):
     print(json.dumps(out), flush=True)
 
 
+def run_batch(args):
+    """Independent Poisson problems (cube resolution n ~ U{8..nmax}, order ~ U{1,2,3},
+    lognormal kappa, all seeded) assembled in FP64 by one geometry launch and one
+    persistent gather launch; compared with a loop of per-problem assemblies and
+    with the batch replayed from a captured CUDA graph."""
+    import ctypes as C
+
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import _ffi, meshgen
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    env = fpp.Environment(device=0, stream=C.c_void_p(stream.cuda_stream), profile=True)
+    rng = np.random.default_rng(4321)
+    ns = rng.integers(8, args.nmax + 1, size=args.nprob)
+    orders = rng.integers(1, 4, size=args.nprob)
+    t0 = time.perf_counter()
+    forms, integrals, keep = [], [], []
+    for k in range(args.nprob):
+        xyz, tets = meshgen.kuhn_box(int(ns[k]), perturb=0.15, seed=1234 + k)
+        kappa = meshgen.lognormal_kappa(len(tets), seed=5678 + k)
+        M = fpp.Mesh(xyz, tets, env=env)
+        V = fpp.Pch(M, int(orders[k]))
+        u, v = V.element(), V.element()
+        integrals.append(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v)))
+        forms.append(fpp.form2(test=V, trial=V))
+        keep.append((M, V))
+    batch = fpp.Batch(forms, integrals)
+    setup_s = time.perf_counter() - t0
+    nnz = sum(f.nnz for f in forms)
+    tets_total = int(sum(6 * int(n) ** 3 for n in ns))
+    batch.assemble()                               # tunes the launch shape
+    cfg = batch.launch_config()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(max(args.warmup, 3)):
+        batch.assemble()
+    env.prof_reset()
+    launches0 = env.launches()
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            batch.assemble()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = (env.launches() - launches0) // max(args.steps, 1)
+    g_cnt, g_ms = env.prof("batch_gather")
+    geo_cnt, geo_ms = env.prof("batch_geometry")
+    # the same problems one by one (two launches each, device-resident kappa)
+    descs, kps = [], []
+    for f, integral, dv in zip(forms, integrals, batch._kappa):
+        d, _ = fpp.Form2._desc_of(integral, _ffi.ALGO_AUTO)
+        descs.append(d)
+        kps.append(dv.device_ptr())
+
+    def loop():
+        for f, d, kp in zip(forms, descs, kps):
+            env.check(env.lib.fgpu_assemble_matrix_dev(env.h, f.h, C.byref(d), kp, 0))
+
+    loop()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(2):
+        loop()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_loop = e0.elapsed_time(e1) / 2
+    wall_loop = (time.perf_counter() - t1) / 2 * 1e3
+    with fpp.capture(env) as g:
+        batch.assemble()
+    g.launch(2)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    g.launch(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_graph = e0.elapsed_time(e1) / args.steps
+    hist = np.bincount(orders, minlength=4)[1:].tolist()
+    out = {"metric": "batched assembly Mnnz/s (independent uneven problems, one persistent launch)",
+           "value": nnz / (ms / 1e3) / 1e6, "unit": "Mnnz/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "dtype": "f64",
+           "data": "synthetic",
+           "config": {"workload": "%d Poisson problems, n ~ U{8..%d}, P1/P2/P3 = %s, lognormal kappa; %d tets, nnz %d"
+                      % (args.nprob, args.nmax, hist, tets_total, nnz)},
+           "gpu_launches_per_step": launches, "launch": cfg, "tuner_ms": None,
+           "kernels_ms": {"batch_gather": g_ms / max(g_cnt, 1), "batch_geometry": geo_ms / max(geo_cnt, 1)},
+           "loop_of_single_assemblies": {"ms_per_step": ms_loop, "host_wall_ms": wall_loop,
+                                         "launches_per_step": 2 * args.nprob},
+           "graph_replay_ms_per_step": ms_graph, "setup_s": setup_s, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
+def run_heat(args):
+    """P2 heat equation on the 64^3 Kuhn cube: backward Euler, (M + dt kappa(t) K) u^{n+1}
+    = M u^n + dt F with kappa(t) = 1 + 0.5 sin t and homogeneous Dirichlet rows. Each step
+    replays one captured CUDA graph (reassembly, right-hand side, Dirichlet rows) after
+    writing kappa(t) to a device scalar, then runs the CG solve (FP64 PCG to 1e-10, warm start)."""
+    import ctypes as C
+    import math
+
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    env = fpp.Environment(device=0, stream=C.c_void_p(stream.cuda_stream), profile=False)
+    n = args.n
+    xyz, tets = meshgen.kuhn_box(n, perturb=0.15, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    u, v = V.element(), V.element()
+    dt = 1.0 / args.heat_steps
+    kt = fpp.DeviceScalar(env, 1.0)
+    mass = fpp.form2(test=V, trial=V)
+    mass.assign(fpp.integrate(fpp.elements(M), fpp.idt(u) * fpp.id(v)))
+    F = fpp.form1(test=V)
+    F.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    bc = fpp.DirichletBC(V, V.boundary_dofs())
+    A = fpp.form2(test=V, trial=V)
+    integral = fpp.integrate(fpp.elements(M), dt * kt * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v))
+    b = V.element()
+    un = V.element()
+
+    def step_ops():
+        A.assign(integral)
+        mass.mult(un, b)
+        b.axpby(dt, F.vec, 1.0)
+        A.apply_bc(bc, rhs=b)
+
+    step_ops()
+    with fpp.capture(env) as g:
+        step_ops()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # reassembly alone: graph replay vs eager calls
+    for _ in range(3):
+        g.launch()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    g.launch(20)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_graph = e0.elapsed_time(e1) / 20
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(20):
+        step_ops()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_eager = e0.elapsed_time(e1) / 20
+    wall_eager = (time.perf_counter() - t0) / 20 * 1e3
+    # the time loop
+    un.zero()
+    its, solve_ms = [], []
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.heat_steps):
+            kt.set(1.0 + 0.5 * math.sin((k + 1) * dt))
+            g.launch()
+            st = A.solve(rhs=b, solution=un, rtol=1e-10)
+            its.append(st["iterations"])
+            solve_ms.append(st["time_ms"])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    l2, h1 = un.errors_sine(4)
+    out = {"metric": "P2 heat equation: graph-replayed reassembly ms/step and backward-Euler s/100 steps",
+           "value": ms_graph, "unit": "ms/reassembly", "n_gpus": 1, "steps": args.heat_steps,
+           "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "P2 heat, %d^3 Kuhn cube (%d tets, N=%d, nnz=%d), dt=%g, kappa(t)=1+0.5 sin t"
+                      % (n, len(tets), V.ndof, A.nnz, dt)},
+           "reassembly": {"graph_ms": ms_graph, "eager_ms": ms_eager, "eager_host_wall_ms": wall_eager,
+                          "mnnz_per_s_graph": A.nnz / (ms_graph / 1e3) / 1e6},
+           "time_loop": {"wall_s": wall, "cg_iterations_mean": float(np.mean(its)), "cg_ms_mean": float(np.mean(solve_ms)),
+                         "final_l2_norm_diff_to_sine": l2},
+           "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "batch":
+        run_batch(args)
+        return
+    if args.workload == "heat":
+        run_heat(args)
+        return
     if args.workload == "elasticity":
         run_elasticity(args)
         return

@@ -12,10 +12,10 @@ LIB_PATH = os.path.join(HERE, "_lib", "libfgpu.so")
 FGPU_OK = 0
 F64, F32, DF64 = 0, 1, 2
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
-ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64 = 0, 1, 2, 3
+ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE = 0, 1, 2, 3, 4
 RHS_SINE, RHS_CONST_VEC, RHS_CONST = 0, 1, 2
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
-PC_NONE, PC_JACOBI = 0, 1
+PC_NONE, PC_JACOBI, PC_CHEB_JACOBI = 0, 1, 2
 ARITH_F64, ARITH_DF64 = 0, 1
 
 ERROR_NAMES = {1: "FGPU_ERR_INVALID", 2: "FGPU_ERR_CUDA", 3: "FGPU_ERR_BAD_ELEMENT", 4: "FGPU_ERR_OUT_OF_RANGE",
@@ -34,7 +34,8 @@ class Config(C.Structure):
 
 class FormDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("kappa", C.c_double), ("kappa_elem", C.c_void_p), ("mass", C.c_double),
-                ("lam", C.c_double), ("mu", C.c_double), ("quad_degree", C.c_int), ("algo", C.c_int)]
+                ("lam", C.c_double), ("mu", C.c_double), ("quad_degree", C.c_int), ("algo", C.c_int),
+                ("kappa_scale", C.c_void_p)]
 
 
 class RhsDesc(C.Structure):
@@ -43,11 +44,13 @@ class RhsDesc(C.Structure):
 
 class SolverCfg(C.Structure):
     _fields_ = [("rtol", C.c_double), ("maxit", C.c_int), ("pc", C.c_int), ("mixed", C.c_int),
-                ("inner_rtol", C.c_double), ("check_every", C.c_int), ("arith", C.c_int)]
+                ("inner_rtol", C.c_double), ("check_every", C.c_int), ("arith", C.c_int),
+                ("cheb_degree", C.c_int), ("cheb_ratio", C.c_double)]
 
 
 class SolveStats(C.Structure):
-    _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("rel_residual", C.c_double), ("time_ms", C.c_double)]
+    _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("rel_residual", C.c_double), ("time_ms", C.c_double),
+                ("eig_max", C.c_double), ("fallback", C.c_int), ("fallback_iterations", C.c_int)]
 
 
 P = C.c_void_p
@@ -104,6 +107,20 @@ SIGNATURES = {
     "fgpu_host_ref_tables": (i32, [i32, i32, P, P, P, P, P, IP]),
     "fgpu_assemble_vector_noalloc": (i32, [P, C.POINTER(RhsDesc), P, i32, P]),
     "fgpu_host_df64_ops": (i32, [i32, i64, P, P, P]),
+    "fgpu_bc_create": (i32, [P, i64, i64, P, P, PP]),
+    "fgpu_bc_apply": (i32, [P, P, P, P, i32, f64]),
+    "fgpu_bc_destroy": (i32, [P]),
+    "fgpu_vector_axpby": (i32, [P, f64, P, f64, P]),
+    "fgpu_vector_copy": (i32, [P, P, P]),
+    "fgpu_graph_begin": (i32, [P]),
+    "fgpu_graph_end": (i32, [P, PP]),
+    "fgpu_graph_launch": (i32, [P, P, i32]),
+    "fgpu_graph_destroy": (i32, [P]),
+    "fgpu_batch_create": (i32, [P, i32, P, P, P, PP]),
+    "fgpu_batch_assemble": (i32, [P, P, i32]),
+    "fgpu_batch_set_launch": (i32, [P, i32, i32]),
+    "fgpu_batch_get_launch": (i32, [P, IP, IP, IP]),
+    "fgpu_batch_destroy": (i32, [P]),
     "fgpu_prof_reset": (i32, [P]),
     "fgpu_prof_get": (i32, [P, C.c_char_p, I64P, DP]),
 }

@@ -1,6 +1,9 @@
 // C-ABI entry points (include/fgpu.h). Host orchestration of the device
 // assembly path; every call returns a status code and never throws.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstring>
 #include <new>
 #include <string>
@@ -44,7 +47,7 @@ int dev_alloc(fgpu_ctx* ctx, T** p, size_t count) {
 
 // Resolve pending profiling events (after a stream sync) and check the status word.
 int finish(fgpu_ctx* ctx, bool sync = true) {
-    if (!sync) return FGPU_OK;
+    if (!sync || ctx->capturing) return FGPU_OK;   // captured calls: the status is checked at graph launch
     int hst = 0;
     cudaError_t e = cudaMemcpyAsync(&hst, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -98,6 +101,12 @@ int ensure_pattern(fgpu_space* V) {
 }
 
 int form_qdeg(const fgpu_space* V, int q) { return q > 0 ? q : 2 * V->order; }
+
+// calls that allocate, synchronize or read host data back cannot be captured
+#define FGPU_NO_CAPTURE(ctx, what)                                                              \
+    do {                                                                                        \
+        if ((ctx) && (ctx)->capturing) return set_err((ctx), FGPU_ERR_INVALID, what ": not allowed while capturing a graph"); \
+    } while (0)
 
 }  // namespace
 
@@ -159,6 +168,7 @@ int64_t fgpu_launch_count(const fgpu_ctx* ctx) { return ctx ? ctx->launches : 0;
 
 // ---------------------------------------------------------------------------
 int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, const int32_t* tets, fgpu_mesh** out) {
+    FGPU_NO_CAPTURE(ctx, "mesh_upload");
     if (!ctx || !out || !xyz || !tets || nv <= 0 || nt <= 0) return set_err(ctx, FGPU_ERR_INVALID, "mesh_upload: bad arguments");
     *out = nullptr;
     for (int64_t k = 0; k < 4 * nt; ++k)
@@ -187,6 +197,7 @@ int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, c
 int fgpu_mesh_set_coords(fgpu_mesh* M, const double* xyz) {
     if (!M || !xyz) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = M->ctx;
+    FGPU_NO_CAPTURE(ctx, "mesh_set_coords");
     FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(M->d_xyz, xyz, 3 * M->nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     std::memcpy(M->h_xyz.data(), xyz, 3 * M->nv * sizeof(double));
     return FGPU_OK;
@@ -203,6 +214,7 @@ int fgpu_mesh_destroy(fgpu_mesh* M) {
 
 // ---------------------------------------------------------------------------
 int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* M, int order, int ncomp, fgpu_space** out) {
+    FGPU_NO_CAPTURE(ctx, "space_create");
     if (!ctx || !M || !out) return set_err(ctx, FGPU_ERR_INVALID, "space_create: bad arguments");
     if (order < 1 || order > 3) return set_err(ctx, FGPU_ERR_INVALID, "order must be 1, 2 or 3");
     if (ncomp != 1 && ncomp != 3) return set_err(ctx, FGPU_ERR_INVALID, "ncomp must be 1 or 3");
@@ -273,6 +285,7 @@ int fgpu_space_destroy(fgpu_space* V) {
 
 // ---------------------------------------------------------------------------
 int fgpu_matrix_create(fgpu_ctx* ctx, fgpu_space* test, fgpu_space* trial, int precision, fgpu_matrix** out) {
+    FGPU_NO_CAPTURE(ctx, "matrix_create");
     if (!ctx || !test || !out) return set_err(ctx, FGPU_ERR_INVALID, "matrix_create: bad arguments");
     if (trial && trial != test) return set_err(ctx, FGPU_ERR_INVALID, "test and trial spaces must be the same space");
     if (precision != FGPU_F64 && precision != FGPU_F32) return set_err(ctx, FGPU_ERR_INVALID, "bad precision");
@@ -311,6 +324,7 @@ int fgpu_matrix_create(fgpu_ctx* ctx, fgpu_space* test, fgpu_space* trial, int p
 }
 
 int fgpu_matrix_create_like(const fgpu_matrix* S, int precision, fgpu_matrix** out) {
+    if (S) FGPU_NO_CAPTURE(S->ctx, "matrix_create_like");
     if (!S || !out) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = S->ctx;
     fgpu_matrix* A = new (std::nothrow) fgpu_matrix();
@@ -351,6 +365,7 @@ int fgpu_matrix_info(const fgpu_matrix* A, int64_t* nrows, int64_t* nnz, int* pr
 }
 
 int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* val) {
+    if (A) FGPU_NO_CAPTURE(A->ctx, "matrix_get_csr");
     if (!A) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = A->ctx;
     FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -395,11 +410,81 @@ int fgpu_matrix_destroy(fgpu_matrix* A) {
     }
     cudaFree(A->d_val);
     cudaFree(A->d_coef);
+    cudaFree(A->d_kbuf);
     delete A;
     return FGPU_OK;
 }
 
 // ---------------------------------------------------------------------------
+// Assembly tuner: for (device, order, precision, elements, nnz) time the fused
+// gather and the two-phase assembly once each (after a warm-up run, into a
+// scratch value array so the caller's matrix is untouched) and keep the faster.
+// Both give the same bits. While capturing a graph without a tuned choice the
+// fused gather is used (it allocates nothing).
+// ---------------------------------------------------------------------------
+static std::mutex g_asm_tune_mutex;
+static std::map<std::tuple<int, int, int, int64_t, int64_t>, int> g_asm_tune;
+
+static int tuned_assembly_algo(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* recs) {
+    const auto key = std::make_tuple(ctx->device, A->space->order, A->precision, A->space->mesh->nt, A->nnz);
+    {
+        std::lock_guard<std::mutex> lock(g_asm_tune_mutex);
+        auto it = g_asm_tune.find(key);
+        if (it != g_asm_tune.end()) return it->second;
+    }
+    if (ctx->capturing) return FGPU_ALGO_GATHER;
+    const size_t vbytes = (size_t)A->nnz * (A->precision == FGPU_F64 ? 8 : 4);
+    void* scratch = nullptr;
+    if (cudaMalloc(&scratch, vbytes) != cudaSuccess) {
+        cudaGetLastError();
+        return FGPU_ALGO_GATHER;             // no room to tune: keep the allocation-free variant
+    }
+    void* saved = A->d_val;
+    A->d_val = scratch;
+    const int save_prof = ctx->profile;
+    ctx->profile = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float ms[2] = {0, 0};
+    const int algos[2] = {FGPU_ALGO_GATHER, FGPU_ALGO_TWO_PHASE};
+    int rc = FGPU_OK;
+    for (int v = 0; v < 2 && rc == FGPU_OK; ++v) {
+        for (int rep = 0; rep < 2 && rc == FGPU_OK; ++rep) {
+            if (rep == 1) cudaEventRecord(e0, ctx->stream);
+            rc = algos[v] == FGPU_ALGO_TWO_PHASE ? launch_assemble_two_phase(ctx, A, tab, recs, 0)
+                                                 : launch_assemble_gather_df(ctx, A, tab, recs, 0);
+            if (rep == 1) cudaEventRecord(e1, ctx->stream);
+        }
+        if (rc == FGPU_OK) {
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms[v], e0, e1);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->profile = save_prof;
+    A->d_val = saved;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(scratch);
+    if (rc == FGPU_ERR_ALLOC) {
+        // the element buffer did not fit: the fused gather it is
+        ctx->err.clear();
+        rc = FGPU_OK;
+        ms[1] = 1e30f;
+    }
+    if (rc) return -rc;
+    const int pick = ms[1] < ms[0] ? FGPU_ALGO_TWO_PHASE : FGPU_ALGO_GATHER;
+    if (pick != FGPU_ALGO_TWO_PHASE) {        // release the element buffer
+        cudaFree(A->d_kbuf);
+        A->d_kbuf = nullptr;
+        A->kbuf_bytes = 0;
+    }
+    std::lock_guard<std::mutex> lock(g_asm_tune_mutex);
+    g_asm_tune[key] = pick;
+    return pick;
+}
+
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
     if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
     fgpu_space* V = A->space;
@@ -409,6 +494,8 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
     const int64_t nt = V->mesh->nt;
     const int rec = f->kind == FGPU_FORM_ELASTICITY ? 16 : 8;
+    if (A->coef_cap < nt * rec && ctx->capturing)
+        return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: assemble once before capturing (record buffer)");
     if (A->coef_cap < nt * rec) {
         cudaFree(A->d_coef);
         A->d_coef = nullptr;
@@ -420,12 +507,20 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     int rc = FGPU_OK;
     if (f->kind == FGPU_FORM_LAPLACE_MASS && !(f->algo == FGPU_ALGO_GATHER_NATIVE_F64 && A->precision == FGPU_F64)) {
         // FP64 matrices: df64 arithmetic on the FP32 pipes; FP32 matrices: binary32
-        rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef));
+        rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef), f->kappa_scale);
         if (rc) return rc;
-        rc = launch_assemble_gather_df(ctx, A, tab, reinterpret_cast<const float4*>(A->d_coef), accumulate);
+        const float4* recs = reinterpret_cast<const float4*>(A->d_coef);
+        int algo = f->algo;
+        if (algo == FGPU_ALGO_AUTO) {
+            algo = tuned_assembly_algo(ctx, A, tab, recs);
+            if (algo < 0) return -algo;
+        }
+        rc = algo == FGPU_ALGO_TWO_PHASE ? launch_assemble_two_phase(ctx, A, tab, recs, accumulate)
+                                         : launch_assemble_gather_df(ctx, A, tab, recs, accumulate);
         if (rc) return rc;
         return finish(ctx);
     }
+    if (f->kappa_scale) return set_err(ctx, FGPU_ERR_INVALID, "kappa_scale: Laplace/mass forms on the default path only");
     rc = launch_geometry(ctx, V->mesh, f->kind, d_kappa, f->kappa, f->mass, f->lambda, f->mu, A->d_coef);
     if (rc) return rc;
     if (f->kind == FGPU_FORM_LAPLACE_MASS) {
@@ -442,6 +537,7 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
 int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, int accumulate) {
     if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
     if (!f->kappa_elem) return assemble_impl(ctx, A, f, nullptr, accumulate);
+    FGPU_NO_CAPTURE(ctx, "assemble_matrix with host kappa (use fgpu_assemble_matrix_dev)");
     const int64_t nt = A->space->mesh->nt;
     double* dk = nullptr;
     int rc = dev_alloc(ctx, &dk, nt);
@@ -458,6 +554,7 @@ int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc
 
 // ---------------------------------------------------------------------------
 int fgpu_vector_create(fgpu_ctx* ctx, int64_t n, fgpu_vector** out) {
+    FGPU_NO_CAPTURE(ctx, "vector_create");
     if (!ctx || !out || n < 0) return set_err(ctx, FGPU_ERR_INVALID, "vector_create: bad arguments");
     fgpu_vector* v = new (std::nothrow) fgpu_vector();
     if (!v) return FGPU_ERR_ALLOC;
@@ -475,6 +572,7 @@ int fgpu_vector_upload(fgpu_vector* v, const double* host) {
     return FGPU_OK;
 }
 int fgpu_vector_download(const fgpu_vector* v, double* host) {
+    if (v) FGPU_NO_CAPTURE(v->ctx, "vector_download");
     if (!v || !host) return FGPU_ERR_INVALID;
     FGPU_CUDA_CHECK(v->ctx, cudaMemcpyAsync(host, v->d, v->n * sizeof(double), cudaMemcpyDeviceToHost, v->ctx->stream));
     FGPU_CUDA_CHECK(v->ctx, cudaStreamSynchronize(v->ctx->stream));
@@ -498,6 +596,7 @@ int fgpu_vector_destroy(fgpu_vector* v) {
 }
 
 int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, fgpu_vector* out, int accumulate) {
+    FGPU_NO_CAPTURE(ctx, "assemble_vector");
     if (!ctx || !V || !rhs || !out || out->n != V->ndof) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad arguments");
     const int qdeg = form_qdeg(V, rhs->quad_degree);
     std::string err;
@@ -514,6 +613,7 @@ int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc
 
 int fgpu_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, fgpu_vector* rhs, int64_t ndofs, const int32_t* dofs,
                    const double* values, int mode, double diag) {
+    FGPU_NO_CAPTURE(ctx, "dirichlet (use fgpu_bc_apply)");
     if (!ctx || !A || (ndofs > 0 && !dofs)) return set_err(ctx, FGPU_ERR_INVALID, "dirichlet: bad arguments");
     if (mode < 0 || mode > 2) return set_err(ctx, FGPU_ERR_INVALID, "dirichlet: bad mode");
     if (rhs && rhs->n != A->nrows) return set_err(ctx, FGPU_ERR_INVALID, "dirichlet: rhs size");
@@ -550,6 +650,7 @@ int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, c
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
     if (!ctx || !A || !b || !x || !cfg || b->n != A->nrows || x->n != A->nrows)
         return set_err(ctx, FGPU_ERR_INVALID, "solve_cg: bad arguments");
+    FGPU_NO_CAPTURE(ctx, "solve_cg");
     int rc = finish(ctx);
     if (rc) return rc;
     if (!cfg->mixed) return solve_pcg(ctx, A, b->d, x->d, cfg, stats);
@@ -567,6 +668,119 @@ int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, c
     if (tmp) fgpu_matrix_destroy(tmp);
     int rc2 = finish(ctx);
     return rc ? rc : rc2;
+}
+
+// ---------------------------------------------------------------------------
+int fgpu_bc_create(fgpu_ctx* ctx, int64_t n, int64_t ndofs, const int32_t* dofs, const double* values, fgpu_bc** out) {
+    if (!ctx || !out || n <= 0 || ndofs < 0 || (ndofs > 0 && !dofs)) return set_err(ctx, FGPU_ERR_INVALID, "bc_create: bad arguments");
+    FGPU_NO_CAPTURE(ctx, "bc_create");
+    *out = nullptr;
+    std::vector<uint8_t> mask(n, 0);
+    std::vector<double> g;
+    if (values) g.assign(n, 0.0);
+    for (int64_t k = 0; k < ndofs; ++k) {
+        if (dofs[k] < 0 || dofs[k] >= n) return set_err(ctx, FGPU_ERR_OUT_OF_RANGE, "bc_create: dof out of range");
+        mask[dofs[k]] = 1;
+        if (values) g[dofs[k]] = values[k];
+    }
+    fgpu_bc* bc = new (std::nothrow) fgpu_bc();
+    if (!bc) return FGPU_ERR_ALLOC;
+    bc->ctx = ctx;
+    bc->n = n;
+    int rc = dev_alloc(ctx, &bc->d_mask, n);
+    if (!rc && values) rc = dev_alloc(ctx, &bc->d_g, n);
+    if (rc) { fgpu_bc_destroy(bc); return rc; }
+    cudaMemcpy(bc->d_mask, mask.data(), n, cudaMemcpyHostToDevice);
+    if (values) cudaMemcpy(bc->d_g, g.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    *out = bc;
+    return FGPU_OK;
+}
+
+int fgpu_bc_apply(fgpu_ctx* ctx, const fgpu_bc* bc, fgpu_matrix* A, fgpu_vector* rhs, int mode, double diag) {
+    if (!ctx || !bc || !A || bc->n != A->nrows || (rhs && rhs->n != A->nrows)) return set_err(ctx, FGPU_ERR_INVALID, "bc_apply: bad arguments");
+    if (mode < 0 || mode > 2) return set_err(ctx, FGPU_ERR_INVALID, "bc_apply: bad mode");
+    int rc = launch_dirichlet(ctx, A, rhs ? rhs->d : nullptr, bc->d_mask, bc->d_g, mode, diag);
+    if (rc) return rc;
+    return finish(ctx);
+}
+
+int fgpu_bc_destroy(fgpu_bc* bc) {
+    if (!bc) return FGPU_OK;
+    cudaFree(bc->d_mask);
+    cudaFree(bc->d_g);
+    delete bc;
+    return FGPU_OK;
+}
+
+int fgpu_vector_axpby(fgpu_ctx* ctx, double a, const fgpu_vector* x, double b, fgpu_vector* y) {
+    if (!ctx || !x || !y || x->n != y->n) return set_err(ctx, FGPU_ERR_INVALID, "vector_axpby: bad arguments");
+    int rc = launch_axpby(ctx, y->n, a, x->d, b, y->d);
+    if (rc) return rc;
+    return finish(ctx);
+}
+
+int fgpu_vector_copy(fgpu_ctx* ctx, const fgpu_vector* src, fgpu_vector* dst) {
+    if (!ctx || !src || !dst || src->n != dst->n) return set_err(ctx, FGPU_ERR_INVALID, "vector_copy: bad arguments");
+    FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(dst->d, src->d, src->n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    return finish(ctx);
+}
+
+// ---------------------------------------------------------------------------
+int fgpu_graph_begin(fgpu_ctx* ctx) {
+    if (!ctx) return FGPU_ERR_INVALID;
+    if (ctx->capturing) return set_err(ctx, FGPU_ERR_INVALID, "graph_begin: already capturing");
+    int rc = finish(ctx);          // drain pending work and profiling events first
+    if (rc) return rc;
+    FGPU_CUDA_CHECK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = 1;
+    ctx->capture_launches0 = ctx->launches;
+    return FGPU_OK;
+}
+
+int fgpu_graph_end(fgpu_ctx* ctx, fgpu_graph** out) {
+    if (!ctx || !out) return FGPU_ERR_INVALID;
+    if (!ctx->capturing) return set_err(ctx, FGPU_ERR_INVALID, "graph_end: not capturing");
+    *out = nullptr;
+    ctx->capturing = 0;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    const int64_t nl = ctx->launches - ctx->capture_launches0;
+    ctx->launches = ctx->capture_launches0;
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return set_err(ctx, FGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    fgpu_graph* g = new (std::nothrow) fgpu_graph();
+    if (!g) { cudaGraphDestroy(graph); return FGPU_ERR_ALLOC; }
+    g->ctx = ctx;
+    g->graph = graph;
+    g->launches = nl;
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (e != cudaSuccess) {
+        fgpu_graph_destroy(g);
+        return set_err(ctx, FGPU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    *out = g;
+    return FGPU_OK;
+}
+
+int fgpu_graph_launch(fgpu_ctx* ctx, fgpu_graph* g, int count) {
+    if (!ctx || !g || g->ctx != ctx || count < 0) return set_err(ctx, FGPU_ERR_INVALID, "graph_launch: bad arguments");
+    FGPU_NO_CAPTURE(ctx, "graph_launch");
+    for (int k = 0; k < count; ++k) {
+        FGPU_CUDA_CHECK(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+        ctx->launches += g->launches;
+    }
+    return finish(ctx);
+}
+
+int fgpu_graph_destroy(fgpu_graph* g) {
+    if (!g) return FGPU_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return FGPU_OK;
 }
 
 int fgpu_host_dof_table(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int32_t* l2g,
@@ -647,6 +861,7 @@ int fgpu_host_df64_ops(int op, int64_t n, const double* a, const double* b, doub
 }
 
 int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, int quad_degree, double* l2, double* h1) {
+    FGPU_NO_CAPTURE(ctx, "norms_sine");
     if (!ctx || !V || !u || !l2 || !h1 || u->n != V->ndof || V->ncomp != 1) return set_err(ctx, FGPU_ERR_INVALID, "norms: bad arguments");
     std::string err;
     DevTables* tab = get_dev_tables(V->order, quad_degree > 0 ? quad_degree : 2 * V->order, err);
@@ -658,6 +873,7 @@ int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, in
 
 int fgpu_prof_reset(fgpu_ctx* ctx) {
     if (!ctx) return FGPU_ERR_INVALID;
+    FGPU_NO_CAPTURE(ctx, "prof_reset");
     finish(ctx);
     ctx->prof.clear();
     return FGPU_OK;
@@ -665,6 +881,7 @@ int fgpu_prof_reset(fgpu_ctx* ctx) {
 
 int fgpu_prof_get(fgpu_ctx* ctx, const char* name, int64_t* count, double* total_ms) {
     if (!ctx || !name) return FGPU_ERR_INVALID;
+    FGPU_NO_CAPTURE(ctx, "prof_get");
     int rc = finish(ctx);
     if (rc) return rc;
     auto it = ctx->prof.find(name);

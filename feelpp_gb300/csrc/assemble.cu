@@ -59,7 +59,21 @@ DevTables* get_dev_tables(int order, int qdeg, std::string& err) {
         T7h[k] = (float)R.T7[k];
         T7l[k] = (float)(R.T7[k] - (double)T7h[k]);
     }
+    const int n = R.n, ntri = n * (n + 1) / 2;
+    std::vector<float> T7th((size_t)7 * ntri), T7tl((size_t)7 * ntri);
+    std::vector<uint16_t> tri((size_t)n * n);
+    for (int i = 0, t = 0; i < n; ++i)
+        for (int j = i; j < n; ++j, ++t) {
+            tri[(size_t)i * n + j] = tri[(size_t)j * n + i] = (uint16_t)t;
+            for (int k = 0; k < 7; ++k) {
+                T7th[(size_t)k * ntri + t] = T7h[((size_t)k * n + i) * n + j];
+                T7tl[(size_t)k * ntri + t] = T7l[((size_t)k * n + i) * n + j];
+            }
+        }
     cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(T7th, &D->d_T7th);
+    if (e == cudaSuccess) e = upload(T7tl, &D->d_T7tl);
+    if (e == cudaSuccess) e = upload(tri, &D->d_tri);
     if (e == cudaSuccess) e = upload(T7h, &D->d_T7h);
     if (e == cudaSuccess) e = upload(T7l, &D->d_T7l);
     if (e == cudaSuccess) e = upload(R.T7, &D->d_T7);
@@ -84,7 +98,7 @@ DevTables* get_dev_tables(int order, int qdeg, std::string& err) {
 // ---------------------------------------------------------------------------
 void prof_begin(fgpu_ctx* ctx, const char* name, PendingEvent& ev) {
     ++ctx->launches;
-    if (!ctx->profile) return;
+    if (!ctx->profile || ctx->capturing) return;
     ev.name = name;
     if (ctx->event_pool.size() >= 2) {
         ev.start = ctx->event_pool.back(); ctx->event_pool.pop_back();
@@ -97,7 +111,7 @@ void prof_begin(fgpu_ctx* ctx, const char* name, PendingEvent& ev) {
 }
 
 void prof_end(fgpu_ctx* ctx, PendingEvent& ev) {
-    if (!ctx->profile) return;
+    if (!ctx->profile || ctx->capturing) return;
     cudaEventRecord(ev.stop, ctx->stream);
     ctx->pending.push_back(ev);
 }
@@ -672,61 +686,70 @@ namespace fgpu {
 // with c_0..5 = kappa * (C^T C)_{00,11,22,01,02,12} / |det K| (= kappa J B^T B, C the
 // cofactor matrix of K, B = C / det K), c_6 = mass * |det K|, J = |det K|.
 // K's entries are formed in FP64 (9 subtractions of vertex coordinates), the rest
-// in df64 (geomap.hpp:1971-1991, 2310-2350).
+// in df64 (geomap.hpp:1971-1991, 2310-2350). ksc: an extra factor of kappa
+// (a time-dependent coefficient read from device memory).
+__device__ __forceinline__ void geometry_df_element(int64_t e, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                                    const double* __restrict__ kappa, df kc, df mc, df ksc,
+                                                    float4* __restrict__ rec, int* __restrict__ status) {
+    int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
+    const double* X0 = xyz + 3 * (int64_t)t.x;
+    const double* Xv[3] = {xyz + 3 * (int64_t)t.y, xyz + 3 * (int64_t)t.z, xyz + 3 * (int64_t)t.w};
+    df K[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) K[r * 3 + c] = df_scale(d2df(Xv[c][r] - X0[r]), 0.5f);
+    df C[9];
+    C[0] = df_sub(df_mul(K[4], K[8]), df_mul(K[5], K[7]));
+    C[1] = df_sub(df_mul(K[5], K[6]), df_mul(K[3], K[8]));
+    C[2] = df_sub(df_mul(K[3], K[7]), df_mul(K[4], K[6]));
+    C[3] = df_sub(df_mul(K[2], K[7]), df_mul(K[1], K[8]));
+    C[4] = df_sub(df_mul(K[0], K[8]), df_mul(K[2], K[6]));
+    C[5] = df_sub(df_mul(K[1], K[6]), df_mul(K[0], K[7]));
+    C[6] = df_sub(df_mul(K[1], K[5]), df_mul(K[2], K[4]));
+    C[7] = df_sub(df_mul(K[2], K[3]), df_mul(K[0], K[5]));
+    C[8] = df_sub(df_mul(K[0], K[4]), df_mul(K[1], K[3]));
+    df det = df_add(df_add(df_mul(K[0], C[0]), df_mul(K[1], C[1])), df_mul(K[2], C[2]));
+    df J = det.hi < 0.0f ? df_neg(det) : det;
+    if (!(J.hi > 0.0f) || !isfinite(J.hi)) atomicOr(status, kStatusBadElement);
+    df inv = df_recip(J);
+    df s = df_mul(df_mul(kappa ? d2df(kappa[e]) : kc, ksc), inv);
+    const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+    df c[8];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        df g = df_add(df_add(df_mul(C[pa[k]], C[pb[k]]), df_mul(C[3 + pa[k]], C[3 + pb[k]])), df_mul(C[6 + pa[k]], C[6 + pb[k]]));
+        c[k] = df_mul(s, g);
+    }
+    c[6] = df_mul(mc, J);
+    c[7] = J;
+    float4* o = rec + 4 * e;
+    o[0] = make_float4(c[0].hi, c[1].hi, c[2].hi, c[3].hi);
+    o[1] = make_float4(c[4].hi, c[5].hi, c[6].hi, c[7].hi);
+    o[2] = make_float4(c[0].lo, c[1].lo, c[2].lo, c[3].lo);
+    o[3] = make_float4(c[4].lo, c[5].lo, c[6].lo, c[7].lo);
+}
+
+// kscale (device scalar or null): time-dependent factor of the stiffness
+// coefficient, read at run time so that captured graphs see its new value.
 __global__ void geometry_df_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
-                                   const double* __restrict__ kappa, double kappa_c, double mass,
+                                   const double* __restrict__ kappa, double kappa_c, double mass, const double* __restrict__ kscale,
                                    float4* __restrict__ rec, int* __restrict__ status) {
     const df kc = d2df(kappa_c), mc = d2df(mass);
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
-        int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
-        const double* X0 = xyz + 3 * (int64_t)t.x;
-        const double* Xv[3] = {xyz + 3 * (int64_t)t.y, xyz + 3 * (int64_t)t.z, xyz + 3 * (int64_t)t.w};
-        df K[9];
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int r = 0; r < 3; ++r) K[r * 3 + c] = df_scale(d2df(Xv[c][r] - X0[r]), 0.5f);
-        df C[9];
-        C[0] = df_sub(df_mul(K[4], K[8]), df_mul(K[5], K[7]));
-        C[1] = df_sub(df_mul(K[5], K[6]), df_mul(K[3], K[8]));
-        C[2] = df_sub(df_mul(K[3], K[7]), df_mul(K[4], K[6]));
-        C[3] = df_sub(df_mul(K[2], K[7]), df_mul(K[1], K[8]));
-        C[4] = df_sub(df_mul(K[0], K[8]), df_mul(K[2], K[6]));
-        C[5] = df_sub(df_mul(K[1], K[6]), df_mul(K[0], K[7]));
-        C[6] = df_sub(df_mul(K[1], K[5]), df_mul(K[2], K[4]));
-        C[7] = df_sub(df_mul(K[2], K[3]), df_mul(K[0], K[5]));
-        C[8] = df_sub(df_mul(K[0], K[4]), df_mul(K[1], K[3]));
-        df det = df_add(df_add(df_mul(K[0], C[0]), df_mul(K[1], C[1])), df_mul(K[2], C[2]));
-        df J = det.hi < 0.0f ? df_neg(det) : det;
-        if (!(J.hi > 0.0f) || !isfinite(J.hi)) atomicOr(status, kStatusBadElement);
-        df inv = df_recip(J);
-        df s = df_mul(kappa ? d2df(kappa[e]) : kc, inv);
-        const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
-        df c[8];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            df g = df_add(df_add(df_mul(C[pa[k]], C[pb[k]]), df_mul(C[3 + pa[k]], C[3 + pb[k]])), df_mul(C[6 + pa[k]], C[6 + pb[k]]));
-            c[k] = df_mul(s, g);
-        }
-        c[6] = df_mul(mc, J);
-        c[7] = J;
-        float4* o = rec + 4 * e;
-        o[0] = make_float4(c[0].hi, c[1].hi, c[2].hi, c[3].hi);
-        o[1] = make_float4(c[4].hi, c[5].hi, c[6].hi, c[7].hi);
-        o[2] = make_float4(c[0].lo, c[1].lo, c[2].lo, c[3].lo);
-        o[3] = make_float4(c[4].lo, c[5].lo, c[6].lo, c[7].lo);
-    }
+    const df ksc = kscale ? d2df(*kscale) : df{1.0f, 0.0f};
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x)
+        geometry_df_element(e, xyz, tets, kappa, kc, mc, ksc, rec, status);
 }
 
 int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
-                       float4* d_rec) {
+                       float4* d_rec, const double* d_kscale) {
     int threads = 256;
     int64_t blocks = std::min<int64_t>((mesh->nt + threads - 1) / threads, 152 * 16);
     if (blocks < 1) blocks = 1;
     PendingEvent ev;
     prof_begin(ctx, "geometry", ev);
     geometry_df_kernel<<<(int)blocks, threads, 0, ctx->stream>>>(mesh->nt, mesh->d_xyz, mesh->d_tets, d_kappa, kappa, mass,
-                                                               d_rec, ctx->d_status);
+                                                               d_kscale, d_rec, ctx->d_status);
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
@@ -783,6 +806,149 @@ int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V) {
 //         TwoSum on binary32), accumulation in df64, output converted to binary64
 //         with integer operations.
 //   F32 : binary32 coefficients, tables and accumulation.
+// Element-matrix entry K_e(i, j) = sum_k c_k T_k(i, j) (the 7 reference tensors
+// of the affine Laplace/mass form) from the element's coefficient record.
+// df64: each product c_k T_k is formed exactly (TwoProduct by FMA, plus the
+// cross terms of the lo parts) and summed with TwoSum; binary32: an FMA chain.
+// (tables Th/Tl of 7 slices of `stride` floats; tix = the entry's index in a slice)
+__device__ __forceinline__ df record_entry_df(const float4* __restrict__ rp, const float* __restrict__ Th,
+                                              const float* __restrict__ Tl, int stride, int tix) {
+    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1), l0 = __ldg(rp + 2), l1 = __ldg(rp + 3);
+    const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+    const float cl[7] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z};
+    float s = 0.0f, err = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        const float th = Th[k * stride + tix], tl = Tl[k * stride + tix];
+        const float p = f_mul(ch[k], th);
+        const float pe = f_fma(ch[k], th, -p);
+        err = f_fma(ch[k], tl, err);
+        err = f_fma(cl[k], th, err);
+        err = f_add(err, pe);
+        if (k == 0) {
+            s = p;
+        } else {
+            df t = two_sum(s, p);
+            s = t.hi;
+            err = f_add(err, t.lo);
+        }
+    }
+    return quick_two_sum(s, err);
+}
+__device__ __forceinline__ float record_entry_f(const float4* __restrict__ rp, const float* __restrict__ Th, int stride, int tix) {
+    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1);
+    const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+    float v = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], Th[k * stride + tix], v);
+    return v;
+}
+
+template <int N>
+struct RecordSource {
+    const float4* __restrict__ rec;
+    const float* __restrict__ Th;     // 7 N N (shared memory)
+    const float* __restrict__ Tl;
+    __device__ __forceinline__ df value_df(int64_t e, int li, int j) const {
+        return record_entry_df(rec + 4 * e, Th, Tl, N * N, li * N + j);
+    }
+    __device__ __forceinline__ float value_f(int64_t e, int li, int j) const {
+        return record_entry_f(rec + 4 * e, Th, N * N, li * N + j);
+    }
+};
+
+// Entries read back from a buffer of element matrices (upper triangles,
+// NTRI = N (N + 1) / 2 per element; tri maps (i, j) to the stored index of
+// (min, max)). The stored values are RecordSource's, so both sources give the
+// same bits.
+template <int N>
+struct BufferSource {
+    static constexpr int NTRI = N * (N + 1) / 2;
+    const void* __restrict__ kbuf;
+    const uint16_t* __restrict__ tri;  // N N (shared memory)
+    __device__ __forceinline__ df value_df(int64_t e, int li, int j) const {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(kbuf) + e * NTRI + tri[li * N + j]);
+        return df{v.x, v.y};
+    }
+    __device__ __forceinline__ float value_f(int64_t e, int li, int j) const {
+        return __ldg(reinterpret_cast<const float*>(kbuf) + e * NTRI + tri[li * N + j]);
+    }
+};
+
+// One pattern row r assembled by one warp: the row's incident elements are
+// taken EPB at a time (lane = slot * N + j evaluates entry (li, j) of element
+// slot), each slot accumulates into its own copy of the row in shared memory
+// (acc: EPB copies with stride maxrow), and the copies are summed in slot order
+// at the end, so the result does not depend on scheduling. acc is all zero on
+// entry and on exit.
+template <int MODE, int N, int EPB, class Src>
+__device__ __forceinline__ void gather_row(int64_t r, const int64_t* __restrict__ sia, const int64_t* __restrict__ inc_ptr,
+                                           const int32_t* __restrict__ inc, const uint8_t* __restrict__ posg, const Src& src,
+                                           int maxrow, void* __restrict__ valv, int accumulate, int* __restrict__ status,
+                                           float* __restrict__ acc, int lane) {
+    constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;   // floats per accumulator entry
+    const int slot = lane / N, j = lane - slot * N;
+    const bool lane_used = lane < EPB * N;
+    float* myacc = acc + (size_t)(slot < EPB ? slot : 0) * maxrow * ACCW;
+    const int64_t start = sia[r];
+    const int len = (int)(sia[r + 1] - start);
+    const int64_t tb = inc_ptr[r], te = inc_ptr[r + 1];
+    if (len > maxrow) {
+        if (lane == 0) atomicOr(status, kStatusRowOverflow);
+        return;
+    }
+    for (int64_t c0 = tb; c0 < te; c0 += 32) {
+        const int nin = (int)min((int64_t)32, te - c0);
+        const int32_t mycode = lane < nin ? inc[c0 + lane] : 0;
+        for (int b = 0; b < nin; b += EPB) {
+            const int idx = b + slot;
+            const int32_t code = __shfl_sync(0xffffffffu, mycode, idx < 32 ? idx : 31);
+            if (lane_used && idx < nin) {
+                const int64_t e = code >> 5;
+                const int li = code & 31;
+                const int pos = posg[e * (N * N) + li * N + j];
+                if (MODE == kModeDF64) {
+                    df a = df_add(df{myacc[2 * pos], myacc[2 * pos + 1]}, src.value_df(e, li, j));
+                    myacc[2 * pos] = a.hi;
+                    myacc[2 * pos + 1] = a.lo;
+                } else {
+                    myacc[pos] = f_add(myacc[pos], src.value_f(e, li, j));
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // write the row: sum the slot copies in slot order (+ the old value for '+='), reset them
+    for (int k = lane; k < len; k += 32) {
+        if (MODE == kModeDF64) {
+            df a{acc[2 * k], acc[2 * k + 1]};
+            acc[2 * k] = 0.0f;
+            acc[2 * k + 1] = 0.0f;
+#pragma unroll
+            for (int s = 1; s < EPB; ++s) {
+                float* q = acc + (size_t)s * maxrow * 2 + 2 * k;
+                a = df_add(a, df{q[0], q[1]});
+                q[0] = 0.0f;
+                q[1] = 0.0f;
+            }
+            double* out = reinterpret_cast<double*>(valv) + start + k;
+            if (accumulate) a = df_add(d2df(*out), a);
+            *out = df2d(a);
+        } else {
+            float a = acc[k];
+            acc[k] = 0.0f;
+#pragma unroll
+            for (int s = 1; s < EPB; ++s) {
+                a = f_add(a, acc[(size_t)s * maxrow + k]);
+                acc[(size_t)s * maxrow + k] = 0.0f;
+            }
+            float* out = reinterpret_cast<float*>(valv) + start + k;
+            *out = accumulate ? f_add(*out, a) : a;
+        }
+    }
+    __syncwarp();
+}
+
 template <int MODE, int N, int EPB>
 __global__ void __launch_bounds__(256) gather_row_kernel(
     int64_t nrows, const int64_t* __restrict__ sia, const int64_t* __restrict__ inc_ptr,
@@ -800,100 +966,15 @@ __global__ void __launch_bounds__(256) gather_row_kernel(
     const int tbytes = ((MODE == kModeDF64 ? 2 : 1) * NT * 4 + 15) & ~15;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
-    constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;   // floats per accumulator entry
+    constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;
     float* acc = reinterpret_cast<float*>(smem + tbytes) + (size_t)warp * EPB * maxrow * ACCW;
     __syncthreads();
-    const int slot = lane / N, j = lane - slot * N;
-    const bool lane_used = lane < EPB * N;
-    float* myacc = acc + (size_t)(slot < EPB ? slot : 0) * maxrow * ACCW;
-    // accumulators start at zero once; the write loop of each row resets what it read
+    // accumulators start at zero once; each row resets what it used
     for (int k = lane; k < EPB * maxrow * ACCW; k += 32) acc[k] = 0.0f;
     __syncwarp();
-    for (int64_t r = (int64_t)blockIdx.x * wpb + warp; r < nrows; r += (int64_t)gridDim.x * wpb) {
-        const int64_t start = sia[r];
-        const int len = (int)(sia[r + 1] - start);
-        const int64_t tb = inc_ptr[r], te = inc_ptr[r + 1];
-        if (len > maxrow) {
-            if (lane == 0) atomicOr(status, kStatusRowOverflow);
-            continue;
-        }
-        for (int64_t c0 = tb; c0 < te; c0 += 32) {
-            const int nin = (int)min((int64_t)32, te - c0);
-            const int32_t mycode = lane < nin ? inc[c0 + lane] : 0;
-            for (int b = 0; b < nin; b += EPB) {
-                const int idx = b + slot;
-                const int32_t code = __shfl_sync(0xffffffffu, mycode, idx < 32 ? idx : 31);
-                if (lane_used && idx < nin) {
-                    const int64_t e = code >> 5;
-                    const int li = code & 31;
-                    const float4* rp = rec + 4 * e;
-                    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1);
-                    const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
-                    const int tix = li * N + j;
-                    const int pos = posg[e * (N * N) + tix];
-                    if (MODE == kModeDF64) {
-                        const float4 l0 = __ldg(rp + 2), l1 = __ldg(rp + 3);
-                        const float cl[7] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z};
-                        float s = 0.0f, err = 0.0f;
-#pragma unroll
-                        for (int k = 0; k < 7; ++k) {
-                            const float th = Th[k * N * N + tix], tl = Tl[k * N * N + tix];
-                            const float p = f_mul(ch[k], th);
-                            const float pe = f_fma(ch[k], th, -p);
-                            err = f_fma(ch[k], tl, err);
-                            err = f_fma(cl[k], th, err);
-                            err = f_add(err, pe);
-                            if (k == 0) {
-                                s = p;
-                            } else {
-                                df t = two_sum(s, p);
-                                s = t.hi;
-                                err = f_add(err, t.lo);
-                            }
-                        }
-                        df a = df_add(df{myacc[2 * pos], myacc[2 * pos + 1]}, quick_two_sum(s, err));
-                        myacc[2 * pos] = a.hi;
-                        myacc[2 * pos + 1] = a.lo;
-                    } else {
-                        float v = 0.0f;
-#pragma unroll
-                        for (int k = 0; k < 7; ++k) v = fmaf(ch[k], Th[k * N * N + tix], v);
-                        myacc[pos] = f_add(myacc[pos], v);
-                    }
-                }
-                __syncwarp();
-            }
-        }
-        // write the row: sum the slot copies in slot order (+ the old value for '+='), reset them
-        for (int k = lane; k < len; k += 32) {
-            if (MODE == kModeDF64) {
-                df a{acc[2 * k], acc[2 * k + 1]};
-                acc[2 * k] = 0.0f;
-                acc[2 * k + 1] = 0.0f;
-#pragma unroll
-                for (int s = 1; s < EPB; ++s) {
-                    float* q = acc + (size_t)s * maxrow * 2 + 2 * k;
-                    a = df_add(a, df{q[0], q[1]});
-                    q[0] = 0.0f;
-                    q[1] = 0.0f;
-                }
-                double* out = reinterpret_cast<double*>(valv) + start + k;
-                if (accumulate) a = df_add(d2df(*out), a);
-                *out = df2d(a);
-            } else {
-                float a = acc[k];
-                acc[k] = 0.0f;
-#pragma unroll
-                for (int s = 1; s < EPB; ++s) {
-                    a = f_add(a, acc[(size_t)s * maxrow + k]);
-                    acc[(size_t)s * maxrow + k] = 0.0f;
-                }
-                float* out = reinterpret_cast<float*>(valv) + start + k;
-                *out = accumulate ? f_add(*out, a) : a;
-            }
-        }
-        __syncwarp();
-    }
+    for (int64_t r = (int64_t)blockIdx.x * wpb + warp; r < nrows; r += (int64_t)gridDim.x * wpb)
+        gather_row<MODE, N, EPB>(r, sia, inc_ptr, inc, posg, RecordSource<N>{rec, Th, Tl}, maxrow, valv, accumulate, status, acc,
+                                 lane);
 }
 
 template <int MODE, int N, int EPB>
@@ -923,6 +1004,289 @@ static int run_gather_row(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, c
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
+}
+
+__global__ void axpby_kernel(int64_t n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = a * x[i] + b * y[i];
+}
+
+int launch_axpby(fgpu_ctx* ctx, int64_t n, double a, const double* x, double b, double* y) {
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8));
+    axpby_kernel<<<(int)blocks, 256, 0, ctx->stream>>>(n, a, x, b, y);
+    ++ctx->launches;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched assembly: many independent problems (meshes, orders, kappas) in one
+// geometry launch and one persistent gather launch. Rows of all problems form
+// one global index space; warps take chunks of rows from a device work queue
+// (atomic counter), find the row's problem by binary search over the row
+// offsets, and run the same per-row body as the single-problem kernel, so a
+// batched matrix is bit-identical to the one assembled alone.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int batch_find(const int64_t* __restrict__ off, int nprob, int64_t g) {
+    int lo = 0, hi = nprob - 1;        // largest p with off[p] <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void batch_geometry_kernel(int nprob, const BatchProblem* __restrict__ probs, const int64_t* __restrict__ elem_off,
+                                      int64_t total, int* __restrict__ status) {
+    int p = -1;
+    int64_t pe0 = 0, pe1 = 0;
+    df kc{0.0f, 0.0f}, mc{0.0f, 0.0f};
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        if (g < pe0 || g >= pe1) {
+            p = batch_find(elem_off, nprob, g);
+            pe0 = elem_off[p];
+            pe1 = elem_off[p + 1];
+            kc = d2df(probs[p].kappa_c);
+            mc = d2df(probs[p].mass);
+        }
+        const BatchProblem& P = probs[p];
+        geometry_df_element(g - pe0, P.xyz, P.tets, P.kappa, kc, mc, df{1.0f, 0.0f}, P.rec, status);
+    }
+}
+
+// table offsets (floats) of orders 1..3 inside the shared table block: 7 n^2 each
+__host__ __device__ constexpr int batch_tab_off(int order) { return order == 1 ? 0 : order == 2 ? 7 * 16 : 7 * 16 + 7 * 100; }
+constexpr int kBatchTabFloats = 7 * 16 + 7 * 100 + 7 * 400;
+
+template <int MODE>
+__global__ void __launch_bounds__(256) batch_gather_kernel(int nprob, const BatchProblem* __restrict__ probs,
+                                                           const int64_t* __restrict__ row_off, int64_t total,
+                                                           const float* __restrict__ Thg, const float* __restrict__ Tlg,
+                                                           int acc_floats, unsigned long long* __restrict__ counter, int chunk,
+                                                           int accumulate, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* Th = reinterpret_cast<float*>(smem);
+    float* Tl = Th + kBatchTabFloats;
+    for (int k = threadIdx.x; k < kBatchTabFloats; k += blockDim.x) {
+        Th[k] = Thg[k];
+        if (MODE == kModeDF64) Tl[k] = Tlg[k];
+    }
+    const int tfloats = ((MODE == kModeDF64 ? 2 : 1) * kBatchTabFloats + 3) & ~3;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* acc = reinterpret_cast<float*>(smem) + tfloats + (size_t)warp * acc_floats;
+    __syncthreads();
+    for (int k = lane; k < acc_floats; k += 32) acc[k] = 0.0f;
+    __syncwarp();
+    int p = -1;
+    int64_t pr0 = 0, pr1 = 0;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if ((int64_t)base >= total) break;
+        const int64_t end = min((int64_t)base + chunk, total);
+        for (int64_t g = (int64_t)base; g < end; ++g) {
+            if (g < pr0 || g >= pr1) {
+                p = batch_find(row_off, nprob, g);
+                pr0 = row_off[p];
+                pr1 = row_off[p + 1];
+            }
+            const BatchProblem& P = probs[p];
+            const int64_t r = g - pr0;
+            switch (P.order) {
+                case 1:
+                    gather_row<MODE, 4, 8>(r, P.sia, P.inc_ptr, P.inc, P.pos,
+                                           RecordSource<4>{P.rec, Th + batch_tab_off(1), Tl + batch_tab_off(1)},
+                                           P.maxrow, P.val, accumulate, status, acc, lane);
+                    break;
+                case 2:
+                    gather_row<MODE, 10, 3>(r, P.sia, P.inc_ptr, P.inc, P.pos,
+                                           RecordSource<10>{P.rec, Th + batch_tab_off(2), Tl + batch_tab_off(2)},
+                                            P.maxrow, P.val, accumulate, status, acc, lane);
+                    break;
+                default:
+                    gather_row<MODE, 20, 1>(r, P.sia, P.inc_ptr, P.inc, P.pos,
+                                           RecordSource<20>{P.rec, Th + batch_tab_off(3), Tl + batch_tab_off(3)},
+                                            P.maxrow, P.val, accumulate, status, acc, lane);
+                    break;
+            }
+        }
+    }
+}
+
+int launch_batch_geometry(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off, int64_t total_elems) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((total_elems + 255) / 256, (int64_t)sms * 16));
+    PendingEvent ev;
+    prof_begin(ctx, "batch_geometry", ev);
+    batch_geometry_kernel<<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_elem_off, total_elems, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// shared tables of orders 1..3 (hi, lo) for the batch kernel, per device
+static std::mutex g_btab_mutex;
+static std::map<int, std::pair<float*, float*>> g_btabs;
+static int batch_tables(fgpu_ctx* ctx, float** h, float** l) {
+    std::lock_guard<std::mutex> lock(g_btab_mutex);
+    auto it = g_btabs.find(ctx->device);
+    if (it != g_btabs.end()) { *h = it->second.first; *l = it->second.second; return FGPU_OK; }
+    float *dh = nullptr, *dl = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&dh, kBatchTabFloats * sizeof(float)));
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&dl, kBatchTabFloats * sizeof(float)));
+    for (int order = 1; order <= 3; ++order) {
+        std::string err;
+        DevTables* t = get_dev_tables(order, 2 * order, err);
+        if (!t) { ctx->err = err; return FGPU_ERR_INVALID; }
+        const size_t nb = (size_t)7 * t->n * t->n * sizeof(float);
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(dh + batch_tab_off(order), t->d_T7h, nb, cudaMemcpyDeviceToDevice));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(dl + batch_tab_off(order), t->d_T7l, nb, cudaMemcpyDeviceToDevice));
+    }
+    g_btabs[ctx->device] = {dh, dl};
+    *h = dh;
+    *l = dl;
+    return FGPU_OK;
+}
+
+int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_row_off, int64_t total_rows,
+                        int f32, int acc_floats, unsigned long long* d_counter, const BatchLaunch& cfg, int accumulate) {
+    float *Th = nullptr, *Tl = nullptr;
+    int rc = batch_tables(ctx, &Th, &Tl);
+    if (rc) return rc;
+    const int threads = cfg.threads, wpb = threads / 32;
+    const size_t tfloats = ((f32 ? 1 : 2) * kBatchTabFloats + 3) & ~3;
+    const size_t smem = (tfloats + (size_t)wpb * acc_floats) * sizeof(float);
+    auto kern = f32 ? batch_gather_kernel<kModeF32> : batch_gather_kernel<kModeDF64>;
+    if (smem > 227 * 1024) { ctx->err = "batch: staging buffers exceed shared memory"; return FGPU_ERR_INVALID; }
+    FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int blocks = std::max(1, std::max(per_sm, 1) * sms);
+    FGPU_CUDA_CHECK(ctx, cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), ctx->stream));
+    PendingEvent ev;
+    prof_begin(ctx, "batch_gather", ev);
+    kern<<<blocks, threads, smem, ctx->stream>>>(nprob, d_probs, d_row_off, total_rows, Th, Tl, acc_floats, d_counter, cfg.chunk,
+                                                 accumulate, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Two-phase assembly. Phase 1 (element_tri_kernel): one thread per (element,
+// upper-triangle entry) computes K_e(i, j), i <= j, from the record; writes are
+// contiguous. Phase 2 (gather_buf_kernel): the row-owner gather of
+// gather_row_kernel reading the entries back instead of recomputing them, so
+// each entry is computed once instead of twice (once per row it belongs to)
+// and the gather becomes a streaming pass.
+// ---------------------------------------------------------------------------
+template <int MODE, int N>
+__global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const float4* __restrict__ rec,
+                                                          const float* __restrict__ Thg, const float* __restrict__ Tlg,
+                                                          void* __restrict__ kbuf) {
+    constexpr int NTRI = N * (N + 1) / 2;
+    __shared__ float Th[7 * NTRI];
+    __shared__ float Tl[MODE == kModeDF64 ? 7 * NTRI : 1];
+    for (int k = threadIdx.x; k < 7 * NTRI; k += blockDim.x) {
+        Th[k] = Thg[k];
+        if (MODE == kModeDF64) Tl[k] = Tlg[k];
+    }
+    __syncthreads();
+    const int64_t total = nt * NTRI;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = g / NTRI;
+        const int t = (int)(g - e * NTRI);
+        if (MODE == kModeDF64) {
+            const df v = record_entry_df(rec + 4 * e, Th, Tl, NTRI, t);
+            reinterpret_cast<float2*>(kbuf)[g] = make_float2(v.hi, v.lo);
+        } else {
+            reinterpret_cast<float*>(kbuf)[g] = record_entry_f(rec + 4 * e, Th, NTRI, t);
+        }
+    }
+}
+
+template <int MODE, int N, int EPB>
+__global__ void __launch_bounds__(256) gather_buf_kernel(
+    int64_t nrows, const int64_t* __restrict__ sia, const int64_t* __restrict__ inc_ptr,
+    const int32_t* __restrict__ inc, const uint8_t* __restrict__ posg, const void* __restrict__ kbuf,
+    const uint16_t* __restrict__ trig, int maxrow, void* __restrict__ valv, int accumulate, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint16_t* tri = reinterpret_cast<uint16_t*>(smem);
+    for (int k = threadIdx.x; k < N * N; k += blockDim.x) tri[k] = trig[k];
+    const int tbytes = (N * N * 2 + 15) & ~15;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;
+    float* acc = reinterpret_cast<float*>(smem + tbytes) + (size_t)warp * EPB * maxrow * ACCW;
+    __syncthreads();
+    for (int k = lane; k < EPB * maxrow * ACCW; k += 32) acc[k] = 0.0f;
+    __syncwarp();
+    const BufferSource<N> src{kbuf, tri};
+    for (int64_t r = (int64_t)blockIdx.x * wpb + warp; r < nrows; r += (int64_t)gridDim.x * wpb)
+        gather_row<MODE, N, EPB>(r, sia, inc_ptr, inc, posg, src, maxrow, valv, accumulate, status, acc, lane);
+}
+
+template <int MODE, int N, int EPB>
+static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+    const DevPattern& P = *A->pattern;
+    const fgpu_space* V = A->space;
+    const int64_t nt = V->mesh->nt;
+    constexpr int NTRI = N * (N + 1) / 2;
+    const size_t need = (size_t)nt * NTRI * (MODE == kModeDF64 ? 8 : 4);
+    if (A->kbuf_bytes < need) {
+        if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (element buffer)"; return FGPU_ERR_INVALID; }
+        cudaFree(A->d_kbuf);
+        A->d_kbuf = nullptr;
+        A->kbuf_bytes = 0;
+        if (cudaMalloc(&A->d_kbuf, need) != cudaSuccess) { cudaGetLastError(); ctx->err = "two-phase assembly: element buffer allocation failed"; return FGPU_ERR_ALLOC; }
+        A->kbuf_bytes = need;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    {
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nt * NTRI + 255) / 256, (int64_t)sms * 16));
+        PendingEvent ev;
+        prof_begin(ctx, "assemble_elements", ev);
+        element_tri_kernel<MODE, N><<<(int)blocks, 256, 0, ctx->stream>>>(nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
+        prof_end(ctx, ev);
+        FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    }
+    const int threads = 256, wpb = threads / 32;
+    const size_t tbytes = ((size_t)N * N * 2 + 15) & ~(size_t)15;
+    const size_t smem = tbytes + (size_t)wpb * EPB * P.max_row * (MODE == kModeDF64 ? 8 : 4);
+    auto kern = gather_buf_kernel<MODE, N, EPB>;
+    if (P.max_row > 256) { ctx->err = "pattern rows longer than 256 entries"; return FGPU_ERR_INVALID; }
+    if (smem > 227 * 1024) { ctx->err = "pattern rows too long for the gather kernel"; return FGPU_ERR_INVALID; }
+    if (smem > 48 * 1024) FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    const int64_t need_blocks = (P.nrows + wpb - 1) / wpb;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(need_blocks, (int64_t)std::max(per_sm, 1) * sms));
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather", ev);
+    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, V->d_inc_ptr, V->d_inc, V->d_pos, A->d_kbuf, tab->d_tri,
+                                                      P.max_row, A->d_val, accumulate, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+    const int order = A->space->order;
+    const bool f32 = A->precision == FGPU_F32;
+    if (A->ncomp != 1) { ctx->err = "Laplace/mass form needs a scalar space"; return FGPU_ERR_INVALID; }
+    if (order == 1) return f32 ? run_two_phase<kModeF32, 4, 8>(ctx, A, tab, rec, accumulate)
+                               : run_two_phase<kModeDF64, 4, 8>(ctx, A, tab, rec, accumulate);
+    if (order == 2) return f32 ? run_two_phase<kModeF32, 10, 3>(ctx, A, tab, rec, accumulate)
+                               : run_two_phase<kModeDF64, 10, 3>(ctx, A, tab, rec, accumulate);
+    if (order == 3) return f32 ? run_two_phase<kModeF32, 20, 1>(ctx, A, tab, rec, accumulate)
+                               : run_two_phase<kModeDF64, 20, 1>(ctx, A, tab, rec, accumulate);
+    ctx->err = "unsupported order";
+    return FGPU_ERR_INVALID;
 }
 
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {

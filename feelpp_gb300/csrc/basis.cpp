@@ -190,6 +190,14 @@ bool build_ref_tables(int order, int qdeg, RefTables& out, std::string& err) {
             }
     }
     for (int i = 0; i < n * n; ++i) out.T7[(size_t)6 * n * n + i] = (double)M[i];
+    // the tensors are symmetric; make them exactly so (the long-double sums of
+    // (i, j) and (j, i) may round apart), so that K_e(i, j) and K_e(j, i) are
+    // computed from the same numbers and an element matrix can be stored as its
+    // upper triangle
+    for (int k = 0; k < 7; ++k)
+        for (int i = 0; i < n; ++i)
+            for (int j = i + 1; j < n; ++j)
+                out.T7[((size_t)k * n + j) * n + i] = out.T7[((size_t)k * n + i) * n + j];
     return true;
 }
 

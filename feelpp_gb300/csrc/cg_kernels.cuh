@@ -129,6 +129,7 @@ template <class PL>
 struct CGScalars {
     typename PL::D rz[2];     // r.z of the current iteration, double-buffered by iteration parity
     typename PL::D rr, bb, tol2;
+    typename PL::D pq;        // p.Ap of the last iteration (read by the Lanczos estimate)
     int it, done, fail, pad;
 };
 
@@ -255,6 +256,7 @@ __global__ void cg_update_kernel(int64_t n, typename PL::S* __restrict__ x, type
         s_alpha = s_bad ? PL::dzero() : PL::ddiv(sc->rz[parity], pq);
     }
     __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->pq = pq;
     if (s_bad) {                       // breakdown: p.Ap <= 0 (same decision in every block)
         if (blockIdx.x == 0 && threadIdx.x == 0) { sc->fail = 1; sc->done = 1; }
         return;
@@ -367,6 +369,14 @@ __global__ void cg_refresh_scalars(const typename PL::D* __restrict__ partial, i
         sc->done = 0;
         sc->fail = 0;
     }
+}
+
+// r = b - q
+template <class PL>
+__global__ void residual_from_q_kernel(int64_t n, const typename PL::S* __restrict__ b, const typename PL::S* __restrict__ q,
+                                       typename PL::S* __restrict__ r) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = PL::st(PL::sub(PL::ld(b[i]), PL::ld(q[i])));
 }
 
 // per-block partial sums of v.v (binary64)

@@ -94,6 +94,22 @@ struct fgpu_ctx {
     int* d_status = nullptr;       // device status word written by kernels (bit flags)
     int64_t launches = 0;          // kernels launched by this context
     int host_threads = 1;
+    int capturing = 0;             // the stream is being captured into a graph
+    int64_t capture_launches0 = 0;
+};
+
+struct fgpu_graph {
+    fgpu_ctx* ctx = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;          // kernels per replay
+};
+
+struct fgpu_bc {
+    fgpu_ctx* ctx = nullptr;
+    int64_t n = 0;
+    uint8_t* d_mask = nullptr;
+    double* d_g = nullptr;         // null: homogeneous
 };
 
 struct fgpu_mesh {
@@ -154,6 +170,8 @@ struct fgpu_matrix {
     void* d_val = nullptr;           // nnz values (double or float)
     double* d_coef = nullptr;        // per-element coefficient records of the last assembly
     int64_t coef_cap = 0;
+    void* d_kbuf = nullptr;          // two-phase assembly: element matrices (upper triangles)
+    size_t kbuf_bytes = 0;
     mutable std::shared_ptr<SellLayout> sell; // solver layout, built on first solve
 };
 
@@ -183,6 +201,9 @@ struct DevTables {                     // device copies of the reference tables
     float* d_Sf = nullptr;
     float* d_T7h = nullptr;            // df64 split of T7: hi = fl32(T), lo = fl32(T - hi)
     float* d_T7l = nullptr;
+    float* d_T7th = nullptr;           // the same split in upper-triangle order: 7 x n(n+1)/2
+    float* d_T7tl = nullptr;
+    uint16_t* d_tri = nullptr;         // n x n: (i, j) -> upper-triangle index of (min, max)
     double* d_phi = nullptr;           // Q n
     double* d_dphi = nullptr;          // Q n 3
     double* d_qx = nullptr;            // Q 3
@@ -200,13 +221,41 @@ int launch_assemble_gather(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, 
 int launch_assemble_colour(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, int kind, const double* d_coef,
                            int accumulate);
 int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
-                       float4* d_rec);
+                       float4* d_rec, const double* d_kscale = nullptr);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V);
+
+// One problem of a batch (device-side descriptor, built by batch.cu).
+struct BatchProblem {
+    int order, n, maxrow, pad;
+    int64_t row0, nrows;             // global row range
+    int64_t elem0, nt;               // global element range
+    const int64_t* sia;              // scalar pattern rows
+    const int64_t* inc_ptr;
+    const int32_t* inc;
+    const uint8_t* pos;
+    const double* xyz;
+    const int32_t* tets;
+    const double* kappa;             // per-element kappa (device) or null
+    double kappa_c, mass;
+    float4* rec;                     // coefficient records (the matrix's d_coef)
+    void* val;                       // matrix values
+};
+struct BatchLaunch {                 // launch configuration picked by the batch tuner
+    int threads = 256;
+    int chunk = 16;                  // rows taken per work-queue grab
+};
+int launch_batch_geometry(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
+                          int64_t total_elems);
+int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_row_off,
+                        int64_t total_rows, int f32, int acc_floats, unsigned long long* d_counter,
+                        const BatchLaunch& cfg, int accumulate);
 int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fkind, const double* fc,
                double* d_out, int accumulate, double* d_work);
 int launch_dirichlet(fgpu_ctx* ctx, fgpu_matrix* A, double* d_rhs, const uint8_t* d_mask, const double* d_g,
                      int mode, double diag);
+int launch_axpby(fgpu_ctx* ctx, int64_t n, double a, const double* x, double b, double* y);
 int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y, double alpha_b, const double* b);
 int launch_convert_values(fgpu_ctx* ctx, const fgpu_matrix* src, fgpu_matrix* dst);
 

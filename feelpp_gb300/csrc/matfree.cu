@@ -219,7 +219,6 @@ struct fgpu_operator {
 namespace fgpu {
 int launch_mf_element_tc(fgpu_ctx* ctx, int n, int64_t nt, const int32_t* l2n, const float4* rec, const float* T7f, const float* x,
                          const uint8_t* mask, float* ye, const int* stop);
-int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass, float4* d_rec);
 int launch_geometry(fgpu_ctx* ctx, const fgpu_mesh* mesh, int kind, const double* d_kappa, double kappa, double mass,
                     double lam, double mu, double* d_coef);
 
@@ -310,7 +309,7 @@ int operator_diagonal(fgpu_ctx* ctx, fgpu_operator* op) {
 // ===========================================================================
 // matrix-free CG
 // ===========================================================================
-#include "cg_kernels.cuh"
+#include "cg_driver.cuh"
 
 namespace fgpu {
 
@@ -389,12 +388,6 @@ __global__ void cast_back_kernel(int64_t n, const T* __restrict__ a, double* __r
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) b[i] = (double)a[i];
 }
 template <class PL>
-__global__ void residual_from_q_kernel(int64_t n, const typename PL::S* __restrict__ b, const typename PL::S* __restrict__ q,
-                                       typename PL::S* __restrict__ r) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        r[i] = PL::st(PL::sub(PL::ld(b[i]), PL::ld(q[i])));
-}
-template <class PL>
 __global__ void dinv_from_diag_kernel(int64_t n, const typename PL::S* __restrict__ d, typename PL::S* __restrict__ dinv, int use_pc) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const typename PL::A v = PL::ld(d[i]);
@@ -445,128 +438,31 @@ static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* 
     ctx->launches += 2;
 }
 
-// Matrix-free PCG with Jacobi (operator diagonal). For the binary32 operator the
-// iterations run from a captured graph like the CSR solver; the binary64 ones
-// launch per iteration (their element phase is long, launch overhead is noise).
-//
-// Optional reliable updates (mixed precision): at a poll point where the
-// recurrence residual has dropped by delta since the last update, or claims
-// convergence, `refresh` folds x into the binary64 solution, zeroes x and
-// replaces r by the binary64 residual; the search direction is kept.
+// Matrix-free PCG with Jacobi or Chebyshev-Jacobi (operator diagonal). The
+// binary32 operator's iterations run from a captured graph like the CSR
+// solver; the binary64 ones launch per iteration (their element phase is
+// long, launch overhead is noise, and it is not gated by the stop flag).
 template <class PL>
-using MfRefreshFn = std::function<int(typename PL::S* x, typename PL::S* r, bool* converged)>;
-
-template <class PL>
-static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b, typename PL::S* x, double rtol, int maxit, int pc,
-                       int check_every, int* iters, int* fail, double* rr_out, double* bb_out,
-                       const MfRefreshFn<PL>* refresh = nullptr, double delta = 0.1, int* nrefresh_out = nullptr,
-                       bool* true_conv = nullptr) {
+static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b, typename PL::S* x, const CgOptions& o, int pc,
+                       CgResult* res, const RefreshFn<PL>* refresh = nullptr) {
     typedef typename PL::S S;
-    typedef typename PL::D D;
     const int64_t n = op->nnodes;
-    cudaStream_t s = ctx->stream;
-    S *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
-    D *partial = nullptr, *pq_partial = nullptr;
-    CGScalars<PL>* sc = nullptr;
-    CGScalars<PL>* hsc = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
     const int vb = vec_blocks(n);
-    const int gb = vb;
-    auto cleanup = [&]() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dinv); cudaFree(partial); cudaFree(pq_partial); cudaFree(sc);
-        if (hsc) cudaFreeHost(hsc);
+    S* dinv = nullptr;
+    if (cudaMalloc(&dinv, n * sizeof(S)) != cudaSuccess) { ctx->err = "matrix-free CG: allocation failed"; return FGPU_ERR_ALLOC; }
+    dinv_from_diag_kernel<PL><<<vb, 256, 0, ctx->stream>>>(n, (const S*)op->d_diag, dinv, pc != FGPU_PC_NONE);
+    ctx->launches++;
+    CgOperator<PL> A;
+    A.apply = [ctx, op, vb](const S* xx, S* yy, typename PL::D* partial, const CGScalars<PL>* sc) {
+        mf_apply_cg<PL>(ctx, op, xx, yy, partial, sc, vb);
+        ctx->launches -= 2;   // cg_run counts the launches of an application
     };
-#define CK(call)                                                             \
-    do {                                                                     \
-        cudaError_t e_ = (call);                                             \
-        if (e_ != cudaSuccess) {                                             \
-            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);   \
-            cleanup();                                                       \
-            return FGPU_ERR_CUDA;                                            \
-        }                                                                    \
-    } while (0)
-    if (check_every & 1) ++check_every;
-    CK(cudaMalloc(&r, n * sizeof(S)));
-    CK(cudaMalloc(&z, n * sizeof(S)));
-    CK(cudaMalloc(&p, n * sizeof(S)));
-    CK(cudaMalloc(&q, n * sizeof(S)));
-    CK(cudaMalloc(&dinv, n * sizeof(S)));
-    CK(cudaMalloc(&partial, 3 * vb * sizeof(D)));
-    CK(cudaMalloc(&pq_partial, vb * sizeof(D)));
-    CK(cudaMalloc(&sc, sizeof(CGScalars<PL>)));
-    CK(cudaMallocHost(&hsc, sizeof(CGScalars<PL>)));
-    dinv_from_diag_kernel<PL><<<vb, 256, 0, s>>>(n, (const S*)op->d_diag, dinv, pc == FGPU_PC_JACOBI);
-    mf_apply_cg<PL>(ctx, op, x, q, nullptr, nullptr, gb);
-    residual_from_q_kernel<PL><<<vb, 256, 0, s>>>(n, b, q, r);
-    cg_init_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, b, r, dinv, z, p, partial);
-    cg_init_scalars<PL><<<1, 256, 0, s>>>(partial, vb, PL::host_from_double(rtol * rtol), sc);
-    ctx->launches += 4;
-    CK(cudaGetLastError());
-    const bool use_graph = op->precision == FGPU_F32;
-    if (use_graph) {
-        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < check_every; ++k) {
-            const int parity = k & 1;
-            mf_apply_cg<PL>(ctx, op, p, q, pq_partial, sc, gb);
-            cg_update_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, x, r, z, p, q, dinv, pq_partial, gb, partial, sc, parity);
-            cg_p_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, p, z, partial, vb, maxit, sc, parity);
-        }
-        cudaError_t e = cudaStreamEndCapture(s, &graph);
-        if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); cleanup(); return FGPU_ERR_CUDA; }
-        CK(cudaGraphInstantiate(&exec, graph, 0));
-    }
-    CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    int guard = 0, parity = 0, nref = 0;
-    double rr_ref = PL::host_to_double(hsc->rr);
-    while (true) {
-        bool want = false;
-        if (hsc->done) {
-            if (!refresh || hsc->fail != 0) break;
-            want = true;                                   // recurrence converged: verify in binary64
-        } else if (refresh && PL::host_to_double(hsc->rr) <= delta * delta * rr_ref) {
-            want = true;
-        }
-        if (want) {
-            bool conv = false;
-            const int rc2 = (*refresh)(x, r, &conv);
-            if (rc2) { cleanup(); return rc2; }
-            ++nref;
-            if (conv) { if (true_conv) *true_conv = true; break; }
-            if (hsc->it >= maxit) { hsc->fail = 2; break; }
-            cg_refresh_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, r, dinv, z, partial, hsc->done ? p : nullptr);
-            cg_refresh_scalars<PL><<<1, 256, 0, s>>>(partial, vb, sc);
-            ctx->launches += 2;
-            CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            rr_ref = PL::host_to_double(hsc->rr);
-            continue;
-        }
-        if (use_graph) {
-            CK(cudaGraphLaunch(exec, s));
-            ctx->launches += 4 * check_every;
-        } else {
-            mf_apply_cg<PL>(ctx, op, p, q, pq_partial, sc, gb);
-            cg_update_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, x, r, z, p, q, dinv, pq_partial, gb, partial, sc, parity);
-            cg_p_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, p, z, partial, vb, maxit, sc, parity);
-            parity ^= 1;
-            ctx->launches += 2;
-        }
-        CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        if (++guard > maxit + 2) break;
-    }
-    if (nrefresh_out) *nrefresh_out = nref;
-    *iters = hsc->it;
-    *fail = hsc->fail;
-    *rr_out = PL::host_to_double(hsc->rr);
-    *bb_out = PL::host_to_double(hsc->bb);
-    cleanup();
-#undef CK
-    return FGPU_OK;
+    A.npq = vb;
+    A.launches = 2;
+    A.graph = op->precision == FGPU_F32;
+    const int rc = cg_run<PL>(ctx, n, A, dinv, b, x, o, res, refresh);
+    cudaFree(dinv);
+    return rc;
 }
 
 static double host_norm(fgpu_ctx* ctx, int64_t n, const double* d) {
@@ -601,8 +497,9 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
-    const int ce = cfg->check_every > 0 ? cfg->check_every : 16;
-    int rc = FGPU_OK, iters = 0, fail = 0, outer = 0;
+    const CgOptions opt = cg_options(cfg);
+    CgResult res;
+    int rc = FGPU_OK, fail = 0, fallback = 0, fallback_its = 0;
     double rn = 0, bn = host_norm(ctx, n, d_b);
     double *r = nullptr, *q = nullptr;
     if (cudaMalloc(&r, n * sizeof(double)) != cudaSuccess || cudaMalloc(&q, n * sizeof(double)) != cudaSuccess) {
@@ -613,9 +510,9 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
     if (!cfg->mixed) {
         if (op->precision == FGPU_F32) { ctx->err = "the plain matrix-free solve needs a binary64 operator"; rc = FGPU_ERR_INVALID; }
         else {
-            double rr = 0, bb = 0;
-            rc = mf_pcg_core<PolF64>(ctx, op, d_b, d_x, cfg->rtol, cfg->maxit, cfg->pc, ce, &iters, &fail, &rr, &bb);
-            outer = 1;
+            rc = mf_pcg_core<PolF64>(ctx, op, d_b, d_x, opt, cfg->pc, &res);
+            fail = res.fail;
+            res.nrefresh = 1;
         }
     } else {
         if (!op32 || op32->precision != FGPU_F32 || op32->space != op->space) { ctx->err = "mixed matrix-free solve needs a binary32 inner operator on the same space"; rc = FGPU_ERR_INVALID; }
@@ -630,34 +527,47 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
         // into the binary64 solution and the residual replaced by b - A64 x.
         if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
         if (rc == FGPU_OK && !(bn == 0.0 || rn <= cfg->rtol * bn)) {
-            const double delta = cfg->inner_rtol > 0 ? cfg->inner_rtol : 0.1;
             const int vb = vec_blocks(n);
             const double scale = rn;   // binary32 system scaled to a unit initial residual
             d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, r, r32, 1.0 / scale);
             cudaMemsetAsync(d32, 0, n * sizeof(float), ctx->stream);
             ctx->launches++;
-            MfRefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
+            int stagnant = 0;
+            RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
                 fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, xl, scale);
                 ctx->launches++;
+                const double rprev = rn;
                 const int r2 = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
                 if (r2) return r2;
                 d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, r, rl, 1.0 / scale);
                 ctx->launches++;
                 *conv = rn <= cfg->rtol * bn;
+                stagnant = (rn > 0.5 * rprev) ? stagnant + 1 : 0;
+                if (!*conv && stagnant >= 2) return kRefreshStagnated;
                 return FGPU_OK;
             };
-            int f = 0;
-            double rr = 0, bb = 0;
-            bool conv = false;
-            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, cfg->rtol * bn / rn, cfg->maxit, cfg->pc, ce, &iters, &f, &rr, &bb,
-                                     &refresh, delta, &outer, &conv);
-            if (rc == FGPU_OK) {
-                if (f == 1) fail = 1;
-                else if (!conv) {
-                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, d32, scale);
-                    ctx->launches++;
-                    rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
-                    if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+            CgOptions o32 = opt;
+            o32.rtol = cfg->rtol * bn / rn;   // the binary32 system starts from a unit residual
+            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, o32, cfg->pc, &res, &refresh);
+            if (rc == FGPU_OK && !res.true_conv) {
+                fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, d32, scale);
+                ctx->launches++;
+                rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                if (rc == FGPU_OK && rn > cfg->rtol * bn) {
+                    if ((res.fail == 1 || res.fail == 3) && res.iters < cfg->maxit) {
+                        // binary32 breakdown or stagnation: finish with the binary64 operator from the current x
+                        CgResult r64;
+                        CgOptions o64 = opt;
+                        o64.maxit = cfg->maxit - res.iters;
+                        rc = mf_pcg_core<PolF64>(ctx, op, d_b, d_x, o64, cfg->pc, &r64);
+                        fallback = 1;
+                        fallback_its = r64.iters;
+                        if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                        if (rc == FGPU_OK && r64.fail == 1) fail = 1;
+                        else if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+                    } else {
+                        fail = res.fail == 1 ? 1 : 2;
+                    }
                 }
             }
         }
@@ -675,10 +585,13 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
     cudaEventDestroy(e1);
     if (rc != FGPU_OK) return rc;
     if (st) {
-        st->iterations = iters;
-        st->outer = outer;
+        st->iterations = res.iters + fallback_its;
+        st->outer = res.nrefresh;
         st->rel_residual = bn > 0 ? rn / bn : 0.0;
         st->time_ms = ms;
+        st->eig_max = res.lmax;
+        st->fallback = fallback;
+        st->fallback_iterations = fallback_its;
     }
     if (fail == 1) { ctx->err = "CG breakdown"; return FGPU_ERR_BREAKDOWN; }
     if (fail == 2) { ctx->err = "matrix-free CG did not reach rtol"; return FGPU_ERR_NOT_CONVERGED; }

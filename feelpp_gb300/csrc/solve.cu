@@ -29,7 +29,7 @@
 #include <tuple>
 #include <vector>
 
-#include "cg_kernels.cuh"
+#include "cg_driver.cuh"
 #include "df64.h"
 #include "fgpu_core.h"
 
@@ -336,123 +336,35 @@ static int plan_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* 
 
 // One PCG solve with policy PL on values `val`, right-hand side b and solution x
 // (initial guess on entry), all in the policy's formats.
-// Optional reliable updates (mixed precision): at a poll point where the
-// recurrence residual has dropped by delta since the last update, or claims
-// convergence, `refresh` folds x into the binary64 solution, zeroes x and
-// replaces r by the binary64 residual; the search direction is kept.
-template <class PL>
-using RefreshFn = std::function<int(typename PL::S* x, typename PL::S* r, bool* converged)>;
-
+// PCG on an assembled matrix: Jacobi diagonal from the matrix, SpMV kernel
+// picked by the tuner, iterations in cg_run (cg_driver.cuh).
 template <class PL>
 static int pcg_core(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* val, const typename PL::S* b,
-                    typename PL::S* x, double rtol, int maxit, int pc, int check_every, int* iters, int* fail,
-                    double* rr_out, double* bb_out, const RefreshFn<PL>* refresh = nullptr, double delta = 0.1,
-                    int* nrefresh_out = nullptr, bool* true_conv = nullptr) {
+                    typename PL::S* x, const CgOptions& o, int pc, CgResult* res, const RefreshFn<PL>* refresh = nullptr) {
     typedef typename PL::S S;
-    typedef typename PL::D D;
     const int64_t n = A->nrows;
-    cudaStream_t s = ctx->stream;
-    S *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
-    D* partial = nullptr;
-    D* pq_partial = nullptr;
-    CGScalars<PL>* sc = nullptr;
-    CGScalars<PL>* hsc = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    SpmvPlan<PL> plan;
-    // partial-sum buffers sized for the largest grid any candidate launches
-    // (the number of CSR blocks grows with the lanes per row)
-    int sblocks = spmv_blocks(A, 32);
     const int vb = vec_blocks(n);
-    const int nbp = std::max(sblocks, vb);
-    auto cleanup = [&]() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dinv); cudaFree(partial); cudaFree(pq_partial);
-        cudaFree(sc);
-        if (hsc) cudaFreeHost(hsc);
+    S *dinv = nullptr, *tmp = nullptr;
+    if (cudaMalloc(&dinv, n * sizeof(S)) != cudaSuccess || cudaMalloc(&tmp, n * sizeof(S)) != cudaSuccess) {
+        cudaFree(dinv);
+        ctx->err = "CG: allocation failed";
+        return FGPU_ERR_ALLOC;
+    }
+    diag_inv_kernel<PL><<<vb, 256, 0, ctx->stream>>>(n, A->d_ia, A->d_ja, val, dinv, pc != FGPU_PC_NONE);
+    ctx->launches++;
+    SpmvPlan<PL> plan;
+    plan_spmv<PL>(ctx, A, val, dinv, tmp, plan);
+    cudaFree(tmp);
+    CgOperator<PL> op;
+    op.apply = [&plan, A, val, ctx](const S* xx, S* yy, typename PL::D* partial, const CGScalars<PL>* sc) {
+        plan.launch(ctx->stream, A, val, xx, yy, 0, nullptr, partial ? xx : nullptr, partial, sc);
     };
-#define CK(call)                                                             \
-    do {                                                                     \
-        cudaError_t e_ = (call);                                             \
-        if (e_ != cudaSuccess) {                                             \
-            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);   \
-            cleanup();                                                       \
-            return FGPU_ERR_CUDA;                                            \
-        }                                                                    \
-    } while (0)
-    if (check_every & 1) ++check_every;   // parity of the scalar double buffer repeats per replay
-    CK(cudaMalloc(&pq_partial, nbp * sizeof(D)));
-    CK(cudaMalloc(&r, n * sizeof(S)));
-    CK(cudaMalloc(&z, n * sizeof(S)));
-    CK(cudaMalloc(&p, n * sizeof(S)));
-    CK(cudaMalloc(&q, n * sizeof(S)));
-    CK(cudaMalloc(&dinv, n * sizeof(S)));
-    CK(cudaMalloc(&partial, 3 * nbp * sizeof(D)));
-    CK(cudaMalloc(&sc, sizeof(CGScalars<PL>)));
-    CK(cudaMallocHost(&hsc, sizeof(CGScalars<PL>)));
-    diag_inv_kernel<PL><<<vb, 256, 0, s>>>(n, A->d_ia, A->d_ja, val, dinv, pc == FGPU_PC_JACOBI);
-    plan_spmv<PL>(ctx, A, val, dinv, q, plan);
-    sblocks = plan.blocks(A);
-    if (sblocks > nbp) { ctx->err = "internal: partial buffer too small"; cleanup(); return FGPU_ERR_INVALID; }
-    plan.launch(s, A, val, x, r, 1, b, nullptr, nullptr, nullptr);
-    cg_init_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, b, r, dinv, z, p, partial);
-    cg_init_scalars<PL><<<1, 256, 0, s>>>(partial, vb, PL::host_from_double(rtol * rtol), sc);
-    ctx->launches += 4;
-    CK(cudaGetLastError());
-    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < check_every; ++k) {
-        const int parity = k & 1;
-        plan.launch(s, A, val, p, q, 0, nullptr, p, pq_partial, sc);
-        cg_update_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, x, r, z, p, q, dinv, pq_partial, sblocks, partial, sc, parity);
-        cg_p_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, p, z, partial, vb, maxit, sc, parity);
-    }
-    {
-        cudaError_t e = cudaStreamEndCapture(s, &graph);
-        if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); cleanup(); return FGPU_ERR_CUDA; }
-    }
-    CK(cudaGraphInstantiate(&exec, graph, 0));
-    CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    int guard = 0, nref = 0;
-    double rr_ref = PL::host_to_double(hsc->rr);
-    while (true) {
-        bool want = false;
-        if (hsc->done) {
-            if (!refresh || hsc->fail != 0) break;
-            want = true;                                   // recurrence converged: verify in binary64
-        } else if (refresh && PL::host_to_double(hsc->rr) <= delta * delta * rr_ref) {
-            want = true;
-        }
-        if (want) {
-            bool conv = false;
-            const int rc2 = (*refresh)(x, r, &conv);
-            if (rc2) { cleanup(); return rc2; }
-            ++nref;
-            if (conv) { if (true_conv) *true_conv = true; break; }
-            if (hsc->it >= maxit) { hsc->fail = 2; break; }
-            cg_refresh_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, r, dinv, z, partial, hsc->done ? p : nullptr);
-            cg_refresh_scalars<PL><<<1, 256, 0, s>>>(partial, vb, sc);
-            ctx->launches += 2;
-            CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            rr_ref = PL::host_to_double(hsc->rr);
-            continue;
-        }
-        CK(cudaGraphLaunch(exec, s));
-        ctx->launches += 3 * check_every;
-        CK(cudaMemcpyAsync(hsc, sc, sizeof(CGScalars<PL>), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        if (++guard > maxit / std::max(check_every, 1) + 2) break;
-    }
-    if (nrefresh_out) *nrefresh_out = nref;
-    *iters = hsc->it;
-    *fail = hsc->fail;
-    *rr_out = PL::host_to_double(hsc->rr);
-    *bb_out = PL::host_to_double(hsc->bb);
-    cleanup();
-#undef CK
-    return FGPU_OK;
+    op.npq = plan.blocks(A);
+    op.launches = 1;
+    op.graph = true;
+    const int rc = cg_run<PL>(ctx, n, op, dinv, b, x, o, res, refresh);
+    cudaFree(dinv);
+    return rc;
 }
 
 // ||b - A x||_2 in native FP64 (binary64 values and vectors); r receives b - A x.
@@ -489,10 +401,10 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
-    const int ce = cfg->check_every > 0 ? cfg->check_every : 16;
+    const CgOptions opt = cg_options(cfg);
+    CgResult res;
     const int64_t n = A->nrows;
-    int iters = 0, fail = 0;
-    double rr = 0, bb = 0, rn = 0;
+    double rn = 0;
     int rc = FGPU_OK;
     if (cfg->arith == FGPU_ARITH_DF64) {
         float2 *val = nullptr, *b = nullptr, *x = nullptr;
@@ -506,7 +418,7 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
             d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_b, b);
             d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_x, x);
             ctx->launches += 3;
-            rc = pcg_core<PolDF64>(ctx, A, val, b, x, cfg->rtol, cfg->maxit, cfg->pc, ce, &iters, &fail, &rr, &bb);
+            rc = pcg_core<PolDF64>(ctx, A, val, b, x, opt, cfg->pc, &res);
             if (rc == FGPU_OK) {
                 df2d_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, x, d_x);
                 ctx->launches++;
@@ -514,8 +426,7 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
         }
         cudaFree(val); cudaFree(b); cudaFree(x);
     } else {
-        rc = pcg_core<PolF64>(ctx, A, (const double*)A->d_val, d_b, d_x, cfg->rtol, cfg->maxit, cfg->pc, ce, &iters, &fail,
-                              &rr, &bb);
+        rc = pcg_core<PolF64>(ctx, A, (const double*)A->d_val, d_b, d_x, opt, cfg->pc, &res);
     }
     if (rc == FGPU_OK) {  // final residual recomputed in binary64 from the matrix
         Scratch64 S;
@@ -529,12 +440,16 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != FGPU_OK) return rc;
-    const double bn = std::sqrt(bb);
+    const double bn = std::sqrt(res.bb);
+    const int fail = res.fail;
     if (st) {
-        st->iterations = iters;
+        st->iterations = res.iters;
         st->outer = 1;
         st->rel_residual = bn > 0 ? rn / bn : 0.0;
         st->time_ms = ms;
+        st->eig_max = res.lmax;
+        st->fallback = 0;
+        st->fallback_iterations = 0;
     }
     if (fail == 1) { ctx->err = "CG breakdown: p.Ap <= 0 (matrix not SPD)"; return FGPU_ERR_BREAKDOWN; }
     if (fail == 2) { ctx->err = "CG reached maxit"; return FGPU_ERR_NOT_CONVERGED; }
@@ -551,7 +466,8 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
     int rc = FGPU_OK;
-    int total = 0, nref = 0, fail = 0;
+    int fail = 0, fallback = 0, fallback_its = 0;
+    CgResult res;
     double rn = 0, bn = 0;
     {
         Scratch64 S;
@@ -570,34 +486,46 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
             bn = std::sqrt(s2);
             rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
             if (rc == FGPU_OK && !(bn == 0.0 || rn <= cfg->rtol * bn)) {
-                const double delta = cfg->inner_rtol > 0 ? cfg->inner_rtol : 0.1;
-                const int ce = cfg->check_every > 0 ? cfg->check_every : 16;
                 const double scale = rn;   // binary32 system scaled to a unit initial residual
                 d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, r32, 1.0 / scale);
                 cudaMemsetAsync(x32, 0, n * sizeof(float), ctx->stream);
+                int stagnant = 0;
                 RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
                     fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, xl, scale);
+                    const double rprev = rn;
                     int r2 = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
                     if (r2) return r2;
                     d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, rl, 1.0 / scale);
                     ctx->launches += 2;
                     *conv = rn <= cfg->rtol * bn;
+                    // two replacements in a row without halving the residual: stagnation
+                    stagnant = (rn > 0.5 * rprev) ? stagnant + 1 : 0;
+                    if (!*conv && stagnant >= 2) return kRefreshStagnated;
                     return FGPU_OK;
                 };
-                int it = 0, f = 0;
-                double rr = 0, bb = 0;
-                bool conv = false;
-                // recurrence tolerance in absolute terms: ||r|| <= rtol ||b|| (relative to the initial ||r|| = rn)
-                rc = pcg_core<PolF32>(ctx, A32, (const float*)A32->d_val, r32, x32, cfg->rtol * bn / rn, cfg->maxit, cfg->pc, ce,
-                                      &it, &f, &rr, &bb, &refresh, delta, &nref, &conv);
-                total = it;
-                if (rc == FGPU_OK) {
-                    if (f == 1) fail = 1;
-                    else if (!conv) {
-                        // fold what is left and measure the final binary64 residual
-                        fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, x32, scale);
-                        rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
-                        if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+                CgOptions o32 = cg_options(cfg);
+                o32.rtol = cfg->rtol * bn / rn;   // the binary32 system starts from a unit residual
+                rc = pcg_core<PolF32>(ctx, A32, (const float*)A32->d_val, r32, x32, o32, cfg->pc, &res, &refresh);
+                if (rc == FGPU_OK && !res.true_conv) {
+                    // fold what is left and measure the binary64 residual
+                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, x32, scale);
+                    rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+                    if (rc == FGPU_OK && rn > cfg->rtol * bn) {
+                        if ((res.fail == 1 || res.fail == 3) && res.iters < cfg->maxit) {
+                            // binary32 breakdown or stagnation (A32 = fl32(A) too far from A at
+                            // this conditioning): finish in FP64 from the current x
+                            CgResult r64;
+                            CgOptions o64 = cg_options(cfg);
+                            o64.maxit = cfg->maxit - res.iters;
+                            rc = pcg_core<PolF64>(ctx, A64, (const double*)A64->d_val, d_b, d_x, o64, cfg->pc, &r64);
+                            fallback_its = r64.iters;
+                            fallback = 1;
+                            if (rc == FGPU_OK) rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+                            if (rc == FGPU_OK && r64.fail == 1) fail = 1;
+                            else if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+                        } else {
+                            fail = res.fail == 1 ? 1 : 2;
+                        }
                     }
                 }
             }
@@ -614,12 +542,15 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
     cudaEventDestroy(e1);
     if (rc != FGPU_OK) return rc;
     if (st) {
-        st->iterations = total;
-        st->outer = nref;
+        st->iterations = res.iters + fallback_its;
+        st->outer = res.nrefresh;
         st->rel_residual = bn > 0 ? rn / bn : 0.0;
         st->time_ms = ms;
+        st->eig_max = res.lmax;
+        st->fallback = fallback;
+        st->fallback_iterations = fallback_its;
     }
-    if (fail == 1) { ctx->err = "CG breakdown in the binary32 iteration"; return FGPU_ERR_BREAKDOWN; }
+    if (fail == 1) { ctx->err = "CG breakdown: p.Ap <= 0 (matrix not SPD)"; return FGPU_ERR_BREAKDOWN; }
     if (fail == 2) { ctx->err = "mixed CG did not reach rtol"; return FGPU_ERR_NOT_CONVERGED; }
     return FGPU_OK;
 }

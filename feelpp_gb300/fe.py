@@ -198,6 +198,60 @@ class DeviceVector:
             pass
 
 
+    def device_ptr(self):
+        d = C.c_void_p()
+        self.env.check(self.env.lib.fgpu_vector_device(self.h, C.byref(d)))
+        return d
+
+    def axpby(self, a, x, b=1.0):
+        """self = a x + b self (VectorPetsc::add / scale)."""
+        self.env.check(self.env.lib.fgpu_vector_axpby(self.env.h, float(a), x.h, float(b), self.h))
+        return self
+
+    def copy_from(self, x):
+        self.env.check(self.env.lib.fgpu_vector_copy(self.env.h, x.h, self.h))
+        return self
+
+
+class _Scaled:
+    """factor * (device scalar): a coefficient read by the kernels when they run."""
+
+    def __init__(self, factor, dev):
+        self.factor, self.dev = float(factor), dev
+
+    def __rmul__(self, coef):
+        if not isinstance(coef, (int, float)):
+            return NotImplemented
+        return _Scaled(float(coef) * self.factor, self.dev)
+
+    __mul__ = __rmul__
+
+
+class DeviceScalar(DeviceVector):
+    """A scalar kept in device memory, e.g. a time-dependent coefficient kappa(t):
+    `dt * kt * inner(gradt(u), grad(v))` scales the stiffness term by its value at the
+    time the assembly kernels run, so a captured graph follows set()."""
+
+    def __init__(self, env, value=0.0):
+        super().__init__(env, 1)
+        self.set(value)
+
+    def set(self, value):
+        self.upload(np.array([float(value)]))
+
+    def __rmul__(self, coef):
+        if not isinstance(coef, (int, float)):
+            return NotImplemented
+        return _Scaled(float(coef), self)
+
+    def __mul__(self, other):
+        if isinstance(other, (int, float)):
+            return _Scaled(float(other), self)
+        if isinstance(other, Expr):
+            return other.__rmul__(self)
+        return NotImplemented
+
+
 class Element(DeviceVector):
     """An element of a function space (coefficient vector resident on the device)."""
 
@@ -292,9 +346,18 @@ class Expr:
 
     def __rmul__(self, coef):
         out = []
+        if isinstance(coef, DeviceScalar):
+            coef = _Scaled(1.0, coef)
         for kind, c in self.terms:
             if kind == "elast":
                 raise ValueError("scale the Lame coefficients instead")
+            if isinstance(coef, _Scaled) or isinstance(c, _Scaled):
+                if kind != "stiff":
+                    raise ValueError("a device coefficient scales the stiffness term only")
+                if isinstance(coef, _Scaled) and isinstance(c, _Scaled):
+                    raise ValueError("one device coefficient per term")
+                out.append((kind, coef * c if isinstance(coef, _Scaled) else _Scaled(float(coef) * c.factor, c.dev)))
+                continue
             if isinstance(coef, np.ndarray) or isinstance(c, np.ndarray):
                 out.append((kind, np.asarray(coef, dtype=np.float64) * c))
             else:
@@ -402,6 +465,23 @@ class Form1:
         self.vec.zero()
 
 
+_PC = {"none": _ffi.PC_NONE, "jacobi": _ffi.PC_JACOBI, "cheb_jacobi": _ffi.PC_CHEB_JACOBI}
+
+
+def _solver_cfg(rtol, maxit, pc, mixed, inner_rtol, check_every, arith, cheb_degree, cheb_ratio):
+    """ksp-rtol, ksp-max-it, pc-type ("jacobi", "cheb_jacobi" or "none")."""
+    if pc not in _PC:
+        raise ValueError("pc must be one of %s" % sorted(_PC))
+    return _ffi.SolverCfg(rtol, maxit, _PC[pc], 1 if mixed else 0, inner_rtol, check_every,
+                          _ffi.ARITH_DF64 if arith == "df64" else _ffi.ARITH_F64, cheb_degree, cheb_ratio)
+
+
+def _stats(st):
+    return {"iterations": st.iterations, "outer": st.outer, "rel_residual": st.rel_residual,
+            "time_ms": st.time_ms, "eig_max": st.eig_max, "fallback": st.fallback,
+            "fallback_iterations": st.fallback_iterations}
+
+
 class Form2:
     """Bilinear form backed by a device CSR matrix with the Feel++ GraphCSR pattern."""
 
@@ -448,9 +528,18 @@ class Form2:
         d.lam, d.mu = 0.0, 0.0
         d.quad_degree = integral.quad
         d.algo = algo
+        d.kappa_scale = None
         kappa_arr = None
         for kind, c in integral.expr.terms:
+            if kind == "stiff" and isinstance(c, _Scaled):
+                if d.kappa != 0.0 or kappa_arr is not None or d.kappa_scale:
+                    raise ValueError("a device-scaled stiffness term must be the only one")
+                d.kappa = c.factor
+                d.kappa_scale = c.dev.device_ptr()
+                continue
             if kind == "stiff":
+                if d.kappa_scale:
+                    raise ValueError("a device-scaled stiffness term must be the only one")
                 if isinstance(c, np.ndarray):
                     kappa_arr = np.ascontiguousarray(c, dtype=np.float64)
                     d.kappa = 0.0
@@ -480,6 +569,12 @@ class Form2:
         self.env.check(self.env.lib.fgpu_dirichlet(self.env.h, self.h, item.rhs.vec.h, len(dofs), _ptr(dofs),
                                                    _ptr(vals), item.type, 1.0))
 
+    def apply_bc(self, bc, rhs=None, type="elimination_symmetric", diag=1.0):  # noqa: A002
+        """Apply a DirichletBC (device-resident rows; capturable in graphs)."""
+        t = {"elimination": 0, "elimination_symmetric": 1, "elimination_keep_diagonal": 2}[type]
+        vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        self.env.check(self.env.lib.fgpu_bc_apply(self.env.h, bc.h, self.h, vec.h if vec is not None else None, t, diag))
+
     def csr(self):
         ia = np.zeros(self.nrows + 1, dtype=np.int64)
         ja = np.zeros(self.nnz, dtype=np.int32)
@@ -496,18 +591,17 @@ class Form2:
         self.env.check(self.env.lib.fgpu_matrix_mult(self.env.h, self.h, x.h, y.h))
 
     def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False, inner_rtol=0.1,
-              check_every=16, arith="f64"):
+              check_every=16, arith="f64", cheb_degree=0, cheb_ratio=0.0):
         """CG + Jacobi (ksp-type=cg, pc-type=jacobi). mixed=True: binary32 CG whose iterate is folded
         into the binary64 solution, and its residual replaced by the binary64 one, each time the
         recurrence residual has dropped by `inner_rtol`; arith="df64": double-float arithmetic for
         the plain solve."""
-        cfg = _ffi.SolverCfg(rtol, maxit, _ffi.PC_JACOBI if pc == "jacobi" else _ffi.PC_NONE, 1 if mixed else 0,
-                             inner_rtol, check_every, _ffi.ARITH_DF64 if arith == "df64" else _ffi.ARITH_F64)
+        cfg = _solver_cfg(rtol, maxit, pc, mixed, inner_rtol, check_every, arith, cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
-        self.env.check(self.env.lib.fgpu_solve_cg(self.env.h, self.h, None, rhs.vec.h, solution.h, C.byref(cfg),
+        vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        self.env.check(self.env.lib.fgpu_solve_cg(self.env.h, self.h, None, vec.h, solution.h, C.byref(cfg),
                                                   C.byref(st)))
-        return {"iterations": st.iterations, "outer": st.outer, "rel_residual": st.rel_residual,
-                "time_ms": st.time_ms}
+        return _stats(st)
 
     def __del__(self):
         try:
@@ -549,17 +643,16 @@ class Operator:
     def apply(self, x, y):
         self.env.check(self.env.lib.fgpu_operator_apply(self.env.h, self.h, x.h, y.h))
 
-    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=0.1, check_every=16):
+    def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=0.1, check_every=16,
+              cheb_degree=0, cheb_ratio=0.0):
         """Matrix-free PCG; with `inner` (a binary32 Operator) the mixed method is used
         (binary32 CG with binary64 residual replacement every `inner_rtol` reduction)."""
-        cfg = _ffi.SolverCfg(rtol, maxit, _ffi.PC_JACOBI if pc == "jacobi" else _ffi.PC_NONE, 1 if inner else 0,
-                             inner_rtol, check_every, _ffi.ARITH_F64)
+        cfg = _solver_cfg(rtol, maxit, pc, inner is not None, inner_rtol, check_every, "f64", cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
         vec = rhs.vec if isinstance(rhs, Form1) else rhs
         self.env.check(self.env.lib.fgpu_solve_cg_operator(self.env.h, self.h, inner.h if inner else None, vec.h,
                                                            solution.h, C.byref(cfg), C.byref(st)))
-        return {"iterations": st.iterations, "outer": st.outer, "rel_residual": st.rel_residual,
-                "time_ms": st.time_ms}
+        return _stats(st)
 
     def __del__(self):
         try:
@@ -579,3 +672,103 @@ def form1(test):
 
 def form2(test, trial=None, precision="f64"):
     return Form2(test, trial, precision)
+
+
+class DirichletBC:
+    """Dirichlet rows held on the device (on() applied repeatedly, e.g. every time step)."""
+
+    def __init__(self, space, dofs, values=None):
+        self.env = space.env
+        dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+        vals = None if values is None else np.ascontiguousarray(values, dtype=np.float64)
+        h = C.c_void_p()
+        self.env.check(self.env.lib.fgpu_bc_create(self.env.h, space.ndof, len(dofs), _ptr(dofs), _ptr(vals), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.env.lib.fgpu_bc_destroy(self.h)
+        except Exception:
+            pass
+
+
+class Graph:
+    """CUDA graph of library calls: `with fpp.capture(env) as g: ...` records, g.launch(n) replays."""
+
+    def __init__(self, env):
+        self.env = env
+        self.h = None
+
+    def __enter__(self):
+        self.env.check(self.env.lib.fgpu_graph_begin(self.env.h))
+        return self
+
+    def __exit__(self, et, ev, tb):
+        h = C.c_void_p()
+        rc = self.env.lib.fgpu_graph_end(self.env.h, C.byref(h))
+        if et is None:
+            self.env.check(rc)
+            self.h = h
+        return False
+
+    def launch(self, count=1):
+        self.env.check(self.env.lib.fgpu_graph_launch(self.env.h, self.h, int(count)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.env.lib.fgpu_graph_destroy(self.h)
+        except Exception:
+            pass
+
+
+def capture(env):
+    return Graph(env)
+
+
+class Batch:
+    """Independent scalar Laplace/mass problems assembled together: one geometry launch and
+    one persistent gather launch for all of them (meshes, orders 1-3, kappas may differ)."""
+
+    def __init__(self, forms, integrals):
+        if len(forms) != len(integrals) or not forms:
+            raise ValueError("one integral per form")
+        self.env = forms[0].env
+        n = len(forms)
+        self.forms = list(forms)
+        descs = (_ffi.FormDesc * n)()
+        self._kappa = []
+        kp = (C.c_void_p * n)()
+        for k, (f, integral) in enumerate(zip(forms, integrals)):
+            d, karr = Form2._desc_of(integral, _ffi.ALGO_AUTO)
+            if d.kind != _ffi.FORM_LAPLACE_MASS or d.kappa_scale:
+                raise ValueError("batches hold Laplace/mass forms with constant or per-element kappa")
+            descs[k] = d
+            if karr is not None:
+                dv = DeviceVector(self.env, len(karr))
+                dv.upload(karr)
+                self._kappa.append(dv)
+                kp[k] = dv.device_ptr().value
+        mats = (C.c_void_p * n)(*[f.h.value for f in forms])
+        h = C.c_void_p()
+        self.env.check(self.env.lib.fgpu_batch_create(self.env.h, n, mats, descs, kp, C.byref(h)))
+        self.h = h
+
+    def assemble(self, accumulate=False):
+        self.env.check(self.env.lib.fgpu_batch_assemble(self.env.h, self.h, 1 if accumulate else 0))
+
+    def set_launch(self, threads, chunk):
+        self.env.check(self.env.lib.fgpu_batch_set_launch(self.h, threads, chunk))
+
+    def launch_config(self):
+        t, c, tu = C.c_int(), C.c_int(), C.c_int()
+        self.env.check(self.env.lib.fgpu_batch_get_launch(self.h, C.byref(t), C.byref(c), C.byref(tu)))
+        return {"threads": t.value, "chunk": c.value, "tuned": bool(tu.value)}
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.env.lib.fgpu_batch_destroy(self.h)
+        except Exception:
+            pass

@@ -47,9 +47,13 @@ extern "C" {
 
 #define FGPU_ALGO_AUTO 0          /* best available algorithm for the form */
 #define FGPU_ALGO_GATHER 1        /* row-owner gather: each CSR row summed by one warp, element order */
-#define FGPU_ALGO_COLOUR 2        /* element-coloured scatter-add, colours in fixed order */
+#define FGPU_ALGO_COLOUR 2        /* reserved (element-coloured scatter-add); runs FGPU_ALGO_GATHER */
 #define FGPU_ALGO_GATHER_NATIVE_F64 3 /* row-owner gather in native FP64 arithmetic (FP64 matrices; the
                                      default FP64 path computes in double-float on the FP32 pipes) */
+#define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles) into a device buffer, then the
+                                     row-owner gather sums them; same bits as FGPU_ALGO_GATHER. AUTO
+                                     times both on the first call for a (device, order, precision,
+                                     mesh size) and keeps the faster */
 
 #define FGPU_RHS_SINE 0           /* f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */
 #define FGPU_RHS_CONST_VEC 1      /* f = (c0, c1, c2) (Pchv) */
@@ -61,11 +65,16 @@ extern "C" {
 
 #define FGPU_PC_NONE 0
 #define FGPU_PC_JACOBI 1
+#define FGPU_PC_CHEB_JACOBI 2     /* degree-K Chebyshev polynomial in D^-1 A (Jacobi-scaled), PETSc
+                                     KSPCHEBYSHEV+PCJACOBI used as a fixed preconditioner */
 
 #define FGPU_ARITH_F64 0          /* solver arithmetic: native FP64 (default) */
 #define FGPU_ARITH_DF64 1         /* double-float on the FP32 pipes (~48 bits; moderately conditioned systems) */
 
 typedef struct fgpu_ctx fgpu_ctx;
+typedef struct fgpu_graph fgpu_graph;
+typedef struct fgpu_bc fgpu_bc;
+typedef struct fgpu_batch fgpu_batch;
 typedef struct fgpu_mesh fgpu_mesh;
 typedef struct fgpu_space fgpu_space;
 typedef struct fgpu_matrix fgpu_matrix;
@@ -86,6 +95,9 @@ typedef struct {
     double lambda, mu;        /* Lame coefficients (FGPU_FORM_ELASTICITY) */
     int quad_degree;          /* exact quadrature degree; 0 = 2*order (feelvf default im(2p)) */
     int algo;                 /* FGPU_ALGO_* */
+    const double* kappa_scale;/* device scalar multiplying kappa, read when the kernels run, so a
+                                 captured graph sees its current value (a time-dependent
+                                 coefficient kappa(t)); NULL = 1. Laplace/mass forms only. */
 } fgpu_form_desc;
 
 typedef struct {
@@ -103,6 +115,10 @@ typedef struct {
                                  binary64 residual replacements (0 = 0.1) */
     int check_every;          /* iterations per convergence poll (0 = 16) */
     int arith;                /* FGPU_ARITH_* of the non-mixed solve */
+    int cheb_degree;          /* FGPU_PC_CHEB_JACOBI: polynomial degree K (0 = 3); K - 1 extra
+                                 operator applications per iteration */
+    double cheb_ratio;        /* FGPU_PC_CHEB_JACOBI: lambda_min / lambda_max of the interval (0 = 0.03);
+                                 lambda_max = 1.1 x a Lanczos estimate (ksp_chebyshev_esteig 0,0.1,0,1.1) */
 } fgpu_solver_cfg;
 
 typedef struct {
@@ -110,6 +126,10 @@ typedef struct {
     int outer;                /* binary64 residual replacements (mixed) */
     double rel_residual;      /* final ||b - A x||_2 / ||b||_2 recomputed in FP64 */
     double time_ms;           /* solve wall time on the device stream */
+    double eig_max;           /* FGPU_PC_CHEB_JACOBI: lambda_max used for D^-1 A (0 otherwise) */
+    int fallback;             /* mixed: 1 when the binary32 iteration broke down (p.Ap <= 0 in
+                                 binary32, an ill-conditioned system) and the solve finished in FP64 */
+    int fallback_iterations;  /* FP64 iterations after the fallback */
 } fgpu_solve_stats;
 
 /* ---- context (replaces Feel::Environment + Backend<double>::build(kind),
@@ -257,6 +277,54 @@ int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double
 #define FGPU_NOALLOC_MAX_ELEMENT_VALUES (1 << 21)
 int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate,
                                  void* stream);
+
+/* ---- Dirichlet rows as a device object, for repeated application (each time
+ *      step's reassembled matrix) and for graph capture. Same semantics as
+ *      fgpu_dirichlet (on(), feelpp/feel/feelvf/on.hpp:1140-1190 ->
+ *      MatrixPetsc::zeroRows, matrixpetsc.cpp:1762-1860); n = rows of the
+ *      matrices it is applied to. ---- */
+int fgpu_bc_create(fgpu_ctx* ctx, int64_t n, int64_t ndofs, const int32_t* dofs, const double* values, fgpu_bc** out);
+int fgpu_bc_apply(fgpu_ctx* ctx, const fgpu_bc* bc, fgpu_matrix* A, fgpu_vector* rhs, int mode, double diag);
+int fgpu_bc_destroy(fgpu_bc* bc);
+
+/* ---- vector updates (VectorPetsc::add / scale, feelpp/feel/feelalg/vectorpetsc.cpp):
+ *      y = a x + b y; dst = src ---- */
+int fgpu_vector_axpby(fgpu_ctx* ctx, double a, const fgpu_vector* x, double b, fgpu_vector* y);
+int fgpu_vector_copy(fgpu_ctx* ctx, const fgpu_vector* src, fgpu_vector* dst);
+
+/* ---- CUDA graphs of library calls (no reference counterpart: Feel++ re-runs
+ *      its host loops every time step). Between fgpu_graph_begin and
+ *      fgpu_graph_end the context's stream is captured; these calls may be
+ *      captured: fgpu_assemble_matrix_dev, fgpu_assemble_matrix without host
+ *      kappa (kappa_elem NULL), fgpu_batch_assemble, fgpu_bc_apply,
+ *      fgpu_matrix_mult, fgpu_vector_axpby, fgpu_vector_copy, fgpu_vector_zero,
+ *      fgpu_vector_upload (from pinned host memory: the copy reads the host
+ *      buffer when the graph runs), fgpu_assemble_vector_noalloc on the
+ *      context's stream. Every captured call must have run once before the
+ *      capture (first calls allocate and upload tables); other calls return
+ *      FGPU_ERR_INVALID while capturing. Status words of captured kernels are
+ *      checked by fgpu_graph_launch, which replays the graph `count` times and
+ *      then synchronizes. ---- */
+int fgpu_graph_begin(fgpu_ctx* ctx);
+int fgpu_graph_end(fgpu_ctx* ctx, fgpu_graph** out);
+int fgpu_graph_launch(fgpu_ctx* ctx, fgpu_graph* g, int count);
+int fgpu_graph_destroy(fgpu_graph* g);
+
+/* ---- batches of independent problems (no reference counterpart as one call:
+ *      replaces a loop of form2 assemblies over independent meshes,
+ *      feelpp/feel/feelvf/integrator.hpp:975-1238 per mesh). mats: nprob
+ *      matrices of scalar spaces (orders 1-3, one precision) created with
+ *      fgpu_matrix_create; descs: their Laplace/mass forms (default quadrature);
+ *      d_kappa: nprob device arrays of per-element kappa (or NULL / NULL
+ *      entries). fgpu_batch_assemble runs one geometry launch and one
+ *      persistent gather launch for all problems; its launch shape is tuned on
+ *      the first '=' call (fgpu_batch_get_launch reports it). ---- */
+int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const fgpu_form_desc* descs,
+                      const double* const* d_kappa, fgpu_batch** out);
+int fgpu_batch_assemble(fgpu_ctx* ctx, fgpu_batch* b, int accumulate);
+int fgpu_batch_set_launch(fgpu_batch* b, int threads, int chunk);
+int fgpu_batch_get_launch(const fgpu_batch* b, int* threads, int* chunk, int* tuned);
+int fgpu_batch_destroy(fgpu_batch* b);
 
 /* df64 (double-float) arithmetic self-check on the host: op 0 round trip double->df64->double,
  * 1 a+b, 2 a*b, 3 1/a, 4 a-b, all through df64; writes n results */

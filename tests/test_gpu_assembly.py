@@ -184,3 +184,25 @@ def test_deterministic_repeat(env):
     u, v = V.element(), V.element()
     a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v)))
     assert np.array_equal(v1, a.values())
+
+
+@pytest.mark.parametrize("order,n", [(1, 6), (2, 4), (3, 3)])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_two_phase_equals_fused_gather(env, order, n, precision):
+    """Element matrices buffered (upper triangles) then gathered give the same bits as the
+    fused gather, for '=' and '+='."""
+    from feelpp_gb300 import _ffi
+    xyz, tets = mesh(n, perturb=0.2)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, order)
+    u, v = V.element(), V.element()
+    integral = fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + 0.7 * (fpp.idt(u) * fpp.id(v)))
+    got = []
+    for algo in (_ffi.ALGO_GATHER, _ffi.ALGO_TWO_PHASE, _ffi.ALGO_AUTO):
+        a = fpp.form2(test=V, trial=V, precision=precision)
+        a.algo = algo
+        a.assign(integral)
+        a += integral
+        got.append(a.values())
+    assert np.array_equal(got[0], got[1]) and np.array_equal(got[0], got[2])

@@ -82,3 +82,19 @@ def test_plain_matfree_solve_df64(env):
     w = V.element()
     a.solve(rhs=l, solution=w, rtol=1e-11)
     assert np.linalg.norm(u.to_numpy() - w.to_numpy()) <= 1e-7 * np.linalg.norm(w.to_numpy())
+
+
+def test_mixed_matfree_cheb_jacobi(env):
+    xyz, tets, M, V, integral, a, l = system(env, 6, 3)
+    op64 = fpp.operator(V, integral, precision="f64")
+    op32 = fpp.operator(V, integral, precision="f32")
+    bd = V.boundary_dofs()
+    op64.set_dirichlet(bd)
+    op32.set_dirichlet(bd)
+    u = V.element()
+    st = op64.solve(l, u, rtol=1e-10, inner=op32, pc="cheb_jacobi", cheb_degree=3)
+    assert st["rel_residual"] <= 1e-10 and st["eig_max"] > 1.0
+    w = V.element()
+    stj = op64.solve(l, w, rtol=1e-10, inner=op32)
+    assert st["iterations"] * 1.5 <= stj["iterations"]
+    assert np.linalg.norm(u.to_numpy() - w.to_numpy()) <= 1e-8 * np.linalg.norm(w.to_numpy())

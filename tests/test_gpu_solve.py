@@ -119,3 +119,51 @@ def test_matrix_mult(env, oracle):
     ia, ja, val = a.csr()
     y = oracle.spmv(ia, ja, val, x)
     assert np.abs(yv.to_numpy() - y).max() <= 1e-13 * np.abs(y).max()
+
+
+def _jacobi_lmax(ia, ja, val):
+    """lambda_max of D^-1 A (as D^-1/2 A D^-1/2) for the small test systems."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import eigsh
+    n = len(ia) - 1
+    A = sp.csr_matrix((val, ja, ia), shape=(n, n))
+    d = 1.0 / np.sqrt(A.diagonal())
+    S = sp.diags(d) @ A @ sp.diags(d)
+    return float(eigsh(S, k=1, which="LA", return_eigenvectors=False)[0])
+
+
+@pytest.mark.parametrize("order,n,degree", [(2, 8, 3), (3, 6, 4)])
+def test_cheb_jacobi_pcg(env, oracle, order, n, degree):
+    """Chebyshev-Jacobi PCG: same converged solution as the oracle's Jacobi PCG,
+    fewer iterations, and a lambda_max estimate (x1.1) just above the true one."""
+    xyz, tets, M, V, u, a, l = poisson(env, n, order)
+    st = a.solve(rhs=l, solution=u, rtol=1e-10, pc="cheb_jacobi", cheb_degree=degree)
+    assert st["rel_residual"] <= 1e-10
+    w = V.element()
+    stj = a.solve(rhs=l, solution=w, rtol=1e-10)
+    assert st["iterations"] * 1.5 <= stj["iterations"]
+    ia, ja, val = a.csr()
+    lt = _jacobi_lmax(ia, ja, val)
+    assert 0.98 * lt <= st["eig_max"] <= 1.15 * lt
+    N, l2g, oia, oja, oval = oracle_system(oracle, xyz, tets, order, mass=0.0)
+    b = oracle.rhs(order, xyz, tets, l2g, N, fkind=0)
+    mask = oracle.boundary_mask(order, xyz, tets, l2g, N)
+    oracle.dirichlet(oia, oja, oval, b, mask, mode=1)
+    x, it, res = oracle.pcg(oia, oja, oval, b, rtol=1e-12)
+    assert np.linalg.norm(u.to_numpy() - x) <= 1e-8 * np.linalg.norm(x)
+
+
+def test_cheb_jacobi_mixed(env):
+    xyz, tets, M, V, u, a, l = poisson(env, 10, 2)
+    st = a.solve(rhs=l, solution=u, rtol=1e-10, mixed=True, pc="cheb_jacobi")
+    assert st["rel_residual"] <= 1e-10 and st["outer"] >= 2
+    w = V.element()
+    stj = a.solve(rhs=l, solution=w, rtol=1e-10)
+    assert np.linalg.norm(u.to_numpy() - w.to_numpy()) <= 1e-8 * np.linalg.norm(w.to_numpy())
+    assert st["iterations"] * 1.5 <= stj["iterations"]
+
+
+def test_bad_pc_name(env):
+    xyz, tets, M, V, u, a, l = poisson(env, 3, 1)
+    with pytest.raises(ValueError):
+        a.solve(rhs=l, solution=u, pc="gamg")
