@@ -279,6 +279,8 @@ int fgpu_space_destroy(fgpu_space* V) {
     cudaFree(V->d_inc_ptr);
     cudaFree(V->d_inc);
     cudaFree(V->d_pos);
+    cudaFree(V->d_gptr);
+    cudaFree(V->d_gidx);
     delete V;
     return FGPU_OK;
 }
@@ -416,73 +418,24 @@ int fgpu_matrix_destroy(fgpu_matrix* A) {
 }
 
 // ---------------------------------------------------------------------------
-// Assembly tuner: for (device, order, precision, elements, nnz) time the fused
-// gather and the two-phase assembly once each (after a warm-up run, into a
-// scratch value array so the caller's matrix is untouched) and keep the faster.
-// Both give the same bits. While capturing a graph without a tuned choice the
-// fused gather is used (it allocates nothing).
+// Algorithm choice for FGPU_ALGO_AUTO: the two-phase assembly (element
+// buffer + gather map) when its buffers exist or fit in free device memory
+// with a 10 % margin, else the fused gather (no extra memory). The choice
+// depends on memory only, never on timings, so AUTO results are reproducible.
 // ---------------------------------------------------------------------------
-static std::mutex g_asm_tune_mutex;
-static std::map<std::tuple<int, int, int, int64_t, int64_t>, int> g_asm_tune;
-
-static int tuned_assembly_algo(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* recs) {
-    const auto key = std::make_tuple(ctx->device, A->space->order, A->precision, A->space->mesh->nt, A->nnz);
-    {
-        std::lock_guard<std::mutex> lock(g_asm_tune_mutex);
-        auto it = g_asm_tune.find(key);
-        if (it != g_asm_tune.end()) return it->second;
-    }
+static int auto_assembly_algo(fgpu_ctx* ctx, const fgpu_matrix* A) {
+    const fgpu_space* V = A->space;
+    const int64_t nt = V->mesh->nt;
+    const int n = V->n, ntri = n * (n + 1) / 2;
+    size_t need = 0;
+    const size_t kb = (size_t)nt * ntri * (A->precision == FGPU_F64 ? 8 : 4);
+    if (A->kbuf_bytes < kb) need += kb;
+    if (!V->d_gptr) need += ((size_t)nt * n * n + (size_t)A->pattern->nnz * 2 + 1) * sizeof(uint32_t);
+    if (need == 0) return FGPU_ALGO_TWO_PHASE;
     if (ctx->capturing) return FGPU_ALGO_GATHER;
-    const size_t vbytes = (size_t)A->nnz * (A->precision == FGPU_F64 ? 8 : 4);
-    void* scratch = nullptr;
-    if (cudaMalloc(&scratch, vbytes) != cudaSuccess) {
-        cudaGetLastError();
-        return FGPU_ALGO_GATHER;             // no room to tune: keep the allocation-free variant
-    }
-    void* saved = A->d_val;
-    A->d_val = scratch;
-    const int save_prof = ctx->profile;
-    ctx->profile = 0;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    float ms[2] = {0, 0};
-    const int algos[2] = {FGPU_ALGO_GATHER, FGPU_ALGO_TWO_PHASE};
-    int rc = FGPU_OK;
-    for (int v = 0; v < 2 && rc == FGPU_OK; ++v) {
-        for (int rep = 0; rep < 2 && rc == FGPU_OK; ++rep) {
-            if (rep == 1) cudaEventRecord(e0, ctx->stream);
-            rc = algos[v] == FGPU_ALGO_TWO_PHASE ? launch_assemble_two_phase(ctx, A, tab, recs, 0)
-                                                 : launch_assemble_gather_df(ctx, A, tab, recs, 0);
-            if (rep == 1) cudaEventRecord(e1, ctx->stream);
-        }
-        if (rc == FGPU_OK) {
-            cudaEventSynchronize(e1);
-            cudaEventElapsedTime(&ms[v], e0, e1);
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    ctx->profile = save_prof;
-    A->d_val = saved;
-    cudaStreamSynchronize(ctx->stream);
-    cudaFree(scratch);
-    if (rc == FGPU_ERR_ALLOC) {
-        // the element buffer did not fit: the fused gather it is
-        ctx->err.clear();
-        rc = FGPU_OK;
-        ms[1] = 1e30f;
-    }
-    if (rc) return -rc;
-    const int pick = ms[1] < ms[0] ? FGPU_ALGO_TWO_PHASE : FGPU_ALGO_GATHER;
-    if (pick != FGPU_ALGO_TWO_PHASE) {        // release the element buffer
-        cudaFree(A->d_kbuf);
-        A->d_kbuf = nullptr;
-        A->kbuf_bytes = 0;
-    }
-    std::lock_guard<std::mutex> lock(g_asm_tune_mutex);
-    g_asm_tune[key] = pick;
-    return pick;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return FGPU_ALGO_GATHER; }
+    return need + need / 10 < free_b ? FGPU_ALGO_TWO_PHASE : FGPU_ALGO_GATHER;
 }
 
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
@@ -511,10 +464,7 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
         if (rc) return rc;
         const float4* recs = reinterpret_cast<const float4*>(A->d_coef);
         int algo = f->algo;
-        if (algo == FGPU_ALGO_AUTO) {
-            algo = tuned_assembly_algo(ctx, A, tab, recs);
-            if (algo < 0) return -algo;
-        }
+        if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(ctx, A);
         rc = algo == FGPU_ALGO_TWO_PHASE ? launch_assemble_two_phase(ctx, A, tab, recs, accumulate)
                                          : launch_assemble_gather_df(ctx, A, tab, recs, accumulate);
         if (rc) return rc;

@@ -857,24 +857,6 @@ struct RecordSource {
     }
 };
 
-// Entries read back from a buffer of element matrices (upper triangles,
-// NTRI = N (N + 1) / 2 per element; tri maps (i, j) to the stored index of
-// (min, max)). The stored values are RecordSource's, so both sources give the
-// same bits.
-template <int N>
-struct BufferSource {
-    static constexpr int NTRI = N * (N + 1) / 2;
-    const void* __restrict__ kbuf;
-    const uint16_t* __restrict__ tri;  // N N (shared memory)
-    __device__ __forceinline__ df value_df(int64_t e, int li, int j) const {
-        const float2 v = __ldg(reinterpret_cast<const float2*>(kbuf) + e * NTRI + tri[li * N + j]);
-        return df{v.x, v.y};
-    }
-    __device__ __forceinline__ float value_f(int64_t e, int li, int j) const {
-        return __ldg(reinterpret_cast<const float*>(kbuf) + e * NTRI + tri[li * N + j]);
-    }
-};
-
 // One pattern row r assembled by one warp: the row's incident elements are
 // taken EPB at a time (lane = slot * N + j evaluates entry (li, j) of element
 // slot), each slot accumulates into its own copy of the row in shared memory
@@ -1177,18 +1159,25 @@ int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, c
 }
 
 // ---------------------------------------------------------------------------
-// Two-phase assembly. Phase 1 (element_tri_kernel): one thread per (element,
-// upper-triangle entry) computes K_e(i, j), i <= j, from the record; writes are
-// contiguous. Phase 2 (gather_buf_kernel): the row-owner gather of
-// gather_row_kernel reading the entries back instead of recomputing them, so
-// each entry is computed once instead of twice (once per row it belongs to)
-// and the gather becomes a streaming pass.
+// Two-phase assembly.
+//   Phase 1 (element_tri_kernel): each element matrix is computed once, as its
+//   upper triangle (NTRI = n (n + 1) / 2 entries; the reference tensors are
+//   exactly symmetric), into a device buffer; one warp per element, lanes over
+//   entries, the element's record loaded once per lane, contiguous writes.
+//   Phase 2 (gather_map_kernel): one thread per CSR entry sums its
+//   contributions in element order through a gather map built once per space
+//   (gptr: nnz + 1 offsets, gidx: buffer index of each contribution), which is
+//   the order in which the reference's element loop adds element blocks into
+//   the matrix (bilinearformcontext.hpp:784-847 -> MatSetValues ADD_VALUES).
+//   No float atomics; the gather is a streaming pass over gptr, gidx and the
+//   CSR values.
 // ---------------------------------------------------------------------------
 template <int MODE, int N>
 __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const float4* __restrict__ rec,
                                                           const float* __restrict__ Thg, const float* __restrict__ Tlg,
                                                           void* __restrict__ kbuf) {
     constexpr int NTRI = N * (N + 1) / 2;
+    constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;      // elements per warp pass (P1: 3)
     __shared__ float Th[7 * NTRI];
     __shared__ float Tl[MODE == kModeDF64 ? 7 * NTRI : 1];
     for (int k = threadIdx.x; k < 7 * NTRI; k += blockDim.x) {
@@ -1196,46 +1185,244 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
         if (MODE == kModeDF64) Tl[k] = Tlg[k];
     }
     __syncthreads();
-    const int64_t total = nt * NTRI;
-    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t e = g / NTRI;
-        const int t = (int)(g - e * NTRI);
-        if (MODE == kModeDF64) {
-            const df v = record_entry_df(rec + 4 * e, Th, Tl, NTRI, t);
-            reinterpret_cast<float2*>(kbuf)[g] = make_float2(v.hi, v.lo);
-        } else {
-            reinterpret_cast<float*>(kbuf)[g] = record_entry_f(rec + 4 * e, Th, NTRI, t);
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / NTRI < EPW ? lane / NTRI : EPW;  // element slot of this lane (EPW: idle)
+    const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
+    const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
+        const int64_t e = e0 + sub;
+        if (sub >= EPW || e >= nt) continue;
+        const float4* rp = rec + 4 * e;
+        for (int t = t0; t < NTRI; t += (EPW > 1 ? NTRI : 32)) {
+            if (MODE == kModeDF64) {
+                const df v = record_entry_df(rp, Th, Tl, NTRI, t);
+                reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = make_float2(v.hi, v.lo);
+            } else {
+                reinterpret_cast<float*>(kbuf)[e * NTRI + t] = record_entry_f(rp, Th, NTRI, t);
+            }
         }
     }
 }
 
-template <int MODE, int N, int EPB>
-__global__ void __launch_bounds__(256) gather_buf_kernel(
-    int64_t nrows, const int64_t* __restrict__ sia, const int64_t* __restrict__ inc_ptr,
-    const int32_t* __restrict__ inc, const uint8_t* __restrict__ posg, const void* __restrict__ kbuf,
-    const uint16_t* __restrict__ trig, int maxrow, void* __restrict__ valv, int accumulate, int* __restrict__ status) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint16_t* tri = reinterpret_cast<uint16_t*>(smem);
-    for (int k = threadIdx.x; k < N * N; k += blockDim.x) tri[k] = trig[k];
-    const int tbytes = (N * N * 2 + 15) & ~15;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    constexpr int ACCW = MODE == kModeDF64 ? 2 : 1;
-    float* acc = reinterpret_cast<float*>(smem + tbytes) + (size_t)warp * EPB * maxrow * ACCW;
-    __syncthreads();
-    for (int k = lane; k < EPB * maxrow * ACCW; k += 32) acc[k] = 0.0f;
-    __syncwarp();
-    const BufferSource<N> src{kbuf, tri};
-    for (int64_t r = (int64_t)blockIdx.x * wpb + warp; r < nrows; r += (int64_t)gridDim.x * wpb)
-        gather_row<MODE, N, EPB>(r, sia, inc_ptr, inc, posg, src, maxrow, valv, accumulate, status, acc, lane);
+template <int MODE>
+__global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
+                                                         const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
+                                                         void* __restrict__ valv, int accumulate) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p0 = __ldg(gptr + k), p1 = __ldg(gptr + k + 1);
+        // contributions in batches of 4: the index and value loads of a batch
+        // are issued together, the sum stays in element order
+        if (MODE == kModeDF64) {
+            const float2* kb = reinterpret_cast<const float2*>(kbuf);
+            df s{0.0f, 0.0f};
+            for (uint32_t p = p0; p < p1; p += 4) {
+                uint32_t ix[4];
+                float2 v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + ix[u]) : make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (p + u < p1) s = (p + u == p0) ? df{v[u].x, v[u].y} : df_add(s, df{v[u].x, v[u].y});
+            }
+            double* out = reinterpret_cast<double*>(valv) + k;
+            if (accumulate) s = df_add(d2df(*out), s);
+            *out = df2d(s);
+        } else {
+            const float* kb = reinterpret_cast<const float*>(kbuf);
+            float s = 0.0f;
+            for (uint32_t p = p0; p < p1; p += 4) {
+                uint32_t ix[4];
+                float v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + ix[u]) : 0.0f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (p + u < p1) s = (p + u == p0) ? v[u] : f_add(s, v[u]);
+            }
+            float* out = reinterpret_cast<float*>(valv) + k;
+            *out = accumulate ? f_add(*out, s) : s;
+        }
+    }
 }
 
-template <int MODE, int N, int EPB>
+// ---- gather map construction (once per space) ----
+// contributions per CSR entry (integer atomics: the counts do not depend on order)
+__global__ void map_count_kernel(int64_t nt, int n, const int32_t* __restrict__ l2n, const int64_t* __restrict__ ia,
+                                 const uint8_t* __restrict__ pos, uint32_t* __restrict__ cnt) {
+    const int64_t total = nt * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t / (n * n);
+        const int i = (int)((t - e * n * n) / n);
+        atomicAdd(cnt + ia[l2n[e * n + i]] + pos[t], 1u);
+    }
+}
+
+// exclusive scan of uint32 counts in chunks of kScanChunk: per-chunk sums, a
+// one-block scan of the sums, then the chunks with their offsets
+constexpr int kScanChunk = 4096;
+__global__ void scan_chunk_sums_kernel(int64_t n, const uint32_t* __restrict__ in, unsigned long long* __restrict__ sums) {
+    __shared__ unsigned long long sh[32];
+    const int64_t c0 = (int64_t)blockIdx.x * kScanChunk;
+    unsigned long long s = 0;
+    for (int k = threadIdx.x; k < kScanChunk; k += blockDim.x)
+        if (c0 + k < n) s += in[c0 + k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+        sums[blockIdx.x] = t;
+    }
+}
+// one block of 1024 threads: each thread scans a contiguous segment of the sums
+__global__ void __launch_bounds__(1024) scan_sums_kernel(int64_t nchunks, unsigned long long* __restrict__ sums) {
+    __shared__ unsigned long long part[1024];
+    const int64_t seg = (nchunks + 1023) / 1024;
+    const int64_t b = threadIdx.x * seg, e = min(b + seg, nchunks);
+    unsigned long long t = 0;
+    for (int64_t c = b; c < e; ++c) t += sums[c];
+    part[threadIdx.x] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long run = 0;
+        for (int k = 0; k < 1024; ++k) {
+            const unsigned long long v = part[k];
+            part[k] = run;
+            run += v;
+        }
+        sums[nchunks] = run;
+    }
+    __syncthreads();
+    unsigned long long run = part[threadIdx.x];
+    for (int64_t c = b; c < e; ++c) {
+        const unsigned long long v = sums[c];
+        sums[c] = run;
+        run += v;
+    }
+}
+__global__ void scan_chunks_kernel(int64_t n, const uint32_t* __restrict__ in, const unsigned long long* __restrict__ sums,
+                                   uint32_t* __restrict__ out) {
+    // one warp per chunk, sequential over 32-entry strips with warp prefix sums
+    const int64_t c = blockIdx.x;
+    const int lane = threadIdx.x;
+    unsigned long long run = sums[c];
+    for (int64_t b = c * kScanChunk; b < min((c + 1) * kScanChunk, n); b += 32) {
+        const int64_t k = b + lane;
+        const uint32_t v = k < n ? in[k] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (k < n) out[k] = (uint32_t)(run + x - v);
+        run += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (c == gridDim.x - 1 && lane == 0) out[n] = (uint32_t)sums[gridDim.x];
+}
+
+// fill: one warp per row, incident elements in element order, lanes over the
+// element row's columns (distinct entries), a per-entry cursor in shared memory
+__global__ void __launch_bounds__(256) map_fill_kernel(int64_t nrows, int n, int ntri, const int64_t* __restrict__ ia,
+                                                       const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                                       const uint8_t* __restrict__ pos, const uint16_t* __restrict__ trig,
+                                                       const uint32_t* __restrict__ gptr, uint32_t* __restrict__ gidx,
+                                                       int* __restrict__ status) {
+    __shared__ uint32_t cur[8][256];
+    __shared__ uint16_t tri[400];
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) tri[k] = trig[k];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t r = (int64_t)blockIdx.x * 8 + warp; r < nrows; r += (int64_t)gridDim.x * 8) {
+        const int64_t start = ia[r];
+        const int len = (int)(ia[r + 1] - start);
+        if (len > 256) {
+            if (lane == 0) atomicOr(status, kStatusRowOverflow);
+            continue;
+        }
+        for (int k = lane; k < len; k += 32) cur[warp][k] = gptr[start + k];
+        __syncwarp();
+        for (int64_t t = inc_ptr[r]; t < inc_ptr[r + 1]; ++t) {
+            const int32_t code = inc[t];
+            const int64_t e = code >> 5;
+            const int li = code & 31;
+            if (lane < n) {
+                const int p = pos[(e * n + li) * n + lane];
+                const uint32_t slot = cur[warp][p];
+                cur[warp][p] = slot + 1;
+                gidx[slot] = (uint32_t)(e * ntri + tri[li * n + lane]);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
+    if (V->d_gptr) return FGPU_OK;
+    const DevPattern& P = *V->pattern;
+    const int n = V->n;
+    const int64_t nt = V->mesh->nt, nnz = P.nnz;
+    const int64_t contrib = nt * n * n;
+    if (contrib >= (int64_t)UINT32_MAX || nt * (int64_t)(n * (n + 1) / 2) >= (int64_t)UINT32_MAX) {
+        ctx->err = "gather map: more than 2^32 contributions";
+        return FGPU_ERR_INVALID;
+    }
+    if (!V->d_pos) { ctx->err = "gather map: no position table"; return FGPU_ERR_INVALID; }
+    std::string err;
+    DevTables* tab = get_dev_tables(V->order, 2 * V->order, err);
+    if (!tab) { ctx->err = err; return FGPU_ERR_INVALID; }
+    uint32_t *cnt = nullptr, *gptr = nullptr, *gidx = nullptr;
+    unsigned long long* sums = nullptr;
+    const int64_t nchunks = (nnz + kScanChunk - 1) / kScanChunk;
+    cudaError_t e = cudaMalloc(&cnt, nnz * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&gptr, (nnz + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&gidx, contrib * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&sums, (nchunks + 1) * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(cnt); cudaFree(gptr); cudaFree(gidx); cudaFree(sums);
+        ctx->err = "gather map: allocation failed";
+        return FGPU_ERR_ALLOC;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    cudaMemsetAsync(cnt, 0, nnz * sizeof(uint32_t), ctx->stream);
+    map_count_kernel<<<sms * 16, 256, 0, ctx->stream>>>(nt, n, V->d_l2n, P.d_ia, V->d_pos, cnt);
+    scan_chunk_sums_kernel<<<(int)nchunks, 256, 0, ctx->stream>>>(nnz, cnt, sums);
+    scan_sums_kernel<<<1, 1024, 0, ctx->stream>>>(nchunks, sums);
+    scan_chunks_kernel<<<(int)nchunks, 32, 0, ctx->stream>>>(nnz, cnt, sums, gptr);
+    map_fill_kernel<<<sms * 8, 256, 0, ctx->stream>>>(P.nrows, n, n * (n + 1) / 2, P.d_ia, V->d_inc_ptr, V->d_inc, V->d_pos,
+                                                      tab->d_tri, gptr, gidx, ctx->d_status);
+    ctx->launches += 5;
+    e = cudaGetLastError();
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(cnt);
+    cudaFree(sums);
+    if (e != cudaSuccess) {
+        cudaFree(gptr); cudaFree(gidx);
+        ctx->err = std::string("gather map: ") + cudaGetErrorString(e);
+        return FGPU_ERR_CUDA;
+    }
+    V->d_gptr = gptr;
+    V->d_gidx = gidx;
+    return FGPU_OK;
+}
+
+template <int MODE, int N>
 static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
-    const DevPattern& P = *A->pattern;
-    const fgpu_space* V = A->space;
+    fgpu_space* V = A->space;
     const int64_t nt = V->mesh->nt;
     constexpr int NTRI = N * (N + 1) / 2;
+    if (!V->d_gptr) {
+        if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (gather map)"; return FGPU_ERR_INVALID; }
+        int rc = launch_build_gather_map(ctx, V);
+        if (rc) return rc;
+    }
     const size_t need = (size_t)nt * NTRI * (MODE == kModeDF64 ? 8 : 4);
     if (A->kbuf_bytes < need) {
         if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (element buffer)"; return FGPU_ERR_INVALID; }
@@ -1248,28 +1435,20 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     {
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nt * NTRI + 255) / 256, (int64_t)sms * 16));
+        constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;
+        const int64_t warps = (nt + EPW - 1) / EPW;
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)sms * 16));
         PendingEvent ev;
         prof_begin(ctx, "assemble_elements", ev);
         element_tri_kernel<MODE, N><<<(int)blocks, 256, 0, ctx->stream>>>(nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     }
-    const int threads = 256, wpb = threads / 32;
-    const size_t tbytes = ((size_t)N * N * 2 + 15) & ~(size_t)15;
-    const size_t smem = tbytes + (size_t)wpb * EPB * P.max_row * (MODE == kModeDF64 ? 8 : 4);
-    auto kern = gather_buf_kernel<MODE, N, EPB>;
-    if (P.max_row > 256) { ctx->err = "pattern rows longer than 256 entries"; return FGPU_ERR_INVALID; }
-    if (smem > 227 * 1024) { ctx->err = "pattern rows too long for the gather kernel"; return FGPU_ERR_INVALID; }
-    if (smem > 48 * 1024) FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
-    const int64_t need_blocks = (P.nrows + wpb - 1) / wpb;
-    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(need_blocks, (int64_t)std::max(per_sm, 1) * sms));
+    const int64_t nnz = A->pattern->nnz;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, (int64_t)sms * 32));
     PendingEvent ev;
     prof_begin(ctx, "assemble_gather", ev);
-    kern<<<(int)blocks, threads, smem, ctx->stream>>>(P.nrows, P.d_ia, V->d_inc_ptr, V->d_inc, V->d_pos, A->d_kbuf, tab->d_tri,
-                                                      P.max_row, A->d_val, accumulate, ctx->d_status);
+    gather_map_kernel<MODE><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
@@ -1279,12 +1458,12 @@ int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* ta
     const int order = A->space->order;
     const bool f32 = A->precision == FGPU_F32;
     if (A->ncomp != 1) { ctx->err = "Laplace/mass form needs a scalar space"; return FGPU_ERR_INVALID; }
-    if (order == 1) return f32 ? run_two_phase<kModeF32, 4, 8>(ctx, A, tab, rec, accumulate)
-                               : run_two_phase<kModeDF64, 4, 8>(ctx, A, tab, rec, accumulate);
-    if (order == 2) return f32 ? run_two_phase<kModeF32, 10, 3>(ctx, A, tab, rec, accumulate)
-                               : run_two_phase<kModeDF64, 10, 3>(ctx, A, tab, rec, accumulate);
-    if (order == 3) return f32 ? run_two_phase<kModeF32, 20, 1>(ctx, A, tab, rec, accumulate)
-                               : run_two_phase<kModeDF64, 20, 1>(ctx, A, tab, rec, accumulate);
+    if (order == 1) return f32 ? run_two_phase<kModeF32, 4>(ctx, A, tab, rec, accumulate)
+                               : run_two_phase<kModeDF64, 4>(ctx, A, tab, rec, accumulate);
+    if (order == 2) return f32 ? run_two_phase<kModeF32, 10>(ctx, A, tab, rec, accumulate)
+                               : run_two_phase<kModeDF64, 10>(ctx, A, tab, rec, accumulate);
+    if (order == 3) return f32 ? run_two_phase<kModeF32, 20>(ctx, A, tab, rec, accumulate)
+                               : run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, accumulate);
     ctx->err = "unsupported order";
     return FGPU_ERR_INVALID;
 }

@@ -168,14 +168,18 @@ __global__ void __launch_bounds__(256) spmv_kernel(int64_t nrows, const int64_t*
     typename PL::D dsum = PL::dzero();
     for (int64_t r0 = (int64_t)blockIdx.x * gpb; r0 < nrows; r0 += (int64_t)gridDim.x * gpb) {
         const int64_t r = r0 + g;
-        typename PL::A s = PL::zero();
+        // row sums accumulate in the dot-product type D (binary64, or df64 for the
+        // binary32 and df64 policies): a binary32 row sum of a smooth vector loses
+        // up to kappa(A) u32 to cancellation, which stalls CG on stiff systems
+        typename PL::D sd = PL::dzero();
         if (r < nrows) {
             const int64_t pe = ia[r + 1];
-            for (int64_t p = ia[r] + lane; p < pe; p += G) s = PL::madd(s, PL::ldv(val[p]), PL::ld(x[ja[p]]));
+            for (int64_t p = ia[r] + lane; p < pe; p += G) sd = PL::dmadd(sd, PL::ldv(val[p]), PL::ld(x[ja[p]]));
         }
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) s = PL::add(s, PL::shfl_xor(s, o));
+        for (int o = G / 2; o > 0; o >>= 1) sd = PL::dadd(sd, PL::dshfl_xor(sd, o));
         if (r < nrows && lane == 0) {
+            const typename PL::A s = PL::from_d(sd);
             const typename PL::S v = PL::st(mode == 1 ? PL::sub(PL::ld(b[r]), s) : s);
             y[r] = v;
             if (wdot) dsum = PL::dmadd(dsum, PL::ld(wdot[r]), PL::ld(v));

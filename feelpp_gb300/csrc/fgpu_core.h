@@ -145,6 +145,8 @@ struct fgpu_space {
     std::shared_ptr<DevPattern> pattern;   // scalar node pattern, built on demand
     fgpu::NodePattern h_pattern;
     uint8_t* d_pos = nullptr;        // T x n x n: position of node l2n[e][j] in row l2n[e][i] (rows <= 255)
+    uint32_t* d_gptr = nullptr;      // two-phase gather map: nnz + 1 offsets into d_gidx
+    uint32_t* d_gidx = nullptr;      // T n n element-buffer indices, per CSR entry in element order
 };
 
 struct SellLayout {                  // SELL-C-sigma (C = 32, sigma = 256) copy of a CSR pattern
@@ -224,6 +226,7 @@ int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kap
                        float4* d_rec, const double* d_kscale = nullptr);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);
 int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V);
 
 // One problem of a batch (device-side descriptor, built by batch.cu).

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <functional>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "df64.h"
@@ -490,6 +491,26 @@ static int mf_residual64(fgpu_ctx* ctx, fgpu_operator* op, const double* b, cons
     return FGPU_OK;
 }
 
+// binary64 PCG with residual replacement at each convergence claim of the
+// recurrence (q: scratch vector of n doubles)
+static int mf_plain_solve(fgpu_ctx* ctx, fgpu_operator* op, const double* d_b, double* d_x, CgOptions o,
+                          const fgpu_solver_cfg* cfg, double bn, double* q, CgResult* res) {
+    o.delta = 0.0;
+    int stagnant = 0;
+    double rlast = 0;
+    RefreshFn<PolF64> refresh = [&](double* xd, double* rd, bool* conv) -> int {
+        double r2n = 0;
+        const int r2 = mf_residual64(ctx, op, d_b, xd, rd, q, &r2n);
+        if (r2) return r2;
+        *conv = r2n <= cfg->rtol * bn;
+        stagnant = (rlast > 0 && r2n > 0.5 * rlast) ? stagnant + 1 : 0;
+        rlast = r2n;
+        if (!*conv && stagnant >= 2) return kRefreshStagnated;
+        return FGPU_OK;
+    };
+    return mf_pcg_core<PolF64>(ctx, op, d_b, d_x, o, cfg->pc, res, &refresh);
+}
+
 int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const double* d_b, double* d_x,
                       const fgpu_solver_cfg* cfg, fgpu_solve_stats* st) {
     const int64_t n = op->nnodes;
@@ -501,68 +522,86 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
     CgResult res;
     int rc = FGPU_OK, fail = 0, fallback = 0, fallback_its = 0;
     double rn = 0, bn = host_norm(ctx, n, d_b);
-    double *r = nullptr, *q = nullptr;
-    if (cudaMalloc(&r, n * sizeof(double)) != cudaSuccess || cudaMalloc(&q, n * sizeof(double)) != cudaSuccess) {
-        cudaFree(r);
+    double *r = nullptr, *q = nullptr, *xc = nullptr, *r2b = nullptr;
+    if (cudaMalloc(&r, n * sizeof(double)) != cudaSuccess || cudaMalloc(&q, n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&xc, n * sizeof(double)) != cudaSuccess || cudaMalloc(&r2b, n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(r); cudaFree(q); cudaFree(xc);
         ctx->err = "matrix-free solve: allocation failed";
         return FGPU_ERR_ALLOC;
     }
+    const int vb = vec_blocks(n);
     if (!cfg->mixed) {
         if (op->precision == FGPU_F32) { ctx->err = "the plain matrix-free solve needs a binary64 operator"; rc = FGPU_ERR_INVALID; }
         else {
-            rc = mf_pcg_core<PolF64>(ctx, op, d_b, d_x, opt, cfg->pc, &res);
-            fail = res.fail;
-            res.nrefresh = 1;
+            rc = mf_plain_solve(ctx, op, d_b, d_x, opt, cfg, bn, q, &res);
+            fail = res.fail == 3 ? 2 : res.fail;
         }
     } else {
         if (!op32 || op32->precision != FGPU_F32 || op32->space != op->space) { ctx->err = "mixed matrix-free solve needs a binary32 inner operator on the same space"; rc = FGPU_ERR_INVALID; }
         float *r32 = nullptr, *d32 = nullptr;
         if (rc == FGPU_OK && (cudaMalloc(&r32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&d32, n * sizeof(float)) != cudaSuccess)) {
+            cudaGetLastError();
             ctx->err = "mixed matrix-free solve: allocation failed";
             rc = FGPU_ERR_ALLOC;
         }
         // reliable updates: the binary32 CG runs on the residual equation with
         // its own search direction; every delta reduction of its recurrence
         // residual (and at its claimed convergence) the correction is folded
-        // into the binary64 solution and the residual replaced by b - A64 x.
-        if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+        // into the binary64 solution, when that lowers the binary64 residual,
+        // and the residual replaced by b - A64 x. A rejected fold, or two in a
+        // row that do not halve the residual, end the binary32 phase.
+        double* rbest = r;
+        double* rcand = r2b;
+        if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, rbest, q, &rn);
         if (rc == FGPU_OK && !(bn == 0.0 || rn <= cfg->rtol * bn)) {
-            const int vb = vec_blocks(n);
             const double scale = rn;   // binary32 system scaled to a unit initial residual
-            d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, r, r32, 1.0 / scale);
+            d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, rbest, r32, 1.0 / scale);
             cudaMemsetAsync(d32, 0, n * sizeof(float), ctx->stream);
             ctx->launches++;
             int stagnant = 0;
-            RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
-                fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, xl, scale);
+            auto fold = [&](float* xl, bool* accepted) -> int {
+                cudaMemcpyAsync(xc, d_x, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+                fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, xc, xl, scale);
                 ctx->launches++;
-                const double rprev = rn;
-                const int r2 = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                double rn_c = 0;
+                const int r2 = mf_residual64(ctx, op, d_b, xc, rcand, q, &rn_c);
                 if (r2) return r2;
-                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, r, rl, 1.0 / scale);
+                *accepted = rn_c < rn;
+                if (*accepted) {
+                    stagnant = rn_c > 0.5 * rn ? stagnant + 1 : 0;
+                    cudaMemcpyAsync(d_x, xc, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+                    std::swap(rbest, rcand);
+                    rn = rn_c;
+                }
+                return FGPU_OK;
+            };
+            RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
+                bool ok = false;
+                const int r2 = fold(xl, &ok);
+                if (r2) return r2;
+                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, rbest, rl, 1.0 / scale);
                 ctx->launches++;
                 *conv = rn <= cfg->rtol * bn;
-                stagnant = (rn > 0.5 * rprev) ? stagnant + 1 : 0;
-                if (!*conv && stagnant >= 2) return kRefreshStagnated;
+                if (!*conv && (!ok || stagnant >= 2)) return kRefreshStagnated;
                 return FGPU_OK;
             };
             CgOptions o32 = opt;
             o32.rtol = cfg->rtol * bn / rn;   // the binary32 system starts from a unit residual
             rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, o32, cfg->pc, &res, &refresh);
             if (rc == FGPU_OK && !res.true_conv) {
-                fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, d32, scale);
-                ctx->launches++;
-                rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                bool ok = false;
+                if (res.fail != 3) rc = fold(d32, &ok);
                 if (rc == FGPU_OK && rn > cfg->rtol * bn) {
-                    if ((res.fail == 1 || res.fail == 3) && res.iters < cfg->maxit) {
-                        // binary32 breakdown or stagnation: finish with the binary64 operator from the current x
+                    if (res.fail != 0 && res.iters < cfg->maxit) {
+                        // binary32 breakdown or stagnation: finish with the binary64 operator from the best iterate
                         CgResult r64;
                         CgOptions o64 = opt;
                         o64.maxit = cfg->maxit - res.iters;
-                        rc = mf_pcg_core<PolF64>(ctx, op, d_b, d_x, o64, cfg->pc, &r64);
+                        rc = mf_plain_solve(ctx, op, d_b, d_x, o64, cfg, bn, q, &r64);
                         fallback = 1;
                         fallback_its = r64.iters;
-                        if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+                        if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, rbest, q, &rn);
                         if (rc == FGPU_OK && r64.fail == 1) fail = 1;
                         else if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
                     } else {
@@ -574,9 +613,14 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
         cudaFree(r32);
         cudaFree(d32);
     }
-    if (rc == FGPU_OK && !cfg->mixed) rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+    if (rc == FGPU_OK && !cfg->mixed) {
+        rc = mf_residual64(ctx, op, d_b, d_x, r, q, &rn);
+        if (rc == FGPU_OK && fail == 0 && rn > cfg->rtol * bn) fail = 2;
+    }
     cudaFree(r);
     cudaFree(q);
+    cudaFree(xc);
+    cudaFree(r2b);
     cudaEventRecord(e1, ctx->stream);
     cudaEventSynchronize(e1);
     float ms = 0;
@@ -586,7 +630,7 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
     if (rc != FGPU_OK) return rc;
     if (st) {
         st->iterations = res.iters + fallback_its;
-        st->outer = res.nrefresh;
+        st->outer = cfg->mixed ? res.nrefresh : 1;
         st->rel_residual = bn > 0 ? rn / bn : 0.0;
         st->time_ms = ms;
         st->eig_max = res.lmax;

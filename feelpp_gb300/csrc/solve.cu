@@ -215,11 +215,12 @@ __global__ void __launch_bounds__(256) sell_spmv_kernel(int64_t nrows, int64_t n
         const int64_t s = i / kSellC;
         const int L = slice_len[s];
         const int64_t base = slice_ptr[s] + (i - s * kSellC);
-        typename PL::A acc = PL::zero();
+        typename PL::D accd = PL::dzero();     // row sums in the dot-product type (see spmv_kernel)
         for (int k = 0; k < L; ++k) {
             const int64_t j = base + (int64_t)k * kSellC;
-            acc = PL::madd(acc, PL::ldv(val[j]), PL::ld(x[col[j]]));
+            accd = PL::dmadd(accd, PL::ldv(val[j]), PL::ld(x[col[j]]));
         }
+        const typename PL::A acc = PL::from_d(accd);
         if (i < nrows) {
             const int32_t row = perm[i];
             const typename PL::S v = PL::st(mode == 1 ? PL::sub(PL::ld(b[row]), acc) : acc);
@@ -401,11 +402,49 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
-    const CgOptions opt = cg_options(cfg);
+    CgOptions opt = cg_options(cfg);
+    opt.delta = 0.0;             // replace the residual only when the recurrence claims convergence
     CgResult res;
     const int64_t n = A->nrows;
     double rn = 0;
     int rc = FGPU_OK;
+    // Residual replacement: when the recurrence residual claims convergence, the
+    // true residual b - A x is computed; if it misses rtol (the recurrence drifts
+    // on stiff systems) it replaces r and the iteration goes on from p = z.
+    Scratch64 R;
+    if (!R.alloc(n)) { ctx->err = "solve: allocation failed"; return FGPU_ERR_ALLOC; }
+    double bn0 = 0;
+    {
+        const int vb = vec_blocks(n);
+        norm2_partial_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_b, R.partial);
+        cudaMemcpyAsync(R.hpart, R.partial, vb * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        for (int k = 0; k < vb; ++k) bn0 += R.hpart[k];
+        bn0 = std::sqrt(bn0);
+    }
+    int stagnant = 0;
+    double rlast = 0;
+    auto check_true = [&](const double* xd, double* rout, bool* conv) -> int {
+        double r2n = 0;
+        const int r2 = f64_residual(ctx, A, d_b, xd, rout, R.partial, R.hpart, &r2n);
+        if (r2) return r2;
+        *conv = r2n <= cfg->rtol * bn0;
+        stagnant = (rlast > 0 && r2n > 0.5 * rlast) ? stagnant + 1 : 0;
+        rlast = r2n;
+        if (!*conv && stagnant >= 2) return kRefreshStagnated;
+        return FGPU_OK;
+    };
+    RefreshFn<PolF64> refresh64 = [&](double* xd, double* rd, bool* conv) -> int { return check_true(xd, rd, conv); };
+    double* xtmp = nullptr;
+    RefreshFn<PolDF64> refresh_df = [&](float2* xd, float2* rd, bool* conv) -> int {
+        if (!xtmp && cudaMalloc(&xtmp, n * sizeof(double)) != cudaSuccess) { cudaGetLastError(); ctx->err = "solve: allocation failed"; return FGPU_ERR_ALLOC; }
+        df2d_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, xd, xtmp);
+        const int r2 = check_true(xtmp, R.r, conv);
+        if (r2) return r2;
+        d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, R.r, rd);
+        ctx->launches += 2;
+        return FGPU_OK;
+    };
     if (cfg->arith == FGPU_ARITH_DF64) {
         float2 *val = nullptr, *b = nullptr, *x = nullptr;
         if (cudaMalloc(&val, A->nnz * sizeof(float2)) != cudaSuccess || cudaMalloc(&b, n * sizeof(float2)) != cudaSuccess ||
@@ -418,7 +457,7 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
             d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_b, b);
             d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_x, x);
             ctx->launches += 3;
-            rc = pcg_core<PolDF64>(ctx, A, val, b, x, opt, cfg->pc, &res);
+            rc = pcg_core<PolDF64>(ctx, A, val, b, x, opt, cfg->pc, &res, &refresh_df);
             if (rc == FGPU_OK) {
                 df2d_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, x, d_x);
                 ctx->launches++;
@@ -426,13 +465,11 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
         }
         cudaFree(val); cudaFree(b); cudaFree(x);
     } else {
-        rc = pcg_core<PolF64>(ctx, A, (const double*)A->d_val, d_b, d_x, opt, cfg->pc, &res);
+        rc = pcg_core<PolF64>(ctx, A, (const double*)A->d_val, d_b, d_x, opt, cfg->pc, &res, &refresh64);
     }
-    if (rc == FGPU_OK) {  // final residual recomputed in binary64 from the matrix
-        Scratch64 S;
-        if (!S.alloc(n)) { ctx->err = "residual: allocation failed"; rc = FGPU_ERR_ALLOC; }
-        else rc = f64_residual(ctx, A, d_b, d_x, S.r, S.partial, S.hpart, &rn);
-    }
+    cudaFree(xtmp);
+    if (rc == FGPU_OK)    // final residual recomputed in binary64 from the matrix
+        rc = f64_residual(ctx, A, d_b, d_x, R.r, R.partial, R.hpart, &rn);
     cudaEventRecord(e1, ctx->stream);
     cudaEventSynchronize(e1);
     float ms = 0;
@@ -440,8 +477,10 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != FGPU_OK) return rc;
-    const double bn = std::sqrt(res.bb);
-    const int fail = res.fail;
+    const double bn = bn0;
+    int fail = res.fail;
+    if (fail == 0 && rn > cfg->rtol * bn) fail = 2;      // maxit with the recurrence short of rtol
+    if (fail == 3) fail = 2;                             // the true residual stopped decreasing
     if (st) {
         st->iterations = res.iters;
         st->outer = 1;
@@ -459,7 +498,11 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
 int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A32, const double* d_b, double* d_x,
                     const fgpu_solver_cfg* cfg, fgpu_solve_stats* st) {
     // Mixed precision with reliable updates: binary32 CG on A32 for the
-    // correction, binary64 solution and binary64 residual replacement.
+    // correction (scaled to a unit initial residual), binary64 solution and
+    // binary64 residual replacement. A replacement is accepted only when it
+    // lowers the binary64 residual (the solution is the best iterate so far);
+    // a rejected one, or two in a row that do not halve it, end the binary32
+    // phase (stagnation) and the solve finishes in FP64 from the best iterate.
     const int64_t n = A64->nrows;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -472,10 +515,15 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
     {
         Scratch64 S;
         float *r32 = nullptr, *x32 = nullptr;
-        if (!S.alloc(n) || cudaMalloc(&r32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&x32, n * sizeof(float)) != cudaSuccess) {
+        double *xc = nullptr, *rc64 = nullptr;
+        if (!S.alloc(n) || cudaMalloc(&r32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&x32, n * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&xc, n * sizeof(double)) != cudaSuccess || cudaMalloc(&rc64, n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
             ctx->err = "mixed solve: allocation failed";
             rc = FGPU_ERR_ALLOC;
         }
+        double* rbest = S.r;      // binary64 residual of the current solution
+        double* rcand = rc64;
         if (rc == FGPU_OK) {
             const int vb = vec_blocks(n);
             norm2_partial_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_b, S.partial);
@@ -484,45 +532,62 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
             double s2 = 0;
             for (int k = 0; k < vb; ++k) s2 += S.hpart[k];
             bn = std::sqrt(s2);
-            rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+            rc = f64_residual(ctx, A64, d_b, d_x, rbest, S.partial, S.hpart, &rn);
             if (rc == FGPU_OK && !(bn == 0.0 || rn <= cfg->rtol * bn)) {
                 const double scale = rn;   // binary32 system scaled to a unit initial residual
-                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, r32, 1.0 / scale);
+                d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, rbest, r32, 1.0 / scale);
                 cudaMemsetAsync(x32, 0, n * sizeof(float), ctx->stream);
                 int stagnant = 0;
-                RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
-                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, xl, scale);
-                    const double rprev = rn;
-                    int r2 = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+                // candidate x + scale x_lo; accepted when its binary64 residual is lower
+                auto fold = [&](float* xl, bool* accepted) -> int {
+                    cudaMemcpyAsync(xc, d_x, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, xc, xl, scale);
+                    ctx->launches++;
+                    double rn_c = 0;
+                    const int r2 = f64_residual(ctx, A64, d_b, xc, rcand, S.partial, S.hpart, &rn_c);
                     if (r2) return r2;
-                    d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, S.r, rl, 1.0 / scale);
-                    ctx->launches += 2;
+                    *accepted = rn_c < rn;
+                    if (*accepted) {
+                        stagnant = rn_c > 0.5 * rn ? stagnant + 1 : 0;
+                        cudaMemcpyAsync(d_x, xc, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+                        std::swap(rbest, rcand);
+                        rn = rn_c;
+                    }
+                    return FGPU_OK;
+                };
+                RefreshFn<PolF32> refresh = [&](float* xl, float* rl, bool* conv) -> int {
+                    bool ok = false;
+                    const int r2 = fold(xl, &ok);
+                    if (r2) return r2;
+                    d2f_scaled_kernel<<<vb, 256, 0, ctx->stream>>>(n, rbest, rl, 1.0 / scale);
+                    ctx->launches++;
                     *conv = rn <= cfg->rtol * bn;
-                    // two replacements in a row without halving the residual: stagnation
-                    stagnant = (rn > 0.5 * rprev) ? stagnant + 1 : 0;
-                    if (!*conv && stagnant >= 2) return kRefreshStagnated;
+                    if (!*conv && (!ok || stagnant >= 2)) return kRefreshStagnated;
                     return FGPU_OK;
                 };
                 CgOptions o32 = cg_options(cfg);
                 o32.rtol = cfg->rtol * bn / rn;   // the binary32 system starts from a unit residual
                 rc = pcg_core<PolF32>(ctx, A32, (const float*)A32->d_val, r32, x32, o32, cfg->pc, &res, &refresh);
                 if (rc == FGPU_OK && !res.true_conv) {
-                    // fold what is left and measure the binary64 residual
-                    fold_kernel<<<vb, 256, 0, ctx->stream>>>(n, d_x, x32, scale);
-                    rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
+                    bool ok = false;
+                    if (res.fail != 3) rc = fold(x32, &ok);       // what the last iterations added, if it helps
                     if (rc == FGPU_OK && rn > cfg->rtol * bn) {
-                        if ((res.fail == 1 || res.fail == 3) && res.iters < cfg->maxit) {
-                            // binary32 breakdown or stagnation (A32 = fl32(A) too far from A at
-                            // this conditioning): finish in FP64 from the current x
-                            CgResult r64;
-                            CgOptions o64 = cg_options(cfg);
-                            o64.maxit = cfg->maxit - res.iters;
-                            rc = pcg_core<PolF64>(ctx, A64, (const double*)A64->d_val, d_b, d_x, o64, cfg->pc, &r64);
-                            fallback_its = r64.iters;
+                        if (res.fail != 0 && res.iters < cfg->maxit) {
+                            // binary32 breakdown or stagnation (A32 = fl32(A) and binary32
+                            // vectors too coarse at this conditioning): finish in FP64
+                            // from the best iterate
+                            fgpu_solver_cfg c64 = *cfg;
+                            c64.mixed = 0;
+                            c64.arith = FGPU_ARITH_F64;
+                            c64.maxit = cfg->maxit - res.iters;
+                            fgpu_solve_stats s64{};
+                            const int rc64 = solve_pcg(ctx, A64, d_b, d_x, &c64, &s64);
+                            fallback_its = s64.iterations;
                             fallback = 1;
-                            if (rc == FGPU_OK) rc = f64_residual(ctx, A64, d_b, d_x, S.r, S.partial, S.hpart, &rn);
-                            if (rc == FGPU_OK && r64.fail == 1) fail = 1;
-                            else if (rc == FGPU_OK && rn > cfg->rtol * bn) fail = 2;
+                            if (rc64 == FGPU_ERR_BREAKDOWN) fail = 1;
+                            else if (rc64 == FGPU_ERR_NOT_CONVERGED) fail = 2;
+                            else rc = rc64;
+                            if (rc == FGPU_OK) rc = f64_residual(ctx, A64, d_b, d_x, rbest, S.partial, S.hpart, &rn);
                         } else {
                             fail = res.fail == 1 ? 1 : 2;
                         }
@@ -533,6 +598,8 @@ int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A3
         }
         cudaFree(r32);
         cudaFree(x32);
+        cudaFree(xc);
+        cudaFree(rc64);
     }
     cudaEventRecord(e1, ctx->stream);
     cudaEventSynchronize(e1);

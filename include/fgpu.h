@@ -50,10 +50,10 @@ extern "C" {
 #define FGPU_ALGO_COLOUR 2        /* reserved (element-coloured scatter-add); runs FGPU_ALGO_GATHER */
 #define FGPU_ALGO_GATHER_NATIVE_F64 3 /* row-owner gather in native FP64 arithmetic (FP64 matrices; the
                                      default FP64 path computes in double-float on the FP32 pipes) */
-#define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles) into a device buffer, then the
-                                     row-owner gather sums them; same bits as FGPU_ALGO_GATHER. AUTO
-                                     times both on the first call for a (device, order, precision,
-                                     mesh size) and keeps the faster */
+#define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles) into a device buffer, then one
+                                     thread per CSR entry sums its contributions in element order
+                                     through a gather map built once per space. AUTO picks it when
+                                     its buffers fit in device memory, else FGPU_ALGO_GATHER */
 
 #define FGPU_RHS_SINE 0           /* f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */
 #define FGPU_RHS_CONST_VEC 1      /* f = (c0, c1, c2) (Pchv) */

@@ -189,8 +189,9 @@ def test_deterministic_repeat(env):
 @pytest.mark.parametrize("order,n", [(1, 6), (2, 4), (3, 3)])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_two_phase_equals_fused_gather(env, order, n, precision):
-    """Element matrices buffered (upper triangles) then gathered give the same bits as the
-    fused gather, for '=' and '+='."""
+    """Element matrices buffered (upper triangles) then summed per CSR entry in element order
+    agree with the fused row-owner gather (which sums per slot) to rounding, for '=' and '+=';
+    AUTO is the two-phase path here."""
     from feelpp_gb300 import _ffi
     xyz, tets = mesh(n, perturb=0.2)
     kappa = meshgen.lognormal_kappa(len(tets))
@@ -205,4 +206,6 @@ def test_two_phase_equals_fused_gather(env, order, n, precision):
         a.assign(integral)
         a += integral
         got.append(a.values())
-    assert np.array_equal(got[0], got[1]) and np.array_equal(got[0], got[2])
+    assert np.array_equal(got[1], got[2])
+    tol = 1e-6 if precision == "f32" else 1e-14
+    assert_values_close(got[1], got[0], rtol=tol, atol=tol, what="two-phase vs fused")

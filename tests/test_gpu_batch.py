@@ -1,8 +1,8 @@
 """Batched assembly of independent problems and CUDA-graph replay (run on a GB300).
 
-A batch runs the same per-row body as the single-problem gather, with the same
-records and position tables, so every batched matrix must equal the matrix
-assembled alone bit for bit; one problem per order is also checked against the
+A batch runs the same per-row body as the single-problem row-owner gather
+(FGPU_ALGO_GATHER), with the same records and position tables, so every
+batched matrix must equal the matrix assembled alone that way bit for bit; one problem per order is also checked against the
 oracle at the FP64 tolerance."""
 import numpy as np
 import pytest
@@ -39,10 +39,13 @@ def test_batch_equals_single_assembly(env, precision):
     cfg = batch.launch_config()
     assert cfg["tuned"] and cfg["threads"] in (128, 256)
     got = [p[6].values().copy() for p in probs]
+    from feelpp_gb300 import _ffi
     for (xyz, tets, kappa, M, V, integral, a), g in zip(probs, got):
         a.zero()
+        a.algo = _ffi.ALGO_GATHER          # the single-problem row-owner gather
         a.assign(integral)
         assert np.array_equal(g, a.values())
+        a.algo = _ffi.ALGO_AUTO
     # '+=' doubles every value (the df64 path adds the stored binary64 value as a
     # double-float: 2^-48 relative; binary32 storage: one rounding)
     batch.assemble(accumulate=True)

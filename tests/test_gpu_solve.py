@@ -167,3 +167,26 @@ def test_bad_pc_name(env):
     xyz, tets, M, V, u, a, l = poisson(env, 3, 1)
     with pytest.raises(ValueError):
         a.solve(rhs=l, solution=u, pc="gamg")
+
+
+def test_stiff_elasticity_true_residual(env):
+    """A slender clamped beam (vector P2, 12x12x12 cells on [0,4]x[0,1]^2) is stiff enough
+    for the CG recurrence residual to drift from b - A x: both solves must still stop on
+    the true residual (residual replacement), and the mixed one must not return a worse
+    iterate than FP64 would (best-iterate folding, FP64 fallback on binary32 stagnation)."""
+    xyz, tets = mesh(12, perturb=0.1, lengths=(4.0, 1.0, 1.0))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, 2)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, 1.0, 0.5), fpp.grad(v))))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.cst_vec(0, 0, -1), fpp.id(v))))
+    a += fpp.on(fpp.markedfaces(M, 0.0), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    st64 = a.solve(rhs=l, solution=u, rtol=1e-10)
+    assert st64["rel_residual"] <= 1e-10
+    w = V.element()
+    stm = a.solve(rhs=l, solution=w, rtol=1e-10, mixed=True)
+    assert stm["rel_residual"] <= 1e-10
+    x64, xm = u.to_numpy(), w.to_numpy()
+    assert np.linalg.norm(xm - x64) <= 1e-6 * np.linalg.norm(x64)
