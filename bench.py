@@ -249,22 +249,39 @@ def run_gb300(args, rank, world, local):
     geo_cnt, geo_ms = env.prof("geometry")
     value = nnz * args.steps * world / (ms_max / 1e3) / 1e6
 
-    # roofline of the dominant kernel (gather assembly)
+    # roofline of the dominant kernel and of the whole assembly step
     hbm_peak, peak_kind = load_peaks()
     n_loc = (args.order + 1) * (args.order + 2) * (args.order + 3) // 6
-    # values written, ia / inc_ptr read, incidence + position table, coefficient records
-    alg_bytes = nnz * 8 + (N + 1) * 8 * 2 + T * n_loc * 4 + T * n_loc * n_loc + T * 64
+    ntri = n_loc * (n_loc + 1) // 2
+    el_cnt, el_ms = env.prof("assemble_elements")
+    two_phase = el_cnt > 0
     per_launch_ms = g_ms / max(g_cnt, 1)
+    if two_phase:
+        # gather map kernel: gptr (nnz + 1) and gidx (T n^2) read, each buffered
+        # element entry (upper triangle, df64 pair) read, CSR values written once
+        alg_bytes = (nnz + 1) * 4 + T * n_loc * n_loc * 4 + T * ntri * 8 + nnz * 8
+    else:
+        # fused gather: values written, ia / inc_ptr read, incidence + position table, records
+        alg_bytes = nnz * 8 + (N + 1) * 8 * 2 + T * n_loc * 4 + T * n_loc * n_loc + T * 64
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
     tr = load_traffic()
     traffic = None
-    if tr and tr.get("order") == args.order:
-        traffic = tr["bytes_per_nnz"] * nnz
+    if tr and tr.get("order") == args.order and tr.get("algo") == ("two_phase" if two_phase else "gather"):
+        traffic = tr["gather_bytes_per_nnz"] * nnz
+    # the whole step against the assembly's algorithmic bytes B_asm: CSR values
+    # written once, ja / ia read once, coordinates, l2g and kappa read once
+    V_count = len(xyz)
+    b_asm = nnz * 8 + nnz * 4 + (N + 1) * 4 + V_count * 24 + T * (n_loc * 4 + 8)
+    step_ms = ms_max / args.steps
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "assemble_gather", "kernel_ms": per_launch_ms, "algorithmic_bytes": alg_bytes,
-                "flops_per_launch": T * n_loc * n_loc * 7 * 2,
-                "geometry_ms": geo_ms / max(geo_cnt, 1)}
+                "kernel": "assemble_gather (%s)" % ("gather_map_kernel, two-phase" if two_phase else "gather_row_kernel"),
+                "kernel_ms": per_launch_ms, "algorithmic_bytes": alg_bytes,
+                "element_kernel_ms": el_ms / max(el_cnt, 1) if two_phase else None,
+                "geometry_ms": geo_ms / max(geo_cnt, 1),
+                "step": {"algorithmic_bytes_B_asm": b_asm, "ms": step_ms,
+                         "achieved_gbs": b_asm / (step_ms / 1e3) / 1e9,
+                         "frac": b_asm / (step_ms / 1e3) / 1e9 / hbm_peak}}
 
     # ---- ablation: the same assembly in native FP64 arithmetic (FP64 pipe) ----
     desc_nat = _ffi.FormDesc()

@@ -810,12 +810,10 @@ int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V) {
 // of the affine Laplace/mass form) from the element's coefficient record.
 // df64: each product c_k T_k is formed exactly (TwoProduct by FMA, plus the
 // cross terms of the lo parts) and summed with TwoSum; binary32: an FMA chain.
-// (tables Th/Tl of 7 slices of `stride` floats; tix = the entry's index in a slice)
-__device__ __forceinline__ df record_entry_df(const float4* __restrict__ rp, const float* __restrict__ Th,
-                                              const float* __restrict__ Tl, int stride, int tix) {
-    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1), l0 = __ldg(rp + 2), l1 = __ldg(rp + 3);
-    const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
-    const float cl[7] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z};
+// (tables Th/Tl of 7 slices of `stride` floats; tix = the entry's index in a slice;
+// ch/cl: the record's 7 coefficients, hi and lo parts)
+__device__ __forceinline__ df coef_entry_df(const float* ch, const float* cl, const float* __restrict__ Th,
+                                            const float* __restrict__ Tl, int stride, int tix) {
     float s = 0.0f, err = 0.0f;
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
@@ -835,13 +833,30 @@ __device__ __forceinline__ df record_entry_df(const float4* __restrict__ rp, con
     }
     return quick_two_sum(s, err);
 }
-__device__ __forceinline__ float record_entry_f(const float4* __restrict__ rp, const float* __restrict__ Th, int stride, int tix) {
-    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1);
-    const float ch[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+__device__ __forceinline__ float coef_entry_f(const float* ch, const float* __restrict__ Th, int stride, int tix) {
     float v = 0.0f;
 #pragma unroll
     for (int k = 0; k < 7; ++k) v = fmaf(ch[k], Th[k * stride + tix], v);
     return v;
+}
+__device__ __forceinline__ void load_record(const float4* __restrict__ rp, float* ch, float* cl, bool lo) {
+    const float4 h0 = __ldg(rp), h1 = __ldg(rp + 1);
+    ch[0] = h0.x; ch[1] = h0.y; ch[2] = h0.z; ch[3] = h0.w; ch[4] = h1.x; ch[5] = h1.y; ch[6] = h1.z;
+    if (lo) {
+        const float4 l0 = __ldg(rp + 2), l1 = __ldg(rp + 3);
+        cl[0] = l0.x; cl[1] = l0.y; cl[2] = l0.z; cl[3] = l0.w; cl[4] = l1.x; cl[5] = l1.y; cl[6] = l1.z;
+    }
+}
+__device__ __forceinline__ df record_entry_df(const float4* __restrict__ rp, const float* __restrict__ Th,
+                                              const float* __restrict__ Tl, int stride, int tix) {
+    float ch[7], cl[7];
+    load_record(rp, ch, cl, true);
+    return coef_entry_df(ch, cl, Th, Tl, stride, tix);
+}
+__device__ __forceinline__ float record_entry_f(const float4* __restrict__ rp, const float* __restrict__ Th, int stride, int tix) {
+    float ch[7], cl[7];
+    load_record(rp, ch, cl, false);
+    return coef_entry_f(ch, Th, stride, tix);
 }
 
 template <int N>
@@ -1193,13 +1208,14 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
     for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
         const int64_t e = e0 + sub;
         if (sub >= EPW || e >= nt) continue;
-        const float4* rp = rec + 4 * e;
+        float ch[7], cl[7];
+        load_record(rec + 4 * e, ch, cl, MODE == kModeDF64);      // once per element and lane
         for (int t = t0; t < NTRI; t += (EPW > 1 ? NTRI : 32)) {
             if (MODE == kModeDF64) {
-                const df v = record_entry_df(rp, Th, Tl, NTRI, t);
+                const df v = coef_entry_df(ch, cl, Th, Tl, NTRI, t);
                 reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = make_float2(v.hi, v.lo);
             } else {
-                reinterpret_cast<float*>(kbuf)[e * NTRI + t] = record_entry_f(rp, Th, NTRI, t);
+                reinterpret_cast<float*>(kbuf)[e * NTRI + t] = coef_entry_f(ch, Th, NTRI, t);
             }
         }
     }
