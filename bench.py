@@ -550,11 +550,26 @@ def run_elasticity(args):
     a += fpp.on(fpp.markedfaces(M, 0.0), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
     solve = None
     if not args.no_solve:
-        s64 = a.solve(rhs=l, solution=u, rtol=1e-10)
+        from feelpp_gb300 import _ffi, fe
+
+        def solve_stats(w, **kw):
+            # the stats are reported even when rtol is not reached (the FP64 noise floor of
+            # this stiff system lies near 1e-9, see the design notes)
+            cfg = fe._solver_cfg(1e-10, 100000, kw.get("pc", "jacobi"), kw.get("mixed", False), 0.1, 16, "f64",
+                                 kw.get("cheb_degree", 0), 0.0)
+            st = _ffi.SolveStats()
+            rc = env.lib.fgpu_solve_cg(env.h, a.h, None, l.vec.h, w.h, C.byref(cfg), C.byref(st))
+            out = fe._stats(st)
+            out["status"] = "ok" if rc == 0 else _ffi.ERROR_NAMES.get(rc, str(rc))
+            return out
+
+        s64 = solve_stats(u)
         u2 = V.element()
-        smx = a.solve(rhs=l, solution=u2, rtol=1e-10, mixed=True)
+        smx = solve_stats(u2, mixed=True)
+        u3 = V.element()
+        sch = solve_stats(u3, pc="cheb_jacobi", cheb_degree=3)
         x64, xmx = u.to_numpy(), u2.to_numpy()
-        solve = {"fp64": s64, "mixed_fp32_refine": smx,
+        solve = {"fp64": s64, "mixed_fp32_refine": smx, "fp64_cheb_jacobi": sch,
                  "displacement_rel_diff_vs_fp64": float(np.linalg.norm(xmx - x64) / np.linalg.norm(x64)),
                  "min_uz": float(x64.reshape(-1, 3)[:, 2].min()),
                  "speedup_mixed_vs_fp64": s64["time_ms"] / smx["time_ms"] if smx["time_ms"] else None}

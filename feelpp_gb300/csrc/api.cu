@@ -199,7 +199,7 @@ int fgpu_mesh_set_coords(fgpu_mesh* M, const double* xyz) {
     fgpu_ctx* ctx = M->ctx;
     FGPU_NO_CAPTURE(ctx, "mesh_set_coords");
     FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(M->d_xyz, xyz, 3 * M->nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    std::memcpy(M->h_xyz.data(), xyz, 3 * M->nv * sizeof(double));
+    M->h_xyz_stale = true;           // the host copy is refreshed when a host-side query needs it
     return FGPU_OK;
 }
 
@@ -265,6 +265,12 @@ int fgpu_space_l2g(const fgpu_space* V, int32_t* out) {
 int fgpu_space_boundary_dofs(const fgpu_space* V, int xmax_on, double xmax, int64_t* count, int32_t* dofs) {
     if (!V || !count) return FGPU_ERR_INVALID;
     std::vector<int32_t> nodes;
+    if (V->mesh->h_xyz_stale) {
+        FGPU_CUDA_CHECK(V->ctx, cudaMemcpyAsync(V->mesh->h_xyz.data(), V->mesh->d_xyz, V->mesh->h_xyz.size() * sizeof(double),
+                                                cudaMemcpyDeviceToHost, V->ctx->stream));
+        FGPU_CUDA_CHECK(V->ctx, cudaStreamSynchronize(V->ctx->stream));
+        V->mesh->h_xyz_stale = false;
+    }
     boundary_nodes(V->mesh->nt, V->mesh->h_tets.data(), V->mesh->h_xyz.data(), V->topo, xmax_on, xmax, nodes);
     *count = (int64_t)nodes.size() * V->ncomp;
     if (dofs)
@@ -370,12 +376,13 @@ int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* 
     if (A) FGPU_NO_CAPTURE(A->ctx, "matrix_get_csr");
     if (!A) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = A->ctx;
+    if (ia) FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(ia, A->d_ia, (A->nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (ja) FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(ja, A->d_ja, A->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
     FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
-    if (ia) FGPU_CUDA_CHECK(ctx, cudaMemcpy(ia, A->d_ia, (A->nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
-    if (ja) FGPU_CUDA_CHECK(ctx, cudaMemcpy(ja, A->d_ja, A->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
     if (val) {
         if (A->precision == FGPU_F64) {
-            FGPU_CUDA_CHECK(ctx, cudaMemcpy(val, A->d_val, A->nnz * sizeof(double), cudaMemcpyDeviceToHost));
+            FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(val, A->d_val, A->nnz * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
         } else {
             std::vector<float> tmp(A->nnz);
             FGPU_CUDA_CHECK(ctx, cudaMemcpy(tmp.data(), A->d_val, A->nnz * sizeof(float), cudaMemcpyDeviceToHost));
@@ -413,6 +420,7 @@ int fgpu_matrix_destroy(fgpu_matrix* A) {
     cudaFree(A->d_val);
     cudaFree(A->d_coef);
     cudaFree(A->d_kbuf);
+    cudaFree(A->d_kappa_stage);
     delete A;
     return FGPU_OK;
 }
@@ -489,13 +497,12 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     if (!f->kappa_elem) return assemble_impl(ctx, A, f, nullptr, accumulate);
     FGPU_NO_CAPTURE(ctx, "assemble_matrix with host kappa (use fgpu_assemble_matrix_dev)");
     const int64_t nt = A->space->mesh->nt;
-    double* dk = nullptr;
-    int rc = dev_alloc(ctx, &dk, nt);
-    if (rc) return rc;
-    cudaMemcpyAsync(dk, f->kappa_elem, nt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-    rc = assemble_impl(ctx, A, f, dk, accumulate);
-    cudaFree(dk);
-    return rc;
+    if (!A->d_kappa_stage) {         // kept with the matrix: no allocation (and no implicit sync) per call
+        int rc = dev_alloc(ctx, &A->d_kappa_stage, nt);
+        if (rc) return rc;
+    }
+    FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(A->d_kappa_stage, f->kappa_elem, nt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return assemble_impl(ctx, A, f, A->d_kappa_stage, accumulate);
 }
 
 int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {

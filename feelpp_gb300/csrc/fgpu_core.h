@@ -115,7 +115,8 @@ struct fgpu_bc {
 struct fgpu_mesh {
     fgpu_ctx* ctx = nullptr;
     int64_t nv = 0, nt = 0;
-    std::vector<double> h_xyz;
+    std::vector<double> h_xyz;       // host copy (refreshed from the device when stale)
+    bool h_xyz_stale = false;
     std::vector<int32_t> h_tets;
     double* d_xyz = nullptr;
     int32_t* d_tets = nullptr;
@@ -172,6 +173,7 @@ struct fgpu_matrix {
     void* d_val = nullptr;           // nnz values (double or float)
     double* d_coef = nullptr;        // per-element coefficient records of the last assembly
     int64_t coef_cap = 0;
+    double* d_kappa_stage = nullptr; // staging copy of a host per-element kappa (T doubles)
     void* d_kbuf = nullptr;          // two-phase assembly: element matrices (upper triangles)
     size_t kbuf_bytes = 0;
     mutable std::shared_ptr<SellLayout> sell; // solver layout, built on first solve
