@@ -57,6 +57,7 @@ def parse():
                         "problems in one persistent launch; heat: graph-replayed reassembly for backward Euler")
     p.add_argument("--perturb", type=float, default=None)
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
+    p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--probe", default=None, choices=[None, "cg"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed)")
     return p.parse_args()
@@ -419,13 +420,16 @@ def run_probe_cg(args):
 
 
 def run_matfree(args):
-    """Config 5: P3 Poisson, matrix-free operator in FP32 (CUDA cores and tensor cores), df64 and
-    native FP64; mixed CG (FP32 inner, FP64 residual) to 1e-10; L2/H1 errors."""
+    """Mixed-precision matrix-free P3 Poisson (unit cube, perturbed 0.1h, kappa = 1, homogeneous
+    Dirichlet): operator applies in FP32 (CUDA cores and tcgen05 tensor cores), df64 and native
+    FP64; CG to 1e-10 with FP64 residual (mixed, Jacobi and Chebyshev-Jacobi), compared with the
+    FP64 matrix-free CG and the FP64 assembled-CSR CG on the same GPU; L2/H1 errors against
+    sin(pi x) sin(pi y) sin(pi z) for each."""
     import ctypes as C
 
     import torch
     import feelpp_gb300 as fpp
-    from feelpp_gb300 import meshgen
+    from feelpp_gb300 import _ffi, fe, meshgen
 
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
@@ -472,27 +476,60 @@ def run_matfree(args):
     lv = l.to_numpy()
     lv[bd] = 0.0
     l.vec.upload(lv)
-    sol = V.element()
-    st_mixed = ops["f64"].solve(l, sol, rtol=1e-10, inner=ops["f32_tensor_cores"])
-    err_mixed = sol.errors_sine(8)
-    sol2 = V.element()
-    st_mixed_cc = ops["f64"].solve(l, sol2, rtol=1e-10, inner=ops["f32_cuda_cores"])
-    solve = {"mixed_fp32_tensor_cores": st_mixed, "mixed_fp32_cuda_cores": st_mixed_cc,
-             "l2_error": err_mixed[0], "h1_error": err_mixed[1]}
+    qe = min(2 * args.order + 2, 8)
+
+    def mf_solve(op, inner=None, pc="jacobi", cheb_degree=0):
+        w = V.element()
+        cfg = fe._solver_cfg(1e-10, 100000, pc, inner is not None, 0.1, 16, "f64", cheb_degree, 0.0)
+        st = _ffi.SolveStats()
+        rc = env.lib.fgpu_solve_cg_operator(env.h, op.h, inner.h if inner else None, l.vec.h, w.h, C.byref(cfg), C.byref(st))
+        out = fe._stats(st)
+        out["status"] = "ok" if rc == 0 else _ffi.ERROR_NAMES.get(rc, str(rc))
+        out["l2_error"], out["h1_error"] = w.errors_sine(qe)
+        return out, w
+
+    solve = {}
+    solve["mixed_fp32_tensor_cores"], w_tc = mf_solve(ops["f64"], ops["f32_tensor_cores"])
+    solve["mixed_fp32_cuda_cores"], _ = mf_solve(ops["f64"], ops["f32_cuda_cores"])
+    solve["mixed_fp32_cheb_jacobi"], _ = mf_solve(ops["f64"], ops["f32_cuda_cores"], pc="cheb_jacobi", cheb_degree=3)
     if args.with_plain:
-        sol3 = V.element()
-        st_plain = ops["df64"].solve(l, sol3, rtol=1e-10)
-        e3 = sol3.errors_sine(8)
-        solve["plain_df64"] = st_plain
-        solve["plain_df64_errors"] = e3
-        solve["l2_error_rel_diff_vs_plain"] = abs(err_mixed[0] - e3[0]) / e3[0]
-    out = {"metric": "P3 matrix-free operator apply GDOF/s & CG time-to-1e-10 (FP32 tensor-core inner + FP64 residual)",
-           "value": applies["f32_tensor_cores"]["gdof_per_s"], "unit": "GDOF/s", "n_gpus": 1,
-           "steps": args.steps, "higher_is_better": True, "dtype": "f32 (3xTF32 tensor cores) / f64 residual",
+        solve["fp64_matfree_df64"], w64 = mf_solve(ops["df64"])
+    csr = None
+    if args.with_csr:
+        # FP64 assembled-CSR path on the same GPU (two-phase assembly, then FP64 PCG)
+        a = fpp.form2(test=V, trial=V)
+        t0 = time.perf_counter()
+        a.assign(integral)
+        torch.cuda.synchronize()
+        setup_and_first_ms = (time.perf_counter() - t0) * 1e3
+        e0.record(stream)
+        a.assign(integral)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        asm_ms = e0.elapsed_time(e1)
+        lc = fpp.form1(test=V)
+        lc.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+        a += fpp.on(fpp.boundaryfaces(M), rhs=lc, element=u, expr=0.0, type="elimination_symmetric")
+        wc = V.element()
+        st = a.solve(rhs=lc, solution=wc, rtol=1e-10)
+        st["l2_error"], st["h1_error"] = wc.errors_sine(qe)
+        wm = V.element()
+        stm = a.solve(rhs=lc, solution=wm, rtol=1e-10, mixed=True)
+        stm["l2_error"], stm["h1_error"] = wm.errors_sine(qe)
+        csr = {"nnz": a.nnz, "assembly_ms": asm_ms, "first_assembly_with_map_build_ms": setup_and_first_ms,
+               "fp64_cg": st, "mixed_cg": stm}
+        del a
+    ref_l2 = solve.get("fp64_matfree_df64", {}).get("l2_error") or (csr["fp64_cg"]["l2_error"] if csr else None)
+    if ref_l2:
+        for k in ("mixed_fp32_tensor_cores", "mixed_fp32_cuda_cores", "mixed_fp32_cheb_jacobi"):
+            solve[k]["l2_error_rel_diff_vs_fp64"] = abs(solve[k]["l2_error"] - ref_l2) / ref_l2
+    out = {"metric": "P%d matrix-free operator apply GDOF/s & CG time-to-1e-10 (FP32 inner + FP64 residual)" % args.order,
+           "value": applies["f32_cuda_cores"]["gdof_per_s"], "unit": "GDOF/s", "n_gpus": 1,
+           "steps": args.steps, "higher_is_better": True, "dtype": "f32 inner / f64 residual",
            "data": "synthetic",
            "config": {"workload": "P%d Poisson matrix-free, %d^3-hex Kuhn cube (%d tets, N=%d), perturb %.2fh, kappa=1"
                       % (args.order, args.n, len(tets), V.ndof, perturb)},
-           "applies": applies, "solve": solve, "clocks": clk.summary()}
+           "applies": applies, "solve": solve, "assembled_csr": csr, "clocks": clk.summary()}
     print(json.dumps(out), flush=True)
 
 

@@ -120,6 +120,7 @@ SIGNATURES = {
     "fgpu_batch_assemble": (i32, [P, P, i32]),
     "fgpu_batch_set_launch": (i32, [P, i32, i32]),
     "fgpu_batch_get_launch": (i32, [P, IP, IP, IP]),
+    "fgpu_batch_set_algo": (i32, [P, i32]),
     "fgpu_batch_destroy": (i32, [P]),
     "fgpu_prof_reset": (i32, [P]),
     "fgpu_prof_get": (i32, [P, C.c_char_p, I64P, DP]),

@@ -151,6 +151,10 @@ int fgpu_destroy(fgpu_ctx* ctx) {
         cudaEventDestroy(ev.stop);
     }
     for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+    for (int i = 0; i < 4; ++i)
+        if (ctx->copy_streams[i]) cudaStreamDestroy(ctx->copy_streams[i]);
+    for (int i = 0; i < 5; ++i)
+        if (ctx->copy_events[i]) cudaEventDestroy(ctx->copy_events[i]);
     cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -372,6 +376,32 @@ int fgpu_matrix_info(const fgpu_matrix* A, int64_t* nrows, int64_t* nnz, int* pr
     return FGPU_OK;
 }
 
+// Device -> host copy of a large array in four chunks on four streams (after the
+// work queued on the context stream), so that several copy engines move it.
+static int chunked_d2h(fgpu_ctx* ctx, void* host, const void* dev, size_t bytes) {
+    if (bytes < ((size_t)16 << 20)) {
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+        return FGPU_OK;
+    }
+    if (!ctx->copy_streams[0]) {
+        for (int i = 0; i < 4; ++i) FGPU_CUDA_CHECK(ctx, cudaStreamCreateWithFlags(&ctx->copy_streams[i], cudaStreamNonBlocking));
+        for (int i = 0; i < 5; ++i) FGPU_CUDA_CHECK(ctx, cudaEventCreateWithFlags(&ctx->copy_events[i], cudaEventDisableTiming));
+    }
+    FGPU_CUDA_CHECK(ctx, cudaEventRecord(ctx->copy_events[4], ctx->stream));
+    const size_t chunk = ((bytes / 4) + 255) & ~(size_t)255;
+    for (int i = 0; i < 4; ++i) {
+        const size_t off = (size_t)i * chunk;
+        if (off >= bytes) break;
+        const size_t nb = std::min(chunk, bytes - off);
+        FGPU_CUDA_CHECK(ctx, cudaStreamWaitEvent(ctx->copy_streams[i], ctx->copy_events[4], 0));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync((char*)host + off, (const char*)dev + off, nb, cudaMemcpyDeviceToHost,
+                                             ctx->copy_streams[i]));
+    }
+    for (int i = 0; i < 4; ++i) FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->copy_streams[i]));
+    return FGPU_OK;
+}
+
 int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* val) {
     if (A) FGPU_NO_CAPTURE(A->ctx, "matrix_get_csr");
     if (!A) return FGPU_ERR_INVALID;
@@ -381,8 +411,8 @@ int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* 
     FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
     if (val) {
         if (A->precision == FGPU_F64) {
-            FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(val, A->d_val, A->nnz * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-            FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+            const int rc = chunked_d2h(ctx, val, A->d_val, A->nnz * sizeof(double));
+            if (rc) return rc;
         } else {
             std::vector<float> tmp(A->nnz);
             FGPU_CUDA_CHECK(ctx, cudaMemcpy(tmp.data(), A->d_val, A->nnz * sizeof(float), cudaMemcpyDeviceToHost));

@@ -1147,6 +1147,150 @@ static int batch_tables(fgpu_ctx* ctx, float** h, float** l) {
     return FGPU_OK;
 }
 
+// ---- two-phase batches: the element kernel and the gather-map kernel of the
+// single-problem path over all problems (same per-entry arithmetic and order,
+// so each matrix gets the bits FGPU_ALGO_TWO_PHASE gives it alone) ----
+// upper-triangle tables of orders 1..3 in one block: 7 n(n+1)/2 each
+__host__ __device__ constexpr int batch_tri_off(int order) { return order == 1 ? 0 : order == 2 ? 7 * 10 : 7 * 10 + 7 * 55; }
+constexpr int kBatchTriFloats = 7 * 10 + 7 * 55 + 7 * 210;
+
+template <int MODE>
+__global__ void __launch_bounds__(256) batch_element_kernel(int nprob, const BatchProblem* __restrict__ probs,
+                                                            const int64_t* __restrict__ elem_off, int64_t total,
+                                                            const float* __restrict__ Thg, const float* __restrict__ Tlg) {
+    __shared__ float Th[kBatchTriFloats];
+    __shared__ float Tl[MODE == kModeDF64 ? kBatchTriFloats : 1];
+    for (int k = threadIdx.x; k < kBatchTriFloats; k += blockDim.x) {
+        Th[k] = Thg[k];
+        if (MODE == kModeDF64) Tl[k] = Tlg[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    int p = -1;
+    int64_t pe0 = 0, pe1 = 0;
+    for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < total; g += nw) {   // one warp per element
+        if (g < pe0 || g >= pe1) {
+            p = batch_find(elem_off, nprob, g);
+            pe0 = elem_off[p];
+            pe1 = elem_off[p + 1];
+        }
+        const BatchProblem& P = probs[p];
+        const int64_t e = g - pe0;
+        const int n = P.n, ntri = n * (n + 1) / 2, to = batch_tri_off(P.order);
+        float ch[7], cl[7];
+        load_record(P.rec + 4 * e, ch, cl, MODE == kModeDF64);
+        for (int t = lane; t < ntri; t += 32) {
+            if (MODE == kModeDF64) {
+                const df v = coef_entry_df(ch, cl, Th + to, Tl + to, ntri, t);
+                reinterpret_cast<float2*>(P.kbuf)[e * ntri + t] = make_float2(v.hi, v.lo);
+            } else {
+                reinterpret_cast<float*>(P.kbuf)[e * ntri + t] = coef_entry_f(ch, Th + to, ntri, t);
+            }
+        }
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) batch_gather_map_kernel(int nprob, const BatchProblem* __restrict__ probs,
+                                                               const int64_t* __restrict__ nz_off, int64_t total, int accumulate) {
+    int p = -1;
+    int64_t pz0 = 0, pz1 = 0;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        if (g < pz0 || g >= pz1) {
+            p = batch_find(nz_off, nprob, g);
+            pz0 = nz_off[p];
+            pz1 = nz_off[p + 1];
+        }
+        const BatchProblem& P = probs[p];
+        const int64_t k = g - pz0;
+        const uint32_t p0 = __ldg(P.gptr + k), p1 = __ldg(P.gptr + k + 1);
+        if (MODE == kModeDF64) {
+            const float2* kb = reinterpret_cast<const float2*>(P.kbuf);
+            df s{0.0f, 0.0f};
+            for (uint32_t q = p0; q < p1; q += 4) {
+                uint32_t ix[4];
+                float2 v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) ix[u] = q + u < p1 ? __ldg(P.gidx + q + u) : 0u;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + ix[u]) : make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (q + u < p1) s = (q + u == p0) ? df{v[u].x, v[u].y} : df_add(s, df{v[u].x, v[u].y});
+            }
+            double* out = reinterpret_cast<double*>(P.val) + k;
+            if (accumulate) s = df_add(d2df(*out), s);
+            *out = df2d(s);
+        } else {
+            const float* kb = reinterpret_cast<const float*>(P.kbuf);
+            float s = 0.0f;
+            for (uint32_t q = p0; q < p1; q += 4) {
+                uint32_t ix[4];
+                float v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) ix[u] = q + u < p1 ? __ldg(P.gidx + q + u) : 0u;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + ix[u]) : 0.0f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (q + u < p1) s = (q + u == p0) ? v[u] : f_add(s, v[u]);
+            }
+            float* out = reinterpret_cast<float*>(P.val) + k;
+            *out = accumulate ? f_add(*out, s) : s;
+        }
+    }
+}
+
+static std::map<int, std::pair<float*, float*>> g_btri;
+static int batch_tri_tables(fgpu_ctx* ctx, float** h, float** l) {
+    std::lock_guard<std::mutex> lock(g_btab_mutex);
+    auto it = g_btri.find(ctx->device);
+    if (it != g_btri.end()) { *h = it->second.first; *l = it->second.second; return FGPU_OK; }
+    float *dh = nullptr, *dl = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&dh, kBatchTriFloats * sizeof(float)));
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&dl, kBatchTriFloats * sizeof(float)));
+    for (int order = 1; order <= 3; ++order) {
+        std::string err;
+        DevTables* t = get_dev_tables(order, 2 * order, err);
+        if (!t) { ctx->err = err; return FGPU_ERR_INVALID; }
+        const size_t nb = (size_t)7 * (t->n * (t->n + 1) / 2) * sizeof(float);
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(dh + batch_tri_off(order), t->d_T7th, nb, cudaMemcpyDeviceToDevice));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(dl + batch_tri_off(order), t->d_T7tl, nb, cudaMemcpyDeviceToDevice));
+    }
+    g_btri[ctx->device] = {dh, dl};
+    *h = dh;
+    *l = dl;
+    return FGPU_OK;
+}
+
+int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
+                           int64_t total_elems, const int64_t* d_nz_off, int64_t total_nnz, int f32, int threads,
+                           int accumulate) {
+    float *Th = nullptr, *Tl = nullptr;
+    int rc = batch_tri_tables(ctx, &Th, &Tl);
+    if (rc) return rc;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    {
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((total_elems + 7) / 8, (int64_t)sms * 16));
+        PendingEvent ev;
+        prof_begin(ctx, "batch_elements", ev);
+        if (f32) batch_element_kernel<kModeF32><<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_elem_off, total_elems, Th, Tl);
+        else batch_element_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_elem_off, total_elems, Th, Tl);
+        prof_end(ctx, ev);
+        FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    }
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((total_nnz + threads - 1) / threads, (int64_t)sms * (2048 / threads) * 4));
+    PendingEvent ev;
+    prof_begin(ctx, "batch_gather", ev);
+    if (f32) batch_gather_map_kernel<kModeF32><<<(int)blocks, threads, 0, ctx->stream>>>(nprob, d_probs, d_nz_off, total_nnz, accumulate);
+    else batch_gather_map_kernel<kModeDF64><<<(int)blocks, threads, 0, ctx->stream>>>(nprob, d_probs, d_nz_off, total_nnz, accumulate);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
 int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_row_off, int64_t total_rows,
                         int f32, int acc_floats, unsigned long long* d_counter, const BatchLaunch& cfg, int accumulate) {
     float *Th = nullptr, *Tl = nullptr;

@@ -5,10 +5,14 @@
 // element loop (feelpp/feel/feelvf/integrator.hpp:975-1238 per mesh). Here the
 // problems' device data (patterns, incidence lists, position tables,
 // coefficient records, CSR values) stay where each matrix owns them; the batch
-// holds a device table of per-problem descriptors and runs one geometry launch
-// and one persistent gather launch over all problems. The launch shape
-// (threads per block, rows per work-queue grab) is picked by timing the
-// candidates on the first '=' assembly (a project-written tuner) and kept.
+// holds a device table of per-problem descriptors and runs the assembly of all
+// problems in a fixed number of launches: when the element buffers and gather
+// maps fit in device memory, the two-phase path (geometry, element matrices,
+// gather map: three launches; each matrix gets the bits FGPU_ALGO_TWO_PHASE
+// gives it alone), else the fused row-owner gather as a persistent kernel with
+// a device work queue (two launches; the bits of FGPU_ALGO_GATHER). The launch
+// shape (threads per block, and rows per work-queue grab for the fused path)
+// is picked by timing the candidates on the first '=' assembly and kept.
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -24,10 +28,12 @@ struct fgpu_batch {
     int nprob = 0;
     int f32 = 0;
     int acc_floats = 0;              // per-warp staging floats (max over problems of EPB * maxrow * width)
-    int64_t total_rows = 0, total_elems = 0;
+    int64_t total_rows = 0, total_elems = 0, total_nnz = 0;
+    bool two_phase = false;          // element buffers + gather maps (else the fused row-owner gather)
     BatchProblem* d_probs = nullptr;
     int64_t* d_row_off = nullptr;
     int64_t* d_elem_off = nullptr;
+    int64_t* d_nz_off = nullptr;
     unsigned long long* d_counter = nullptr;
     BatchLaunch launch;
     bool tuned = false;
@@ -60,12 +66,19 @@ int batch_finish(fgpu_ctx* ctx) {
     return FGPU_OK;
 }
 
-int run(fgpu_batch* b, const BatchLaunch& cfg, int accumulate) {
+int run_gather(fgpu_batch* b, const BatchLaunch& cfg, int accumulate) {
     fgpu_ctx* ctx = b->ctx;
-    int rc = launch_batch_geometry(ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems);
-    if (rc) return rc;
+    if (b->two_phase)
+        return launch_batch_two_phase(ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems, b->d_nz_off, b->total_nnz, b->f32,
+                                      cfg.threads, accumulate);
     return launch_batch_gather(ctx, b->nprob, b->d_probs, b->d_row_off, b->total_rows, b->f32, b->acc_floats, b->d_counter, cfg,
                                accumulate);
+}
+
+int run(fgpu_batch* b, const BatchLaunch& cfg, int accumulate) {
+    int rc = launch_batch_geometry(b->ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems);
+    if (rc) return rc;
+    return run_gather(b, cfg, accumulate);
 }
 
 // Time each launch shape once (plus one warm-up) and keep the fastest.
@@ -83,15 +96,14 @@ int tune(fgpu_batch* b) {
     int rc = FGPU_OK;
     for (int t : threads) {
         for (int c : chunks) {
+            if (b->two_phase && c != chunks[0]) continue;   // the two-phase gather has no work queue
             BatchLaunch cfg;
             cfg.threads = t;
             cfg.chunk = c;
-            rc = launch_batch_gather(ctx, b->nprob, b->d_probs, b->d_row_off, b->total_rows, b->f32, b->acc_floats, b->d_counter,
-                                     cfg, 0);
+            rc = run_gather(b, cfg, 0);
             if (rc) break;
             cudaEventRecord(e0, ctx->stream);
-            rc = launch_batch_gather(ctx, b->nprob, b->d_probs, b->d_row_off, b->total_rows, b->f32, b->acc_floats, b->d_counter,
-                                     cfg, 0);
+            rc = run_gather(b, cfg, 0);
             cudaEventRecord(e1, ctx->stream);
             if (rc) break;
             cudaEventSynchronize(e1);
@@ -171,8 +183,49 @@ int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const 
         elem_off[k + 1] = elem_off[k] + V->mesh->nt;
         acc = std::max(acc, epb_of(V->order) * P.maxrow * (mf32 ? 1 : 2));
     }
+    // two-phase when every space's gather map and every matrix's element buffer exist or fit
+    bool two_phase = true;
+    {
+        size_t need = 0;
+        for (int k = 0; k < nprob; ++k) {
+            const fgpu_matrix* A = mats[k];
+            const fgpu_space* V = A->space;
+            const int n = V->n;
+            const size_t kb = (size_t)V->mesh->nt * (n * (n + 1) / 2) * (f32 ? 4 : 8);
+            if (A->kbuf_bytes < kb) need += kb;
+            if (!V->d_gptr) need += ((size_t)V->mesh->nt * n * n + (size_t)A->pattern->nnz * 2 + 1) * sizeof(uint32_t);
+            if ((int64_t)V->mesh->nt * n * n >= (int64_t)UINT32_MAX) two_phase = false;
+        }
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); two_phase = false; }
+        if (need + need / 10 >= free_b) two_phase = false;
+    }
+    std::vector<int64_t> nz_off(nprob + 1, 0);
+    for (int k = 0; k < nprob && two_phase; ++k) {
+        fgpu_matrix* A = mats[k];
+        fgpu_space* V = A->space;
+        const int n = V->n;
+        const size_t kb = (size_t)V->mesh->nt * (n * (n + 1) / 2) * (f32 ? 4 : 8);
+        if (!V->d_gptr && launch_build_gather_map(ctx, V) != FGPU_OK) { two_phase = false; break; }
+        if (A->kbuf_bytes < kb) {
+            cudaFree(A->d_kbuf);
+            A->d_kbuf = nullptr;
+            A->kbuf_bytes = 0;
+            if (cudaMalloc(&A->d_kbuf, kb) != cudaSuccess) { cudaGetLastError(); two_phase = false; break; }
+            A->kbuf_bytes = kb;
+        }
+        probs[k].nz0 = nz_off[k];
+        probs[k].nnz = A->pattern->nnz;
+        probs[k].gptr = V->d_gptr;
+        probs[k].gidx = V->d_gidx;
+        probs[k].kbuf = A->d_kbuf;
+        nz_off[k + 1] = nz_off[k] + A->pattern->nnz;
+    }
+    ctx->err.clear();
     fgpu_batch* b = new (std::nothrow) fgpu_batch();
     if (!b) return FGPU_ERR_ALLOC;
+    b->two_phase = two_phase;
+    b->total_nnz = two_phase ? nz_off[nprob] : 0;
     b->ctx = ctx;
     b->nprob = nprob;
     b->f32 = f32;
@@ -184,6 +237,8 @@ int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const 
     if (e == cudaSuccess) e = cudaMalloc(&b->d_row_off, (nprob + 1) * sizeof(int64_t));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_elem_off, (nprob + 1) * sizeof(int64_t));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_nz_off, (nprob + 1) * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_nz_off, nz_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_probs, probs.data(), nprob * sizeof(BatchProblem), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_row_off, row_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_elem_off, elem_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
@@ -217,10 +272,24 @@ int fgpu_batch_set_launch(fgpu_batch* b, int threads, int chunk) {
     return FGPU_OK;
 }
 
+int fgpu_batch_set_algo(fgpu_batch* b, int algo) {
+    if (!b) return FGPU_ERR_INVALID;
+    if (algo == FGPU_ALGO_GATHER) {
+        b->two_phase = false;
+    } else if (algo == FGPU_ALGO_TWO_PHASE || algo == FGPU_ALGO_AUTO) {
+        if (b->total_nnz == 0) return batch_err(b->ctx, FGPU_ERR_INVALID, "batch: no two-phase buffers (device memory)");
+        b->two_phase = true;
+    } else {
+        return batch_err(b->ctx, FGPU_ERR_INVALID, "batch: algorithm must be GATHER, TWO_PHASE or AUTO");
+    }
+    b->tuned = false;
+    return FGPU_OK;
+}
+
 int fgpu_batch_get_launch(const fgpu_batch* b, int* threads, int* chunk, int* tuned) {
     if (!b) return FGPU_ERR_INVALID;
     if (threads) *threads = b->launch.threads;
-    if (chunk) *chunk = b->launch.chunk;
+    if (chunk) *chunk = b->two_phase ? 0 : b->launch.chunk;      // 0: two-phase batch (no work queue)
     if (tuned) *tuned = b->tuned ? 1 : 0;
     return FGPU_OK;
 }
@@ -231,6 +300,7 @@ int fgpu_batch_destroy(fgpu_batch* b) {
     cudaFree(b->d_row_off);
     cudaFree(b->d_elem_off);
     cudaFree(b->d_counter);
+    cudaFree(b->d_nz_off);
     delete b;
     return FGPU_OK;
 }

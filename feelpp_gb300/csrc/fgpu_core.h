@@ -96,6 +96,8 @@ struct fgpu_ctx {
     int host_threads = 1;
     int capturing = 0;             // the stream is being captured into a graph
     int64_t capture_launches0 = 0;
+    cudaStream_t copy_streams[4] = {nullptr, nullptr, nullptr, nullptr};   // large host<->device copies in chunks
+    cudaEvent_t copy_events[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 struct fgpu_graph {
@@ -246,6 +248,11 @@ struct BatchProblem {
     double kappa_c, mass;
     float4* rec;                     // coefficient records (the matrix's d_coef)
     void* val;                       // matrix values
+    // two-phase batches
+    int64_t nz0, nnz;                // global CSR entry range
+    const uint32_t* gptr;            // the space's gather map
+    const uint32_t* gidx;
+    void* kbuf;                      // the matrix's element buffer
 };
 struct BatchLaunch {                 // launch configuration picked by the batch tuner
     int threads = 256;
@@ -253,6 +260,9 @@ struct BatchLaunch {                 // launch configuration picked by the batch
 };
 int launch_batch_geometry(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
                           int64_t total_elems);
+int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
+                           int64_t total_elems, const int64_t* d_nz_off, int64_t total_nnz, int f32, int threads,
+                           int accumulate);
 int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_row_off,
                         int64_t total_rows, int f32, int acc_floats, unsigned long long* d_counter,
                         const BatchLaunch& cfg, int accumulate);

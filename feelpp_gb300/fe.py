@@ -761,10 +761,15 @@ class Batch:
     def set_launch(self, threads, chunk):
         self.env.check(self.env.lib.fgpu_batch_set_launch(self.h, threads, chunk))
 
+    def set_algo(self, algo):
+        """"gather" (fused persistent row-owner gather) or "two_phase" (element buffers + gather maps)."""
+        self.env.check(self.env.lib.fgpu_batch_set_algo(self.h, {"gather": _ffi.ALGO_GATHER,
+                                                                 "two_phase": _ffi.ALGO_TWO_PHASE}[algo]))
+
     def launch_config(self):
         t, c, tu = C.c_int(), C.c_int(), C.c_int()
         self.env.check(self.env.lib.fgpu_batch_get_launch(self.h, C.byref(t), C.byref(c), C.byref(tu)))
-        return {"threads": t.value, "chunk": c.value, "tuned": bool(tu.value)}
+        return {"threads": t.value, "chunk": c.value, "tuned": bool(tu.value), "two_phase": c.value == 0}
 
     def __del__(self):
         try:

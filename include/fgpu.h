@@ -316,13 +316,17 @@ int fgpu_graph_destroy(fgpu_graph* g);
  *      matrices of scalar spaces (orders 1-3, one precision) created with
  *      fgpu_matrix_create; descs: their Laplace/mass forms (default quadrature);
  *      d_kappa: nprob device arrays of per-element kappa (or NULL / NULL
- *      entries). fgpu_batch_assemble runs one geometry launch and one
- *      persistent gather launch for all problems; its launch shape is tuned on
- *      the first '=' call (fgpu_batch_get_launch reports it). ---- */
+ *      entries). fgpu_batch_assemble runs all problems in three launches
+ *      (geometry, element matrices, gather map: the bits of FGPU_ALGO_TWO_PHASE)
+ *      when their buffers fit in device memory, else two (geometry, persistent
+ *      fused gather with a device work queue: the bits of FGPU_ALGO_GATHER); the
+ *      launch shape is tuned on the first '=' call; fgpu_batch_get_launch
+ *      reports it, chunk = 0 for a two-phase batch. ---- */
 int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const fgpu_form_desc* descs,
                       const double* const* d_kappa, fgpu_batch** out);
 int fgpu_batch_assemble(fgpu_ctx* ctx, fgpu_batch* b, int accumulate);
 int fgpu_batch_set_launch(fgpu_batch* b, int threads, int chunk);
+int fgpu_batch_set_algo(fgpu_batch* b, int algo);   /* FGPU_ALGO_GATHER, _TWO_PHASE or _AUTO; re-tunes */
 int fgpu_batch_get_launch(const fgpu_batch* b, int* threads, int* chunk, int* tuned);
 int fgpu_batch_destroy(fgpu_batch* b);
 

@@ -1,8 +1,9 @@
 """Batched assembly of independent problems and CUDA-graph replay (run on a GB300).
 
-A batch runs the same per-row body as the single-problem row-owner gather
-(FGPU_ALGO_GATHER), with the same records and position tables, so every
-batched matrix must equal the matrix assembled alone that way bit for bit; one problem per order is also checked against the
+A batch runs the same kernels' bodies as the single-problem paths (the two-phase
+element/gather-map kernels, or the fused row-owner gather), with the same records,
+maps and tables, so every batched matrix must equal the matrix assembled alone by
+the same algorithm bit for bit; one problem per order is also checked against the
 oracle at the FP64 tolerance."""
 import numpy as np
 import pytest
@@ -32,17 +33,19 @@ SPECS = [(3, 1), (5, 2), (2, 3), (7, 1), (4, 3), (3, 2), (6, 2), (1, 1), (2, 2),
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_batch_equals_single_assembly(env, precision):
+@pytest.mark.parametrize("algo", ["two_phase", "gather"])
+def test_batch_equals_single_assembly(env, precision, algo):
+    from feelpp_gb300 import _ffi
     probs = _problems(env, SPECS, precision)
     batch = fpp.Batch([p[6] for p in probs], [p[5] for p in probs])
+    batch.set_algo(algo)
     batch.assemble()
     cfg = batch.launch_config()
-    assert cfg["tuned"] and cfg["threads"] in (128, 256)
+    assert cfg["tuned"] and cfg["threads"] in (128, 256) and cfg["two_phase"] == (algo == "two_phase")
     got = [p[6].values().copy() for p in probs]
-    from feelpp_gb300 import _ffi
     for (xyz, tets, kappa, M, V, integral, a), g in zip(probs, got):
         a.zero()
-        a.algo = _ffi.ALGO_GATHER          # the single-problem row-owner gather
+        a.algo = _ffi.ALGO_TWO_PHASE if algo == "two_phase" else _ffi.ALGO_GATHER
         a.assign(integral)
         assert np.array_equal(g, a.values())
         a.algo = _ffi.ALGO_AUTO
