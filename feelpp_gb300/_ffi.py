@@ -29,7 +29,8 @@ class FgpuError(RuntimeError):
 
 
 class Config(C.Structure):
-    _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("profile", C.c_int), ("host_threads", C.c_int)]
+    _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("profile", C.c_int), ("host_threads", C.c_int),
+                ("host_setup", C.c_int)]
 
 
 class FormDesc(C.Structure):

@@ -77,6 +77,33 @@ int ensure_pattern(fgpu_space* V) {
     if (V->pattern) return FGPU_OK;
     fgpu_ctx* ctx = V->ctx;
     std::string err;
+    if (!ctx->host_setup) {
+        auto P = std::make_shared<DevPattern>();
+        ctx->err.clear();
+        const int rcd = build_pattern_device(ctx, V, *P, V->h_pattern.ia);
+        if (rcd == FGPU_OK) {
+            V->h_pattern.nrows = P->nrows;
+            V->h_pattern.nnz = P->nnz;
+            V->h_pattern.max_row = P->max_row;
+            V->pattern = P;
+            if (P->max_row <= 256) {
+                int rc = launch_build_positions(ctx, V);
+                if (rc) return rc;
+                rc = finish(ctx);
+                if (rc) return rc;
+            }
+            return FGPU_OK;
+        }
+        if (rcd != FGPU_ERR_INVALID) return rcd;
+        ctx->err.clear();                 // rows too long for the device sort: host path
+        if (V->topo.inc_ptr.size() != (size_t)V->topo.nnodes + 1 || V->topo.inc.empty()) {
+            // the device-built topology keeps no host incidence: fetch it
+            V->topo.inc_ptr.resize(V->topo.nnodes + 1);
+            V->topo.inc.resize((size_t)V->mesh->nt * V->n);
+            FGPU_CUDA_CHECK(ctx, cudaMemcpy(V->topo.inc_ptr.data(), V->d_inc_ptr, V->topo.inc_ptr.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+            FGPU_CUDA_CHECK(ctx, cudaMemcpy(V->topo.inc.data(), V->d_inc, V->topo.inc.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        }
+    }
     if (!build_node_pattern(V->topo, V->mesh->nt, V->h_pattern, ctx->host_threads, err))
         return set_err(ctx, FGPU_ERR_ALLOC, err);
     auto P = std::make_shared<DevPattern>();
@@ -122,6 +149,7 @@ int fgpu_create(const fgpu_config* cfg, fgpu_ctx** out) {
     int ht = cfg ? cfg->host_threads : 0;
     if (ht <= 0) ht = (int)std::max(1u, std::thread::hardware_concurrency());
     ctx->host_threads = ht;
+    ctx->host_setup = cfg ? cfg->host_setup : 0;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) {
         delete ctx;
@@ -231,6 +259,22 @@ int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* M, int order, int ncomp, fgpu_sp
     V->ncomp = ncomp;
     V->n = nloc_of(order);
     std::string err;
+    if (!ctx->host_setup) {
+        // dof table and incidence on the device; the host path takes the meshes it cannot handle
+        ctx->err.clear();
+        const int rcd = build_space_device(ctx, V);
+        if (rcd == FGPU_OK) {
+            V->ndof = V->topo.nnodes * ncomp;
+            *out = V;
+            return FGPU_OK;
+        }
+        cudaFree(V->d_l2n); cudaFree(V->d_inc_ptr); cudaFree(V->d_inc);
+        V->d_l2n = nullptr; V->d_inc_ptr = nullptr; V->d_inc = nullptr;
+        V->topo = Topology();
+        V->dev_topology = false;
+        if (rcd != FGPU_ERR_INVALID) { delete V; return rcd; }   // bad input or a device error
+        ctx->err.clear();                                          // outside the device path's limits
+    }
     if (!build_topology(M->nv, M->nt, M->h_tets.data(), order, V->topo, err)) {
         delete V;
         return set_err(ctx, FGPU_ERR_INVALID, err);

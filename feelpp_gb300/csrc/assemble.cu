@@ -26,6 +26,7 @@
 
 #include "df64.h"
 #include "fgpu_core.h"
+#include "scan.cuh"
 
 namespace fgpu {
 
@@ -1427,70 +1428,6 @@ __global__ void map_count_kernel(int64_t nt, int n, const int32_t* __restrict__ 
     }
 }
 
-// exclusive scan of uint32 counts in chunks of kScanChunk: per-chunk sums, a
-// one-block scan of the sums, then the chunks with their offsets
-constexpr int kScanChunk = 4096;
-__global__ void scan_chunk_sums_kernel(int64_t n, const uint32_t* __restrict__ in, unsigned long long* __restrict__ sums) {
-    __shared__ unsigned long long sh[32];
-    const int64_t c0 = (int64_t)blockIdx.x * kScanChunk;
-    unsigned long long s = 0;
-    for (int k = threadIdx.x; k < kScanChunk; k += blockDim.x)
-        if (c0 + k < n) s += in[c0 + k];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
-        sums[blockIdx.x] = t;
-    }
-}
-// one block of 1024 threads: each thread scans a contiguous segment of the sums
-__global__ void __launch_bounds__(1024) scan_sums_kernel(int64_t nchunks, unsigned long long* __restrict__ sums) {
-    __shared__ unsigned long long part[1024];
-    const int64_t seg = (nchunks + 1023) / 1024;
-    const int64_t b = threadIdx.x * seg, e = min(b + seg, nchunks);
-    unsigned long long t = 0;
-    for (int64_t c = b; c < e; ++c) t += sums[c];
-    part[threadIdx.x] = t;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long run = 0;
-        for (int k = 0; k < 1024; ++k) {
-            const unsigned long long v = part[k];
-            part[k] = run;
-            run += v;
-        }
-        sums[nchunks] = run;
-    }
-    __syncthreads();
-    unsigned long long run = part[threadIdx.x];
-    for (int64_t c = b; c < e; ++c) {
-        const unsigned long long v = sums[c];
-        sums[c] = run;
-        run += v;
-    }
-}
-__global__ void scan_chunks_kernel(int64_t n, const uint32_t* __restrict__ in, const unsigned long long* __restrict__ sums,
-                                   uint32_t* __restrict__ out) {
-    // one warp per chunk, sequential over 32-entry strips with warp prefix sums
-    const int64_t c = blockIdx.x;
-    const int lane = threadIdx.x;
-    unsigned long long run = sums[c];
-    for (int64_t b = c * kScanChunk; b < min((c + 1) * kScanChunk, n); b += 32) {
-        const int64_t k = b + lane;
-        const uint32_t v = k < n ? in[k] : 0u;
-        uint32_t x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (k < n) out[k] = (uint32_t)(run + x - v);
-        run += __shfl_sync(0xffffffffu, x, 31);
-    }
-    if (c == gridDim.x - 1 && lane == 0) out[n] = (uint32_t)sums[gridDim.x];
-}
-
 // fill: one warp per row, incident elements in element order, lanes over the
 // element row's columns (distinct entries), a per-entry cursor in shared memory
 __global__ void __launch_bounds__(256) map_fill_kernel(int64_t nrows, int n, int ntri, const int64_t* __restrict__ ia,
@@ -1542,15 +1479,12 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
     DevTables* tab = get_dev_tables(V->order, 2 * V->order, err);
     if (!tab) { ctx->err = err; return FGPU_ERR_INVALID; }
     uint32_t *cnt = nullptr, *gptr = nullptr, *gidx = nullptr;
-    unsigned long long* sums = nullptr;
-    const int64_t nchunks = (nnz + kScanChunk - 1) / kScanChunk;
     cudaError_t e = cudaMalloc(&cnt, nnz * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&gptr, (nnz + 1) * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&gidx, contrib * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&sums, (nchunks + 1) * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(cnt); cudaFree(gptr); cudaFree(gidx); cudaFree(sums);
+        cudaFree(cnt); cudaFree(gptr); cudaFree(gidx);
         ctx->err = "gather map: allocation failed";
         return FGPU_ERR_ALLOC;
     }
@@ -1558,16 +1492,15 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     cudaMemsetAsync(cnt, 0, nnz * sizeof(uint32_t), ctx->stream);
     map_count_kernel<<<sms * 16, 256, 0, ctx->stream>>>(nt, n, V->d_l2n, P.d_ia, V->d_pos, cnt);
-    scan_chunk_sums_kernel<<<(int)nchunks, 256, 0, ctx->stream>>>(nnz, cnt, sums);
-    scan_sums_kernel<<<1, 1024, 0, ctx->stream>>>(nchunks, sums);
-    scan_chunks_kernel<<<(int)nchunks, 32, 0, ctx->stream>>>(nnz, cnt, sums, gptr);
+    uint64_t total = 0;
+    int rcs = scan_u32(ctx, cnt, gptr, nnz, &total);
+    if (rcs) { cudaFree(cnt); cudaFree(gptr); cudaFree(gidx); return rcs; }
     map_fill_kernel<<<sms * 8, 256, 0, ctx->stream>>>(P.nrows, n, n * (n + 1) / 2, P.d_ia, V->d_inc_ptr, V->d_inc, V->d_pos,
                                                       tab->d_tri, gptr, gidx, ctx->d_status);
-    ctx->launches += 5;
+    ctx->launches += 2;
     e = cudaGetLastError();
     cudaStreamSynchronize(ctx->stream);
     cudaFree(cnt);
-    cudaFree(sums);
     if (e != cudaSuccess) {
         cudaFree(gptr); cudaFree(gidx);
         ctx->err = std::string("gather map: ") + cudaGetErrorString(e);

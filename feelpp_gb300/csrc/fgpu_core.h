@@ -94,6 +94,7 @@ struct fgpu_ctx {
     int* d_status = nullptr;       // device status word written by kernels (bit flags)
     int64_t launches = 0;          // kernels launched by this context
     int host_threads = 1;
+    int host_setup = 0;            // 1: dof tables and patterns built on the host (default: device)
     int capturing = 0;             // the stream is being captured into a graph
     int64_t capture_launches0 = 0;
     cudaStream_t copy_streams[4] = {nullptr, nullptr, nullptr, nullptr};   // large host<->device copies in chunks
@@ -148,6 +149,8 @@ struct fgpu_space {
     std::shared_ptr<DevPattern> pattern;   // scalar node pattern, built on demand
     fgpu::NodePattern h_pattern;
     uint8_t* d_pos = nullptr;        // T x n x n: position of node l2n[e][j] in row l2n[e][i] (rows <= 255)
+    bool dev_topology = false;       // dof table / incidence built on the device
+    int max_incidence = 0;           // longest node -> element list (device build)
     uint32_t* d_gptr = nullptr;      // two-phase gather map: nnz + 1 offsets into d_gidx
     uint32_t* d_gidx = nullptr;      // T n n element-buffer indices, per CSR entry in element order
 };
@@ -231,6 +234,8 @@ int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kap
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);
+int build_space_device(fgpu_ctx* ctx, fgpu_space* V);
+int build_pattern_device(fgpu_ctx* ctx, fgpu_space* V, DevPattern& P, std::vector<int64_t>& h_ia);
 int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V);
 
 // One problem of a batch (device-side descriptor, built by batch.cu).

@@ -33,37 +33,61 @@ namespace fgpu {
 // element phase
 // ---------------------------------------------------------------------------
 // binary32: one thread per element; T (7 n n floats) in shared memory.
+// binary32 element phase, one thread per element. The warp's 32 elements'
+// l2n rows are staged in shared memory with coalesced loads (row stride N + 1:
+// no bank conflicts), the element values are written local-index-major
+// (coalesced). Gated by the CG stop flag when `stop` is set.
+template <int N>
+__device__ __forceinline__ void mf_element_f32_body(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
+                                                    const float* __restrict__ Tg, const float* __restrict__ x,
+                                                    const uint8_t* __restrict__ mask, float* __restrict__ ye) {
+    constexpr int NT = 7 * N * N;
+    __shared__ float T[NT];
+    __shared__ int32_t sl2n[4][32 * (N + 1)];
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int32_t* my = sl2n[warp];
+    for (int64_t e0 = ((int64_t)blockIdx.x * 4 + warp) * 32; e0 < nt; e0 += (int64_t)gridDim.x * 128) {
+        const int ne = (int)min((int64_t)32, nt - e0);
+        for (int k = lane; k < ne * N; k += 32) {
+            const int el = k / N, j = k - el * N;
+            my[el * (N + 1) + j] = __ldg(l2n + e0 * N + k);
+        }
+        __syncwarp();
+        const int64_t e = e0 + lane;
+        if (lane < ne) {
+            float xe[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const int32_t d = my[lane * (N + 1) + j];
+                xe[j] = (mask && mask[d]) ? 0.0f : __ldg(x + d);
+            }
+            const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
+            const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+#pragma unroll 1
+            for (int i = 0; i < N; ++i) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 7; ++k) {
+                    const float* Tk = T + (k * N + i) * N;
+                    float sum = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < N; ++j) sum = fmaf(Tk[j], xe[j], sum);
+                    acc = fmaf(c[k], sum, acc);
+                }
+                ye[(int64_t)i * nt + e] = acc;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(128) mf_element_f32_kernel(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
                                                             const float* __restrict__ Tg, const float* __restrict__ x,
                                                             const uint8_t* __restrict__ mask, float* __restrict__ ye) {
-    constexpr int NT = 7 * N * N;
-    __shared__ float T[NT];
-    for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
-    __syncthreads();
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
-        float xe[N];
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-            const int32_t d = l2n[e * N + j];
-            xe[j] = (mask && mask[d]) ? 0.0f : x[d];
-        }
-        const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
-        const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
-#pragma unroll 1
-        for (int i = 0; i < N; ++i) {
-            float acc = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                const float* Tk = T + (k * N + i) * N;
-                float s = 0.0f;
-#pragma unroll
-                for (int j = 0; j < N; ++j) s = fmaf(Tk[j], xe[j], s);
-                acc = fmaf(c[k], s, acc);
-            }
-            ye[e * N + i] = acc;
-        }
-    }
+    mf_element_f32_body<N>(nt, l2n, rec, Tg, x, mask, ye);
 }
 
 // native binary64: one thread per element (FP64 pipe), coefficients from the
@@ -95,7 +119,7 @@ __global__ void __launch_bounds__(128) mf_element_f64_kernel(int64_t nt, const i
                 for (int j = 0; j < N; ++j) s = fma(Tk[j], xe[j], s);
                 acc = fma(c[k], s, acc);
             }
-            ye[e * N + i] = acc;
+            ye[(int64_t)i * nt + e] = acc;
         }
     }
 }
@@ -136,16 +160,18 @@ __global__ void __launch_bounds__(128) mf_element_df_kernel(int64_t nt, const in
                 for (int j = 0; j < N; ++j) s = df_add(s, df_mul(df{Th[o + j], Tl[o + j]}, xe[j]));
                 acc = df_add(acc, df_mul(c[k], s));
             }
-            ye[e * N + i] = df2d(acc);
+            ye[(int64_t)i * nt + e] = df2d(acc);
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// node phase: y[m] = sum_{(e,li) in inc(m)} ye[e][li] (element order); Dirichlet rows y = x
+// node phase: y[m] = sum_{(e,li) in inc(m)} ye[li][e] (element order); Dirichlet rows y = x.
+// Element values are stored local-index-major (ye[i * nt + e]) so that the
+// element kernels, one thread per element, write them coalesced.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void mf_gather_kernel(int64_t nnodes, int N, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+__global__ void mf_gather_kernel(int64_t nnodes, int64_t nt, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                  const T* __restrict__ ye, const T* __restrict__ x, const uint8_t* __restrict__ mask,
                                  T* __restrict__ y) {
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
@@ -153,17 +179,26 @@ __global__ void mf_gather_kernel(int64_t nnodes, int N, const int64_t* __restric
             y[m] = x[m];
             continue;
         }
+        // incident element values in batches of 4 (loads issued together), summed in element order
         T s = 0;
-        for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
-            const int32_t code = inc[t];
-            s += ye[(int64_t)(code >> 5) * N + (code & 31)];
+        const int64_t t0 = inc_ptr[m], t1 = inc_ptr[m + 1];
+        for (int64_t t = t0; t < t1; t += 4) {
+            int32_t code[4];
+            T v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) code[u] = t + u < t1 ? __ldg(inc + t + u) : 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = t + u < t1 ? __ldg(ye + (int64_t)(code[u] & 31) * nt + (code[u] >> 5)) : T(0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (t + u < t1) s += v[u];
         }
         y[m] = s;
     }
 }
 
 // df64 summation of binary64 element values (keeps ~48 bits in the node sum)
-__global__ void mf_gather_df_kernel(int64_t nnodes, int N, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+__global__ void mf_gather_df_kernel(int64_t nnodes, int64_t nt, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                     const double* __restrict__ ye, const double* __restrict__ x, const uint8_t* __restrict__ mask,
                                     double* __restrict__ y) {
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
@@ -174,7 +209,7 @@ __global__ void mf_gather_df_kernel(int64_t nnodes, int N, const int64_t* __rest
         df s{0.0f, 0.0f};
         for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
             const int32_t code = inc[t];
-            s = df_add(s, d2df(ye[(int64_t)(code >> 5) * N + (code & 31)]));
+            s = df_add(s, d2df(ye[(int64_t)(code & 31) * nt + (code >> 5)]));
         }
         y[m] = df2d(s);
     }
@@ -191,7 +226,7 @@ __global__ void mf_diag_element_kernel(int64_t nt, int N, const float4* __restri
         for (int i = 0; i < N; ++i) {
             double s = 0;
             for (int k = 0; k < 7; ++k) s += c[k] * T7[(k * N + i) * N + i];
-            ye[e * N + i] = (T)s;
+            ye[(int64_t)i * nt + e] = (T)s;
         }
     }
 }
@@ -269,11 +304,11 @@ int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y) {
     prof_begin(ctx, "matfree_gather", ev2);
     const int gb = blocks_for(op->nnodes, 256, 152 * 16);
     if (op->precision == FGPU_F32)
-        mf_gather_kernel<float><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, (const float*)x, op->d_mask, (float*)y);
+        mf_gather_kernel<float><<<gb, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, (const float*)x, op->d_mask, (float*)y);
     else if (op->precision == FGPU_F64)
-        mf_gather_kernel<double><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)x, op->d_mask, (double*)y);
+        mf_gather_kernel<double><<<gb, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)x, op->d_mask, (double*)y);
     else
-        mf_gather_df_kernel<<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)x, op->d_mask, (double*)y);
+        mf_gather_df_kernel<<<gb, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)x, op->d_mask, (double*)y);
     prof_end(ctx, ev2);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
@@ -296,8 +331,8 @@ int operator_diagonal(fgpu_ctx* ctx, fgpu_operator* op) {
     if (f32) mf_diag_element_kernel<float><<<eb, 256, 0, ctx->stream>>>(op->nt, n, op->d_rec, op->tab->d_T7, (float*)op->d_ye);
     else mf_diag_element_kernel<double><<<eb, 256, 0, ctx->stream>>>(op->nt, n, op->d_rec, op->tab->d_T7, (double*)op->d_ye);
     const int gb = blocks_for(op->nnodes, 256, 152 * 16);
-    if (f32) mf_gather_kernel<float><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, (const float*)ones, op->d_mask, (float*)op->d_diag);
-    else mf_gather_kernel<double><<<gb, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)ones, op->d_mask, (double*)op->d_diag);
+    if (f32) mf_gather_kernel<float><<<gb, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, (const float*)ones, op->d_mask, (float*)op->d_diag);
+    else mf_gather_kernel<double><<<gb, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc, (const double*)op->d_ye, (const double*)ones, op->d_mask, (double*)op->d_diag);
     ctx->launches += 2;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     cudaFree(ones);
@@ -316,7 +351,7 @@ namespace fgpu {
 
 // q = A p fused with the p.q partial sums (node phase of the apply)
 template <class PL>
-__global__ void mf_gather_dot_kernel(int64_t nnodes, int N, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+__global__ void mf_gather_dot_kernel(int64_t nnodes, int64_t nt, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                      const typename PL::S* __restrict__ ye, const typename PL::S* __restrict__ x,
                                      const uint8_t* __restrict__ mask, typename PL::S* __restrict__ y,
                                      typename PL::D* __restrict__ partial, const CGScalars<PL>* __restrict__ sc) {
@@ -328,10 +363,20 @@ __global__ void mf_gather_dot_kernel(int64_t nnodes, int N, const int64_t* __res
         if (mask && mask[m]) {
             v = x[m];
         } else {
+            // incident element values in batches of 4 (loads issued together), summed in element order
             typename PL::A s = PL::zero();
-            for (int64_t t = inc_ptr[m]; t < inc_ptr[m + 1]; ++t) {
-                const int32_t code = inc[t];
-                s = PL::add(s, PL::ld(ye[(int64_t)(code >> 5) * N + (code & 31)]));
+            const int64_t t0 = inc_ptr[m], t1 = inc_ptr[m + 1];
+            for (int64_t t = t0; t < t1; t += 4) {
+                int32_t code[4];
+                typename PL::S w[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) code[u] = t + u < t1 ? __ldg(inc + t + u) : 0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (t + u < t1) w[u] = ye[(int64_t)(code[u] & 31) * nt + (code[u] >> 5)];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (t + u < t1) s = PL::add(s, PL::ld(w[u]));
             }
             v = PL::st(s);
         }
@@ -351,33 +396,7 @@ __global__ void __launch_bounds__(128) mf_element_f32_gated(int64_t nt, const in
                                                            const uint8_t* __restrict__ mask, float* __restrict__ ye,
                                                            const int* __restrict__ stop) {
     if (stop && *stop) return;
-    constexpr int NT = 7 * N * N;
-    __shared__ float T[NT];
-    for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
-    __syncthreads();
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
-        float xe[N];
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-            const int32_t d = l2n[e * N + j];
-            xe[j] = (mask && mask[d]) ? 0.0f : x[d];
-        }
-        const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
-        const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
-#pragma unroll 1
-        for (int i = 0; i < N; ++i) {
-            float acc = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                const float* Tk = T + (k * N + i) * N;
-                float s = 0.0f;
-#pragma unroll
-                for (int j = 0; j < N; ++j) s = fmaf(Tk[j], xe[j], s);
-                acc = fmaf(c[k], s, acc);
-            }
-            ye[e * N + i] = acc;
-        }
-    }
+    mf_element_f32_body<N>(nt, l2n, rec, Tg, x, mask, ye);
 }
 
 template <typename T>
@@ -434,7 +453,7 @@ static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* 
         }
         ctx->profile = save;
     }
-    mf_gather_dot_kernel<PL><<<gblocks, 256, 0, ctx->stream>>>(op->nnodes, n, V->d_inc_ptr, V->d_inc,
+    mf_gather_dot_kernel<PL><<<gblocks, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc,
                                                               (const typename PL::S*)op->d_ye, x, op->d_mask, y, partial, sc);
     ctx->launches += 2;
 }

@@ -146,7 +146,7 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem_d, const unsigned char* A
 }
 
 // ---------------------------------------------------------------------------
-// Element phase: ye[e][i] = sum_k c_{e,k} (T_k x_e)_i for all elements.
+// Element phase: ye[i][e] = sum_k c_{e,k} (T_k x_e)_i for all elements.
 // Shared memory: Bh, Bl (NMMA x KPAD tf32), Ah, Al (128 x KPAD tf32).
 // ---------------------------------------------------------------------------
 template <int N>
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kTcThreads) mf_element_tc_kernel(int64_t nt, c
         }
         if (e < nt) {
 #pragma unroll
-            for (int i = 0; i < N; ++i) ye[e * N + i] = y[i];
+            for (int i = 0; i < N; ++i) ye[(int64_t)i * nt + e] = y[i];
         }
         // all TMEM reads and smem A reads done before the next tile overwrites them
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

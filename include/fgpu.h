@@ -85,6 +85,9 @@ typedef struct {
     void* stream;      /* cudaStream_t to launch on, or NULL for a library-owned stream */
     int profile;       /* 1: time every kernel launch with CUDA events (fgpu_prof_get) */
     int host_threads;  /* host threads for setup work (pattern build); 0 = all cores */
+    int host_setup;    /* 1: build dof tables, incidence and patterns on the host (topology.cpp);
+                          0 (default): on the device (topology_dev.cu; same arrays), with the host
+                          path used automatically for meshes of 2^21 vertices or more */
 } fgpu_config;
 
 typedef struct {
