@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libfgpu.so")
 FGPU_OK = 0
 F64, F32, DF64 = 0, 1, 2
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
+RANGE_ELEMENTS, RANGE_BOUNDARY_FACES, RANGE_MARKED_FACES = 0, 1, 2
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE = 0, 1, 2, 3, 4
 RHS_SINE, RHS_CONST_VEC, RHS_CONST = 0, 1, 2
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
@@ -36,11 +37,12 @@ class Config(C.Structure):
 class FormDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("kappa", C.c_double), ("kappa_elem", C.c_void_p), ("mass", C.c_double),
                 ("lam", C.c_double), ("mu", C.c_double), ("quad_degree", C.c_int), ("algo", C.c_int),
-                ("kappa_scale", C.c_void_p)]
+                ("kappa_scale", C.c_void_p), ("range", C.c_int), ("range_xmax", C.c_double)]
 
 
 class RhsDesc(C.Structure):
-    _fields_ = [("kind", C.c_int), ("c", C.c_double * 3), ("quad_degree", C.c_int)]
+    _fields_ = [("kind", C.c_int), ("c", C.c_double * 3), ("quad_degree", C.c_int), ("range", C.c_int),
+                ("range_xmax", C.c_double)]
 
 
 class SolverCfg(C.Structure):

@@ -332,6 +332,7 @@ int fgpu_space_destroy(fgpu_space* V) {
     cudaFree(V->d_l2n);
     cudaFree(V->d_inc_ptr);
     cudaFree(V->d_inc);
+    for (auto& fs : V->face_sets) cudaFree(fs.d_faces);
     cudaFree(V->d_pos);
     cudaFree(V->d_gptr);
     cudaFree(V->d_gidx);
@@ -510,7 +511,7 @@ static int auto_assembly_algo(fgpu_ctx* ctx, const fgpu_matrix* A) {
     const int64_t nt = V->mesh->nt;
     const int n = V->n, ntri = n * (n + 1) / 2;
     size_t need = 0;
-    const size_t kb = (size_t)nt * ntri * (A->precision == FGPU_F64 ? 8 : 4);
+    const size_t kb = (size_t)nt * ntri * (A->ncomp == 3 ? 9 : 1) * (A->precision == FGPU_F64 ? 8 : 4);
     if (A->kbuf_bytes < kb) need += kb;
     if (!V->d_gptr) need += ((size_t)nt * n * n + (size_t)A->pattern->nnz * 2 + 1) * sizeof(uint32_t);
     if (need == 0) return FGPU_ALGO_TWO_PHASE;
@@ -522,6 +523,14 @@ static int auto_assembly_algo(fgpu_ctx* ctx, const fgpu_matrix* A) {
 
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
     if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
+    if (f->range == FGPU_RANGE_BOUNDARY_FACES || f->range == FGPU_RANGE_MARKED_FACES) {
+        if (f->kind != FGPU_FORM_LAPLACE_MASS || f->kappa != 0.0 || d_kappa || f->kappa_scale)
+            return set_err(ctx, FGPU_ERR_INVALID, "face integrals: only the mass term alpha*idt(u)*id(v)");
+        const int rc = launch_face_matrix(ctx, A, f->range, f->range_xmax, f->mass, accumulate);
+        if (rc) return rc;
+        return finish(ctx);
+    }
+    if (f->range != FGPU_RANGE_ELEMENTS) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad range");
     fgpu_space* V = A->space;
     const int qdeg = form_qdeg(V, f->quad_degree);
     std::string err;
@@ -553,6 +562,15 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
         return finish(ctx);
     }
     if (f->kappa_scale) return set_err(ctx, FGPU_ERR_INVALID, "kappa_scale: Laplace/mass forms on the default path only");
+    if (f->kind == FGPU_FORM_ELASTICITY && (f->algo == FGPU_ALGO_TWO_PHASE ||
+                                            (f->algo == FGPU_ALGO_AUTO && auto_assembly_algo(ctx, A) == FGPU_ALGO_TWO_PHASE))) {
+        // df64 (FP64 matrices) or binary32 element blocks, then the gather map
+        rc = launch_geometry_el_df(ctx, V->mesh, f->lambda, f->mu, reinterpret_cast<float4*>(A->d_coef));
+        if (rc) return rc;
+        rc = launch_assemble_elasticity_two_phase(ctx, A, tab, reinterpret_cast<const float4*>(A->d_coef), accumulate);
+        if (rc) return rc;
+        return finish(ctx);
+    }
     rc = launch_geometry(ctx, V->mesh, f->kind, d_kappa, f->kappa, f->mass, f->lambda, f->mu, A->d_coef);
     if (rc) return rc;
     if (f->kind == FGPU_FORM_LAPLACE_MASS) {
@@ -629,6 +647,13 @@ int fgpu_vector_destroy(fgpu_vector* v) {
 int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, fgpu_vector* out, int accumulate) {
     FGPU_NO_CAPTURE(ctx, "assemble_vector");
     if (!ctx || !V || !rhs || !out || out->n != V->ndof) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad arguments");
+    if (rhs->range == FGPU_RANGE_BOUNDARY_FACES || rhs->range == FGPU_RANGE_MARKED_FACES) {
+        if (rhs->kind != FGPU_RHS_CONST) return set_err(ctx, FGPU_ERR_INVALID, "face integrals: constant loads g*id(v)");
+        const int rc = launch_face_load(ctx, V, rhs->range, rhs->range_xmax, rhs->c[0], out->d, accumulate);
+        if (rc) return rc;
+        return finish(ctx);
+    }
+    if (rhs->range != FGPU_RANGE_ELEMENTS) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad range");
     const int qdeg = form_qdeg(V, rhs->quad_degree);
     std::string err;
     DevTables* tab = get_dev_tables(V->order, qdeg, err);

@@ -71,7 +71,17 @@ DevTables* get_dev_tables(int order, int qdeg, std::string& err) {
                 T7tl[(size_t)k * ntri + t] = T7l[((size_t)k * n + i) * n + j];
             }
         }
+    std::vector<float> Sth((size_t)9 * ntri), Stl((size_t)9 * ntri);
+    for (int i = 0, t = 0; i < n; ++i)
+        for (int j = i; j < n; ++j, ++t)
+            for (int ab = 0; ab < 9; ++ab) {
+                const double v = R.S[((size_t)ab * n + i) * n + j];
+                Sth[(size_t)ab * ntri + t] = (float)v;
+                Stl[(size_t)ab * ntri + t] = (float)(v - (double)(float)v);
+            }
     cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(Sth, &D->d_Sth);
+    if (e == cudaSuccess) e = upload(Stl, &D->d_Stl);
     if (e == cudaSuccess) e = upload(T7th, &D->d_T7th);
     if (e == cudaSuccess) e = upload(T7tl, &D->d_T7tl);
     if (e == cudaSuccess) e = upload(tri, &D->d_tri);
@@ -1215,7 +1225,7 @@ __global__ void __launch_bounds__(256) batch_gather_map_kernel(int nprob, const 
 #pragma unroll
                 for (int u = 0; u < 4; ++u) ix[u] = q + u < p1 ? __ldg(P.gidx + q + u) : 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + ix[u]) : make_float2(0.0f, 0.0f);
+                for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     if (q + u < p1) s = (q + u == p0) ? df{v[u].x, v[u].y} : df_add(s, df{v[u].x, v[u].y});
@@ -1232,7 +1242,7 @@ __global__ void __launch_bounds__(256) batch_gather_map_kernel(int nprob, const 
 #pragma unroll
                 for (int u = 0; u < 4; ++u) ix[u] = q + u < p1 ? __ldg(P.gidx + q + u) : 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + ix[u]) : 0.0f;
+                for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : 0.0f;
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     if (q + u < p1) s = (q + u == p0) ? v[u] : f_add(s, v[u]);
@@ -1388,7 +1398,7 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
 #pragma unroll
                 for (int u = 0; u < 4; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + ix[u]) : make_float2(0.0f, 0.0f);
+                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     if (p + u < p1) s = (p + u == p0) ? df{v[u].x, v[u].y} : df_add(s, df{v[u].x, v[u].y});
@@ -1405,7 +1415,7 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
 #pragma unroll
                 for (int u = 0; u < 4; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + ix[u]) : 0.0f;
+                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : 0.0f;
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     if (p + u < p1) s = (p + u == p0) ? v[u] : f_add(s, v[u]);
@@ -1457,7 +1467,8 @@ __global__ void __launch_bounds__(256) map_fill_kernel(int64_t nrows, int n, int
                 const int p = pos[(e * n + li) * n + lane];
                 const uint32_t slot = cur[warp][p];
                 cur[warp][p] = slot + 1;
-                gidx[slot] = (uint32_t)(e * ntri + tri[li * n + lane]);
+                // bit 31: the contribution is K_e(li, lj) with li > lj, stored as (lj, li)
+                gidx[slot] = (uint32_t)(e * ntri + tri[li * n + lane]) | (li > lane ? 0x80000000u : 0u);
             }
             __syncwarp();
         }
@@ -1470,8 +1481,8 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
     const int n = V->n;
     const int64_t nt = V->mesh->nt, nnz = P.nnz;
     const int64_t contrib = nt * n * n;
-    if (contrib >= (int64_t)UINT32_MAX || nt * (int64_t)(n * (n + 1) / 2) >= (int64_t)UINT32_MAX) {
-        ctx->err = "gather map: more than 2^32 contributions";
+    if (contrib >= (int64_t)UINT32_MAX || nt * (int64_t)(n * (n + 1) / 2) >= ((int64_t)1 << 31)) {
+        ctx->err = "gather map: more than 2^32 contributions or 2^31 buffered entries";
         return FGPU_ERR_INVALID;
     }
     if (!V->d_pos) { ctx->err = "gather map: no position table"; return FGPU_ERR_INVALID; }
@@ -1563,6 +1574,278 @@ int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* ta
     if (order == 3) return f32 ? run_two_phase<kModeF32, 20>(ctx, A, tab, rec, accumulate)
                                : run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, accumulate);
     ctx->err = "unsupported order";
+    return FGPU_ERR_INVALID;
+}
+
+// ---------------------------------------------------------------------------
+// Two-phase vector P1/P2 linear elasticity in df64 (or binary32).
+// lambda div u div v + 2 mu eps(u):eps(v) (qs_elasticity.cpp:46-63): for the
+// scalar pair (i, j) with X_ab = S_ab(i, j) (reference tensors) and
+// Y = B X B^T (B = K^-T), the 3x3 block of K_e at rows (c, i), columns (d, j) is
+//   lambda J Y_cd + mu J Y_dc + delta_cd mu J tr(Y).
+// Records: 24 floats per element: hi parts of (B_00..B_22, lambda J, mu J, 0), then lo parts.
+// Phase 1 stores the blocks of the pairs i <= j (n(n+1)/2 x 9 values per element);
+// phase 2, one warp per scalar pattern row, lanes over its entries, sums the 9
+// entries of each node pair over the contributions of the gather map in element
+// order (a contribution with li > lj reads its block transposed) and writes them
+// into the expanded CSR (row 3m+c, columns 3n'+d).
+// ---------------------------------------------------------------------------
+__global__ void geometry_el_df_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets, double lam,
+                                      double mu, float4* __restrict__ rec, int* __restrict__ status) {
+    const df lamd = d2df(lam), mud = d2df(mu);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        const int4 t = *reinterpret_cast<const int4*>(tets + 4 * e);
+        const double* X0 = xyz + 3 * (int64_t)t.x;
+        const double* Xv[3] = {xyz + 3 * (int64_t)t.y, xyz + 3 * (int64_t)t.z, xyz + 3 * (int64_t)t.w};
+        df K[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) K[r * 3 + c] = df_scale(d2df(Xv[c][r] - X0[r]), 0.5f);
+        df C[9];
+        C[0] = df_sub(df_mul(K[4], K[8]), df_mul(K[5], K[7]));
+        C[1] = df_sub(df_mul(K[5], K[6]), df_mul(K[3], K[8]));
+        C[2] = df_sub(df_mul(K[3], K[7]), df_mul(K[4], K[6]));
+        C[3] = df_sub(df_mul(K[2], K[7]), df_mul(K[1], K[8]));
+        C[4] = df_sub(df_mul(K[0], K[8]), df_mul(K[2], K[6]));
+        C[5] = df_sub(df_mul(K[1], K[6]), df_mul(K[0], K[7]));
+        C[6] = df_sub(df_mul(K[1], K[5]), df_mul(K[2], K[4]));
+        C[7] = df_sub(df_mul(K[2], K[3]), df_mul(K[0], K[5]));
+        C[8] = df_sub(df_mul(K[0], K[4]), df_mul(K[1], K[3]));
+        const df det = df_add(df_add(df_mul(K[0], C[0]), df_mul(K[1], C[1])), df_mul(K[2], C[2]));
+        const df J = det.hi < 0.0f ? df_neg(det) : det;
+        if (!(J.hi > 0.0f) || !isfinite(J.hi)) atomicOr(status, kStatusBadElement);
+        const df inv = df_recip(det);
+        df v[12];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = df_mul(C[i], inv);      // B = C / det = K^-T
+        v[9] = df_mul(lamd, J);
+        v[10] = df_mul(mud, J);
+        v[11] = df{0.0f, 0.0f};
+        float4* o = rec + 6 * e;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            o[q] = make_float4(v[4 * q].hi, v[4 * q + 1].hi, v[4 * q + 2].hi, v[4 * q + 3].hi);
+            o[3 + q] = make_float4(v[4 * q].lo, v[4 * q + 1].lo, v[4 * q + 2].lo, v[4 * q + 3].lo);
+        }
+    }
+}
+
+int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec) {
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((mesh->nt + 255) / 256, 152 * 16));
+    PendingEvent ev;
+    prof_begin(ctx, "geometry", ev);
+    geometry_el_df_kernel<<<(int)blocks, 256, 0, ctx->stream>>>(mesh->nt, mesh->d_xyz, mesh->d_tets, lam, mu, d_rec, ctx->d_status);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+// one 3x3 block from the pair's reference tensors (Xh/Xl: S_ab hi/lo) and the
+// element's B, lambda J, mu J; df64 or binary32 (MODE)
+template <int MODE>
+__device__ __forceinline__ void el_block(const float* Xh, const float* Xl, const df* B, df lJ, df mJ, df* out) {
+    if (MODE == kModeDF64) {
+        df X[9], Z[9], Y[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) X[k] = quick_two_sum(Xh[k], Xl[k]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                Z[a * 3 + d] = df_add(df_add(df_mul(X[a * 3 + 0], B[d * 3 + 0]), df_mul(X[a * 3 + 1], B[d * 3 + 1])),
+                                      df_mul(X[a * 3 + 2], B[d * 3 + 2]));
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                Y[c * 3 + d] = df_add(df_add(df_mul(B[c * 3 + 0], Z[0 * 3 + d]), df_mul(B[c * 3 + 1], Z[1 * 3 + d])),
+                                      df_mul(B[c * 3 + 2], Z[2 * 3 + d]));
+        const df tr = df_add(df_add(Y[0], Y[4]), Y[8]);
+        const df mtr = df_mul(mJ, tr);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                df v = df_add(df_mul(lJ, Y[c * 3 + d]), df_mul(mJ, Y[d * 3 + c]));
+                if (c == d) v = df_add(v, mtr);
+                out[c * 3 + d] = v;
+            }
+    } else {
+        float Bf[9], Z[9], Y[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Bf[k] = B[k].hi;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                Z[a * 3 + d] = fmaf(Xh[a * 3 + 0], Bf[d * 3 + 0], fmaf(Xh[a * 3 + 1], Bf[d * 3 + 1], Xh[a * 3 + 2] * Bf[d * 3 + 2]));
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                Y[c * 3 + d] = fmaf(Bf[c * 3 + 0], Z[0 * 3 + d], fmaf(Bf[c * 3 + 1], Z[1 * 3 + d], Bf[c * 3 + 2] * Z[2 * 3 + d]));
+        const float tr = Y[0] + Y[4] + Y[8];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                float v = fmaf(lJ.hi, Y[c * 3 + d], mJ.hi * Y[d * 3 + c]);
+                if (c == d) v = fmaf(mJ.hi, tr, v);
+                out[c * 3 + d] = df{v, 0.0f};
+            }
+    }
+}
+
+template <int MODE, int N>
+__global__ void __launch_bounds__(128) element_el_kernel(int64_t nt, const float4* __restrict__ rec, const float* __restrict__ Shg,
+                                                         const float* __restrict__ Slg, void* __restrict__ kbuf) {
+    constexpr int NTRI = N * (N + 1) / 2;
+    __shared__ float Sh[9 * NTRI];
+    __shared__ float Sl[9 * NTRI];
+    for (int k = threadIdx.x; k < 9 * NTRI; k += blockDim.x) {
+        Sh[k] = Shg[k];
+        Sl[k] = Slg[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < nt; e += nw) {   // one warp per element
+        const float4* rp = rec + 6 * e;
+        df B[9], lJ, mJ;
+        {
+            float h[12], l[12];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 a = __ldg(rp + q), b = __ldg(rp + 3 + q);
+                h[4 * q] = a.x; h[4 * q + 1] = a.y; h[4 * q + 2] = a.z; h[4 * q + 3] = a.w;
+                l[4 * q] = b.x; l[4 * q + 1] = b.y; l[4 * q + 2] = b.z; l[4 * q + 3] = b.w;
+            }
+#pragma unroll
+            for (int k = 0; k < 9; ++k) B[k] = df{h[k], l[k]};
+            lJ = df{h[9], l[9]};
+            mJ = df{h[10], l[10]};
+        }
+        for (int t = lane; t < NTRI; t += 32) {
+            float Xh[9], Xl[9];
+#pragma unroll
+            for (int ab = 0; ab < 9; ++ab) {
+                Xh[ab] = Sh[ab * NTRI + t];
+                Xl[ab] = Sl[ab * NTRI + t];
+            }
+            df blk[9];
+            el_block<MODE>(Xh, Xl, B, lJ, mJ, blk);
+            const int64_t o = (e * NTRI + t) * 9;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                if (MODE == kModeDF64) reinterpret_cast<float2*>(kbuf)[o + k] = make_float2(blk[k].hi, blk[k].lo);
+                else reinterpret_cast<float*>(kbuf)[o + k] = blk[k].hi;
+            }
+        }
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) gather_el_kernel(int64_t nrows, const int64_t* __restrict__ sia, const uint32_t* __restrict__ gptr,
+                                                        const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
+                                                        void* __restrict__ valv, int accumulate) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t m = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; m < nrows; m += nw) {
+        const int64_t s0 = sia[m];
+        const int len = (int)(sia[m + 1] - s0);
+        for (int pos = lane; pos < len; pos += 32) {
+            const int64_t ks = s0 + pos;
+            const uint32_t p0 = __ldg(gptr + ks), p1 = __ldg(gptr + ks + 1);
+            df acc[9];
+            float accf[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) { acc[k] = df{0.0f, 0.0f}; accf[k] = 0.0f; }
+            for (uint32_t p = p0; p < p1; ++p) {
+                const uint32_t g = __ldg(gidx + p);
+                const bool tr = (g & 0x80000000u) != 0;
+                const int64_t base = (int64_t)(g & 0x7FFFFFFFu) * 9;
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        const int k = tr ? d * 3 + c : c * 3 + d;
+                        if (MODE == kModeDF64) {
+                            const float2 v = __ldg(reinterpret_cast<const float2*>(kbuf) + base + k);
+                            acc[c * 3 + d] = p == p0 ? df{v.x, v.y} : df_add(acc[c * 3 + d], df{v.x, v.y});
+                        } else {
+                            const float v = __ldg(reinterpret_cast<const float*>(kbuf) + base + k);
+                            accf[c * 3 + d] = p == p0 ? v : f_add(accf[c * 3 + d], v);
+                        }
+                    }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const int64_t o = 9 * s0 + (int64_t)c * 3 * len + 3 * pos + d;
+                    if (MODE == kModeDF64) {
+                        double* out = reinterpret_cast<double*>(valv) + o;
+                        df a = acc[c * 3 + d];
+                        if (accumulate) a = df_add(d2df(*out), a);
+                        *out = df2d(a);
+                    } else {
+                        float* out = reinterpret_cast<float*>(valv) + o;
+                        *out = accumulate ? f_add(*out, accf[c * 3 + d]) : accf[c * 3 + d];
+                    }
+                }
+        }
+    }
+}
+
+template <int MODE, int N>
+static int run_el_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+    fgpu_space* V = A->space;
+    const int64_t nt = V->mesh->nt;
+    constexpr int NTRI = N * (N + 1) / 2;
+    if (!V->d_gptr) {
+        if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (gather map)"; return FGPU_ERR_INVALID; }
+        int rc = launch_build_gather_map(ctx, V);
+        if (rc) return rc;
+    }
+    const size_t need = (size_t)nt * NTRI * 9 * (MODE == kModeDF64 ? 8 : 4);
+    if (A->kbuf_bytes < need) {
+        if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (element buffer)"; return FGPU_ERR_INVALID; }
+        cudaFree(A->d_kbuf);
+        A->d_kbuf = nullptr;
+        A->kbuf_bytes = 0;
+        if (cudaMalloc(&A->d_kbuf, need) != cudaSuccess) { cudaGetLastError(); ctx->err = "two-phase assembly: element buffer allocation failed"; return FGPU_ERR_ALLOC; }
+        A->kbuf_bytes = need;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    {
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nt + 3) / 4, (int64_t)sms * 16));
+        PendingEvent ev;
+        prof_begin(ctx, "assemble_elements", ev);
+        element_el_kernel<MODE, N><<<(int)blocks, 128, 0, ctx->stream>>>(nt, rec, tab->d_Sth, tab->d_Stl, A->d_kbuf);
+        prof_end(ctx, ev);
+        FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    }
+    const DevPattern& P = *A->pattern;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((P.nrows + 7) / 8, (int64_t)sms * 16));
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather_elasticity", ev);
+    gather_el_kernel<MODE><<<(int)blocks, 256, 0, ctx->stream>>>(P.nrows, P.d_ia, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+int launch_assemble_elasticity_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+    const int order = A->space->order;
+    const bool f32 = A->precision == FGPU_F32;
+    if (A->ncomp != 3) { ctx->err = "elasticity needs a 3-component space"; return FGPU_ERR_INVALID; }
+    if (order == 1) return f32 ? run_el_two_phase<kModeF32, 4>(ctx, A, tab, rec, accumulate)
+                               : run_el_two_phase<kModeDF64, 4>(ctx, A, tab, rec, accumulate);
+    if (order == 2) return f32 ? run_el_two_phase<kModeF32, 10>(ctx, A, tab, rec, accumulate)
+                               : run_el_two_phase<kModeDF64, 10>(ctx, A, tab, rec, accumulate);
+    ctx->err = "elasticity supports P1 and P2";
     return FGPU_ERR_INVALID;
 }
 

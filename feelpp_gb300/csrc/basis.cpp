@@ -113,6 +113,106 @@ bool invert(std::vector<LD> A, int n, std::vector<LD>& X) {
 
 }  // namespace
 
+namespace {
+
+// Gauss-Legendre rule with k points on [0, 1] (Newton on P_k from the
+// Chebyshev-like initial guesses; long double).
+void gauss_legendre01(int k, std::vector<LD>& x, std::vector<LD>& w) {
+    x.resize(k);
+    w.resize(k);
+    const LD pi = 3.141592653589793238462643383279502884L;
+    for (int i = 0; i < k; ++i) {
+        LD t = std::cos(pi * (i + 0.75L) / (k + 0.5L));
+        LD dp = 1;
+        for (int it = 0; it < 100; ++it) {
+            LD p0 = 1, p1 = t;
+            for (int m = 2; m <= k; ++m) {
+                const LD p2 = ((2 * m - 1) * t * p1 - (m - 1) * p0) / m;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = k * (t * p1 - p0) / (t * t - 1);
+            const LD dt = p1 / dp;
+            t -= dt;
+            if (std::fabs(dt) < 1e-30L) break;
+        }
+        x[i] = (1 - t) / 2;
+        w[i] = 1 / ((1 - t * t) * dp * dp);   // weight on [-1,1] is 2 / ((1 - t^2) P'^2); halved for [0,1]
+    }
+}
+
+}  // namespace
+
+// Face tables for boundary integrals (integrator.hpp MESH_FACES): for each
+// reference face f (vertices kFaceVerts[f]), per unit face area,
+//   Mf[f](i, j) = (1/|f|) int_f phi_i phi_j,   Lf[f](i) = (1/|f|) int_f phi_i,
+// with a collapsed (Duffy) Gauss-Legendre rule of (p + 2)^2 points on the face
+// triangle, exact for the degree-2p integrands. Only the dofs on the face are
+// nonzero (fl[f]).
+bool build_face_tables(int order, FaceTables& out, std::string& err) {
+    if (order < 1 || order > 3) { err = "order must be 1, 2 or 3"; return false; }
+    std::vector<double> nodes;
+    lagrange_nodes(order, nodes);
+    const int n = nloc_of(order);
+    std::vector<Mono> mono = monomials(order);
+    std::vector<LD> V((size_t)n * n), C;
+    for (int k = 0; k < n; ++k) {
+        LD x = ((LD)nodes[3 * k] + 1) / 2, y = ((LD)nodes[3 * k + 1] + 1) / 2, z = ((LD)nodes[3 * k + 2] + 1) / 2;
+        for (int m = 0; m < n; ++m) V[(size_t)k * n + m] = ipow(x, mono[m].a) * ipow(y, mono[m].b) * ipow(z, mono[m].c);
+    }
+    if (!invert(V, n, C)) { err = "singular Vandermonde"; return false; }
+    const int kq = order + 2;
+    std::vector<LD> gx, gw;
+    gauss_legendre01(kq, gx, gw);
+    out.order = order;
+    out.n = n;
+    out.Mf.assign((size_t)4 * n * n, 0.0);
+    out.Lf.assign((size_t)4 * n, 0.0);
+    for (int f = 0; f < 4; ++f) {
+        LD A[3], E1[3], E2[3];
+        for (int d = 0; d < 3; ++d) {
+            A[d] = kRefVerts[kFaceVerts[f][0]][d];
+            E1[d] = (LD)kRefVerts[kFaceVerts[f][1]][d] - A[d];
+            E2[d] = (LD)kRefVerts[kFaceVerts[f][2]][d] - A[d];
+        }
+        std::vector<LD> M((size_t)n * n, 0), L(n, 0);
+        LD wsum = 0;
+        std::vector<LD> phi(n);
+        for (int a = 0; a < kq; ++a)
+            for (int b = 0; b < kq; ++b) {
+                // (s, t) = (u, v (1 - u)) on the unit triangle, jacobian (1 - u)
+                const LD u = gx[a], v = gx[b];
+                const LD s2 = u, t2 = v * (1 - u), w = gw[a] * gw[b] * (1 - u);
+                LD P[3];
+                for (int d = 0; d < 3; ++d) P[d] = A[d] + s2 * E1[d] + t2 * E2[d];
+                const LD x = (P[0] + 1) / 2, y = (P[1] + 1) / 2, z = (P[2] + 1) / 2;
+                for (int i = 0; i < n; ++i) {
+                    LD vv = 0;
+                    for (int m = 0; m < n; ++m) {
+                        const LD c = C[(size_t)m * n + i];
+                        if (c != 0) vv += c * ipow(x, mono[m].a) * ipow(y, mono[m].b) * ipow(z, mono[m].c);
+                    }
+                    phi[i] = vv;
+                }
+                wsum += w;
+                for (int i = 0; i < n; ++i) {
+                    L[i] += w * phi[i];
+                    for (int j = 0; j < n; ++j) M[(size_t)i * n + j] += w * phi[i] * phi[j];
+                }
+            }
+        // the weights sum to the unit triangle's area 1/2: normalise to unit face area
+        for (int i = 0; i < n; ++i) {
+            LD li = L[i] / wsum;
+            out.Lf[(size_t)f * n + i] = std::fabs(li) < 1e-15L ? 0.0 : (double)li;
+            for (int j = 0; j < n; ++j) {
+                LD mij = M[(size_t)i * n + j] / wsum;
+                out.Mf[((size_t)f * n + i) * n + j] = std::fabs(mij) < 1e-15L ? 0.0 : (double)mij;
+            }
+        }
+    }
+    return true;
+}
+
 bool build_ref_tables(int order, int qdeg, RefTables& out, std::string& err) {
     if (order < 1 || order > 3) { err = "order must be 1, 2 or 3"; return false; }
     if (qdeg < 1 || qdeg > kMaxTetRuleDegree) { err = "quadrature degree must be in [1, 8]"; return false; }
@@ -176,6 +276,16 @@ bool build_ref_tables(int order, int qdeg, RefTables& out, std::string& err) {
             }
     }
     for (size_t k = 0; k < S.size(); ++k) out.S[k] = (double)S[k];
+    // S_ba(j, i) and S_ab(i, j) are the same integral; make them the same number
+    // (the long-double sums round their products in different orders), so that an
+    // element matrix can be stored as blocks of its upper triangle
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    const bool upper = i < j || (i == j && a <= b);
+                    if (!upper) out.S[((size_t)(a * 3 + b) * n + i) * n + j] = out.S[((size_t)(b * 3 + a) * n + j) * n + i];
+                }
     for (size_t k = 0; k < M.size(); ++k) out.M[k] = (double)M[k];
     // T7: c0*S00 + c1*S11 + c2*S22 + c3*(S01+S10) + c4*(S02+S20) + c5*(S12+S21) + c6*M
     const int pairs[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};

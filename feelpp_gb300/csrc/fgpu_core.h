@@ -38,6 +38,13 @@ struct RefTables {
 bool lagrange_nodes(int order, std::vector<double>& xyz);
 bool build_ref_tables(int order, int qdeg, RefTables& out, std::string& err);
 
+struct FaceTables {                  // boundary-face integrals per unit face area
+    int order = 0, n = 0;
+    std::vector<double> Mf;          // 4 x n x n : (1/|f|) int_f phi_i phi_j
+    std::vector<double> Lf;          // 4 x n     : (1/|f|) int_f phi_i
+};
+bool build_face_tables(int order, FaceTables& out, std::string& err);
+
 // ---------------------------------------------------------------------------
 // Host topology: entities, DOF numbering, colouring, sparsity pattern.
 // ---------------------------------------------------------------------------
@@ -62,6 +69,8 @@ bool build_node_pattern(const Topology& topo, int64_t nt, NodePattern& pat, int 
 
 int colour_elements(int64_t nv, int64_t nt, const int32_t* tets, std::vector<int32_t>& perm,
                     std::vector<int64_t>& colour_ptr);
+int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax,
+                            std::vector<int32_t>& faces, std::vector<int64_t>& colour_ptr);
 
 // Boundary dof nodes: the nodes carried by faces owned by one element; when
 // `xmax_on` only the faces whose three vertices satisfy x <= xmax (+1e-12).
@@ -151,6 +160,13 @@ struct fgpu_space {
     uint8_t* d_pos = nullptr;        // T x n x n: position of node l2n[e][j] in row l2n[e][i] (rows <= 255)
     bool dev_topology = false;       // dof table / incidence built on the device
     int max_incidence = 0;           // longest node -> element list (device build)
+    struct FaceSet {                 // boundary faces of a range, coloured (scatter without conflicts)
+        int xmax_on = 0;
+        double xmax = 0;
+        int32_t* d_faces = nullptr;  // e * 4 + f, sorted by colour
+        std::vector<int64_t> colour_ptr;
+    };
+    std::vector<FaceSet> face_sets;
     uint32_t* d_gptr = nullptr;      // two-phase gather map: nnz + 1 offsets into d_gidx
     uint32_t* d_gidx = nullptr;      // T n n element-buffer indices, per CSR entry in element order
 };
@@ -213,6 +229,8 @@ struct DevTables {                     // device copies of the reference tables
     float* d_T7th = nullptr;           // the same split in upper-triangle order: 7 x n(n+1)/2
     float* d_T7tl = nullptr;
     uint16_t* d_tri = nullptr;         // n x n: (i, j) -> upper-triangle index of (min, max)
+    float* d_Sth = nullptr;            // elasticity tensors S_ab(i, j), i <= j, df64 split: 9 x n(n+1)/2
+    float* d_Stl = nullptr;
     double* d_phi = nullptr;           // Q n
     double* d_dphi = nullptr;          // Q n 3
     double* d_qx = nullptr;            // Q 3
@@ -233,7 +251,11 @@ int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kap
                        float4* d_rec, const double* d_kscale = nullptr);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec);
+int launch_assemble_elasticity_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);
+int launch_face_matrix(fgpu_ctx* ctx, fgpu_matrix* A, int range, double xmax, double alpha, int accumulate);
+int launch_face_load(fgpu_ctx* ctx, const fgpu_space* V, int range, double xmax, double g, double* d_rhs, int accumulate);
 int build_space_device(fgpu_ctx* ctx, fgpu_space* V);
 int build_pattern_device(fgpu_ctx* ctx, fgpu_space* V, DevPattern& P, std::vector<int64_t>& h_ia);
 int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V);

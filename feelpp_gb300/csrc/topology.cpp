@@ -247,6 +247,56 @@ int colour_elements(int64_t nv, int64_t nt, const int32_t* tets, std::vector<int
     return nc;
 }
 
+// Boundary faces (faces of exactly one element) as e * 4 + f, in element order;
+// with xmax_on only those whose three vertices have x <= xmax (+1e-12). Then a
+// greedy colouring in that order (faces sharing a vertex get different
+// colours): `faces` comes back sorted by colour (stable), colour_ptr delimits
+// the colours. Returns the number of colours (-1: more than 64 needed).
+int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax,
+                            std::vector<int32_t>& faces, std::vector<int64_t>& colour_ptr) {
+    std::vector<int32_t> keys, face_of_slot;
+    face_keys(nt, tets, keys);
+    int64_t nv = 0;
+    for (int64_t k = 0; k < 4 * nt; ++k) nv = std::max<int64_t>(nv, tets[k] + 1);
+    const int64_t nf = identify_entities<3>(nv, nt * 4, keys.data(), face_of_slot);
+    std::vector<uint8_t> cnt(nf, 0);
+    for (int64_t s = 0; s < nt * 4; ++s)
+        if (cnt[face_of_slot[s]] < 2) cnt[face_of_slot[s]]++;
+    std::vector<int32_t> list;
+    for (int64_t e = 0; e < nt; ++e)
+        for (int f = 0; f < 4; ++f) {
+            if (cnt[face_of_slot[e * 4 + f]] != 1) continue;
+            if (xmax_on) {
+                bool ok = true;
+                for (int v = 0; v < 3; ++v) ok = ok && xyz[3 * (int64_t)tets[4 * e + kFaceVerts[f][v]]] <= xmax + 1e-12;
+                if (!ok) continue;
+            }
+            list.push_back((int32_t)(e * 4 + f));
+        }
+    std::vector<uint64_t> used(nv, 0);
+    std::vector<uint8_t> col(list.size());
+    int nc = 0;
+    for (size_t k = 0; k < list.size(); ++k) {
+        const int64_t e = list[k] >> 2;
+        const int f = list[k] & 3;
+        uint64_t m = 0;
+        for (int v = 0; v < 3; ++v) m |= used[tets[4 * e + kFaceVerts[f][v]]];
+        int c = 0;
+        while (c < 64 && ((m >> c) & 1)) ++c;
+        if (c == 64) return -1;
+        col[k] = (uint8_t)c;
+        nc = std::max(nc, c + 1);
+        for (int v = 0; v < 3; ++v) used[tets[4 * e + kFaceVerts[f][v]]] |= (1ull << c);
+    }
+    colour_ptr.assign(nc + 1, 0);
+    for (size_t k = 0; k < list.size(); ++k) colour_ptr[col[k] + 1]++;
+    for (int c = 0; c < nc; ++c) colour_ptr[c + 1] += colour_ptr[c];
+    std::vector<int64_t> fill(colour_ptr.begin(), colour_ptr.end() - 1);
+    faces.resize(list.size());
+    for (size_t k = 0; k < list.size(); ++k) faces[fill[col[k]]++] = list[k];
+    return nc;
+}
+
 bool boundary_nodes(int64_t nt, const int32_t* tets, const double* xyz, const Topology& topo, int xmax_on,
                     double xmax, std::vector<int32_t>& nodes) {
     std::vector<int32_t> keys, face_of_slot;

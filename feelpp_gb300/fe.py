@@ -281,6 +281,15 @@ def elements(mesh):
     return _Range(mesh, "elements")
 
 
+def _range_code(rng):
+    """(FGPU_RANGE_*, xmax) of an integration range; integrate() without a range means elements."""
+    if rng is None or rng.kind == "elements":
+        return _ffi.RANGE_ELEMENTS, 0.0
+    if rng.kind == "boundaryfaces":
+        return _ffi.RANGE_BOUNDARY_FACES, 0.0
+    return _ffi.RANGE_MARKED_FACES, float(rng.xmax)
+
+
 def boundaryfaces(mesh):
     return _Range(mesh, "boundaryfaces")
 
@@ -456,6 +465,7 @@ class Form1:
         for k in range(3):
             d.c[k] = src.c[k]
         d.quad_degree = integral.quad
+        d.range, d.range_xmax = _range_code(integral.range)
         self.env.check(self.env.lib.fgpu_assemble_vector(self.env.h, self.space.h, C.byref(d), self.vec.h, accumulate))
 
     def to_numpy(self):
@@ -529,6 +539,7 @@ class Form2:
         d.quad_degree = integral.quad
         d.algo = algo
         d.kappa_scale = None
+        d.range, d.range_xmax = _range_code(integral.range)
         kappa_arr = None
         for kind, c in integral.expr.terms:
             if kind == "stiff" and isinstance(c, _Scaled):

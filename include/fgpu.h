@@ -50,10 +50,16 @@ extern "C" {
 #define FGPU_ALGO_COLOUR 2        /* reserved (element-coloured scatter-add); runs FGPU_ALGO_GATHER */
 #define FGPU_ALGO_GATHER_NATIVE_F64 3 /* row-owner gather in native FP64 arithmetic (FP64 matrices; the
                                      default FP64 path computes in double-float on the FP32 pipes) */
-#define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles) into a device buffer, then one
-                                     thread per CSR entry sums its contributions in element order
-                                     through a gather map built once per space. AUTO picks it when
-                                     its buffers fit in device memory, else FGPU_ALGO_GATHER */
+#define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles; 3x3 blocks for elasticity) into
+                                     a device buffer in df64 (FP64 matrices) or binary32, then each CSR
+                                     entry sums its contributions in element order through a gather map
+                                     built once per space. AUTO picks it when its buffers fit in device
+                                     memory, else FGPU_ALGO_GATHER (elasticity: native FP64 / binary32) */
+
+#define FGPU_RANGE_ELEMENTS 0       /* _range=elements(mesh) */
+#define FGPU_RANGE_BOUNDARY_FACES 1 /* _range=boundaryfaces(mesh): faces of one element */
+#define FGPU_RANGE_MARKED_FACES 2   /* boundary faces whose vertices all have x <= range_xmax
+                                       (markedfaces of a plane), e.g. a clamped or loaded end */
 
 #define FGPU_RHS_SINE 0           /* f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */
 #define FGPU_RHS_CONST_VEC 1      /* f = (c0, c1, c2) (Pchv) */
@@ -101,12 +107,17 @@ typedef struct {
     const double* kappa_scale;/* device scalar multiplying kappa, read when the kernels run, so a
                                  captured graph sees its current value (a time-dependent
                                  coefficient kappa(t)); NULL = 1. Laplace/mass forms only. */
+    int range;                /* FGPU_RANGE_*; on faces only the mass term (alpha = mass) of a
+                                 Laplace/mass form on a scalar space: int_faces alpha u v (Robin) */
+    double range_xmax;        /* FGPU_RANGE_MARKED_FACES */
 } fgpu_form_desc;
 
 typedef struct {
     int kind;                 /* FGPU_RHS_* */
     double c[3];
     int quad_degree;          /* 0 = 2*order */
+    int range;                /* FGPU_RANGE_*; on faces: FGPU_RHS_CONST, int_faces c0 v (Neumann) */
+    double range_xmax;        /* FGPU_RANGE_MARKED_FACES */
 } fgpu_rhs_desc;
 
 typedef struct {

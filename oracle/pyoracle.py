@@ -186,3 +186,88 @@ def errors(order, xyz, tets, l2g, u, qdeg):
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+# ---------------------------------------------------------------------------
+# Boundary-face integrals (integrator.hpp MESH_FACES, :786-795), restated with
+# numpy on top of the oracle's basis tabulation: boundary faces are the faces
+# of one element (found by counting sorted vertex triples), visited in element
+# order; each face integral uses a collapsed Gauss-Legendre rule (numpy's
+# leggauss, 6 x 6 points, exact far beyond the degree-6 integrands) in the
+# element's reference coordinates, scaled by the physical face area (affine
+# faces). Face blocks are added like MatSetValues(ADD_VALUES).
+# ---------------------------------------------------------------------------
+_REF_VERTS = np.array([[-1.0, -1.0, -1.0], [1.0, -1.0, -1.0], [-1.0, 1.0, -1.0], [-1.0, -1.0, 1.0]])
+_FACE_VERTS = np.array([[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]])
+
+
+def boundary_faces(xyz, tets, xplane=None):
+    """(element, local face) of the faces of exactly one element, in element order; with xplane only
+    those whose three vertices have x <= xplane + 1e-12."""
+    counts = {}
+    keys = []
+    for e, t in enumerate(tets):
+        for f in range(4):
+            k = tuple(sorted(int(t[v]) for v in _FACE_VERTS[f]))
+            keys.append(k)
+            counts[k] = counts.get(k, 0) + 1
+    out = []
+    for idx, k in enumerate(keys):
+        if counts[k] != 1:
+            continue
+        e, f = divmod(idx, 4)
+        if xplane is not None and not all(xyz[v, 0] <= xplane + 1e-12 for v in k):
+            continue
+        out.append((e, f))
+    return out
+
+
+def _face_rule(f, npts=6):
+    g, w = np.polynomial.legendre.leggauss(npts)
+    u = (g + 1) / 2
+    wu = w / 2
+    A, B, C = _REF_VERTS[_FACE_VERTS[f]]
+    pts, wts = [], []
+    for i in range(npts):
+        for j in range(npts):
+            s, t = u[i], u[j] * (1 - u[i])
+            pts.append(A + s * (B - A) + t * (C - A))
+            wts.append(wu[i] * wu[j] * (1 - u[i]))
+    wts = np.array(wts)
+    return np.array(pts), wts / wts.sum()          # weights per unit face area
+
+
+def _face_area(xyz, tets, e, f):
+    P = xyz[tets[e][_FACE_VERTS[f]]]
+    return 0.5 * np.linalg.norm(np.cross(P[1] - P[0], P[2] - P[0]))
+
+
+def face_matrix(order, xyz, tets, l2g, ia, ja, alpha, xplane=None, val=None):
+    """val (nnz) += alpha int_faces phi_i phi_j, scattered into the CSR (ia, ja)."""
+    val = np.zeros(len(ja)) if val is None else val
+    tab = {}
+    for e, f in boundary_faces(xyz, tets, xplane):
+        if f not in tab:
+            pts, w = _face_rule(f)
+            phi, _ = tabulate(order, pts)
+            tab[f] = (phi * w[:, None]).T @ phi
+        blk = alpha * _face_area(xyz, tets, e, f) * tab[f]
+        dofs = l2g[e]
+        for a, r in enumerate(dofs):
+            cols = ja[ia[r]:ia[r + 1]]
+            for b, c in enumerate(dofs):
+                val[ia[r] + np.searchsorted(cols, c)] += blk[a, b]
+    return val
+
+
+def face_load(order, xyz, tets, l2g, N, g, xplane=None):
+    """F (N) = g int_faces phi_i."""
+    F = np.zeros(N)
+    tab = {}
+    for e, f in boundary_faces(xyz, tets, xplane):
+        if f not in tab:
+            pts, w = _face_rule(f)
+            phi, _ = tabulate(order, pts)
+            tab[f] = w @ phi
+        F[l2g[e]] += g * _face_area(xyz, tets, e, f) * tab[f]
+    return F

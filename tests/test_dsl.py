@@ -69,3 +69,15 @@ def test_solver_cfg_names():
     assert cfg.pc == _ffi.PC_CHEB_JACOBI and cfg.mixed == 1 and cfg.cheb_degree == 3
     with pytest.raises(ValueError):
         fe._solver_cfg(1e-10, 100, "gamg", False, 0.1, 16, "f64", 0, 0.0)
+
+
+def test_face_ranges():
+    class _M:
+        pass
+    m = _M()
+    d, _ = fe.Form2._desc_of(fe._Integral(fe.boundaryfaces(m), 2.0 * _mass(), 0), _ffi.ALGO_AUTO)
+    assert d.range == _ffi.RANGE_BOUNDARY_FACES and d.mass == 2.0
+    d, _ = fe.Form2._desc_of(fe._Integral(fe.markedfaces(m, 0.5), _mass(), 0), _ffi.ALGO_AUTO)
+    assert d.range == _ffi.RANGE_MARKED_FACES and d.range_xmax == 0.5
+    d, _ = fe.Form2._desc_of(fe._Integral(fe.elements(m), _stiff(), 0), _ffi.ALGO_AUTO)
+    assert d.range == _ffi.RANGE_ELEMENTS

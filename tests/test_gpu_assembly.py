@@ -209,3 +209,25 @@ def test_two_phase_equals_fused_gather(env, order, n, precision):
     assert np.array_equal(got[1], got[2])
     tol = 1e-6 if precision == "f32" else 1e-14
     assert_values_close(got[1], got[0], rtol=tol, atol=tol, what="two-phase vs fused")
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_elasticity_two_phase_vs_native(env, order, precision):
+    """Vector elasticity: df64 / binary32 two-phase blocks against the row-owner gather
+    (native FP64 / binary32 arithmetic), same pattern, values to rounding."""
+    from feelpp_gb300 import _ffi
+    xyz, tets = mesh(3, perturb=0.2, lengths=(2.0, 1.0, 1.0))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, order)
+    u, v = V.element(), V.element()
+    integral = fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, 1.3, 0.6), fpp.grad(v)))
+    got = []
+    for algo in (_ffi.ALGO_GATHER, _ffi.ALGO_TWO_PHASE):
+        a = fpp.form2(test=V, trial=V, precision=precision)
+        a.algo = algo
+        a.assign(integral)
+        a += integral
+        got.append(a.values())
+    tol = 2e-6 if precision == "f32" else 1e-13
+    assert_values_close(got[1], got[0], rtol=tol, atol=tol, what="elasticity two-phase vs gather")

@@ -174,3 +174,41 @@ def test_manufactured_convergence_rates(oracle):
     rl2 = math.log2(errs[0][0] / errs[1][0])
     rh1 = math.log2(errs[0][1] / errs[1][1])
     assert rl2 > 1.7 and rh1 > 0.85
+
+
+def test_face_integral_kats(oracle):
+    """Known answers of the boundary-face restatement: the P1 face mass matrix is
+    |f|/12 [[2,1,1],[1,2,1],[1,1,2]]; P2 vertex functions integrate to 0 over a
+    triangle and edge functions to |f|/3; the face masses of the unit cube sum to its
+    surface area 6."""
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    tets = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    faces = oracle.boundary_faces(xyz, tets)
+    assert len(faces) == 4
+    for order in (1, 2):
+        N, l2g = oracle.dof_table(tets, order)
+        F = oracle.face_load(order, xyz, tets, l2g, N, 1.0, xplane=None)
+        assert abs(F.sum() - (3 * 0.5 + np.sqrt(3) / 2)) < 1e-13      # total surface area
+    # P1 face mass on the face z = 0 (vertices 0, 1, 2; area 1/2)
+    N, l2g = oracle.dof_table(tets, 1)
+    ia, ja = oracle.pattern(N, l2g)
+    val = np.zeros(len(ja))
+    pts, w = oracle._face_rule(3)
+    phi, _ = oracle.tabulate(1, pts)
+    M = (phi * w[:, None]).T @ phi * 0.5
+    expect = 0.5 / 12 * np.array([[2, 1, 1], [1, 2, 1], [1, 1, 2]])
+    assert np.allclose(M[np.ix_([0, 1, 2], [0, 1, 2])], expect, rtol=0, atol=1e-15)
+    # P2 on the same face: vertex functions integrate to 0, edge functions to |f|/3
+    pts, w = oracle._face_rule(3)
+    phi, _ = oracle.tabulate(2, pts)
+    L = w @ phi * 0.5
+    assert np.allclose(L[[0, 1, 2]], 0.0, atol=1e-15)
+    face3_edges = [4 + j for j in range(6) if set([(1, 2), (2, 0), (0, 1), (0, 3), (1, 3), (2, 3)][j]) <= {0, 1, 2}]
+    assert np.allclose(L[face3_edges], 0.5 / 3, atol=1e-15)
+    # unit cube: sum of all boundary face masses = 6
+    from feelpp_gb300 import meshgen
+    xyz, tets = meshgen.kuhn_box(3, perturb=0.0)
+    N, l2g = oracle.dof_table(tets, 2)
+    ia, ja = oracle.pattern(N, l2g)
+    val = oracle.face_matrix(2, xyz, tets, l2g, ia, ja, 1.0)
+    assert abs(val.sum() - 6.0) < 1e-12
