@@ -421,8 +421,10 @@ class _Integral:
 
 
 def integrate(range, expr, quad=0):  # noqa: A002 - Feel++ keyword
-    if range.kind != "elements":
-        raise ValueError("only element integrals are on the device path")
+    """integrate(_range=elements(mesh) | boundaryfaces(mesh) | markedfaces(mesh, xmax), _expr=...).
+    On faces: alpha*idt(u)*id(v) (Robin mass) in a form2, g*id(v) (constant load) in a form1."""
+    if range.kind not in ("elements", "boundaryfaces", "markedfaces"):
+        raise ValueError("unknown integration range")
     return _Integral(range, expr, quad)
 
 
