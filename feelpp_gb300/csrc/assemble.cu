@@ -1378,11 +1378,14 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 
 // One thread per CSR entry, its contributions in batches of 4 (the index and
 // value loads of a batch are issued together; the sum stays in element
-// order). Measured against two alternatives at P2 48^3 (0.32 ms): entries
-// sorted by contribution count within 256-entry windows (0.50 ms: the
-// permuted writes lose their coalescing) and a warp-flat load of the 32
-// entries' contributions staged in shared memory (0.39 ms: fewer loads in
-// flight per warp).
+// order). Measured against three alternatives at P2 48^3 (this: 0.32 ms):
+// entries sorted by contribution count within 256-entry windows (0.50 ms: the
+// permuted writes lose their coalescing); a warp-flat load of the 32 entries'
+// contributions staged in shared memory (0.39 ms: fewer loads in flight per
+// warp); a split into entries with at most 2 contributions (one unrolled step,
+// 0.21 ms, 70 % of DRAM peak) and the others taken from a list sorted by count
+// (0.30 ms: the sorted list scatters the reads of the element buffer, 1.75 GB
+// of DRAM reads for 5.4 M entries).
 template <int MODE>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
