@@ -443,11 +443,13 @@ def run_matfree(args):
     integral = fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v)))
     bd = V.boundary_dofs()
     ops = {}
-    for name, prec, tc in [("f32_tensor_cores", "f32", True), ("f32_cuda_cores", "f32", False), ("df64", "df64", False),
-                           ("f64", "f64", False)]:
+    for name, prec, tc in [("f32_tensor_cores", "f32", True), ("f32_cuda_cores", "f32", False),
+                           ("f32_colour_scatter", "f32", False), ("df64", "df64", False), ("f64", "f64", False)]:
         op = fpp.operator(V, integral, precision=prec)
         if tc:
             op.use_tensor_cores(True)
+        if name == "f32_colour_scatter":
+            op.set_algo("colour")
         op.set_dirichlet(bd)
         ops[name] = op
     x, y = V.element(), V.element()
@@ -492,6 +494,7 @@ def run_matfree(args):
     solve["mixed_fp32_tensor_cores"], w_tc = mf_solve(ops["f64"], ops["f32_tensor_cores"])
     solve["mixed_fp32_cuda_cores"], _ = mf_solve(ops["f64"], ops["f32_cuda_cores"])
     solve["mixed_fp32_cheb_jacobi"], _ = mf_solve(ops["f64"], ops["f32_cuda_cores"], pc="cheb_jacobi", cheb_degree=3)
+    solve["mixed_fp32_colour_scatter"], _ = mf_solve(ops["f64"], ops["f32_colour_scatter"])
     if args.with_plain:
         solve["fp64_matfree_df64"], w64 = mf_solve(ops["df64"])
     csr = None
@@ -521,7 +524,7 @@ def run_matfree(args):
         del a
     ref_l2 = solve.get("fp64_matfree_df64", {}).get("l2_error") or (csr["fp64_cg"]["l2_error"] if csr else None)
     if ref_l2:
-        for k in ("mixed_fp32_tensor_cores", "mixed_fp32_cuda_cores", "mixed_fp32_cheb_jacobi"):
+        for k in ("mixed_fp32_tensor_cores", "mixed_fp32_cuda_cores", "mixed_fp32_cheb_jacobi", "mixed_fp32_colour_scatter"):
             solve[k]["l2_error_rel_diff_vs_fp64"] = abs(solve[k]["l2_error"] - ref_l2) / ref_l2
     out = {"metric": "P%d matrix-free operator apply GDOF/s & CG time-to-1e-10 (FP32 inner + FP64 residual)" % args.order,
            "value": applies["f32_cuda_cores"]["gdof_per_s"], "unit": "GDOF/s", "n_gpus": 1,

@@ -103,6 +103,7 @@ SIGNATURES = {
     "fgpu_operator_apply": (i32, [P, P, P, P]),
     "fgpu_operator_destroy": (i32, [P]),
     "fgpu_operator_set_tensor_cores": (i32, [P, i32]),
+    "fgpu_operator_set_algo": (i32, [P, i32]),
     "fgpu_tc_selftest": (i32, [P, P, P, P]),
     "fgpu_solve_cg_operator": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
     "fgpu_host_dof_table": (i32, [i64, i64, P, i32, i32, P, I64P]),

@@ -33,51 +33,66 @@ namespace fgpu {
 // element phase
 // ---------------------------------------------------------------------------
 // binary32: one thread per element; T (7 n n floats) in shared memory.
-// binary32 element phase, one thread per element. The warp's 32 elements'
-// l2n rows are staged in shared memory with coalesced loads (row stride N + 1:
-// no bank conflicts), the element values are written local-index-major
-// (coalesced). Gated by the CG stop flag when `stop` is set.
+// binary32 element phase, two elements per thread (each reference-tensor value
+// read from shared memory serves both: the loop is bound by shared-memory loads,
+// not FMAs). The warp's 64 elements' l2n rows are staged in shared memory with
+// coalesced loads (row stride N + 1: no bank conflicts); element values are
+// written local-index-major (coalesced).
 template <int N>
 __device__ __forceinline__ void mf_element_f32_body(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
                                                     const float* __restrict__ Tg, const float* __restrict__ x,
                                                     const uint8_t* __restrict__ mask, float* __restrict__ ye) {
     constexpr int NT = 7 * N * N;
+    constexpr int EW = 64;                       // elements per warp pass
     __shared__ float T[NT];
-    __shared__ int32_t sl2n[4][32 * (N + 1)];
+    __shared__ int32_t sl2n[4][EW * (N + 1)];
     for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int32_t* my = sl2n[warp];
-    for (int64_t e0 = ((int64_t)blockIdx.x * 4 + warp) * 32; e0 < nt; e0 += (int64_t)gridDim.x * 128) {
-        const int ne = (int)min((int64_t)32, nt - e0);
+    for (int64_t e0 = ((int64_t)blockIdx.x * 4 + warp) * EW; e0 < nt; e0 += (int64_t)gridDim.x * 4 * EW) {
+        const int ne = (int)min((int64_t)EW, nt - e0);
         for (int k = lane; k < ne * N; k += 32) {
             const int el = k / N, j = k - el * N;
             my[el * (N + 1) + j] = __ldg(l2n + e0 * N + k);
         }
         __syncwarp();
-        const int64_t e = e0 + lane;
-        if (lane < ne) {
-            float xe[N];
+        // lane handles elements e0 + lane and e0 + 32 + lane
+        const bool va = lane < ne, vb = lane + 32 < ne;
+        float xa[N], xb[N];
 #pragma unroll
-            for (int j = 0; j < N; ++j) {
-                const int32_t d = my[lane * (N + 1) + j];
-                xe[j] = (mask && mask[d]) ? 0.0f : __ldg(x + d);
-            }
-            const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
-            const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+        for (int j = 0; j < N; ++j) {
+            const int32_t da = va ? my[lane * (N + 1) + j] : 0;
+            const int32_t db = vb ? my[(lane + 32) * (N + 1) + j] : 0;
+            xa[j] = (!va || (mask && mask[da])) ? 0.0f : __ldg(x + da);
+            xb[j] = (!vb || (mask && mask[db])) ? 0.0f : __ldg(x + db);
+        }
+        float ca[7], cb[7];
+        {
+            const int64_t ea = va ? e0 + lane : e0, eb = vb ? e0 + 32 + lane : e0;
+            const float4 a0 = __ldg(rec + 4 * ea), a1 = __ldg(rec + 4 * ea + 1);
+            const float4 b0 = __ldg(rec + 4 * eb), b1 = __ldg(rec + 4 * eb + 1);
+            ca[0] = a0.x; ca[1] = a0.y; ca[2] = a0.z; ca[3] = a0.w; ca[4] = a1.x; ca[5] = a1.y; ca[6] = a1.z;
+            cb[0] = b0.x; cb[1] = b0.y; cb[2] = b0.z; cb[3] = b0.w; cb[4] = b1.x; cb[5] = b1.y; cb[6] = b1.z;
+        }
 #pragma unroll 1
-            for (int i = 0; i < N; ++i) {
-                float acc = 0.0f;
+        for (int i = 0; i < N; ++i) {
+            float acca = 0.0f, accb = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 7; ++k) {
-                    const float* Tk = T + (k * N + i) * N;
-                    float sum = 0.0f;
+            for (int k = 0; k < 7; ++k) {
+                const float* Tk = T + (k * N + i) * N;
+                float sa = 0.0f, sb = 0.0f;
 #pragma unroll
-                    for (int j = 0; j < N; ++j) sum = fmaf(Tk[j], xe[j], sum);
-                    acc = fmaf(c[k], sum, acc);
+                for (int j = 0; j < N; ++j) {
+                    const float t = Tk[j];
+                    sa = fmaf(t, xa[j], sa);
+                    sb = fmaf(t, xb[j], sb);
                 }
-                ye[(int64_t)i * nt + e] = acc;
+                acca = fmaf(ca[k], sa, acca);
+                accb = fmaf(cb[k], sb, accb);
             }
+            if (va) ye[(int64_t)i * nt + e0 + lane] = acca;
+            if (vb) ye[(int64_t)i * nt + e0 + 32 + lane] = accb;
         }
         __syncwarp();
     }
@@ -215,6 +230,69 @@ __global__ void mf_gather_df_kernel(int64_t nnodes, int64_t nt, const int64_t* _
     }
 }
 
+// x with the Dirichlet entries zeroed (the element phase then gathers without
+// reading the mask); gated by the CG stop flag
+__global__ void mask_copy_f32_kernel(int64_t n, const float* __restrict__ x, const uint8_t* __restrict__ mask, float* __restrict__ xm,
+                                     const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        xm[i] = mask[i] ? 0.0f : x[i];
+}
+
+// ---- graph-coloured scatter (FGPU_ALGO_COLOUR): elements coloured so that two
+// elements of a colour share no vertex (hence no dof); per colour, one thread
+// per element computes y_e = K_e x_e and adds it into y directly. No element
+// buffer and no node phase; every entry of y receives its element
+// contributions in colour order (deterministic, no atomics).
+template <int N>
+__global__ void __launch_bounds__(128) mf_scatter_f32_kernel(int64_t c0, int64_t c1, const int32_t* __restrict__ perm,
+                                                             const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
+                                                             const float* __restrict__ Tg, const float* __restrict__ xm,
+                                                             const uint8_t* __restrict__ mask, float* __restrict__ y,
+                                                             const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    constexpr int NT = 7 * N * N;
+    __shared__ float T[NT];
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
+    __syncthreads();
+    for (int64_t k = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c1; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = perm[k];
+        int32_t d[N];
+        float xe[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            d[j] = __ldg(l2n + e * N + j);
+            xe[j] = __ldg(xm + d[j]);          // x with the Dirichlet entries zeroed
+        }
+        const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
+        const float c[7] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z};
+#pragma unroll 1
+        for (int i = 0; i < N; ++i) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int kk = 0; kk < 7; ++kk) {
+                const float* Tk = T + (kk * N + i) * N;
+                float sum = 0.0f;
+#pragma unroll
+                for (int j = 0; j < N; ++j) sum = fmaf(Tk[j], xe[j], sum);
+                acc = fmaf(c[kk], sum, acc);
+            }
+            if (!(mask && mask[d[i]])) y[d[i]] += acc;
+        }
+    }
+}
+
+// y = (Dirichlet rows) x, else 0; and the masked copy xm of x
+__global__ void scatter_init_f32_kernel(int64_t n, const float* __restrict__ x, const uint8_t* __restrict__ mask,
+                                        float* __restrict__ y, float* __restrict__ xm, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const bool m = mask && mask[i];
+        y[i] = m ? x[i] : 0.0f;
+        xm[i] = m ? 0.0f : x[i];
+    }
+}
+
 // diagonal of the operator (Jacobi): element diagonals then the node gather
 template <typename T>
 __global__ void mf_diag_element_kernel(int64_t nt, int N, const float4* __restrict__ rec, const double* __restrict__ T7,
@@ -248,8 +326,11 @@ struct fgpu_operator {
     uint8_t* d_mask = nullptr;       // Dirichlet mask (nnodes) or null
     void* d_diag = nullptr;          // operator diagonal (float or double)
     float* d_xf = nullptr;           // binary32 work vectors for the F32 solve
+    float* d_xm = nullptr;           // binary32 x with the Dirichlet entries zeroed (element phase input)
     int64_t nt = 0, nnodes = 0;
     int use_tc = 0;                  // binary32 element phase on the tensor cores (tcgen05, P2/P3)
+    int algo = FGPU_ALGO_GATHER;     // FGPU_ALGO_GATHER (element buffer + node gather) or FGPU_ALGO_COLOUR
+    float* d_xs = nullptr;           // colour scatter: masked copy of x
 };
 
 namespace fgpu {
@@ -262,6 +343,8 @@ static int blocks_for(int64_t n, int threads, int cap) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, cap));
 }
 
+static int mf_apply_colour_f32(fgpu_ctx* ctx, fgpu_operator* op, const float* x, float* y, const int* stop);
+
 // y = A x; x, y device arrays of nnodes entries in the operator's storage type
 // (float for F32, double for F64 / DF64)
 int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y) {
@@ -269,16 +352,32 @@ int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y) {
     const int n = V->n;
     const int64_t nt = op->nt;
     PendingEvent ev;
+    if (op->precision == FGPU_F32 && op->algo == FGPU_ALGO_COLOUR) {
+        prof_begin(ctx, "matfree_element", ev);
+        ctx->launches += mf_apply_colour_f32(ctx, op, (const float*)x, (float*)y, nullptr);
+        prof_end(ctx, ev);
+        FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+        return FGPU_OK;
+    }
     prof_begin(ctx, "matfree_element", ev);
     const int eb = blocks_for(nt, 128, 152 * 16);
+    const float* xe = (const float*)x;
+    const uint8_t* me = op->d_mask;
+    if (op->precision == FGPU_F32 && op->d_mask && op->d_xm) {
+        mask_copy_f32_kernel<<<blocks_for(op->nnodes, 256, 152 * 8), 256, 0, ctx->stream>>>(op->nnodes, (const float*)x, op->d_mask,
+                                                                                        op->d_xm, nullptr);
+        ++ctx->launches;
+        xe = op->d_xm;
+        me = nullptr;
+    }
     if (op->precision == FGPU_F32 && op->use_tc && (n == 10 || n == 20)) {
-        int rc = launch_mf_element_tc(ctx, n, nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, nullptr);
+        int rc = launch_mf_element_tc(ctx, n, nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, nullptr);
         if (rc) return rc;
     } else if (op->precision == FGPU_F32) {
         switch (n) {
-            case 4: mf_element_f32_kernel<4><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
-            case 10: mf_element_f32_kernel<10><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
-            case 20: mf_element_f32_kernel<20><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye); break;
+            case 4: mf_element_f32_kernel<4><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye); break;
+            case 10: mf_element_f32_kernel<10><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye); break;
+            case 20: mf_element_f32_kernel<20><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye); break;
             default: return FGPU_ERR_INVALID;
         }
     } else if (op->precision == FGPU_F64) {
@@ -346,6 +445,22 @@ int operator_diagonal(fgpu_ctx* ctx, fgpu_operator* op) {
 // matrix-free CG
 // ===========================================================================
 #include "cg_driver.cuh"
+
+namespace fgpu {
+// per-block partials of x.y
+template <class PL>
+__global__ void dot_partial_kernel(int64_t n, const typename PL::S* __restrict__ x, const typename PL::S* __restrict__ y,
+                                   typename PL::D* __restrict__ partial, const CGScalars<PL>* __restrict__ sc) {
+    if (sc && sc->done) return;
+    __shared__ typename PL::D sh[32];
+    typename PL::D s = PL::dzero();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = PL::dmadd(s, PL::ld(x[i]), PL::ld(y[i]));
+    const typename PL::D t = block_sum<PL>(s, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+}  // namespace fgpu
 
 namespace fgpu {
 
@@ -418,20 +533,60 @@ __global__ void dinv_from_diag_kernel(int64_t n, const typename PL::S* __restric
 int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y);
 
 // element phase + fused node phase; F32 uses the gated kernel (graph-safe)
+// FGPU_ALGO_COLOUR binary32 apply: y = A x, with optional x.y partials
+static int mf_apply_colour_f32(fgpu_ctx* ctx, fgpu_operator* op, const float* x, float* y, const int* stop) {
+    const fgpu_space* V = op->space;
+    const fgpu_mesh* M = V->mesh;
+    const int n = V->n;
+    int nl = 1;
+    scatter_init_f32_kernel<<<blocks_for(op->nnodes, 256, 152 * 8), 256, 0, ctx->stream>>>(op->nnodes, x, op->d_mask, y, op->d_xs, stop);
+    for (int c = 0; c < M->ncolours; ++c) {
+        const int64_t c0 = M->colour_ptr[c], c1 = M->colour_ptr[c + 1];
+        if (c1 <= c0) continue;
+        const int b = blocks_for(c1 - c0, 128, 152 * 16);
+        switch (n) {
+            case 4: mf_scatter_f32_kernel<4><<<b, 128, 0, ctx->stream>>>(c0, c1, M->d_colour_perm, V->d_l2n, op->d_rec, op->tab->d_T7f, op->d_xs, op->d_mask, y, stop); break;
+            case 10: mf_scatter_f32_kernel<10><<<b, 128, 0, ctx->stream>>>(c0, c1, M->d_colour_perm, V->d_l2n, op->d_rec, op->tab->d_T7f, op->d_xs, op->d_mask, y, stop); break;
+            default: mf_scatter_f32_kernel<20><<<b, 128, 0, ctx->stream>>>(c0, c1, M->d_colour_perm, V->d_l2n, op->d_rec, op->tab->d_T7f, op->d_xs, op->d_mask, y, stop); break;
+        }
+        ++nl;
+    }
+    return nl;
+}
+
+// returns the number of kernels launched
 template <class PL>
-static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* x, typename PL::S* y, typename PL::D* partial,
-                        const CGScalars<PL>* sc, int gblocks) {
+static int mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* x, typename PL::S* y, typename PL::D* partial,
+                       const CGScalars<PL>* sc, int gblocks) {
     const fgpu_space* V = op->space;
     const int n = V->n;
     const int eb = blocks_for(op->nt, 128, 152 * 16);
     const int* stop = sc ? &sc->done : nullptr;
+    if (op->precision == FGPU_F32 && op->algo == FGPU_ALGO_COLOUR) {
+        int nc = mf_apply_colour_f32(ctx, op, (const float*)x, (float*)y, stop);
+        if (partial) {
+            dot_partial_kernel<PL><<<gblocks, 256, 0, ctx->stream>>>(op->nnodes, x, y, partial, sc);
+            ++nc;
+        }
+        return nc;
+    }
+    int nl = 2;
+    const float* xe = (const float*)x;
+    const uint8_t* me = op->d_mask;
+    if (op->precision == FGPU_F32 && op->d_mask && op->d_xm) {
+        mask_copy_f32_kernel<<<blocks_for(op->nnodes, 256, 152 * 8), 256, 0, ctx->stream>>>(op->nnodes, (const float*)x, op->d_mask,
+                                                                                        op->d_xm, stop);
+        ++nl;
+        xe = op->d_xm;
+        me = nullptr;
+    }
     if (op->precision == FGPU_F32 && op->use_tc && (n == 10 || n == 20)) {
-        launch_mf_element_tc(ctx, n, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop);
+        launch_mf_element_tc(ctx, n, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop);
     } else if (op->precision == FGPU_F32) {
         switch (n) {
-            case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
-            case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
-            default: mf_element_f32_gated<20><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, (const float*)x, op->d_mask, (float*)op->d_ye, stop); break;
+            case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+            case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+            default: mf_element_f32_gated<20><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
         }
     } else {
         // binary64 element phases (native or df64); not gated: the FP64 matrix-free solve polls every iteration
@@ -455,7 +610,7 @@ static void mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* 
     }
     mf_gather_dot_kernel<PL><<<gblocks, 256, 0, ctx->stream>>>(op->nnodes, op->nt, V->d_inc_ptr, V->d_inc,
                                                               (const typename PL::S*)op->d_ye, x, op->d_mask, y, partial, sc);
-    ctx->launches += 2;
+    return nl;
 }
 
 // Matrix-free PCG with Jacobi or Chebyshev-Jacobi (operator diagonal). The
@@ -474,11 +629,17 @@ static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b
     ctx->launches++;
     CgOperator<PL> A;
     A.apply = [ctx, op, vb](const S* xx, S* yy, typename PL::D* partial, const CGScalars<PL>* sc) {
-        mf_apply_cg<PL>(ctx, op, xx, yy, partial, sc, vb);
-        ctx->launches -= 2;   // cg_run counts the launches of an application
+        mf_apply_cg<PL>(ctx, op, xx, yy, partial, sc, vb);   // cg_run counts the launches of an application
     };
     A.npq = vb;
-    A.launches = 2;
+    if (op->precision == FGPU_F32 && op->algo == FGPU_ALGO_COLOUR) {
+        int nc = 0;
+        for (int c = 0; c < op->space->mesh->ncolours; ++c)
+            if (op->space->mesh->colour_ptr[c + 1] > op->space->mesh->colour_ptr[c]) ++nc;
+        A.launches = 2 + nc;          // init, colours, dot
+    } else {
+        A.launches = (op->precision == FGPU_F32 && op->d_mask && op->d_xm) ? 3 : 2;
+    }
     A.graph = op->precision == FGPU_F32;
     const int rc = cg_run<PL>(ctx, n, A, dinv, b, x, o, res, refresh);
     cudaFree(dinv);
@@ -502,7 +663,7 @@ static double host_norm(fgpu_ctx* ctx, int64_t n, const double* d) {
 
 // ||b - A x|| with the binary64 (native or df64) operator
 static int mf_residual64(fgpu_ctx* ctx, fgpu_operator* op, const double* b, const double* x, double* r, double* q, double* out) {
-    mf_apply_cg<PolF64>(ctx, op, x, q, nullptr, nullptr, vec_blocks(op->nnodes));
+    ctx->launches += mf_apply_cg<PolF64>(ctx, op, x, q, nullptr, nullptr, vec_blocks(op->nnodes));
     residual_from_q_kernel<PolF64><<<vec_blocks(op->nnodes), 256, 0, ctx->stream>>>(op->nnodes, b, q, r);
     ctx->launches++;
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
@@ -721,6 +882,7 @@ extern "C" int fgpu_operator_set_dirichlet(fgpu_operator* op, int64_t ndofs, con
         m[dofs[k]] = 1;
     }
     if (!op->d_mask) FGPU_CUDA_CHECK(ctx, cudaMalloc(&op->d_mask, op->nnodes));
+    if (op->precision == FGPU_F32 && !op->d_xm) FGPU_CUDA_CHECK(ctx, cudaMalloc(&op->d_xm, op->nnodes * sizeof(float)));
     FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(op->d_mask, m.data(), op->nnodes, cudaMemcpyHostToDevice, ctx->stream));
     int rc = operator_diagonal(ctx, op);
     if (rc) return rc;
@@ -765,6 +927,26 @@ extern "C" int fgpu_operator_set_tensor_cores(fgpu_operator* op, int on) {
     return FGPU_OK;
 }
 
+extern "C" int fgpu_operator_set_algo(fgpu_operator* op, int algo) {
+    if (!op) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = op->ctx;
+    if (algo == FGPU_ALGO_GATHER || algo == FGPU_ALGO_AUTO) { op->algo = FGPU_ALGO_GATHER; return FGPU_OK; }
+    if (algo != FGPU_ALGO_COLOUR) { ctx->err = "operator: algorithm must be GATHER or COLOUR"; return FGPU_ERR_INVALID; }
+    if (op->precision != FGPU_F32 || op->use_tc) { ctx->err = "colour scatter: binary32 CUDA-core operators only"; return FGPU_ERR_INVALID; }
+    fgpu_mesh* M = op->space->mesh;
+    if (!M->d_colour_perm) {
+        std::vector<int32_t> perm;
+        const int nc = colour_elements(M->nv, M->nt, M->h_tets.data(), perm, M->colour_ptr);
+        if (nc < 0) { ctx->err = "colour scatter: more than 64 colours"; return FGPU_ERR_INVALID; }
+        FGPU_CUDA_CHECK(ctx, cudaMalloc(&M->d_colour_perm, perm.size() * sizeof(int32_t)));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(M->d_colour_perm, perm.data(), perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        M->ncolours = nc;
+    }
+    if (!op->d_xs) FGPU_CUDA_CHECK(ctx, cudaMalloc(&op->d_xs, op->nnodes * sizeof(float)));
+    op->algo = FGPU_ALGO_COLOUR;
+    return FGPU_OK;
+}
+
 extern "C" int fgpu_operator_destroy(fgpu_operator* op) {
     if (!op) return FGPU_OK;
     cudaFree(op->d_rec);
@@ -773,6 +955,8 @@ extern "C" int fgpu_operator_destroy(fgpu_operator* op) {
     cudaFree(op->d_mask);
     cudaFree(op->d_diag);
     cudaFree(op->d_xf);
+    cudaFree(op->d_xm);
+    cudaFree(op->d_xs);
     delete op;
     return FGPU_OK;
 }

@@ -649,6 +649,11 @@ class Operator:
         """binary32 P2/P3 operators: element phase on the tensor cores (tcgen05, 3xTF32)."""
         self.env.check(self.env.lib.fgpu_operator_set_tensor_cores(self.h, 1 if on else 0))
 
+    def set_algo(self, algo):
+        """"gather" (element buffer + node gather) or "colour" (graph-coloured scatter, binary32)."""
+        self.env.check(self.env.lib.fgpu_operator_set_algo(self.h, {"gather": _ffi.ALGO_GATHER,
+                                                                    "colour": _ffi.ALGO_COLOUR}[algo]))
+
     def set_dirichlet(self, dofs):
         dofs = np.ascontiguousarray(dofs, dtype=np.int32)
         self.env.check(self.env.lib.fgpu_operator_set_dirichlet(self.h, len(dofs), _ptr(dofs)))

@@ -47,7 +47,8 @@ extern "C" {
 
 #define FGPU_ALGO_AUTO 0          /* best available algorithm for the form */
 #define FGPU_ALGO_GATHER 1        /* row-owner gather: each CSR row summed by one warp, element order */
-#define FGPU_ALGO_COLOUR 2        /* reserved (element-coloured scatter-add); runs FGPU_ALGO_GATHER */
+#define FGPU_ALGO_COLOUR 2        /* element-coloured scatter-add (matrix-free binary32 operators,
+                                     fgpu_operator_set_algo); assembly runs FGPU_ALGO_GATHER */
 #define FGPU_ALGO_GATHER_NATIVE_F64 3 /* row-owner gather in native FP64 arithmetic (FP64 matrices; the
                                      default FP64 path computes in double-float on the FP32 pipes) */
 #define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles; 3x3 blocks for elasticity) into
@@ -253,6 +254,10 @@ int fgpu_operator_destroy(fgpu_operator* op);
 /* run the binary32 element phase on the tensor cores (tcgen05.mma kind::tf32, 3xTF32 split,
  * accumulator in tensor memory); P2 / P3 binary32 operators */
 int fgpu_operator_set_tensor_cores(fgpu_operator* op, int on);
+/* binary32 operators: FGPU_ALGO_GATHER (element buffer, then one node-ordered gather; default) or
+ * FGPU_ALGO_COLOUR (elements coloured so that a colour shares no vertex, one launch per colour
+ * adds y_e into y: no element buffer, no node phase; sums in colour order) */
+int fgpu_operator_set_algo(fgpu_operator* op, int algo);
 /* tensor-core self-check: D = A B^T with A 128 x 24 and B 144 x 24 (row-major binary32, host
  * arrays) through the same staging / descriptors / MMA / read-back as the operator */
 int fgpu_tc_selftest(fgpu_ctx* ctx, const float* A, const float* B, float* D);

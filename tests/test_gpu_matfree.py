@@ -98,3 +98,50 @@ def test_mixed_matfree_cheb_jacobi(env):
     stj = op64.solve(l, w, rtol=1e-10, inner=op32)
     assert st["iterations"] * 1.5 <= stj["iterations"]
     assert np.linalg.norm(u.to_numpy() - w.to_numpy()) <= 1e-8 * np.linalg.norm(w.to_numpy())
+
+
+@pytest.mark.parametrize("order,n,dirichlet", [(1, 8, True), (2, 6, True), (3, 4, False)])
+def test_colour_scatter_apply(env, order, n, dirichlet):
+    xyz, tets, M, V, integral, a, l = system(env, n, order, with_dirichlet=dirichlet)
+    opg = fpp.operator(V, integral, precision="f32")
+    opc = fpp.operator(V, integral, precision="f32")
+    opc.set_algo("colour")
+    if dirichlet:
+        opg.set_dirichlet(V.boundary_dofs())
+        opc.set_dirichlet(V.boundary_dofs())
+    x = np.random.default_rng(7).standard_normal(V.ndof)
+    xv, yg, yc, zv = V.element(), V.element(), V.element(), V.element()
+    xv.upload(x)
+    opg.apply(xv, yg)
+    opc.apply(xv, yc)
+    a.mult(xv, zv)
+    z = zv.to_numpy()
+    assert np.abs(yc.to_numpy() - z).max() <= TOL["f32"] * np.abs(z).max()
+    assert np.abs(yc.to_numpy() - yg.to_numpy()).max() <= TOL["f32"] * np.abs(z).max()
+    # the colour order is fixed: two applies give the same bits
+    y2 = V.element()
+    opc.apply(xv, y2)
+    assert np.array_equal(y2.to_numpy(), yc.to_numpy())
+
+
+def test_colour_scatter_mixed_solve(env):
+    xyz, tets, M, V, integral, a, l = system(env, 6, 3)
+    op64 = fpp.operator(V, integral, precision="f64")
+    op32 = fpp.operator(V, integral, precision="f32")
+    op32.set_algo("colour")
+    bd = V.boundary_dofs()
+    op64.set_dirichlet(bd)
+    op32.set_dirichlet(bd)
+    u = V.element()
+    st = op64.solve(l, u, rtol=1e-10, inner=op32)
+    assert st["rel_residual"] <= 1e-10
+    w = V.element()
+    a.solve(rhs=l, solution=w, rtol=1e-11)
+    assert np.linalg.norm(u.to_numpy() - w.to_numpy()) <= 1e-8 * np.linalg.norm(w.to_numpy())
+
+
+def test_colour_scatter_rejects_f64(env):
+    xyz, tets, M, V, integral, a, l = system(env, 4, 1)
+    op = fpp.operator(V, integral, precision="f64")
+    with pytest.raises(Exception):
+        op.set_algo("colour")
