@@ -14,7 +14,7 @@ F64, F32, DF64 = 0, 1, 2
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
 RANGE_ELEMENTS, RANGE_BOUNDARY_FACES, RANGE_MARKED_FACES = 0, 1, 2
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE = 0, 1, 2, 3, 4
-RHS_SINE, RHS_CONST_VEC, RHS_CONST = 0, 1, 2
+RHS_SINE, RHS_CONST_VEC, RHS_CONST, RHS_FACE = 0, 1, 2, 3
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
 PC_NONE, PC_JACOBI, PC_CHEB_JACOBI = 0, 1, 2
 ARITH_F64, ARITH_DF64 = 0, 1
@@ -37,7 +37,8 @@ class Config(C.Structure):
 class FormDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("kappa", C.c_double), ("kappa_elem", C.c_void_p), ("mass", C.c_double),
                 ("lam", C.c_double), ("mu", C.c_double), ("quad_degree", C.c_int), ("algo", C.c_int),
-                ("kappa_scale", C.c_void_p), ("range", C.c_int), ("range_xmax", C.c_double)]
+                ("kappa_scale", C.c_void_p), ("range", C.c_int), ("range_xmax", C.c_double), ("mass_h", C.c_double),
+                ("dn_trial", C.c_double), ("dn_test", C.c_double)]
 
 
 class RhsDesc(C.Structure):

@@ -525,12 +525,15 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
     if (f->range == FGPU_RANGE_BOUNDARY_FACES || f->range == FGPU_RANGE_MARKED_FACES) {
         if (f->kind != FGPU_FORM_LAPLACE_MASS || f->kappa != 0.0 || d_kappa || f->kappa_scale)
-            return set_err(ctx, FGPU_ERR_INVALID, "face integrals: only the mass term alpha*idt(u)*id(v)");
-        const int rc = launch_face_matrix(ctx, A, f->range, f->range_xmax, f->mass, accumulate);
+            return set_err(ctx, FGPU_ERR_INVALID,
+                           "face integrals: terms idt(u)*id(v), idt(u)*id(v)/hFace(), (gradt(u).N)*id(v), (grad(v).N)*idt(u)");
+        const int rc = launch_face_matrix(ctx, A, f->range, f->range_xmax, f->mass, f->mass_h, f->dn_trial, f->dn_test, accumulate);
         if (rc) return rc;
         return finish(ctx);
     }
     if (f->range != FGPU_RANGE_ELEMENTS) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad range");
+    if (f->mass_h != 0.0 || f->dn_trial != 0.0 || f->dn_test != 0.0)
+        return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: hFace()/N() terms on face ranges only");
     fgpu_space* V = A->space;
     const int qdeg = form_qdeg(V, f->quad_degree);
     std::string err;
@@ -648,12 +651,16 @@ int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc
     FGPU_NO_CAPTURE(ctx, "assemble_vector");
     if (!ctx || !V || !rhs || !out || out->n != V->ndof) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad arguments");
     if (rhs->range == FGPU_RANGE_BOUNDARY_FACES || rhs->range == FGPU_RANGE_MARKED_FACES) {
-        if (rhs->kind != FGPU_RHS_CONST) return set_err(ctx, FGPU_ERR_INVALID, "face integrals: constant loads g*id(v)");
-        const int rc = launch_face_load(ctx, V, rhs->range, rhs->range_xmax, rhs->c[0], out->d, accumulate);
+        if (rhs->kind != FGPU_RHS_CONST && rhs->kind != FGPU_RHS_FACE)
+            return set_err(ctx, FGPU_ERR_INVALID, "face integrals: loads FGPU_RHS_CONST or FGPU_RHS_FACE");
+        const bool ft = rhs->kind == FGPU_RHS_FACE;
+        const int rc = launch_face_load(ctx, V, rhs->range, rhs->range_xmax, rhs->c[0], ft ? rhs->c[1] : 0.0, ft ? rhs->c[2] : 0.0,
+                                        out->d, accumulate);
         if (rc) return rc;
         return finish(ctx);
     }
     if (rhs->range != FGPU_RANGE_ELEMENTS) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad range");
+    if (rhs->kind == FGPU_RHS_FACE) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: FGPU_RHS_FACE on face ranges only");
     const int qdeg = form_qdeg(V, rhs->quad_degree);
     std::string err;
     DevTables* tab = get_dev_tables(V->order, qdeg, err);

@@ -168,6 +168,8 @@ bool build_face_tables(int order, FaceTables& out, std::string& err) {
     out.n = n;
     out.Mf.assign((size_t)4 * n * n, 0.0);
     out.Lf.assign((size_t)4 * n, 0.0);
+    out.Gf.assign((size_t)4 * 3 * n * n, 0.0);
+    out.Df.assign((size_t)4 * 3 * n, 0.0);
     for (int f = 0; f < 4; ++f) {
         LD A[3], E1[3], E2[3];
         for (int d = 0; d < 3; ++d) {
@@ -175,9 +177,9 @@ bool build_face_tables(int order, FaceTables& out, std::string& err) {
             E1[d] = (LD)kRefVerts[kFaceVerts[f][1]][d] - A[d];
             E2[d] = (LD)kRefVerts[kFaceVerts[f][2]][d] - A[d];
         }
-        std::vector<LD> M((size_t)n * n, 0), L(n, 0);
+        std::vector<LD> M((size_t)n * n, 0), L(n, 0), G((size_t)3 * n * n, 0), D((size_t)3 * n, 0);
         LD wsum = 0;
-        std::vector<LD> phi(n);
+        std::vector<LD> phi(n), dphi((size_t)3 * n);
         for (int a = 0; a < kq; ++a)
             for (int b = 0; b < kq; ++b) {
                 // (s, t) = (u, v (1 - u)) on the unit triangle, jacobian (1 - u)
@@ -187,17 +189,30 @@ bool build_face_tables(int order, FaceTables& out, std::string& err) {
                 for (int d = 0; d < 3; ++d) P[d] = A[d] + s2 * E1[d] + t2 * E2[d];
                 const LD x = (P[0] + 1) / 2, y = (P[1] + 1) / 2, z = (P[2] + 1) / 2;
                 for (int i = 0; i < n; ++i) {
-                    LD vv = 0;
+                    LD vv = 0, gx = 0, gy = 0, gz = 0;
                     for (int m = 0; m < n; ++m) {
                         const LD c = C[(size_t)m * n + i];
-                        if (c != 0) vv += c * ipow(x, mono[m].a) * ipow(y, mono[m].b) * ipow(z, mono[m].c);
+                        if (c == 0) continue;
+                        const int ea = mono[m].a, eb = mono[m].b, ec = mono[m].c;
+                        vv += c * ipow(x, ea) * ipow(y, eb) * ipow(z, ec);
+                        // d/dxhat = (1/2) d/dxi on the [-1,1] reference element
+                        if (ea) gx += c * ea * ipow(x, ea - 1) * ipow(y, eb) * ipow(z, ec) / 2;
+                        if (eb) gy += c * eb * ipow(x, ea) * ipow(y, eb - 1) * ipow(z, ec) / 2;
+                        if (ec) gz += c * ec * ipow(x, ea) * ipow(y, eb) * ipow(z, ec - 1) / 2;
                     }
                     phi[i] = vv;
+                    dphi[i] = gx;
+                    dphi[(size_t)n + i] = gy;
+                    dphi[(size_t)2 * n + i] = gz;
                 }
                 wsum += w;
                 for (int i = 0; i < n; ++i) {
                     L[i] += w * phi[i];
                     for (int j = 0; j < n; ++j) M[(size_t)i * n + j] += w * phi[i] * phi[j];
+                    for (int a = 0; a < 3; ++a) {
+                        D[(size_t)a * n + i] += w * dphi[(size_t)a * n + i];
+                        for (int j = 0; j < n; ++j) G[((size_t)a * n + i) * n + j] += w * phi[i] * dphi[(size_t)a * n + j];
+                    }
                 }
             }
         // the weights sum to the unit triangle's area 1/2: normalise to unit face area
@@ -207,6 +222,14 @@ bool build_face_tables(int order, FaceTables& out, std::string& err) {
             for (int j = 0; j < n; ++j) {
                 LD mij = M[(size_t)i * n + j] / wsum;
                 out.Mf[((size_t)f * n + i) * n + j] = std::fabs(mij) < 1e-15L ? 0.0 : (double)mij;
+            }
+            for (int a = 0; a < 3; ++a) {
+                const LD di = D[(size_t)a * n + i] / wsum;
+                out.Df[((size_t)f * 3 + a) * n + i] = std::fabs(di) < 1e-15L ? 0.0 : (double)di;
+                for (int j = 0; j < n; ++j) {
+                    const LD g = G[((size_t)a * n + i) * n + j] / wsum;
+                    out.Gf[(((size_t)f * 3 + a) * n + i) * n + j] = std::fabs(g) < 1e-15L ? 0.0 : (double)g;
+                }
             }
         }
     }

@@ -42,6 +42,8 @@ struct FaceTables {                  // boundary-face integrals per unit face ar
     int order = 0, n = 0;
     std::vector<double> Mf;          // 4 x n x n : (1/|f|) int_f phi_i phi_j
     std::vector<double> Lf;          // 4 x n     : (1/|f|) int_f phi_i
+    std::vector<double> Gf;          // 4 x 3 x n x n : (1/|f|) int_f phi_i dphi_j/dxhat_a
+    std::vector<double> Df;          // 4 x 3 x n : (1/|f|) int_f dphi_i/dxhat_a
 };
 bool build_face_tables(int order, FaceTables& out, std::string& err);
 
@@ -69,7 +71,7 @@ bool build_node_pattern(const Topology& topo, int64_t nt, NodePattern& pat, int 
 
 int colour_elements(int64_t nv, int64_t nt, const int32_t* tets, std::vector<int32_t>& perm,
                     std::vector<int64_t>& colour_ptr);
-int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax,
+int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax, int whole_element,
                             std::vector<int32_t>& faces, std::vector<int64_t>& colour_ptr);
 
 // Boundary dof nodes: the nodes carried by faces owned by one element; when
@@ -163,6 +165,7 @@ struct fgpu_space {
     struct FaceSet {                 // boundary faces of a range, coloured (scatter without conflicts)
         int xmax_on = 0;
         double xmax = 0;
+        int whole = 0;               // coloured over whole elements (normal-derivative terms)
         int32_t* d_faces = nullptr;  // e * 4 + f, sorted by colour
         std::vector<int64_t> colour_ptr;
     };
@@ -254,8 +257,10 @@ int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* ta
 int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec);
 int launch_assemble_elasticity_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);
-int launch_face_matrix(fgpu_ctx* ctx, fgpu_matrix* A, int range, double xmax, double alpha, int accumulate);
-int launch_face_load(fgpu_ctx* ctx, const fgpu_space* V, int range, double xmax, double g, double* d_rhs, int accumulate);
+int launch_face_matrix(fgpu_ctx* ctx, fgpu_matrix* A, int range, double xmax, double mass, double mass_h, double dn_trial,
+                       double dn_test, int accumulate);
+int launch_face_load(fgpu_ctx* ctx, const fgpu_space* V, int range, double xmax, double g, double g_h, double g_dn,
+                     double* d_rhs, int accumulate);
 int build_space_device(fgpu_ctx* ctx, fgpu_space* V);
 int build_pattern_device(fgpu_ctx* ctx, fgpu_space* V, DevPattern& P, std::vector<int64_t>& h_ia);
 int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V);

@@ -249,10 +249,10 @@ int colour_elements(int64_t nv, int64_t nt, const int32_t* tets, std::vector<int
 
 // Boundary faces (faces of exactly one element) as e * 4 + f, in element order;
 // with xmax_on only those whose three vertices have x <= xmax (+1e-12). Then a
-// greedy colouring in that order (faces sharing a vertex get different
-// colours): `faces` comes back sorted by colour (stable), colour_ptr delimits
+// greedy colouring in that order (faces sharing a vertex, or with whole_element
+// faces whose elements share a vertex, get different colours): `faces` comes back sorted by colour (stable), colour_ptr delimits
 // the colours. Returns the number of colours (-1: more than 64 needed).
-int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax,
+int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax, int whole_element,
                             std::vector<int32_t>& faces, std::vector<int64_t>& colour_ptr) {
     std::vector<int32_t> keys, face_of_slot;
     face_keys(nt, tets, keys);
@@ -279,14 +279,22 @@ int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, 
     for (size_t k = 0; k < list.size(); ++k) {
         const int64_t e = list[k] >> 2;
         const int f = list[k] & 3;
+        // conflicts over the face's vertices, or over all four vertices of its element when the face
+        // block couples every element dof (normal-derivative terms)
+        int vs[4], nvs = 0;
+        if (whole_element) {
+            for (int v = 0; v < 4; ++v) vs[nvs++] = tets[4 * e + v];
+        } else {
+            for (int v = 0; v < 3; ++v) vs[nvs++] = tets[4 * e + kFaceVerts[f][v]];
+        }
         uint64_t m = 0;
-        for (int v = 0; v < 3; ++v) m |= used[tets[4 * e + kFaceVerts[f][v]]];
+        for (int v = 0; v < nvs; ++v) m |= used[vs[v]];
         int c = 0;
         while (c < 64 && ((m >> c) & 1)) ++c;
         if (c == 64) return -1;
         col[k] = (uint8_t)c;
         nc = std::max(nc, c + 1);
-        for (int v = 0; v < 3; ++v) used[tets[4 * e + kFaceVerts[f][v]]] |= (1ull << c);
+        for (int v = 0; v < nvs; ++v) used[vs[v]] |= (1ull << c);
     }
     colour_ptr.assign(nc + 1, 0);
     for (size_t k = 0; k < list.size(); ++k) colour_ptr[col[k] + 1]++;

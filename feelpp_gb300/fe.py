@@ -299,20 +299,50 @@ def markedfaces(mesh, xmax):
     return _Range(mesh, "markedfaces", xmax)
 
 
+class _Normal:
+    """N(): the unit outward normal of a boundary face."""
+
+
+class _HFace:
+    """hFace(): the longest edge of a boundary face (feelpp/feel/feelmesh/geond.hpp:737-757)."""
+
+
+def N():  # noqa: N802 - Feel++ name
+    return _Normal()
+
+
+def hFace():  # noqa: N802 - Feel++ name
+    return _HFace()
+
+
+def _is_num(c):
+    return isinstance(c, (int, float, np.floating, np.integer))
+
+
 class _Op:
-    def __init__(self, kind, f):
-        self.kind, self.f = kind, f
+    """gradt(u), grad(v), idt(u), id(v), optionally times a coefficient and (for the gradients) N()."""
+
+    __array_ufunc__ = None  # ndarray * _Op -> _Op.__rmul__ (per-element coefficients)
+
+    def __init__(self, kind, f, coef=1.0):
+        self.kind, self.f, self.coef = kind, f, coef
 
     def __mul__(self, other):
+        if isinstance(other, _Normal) and self.kind in ("gradt", "grad"):
+            return _Op(self.kind + "_n", self.f, self.coef)
         if isinstance(other, _Op) and {self.kind, other.kind} == {"idt", "id"}:
-            return Expr([("mass", 1.0)])
+            return Expr([("mass", self.coef * other.coef)])
         if isinstance(other, _Op) and self.kind == "id":
             return other.__mul__(self)
+        if _is_num(other) or isinstance(other, np.ndarray):
+            return self.__rmul__(other)
         return NotImplemented
 
     def __rmul__(self, coef):
         if self.kind == "id":
             return LinearExpr(_source(coef))
+        if _is_num(coef) or isinstance(coef, np.ndarray):
+            return _Op(self.kind, self.f, coef * self.coef)
         return NotImplemented
 
 
@@ -343,7 +373,9 @@ def stress(u, lam, mu):
 
 
 class Expr:
-    """Sum of bilinear terms: ("stiff", k), ("mass", m), ("elast", (lam, mu))."""
+    """Sum of bilinear terms: ("stiff", k), ("mass", m), ("elast", (lam, mu)); on faces also
+    ("mass_h", m) for m*idt(u)*id(v)/hFace(), ("dn_trial", c) for c*inner(gradt(u)*N(), id(v)) and
+    ("dn_test", c) for c*inner(grad(v)*N(), idt(u))."""
 
     __array_ufunc__ = None  # let ndarray * Expr dispatch to Expr.__rmul__
 
@@ -352,6 +384,22 @@ class Expr:
 
     def __add__(self, other):
         return Expr(self.terms + other.terms)
+
+    def __neg__(self):
+        return (-1.0) * self
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    def __truediv__(self, other):
+        if isinstance(other, _HFace):
+            out = []
+            for kind, c in self.terms:
+                if kind != "mass":
+                    raise ValueError("only idt(u)*id(v) may be divided by hFace()")
+                out.append(("mass_h", c))
+            return Expr(out)
+        return (1.0 / float(other)) * self
 
     def __rmul__(self, coef):
         out = []
@@ -377,10 +425,21 @@ class Expr:
 
 
 def inner(a, b):
-    if isinstance(a, _Op) and isinstance(b, _Op) and {a.kind, b.kind} == {"gradt", "grad"}:
-        return Expr([("stiff", 1.0)])
+    if isinstance(a, _Op) and isinstance(b, _Op):
+        kinds = {a.kind, b.kind}
+        c = a.coef * b.coef
+        if kinds == {"gradt", "grad"}:
+            return Expr([("stiff", c)])
+        if kinds == {"gradt_n", "id"}:
+            return Expr([("dn_trial", c)])
+        if kinds == {"grad_n", "idt"}:
+            return Expr([("dn_test", c)])
     if isinstance(a, _Stress) and isinstance(b, _Op) and b.kind == "grad":
         return Expr([("elast", (a.lam, a.mu))])
+    if isinstance(b, _Op) and b.kind == "grad_n" and _is_num(a):
+        a, b = b, a
+    if isinstance(a, _Op) and a.kind == "grad_n" and _is_num(b):
+        return LinearExpr(terms=[("dn", float(a.coef) * float(b))])
     if isinstance(b, _Op) and b.kind == "id":
         return LinearExpr(_source(a))
     raise ValueError("unsupported inner product")
@@ -411,8 +470,52 @@ def cst_vec(a, b, c):
 
 
 class LinearExpr:
-    def __init__(self, source):
-        self.source = source
+    """Sum of linear terms: ("src", _Source) for f*id(v); on faces also ("src_h", g) for
+    g*id(v)/hFace() and ("dn", c) for c*inner(grad(v)*N(), 1)."""
+
+    __array_ufunc__ = None
+
+    def __init__(self, source=None, terms=None):
+        self.terms = list(terms) if terms is not None else [("src", source)]
+
+    @property
+    def source(self):
+        if len(self.terms) != 1 or self.terms[0][0] != "src":
+            raise ValueError("not a single source term")
+        return self.terms[0][1]
+
+    def __add__(self, other):
+        return LinearExpr(terms=self.terms + other.terms)
+
+    def __neg__(self):
+        return (-1.0) * self
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    def __rmul__(self, coef):
+        f = float(coef)
+        out = []
+        for kind, c in self.terms:
+            if kind == "src":
+                if c.kind == _ffi.RHS_SINE and f != 1.0:
+                    raise ValueError("the sine source takes no coefficient")
+                out.append(("src", _Source(c.kind, tuple(f * x for x in c.c))))
+            else:
+                out.append((kind, f * c))
+        return LinearExpr(terms=out)
+
+    __mul__ = __rmul__
+
+    def __truediv__(self, other):
+        if isinstance(other, _HFace):
+            out = []
+            for kind, c in self.terms:
+                if kind != "src" or c.kind != _ffi.RHS_CONST:
+                    raise ValueError("only a constant g*id(v) may be divided by hFace()")
+                out.append(("src_h", c.c[0]))
+            return LinearExpr(terms=out)
+        return (1.0 / float(other)) * self
 
 
 class _Integral:
@@ -422,7 +525,9 @@ class _Integral:
 
 def integrate(range, expr, quad=0):  # noqa: A002 - Feel++ keyword
     """integrate(_range=elements(mesh) | boundaryfaces(mesh) | markedfaces(mesh, xmax), _expr=...).
-    On faces: alpha*idt(u)*id(v) (Robin mass) in a form2, g*id(v) (constant load) in a form1."""
+    On faces, with constant coefficients: alpha*idt(u)*id(v) (Robin), beta*idt(u)*id(v)/hFace(),
+    c*inner(gradt(u)*N(), id(v)) and c*inner(grad(v)*N(), idt(u)) (Nitsche) in a form2; g*id(v),
+    g*id(v)/hFace() and c*inner(grad(v)*N(), g) in a form1."""
     if range.kind not in ("elements", "boundaryfaces", "markedfaces"):
         raise ValueError("unknown integration range")
     return _Integral(range, expr, quad)
@@ -461,14 +566,39 @@ class Form1:
         return self
 
     def _assemble(self, integral, accumulate):
-        src = integral.expr.source
-        d = _ffi.RhsDesc()
-        d.kind = src.kind
-        for k in range(3):
-            d.c[k] = src.c[k]
-        d.quad_degree = integral.quad
-        d.range, d.range_xmax = _range_code(integral.range)
-        self.env.check(self.env.lib.fgpu_assemble_vector(self.env.h, self.space.h, C.byref(d), self.vec.h, accumulate))
+        expr = integral.expr
+        if isinstance(expr, _Op) and expr.kind == "id":
+            expr = LinearExpr(_source(1.0))
+        rng, xmax = _range_code(integral.range)
+        descs = []
+        face = [0.0, 0.0, 0.0]          # FGPU_RHS_FACE: id(v), id(v)/hFace(), inner(grad(v), N())
+        has_face = False
+        for kind, c in expr.terms:
+            if kind == "src" and not (rng != _ffi.RANGE_ELEMENTS and c.kind == _ffi.RHS_CONST):
+                descs.append((c.kind, c.c))
+            elif kind == "src":
+                face[0] += c.c[0]
+            elif kind == "src_h":
+                face[1] += c
+                has_face = True
+            else:
+                face[2] += c
+                has_face = True
+        if rng == _ffi.RANGE_ELEMENTS and has_face:
+            raise ValueError("hFace() and N() terms need a face range")
+        if rng != _ffi.RANGE_ELEMENTS:
+            if descs:
+                raise ValueError("face loads: constant coefficients only")
+            descs.append((_ffi.RHS_FACE, tuple(face)) if has_face else (_ffi.RHS_CONST, (face[0], 0.0, 0.0)))
+        for k, (kind, cc) in enumerate(descs):
+            d = _ffi.RhsDesc()
+            d.kind = kind
+            for j in range(3):
+                d.c[j] = cc[j]
+            d.quad_degree = integral.quad
+            d.range, d.range_xmax = rng, xmax
+            self.env.check(self.env.lib.fgpu_assemble_vector(self.env.h, self.space.h, C.byref(d), self.vec.h,
+                                                             accumulate if k == 0 else 1))
 
     def to_numpy(self):
         return self.vec.to_numpy()
@@ -541,6 +671,7 @@ class Form2:
         d.quad_degree = integral.quad
         d.algo = algo
         d.kappa_scale = None
+        d.mass_h = d.dn_trial = d.dn_test = 0.0
         d.range, d.range_xmax = _range_code(integral.range)
         kappa_arr = None
         for kind, c in integral.expr.terms:
@@ -558,10 +689,10 @@ class Form2:
                     d.kappa = 0.0
                 else:
                     d.kappa += c
-            elif kind == "mass":
+            elif kind in ("mass", "mass_h", "dn_trial", "dn_test"):
                 if isinstance(c, np.ndarray):
-                    raise ValueError("the mass coefficient must be constant")
-                d.mass += c
+                    raise ValueError("the %s coefficient must be constant" % kind)
+                setattr(d, kind, getattr(d, kind) + c)
             elif kind == "elast":
                 d.kind = _ffi.FORM_ELASTICITY
                 d.lam, d.mu = c

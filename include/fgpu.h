@@ -65,6 +65,8 @@ extern "C" {
 #define FGPU_RHS_SINE 0           /* f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */
 #define FGPU_RHS_CONST_VEC 1      /* f = (c0, c1, c2) (Pchv) */
 #define FGPU_RHS_CONST 2          /* f = c0 */
+#define FGPU_RHS_FACE 3           /* face ranges only: c0*id(v) + c1*id(v)/hFace() + c2*inner(grad(v),N()),
+                                     e.g. the Nitsche load -inner(k*grad(v)*N(),g) + gamma*k*g*id(v)/hFace() */
 
 #define FGPU_ON_ELIMINATION 0     /* MatZeroRows: row zeroed, diag set, b_i = diag*g_i (default) */
 #define FGPU_ON_ELIMINATION_SYMMETRIC 1 /* MatZeroRowsColumns: also b_j -= A_ji g_i, column zeroed */
@@ -108,16 +110,24 @@ typedef struct {
     const double* kappa_scale;/* device scalar multiplying kappa, read when the kernels run, so a
                                  captured graph sees its current value (a time-dependent
                                  coefficient kappa(t)); NULL = 1. Laplace/mass forms only. */
-    int range;                /* FGPU_RANGE_*; on faces only the mass term (alpha = mass) of a
-                                 Laplace/mass form on a scalar space: int_faces alpha u v (Robin) */
+    int range;                /* FGPU_RANGE_*; on faces (scalar spaces, kappa = 0):
+                                 int_f mass*u*v + mass_h*u*v/hFace + dn_trial*(grad u.N)*v
+                                       + dn_test*(grad v.N)*u
+                                 (Robin: mass; symmetric Nitsche: dn_trial = dn_test = -k,
+                                 mass_h = gamma*k), N the unit outward normal, hFace the
+                                 longest edge of the face */
     double range_xmax;        /* FGPU_RANGE_MARKED_FACES */
+    double mass_h;            /* faces only: coefficient of idt(u)*id(v)/hFace() */
+    double dn_trial;          /* faces only: coefficient of inner(gradt(u)*N(), id(v)) */
+    double dn_test;           /* faces only: coefficient of inner(grad(v)*N(), idt(u)) */
 } fgpu_form_desc;
 
 typedef struct {
     int kind;                 /* FGPU_RHS_* */
     double c[3];
     int quad_degree;          /* 0 = 2*order */
-    int range;                /* FGPU_RANGE_*; on faces: FGPU_RHS_CONST, int_faces c0 v (Neumann) */
+    int range;                /* FGPU_RANGE_*; on faces: FGPU_RHS_CONST (int_f c0 v, Neumann) or
+                                 FGPU_RHS_FACE */
     double range_xmax;        /* FGPU_RANGE_MARKED_FACES */
 } fgpu_rhs_desc;
 

@@ -271,3 +271,53 @@ def face_load(order, xyz, tets, l2g, N, g, xplane=None):
             tab[f] = w @ phi
         F[l2g[e]] += g * _face_area(xyz, tets, e, f) * tab[f]
     return F
+
+
+def _face_normal_h(xyz, tets, e, f):
+    """Unit outward normal and hFace (longest face edge, feelpp/feel/feelmesh/geond.hpp:737-757)."""
+    P = xyz[tets[e][_FACE_VERTS[f]]]
+    c = np.cross(P[1] - P[0], P[2] - P[0])
+    nrm = c / np.linalg.norm(c)
+    if np.dot(nrm, xyz[tets[e][f]] - P[0]) > 0:
+        nrm = -nrm
+    h = max(np.linalg.norm(P[1] - P[0]), np.linalg.norm(P[2] - P[0]), np.linalg.norm(P[2] - P[1]))
+    return nrm, h
+
+
+def face_terms_matrix(order, xyz, tets, l2g, ia, ja, mass=0.0, mass_h=0.0, dn_trial=0.0, dn_test=0.0, xplane=None,
+                      val=None):
+    """val (nnz) += int_faces mass u v + mass_h u v / hFace + dn_trial (grad u . N) v + dn_test (grad v . N) u,
+    by quadrature in physical space (gradients B grad_ref, B from the oracle's geometry)."""
+    val = np.zeros(len(ja)) if val is None else val
+    _, Bs, _ = geometry(xyz, tets)
+    for e, f in boundary_faces(xyz, tets, xplane):
+        pts, w = _face_rule(f)
+        phi, dref = tabulate(order, pts)                       # (q, n), (q, n, 3)
+        grad = np.einsum("da,qna->qnd", Bs[e], dref)          # physical gradients
+        nrm, h = _face_normal_h(xyz, tets, e, f)
+        dn = grad @ nrm                                        # (q, n)
+        A = _face_area(xyz, tets, e, f)
+        blk = (mass + mass_h / h) * (phi * w[:, None]).T @ phi
+        blk += dn_trial * (phi * w[:, None]).T @ dn            # (i, j): phi_i (grad phi_j . n)
+        blk += dn_test * (dn * w[:, None]).T @ phi             # (i, j): (grad phi_i . n) phi_j
+        blk *= A
+        dofs = l2g[e]
+        for a, r in enumerate(dofs):
+            cols = ja[ia[r]:ia[r + 1]]
+            for b, c in enumerate(dofs):
+                val[ia[r] + np.searchsorted(cols, c)] += blk[a, b]
+    return val
+
+
+def face_terms_load(order, xyz, tets, l2g, N, g=0.0, g_h=0.0, g_dn=0.0, xplane=None):
+    """F (N) = int_faces g v + g_h v / hFace + g_dn (grad v . N)."""
+    F = np.zeros(N)
+    _, Bs, _ = geometry(xyz, tets)
+    for e, f in boundary_faces(xyz, tets, xplane):
+        pts, w = _face_rule(f)
+        phi, dref = tabulate(order, pts)
+        grad = np.einsum("da,qna->qnd", Bs[e], dref)
+        nrm, h = _face_normal_h(xyz, tets, e, f)
+        A = _face_area(xyz, tets, e, f)
+        F[l2g[e]] += A * ((g + g_h / h) * (w @ phi) + g_dn * (w @ (grad @ nrm)))
+    return F

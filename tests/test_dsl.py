@@ -81,3 +81,28 @@ def test_face_ranges():
     assert d.range == _ffi.RANGE_MARKED_FACES and d.range_xmax == 0.5
     d, _ = fe.Form2._desc_of(fe._Integral(fe.elements(m), _stiff(), 0), _ffi.ALGO_AUTO)
     assert d.range == _ffi.RANGE_ELEMENTS
+
+
+def test_nitsche_bilinear_terms():
+    """cg_laplacian.hpp's weak-Dirichlet integrand maps to the face descriptor fields."""
+    k = 1.5
+    u, v = None, None
+    e = (-fe.inner(k * fe.gradt(u) * fe.N(), fe.id(v)) - fe.inner(k * fe.grad(v) * fe.N(), fe.idt(u))
+         + 2 * k * fe.idt(u) * fe.id(v) / fe.hFace() + 0.25 * fe.idt(u) * fe.id(v))
+    d, karr = fe.Form2._desc_of(_integral(e), _ffi.ALGO_AUTO)
+    assert d.dn_trial == -k and d.dn_test == -k and d.mass_h == 2 * k and d.mass == 0.25 and d.kappa == 0.0
+    assert karr is None
+    # k*gradt(u) inside inner(., grad(v)) is the stiffness coefficient
+    d2, _ = fe.Form2._desc_of(_integral(fe.inner(k * fe.gradt(u), fe.grad(v))), _ffi.ALGO_AUTO)
+    assert d2.kappa == k
+
+
+def test_nitsche_linear_terms():
+    k, g = 2.0, 0.3
+    le = -fe.inner(k * fe.grad(None) * fe.N(), g) + 2 * k * g * fe.id(None) / fe.hFace()
+    kinds = dict(le.terms)
+    assert kinds["dn"] == pytest.approx(-k * g) and kinds["src_h"] == pytest.approx(2 * k * g)
+    with pytest.raises(ValueError):
+        fe.sine_source() * fe.id(None) / fe.hFace()
+    with pytest.raises(ValueError):
+        (fe.inner(fe.gradt(None), fe.grad(None))) / fe.hFace()

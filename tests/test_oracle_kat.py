@@ -212,3 +212,62 @@ def test_face_integral_kats(oracle):
     ia, ja = oracle.pattern(N, l2g)
     val = oracle.face_matrix(2, xyz, tets, l2g, ia, ja, 1.0)
     assert abs(val.sum() - 6.0) < 1e-12
+
+
+def _csr_dense(ia, ja, val, N):
+    A = np.zeros((N, N))
+    for r in range(N):
+        A[r, ja[ia[r]:ia[r + 1]]] = val[ia[r]:ia[r + 1]]
+    return A
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_nitsche_face_terms_kats(oracle, order):
+    """Known answers of the Nitsche face restatement (cg_laplacian.hpp weak Dirichlet terms):
+    divergence theorem: for the interpolant x of a linear function l, the boundary matrix of
+    int (grad u . N) v applied to x equals the stiffness matrix applied to x (grad l is constant,
+    sum_F int_F (grad l . n) phi_i = int_Omega grad l . grad phi_i); the (grad v . N) u matrix is its
+    transpose; the load int (grad v . N) equals that transpose applied to ones; hFace is the longest
+    face edge; the u v / hFace term is the face mass scaled per face."""
+    xyz, tets = mesh(2, perturb=0.2)
+    N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, order, mass=0.0)
+    Dt = _csr_dense(ia, ja, oracle.face_terms_matrix(order, xyz, tets, l2g, ia, ja, dn_trial=1.0), N)
+    Ds = _csr_dense(ia, ja, oracle.face_terms_matrix(order, xyz, tets, l2g, ia, ja, dn_test=1.0), N)
+    Kd = _csr_dense(ia, ja, K, N)
+    # dof coordinates: interpolate l(x) = 0.3 + x - 2 y + 0.5 z through the nodal values
+    pts = np.zeros((N, 3))
+    nodes = oracle.nodes(order)
+    for e, t in enumerate(tets):
+        X = xyz[t]
+        lam = np.column_stack([-(nodes.sum(1) + 1) / 2, (nodes + 1) / 2])   # barycentrics on [-1,1]^3
+        pts[l2g[e]] = lam @ X
+    x = 0.3 + pts[:, 0] - 2 * pts[:, 1] + 0.5 * pts[:, 2]
+    scale = np.abs(Kd @ x).max()
+    assert np.abs(Dt @ x - Kd @ x).max() <= 1e-12 * scale
+    assert np.abs(Ds - Dt.T).max() <= 1e-13 * np.abs(Dt).max()
+    Fdn = oracle.face_terms_load(order, xyz, tets, l2g, N, g_dn=1.0)
+    assert np.abs(Fdn - Ds @ np.ones(N)).max() <= 1e-12 * np.abs(Fdn).max()
+    # the interpolant of a constant has zero normal derivative
+    assert np.abs(Dt @ np.ones(N)).max() <= 1e-12 * np.abs(Dt).max()
+    # u v / hFace against the face mass with hFace of each face
+    one = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    t1 = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    hs = [oracle._face_normal_h(one, t1, 0, f)[1] for f in range(4)]
+    assert np.allclose(hs, np.sqrt(2), rtol=0, atol=1e-15)        # every face has a sqrt(2) edge
+    nrm, _ = oracle._face_normal_h(one, t1, 0, 3)                # face z = 0: outward is -z
+    assert np.allclose(nrm, [0, 0, -1], atol=1e-15)
+
+
+def test_nitsche_constant_solution(oracle):
+    """Symmetric Nitsche (gamma = 20) with f = 0 and g = c reproduces u = c: the discrete problem is
+    consistent for constants (the grad u . N terms vanish and the load matches the g terms)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    order, k, gamma, c = 2, 1.5, 20.0, 0.7
+    xyz, tets = mesh(3, perturb=0.15)
+    N, l2g, ia, ja, K = oracle_system(oracle, xyz, tets, order, mass=0.0, kappa=np.full(len(tets), k))
+    val = oracle.face_terms_matrix(order, xyz, tets, l2g, ia, ja, mass_h=gamma * k, dn_trial=-k, dn_test=-k, val=K.copy())
+    F = oracle.face_terms_load(order, xyz, tets, l2g, N, g_h=gamma * k * c, g_dn=-k * c)
+    A = sp.csr_matrix((val, ja, ia), shape=(N, N))
+    u = spla.spsolve(A.tocsc(), F)
+    assert np.abs(u - c).max() <= 1e-10
