@@ -16,7 +16,7 @@ RANGE_ELEMENTS, RANGE_BOUNDARY_FACES, RANGE_MARKED_FACES = 0, 1, 2
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE = 0, 1, 2, 3, 4
 RHS_SINE, RHS_CONST_VEC, RHS_CONST, RHS_FACE = 0, 1, 2, 3
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
-PC_NONE, PC_JACOBI, PC_CHEB_JACOBI = 0, 1, 2
+PC_NONE, PC_JACOBI, PC_CHEB_JACOBI, PC_GAMG = 0, 1, 2, 3
 ARITH_F64, ARITH_DF64 = 0, 1
 
 ERROR_NAMES = {1: "FGPU_ERR_INVALID", 2: "FGPU_ERR_CUDA", 3: "FGPU_ERR_BAD_ELEMENT", 4: "FGPU_ERR_OUT_OF_RANGE",
@@ -50,6 +50,11 @@ class SolverCfg(C.Structure):
     _fields_ = [("rtol", C.c_double), ("maxit", C.c_int), ("pc", C.c_int), ("mixed", C.c_int),
                 ("inner_rtol", C.c_double), ("check_every", C.c_int), ("arith", C.c_int),
                 ("cheb_degree", C.c_int), ("cheb_ratio", C.c_double)]
+
+
+class AmgCfg(C.Structure):
+    _fields_ = [("threshold", C.c_double), ("max_levels", C.c_int), ("coarse_eq_lim", C.c_int), ("agg_smooths", C.c_int),
+                ("smoother_degree", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -98,6 +103,17 @@ SIGNATURES = {
     "fgpu_dirichlet": (i32, [P, P, P, i64, P, P, i32, f64]),
     "fgpu_matrix_mult": (i32, [P, P, P, P]),
     "fgpu_solve_cg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
+    "fgpu_amg_create": (i32, [P, P, C.POINTER(AmgCfg), PP]),
+    "fgpu_amg_update": (i32, [P]),
+    "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),
+    "fgpu_amg_destroy": (i32, [P]),
+    "fgpu_solve_cg_amg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
+    "fgpu_amg_host_build": (i32, [i64, P, P, P, C.POINTER(AmgCfg), i32, PP]),
+    "fgpu_amg_host_levels": (i32, [P]),
+    "fgpu_amg_host_level": (i32, [P, i32, P, P, P, P, DP]),
+    "fgpu_amg_host_export": (i32, [P, i32, P, P, P, P, P, P, P]),
+    "fgpu_amg_host_coarse_inverse": (i32, [P, P]),
+    "fgpu_amg_host_destroy": (i32, [P]),
     "fgpu_norms_sine": (i32, [P, P, P, i32, DP, DP]),
     "fgpu_operator_create": (i32, [P, P, C.POINTER(FormDesc), i32, PP]),
     "fgpu_operator_set_dirichlet": (i32, [P, i64, P]),

@@ -1,0 +1,490 @@
+// Smoothed-aggregation AMG preconditioner on the device: the hierarchy is
+// built on the host (amg_setup.cpp) from the assembled FP64 matrix, then
+// every level lives in HBM in binary32 (values; the fine level reuses the
+// matrix's own row pointers and column indices) and one V-cycle runs as a
+// fixed sequence of kernels that the CG driver captures into its CUDA graph.
+//
+// V-cycle (PETSc PCMG multiplicative, one pre- and one post-smoothing; the
+// reference's levels use Richardson/SOR, feelpp/feel/feelalg/backend.cpp:
+// 836-845, which is sequential by nature; here the level smoother is the
+// Chebyshev polynomial in D^-1 A on [0.1, 1.1] lmax, PETSc GAMG's own default,
+// so the preconditioner stays a fixed symmetric linear operator):
+//   x_l = S_l(b_l)                      pre-smoothing from zero
+//   b_{l+1} = R_l (b_l - A_l x_l)       restriction of the residual
+//   x_{l+1} = V(l+1)                    (coarsest: dense inverse, or smoothing)
+//   x_l += P_l x_{l+1}                  prolongation
+//   x_l += S_l(b_l - A_l x_l)           post-smoothing
+// The CG iterations stay in the solver's arithmetic (FP64); only the
+// preconditioner runs in binary32.
+//
+// Each level operator is applied by one kernel per sweep with G lanes per row
+// (G from the mean row length) and the smoother/residual update fused into
+// its epilogue; the lanes of a row sum in a fixed order, so a V-cycle is
+// deterministic.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "cg_driver.cuh"
+
+struct fgpu_amg {
+    fgpu_ctx* ctx = nullptr;
+    const fgpu_matrix* A = nullptr;
+    struct Level {
+        int64_t n = 0, nnz = 0;
+        const int64_t* ia = nullptr;
+        const int32_t* ja = nullptr;
+        int64_t* own_ia = nullptr;
+        int32_t* own_ja = nullptr;
+        float* a = nullptr;
+        float* dinv = nullptr;
+        int G = 8;
+        int64_t* p_ia = nullptr;     // P_l: n x n_{l+1}
+        int32_t* p_ja = nullptr;
+        float* p_a = nullptr;
+        int64_t p_nnz = 0;
+        int pG = 4;
+        int64_t* r_ia = nullptr;     // R_l = P_l^T: n_{l+1} x n
+        int32_t* r_ja = nullptr;
+        float* r_a = nullptr;
+        int64_t r_nnz = 0;
+        int rG = 8;
+        float *x = nullptr, *b = nullptr, *w = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr;
+        float inv_theta = 1.0f;
+        std::vector<float> c1, c2;   // Chebyshev steps 1..K-1
+        double lmax = 0;
+    };
+    std::vector<Level> L;
+    float* coarse_inv = nullptr;     // dense inverse of the coarsest operator (or null: smoothing)
+    int degree = 3;                  // Chebyshev degree of the level smoothers
+    int coarse_degree = 12;          // coarsest-level smoothing degree without a dense inverse
+    double setup_ms = 0;
+    int launches_per_cycle = 0;
+    fgpu_amg_cfg cfg{};
+};
+
+namespace fgpu {
+
+namespace {
+
+enum AmgMode { kResid = 0, kResidStart = 1, kCheb = 2, kPlain = 3, kAdd = 4 };
+
+struct AmgSweep {
+    int64_t n = 0;
+    const int64_t* ia = nullptr;
+    const int32_t* ja = nullptr;
+    const float* a = nullptr;
+    const float* x = nullptr;        // SpMV input
+    const float* b = nullptr;
+    const float* dinv = nullptr;
+    float* w = nullptr;
+    const float* dprev = nullptr;
+    float* dnew = nullptr;
+    float* acc = nullptr;
+    float* out = nullptr;            // kResid / kPlain / kAdd output; kCheb last step target (or null)
+    float c1 = 0, c2 = 0, inv_theta = 1;
+    int last = 0;
+};
+
+// one sweep of a level operator: s_i = sum_j a_ij x_j, then the mode's epilogue
+template <int G, int MODE>
+__global__ void __launch_bounds__(256) amg_sweep_kernel(AmgSweep s, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int lane = threadIdx.x & (G - 1);
+    const int gw = (threadIdx.x & 31) / G;                 // group within the warp
+    const int64_t groups = (int64_t)gridDim.x * (blockDim.x / G);
+    // the loop condition is uniform over the warp (its first group's row), so
+    // every lane reaches the full-warp shuffles; rows past n contribute nothing
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; i - gw < s.n; i += groups) {
+        const bool valid = i < s.n;
+        const int64_t p0 = valid ? s.ia[i] : 0, p1 = valid ? s.ia[i + 1] : 0;
+        float acc = 0.0f;
+        for (int64_t p = p0 + lane; p < p1; p += G) acc = fmaf(__ldg(s.a + p), __ldg(s.x + __ldg(s.ja + p)), acc);
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (lane != 0 || !valid) continue;
+        if (MODE == kResid) {
+            s.out[i] = s.b[i] - acc;
+        } else if (MODE == kResidStart) {
+            const float wi = s.b[i] - acc;
+            const float d = s.dinv[i] * wi * s.inv_theta;
+            s.w[i] = wi;
+            s.dnew[i] = d;
+            s.acc[i] = d;
+        } else if (MODE == kCheb) {
+            const float wi = s.w[i] - acc;
+            const float dn = fmaf(s.c1, s.dprev[i], s.c2 * s.dinv[i] * wi);
+            if (s.last && s.out) {
+                s.out[i] += s.acc[i] + dn;
+            } else {
+                s.acc[i] += dn;
+                if (!s.last) {
+                    s.w[i] = wi;
+                    s.dnew[i] = dn;
+                }
+            }
+        } else if (MODE == kPlain) {
+            s.out[i] = acc;
+        } else {
+            s.out[i] += acc;
+        }
+    }
+}
+
+__device__ __forceinline__ float to_f32(double v) { return (float)v; }
+__device__ __forceinline__ float to_f32(float2 v) { return v.x + v.y; }
+__device__ __forceinline__ float to_f32(float v) { return v; }
+
+// pre-smoothing start from zero: b = (float) r (fine level) or b as is; d0 = D^-1 b / theta; x = d0; w = b
+template <typename T>
+__global__ void amg_start_kernel(int64_t n, const T* __restrict__ bin, float* __restrict__ b, const float* __restrict__ dinv,
+                                 float inv_theta, float* __restrict__ x, float* __restrict__ w, float* __restrict__ d0,
+                                 const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float bi = to_f32(bin[i]);
+        if (b != (const float*)bin) b[i] = bi;
+        const float d = dinv[i] * bi * inv_theta;
+        x[i] = d;
+        w[i] = bi;
+        d0[i] = d;
+    }
+}
+
+// coarsest level: x = Ainv b, one warp per row (fixed lane order)
+__global__ void amg_dense_kernel(int64_t n, const float* __restrict__ M, const float* __restrict__ b, float* __restrict__ x,
+                                 const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < n; i += (int64_t)gridDim.x * blockDim.x / 32) {
+        float acc = 0.0f;
+        for (int64_t j = lane; j < n; j += 32) acc = fmaf(M[i * n + j], b[j], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) x[i] = acc;
+    }
+}
+
+// z = x0 in the solver's storage, per-block r.z partials (the layout of the CG kernels), p = z when asked
+template <class PL>
+__global__ void amg_finish_kernel(int64_t n, const float* __restrict__ x0, const typename PL::S* __restrict__ r,
+                                  typename PL::S* __restrict__ z, typename PL::D* __restrict__ partial_rz,
+                                  typename PL::S* __restrict__ p_out, const CGScalars<PL>* __restrict__ sc) {
+    if (sc && sc->done) return;
+    __shared__ typename PL::D sh[32];
+    typename PL::D rz = PL::dzero();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        typename PL::A zi;
+        if constexpr (PL::id == 1) zi = df{x0[i], 0.0f};
+        else zi = (typename PL::A)x0[i];
+        const typename PL::S zs = PL::st(zi);
+        z[i] = zs;
+        if (p_out) p_out[i] = zs;
+        rz = PL::dmadd(rz, PL::ld(r[i]), PL::ld(zs));
+    }
+    const typename PL::D t = block_sum<PL>(rz, sh);
+    if (threadIdx.x == 0) partial_rz[blockIdx.x] = t;
+}
+
+__global__ void d2f_kernel(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = (float)in[i];
+}
+
+int lanes_for(int64_t n, int64_t nnz) {
+    const double m = n > 0 ? (double)nnz / (double)n : 1.0;
+    return m <= 6 ? 4 : m <= 12 ? 8 : m <= 24 ? 16 : 32;
+}
+
+int grid_for(int64_t rows, int G) {
+    const int64_t per = 256 / G;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((rows + per - 1) / per, 152 * 16));
+}
+
+template <int MODE>
+void sweep(cudaStream_t st, int G, const AmgSweep& s, const int* stop) {
+    const int g = grid_for(s.n, G);
+    switch (G) {
+        case 4: amg_sweep_kernel<4, MODE><<<g, 256, 0, st>>>(s, stop); break;
+        case 8: amg_sweep_kernel<8, MODE><<<g, 256, 0, st>>>(s, stop); break;
+        case 16: amg_sweep_kernel<16, MODE><<<g, 256, 0, st>>>(s, stop); break;
+        default: amg_sweep_kernel<32, MODE><<<g, 256, 0, st>>>(s, stop); break;
+    }
+}
+
+int vblocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8)); }
+
+// Chebyshev steps 1..K-1 on level l accumulating into acc; the last step adds acc + d into target when set
+int cheb_steps(cudaStream_t st, fgpu_amg::Level& V, int K, float* acc, float* target, const int* stop) {
+    int nl = 0;
+    for (int k = 1; k < K; ++k) {
+        AmgSweep s;
+        s.n = V.n; s.ia = V.ia; s.ja = V.ja; s.a = V.a;
+        s.dprev = (k & 1) ? V.d0 : V.d1;
+        s.dnew = (k & 1) ? V.d1 : V.d0;
+        s.x = s.dprev;
+        s.dinv = V.dinv;
+        s.w = V.w;
+        s.acc = acc;
+        s.c1 = V.c1[k - 1];
+        s.c2 = V.c2[k - 1];
+        s.last = k == K - 1;
+        s.out = s.last ? target : nullptr;
+        sweep<kCheb>(st, V.G, s, stop);
+        ++nl;
+    }
+    return nl;
+}
+
+}  // namespace
+
+// One V-cycle: level-0 right-hand side r (solver storage S), result in L[0].x.
+template <typename T>
+int amg_vcycle(fgpu_amg* M, const T* r, const int* stop) {
+    cudaStream_t st = M->ctx->stream;
+    const int nlev = (int)M->L.size();
+    const int K = M->degree;
+    int nl = 0;
+    for (int l = 0; l < nlev; ++l) {
+        fgpu_amg::Level& V = M->L[l];
+        const bool coarsest = l == nlev - 1;
+        if (coarsest && M->coarse_inv) {
+            const int g = (int)std::max<int64_t>(1, std::min<int64_t>((V.n * 32 + 255) / 256, 152 * 8));
+            amg_dense_kernel<<<g, 256, 0, st>>>(V.n, M->coarse_inv, V.b, V.x, stop);
+            ++nl;
+            break;
+        }
+        const int Kl = coarsest ? M->coarse_degree : K;
+        if (l == 0) amg_start_kernel<T><<<vblocks(V.n), 256, 0, st>>>(V.n, r, V.b, V.dinv, V.inv_theta, V.x, V.w, V.d0, stop);
+        else amg_start_kernel<float><<<vblocks(V.n), 256, 0, st>>>(V.n, V.b, V.b, V.dinv, V.inv_theta, V.x, V.w, V.d0, stop);
+        ++nl;
+        if (coarsest) {
+            // Chebyshev coefficients of the coarsest level are sized for coarse_degree
+            nl += cheb_steps(st, V, Kl, V.x, nullptr, stop);
+            break;
+        }
+        nl += cheb_steps(st, V, Kl, V.x, nullptr, stop);
+        AmgSweep s;
+        s.n = V.n; s.ia = V.ia; s.ja = V.ja; s.a = V.a; s.x = V.x; s.b = V.b; s.out = V.w;
+        sweep<kResid>(st, V.G, s, stop);
+        fgpu_amg::Level& C = M->L[l + 1];
+        AmgSweep rs;
+        rs.n = C.n; rs.ia = V.r_ia; rs.ja = V.r_ja; rs.a = V.r_a; rs.x = V.w; rs.out = C.b;
+        sweep<kPlain>(st, V.rG, rs, stop);
+        nl += 2;
+    }
+    for (int l = nlev - 2; l >= 0; --l) {
+        fgpu_amg::Level& V = M->L[l];
+        fgpu_amg::Level& C = M->L[l + 1];
+        AmgSweep ps;
+        ps.n = V.n; ps.ia = V.p_ia; ps.ja = V.p_ja; ps.a = V.p_a; ps.x = C.x; ps.out = V.x;
+        sweep<kAdd>(st, V.pG, ps, stop);
+        AmgSweep s;
+        s.n = V.n; s.ia = V.ia; s.ja = V.ja; s.a = V.a; s.x = V.x; s.b = V.b; s.dinv = V.dinv; s.w = V.w; s.dnew = V.d0;
+        s.acc = V.e; s.inv_theta = V.inv_theta;
+        sweep<kResidStart>(st, V.G, s, stop);
+        nl += 2 + cheb_steps(st, V, M->degree, V.e, V.x, stop);
+    }
+    return nl;
+}
+
+template int amg_vcycle<double>(fgpu_amg*, const double*, const int*);
+template int amg_vcycle<float2>(fgpu_amg*, const float2*, const int*);
+template int amg_vcycle<float>(fgpu_amg*, const float*, const int*);
+
+// PcHook for the CG driver: z = V(r), r.z partials, optional p = z
+template <class PL>
+PcHook<PL> amg_pc_hook(fgpu_amg* M) {
+    PcHook<PL> h;
+    h.apply = [M](const typename PL::S* r, typename PL::S* z, typename PL::D* partial_rz, typename PL::S* p_out,
+                  const CGScalars<PL>* gate) {
+        const int* stop = gate ? &gate->done : nullptr;
+        int nl = amg_vcycle<typename PL::S>(M, r, stop);
+        amg_finish_kernel<PL><<<vec_blocks(M->L[0].n), kVecThreads, 0, M->ctx->stream>>>(M->L[0].n, M->L[0].x, r, z, partial_rz, p_out,
+                                                                                        gate);
+        M->ctx->launches += nl + 1;
+    };
+    h.launches = M->launches_per_cycle + 1;
+    return h;
+}
+
+template PcHook<PolF64> amg_pc_hook<PolF64>(fgpu_amg*);
+template PcHook<PolDF64> amg_pc_hook<PolDF64>(fgpu_amg*);
+template PcHook<PolF32> amg_pc_hook<PolF32>(fgpu_amg*);
+
+namespace {
+
+void free_level(fgpu_amg::Level& V) {
+    cudaFree(V.own_ia); cudaFree(V.own_ja); cudaFree(V.a); cudaFree(V.dinv);
+    cudaFree(V.p_ia); cudaFree(V.p_ja); cudaFree(V.p_a); cudaFree(V.r_ia); cudaFree(V.r_ja); cudaFree(V.r_a);
+    cudaFree(V.x); cudaFree(V.b); cudaFree(V.w); cudaFree(V.d0); cudaFree(V.d1); cudaFree(V.e);
+    V = fgpu_amg::Level();
+}
+
+void cheb_coefs(fgpu_amg::Level& V, int K) {
+    const double emax = 1.1 * V.lmax, emin = 0.1 * V.lmax;
+    const double theta = 0.5 * (emax + emin), delta = 0.5 * (emax - emin), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    V.inv_theta = (float)(1.0 / theta);
+    V.c1.clear();
+    V.c2.clear();
+    for (int k = 1; k < K; ++k) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        V.c1.push_back((float)(rn * rho));
+        V.c2.push_back((float)(2.0 * rn / delta));
+        rho = rn;
+    }
+}
+
+template <typename T>
+cudaError_t upload(T** dst, const T* src, size_t n) {
+    cudaError_t e = cudaMalloc(dst, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess && n) e = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+cudaError_t upload_f32(float** dst, const std::vector<double>& v) {
+    std::vector<float> f(v.size());
+    for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+    return upload(dst, f.data(), f.size());
+}
+
+}  // namespace
+
+int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg* M) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int64_t n = A->nrows, nnz = A->nnz;
+    HostCsr H0;
+    H0.nrows = H0.ncols = n;
+    H0.ia.resize(n + 1);
+    H0.ja.resize(nnz);
+    H0.a.resize(nnz);
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ia.data(), A->d_ia, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ja.data(), A->d_ja, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.a.data(), A->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
+    AmgHostCfg hc;
+    if (cfg) {
+        hc.threshold = cfg->threshold;
+        if (cfg->max_levels > 0) hc.max_levels = cfg->max_levels;
+        if (cfg->coarse_eq_lim > 0) hc.coarse_eq_lim = cfg->coarse_eq_lim;
+        hc.agg_smooths = cfg->agg_smooths == 0 ? 1 : cfg->agg_smooths < 0 ? 0 : cfg->agg_smooths;
+        if (cfg->smoother_degree >= 2) M->degree = cfg->smoother_degree;
+    }
+    hc.nthreads = ctx->host_threads;
+    AmgHierarchy H;
+    std::string err;
+    if (!amg_build_host(std::move(H0), hc, H, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
+    const int nlev = (int)H.levels.size();
+    M->L.assign(nlev, fgpu_amg::Level());
+    int nl = 0;
+    for (int l = 0; l < nlev; ++l) {
+        AmgHostLevel& hl = H.levels[l];
+        fgpu_amg::Level& V = M->L[l];
+        V.n = hl.A.nrows;
+        V.nnz = (int64_t)hl.A.ja.size();
+        V.lmax = hl.lmax;
+        const bool coarsest = l == nlev - 1;
+        cheb_coefs(V, coarsest ? M->coarse_degree : M->degree);
+        V.G = lanes_for(V.n, V.nnz);
+        std::vector<double> dinv(V.n, 0.0);
+        for (int64_t i = 0; i < V.n; ++i)
+            for (int64_t p = hl.A.ia[i]; p < hl.A.ia[i + 1]; ++p)
+                if (hl.A.ja[p] == i) dinv[i] = 1.0 / hl.A.a[p];
+        FGPU_CUDA_CHECK(ctx, upload_f32(&V.dinv, dinv));
+        if (l == 0) {
+            V.ia = A->d_ia;
+            V.ja = A->d_ja;
+            FGPU_CUDA_CHECK(ctx, cudaMalloc(&V.a, std::max<int64_t>(V.nnz, 1) * sizeof(float)));
+            d2f_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>((V.nnz + 255) / 256, 152 * 32)), 256, 0, ctx->stream>>>(
+                V.nnz, (const double*)A->d_val, V.a);
+            ctx->launches++;
+        } else {
+            FGPU_CUDA_CHECK(ctx, upload(&V.own_ia, hl.A.ia.data(), hl.A.ia.size()));
+            FGPU_CUDA_CHECK(ctx, upload(&V.own_ja, hl.A.ja.data(), hl.A.ja.size()));
+            FGPU_CUDA_CHECK(ctx, upload_f32(&V.a, hl.A.a));
+            V.ia = V.own_ia;
+            V.ja = V.own_ja;
+        }
+        if (!coarsest) {
+            V.p_nnz = (int64_t)hl.P.ja.size();
+            V.r_nnz = (int64_t)hl.R.ja.size();
+            V.pG = lanes_for(hl.P.nrows, V.p_nnz);
+            V.rG = lanes_for(hl.R.nrows, V.r_nnz);
+            FGPU_CUDA_CHECK(ctx, upload(&V.p_ia, hl.P.ia.data(), hl.P.ia.size()));
+            FGPU_CUDA_CHECK(ctx, upload(&V.p_ja, hl.P.ja.data(), hl.P.ja.size()));
+            FGPU_CUDA_CHECK(ctx, upload_f32(&V.p_a, hl.P.a));
+            FGPU_CUDA_CHECK(ctx, upload(&V.r_ia, hl.R.ia.data(), hl.R.ia.size()));
+            FGPU_CUDA_CHECK(ctx, upload(&V.r_ja, hl.R.ja.data(), hl.R.ja.size()));
+            FGPU_CUDA_CHECK(ctx, upload_f32(&V.r_a, hl.R.a));
+        }
+        float** vecs[6] = {&V.x, &V.b, &V.w, &V.d0, &V.d1, &V.e};
+        for (float** v : vecs) FGPU_CUDA_CHECK(ctx, cudaMalloc(v, std::max<int64_t>(V.n, 1) * sizeof(float)));
+        if (coarsest && !H.coarse_inv.empty()) {
+            FGPU_CUDA_CHECK(ctx, upload_f32(&M->coarse_inv, H.coarse_inv));
+            nl += 1;
+        } else if (coarsest) {
+            nl += M->coarse_degree;               // start + coarse_degree - 1 steps
+        } else {
+            nl += 1 + (M->degree - 1) + 2 + 2 + (M->degree - 1) + 0;   // start, steps, resid, restrict | prolong, resid-start, steps
+        }
+    }
+    M->launches_per_cycle = nl;
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    M->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return FGPU_OK;
+}
+
+}  // namespace fgpu
+
+using namespace fgpu;
+
+extern "C" int fgpu_amg_create(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg** out) {
+    if (!ctx || !A || !out) return FGPU_ERR_INVALID;
+    if (ctx->capturing) { ctx->err = "gamg: set-up is not capturable"; return FGPU_ERR_INVALID; }
+    if (A->precision != FGPU_F64) { ctx->err = "gamg: FP64 matrices only"; return FGPU_ERR_INVALID; }
+    *out = nullptr;
+    fgpu_amg* M = new fgpu_amg();
+    M->ctx = ctx;
+    M->A = A;
+    if (cfg) M->cfg = *cfg;
+    const int rc = amg_setup(ctx, A, &M->cfg, M);
+    if (rc) {
+        for (auto& V : M->L) free_level(V);
+        cudaFree(M->coarse_inv);
+        delete M;
+        return rc;
+    }
+    *out = M;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_amg_update(fgpu_amg* M) {
+    if (!M) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = M->ctx;
+    if (ctx->capturing) { ctx->err = "gamg: set-up is not capturable"; return FGPU_ERR_INVALID; }
+    for (auto& V : M->L) free_level(V);
+    cudaFree(M->coarse_inv);
+    M->coarse_inv = nullptr;
+    return amg_setup(ctx, M->A, &M->cfg, M);
+}
+
+extern "C" int fgpu_amg_info(const fgpu_amg* M, int* nlevels, int64_t* rows, int64_t* nnz, double* setup_ms) {
+    if (!M) return FGPU_ERR_INVALID;
+    if (nlevels) *nlevels = (int)M->L.size();
+    for (size_t l = 0; l < M->L.size() && l < 16; ++l) {
+        if (rows) rows[l] = M->L[l].n;
+        if (nnz) nnz[l] = M->L[l].nnz;
+    }
+    if (setup_ms) *setup_ms = M->setup_ms;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_amg_destroy(fgpu_amg* M) {
+    if (!M) return FGPU_OK;
+    for (auto& V : M->L) free_level(V);
+    cudaFree(M->coarse_inv);
+    delete M;
+    return FGPU_OK;
+}

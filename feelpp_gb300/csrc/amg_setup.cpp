@@ -1,0 +1,488 @@
+// Smoothed-aggregation AMG hierarchy (host set-up), the preconditioner the
+// reference's users select with pc-type=gamg (PETSc PCGAMG, type "agg";
+// feelpp/feel/feelalg/preconditionerpetsc.cpp:2229-2330, defaults
+// feelpp/feel/feelalg/backend.cpp:813-818: threshold 0, coarse-eq-lim 800,
+// nsmooths 1, 10 levels).
+//
+// Per level (Vanek, Mandel, Brezina, "Algebraic multigrid by smoothed
+// aggregation for second and fourth order elliptic problems", Computing 56,
+// 1996):
+//   1. strength graph: j is a strong neighbour of i when
+//      |a_ij| > theta sqrt(|a_ii a_jj|) (theta = 0: every stored coupling),
+//      symmetrised;
+//   2. greedy aggregation in three passes (root aggregates of whole free
+//      neighbourhoods; leftovers join a neighbouring root aggregate; the rest
+//      form aggregates of their free neighbourhoods); nodes without strong
+//      neighbours (rows eliminated by on(), decoupled) are left out: their
+//      prolongator rows are zero and the smoother solves them exactly;
+//   3. tentative prolongator: P0(i, agg(i)) = 1/sqrt(|agg|) (the constant near
+//      null space, orthonormal columns);
+//   4. prolongator smoothing: P = (I - omega D^-1 A) P0, omega = 4 / (3 lmax),
+//      lmax = lmax(D^-1 A) from a Lanczos estimate;
+//   5. Galerkin coarse operator A_c = P^T A P (R = P^T stored explicitly),
+//      by row-wise sparse products with a dense accumulator per thread;
+// until the level has at most coarse_eq_lim rows or max_levels is reached;
+// the coarsest operator is inverted densely (Cholesky) when small enough.
+//
+// Everything is deterministic: the row loops are split among threads, but
+// each output entry is accumulated in a fixed order and rows keep sorted
+// columns, so the hierarchy does not depend on the thread count.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fgpu_core.h"
+
+namespace fgpu {
+
+namespace {
+
+void parallel_rows(int nthreads, int64_t n, const std::function<void(int, int64_t, int64_t)>& fn) {
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, (n + 4095) / 4096));
+    if (T == 1) { fn(0, 0, n); return; }
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t) {
+        const int64_t b = n * t / T, e = n * (t + 1) / T;
+        th.emplace_back(fn, t, b, e);
+    }
+    for (auto& x : th) x.join();
+}
+
+// C = A * B (rows of A times B), Gustavson with a dense accumulator; columns
+// of every row sorted. Each entry sums its products in (A column, B column) order.
+void spgemm(const HostCsr& A, const HostCsr& B, HostCsr& C, int nthreads) {
+    C.nrows = A.nrows;
+    C.ncols = B.ncols;
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, (A.nrows + 4095) / 4096));
+    std::vector<std::vector<int32_t>> tj(T);
+    std::vector<std::vector<double>> ta(T);
+    std::vector<int64_t> len(A.nrows, 0);
+    parallel_rows(T, A.nrows, [&](int t, int64_t r0, int64_t r1) {
+        std::vector<double> acc(B.ncols, 0.0);
+        std::vector<int32_t> mark(B.ncols, -1), cols;
+        auto& J = tj[t];
+        auto& V = ta[t];
+        for (int64_t i = r0; i < r1; ++i) {
+            cols.clear();
+            for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p) {
+                const int32_t k = A.ja[p];
+                const double a = A.a[p];
+                for (int64_t q = B.ia[k]; q < B.ia[k + 1]; ++q) {
+                    const int32_t j = B.ja[q];
+                    if (mark[j] != (int32_t)(i & 0x7fffffff)) {
+                        mark[j] = (int32_t)(i & 0x7fffffff);
+                        acc[j] = 0.0;
+                        cols.push_back(j);
+                    }
+                    acc[j] += a * B.a[q];
+                }
+            }
+            std::sort(cols.begin(), cols.end());
+            for (int32_t j : cols) {
+                J.push_back(j);
+                V.push_back(acc[j]);
+            }
+            len[i] = (int64_t)cols.size();
+        }
+    });
+    C.ia.assign(A.nrows + 1, 0);
+    for (int64_t i = 0; i < A.nrows; ++i) C.ia[i + 1] = C.ia[i] + len[i];
+    C.ja.resize(C.ia[A.nrows]);
+    C.a.resize(C.ia[A.nrows]);
+    int64_t off = 0;
+    for (int t = 0; t < T; ++t) {
+        std::copy(tj[t].begin(), tj[t].end(), C.ja.begin() + off);
+        std::copy(ta[t].begin(), ta[t].end(), C.a.begin() + off);
+        off += (int64_t)tj[t].size();
+    }
+}
+
+void transpose(const HostCsr& A, HostCsr& T) {
+    T.nrows = A.ncols;
+    T.ncols = A.nrows;
+    T.ia.assign(A.ncols + 1, 0);
+    for (int64_t p = 0; p < A.ia[A.nrows]; ++p) T.ia[A.ja[p] + 1]++;
+    for (int64_t j = 0; j < A.ncols; ++j) T.ia[j + 1] += T.ia[j];
+    T.ja.resize(A.ia[A.nrows]);
+    T.a.resize(A.ia[A.nrows]);
+    std::vector<int64_t> fill(T.ia.begin(), T.ia.end() - 1);
+    for (int64_t i = 0; i < A.nrows; ++i)
+        for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p) {
+            const int64_t q = fill[A.ja[p]]++;
+            T.ja[q] = (int32_t)i;
+            T.a[q] = A.a[p];
+        }
+}
+
+std::vector<double> diagonal(const HostCsr& A) {
+    std::vector<double> d(A.nrows, 0.0);
+    for (int64_t i = 0; i < A.nrows; ++i)
+        for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
+            if (A.ja[p] == i) d[i] = A.a[p];
+    return d;
+}
+
+// lmax(D^-1 A) of a symmetric positive definite A: Lanczos on D^-1/2 A D^-1/2
+// (m steps from a fixed pseudo-random start), largest Ritz value by bisection
+double lmax_estimate(const HostCsr& A, const std::vector<double>& d, int m, int nthreads) {
+    const int64_t n = A.nrows;
+    if (n == 0) return 1.0;
+    std::vector<double> s(n), v(n), vold(n, 0.0), w(n);
+    for (int64_t i = 0; i < n; ++i) s[i] = d[i] > 0 ? 1.0 / std::sqrt(d[i]) : 0.0;
+    uint64_t h = 0x9E3779B97F4A7C15ull;
+    double nv = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        h ^= h >> 33; h *= 0xff51afd7ed558ccdull; h ^= h >> 33;
+        v[i] = (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+        nv += v[i] * v[i];
+    }
+    nv = std::sqrt(nv);
+    for (auto& x : v) x /= nv;
+    std::vector<double> al, be;
+    double bprev = 0;
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, (n + 4095) / 4096));
+    std::vector<double> part(T);
+    for (int k = 0; k < m; ++k) {
+        parallel_rows(T, n, [&](int, int64_t r0, int64_t r1) {
+            for (int64_t i = r0; i < r1; ++i) {
+                double acc = 0;
+                for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p) acc += A.a[p] * s[A.ja[p]] * v[A.ja[p]];
+                w[i] = s[i] * acc;
+            }
+        });
+        double a = 0;
+        for (int64_t i = 0; i < n; ++i) a += w[i] * v[i];
+        double b = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            w[i] -= a * v[i] + bprev * vold[i];
+            b += w[i] * w[i];
+        }
+        b = std::sqrt(b);
+        al.push_back(a);
+        if (b < 1e-14 * std::fabs(a) || k + 1 == m) break;
+        be.push_back(b);
+        for (int64_t i = 0; i < n; ++i) {
+            vold[i] = v[i];
+            v[i] = w[i] / b;
+        }
+        bprev = b;
+    }
+    // largest eigenvalue of the tridiagonal (al, be) by Sturm bisection
+    const int mm = (int)al.size();
+    double hi = 0;
+    for (int j = 0; j < mm; ++j) {
+        double g = std::fabs(al[j]);
+        if (j > 0) g += std::fabs(be[j - 1]);
+        if (j + 1 < mm) g += std::fabs(be[j]);
+        hi = std::max(hi, g);
+    }
+    double lo = 0;
+    auto below = [&](double x) {
+        int c = 0;
+        double q = 1.0;
+        for (int j = 0; j < mm; ++j) {
+            q = al[j] - x - (j > 0 ? be[j - 1] * be[j - 1] / q : 0.0);
+            if (q == 0.0) q = -1e-300;
+            if (q < 0) ++c;
+        }
+        return c;
+    };
+    for (int it = 0; it < 200 && hi - lo > 1e-10 * hi; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (below(mid) == mm) hi = mid;
+        else lo = mid;
+    }
+    return hi > 0 ? hi : 1.0;
+}
+
+// strong neighbours (symmetrised, without the diagonal) as a CSR graph
+void strength(const HostCsr& A, const std::vector<double>& d, double theta, std::vector<int64_t>& sp, std::vector<int32_t>& sj) {
+    const int64_t n = A.nrows;
+    std::vector<int64_t> cnt(n + 1, 0);
+    auto strong = [&](int64_t i, int64_t p) {
+        const int32_t j = A.ja[p];
+        if (j == i || A.a[p] == 0.0) return false;
+        return std::fabs(A.a[p]) > theta * std::sqrt(std::fabs(d[i] * d[j]));
+    };
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
+            if (strong(i, p)) cnt[i + 1]++;
+    // symmetrise: a coupling counts when either direction is strong
+    sp.assign(n + 1, 0);
+    std::vector<int32_t> tmpj;
+    std::vector<int64_t> tp(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) tp[i + 1] = tp[i] + cnt[i + 1];
+    tmpj.resize(tp[n]);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t q = tp[i];
+        for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
+            if (strong(i, p)) tmpj[q++] = A.ja[p];
+    }
+    // transpose of the strong graph, merged with it (sorted, unique)
+    std::vector<int64_t> tc(n + 1, 0);
+    for (int64_t q = 0; q < tp[n]; ++q) tc[tmpj[q] + 1]++;
+    for (int64_t i = 0; i < n; ++i) tc[i + 1] += tc[i];
+    std::vector<int32_t> tj(tp[n]);
+    {
+        std::vector<int64_t> f(tc.begin(), tc.end() - 1);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t q = tp[i]; q < tp[i + 1]; ++q) tj[f[tmpj[q]]++] = (int32_t)i;
+    }
+    sj.clear();
+    sj.reserve(tp[n] + tp[n] / 8);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t a = tp[i], b = tc[i];
+        const int64_t ae = tp[i + 1], bend = tc[i + 1];
+        while (a < ae || b < bend) {
+            int32_t v;
+            if (b >= bend || (a < ae && tmpj[a] < tj[b])) v = tmpj[a++];
+            else if (a >= ae || tj[b] < tmpj[a]) v = tj[b++];
+            else { v = tmpj[a++]; ++b; }
+            sj.push_back(v);
+        }
+        sp[i + 1] = (int64_t)sj.size();
+    }
+}
+
+// greedy aggregation; returns the number of aggregates, agg[i] = -1 for nodes left out
+int64_t aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg) {
+    agg.assign(n, -1);
+    int64_t nagg = 0;
+    // pass 1: roots whose whole strong neighbourhood is free
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] != -1 || sp[i + 1] == sp[i]) continue;
+        bool free = true;
+        for (int64_t q = sp[i]; q < sp[i + 1] && free; ++q) free = agg[sj[q]] == -1;
+        if (!free) continue;
+        agg[i] = (int32_t)nagg;
+        for (int64_t q = sp[i]; q < sp[i + 1]; ++q) agg[sj[q]] = (int32_t)nagg;
+        ++nagg;
+    }
+    // pass 2: free nodes join the aggregate of their first aggregated neighbour (pass-1 state)
+    std::vector<int32_t> snap(agg);
+    for (int64_t i = 0; i < n; ++i) {
+        if (snap[i] != -1 || sp[i + 1] == sp[i]) continue;
+        for (int64_t q = sp[i]; q < sp[i + 1]; ++q)
+            if (snap[sj[q]] != -1) { agg[i] = snap[sj[q]]; break; }
+    }
+    // pass 3: the rest form aggregates with their free neighbours
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] != -1 || sp[i + 1] == sp[i]) continue;
+        agg[i] = (int32_t)nagg;
+        for (int64_t q = sp[i]; q < sp[i + 1]; ++q)
+            if (agg[sj[q]] == -1) agg[sj[q]] = (int32_t)nagg;
+        ++nagg;
+    }
+    return nagg;
+}
+
+// P = (I - omega D^-1 A) P0 with P0(i, agg(i)) = 1/sqrt(|agg|)
+void smoothed_prolongator(const HostCsr& A, const std::vector<double>& d, const std::vector<int32_t>& agg, int64_t nagg, double omega,
+                          int nsmooth, HostCsr& P, int nthreads) {
+    std::vector<double> sz(nagg, 0.0);
+    for (int64_t i = 0; i < A.nrows; ++i)
+        if (agg[i] >= 0) sz[agg[i]] += 1.0;
+    std::vector<double> s0(nagg);
+    for (int64_t c = 0; c < nagg; ++c) s0[c] = 1.0 / std::sqrt(sz[c]);
+    HostCsr P0;
+    P0.nrows = A.nrows;
+    P0.ncols = nagg;
+    P0.ia.assign(A.nrows + 1, 0);
+    for (int64_t i = 0; i < A.nrows; ++i) P0.ia[i + 1] = P0.ia[i] + (agg[i] >= 0 ? 1 : 0);
+    P0.ja.resize(P0.ia[A.nrows]);
+    P0.a.resize(P0.ia[A.nrows]);
+    for (int64_t i = 0; i < A.nrows; ++i)
+        if (agg[i] >= 0) {
+            P0.ja[P0.ia[i]] = agg[i];
+            P0.a[P0.ia[i]] = s0[agg[i]];
+        }
+    if (nsmooth <= 0) { P = std::move(P0); return; }
+    HostCsr AP;
+    spgemm(A, P0, AP, nthreads);
+    // P = P0 - omega D^-1 (A P0): merge the sorted rows
+    P.nrows = A.nrows;
+    P.ncols = nagg;
+    P.ia.assign(A.nrows + 1, 0);
+    P.ja.clear();
+    P.a.clear();
+    P.ja.reserve(AP.ja.size() + P0.ja.size());
+    P.a.reserve(AP.ja.size() + P0.ja.size());
+    for (int64_t i = 0; i < A.nrows; ++i) {
+        const double f = d[i] != 0.0 ? omega / d[i] : 0.0;
+        int64_t p = P0.ia[i];
+        const int64_t pe = P0.ia[i + 1];
+        for (int64_t q = AP.ia[i]; q < AP.ia[i + 1]; ++q) {
+            while (p < pe && P0.ja[p] < AP.ja[q]) { P.ja.push_back(P0.ja[p]); P.a.push_back(P0.a[p]); ++p; }
+            double v = -f * AP.a[q];
+            if (p < pe && P0.ja[p] == AP.ja[q]) { v += P0.a[p]; ++p; }
+            P.ja.push_back(AP.ja[q]);
+            P.a.push_back(v);
+        }
+        while (p < pe) { P.ja.push_back(P0.ja[p]); P.a.push_back(P0.a[p]); ++p; }
+        P.ia[i + 1] = (int64_t)P.ja.size();
+    }
+}
+
+// dense inverse of a symmetric positive definite matrix (Cholesky); false when not SPD
+bool spd_inverse(int64_t n, std::vector<double>& M) {
+    std::vector<double> L(M);
+    for (int64_t j = 0; j < n; ++j) {
+        double s = L[j * n + j];
+        for (int64_t k = 0; k < j; ++k) s -= L[j * n + k] * L[j * n + k];
+        if (!(s > 0)) return false;
+        const double ljj = std::sqrt(s);
+        L[j * n + j] = ljj;
+        for (int64_t i = j + 1; i < n; ++i) {
+            double t = L[i * n + j];
+            for (int64_t k = 0; k < j; ++k) t -= L[i * n + k] * L[j * n + k];
+            L[i * n + j] = t / ljj;
+        }
+    }
+    // columns of the inverse: solve L L^T x = e_c
+    std::vector<double> inv((size_t)n * n), y(n);
+    for (int64_t c = 0; c < n; ++c) {
+        for (int64_t i = 0; i < n; ++i) {
+            double t = i == c ? 1.0 : 0.0;
+            for (int64_t k = 0; k < i; ++k) t -= L[i * n + k] * y[k];
+            y[i] = t / L[i * n + i];
+        }
+        for (int64_t i = n - 1; i >= 0; --i) {
+            double t = y[i];
+            for (int64_t k = i + 1; k < n; ++k) t -= L[k * n + i] * inv[k * n + c];
+            inv[i * n + c] = t / L[i * n + i];
+        }
+    }
+    M.swap(inv);
+    return true;
+}
+
+}  // namespace
+
+bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err) {
+    const int nthreads = cfg.nthreads > 0 ? cfg.nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
+    const int max_levels = cfg.max_levels > 0 ? cfg.max_levels : 10;
+    const int64_t coarse_lim = cfg.coarse_eq_lim > 0 ? cfg.coarse_eq_lim : 800;
+    H.levels.clear();
+    H.coarse_inv.clear();
+    H.levels.emplace_back();
+    H.levels[0].A = std::move(A0);
+    for (int l = 0; l + 1 < max_levels; ++l) {
+        AmgHostLevel& L = H.levels[l];
+        const HostCsr& A = L.A;
+        if (A.nrows <= coarse_lim) break;
+        const std::vector<double> d = diagonal(A);
+        for (int64_t i = 0; i < A.nrows; ++i)
+            if (!(d[i] > 0)) { err = "gamg: the diagonal must be positive (SPD matrix)"; return false; }
+        L.lmax = lmax_estimate(A, d, 12, nthreads);
+        std::vector<int64_t> sp;
+        std::vector<int32_t> sj;
+        strength(A, d, cfg.threshold, sp, sj);
+        const int64_t nagg = aggregate(A.nrows, sp, sj, L.agg);
+        if (nagg == 0 || nagg >= A.nrows) break;              // nothing to coarsen
+        const double omega = 4.0 / (3.0 * L.lmax);
+        smoothed_prolongator(A, d, L.agg, nagg, omega, cfg.agg_smooths, L.P, nthreads);
+        transpose(L.P, L.R);
+        HostCsr AP, Ac;
+        spgemm(A, L.P, AP, nthreads);
+        spgemm(L.R, AP, Ac, nthreads);
+        H.levels.emplace_back();
+        H.levels.back().A = std::move(Ac);
+        if ((double)nagg > 0.9 * (double)H.levels[l].A.nrows) break;   // stagnating coarsening
+    }
+    AmgHostLevel& C = H.levels.back();
+    {
+        const std::vector<double> d = diagonal(C.A);
+        for (int64_t i = 0; i < C.A.nrows; ++i)
+            if (!(d[i] > 0)) { err = "gamg: coarse diagonal not positive (matrix not SPD)"; return false; }
+        C.lmax = lmax_estimate(C.A, d, 12, nthreads);
+    }
+    if (C.A.nrows <= kAmgDenseCoarse) {
+        const int64_t n = C.A.nrows;
+        std::vector<double> M((size_t)n * n, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t p = C.A.ia[i]; p < C.A.ia[i + 1]; ++p) M[i * n + C.A.ja[p]] = C.A.a[p];
+        if (spd_inverse(n, M)) H.coarse_inv.swap(M);
+    }
+    return true;
+}
+
+}  // namespace fgpu
+
+// ---------------------------------------------------------------------------
+// Host-only entry points: build and inspect a hierarchy from a host CSR (no
+// device needed), for checking the set-up against its definition.
+// ---------------------------------------------------------------------------
+struct fgpu_amg_host {
+    fgpu::AmgHierarchy H;
+};
+
+extern "C" int fgpu_amg_host_build(int64_t n, const int64_t* ia, const int32_t* ja, const double* a, const fgpu_amg_cfg* cfg,
+                                   int nthreads, fgpu_amg_host** out) {
+    if (!out || n < 0 || (n > 0 && (!ia || !ja || !a))) return FGPU_ERR_INVALID;
+    *out = nullptr;
+    fgpu::HostCsr A;
+    A.nrows = A.ncols = n;
+    A.ia.assign(ia, ia + n + 1);
+    A.ja.assign(ja, ja + ia[n]);
+    A.a.assign(a, a + ia[n]);
+    fgpu::AmgHostCfg hc;
+    if (cfg) {
+        hc.threshold = cfg->threshold;
+        if (cfg->max_levels > 0) hc.max_levels = cfg->max_levels;
+        if (cfg->coarse_eq_lim > 0) hc.coarse_eq_lim = cfg->coarse_eq_lim;
+        hc.agg_smooths = cfg->agg_smooths == 0 ? 1 : cfg->agg_smooths < 0 ? 0 : cfg->agg_smooths;
+    }
+    hc.nthreads = nthreads;
+    fgpu_amg_host* h = new fgpu_amg_host();
+    std::string err;
+    if (!fgpu::amg_build_host(std::move(A), hc, h->H, err)) {
+        delete h;
+        return FGPU_ERR_INVALID;
+    }
+    *out = h;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_amg_host_levels(const fgpu_amg_host* h) { return h ? (int)h->H.levels.size() : 0; }
+
+extern "C" int fgpu_amg_host_level(const fgpu_amg_host* h, int l, int64_t* n, int64_t* nnz, int64_t* p_nnz, int64_t* p_cols,
+                                   double* lmax) {
+    if (!h || l < 0 || l >= (int)h->H.levels.size()) return FGPU_ERR_INVALID;
+    const fgpu::AmgHostLevel& L = h->H.levels[l];
+    if (n) *n = L.A.nrows;
+    if (nnz) *nnz = (int64_t)L.A.ja.size();
+    if (p_nnz) *p_nnz = (int64_t)L.P.ja.size();
+    if (p_cols) *p_cols = L.P.ncols;
+    if (lmax) *lmax = L.lmax;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_amg_host_export(const fgpu_amg_host* h, int l, int64_t* ia, int32_t* ja, double* a, int64_t* pia, int32_t* pja,
+                                    double* pa, int32_t* agg) {
+    if (!h || l < 0 || l >= (int)h->H.levels.size()) return FGPU_ERR_INVALID;
+    const fgpu::AmgHostLevel& L = h->H.levels[l];
+    if (ia) std::copy(L.A.ia.begin(), L.A.ia.end(), ia);
+    if (ja) std::copy(L.A.ja.begin(), L.A.ja.end(), ja);
+    if (a) std::copy(L.A.a.begin(), L.A.a.end(), a);
+    if (pia) std::copy(L.P.ia.begin(), L.P.ia.end(), pia);
+    if (pja) std::copy(L.P.ja.begin(), L.P.ja.end(), pja);
+    if (pa) std::copy(L.P.a.begin(), L.P.a.end(), pa);
+    if (agg) std::copy(L.agg.begin(), L.agg.end(), agg);
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_amg_host_coarse_inverse(const fgpu_amg_host* h, double* out) {
+    if (!h) return FGPU_ERR_INVALID;
+    if (h->H.coarse_inv.empty()) return 0;
+    if (out) std::copy(h->H.coarse_inv.begin(), h->H.coarse_inv.end(), out);
+    return 1;
+}
+
+extern "C" int fgpu_amg_host_destroy(fgpu_amg_host* h) {
+    delete h;
+    return FGPU_OK;
+}

@@ -716,6 +716,7 @@ int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, c
     FGPU_NO_CAPTURE(ctx, "solve_cg");
     int rc = finish(ctx);
     if (rc) return rc;
+    if (cfg->pc == FGPU_PC_GAMG) return set_err(ctx, FGPU_ERR_INVALID, "solve_cg: pc gamg runs through fgpu_solve_cg_amg");
     if (!cfg->mixed) return solve_pcg(ctx, A, b->d, x->d, cfg, stats);
     if (A->precision != FGPU_F64) return set_err(ctx, FGPU_ERR_INVALID, "mixed solve needs an FP64 matrix");
     fgpu_matrix* tmp = nullptr;
@@ -730,6 +731,19 @@ int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, c
     rc = solve_pcg_mixed(ctx, A, a32, b->d, x->d, cfg, stats);
     if (tmp) fgpu_matrix_destroy(tmp);
     int rc2 = finish(ctx);
+    return rc ? rc : rc2;
+}
+
+int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
+                      const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
+    if (!ctx || !A || !amg || !b || !x || !cfg || b->n != A->nrows || x->n != A->nrows)
+        return set_err(ctx, FGPU_ERR_INVALID, "solve_cg_amg: bad arguments");
+    if (cfg->mixed) return set_err(ctx, FGPU_ERR_INVALID, "solve_cg_amg: the mixed solver takes Jacobi preconditioners only");
+    FGPU_NO_CAPTURE(ctx, "solve_cg_amg");
+    int rc = finish(ctx);
+    if (rc) return rc;
+    rc = solve_pcg(ctx, A, b->d, x->d, cfg, stats, amg);
+    const int rc2 = finish(ctx);
     return rc ? rc : rc2;
 }
 

@@ -65,6 +65,18 @@ template <class PL>
 using RefreshFn = std::function<int(typename PL::S* x, typename PL::S* r, bool* converged)>;
 static constexpr int kRefreshStagnated = 1000;
 
+// An external preconditioner (AMG V-cycle): z = M r, per-block partial sums of
+// r.z into rz_partial (vec_blocks(n) blocks of kVecThreads, the layout the CG
+// kernels read) and, when p_out is set, p = z. Every kernel returns at once
+// when gate && gate->done. `launches` = kernels per application.
+template <class PL>
+struct PcHook {
+    std::function<void(const typename PL::S* r, typename PL::S* z, typename PL::D* rz_partial, typename PL::S* p_out,
+                       const CGScalars<PL>* gate)>
+        apply;
+    int launches = 0;
+};
+
 // dst = scale * src
 template <class PL>
 __global__ void scale_vec_kernel(int64_t n, const typename PL::S* __restrict__ src, typename PL::S* __restrict__ dst,
@@ -160,13 +172,13 @@ static inline CgOptions cg_options(const fgpu_solver_cfg* cfg) {
 template <class PL>
 static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typename PL::S* dinv,
                   const typename PL::S* b, typename PL::S* x, const CgOptions& o, CgResult* res,
-                  const RefreshFn<PL>* refresh = nullptr) {
+                  const RefreshFn<PL>* refresh = nullptr, const PcHook<PL>* pch = nullptr) {
     typedef typename PL::S S;
     typedef typename PL::D D;
     cudaStream_t s = ctx->stream;
     const int vb = vec_blocks(n);
     const int nbp = std::max(A.npq, vb);
-    const bool cheb = o.cheb_degree >= 2;
+    const bool cheb = !pch && o.cheb_degree >= 2;
     const int K = cheb ? o.cheb_degree : 0;
     int check_every = std::max(o.check_every, 1);
     if (check_every & 1) ++check_every;   // parity of the scalar double buffer repeats per replay
@@ -277,6 +289,7 @@ static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typen
     cg_init_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, b, r, dz, z, p, partial);
     ctx->launches += A.launches + 2;
     if (cheb) precond(p, nullptr);
+    if (pch) pch->apply(r, z, partial + vb, p, nullptr);
     cg_init_scalars<PL><<<1, 256, 0, s>>>(partial, vb, PL::host_from_double(o.rtol * o.rtol), sc);
     ctx->launches++;
     CK(cudaGetLastError());
@@ -285,6 +298,7 @@ static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typen
         cg_update_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, x, r, z, p, q, dz, pq_partial, A.npq, partial, sc, parity);
         ctx->launches += A.launches + 1;
         if (cheb) precond(nullptr, sc);
+        if (pch) pch->apply(r, z, partial + vb, nullptr, sc);
         cg_p_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, p, z, partial, vb, o.maxit, sc, parity);
         ctx->launches++;
     };
@@ -297,7 +311,8 @@ static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typen
         ctx->launches = l0;
         CK(cudaGraphInstantiate(&exec, graph, 0));
     }
-    const int64_t per_replay = (int64_t)check_every * (A.launches + 2 + (cheb ? (K - 1) * (A.launches + 1) : 0));
+    const int64_t per_replay =
+        (int64_t)check_every * (A.launches + 2 + (cheb ? (K - 1) * (A.launches + 1) : 0) + (pch ? pch->launches : 0));
     CK(poll());
     int guard = 0, parity = 0, nref = 0, nbreak = 0;
     double rr_ref = PL::host_to_double(hsc->rr);
@@ -324,6 +339,7 @@ static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typen
             cg_refresh_kernel<PL><<<vb, kVecThreads, 0, s>>>(n, r, dz, z, partial, p_restart);
             ctx->launches++;
             if (cheb) precond(p_restart, nullptr);
+            if (pch) pch->apply(r, z, partial + vb, p_restart, nullptr);
             cg_refresh_scalars<PL><<<1, 256, 0, s>>>(partial, vb, sc);
             ctx->launches++;
             CK(cudaGetLastError());
@@ -354,5 +370,9 @@ static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typen
 #undef CK
     return FGPU_OK;
 }
+
+// the AMG V-cycle as a CG preconditioner (amg.cu)
+template <class PL>
+PcHook<PL> amg_pc_hook(fgpu_amg* M);
 
 }  // namespace fgpu

@@ -74,6 +74,33 @@ int colour_elements(int64_t nv, int64_t nt, const int32_t* tets, std::vector<int
 int boundary_faces_coloured(int64_t nt, const int32_t* tets, const double* xyz, int xmax_on, double xmax, int whole_element,
                             std::vector<int32_t>& faces, std::vector<int64_t>& colour_ptr);
 
+// Smoothed-aggregation AMG hierarchy built on the host (amg_setup.cpp).
+struct HostCsr {
+    int64_t nrows = 0, ncols = 0;
+    std::vector<int64_t> ia;
+    std::vector<int32_t> ja;
+    std::vector<double> a;
+};
+struct AmgHostLevel {
+    HostCsr A;                       // level operator
+    HostCsr P, R;                    // prolongator from the next coarser level, R = P^T (empty on the coarsest)
+    std::vector<int32_t> agg;        // aggregate of each row (-1: left out)
+    double lmax = 0;                 // lmax(D^-1 A) estimate (Lanczos)
+};
+struct AmgHostCfg {
+    double threshold = 0.0;          // strength threshold (pc-gamg-threshold)
+    int max_levels = 10;             // pc-mg-levels
+    int coarse_eq_lim = 800;         // pc-gamg-coarse-eq-lim
+    int agg_smooths = 1;             // pc-gamg-nsmooths (0: unsmoothed aggregation)
+    int nthreads = 0;                // host threads (0: all)
+};
+struct AmgHierarchy {
+    std::vector<AmgHostLevel> levels;
+    std::vector<double> coarse_inv;  // dense inverse of the coarsest operator (row-major), or empty
+};
+constexpr int64_t kAmgDenseCoarse = 2048;   // largest coarsest level inverted densely
+bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err);
+
 // Boundary dof nodes: the nodes carried by faces owned by one element; when
 // `xmax_on` only the faces whose three vertices satisfy x <= xmax (+1e-12).
 bool boundary_nodes(int64_t nt, const int32_t* tets, const double* xyz, const Topology& topo, int xmax_on,
@@ -307,7 +334,7 @@ int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y,
 int launch_convert_values(fgpu_ctx* ctx, const fgpu_matrix* src, fgpu_matrix* dst);
 
 int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_x, const fgpu_solver_cfg* cfg,
-              fgpu_solve_stats* st);
+              fgpu_solve_stats* st, fgpu_amg* amg = nullptr);
 int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A32, const double* d_b, double* d_x,
                     const fgpu_solver_cfg* cfg, fgpu_solve_stats* st);
 

@@ -341,7 +341,8 @@ static int plan_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* 
 // picked by the tuner, iterations in cg_run (cg_driver.cuh).
 template <class PL>
 static int pcg_core(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* val, const typename PL::S* b,
-                    typename PL::S* x, const CgOptions& o, int pc, CgResult* res, const RefreshFn<PL>* refresh = nullptr) {
+                    typename PL::S* x, const CgOptions& o, int pc, CgResult* res, const RefreshFn<PL>* refresh = nullptr,
+                    fgpu_amg* amg = nullptr) {
     typedef typename PL::S S;
     const int64_t n = A->nrows;
     const int vb = vec_blocks(n);
@@ -363,7 +364,9 @@ static int pcg_core(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* v
     op.npq = plan.blocks(A);
     op.launches = 1;
     op.graph = true;
-    const int rc = cg_run<PL>(ctx, n, op, dinv, b, x, o, res, refresh);
+    PcHook<PL> hook;
+    if (amg) hook = amg_pc_hook<PL>(amg);
+    const int rc = cg_run<PL>(ctx, n, op, dinv, b, x, o, res, refresh, amg ? &hook : nullptr);
     cudaFree(dinv);
     return rc;
 }
@@ -396,7 +399,7 @@ struct Scratch64 {
 };
 
 int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_x, const fgpu_solver_cfg* cfg,
-              fgpu_solve_stats* st) {
+              fgpu_solve_stats* st, fgpu_amg* amg) {
     if (A->precision != FGPU_F64) { ctx->err = "solve needs an FP64 matrix"; return FGPU_ERR_INVALID; }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -457,7 +460,7 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
             d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_b, b);
             d2df_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, d_x, x);
             ctx->launches += 3;
-            rc = pcg_core<PolDF64>(ctx, A, val, b, x, opt, cfg->pc, &res, &refresh_df);
+            rc = pcg_core<PolDF64>(ctx, A, val, b, x, opt, cfg->pc, &res, &refresh_df, amg);
             if (rc == FGPU_OK) {
                 df2d_kernel<<<vec_blocks(n), 256, 0, ctx->stream>>>(n, x, d_x);
                 ctx->launches++;
@@ -465,7 +468,7 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
         }
         cudaFree(val); cudaFree(b); cudaFree(x);
     } else {
-        rc = pcg_core<PolF64>(ctx, A, (const double*)A->d_val, d_b, d_x, opt, cfg->pc, &res, &refresh64);
+        rc = pcg_core<PolF64>(ctx, A, (const double*)A->d_val, d_b, d_x, opt, cfg->pc, &res, &refresh64, amg);
     }
     cudaFree(xtmp);
     if (rc == FGPU_OK)    // final residual recomputed in binary64 from the matrix

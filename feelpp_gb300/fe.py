@@ -607,11 +607,11 @@ class Form1:
         self.vec.zero()
 
 
-_PC = {"none": _ffi.PC_NONE, "jacobi": _ffi.PC_JACOBI, "cheb_jacobi": _ffi.PC_CHEB_JACOBI}
+_PC = {"none": _ffi.PC_NONE, "jacobi": _ffi.PC_JACOBI, "cheb_jacobi": _ffi.PC_CHEB_JACOBI, "gamg": _ffi.PC_GAMG}
 
 
 def _solver_cfg(rtol, maxit, pc, mixed, inner_rtol, check_every, arith, cheb_degree, cheb_ratio):
-    """ksp-rtol, ksp-max-it, pc-type ("jacobi", "cheb_jacobi" or "none")."""
+    """ksp-rtol, ksp-max-it, pc-type ("jacobi", "cheb_jacobi", "gamg" or "none")."""
     if pc not in _PC:
         raise ValueError("pc must be one of %s" % sorted(_PC))
     return _ffi.SolverCfg(rtol, maxit, _PC[pc], 1 if mixed else 0, inner_rtol, check_every,
@@ -628,6 +628,7 @@ class Form2:
     """Bilinear form backed by a device CSR matrix with the Feel++ GraphCSR pattern."""
 
     def __init__(self, test, trial=None, precision="f64"):
+        self._version = 0
         self.space = test
         self.env = test.env
         self.precision = _ffi.F64 if precision == "f64" else _ffi.F32
@@ -655,6 +656,7 @@ class Form2:
         return self
 
     def zero(self):
+        self._version = getattr(self, "_version", 0) + 1
         self.env.check(self.env.lib.fgpu_matrix_zero(self.h))
 
     def _desc(self, integral):
@@ -699,6 +701,7 @@ class Form2:
         return d, kappa_arr
 
     def _assemble(self, integral, accumulate):
+        self._version = getattr(self, "_version", 0) + 1
         d, kappa_arr = self._desc(integral)
         self._kappa_host = kappa_arr  # keep alive during the call
         if kappa_arr is not None:
@@ -706,6 +709,7 @@ class Form2:
         self.env.check(self.env.lib.fgpu_assemble_matrix(self.env.h, self.h, C.byref(d), accumulate))
 
     def _on(self, item):
+        self._version = getattr(self, "_version", 0) + 1
         dofs = self.space.boundary_dofs(item.range.xmax if item.range.kind == "markedfaces" else None)
         vals = None
         if item.expr != 0.0:
@@ -716,6 +720,7 @@ class Form2:
     def apply_bc(self, bc, rhs=None, type="elimination_symmetric", diag=1.0):  # noqa: A002
         """Apply a DirichletBC (device-resident rows; capturable in graphs)."""
         t = {"elimination": 0, "elimination_symmetric": 1, "elimination_keep_diagonal": 2}[type]
+        self._version = getattr(self, "_version", 0) + 1
         vec = rhs.vec if isinstance(rhs, Form1) else rhs
         self.env.check(self.env.lib.fgpu_bc_apply(self.env.h, bc.h, self.h, vec.h if vec is not None else None, t, diag))
 
@@ -735,17 +740,39 @@ class Form2:
         self.env.check(self.env.lib.fgpu_matrix_mult(self.env.h, self.h, x.h, y.h))
 
     def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False, inner_rtol=0.1,
-              check_every=16, arith="f64", cheb_degree=0, cheb_ratio=0.0):
+              check_every=16, arith="f64", cheb_degree=0, cheb_ratio=0.0, gamg=None):
         """CG + Jacobi (ksp-type=cg, pc-type=jacobi). mixed=True: binary32 CG whose iterate is folded
         into the binary64 solution, and its residual replaced by the binary64 one, each time the
         recurrence residual has dropped by `inner_rtol`; arith="df64": double-float arithmetic for
-        the plain solve."""
+        the plain solve. pc="gamg": smoothed-aggregation AMG V-cycle, the hierarchy built on first use
+        (options in `gamg`, see AMG) and rebuilt when the matrix changed since."""
         cfg = _solver_cfg(rtol, maxit, pc, mixed, inner_rtol, check_every, arith, cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
         vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        if pc == "gamg":
+            amg = self.gamg(**(gamg or {}))
+            self.env.check(self.env.lib.fgpu_solve_cg_amg(self.env.h, self.h, amg.h, vec.h, solution.h, C.byref(cfg),
+                                                          C.byref(st)))
+            out = _stats(st)
+            out["gamg"] = amg.info()
+            return out
         self.env.check(self.env.lib.fgpu_solve_cg(self.env.h, self.h, None, vec.h, solution.h, C.byref(cfg),
                                                   C.byref(st)))
         return _stats(st)
+
+    def gamg(self, **opts):
+        """The AMG hierarchy of this matrix (built, or rebuilt when the values changed since)."""
+        amg = getattr(self, "_amg", None)
+        if amg is not None and amg.opts != opts:
+            amg = None
+        if amg is None:
+            amg = AMG(self, **opts)
+            self._amg = amg
+            self._amg_version = self._version
+        elif self._amg_version != self._version:
+            amg.update()
+            self._amg_version = self._version
+        return amg
 
     def __del__(self):
         try:
@@ -753,6 +780,42 @@ class Form2:
                 self.env.lib.fgpu_matrix_destroy(self.h)
         except Exception:
             pass
+
+
+class AMG:
+    """Smoothed-aggregation AMG hierarchy of an assembled FP64 form (pc-type=gamg; PETSc PCGAMG "agg"
+    options of the reference: threshold (pc-gamg-threshold), max_levels (pc-mg-levels), coarse_eq_lim
+    (pc-gamg-coarse-eq-lim), agg_smooths (pc-gamg-nsmooths; -1 = unsmoothed), smoother_degree
+    (Chebyshev degree of the level smoothers). 0 selects the default."""
+
+    def __init__(self, form, threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0):
+        self.env, self.form = form.env, form
+        self.opts = dict(threshold=threshold, max_levels=max_levels, coarse_eq_lim=coarse_eq_lim, agg_smooths=agg_smooths,
+                         smoother_degree=smoother_degree)
+        cfg = _ffi.AmgCfg(float(threshold), max_levels, coarse_eq_lim, agg_smooths, smoother_degree)
+        h = C.c_void_p()
+        self.env.check(self.env.lib.fgpu_amg_create(self.env.h, form.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def update(self):
+        self.env.check(self.env.lib.fgpu_amg_update(self.h))
+
+    def info(self):
+        nl = C.c_int()
+        rows = np.zeros(16, dtype=np.int64)
+        nnz = np.zeros(16, dtype=np.int64)
+        ms = C.c_double()
+        self.env.check(self.env.lib.fgpu_amg_info(self.h, C.byref(nl), _ptr(rows), _ptr(nnz), C.byref(ms)))
+        return {"levels": nl.value, "rows": rows[:nl.value].tolist(), "nnz": nnz[:nl.value].tolist(),
+                "setup_ms": ms.value}
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                self.env.lib.fgpu_amg_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
 
 
 class Operator:

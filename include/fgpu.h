@@ -76,6 +76,8 @@ extern "C" {
 #define FGPU_PC_JACOBI 1
 #define FGPU_PC_CHEB_JACOBI 2     /* degree-K Chebyshev polynomial in D^-1 A (Jacobi-scaled), PETSc
                                      KSPCHEBYSHEV+PCJACOBI used as a fixed preconditioner */
+#define FGPU_PC_GAMG 3            /* smoothed-aggregation AMG V-cycle (pc-type=gamg): fgpu_amg_create,
+                                     then fgpu_solve_cg_amg */
 
 #define FGPU_ARITH_F64 0          /* solver arithmetic: native FP64 (default) */
 #define FGPU_ARITH_DF64 1         /* double-float on the FP32 pipes (~48 bits; moderately conditioned systems) */
@@ -84,6 +86,7 @@ typedef struct fgpu_ctx fgpu_ctx;
 typedef struct fgpu_graph fgpu_graph;
 typedef struct fgpu_bc fgpu_bc;
 typedef struct fgpu_batch fgpu_batch;
+typedef struct fgpu_amg fgpu_amg;
 typedef struct fgpu_mesh fgpu_mesh;
 typedef struct fgpu_space fgpu_space;
 typedef struct fgpu_matrix fgpu_matrix;
@@ -145,6 +148,14 @@ typedef struct {
     double cheb_ratio;        /* FGPU_PC_CHEB_JACOBI: lambda_min / lambda_max of the interval (0 = 0.03);
                                  lambda_max = 1.1 x a Lanczos estimate (ksp_chebyshev_esteig 0,0.1,0,1.1) */
 } fgpu_solver_cfg;
+
+typedef struct {              /* smoothed-aggregation AMG (PETSc PCGAMG "agg" options of the reference) */
+    double threshold;         /* pc-gamg-threshold: drop couplings |a_ij| <= threshold sqrt(a_ii a_jj) (0) */
+    int max_levels;           /* pc-mg-levels (0 = 10) */
+    int coarse_eq_lim;        /* pc-gamg-coarse-eq-lim (0 = 800) */
+    int agg_smooths;          /* pc-gamg-nsmooths: 0 = default 1 (smoothed aggregation); -1 = none */
+    int smoother_degree;      /* Chebyshev degree of the level smoothers (0 = 3, i.e. 2 operator sweeps) */
+} fgpu_amg_cfg;
 
 typedef struct {
     int iterations;           /* total (inner) CG iterations */
@@ -245,6 +256,35 @@ int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, 
  *      NULL: then it is made from A). x is the initial guess and the solution. ---- */
 int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+
+/* ---- --pc-type=gamg (PCGAMG smoothed aggregation, feelpp/feel/feelalg/preconditionerpetsc.cpp:2229-2330):
+ *      fgpu_amg_create builds the hierarchy from the FP64 matrix A as it is now (host set-up: strength
+ *      graph, aggregation, smoothed prolongators, Galerkin products; levels then kept on the device in
+ *      binary32); fgpu_amg_update rebuilds it from A's current values; fgpu_solve_cg_amg runs CG in the
+ *      arithmetic of cfg->arith (FP64 or df64; cfg->mixed must be 0) preconditioned by one V-cycle per
+ *      iteration (Chebyshev level smoothers, dense coarsest solve). A must outlive the hierarchy. ---- */
+int fgpu_amg_create(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg** out);
+int fgpu_amg_update(fgpu_amg* amg);
+/* levels, rows[level], nnz[level] (arrays of at least 16 entries or NULL), host set-up time in ms */
+int fgpu_amg_info(const fgpu_amg* amg, int* nlevels, int64_t* rows, int64_t* nnz, double* setup_ms);
+int fgpu_amg_destroy(fgpu_amg* amg);
+int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
+                      const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+
+/* host-only hierarchy (no device): the same set-up from a host CSR, for inspection and tests.
+ * fgpu_amg_host_level: rows, nnz of A_l, nnz and columns of P_l (0 on the coarsest), lmax(D^-1 A_l);
+ * fgpu_amg_host_export: copies A_l (ia n+1, ja, a), P_l (ia n+1, ja, a) and the aggregate of each
+ * row (-1: left out) into caller arrays (NULL skips); fgpu_amg_host_coarse_inverse: 1 and the dense
+ * inverse of the coarsest operator (row-major) when one was formed, else 0. */
+typedef struct fgpu_amg_host fgpu_amg_host;
+int fgpu_amg_host_build(int64_t n, const int64_t* ia, const int32_t* ja, const double* a, const fgpu_amg_cfg* cfg, int nthreads,
+                        fgpu_amg_host** out);
+int fgpu_amg_host_levels(const fgpu_amg_host* h);
+int fgpu_amg_host_level(const fgpu_amg_host* h, int level, int64_t* n, int64_t* nnz, int64_t* p_nnz, int64_t* p_cols, double* lmax);
+int fgpu_amg_host_export(const fgpu_amg_host* h, int level, int64_t* ia, int32_t* ja, double* a, int64_t* pia, int32_t* pja,
+                         double* pa, int32_t* agg);
+int fgpu_amg_host_coarse_inverse(const fgpu_amg_host* h, double* out);
+int fgpu_amg_host_destroy(fgpu_amg_host* h);
 
 /* ---- error norms of a scalar field against u = sin(pi x) sin(pi y) sin(pi z):
  *      normL2(u_h - u) and the H1 seminorm (feelpp/feel/feelvf/norml2.hpp:37, normh1.hpp) ---- */
