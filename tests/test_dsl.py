@@ -67,8 +67,9 @@ def test_elasticity_and_sources():
 def test_solver_cfg_names():
     cfg = fe._solver_cfg(1e-10, 100, "cheb_jacobi", True, 0.1, 16, "f64", 3, 0.03)
     assert cfg.pc == _ffi.PC_CHEB_JACOBI and cfg.mixed == 1 and cfg.cheb_degree == 3
+    assert fe._solver_cfg(1e-10, 100, "gamg", False, 0.1, 16, "f64", 0, 0.0).pc == _ffi.PC_GAMG
     with pytest.raises(ValueError):
-        fe._solver_cfg(1e-10, 100, "gamg", False, 0.1, 16, "f64", 0, 0.0)
+        fe._solver_cfg(1e-10, 100, "ilu", False, 0.1, 16, "f64", 0, 0.0)
 
 
 def test_face_ranges():
