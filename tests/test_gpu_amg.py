@@ -82,4 +82,4 @@ def test_gamg_rejected_without_hierarchy(env):
     st = _ffi.SolveStats()
     w = V.element()
     rc = env.lib.fgpu_solve_cg(env.h, a.h, None, l.vec.h, w.h, C.byref(cfg), C.byref(st))
-    assert rc == _ffi.ERR_INVALID
+    assert _ffi.ERROR_NAMES[rc] == "FGPU_ERR_INVALID"
