@@ -17,10 +17,12 @@
 // The CG iterations stay in the solver's arithmetic (FP64); only the
 // preconditioner runs in binary32.
 //
-// Each level operator is applied by one kernel per sweep with G lanes per row
-// (G from the mean row length) and the smoother/residual update fused into
-// its epilogue; the lanes of a row sum in a fixed order, so a V-cycle is
-// deterministic.
+// Each level operator is stored in SELL-C-sigma form (32-row slices, rows
+// sorted by length inside 256-row windows, entries column-major: one thread
+// per row, coalesced loads) and applied by one kernel per sweep with the
+// smoother/residual update fused into its epilogue; prolongators and
+// restrictions stay in CSR with G lanes per row (G from the mean row length).
+// Every row is summed in a fixed order, so a V-cycle is deterministic.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -34,13 +36,15 @@ struct fgpu_amg {
     const fgpu_matrix* A = nullptr;
     struct Level {
         int64_t n = 0, nnz = 0;
-        const int64_t* ia = nullptr;
-        const int32_t* ja = nullptr;
-        int64_t* own_ia = nullptr;
-        int32_t* own_ja = nullptr;
-        float* a = nullptr;
         float* dinv = nullptr;
-        int G = 8;
+        // the level operator in SELL-C-sigma form (C = 32, sigma = 256): one thread per row,
+        // entries column-major inside each 32-row slice
+        int64_t nslices = 0;
+        int64_t* s_ptr = nullptr;
+        int32_t* s_len = nullptr;
+        int32_t* s_perm = nullptr;
+        int32_t* s_col = nullptr;
+        float* s_val = nullptr;
         int64_t* p_ia = nullptr;     // P_l: n x n_{l+1}
         int32_t* p_ja = nullptr;
         float* p_a = nullptr;
@@ -88,7 +92,77 @@ struct AmgSweep {
     int last = 0;
 };
 
-// one sweep of a level operator: s_i = sum_j a_ij x_j, then the mode's epilogue
+template <int MODE>
+__device__ __forceinline__ void amg_epilogue(const AmgSweep& s, int64_t i, float acc) {
+    if (MODE == kResid) {
+        s.out[i] = s.b[i] - acc;
+    } else if (MODE == kResidStart) {
+        const float wi = s.b[i] - acc;
+        const float d = s.dinv[i] * wi * s.inv_theta;
+        s.w[i] = wi;
+        s.dnew[i] = d;
+        s.acc[i] = d;
+    } else if (MODE == kCheb) {
+        const float wi = s.w[i] - acc;
+        const float dn = fmaf(s.c1, s.dprev[i], s.c2 * s.dinv[i] * wi);
+        if (s.last && s.out) {
+            s.out[i] += s.acc[i] + dn;
+        } else {
+            s.acc[i] += dn;
+            if (!s.last) {
+                s.w[i] = wi;
+                s.dnew[i] = dn;
+            }
+        }
+    } else if (MODE == kPlain) {
+        s.out[i] = acc;
+    } else {
+        s.out[i] += acc;
+    }
+}
+
+struct AmgSell {
+    int64_t nslices = 0;
+    const int64_t* ptr = nullptr;
+    const int32_t* len = nullptr;
+    const int32_t* perm = nullptr;
+    const int32_t* col = nullptr;
+    const float* val = nullptr;
+};
+
+// one sweep of a level operator in SELL form: thread per (sorted) row, then the epilogue on the
+// original row; every lane of a warp belongs to one slice, so the entry loop is warp-uniform
+template <int MODE>
+__global__ void __launch_bounds__(256) amg_sell_kernel(AmgSweep s, AmgSell m, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int64_t total = m.nslices * 32;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t sl = i >> 5;
+        const int L = __ldg(m.len + sl);
+        const int64_t base = __ldg(m.ptr + sl) + (i & 31);
+        // four entries' loads issued together (memory-level parallelism), summed in entry order
+        float acc = 0.0f;
+        int k = 0;
+        for (; k + 4 <= L; k += 4) {
+            const int64_t j = base + (int64_t)k * 32;
+            const int32_t c0 = __ldg(m.col + j), c1 = __ldg(m.col + j + 32), c2 = __ldg(m.col + j + 64), c3 = __ldg(m.col + j + 96);
+            const float v0 = __ldg(m.val + j), v1 = __ldg(m.val + j + 32), v2 = __ldg(m.val + j + 64), v3 = __ldg(m.val + j + 96);
+            const float x0 = __ldg(s.x + c0), x1 = __ldg(s.x + c1), x2 = __ldg(s.x + c2), x3 = __ldg(s.x + c3);
+            acc = fmaf(v0, x0, acc);
+            acc = fmaf(v1, x1, acc);
+            acc = fmaf(v2, x2, acc);
+            acc = fmaf(v3, x3, acc);
+        }
+        for (; k < L; ++k) {
+            const int64_t j = base + (int64_t)k * 32;
+            acc = fmaf(__ldg(m.val + j), __ldg(s.x + __ldg(m.col + j)), acc);
+        }
+        if (i < s.n) amg_epilogue<MODE>(s, __ldg(m.perm + i), acc);
+    }
+}
+
+// one sweep of a CSR operator (the prolongators and restrictions): s_i = sum_j a_ij x_j with G lanes
+// per row, then the mode's epilogue
 template <int G, int MODE>
 __global__ void __launch_bounds__(256) amg_sweep_kernel(AmgSweep s, const int* __restrict__ stop) {
     if (stop && *stop) return;
@@ -105,31 +179,7 @@ __global__ void __launch_bounds__(256) amg_sweep_kernel(AmgSweep s, const int* _
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
         if (lane != 0 || !valid) continue;
-        if (MODE == kResid) {
-            s.out[i] = s.b[i] - acc;
-        } else if (MODE == kResidStart) {
-            const float wi = s.b[i] - acc;
-            const float d = s.dinv[i] * wi * s.inv_theta;
-            s.w[i] = wi;
-            s.dnew[i] = d;
-            s.acc[i] = d;
-        } else if (MODE == kCheb) {
-            const float wi = s.w[i] - acc;
-            const float dn = fmaf(s.c1, s.dprev[i], s.c2 * s.dinv[i] * wi);
-            if (s.last && s.out) {
-                s.out[i] += s.acc[i] + dn;
-            } else {
-                s.acc[i] += dn;
-                if (!s.last) {
-                    s.w[i] = wi;
-                    s.dnew[i] = dn;
-                }
-            }
-        } else if (MODE == kPlain) {
-            s.out[i] = acc;
-        } else {
-            s.out[i] += acc;
-        }
+        amg_epilogue<MODE>(s, i, acc);
     }
 }
 
@@ -188,10 +238,6 @@ __global__ void amg_finish_kernel(int64_t n, const float* __restrict__ x0, const
     if (threadIdx.x == 0) partial_rz[blockIdx.x] = t;
 }
 
-__global__ void d2f_kernel(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = (float)in[i];
-}
-
 int lanes_for(int64_t n, int64_t nnz) {
     const double m = n > 0 ? (double)nnz / (double)n : 1.0;
     return m <= 6 ? 4 : m <= 12 ? 8 : m <= 24 ? 16 : 32;
@@ -213,6 +259,19 @@ void sweep(cudaStream_t st, int G, const AmgSweep& s, const int* stop) {
     }
 }
 
+template <int MODE>
+void sell_sweep(cudaStream_t st, const fgpu_amg::Level& V, const AmgSweep& s, const int* stop) {
+    AmgSell m;
+    m.nslices = V.nslices;
+    m.ptr = V.s_ptr;
+    m.len = V.s_len;
+    m.perm = V.s_perm;
+    m.col = V.s_col;
+    m.val = V.s_val;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((V.nslices * 32 + 255) / 256, 152 * 16));
+    amg_sell_kernel<MODE><<<g, 256, 0, st>>>(s, m, stop);
+}
+
 int vblocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8)); }
 
 // Chebyshev steps 1..K-1 on level l accumulating into acc; the last step adds acc + d into target when set
@@ -220,7 +279,7 @@ int cheb_steps(cudaStream_t st, fgpu_amg::Level& V, int K, float* acc, float* ta
     int nl = 0;
     for (int k = 1; k < K; ++k) {
         AmgSweep s;
-        s.n = V.n; s.ia = V.ia; s.ja = V.ja; s.a = V.a;
+        s.n = V.n;
         s.dprev = (k & 1) ? V.d0 : V.d1;
         s.dnew = (k & 1) ? V.d1 : V.d0;
         s.x = s.dprev;
@@ -231,7 +290,7 @@ int cheb_steps(cudaStream_t st, fgpu_amg::Level& V, int K, float* acc, float* ta
         s.c2 = V.c2[k - 1];
         s.last = k == K - 1;
         s.out = s.last ? target : nullptr;
-        sweep<kCheb>(st, V.G, s, stop);
+        sell_sweep<kCheb>(st, V, s, stop);
         ++nl;
     }
     return nl;
@@ -266,8 +325,8 @@ int amg_vcycle(fgpu_amg* M, const T* r, const int* stop) {
         }
         nl += cheb_steps(st, V, Kl, V.x, nullptr, stop);
         AmgSweep s;
-        s.n = V.n; s.ia = V.ia; s.ja = V.ja; s.a = V.a; s.x = V.x; s.b = V.b; s.out = V.w;
-        sweep<kResid>(st, V.G, s, stop);
+        s.n = V.n; s.x = V.x; s.b = V.b; s.out = V.w;
+        sell_sweep<kResid>(st, V, s, stop);
         fgpu_amg::Level& C = M->L[l + 1];
         AmgSweep rs;
         rs.n = C.n; rs.ia = V.r_ia; rs.ja = V.r_ja; rs.a = V.r_a; rs.x = V.w; rs.out = C.b;
@@ -281,9 +340,9 @@ int amg_vcycle(fgpu_amg* M, const T* r, const int* stop) {
         ps.n = V.n; ps.ia = V.p_ia; ps.ja = V.p_ja; ps.a = V.p_a; ps.x = C.x; ps.out = V.x;
         sweep<kAdd>(st, V.pG, ps, stop);
         AmgSweep s;
-        s.n = V.n; s.ia = V.ia; s.ja = V.ja; s.a = V.a; s.x = V.x; s.b = V.b; s.dinv = V.dinv; s.w = V.w; s.dnew = V.d0;
+        s.n = V.n; s.x = V.x; s.b = V.b; s.dinv = V.dinv; s.w = V.w; s.dnew = V.d0;
         s.acc = V.e; s.inv_theta = V.inv_theta;
-        sweep<kResidStart>(st, V.G, s, stop);
+        sell_sweep<kResidStart>(st, V, s, stop);
         nl += 2 + cheb_steps(st, V, M->degree, V.e, V.x, stop);
     }
     return nl;
@@ -316,7 +375,8 @@ template PcHook<PolF32> amg_pc_hook<PolF32>(fgpu_amg*);
 namespace {
 
 void free_level(fgpu_amg::Level& V) {
-    cudaFree(V.own_ia); cudaFree(V.own_ja); cudaFree(V.a); cudaFree(V.dinv);
+    cudaFree(V.dinv);
+    cudaFree(V.s_ptr); cudaFree(V.s_len); cudaFree(V.s_perm); cudaFree(V.s_col); cudaFree(V.s_val);
     cudaFree(V.p_ia); cudaFree(V.p_ja); cudaFree(V.p_a); cudaFree(V.r_ia); cudaFree(V.r_ja); cudaFree(V.r_a);
     cudaFree(V.x); cudaFree(V.b); cudaFree(V.w); cudaFree(V.d0); cudaFree(V.d1); cudaFree(V.e);
     V = fgpu_amg::Level();
@@ -341,6 +401,50 @@ template <typename T>
 cudaError_t upload(T** dst, const T* src, size_t n) {
     cudaError_t e = cudaMalloc(dst, std::max<size_t>(n, 1) * sizeof(T));
     if (e == cudaSuccess && n) e = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// SELL-C-sigma of a host CSR: rows sorted by length (descending, ties by row) inside windows
+// of 256 rows, slices of 32 rows padded to their longest row (padding: column = the row, value 0)
+cudaError_t upload_sell(fgpu_amg::Level& V, const HostCsr& A) {
+    constexpr int kC = 32, kSigma = 256;
+    const int64_t n = A.nrows;
+    V.nslices = (n + kC - 1) / kC;
+    std::vector<int32_t> perm(n), len(V.nslices, 0);
+    for (int64_t w0 = 0; w0 < n; w0 += kSigma) {
+        const int64_t w1 = std::min<int64_t>(n, w0 + kSigma);
+        for (int64_t r = w0; r < w1; ++r) perm[r] = (int32_t)r;
+        std::sort(perm.begin() + w0, perm.begin() + w1, [&](int32_t a, int32_t b) {
+            const int64_t la = A.ia[a + 1] - A.ia[a], lb = A.ia[b + 1] - A.ia[b];
+            return la != lb ? la > lb : a < b;
+        });
+    }
+    std::vector<int64_t> ptr(V.nslices + 1, 0);
+    for (int64_t sl = 0; sl < V.nslices; ++sl) {
+        int64_t L = 0;
+        for (int64_t i = sl * kC; i < std::min<int64_t>(n, (sl + 1) * kC); ++i) L = std::max<int64_t>(L, A.ia[perm[i] + 1] - A.ia[perm[i]]);
+        len[sl] = (int32_t)L;
+        ptr[sl + 1] = ptr[sl] + L * kC;
+    }
+    std::vector<int32_t> col(ptr[V.nslices]);
+    std::vector<float> val(ptr[V.nslices]);
+    for (int64_t i = 0; i < V.nslices * kC; ++i) {
+        const int64_t sl = i / kC;
+        const int64_t base = ptr[sl] + (i - sl * kC);
+        const int32_t row = i < n ? perm[i] : -1;
+        const int64_t b = row >= 0 ? A.ia[row] : 0, e = row >= 0 ? A.ia[row + 1] : 0;
+        for (int64_t k = 0; k < len[sl]; ++k) {
+            const int64_t p = b + k;
+            const bool real = p < e;
+            col[base + k * kC] = real ? A.ja[p] : (row >= 0 ? row : 0);
+            val[base + k * kC] = real ? (float)A.a[p] : 0.0f;
+        }
+    }
+    cudaError_t e = upload(&V.s_ptr, ptr.data(), ptr.size());
+    if (e == cudaSuccess) e = upload(&V.s_len, len.data(), len.size());
+    if (e == cudaSuccess) e = upload(&V.s_perm, perm.data(), perm.size());
+    if (e == cudaSuccess) e = upload(&V.s_col, col.data(), col.size());
+    if (e == cudaSuccess) e = upload(&V.s_val, val.data(), val.size());
     return e;
 }
 
@@ -387,26 +491,12 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
         V.lmax = hl.lmax;
         const bool coarsest = l == nlev - 1;
         cheb_coefs(V, coarsest ? M->coarse_degree : M->degree);
-        V.G = lanes_for(V.n, V.nnz);
         std::vector<double> dinv(V.n, 0.0);
         for (int64_t i = 0; i < V.n; ++i)
             for (int64_t p = hl.A.ia[i]; p < hl.A.ia[i + 1]; ++p)
                 if (hl.A.ja[p] == i) dinv[i] = 1.0 / hl.A.a[p];
         FGPU_CUDA_CHECK(ctx, upload_f32(&V.dinv, dinv));
-        if (l == 0) {
-            V.ia = A->d_ia;
-            V.ja = A->d_ja;
-            FGPU_CUDA_CHECK(ctx, cudaMalloc(&V.a, std::max<int64_t>(V.nnz, 1) * sizeof(float)));
-            d2f_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>((V.nnz + 255) / 256, 152 * 32)), 256, 0, ctx->stream>>>(
-                V.nnz, (const double*)A->d_val, V.a);
-            ctx->launches++;
-        } else {
-            FGPU_CUDA_CHECK(ctx, upload(&V.own_ia, hl.A.ia.data(), hl.A.ia.size()));
-            FGPU_CUDA_CHECK(ctx, upload(&V.own_ja, hl.A.ja.data(), hl.A.ja.size()));
-            FGPU_CUDA_CHECK(ctx, upload_f32(&V.a, hl.A.a));
-            V.ia = V.own_ia;
-            V.ja = V.own_ja;
-        }
+        FGPU_CUDA_CHECK(ctx, upload_sell(V, hl.A));
         if (!coarsest) {
             V.p_nnz = (int64_t)hl.P.ja.size();
             V.r_nnz = (int64_t)hl.R.ja.size();

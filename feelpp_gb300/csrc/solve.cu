@@ -216,7 +216,19 @@ __global__ void __launch_bounds__(256) sell_spmv_kernel(int64_t nrows, int64_t n
         const int L = slice_len[s];
         const int64_t base = slice_ptr[s] + (i - s * kSellC);
         typename PL::D accd = PL::dzero();     // row sums in the dot-product type (see spmv_kernel)
-        for (int k = 0; k < L; ++k) {
+        // four entries' loads issued together (memory-level parallelism), summed in entry order
+        int k = 0;
+        for (; k + 4 <= L; k += 4) {
+            const int64_t j = base + (int64_t)k * kSellC;
+            const int32_t c0 = col[j], c1 = col[j + kSellC], c2 = col[j + 2 * kSellC], c3 = col[j + 3 * kSellC];
+            const typename PL::V v0 = val[j], v1 = val[j + kSellC], v2 = val[j + 2 * kSellC], v3 = val[j + 3 * kSellC];
+            const typename PL::S x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+            accd = PL::dmadd(accd, PL::ldv(v0), PL::ld(x0));
+            accd = PL::dmadd(accd, PL::ldv(v1), PL::ld(x1));
+            accd = PL::dmadd(accd, PL::ldv(v2), PL::ld(x2));
+            accd = PL::dmadd(accd, PL::ldv(v3), PL::ld(x3));
+        }
+        for (; k < L; ++k) {
             const int64_t j = base + (int64_t)k * kSellC;
             accd = PL::dmadd(accd, PL::ldv(val[j]), PL::ld(x[col[j]]));
         }
