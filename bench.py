@@ -59,8 +59,10 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg"],
-                   help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed)")
+    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg"],
+                   help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
+                        "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
+                        "AMG-preconditioned CG solve to 1e-10")
     return p.parse_args()
 
 
@@ -427,6 +429,24 @@ def run_probe_cg(args):
             a.solve(rhs=l, solution=w, rtol=1e-10, maxit=48, mixed=mixed)
         except fpp.FgpuError as e:
             print("stopped:", e)
+
+
+def run_probe_gamg(args):
+    """One AMG-preconditioned CG solve (pc=gamg, rtol 1e-10) of the Poisson system on the bench mesh
+    (kappa = 1, homogeneous Dirichlet), for kernel profiling; prints iterations and times."""
+    import feelpp_gb300 as fpp
+    env = fpp.Environment()
+    _, xyz, tets, kappa, M, V = build_workload(args.n, args.order, env)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v))))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    w = V.element()
+    st = a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
+    print(json.dumps({"iterations": st["iterations"], "time_ms": st["time_ms"], "rel_residual": st["rel_residual"],
+                      "gamg": st["gamg"]}), flush=True)
 
 
 def run_matfree(args):
@@ -836,6 +856,9 @@ def main():
         return
     if args.probe == "cg":
         run_probe_cg(args)
+        return
+    if args.probe == "gamg":
+        run_probe_gamg(args)
         return
     if args.workload == "matfree":
         run_matfree(args)
