@@ -55,3 +55,25 @@ def lognormal_kappa(nt, seed=5678):
 
 def unit_cube(n, perturb=0.0, seed=1234):
     return kuhn_box(n, perturb=perturb, seed=seed)
+
+
+# local edges of a tetrahedron in the reference dof order (vertex pairs)
+EDGE_VERTS = ((1, 2), (2, 0), (0, 1), (0, 3), (1, 3), (2, 3))
+
+
+def bulge_map(xyz, amp):
+    """Smooth map of the unit cube onto a curved domain: x + amp (sin pi y sin pi z, sin pi z sin pi x,
+    sin pi x sin pi y); every face of the cube bulges outwards or inwards."""
+    x, y, z = xyz[..., 0], xyz[..., 1], xyz[..., 2]
+    s = np.sin
+    return np.stack([x + amp * s(np.pi * y) * s(np.pi * z), y + amp * s(np.pi * z) * s(np.pi * x),
+                     z + amp * s(np.pi * x) * s(np.pi * y)], axis=-1)
+
+
+def curved_box(n, amp=0.1, perturb=0.0, seed=1234):
+    """Kuhn mesh of the unit cube mapped by bulge_map, as curved (P2-geometry) tetrahedra: vertices and
+    edge nodes are images of the straight mesh's vertices and edge midpoints. Returns xyz (V x 3),
+    tets (T x 4) and ho (T x 6 x 3, the edge nodes in EDGE_VERTS order)."""
+    xyz0, tets = kuhn_box(n, perturb=perturb, seed=seed)
+    mids = np.stack([0.5 * (xyz0[tets[:, a]] + xyz0[tets[:, b]]) for a, b in EDGE_VERTS], axis=1)
+    return bulge_map(xyz0, amp), tets, bulge_map(mids, amp)

@@ -538,6 +538,8 @@ bool make_tab(int order, int qdeg, Tab& t) {
 // the reference element are (-1/2,-1/2,-1/2), (1/2,0,0), (0,1/2,0), (0,0,1/2).
 // The 3x3 inverse is the cofactor formula (Eigen's compute_inverse<3x3>).
 // ---------------------------------------------------------------------------
+static void geomap_finish(const double K[9], double& J, double B[9], double& detK);
+
 void geomap(const double* xyz, const int32_t* tet, double K[9], double& J, double B[9], double& detK) {
     const double g[4][3] = {{-0.5, -0.5, -0.5}, {0.5, 0, 0}, {0, 0.5, 0}, {0, 0, 0.5}};
     for (int i = 0; i < 9; ++i) K[i] = 0;
@@ -546,6 +548,24 @@ void geomap(const double* xyz, const int32_t* tet, double K[9], double& J, doubl
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 3; ++c) K[3 * r + c] += X[r] * g[v][c];
     }
+    geomap_finish(K, J, B, detK);
+}
+
+// Curved (P2) tetrahedra: x(xh) = sum_g X_g psi_g(xh) over the 10 P2 Lagrange
+// functions (vertices, then edge midpoints in e2p order); at each quadrature
+// point K = sum_g X_g (grad psi_g)^T, then J and B as for the affine map
+// (feelpp/feel/feelpoly/geomap.hpp:2310-2350; the context recomputes K at every
+// point when the map is not linear, :1014-1042).
+static void geomap_ho(const double X[10][3], const double* dpsi /* 10 x 3 */, double K[9], double& J, double B[9],
+                      double& detK) {
+    for (int i = 0; i < 9; ++i) K[i] = 0;
+    for (int g = 0; g < 10; ++g)
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) K[3 * r + c] += X[g][r] * dpsi[3 * g + c];
+    geomap_finish(K, J, B, detK);
+}
+
+static void geomap_finish(const double K[9], double& J, double B[9], double& detK) {
     double c00 = K[4] * K[8] - K[5] * K[7];
     double c01 = K[5] * K[6] - K[3] * K[8];
     double c02 = K[3] * K[7] - K[4] * K[6];
@@ -860,6 +880,79 @@ int orc_rhs(int order, int ncomp, int qdeg, const double* xyz, int64_t T, const 
             }
         }
         for (int i = 0; i < nle; ++i) F[l2g[e * nle + i]] += Fe[i];
+    }
+    return 0;
+}
+
+// Scalar Laplace/mass matrix and load vector on curved (P2-geometry) tetrahedra:
+// ho = T x 6 x 3 coordinates of the edge nodes (e2p order). Same quadrature sums
+// as orc_assemble / orc_rhs with the map evaluated per point.
+static void element_nodes(const double* xyz, const int32_t* tet, const double* ho, double X[10][3]) {
+    for (int v = 0; v < 4; ++v)
+        for (int r = 0; r < 3; ++r) X[v][r] = xyz[3 * (int64_t)tet[v] + r];
+    for (int j = 0; j < 6; ++j)
+        for (int r = 0; r < 3; ++r) X[4 + j][r] = ho[3 * j + r];
+}
+
+int orc_assemble_ho(int order, int qdeg, const double* xyz, int64_t T, const int32_t* tets, const double* ho,
+                    const int32_t* l2g, const double* kappa, double kappa_const, double mass, const int64_t* ia,
+                    const int32_t* ja, double* val) {
+    Tab tab, geo;
+    if (!make_tab(order, qdeg, tab) || !make_tab(2, qdeg, geo)) return -1;
+    const int n = tab.n, Q = tab.Q;
+    vector<double> Ke((size_t)n * n), gp(n * 3);
+    for (int64_t e = 0; e < T; ++e) {
+        double X[10][3];
+        element_nodes(xyz, tets + 4 * e, ho + 18 * e, X);
+        const double kap = kappa ? kappa[e] : kappa_const;
+        std::fill(Ke.begin(), Ke.end(), 0.0);
+        for (int q = 0; q < Q; ++q) {
+            double K[9], B[9], J, d;
+            geomap_ho(X, &geo.dphi[(size_t)q * 10 * 3], K, J, B, d);
+            const double wJ = tab.w[q] * J;
+            for (int i = 0; i < n; ++i) {
+                const double* gh = &tab.dphi[(size_t)(q * n + i) * 3];
+                for (int r = 0; r < 3; ++r) gp[i * 3 + r] = B[3 * r] * gh[0] + B[3 * r + 1] * gh[1] + B[3 * r + 2] * gh[2];
+            }
+            const double* ph = &tab.phi[(size_t)q * n];
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    double g = gp[j * 3] * gp[i * 3] + gp[j * 3 + 1] * gp[i * 3 + 1] + gp[j * 3 + 2] * gp[i * 3 + 2];
+                    Ke[(size_t)i * n + j] += wJ * (kap * g + mass * ph[j] * ph[i]);
+                }
+        }
+        const int32_t* rows = l2g + e * n;
+        for (int i = 0; i < n; ++i) {
+            const int32_t* b = ja + ia[rows[i]];
+            const int32_t* en = ja + ia[rows[i] + 1];
+            for (int j = 0; j < n; ++j) val[std::lower_bound(b, en, rows[j]) - ja] += Ke[(size_t)i * n + j];
+        }
+    }
+    return 0;
+}
+
+int orc_rhs_ho(int order, int qdeg, const double* xyz, int64_t T, const int32_t* tets, const double* ho, const int32_t* l2g,
+               int fkind, const double* fc, double* F) {
+    Tab tab, geo;
+    if (!make_tab(order, qdeg, tab) || !make_tab(2, qdeg, geo)) return -1;
+    const int n = tab.n, Q = tab.Q;
+    vector<double> Fe(n);
+    for (int64_t e = 0; e < T; ++e) {
+        double X[10][3];
+        element_nodes(xyz, tets + 4 * e, ho + 18 * e, X);
+        std::fill(Fe.begin(), Fe.end(), 0.0);
+        for (int q = 0; q < Q; ++q) {
+            double K[9], B[9], J, d;
+            geomap_ho(X, &geo.dphi[(size_t)q * 10 * 3], K, J, B, d);
+            double P[3] = {0, 0, 0};
+            for (int g = 0; g < 10; ++g)
+                for (int r = 0; r < 3; ++r) P[r] += X[g][r] * geo.phi[(size_t)q * 10 + g];
+            const double f = fkind == 0 ? 3.0 * M_PI * M_PI * std::sin(M_PI * P[0]) * std::sin(M_PI * P[1]) * std::sin(M_PI * P[2])
+                                        : fc[0];
+            const double wJ = tab.w[q] * J;
+            for (int i = 0; i < n; ++i) Fe[i] += wJ * f * tab.phi[(size_t)q * n + i];
+        }
+        for (int i = 0; i < n; ++i) F[l2g[e * n + i]] += Fe[i];
     }
     return 0;
 }

@@ -29,6 +29,8 @@ def lib():
             "orc_geometry": (i32, [P, i64, P, P, P, P]),
             "orc_assemble": (i32, [i32, i32, i32, P, i64, P, P, i32, P, f64, f64, f64, f64, i64, P, P, P, i32, i64]),
             "orc_rhs": (i32, [i32, i32, i32, P, i64, P, P, i32, P, P]),
+            "orc_assemble_ho": (i32, [i32, i32, P, i64, P, P, P, P, f64, f64, P, P, P]),
+            "orc_rhs_ho": (i32, [i32, i32, P, i64, P, P, P, i32, P, P]),
             "orc_boundary_mask": (i32, [i32, i32, P, i64, P, P, i32, f64, i64, P]),
             "orc_dirichlet": (i32, [i64, P, P, P, P, P, P, i32, f64]),
             "orc_spmv": (i32, [i64, P, P, P, P, P]),
@@ -320,4 +322,28 @@ def face_terms_load(order, xyz, tets, l2g, N, g=0.0, g_h=0.0, g_dn=0.0, xplane=N
         nrm, h = _face_normal_h(xyz, tets, e, f)
         A = _face_area(xyz, tets, e, f)
         F[l2g[e]] += A * ((g + g_h / h) * (w @ phi) + g_dn * (w @ (grad @ nrm)))
+    return F
+
+
+def assemble_ho(order, xyz, tets, ho, l2g, ia, ja, kappa=None, kappa_const=1.0, mass=0.0, qdeg=None):
+    """Scalar kappa grad.grad + mass u v on curved (P2-geometry) tetrahedra; ho = T x 6 x 3 edge nodes."""
+    qdeg = 2 * order + 2 if qdeg is None else qdeg
+    val = np.zeros(len(ja))
+    kap = None if kappa is None else _c(kappa, np.float64)
+    rc = lib().orc_assemble_ho(order, qdeg, _p(_c(xyz, np.float64)), len(tets), _p(_c(tets, np.int32)),
+                               _p(_c(ho, np.float64)), _p(_c(l2g, np.int32)), _p(kap), kappa_const, mass,
+                               _p(_c(ia, np.int64)), _p(_c(ja, np.int32)), _p(val))
+    if rc != 0:
+        raise RuntimeError("orc_assemble_ho failed: %d" % rc)
+    return val
+
+
+def rhs_ho(order, xyz, tets, ho, l2g, N, fkind=0, c=0.0, qdeg=None):
+    qdeg = 2 * order + 2 if qdeg is None else qdeg
+    F = np.zeros(N)
+    fc = np.array([c, 0.0, 0.0])
+    rc = lib().orc_rhs_ho(order, qdeg, _p(_c(xyz, np.float64)), len(tets), _p(_c(tets, np.int32)), _p(_c(ho, np.float64)),
+                          _p(_c(l2g, np.int32)), fkind, _p(fc), _p(F))
+    if rc != 0:
+        raise RuntimeError("orc_rhs_ho failed: %d" % rc)
     return F

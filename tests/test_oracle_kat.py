@@ -271,3 +271,54 @@ def test_nitsche_constant_solution(oracle):
     A = sp.csr_matrix((val, ja, ia), shape=(N, N))
     u = spla.spsolve(A.tocsc(), F)
     assert np.abs(u - c).max() <= 1e-10
+
+
+def _dof_coords_ho(oracle, order, xyz, tets, ho, l2g, N):
+    """Physical coordinates of the dofs on curved tetrahedra: x = sum_g X_g psi_g(node)."""
+    nodes = oracle.nodes(order)
+    psi, _ = oracle.tabulate(2, nodes)                      # (n, 10)
+    pts = np.zeros((N, 3))
+    for e, t in enumerate(tets):
+        X = np.vstack([xyz[t], ho[e]])                      # (10, 3)
+        pts[l2g[e]] = psi @ X
+    return pts
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_curved_geometry_kats(oracle, order):
+    """Known answers of the curved-tetrahedron (P2 geometry) restatement: with straight edges it equals
+    the affine assembly; on a curved mesh the mass matrix sums to the discrete volume, which converges to
+    the volume of the mapped cube; the Laplacian kills constants, and (order >= 2, where the curved space
+    contains the linear functions) the energy of u = a.x is |a|^2 times the discrete volume."""
+    from feelpp_gb300 import meshgen
+    xyz, tets, ho = meshgen.curved_box(3, amp=0.0, perturb=0.2)
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, order, mass=0.5, qdeg=2 * order + 2)
+    vho = oracle.assemble_ho(order, xyz, tets, ho, l2g, ia, ja, mass=0.5)
+    assert np.abs(vho - val).max() <= 1e-13 * np.abs(val).max()
+    F = oracle.rhs(order, xyz, tets, l2g, N, fkind=0, qdeg=2 * order + 2)
+    assert np.abs(oracle.rhs_ho(order, xyz, tets, ho, l2g, N) - F).max() <= 1e-13 * np.abs(F).max()
+    # a cube whose top face bulges: (x, y, z) -> (x, y, z + a z sin(pi x) sin(pi y)), volume 1 + 4a/pi^2
+    amp = 0.2
+
+    def top_bulge(p):
+        return np.stack([p[..., 0], p[..., 1], p[..., 2] * (1 + amp * np.sin(np.pi * p[..., 0]) * np.sin(np.pi * p[..., 1]))],
+                        axis=-1)
+
+    vols = []
+    for n in (2, 4):
+        xyz0, tets = meshgen.kuhn_box(n)
+        mids = np.stack([0.5 * (xyz0[tets[:, a]] + xyz0[tets[:, b]]) for a, b in meshgen.EDGE_VERTS], axis=1)
+        xyz, ho = top_bulge(xyz0), top_bulge(mids)
+        N, l2g = oracle.dof_table(tets, order)
+        ia, ja = oracle.pattern(N, l2g)
+        M = oracle.assemble_ho(order, xyz, tets, ho, l2g, ia, ja, kappa_const=0.0, mass=1.0)
+        vols.append(M.sum())
+        K = oracle.assemble_ho(order, xyz, tets, ho, l2g, ia, ja, kappa_const=1.0, mass=0.0)
+        Kd = _csr_dense(ia, ja, K, N)
+        assert np.abs(Kd @ np.ones(N)).max() <= 1e-12 * np.abs(Kd).max()
+        if order >= 2:
+            a = np.array([0.3, -1.1, 0.7])
+            u = _dof_coords_ho(oracle, order, xyz, tets, ho, l2g, N) @ a
+            assert abs(u @ Kd @ u - (a @ a) * M.sum()) <= 1e-12 * (a @ a)
+    exact = 1.0 + 4.0 * amp / np.pi ** 2
+    assert abs(vols[1] - exact) < 0.2 * abs(vols[0] - exact) and abs(vols[1] - exact) < 1e-3
