@@ -107,6 +107,7 @@ SIGNATURES = {
     "fgpu_amg_update": (i32, [P]),
     "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),
     "fgpu_amg_destroy": (i32, [P]),
+    "fgpu_mesh_set_ho_nodes": (i32, [P, P]),
     "fgpu_solve_cg_amg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
     "fgpu_amg_host_build": (i32, [i64, P, P, P, C.POINTER(AmgCfg), i32, PP]),
     "fgpu_amg_host_levels": (i32, [P]),

@@ -240,6 +240,7 @@ int fgpu_mesh_destroy(fgpu_mesh* M) {
     cudaFree(M->d_xyz);
     cudaFree(M->d_tets);
     cudaFree(M->d_colour_perm);
+    cudaFree(M->d_ho);
     delete M;
     return FGPU_OK;
 }
@@ -524,6 +525,7 @@ static int auto_assembly_algo(fgpu_ctx* ctx, const fgpu_matrix* A) {
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
     if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
     if (f->range == FGPU_RANGE_BOUNDARY_FACES || f->range == FGPU_RANGE_MARKED_FACES) {
+        if (A->space->mesh->d_ho) return set_err(ctx, FGPU_ERR_INVALID, "face integrals: flat faces only (the mesh has curved elements)");
         if (f->kind != FGPU_FORM_LAPLACE_MASS || f->kappa != 0.0 || d_kappa || f->kappa_scale)
             return set_err(ctx, FGPU_ERR_INVALID,
                            "face integrals: terms idt(u)*id(v), idt(u)*id(v)/hFace(), (gradt(u).N)*id(v), (grad(v).N)*idt(u)");
@@ -535,6 +537,11 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     if (f->mass_h != 0.0 || f->dn_trial != 0.0 || f->dn_test != 0.0)
         return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: hFace()/N() terms on face ranges only");
     fgpu_space* V = A->space;
+    if (V->mesh->d_ho) {             // curved (P2-geometry) elements: quadrature element kernel + gather map
+        const int rc = launch_assemble_ho(ctx, A, f, d_kappa, accumulate);
+        if (rc) return rc;
+        return finish(ctx);
+    }
     const int qdeg = form_qdeg(V, f->quad_degree);
     std::string err;
     DevTables* tab = get_dev_tables(V->order, qdeg, err);
@@ -651,6 +658,7 @@ int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc
     FGPU_NO_CAPTURE(ctx, "assemble_vector");
     if (!ctx || !V || !rhs || !out || out->n != V->ndof) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad arguments");
     if (rhs->range == FGPU_RANGE_BOUNDARY_FACES || rhs->range == FGPU_RANGE_MARKED_FACES) {
+        if (V->mesh->d_ho) return set_err(ctx, FGPU_ERR_INVALID, "face integrals: flat faces only (the mesh has curved elements)");
         if (rhs->kind != FGPU_RHS_CONST && rhs->kind != FGPU_RHS_FACE)
             return set_err(ctx, FGPU_ERR_INVALID, "face integrals: loads FGPU_RHS_CONST or FGPU_RHS_FACE");
         const bool ft = rhs->kind == FGPU_RHS_FACE;
@@ -661,6 +669,11 @@ int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc
     }
     if (rhs->range != FGPU_RANGE_ELEMENTS) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad range");
     if (rhs->kind == FGPU_RHS_FACE) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: FGPU_RHS_FACE on face ranges only");
+    if (V->mesh->d_ho) {
+        const int rc = launch_rhs_ho(ctx, V, rhs, out->d, accumulate);
+        const int rc2 = finish(ctx);
+        return rc ? rc : rc2;
+    }
     const int qdeg = form_qdeg(V, rhs->quad_degree);
     std::string err;
     DevTables* tab = get_dev_tables(V->order, qdeg, err);
@@ -940,6 +953,7 @@ int fgpu_host_df64_ops(int op, int64_t n, const double* a, const double* b, doub
 int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, int quad_degree, double* l2, double* h1) {
     FGPU_NO_CAPTURE(ctx, "norms_sine");
     if (!ctx || !V || !u || !l2 || !h1 || u->n != V->ndof || V->ncomp != 1) return set_err(ctx, FGPU_ERR_INVALID, "norms: bad arguments");
+    if (V->mesh->d_ho) return set_err(ctx, FGPU_ERR_INVALID, "norms: affine elements only");
     std::string err;
     DevTables* tab = get_dev_tables(V->order, quad_degree > 0 ? quad_degree : 2 * V->order, err);
     if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);

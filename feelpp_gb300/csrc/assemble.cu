@@ -1566,6 +1566,54 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     return FGPU_OK;
 }
 
+// Two-phase helpers for element kernels defined elsewhere (curved elements): the gather map and an
+// element buffer of at least `need` bytes, then phase 2 for the matrix's precision.
+int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need) {
+    fgpu_space* V = A->space;
+    if (!V->d_gptr) {
+        if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (gather map)"; return FGPU_ERR_INVALID; }
+        int rc = launch_build_gather_map(ctx, V);
+        if (rc) return rc;
+    }
+    if (A->kbuf_bytes < need) {
+        if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (element buffer)"; return FGPU_ERR_INVALID; }
+        cudaFree(A->d_kbuf);
+        A->d_kbuf = nullptr;
+        A->kbuf_bytes = 0;
+        if (cudaMalloc(&A->d_kbuf, need) != cudaSuccess) { cudaGetLastError(); ctx->err = "two-phase assembly: element buffer allocation failed"; return FGPU_ERR_ALLOC; }
+        A->kbuf_bytes = need;
+    }
+    return FGPU_OK;
+}
+
+int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate) {
+    fgpu_space* V = A->space;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t nnz = A->pattern->nnz;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, (int64_t)sms * 32));
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather", ev);
+    if (A->precision == FGPU_F32)
+        gather_map_kernel<kModeF32><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
+    else
+        gather_map_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
+int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate) {
+    const int64_t nn = V->topo.nnodes;
+    const int64_t gb = std::max<int64_t>(1, std::min<int64_t>((nn + 255) / 256, 152 * 16));
+    PendingEvent ev;
+    prof_begin(ctx, "rhs_gather", ev);
+    rhs_gather_kernel<<<(int)gb, 256, 0, ctx->stream>>>(nn, V->n, V->ncomp, V->d_inc_ptr, V->d_inc, d_work, d_out, accumulate);
+    prof_end(ctx, ev);
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
     const int order = A->space->order;
     const bool f32 = A->precision == FGPU_F32;

@@ -161,6 +161,7 @@ struct fgpu_mesh {
     std::vector<int32_t> h_tets;
     double* d_xyz = nullptr;
     int32_t* d_tets = nullptr;
+    double* d_ho = nullptr;          // curved (P2-geometry) elements: T x 6 x 3 edge nodes (e2p order), or null
     // element colouring (lazily built): elements sorted by colour
     int ncolours = 0;
     std::vector<int64_t> colour_ptr;
@@ -284,6 +285,11 @@ int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* ta
 int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec);
 int launch_assemble_elasticity_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);
+int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
+int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);
+int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate);
+int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate);
+int launch_rhs_ho(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate);
 int launch_face_matrix(fgpu_ctx* ctx, fgpu_matrix* A, int range, double xmax, double mass, double mass_h, double dn_trial,
                        double dn_test, int accumulate);
 int launch_face_load(fgpu_ctx* ctx, const fgpu_space* V, int range, double xmax, double g, double g_h, double g_dn,

@@ -1,0 +1,386 @@
+// Curved (P2-geometry) tetrahedra: the GEOMAP_HO path of the reference
+// (feelpp/feel/feelpoly/geomap.hpp: for a non-linear map the context
+// recomputes K = G grad(psi)^T, J and B = K^-T at every quadrature point,
+// :1014-1042, :2310-2350) for the scalar Laplace/mass form and the load vector.
+//
+// The map is x(xh) = sum_g X_g psi_g(xh) with the 10 P2 Lagrange functions
+// (vertices, then the edge nodes in e2p order). Element matrices by quadrature:
+//   K_e(i, j) = sum_q dphi_i(q)^T G_q dphi_j(q) + m_q phi_i(q) phi_j(q),
+//   G_q = w_q |det K_q| kappa B_q^T B_q,  m_q = w_q |det K_q| mass,
+// where dphi are reference gradients. One warp per element: the lanes first
+// take one quadrature point each and form G_q, m_q in binary64 (the map and
+// its inverse), stored in shared memory as double-float pairs; then for every
+// q the lanes form W_q = G_q dphi_j(q) for one local dof each, and each lane
+// adds dphi_i . W_j + m_q phi_i phi_j into the upper-triangle entries it owns
+// (double-float on the FP32 pipes for FP64 matrices, binary32 for FP32). The
+// element matrices go to the two-phase element buffer and the gather map sums
+// them per CSR entry in element order, as for affine elements.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "df64.h"
+#include "fgpu_core.h"
+
+namespace fgpu {
+
+namespace {
+
+enum HoMode { kHoF32 = 0, kHoDF64 = 1 };
+
+template <int N>
+struct HoLimits {
+    static constexpr int QMAX = N == 4 ? 14 : N == 10 ? 31 : 43;   // quadrature degree <= 5 / 7 / 8
+};
+
+struct HoTables {
+    int n = 0, Q = 0, ntri = 0;
+    float* d_dh = nullptr;     // Q n 3: reference gradients of the space's basis (df64 hi)
+    float* d_dl = nullptr;     //        (df64 lo)
+    float* d_ph = nullptr;     // Q n: basis values (df64 hi)
+    float* d_pl = nullptr;     //      (df64 lo)
+    double* d_phi = nullptr;   // Q n (binary64, load vector)
+    double* d_gd = nullptr;    // Q 10 3: reference gradients of the P2 geometric basis
+    double* d_gp = nullptr;    // Q 10: P2 geometric basis values
+    double* d_qw = nullptr;    // Q
+    uint8_t* d_ti = nullptr;   // ntri: row of each upper-triangle entry
+    uint8_t* d_tj = nullptr;   // ntri: column
+};
+
+std::mutex g_ho_mutex;
+std::map<std::tuple<int, int, int>, HoTables*> g_ho_tabs;
+
+template <typename T>
+cudaError_t up(T** dst, const std::vector<T>& v) {
+    cudaError_t e = cudaMalloc(dst, std::max<size_t>(v.size(), 1) * sizeof(T));
+    if (e == cudaSuccess && !v.empty()) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg) {
+    std::lock_guard<std::mutex> lock(g_ho_mutex);
+    const auto key = std::make_tuple(ctx->device, order, qdeg);
+    auto it = g_ho_tabs.find(key);
+    if (it != g_ho_tabs.end()) return it->second;
+    RefTables R, G;
+    std::string err;
+    if (!build_ref_tables(order, qdeg, R, err) || !build_ref_tables(2, qdeg, G, err)) { ctx->err = err; return nullptr; }
+    HoTables* T = new HoTables();
+    T->n = R.n;
+    T->Q = R.Q;
+    T->ntri = R.n * (R.n + 1) / 2;
+    std::vector<float> dh(R.dphi.size()), dl(R.dphi.size()), ph(R.phi.size()), pl(R.phi.size());
+    for (size_t k = 0; k < R.dphi.size(); ++k) {
+        dh[k] = (float)R.dphi[k];
+        dl[k] = (float)(R.dphi[k] - (double)dh[k]);
+    }
+    for (size_t k = 0; k < R.phi.size(); ++k) {
+        ph[k] = (float)R.phi[k];
+        pl[k] = (float)(R.phi[k] - (double)ph[k]);
+    }
+    std::vector<uint8_t> ti, tj;
+    for (int i = 0; i < R.n; ++i)
+        for (int j = i; j < R.n; ++j) {
+            ti.push_back((uint8_t)i);
+            tj.push_back((uint8_t)j);
+        }
+    cudaError_t e = up(&T->d_dh, dh);
+    if (e == cudaSuccess) e = up(&T->d_dl, dl);
+    if (e == cudaSuccess) e = up(&T->d_ph, ph);
+    if (e == cudaSuccess) e = up(&T->d_pl, pl);
+    if (e == cudaSuccess) e = up(&T->d_phi, R.phi);
+    if (e == cudaSuccess) e = up(&T->d_gd, G.dphi);
+    if (e == cudaSuccess) e = up(&T->d_gp, G.phi);
+    if (e == cudaSuccess) e = up(&T->d_qw, R.qw);
+    if (e == cudaSuccess) e = up(&T->d_ti, ti);
+    if (e == cudaSuccess) e = up(&T->d_tj, tj);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ctx->err = std::string("curved-element tables: ") + cudaGetErrorString(e);
+        delete T;
+        return nullptr;
+    }
+    g_ho_tabs[key] = T;
+    return T;
+}
+
+// K = sum_g X_g grad(psi_g)^T at one point, then |det K| and B = K^-T (cofactors / det)
+__device__ __forceinline__ double ho_map(const double* X /* 10 x 3 */, const double* gd /* 10 x 3 */, double B[9]) {
+    double K[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) K[k] = 0.0;
+    for (int g = 0; g < 10; ++g)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) K[3 * r + c] = fma(X[3 * g + r], gd[3 * g + c], K[3 * r + c]);
+    const double c00 = K[4] * K[8] - K[5] * K[7], c01 = K[5] * K[6] - K[3] * K[8], c02 = K[3] * K[7] - K[4] * K[6];
+    const double det = K[0] * c00 + K[1] * c01 + K[2] * c02;
+    const double cof[9] = {c00, c01, c02,
+                           K[2] * K[7] - K[1] * K[8], K[0] * K[8] - K[2] * K[6], K[1] * K[6] - K[0] * K[7],
+                           K[1] * K[5] - K[2] * K[4], K[2] * K[3] - K[0] * K[5], K[0] * K[4] - K[1] * K[3]};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B[k] = cof[k] / det;
+    return det;
+}
+
+__device__ __forceinline__ df ldf(const float* h, const float* l, int k) { return df{h[k], l[k]}; }
+__device__ __forceinline__ df dfun(float2 v) { return df{v.x, v.y}; }
+__device__ __forceinline__ float2 dfpack(df v) { return make_float2(v.hi, v.lo); }
+
+template <int MODE, int N>
+__global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                                         const double* __restrict__ ho, int Q, const float* __restrict__ Dhg,
+                                                         const float* __restrict__ Dlg, const float* __restrict__ Phg,
+                                                         const float* __restrict__ Plg, const double* __restrict__ gd,
+                                                         const double* __restrict__ qw, const uint8_t* __restrict__ tig,
+                                                         const uint8_t* __restrict__ tjg, const double* __restrict__ d_kappa,
+                                                         double kappa, double mass, const double* __restrict__ kscale,
+                                                         void* __restrict__ kbuf, int* __restrict__ status) {
+    constexpr int NTRI = N * (N + 1) / 2;
+    constexpr int QM = HoLimits<N>::QMAX;
+    constexpr int PER = (NTRI + 31) / 32;          // entries per lane
+    __shared__ float Dh[QM * N * 3], Dl[QM * N * 3], Ph[QM * N], Pl[QM * N];
+    __shared__ uint8_t ti[NTRI], tj[NTRI];
+    __shared__ float2 Gs[4][QM * 7];               // per warp: G_q (00, 11, 22, 01, 02, 12) and m_q
+    __shared__ float2 Ws[4][3 * N];                // per warp: W_q = G_q dphi_j
+    __shared__ double Xs[4][30];                   // per warp: the element's 10 nodes
+    for (int k = threadIdx.x; k < Q * N * 3; k += blockDim.x) { Dh[k] = Dhg[k]; Dl[k] = Dlg[k]; }
+    for (int k = threadIdx.x; k < Q * N; k += blockDim.x) { Ph[k] = Phg[k]; Pl[k] = Plg[k]; }
+    for (int k = threadIdx.x; k < NTRI; k += blockDim.x) { ti[k] = tig[k]; tj[k] = tjg[k]; }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const double ks = kscale ? *kscale : 1.0;
+    for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; e < nt; e += nw) {
+        // the element's nodes: 4 vertices, 6 edge nodes
+        if (lane < 12) {
+            const int v = lane / 3, r = lane % 3;
+            Xs[warp][lane] = xyz[3 * (int64_t)tets[4 * e + v] + r];
+        } else if (lane < 30) {
+            Xs[warp][lane] = ho[18 * e + (lane - 12)];
+        }
+        __syncwarp();
+        const double kap = (d_kappa ? d_kappa[e] : kappa) * ks;
+        // geometry: one quadrature point per lane, binary64
+        for (int q = lane; q < Q; q += 32) {
+            double B[9];
+            const double det = ho_map(Xs[warp], gd + (size_t)q * 30, B);
+            const double J = fabs(det);
+            if (!(J > 0.0) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+            const double wJ = qw[q] * J, s = wJ * kap;
+            double g[7];
+            g[0] = s * (B[0] * B[0] + B[3] * B[3] + B[6] * B[6]);
+            g[1] = s * (B[1] * B[1] + B[4] * B[4] + B[7] * B[7]);
+            g[2] = s * (B[2] * B[2] + B[5] * B[5] + B[8] * B[8]);
+            g[3] = s * (B[0] * B[1] + B[3] * B[4] + B[6] * B[7]);
+            g[4] = s * (B[0] * B[2] + B[3] * B[5] + B[6] * B[8]);
+            g[5] = s * (B[1] * B[2] + B[4] * B[5] + B[7] * B[8]);
+            g[6] = wJ * mass;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                const float hi = (float)g[k];
+                Gs[warp][q * 7 + k] = make_float2(hi, (float)(g[k] - (double)hi));
+            }
+        }
+        __syncwarp();
+        df acc[PER];
+        float accf[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) { acc[u] = df{0.0f, 0.0f}; accf[u] = 0.0f; }
+        for (int q = 0; q < Q; ++q) {
+            const float2* G = &Gs[warp][q * 7];
+            if (lane < N) {
+                const int b0 = (q * N + lane) * 3;
+                if (MODE == kHoDF64) {
+                    const df d0 = ldf(Dh, Dl, b0), d1 = ldf(Dh, Dl, b0 + 1), d2 = ldf(Dh, Dl, b0 + 2);
+                    const df g00 = dfun(G[0]), g11 = dfun(G[1]), g22 = dfun(G[2]), g01 = dfun(G[3]), g02 = dfun(G[4]), g12 = dfun(G[5]);
+                    const df w0 = df_add(df_add(df_mul(g00, d0), df_mul(g01, d1)), df_mul(g02, d2));
+                    const df w1 = df_add(df_add(df_mul(g01, d0), df_mul(g11, d1)), df_mul(g12, d2));
+                    const df w2 = df_add(df_add(df_mul(g02, d0), df_mul(g12, d1)), df_mul(g22, d2));
+                    Ws[warp][lane] = dfpack(w0);
+                    Ws[warp][N + lane] = dfpack(w1);
+                    Ws[warp][2 * N + lane] = dfpack(w2);
+                } else {
+                    const float d0 = Dh[b0], d1 = Dh[b0 + 1], d2 = Dh[b0 + 2];
+                    Ws[warp][lane] = make_float2(fmaf(G[0].x, d0, fmaf(G[3].x, d1, G[4].x * d2)), 0.0f);
+                    Ws[warp][N + lane] = make_float2(fmaf(G[3].x, d0, fmaf(G[1].x, d1, G[5].x * d2)), 0.0f);
+                    Ws[warp][2 * N + lane] = make_float2(fmaf(G[4].x, d0, fmaf(G[5].x, d1, G[2].x * d2)), 0.0f);
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int t = lane + 32 * u;
+                if (t >= NTRI) break;
+                const int i = ti[t], j = tj[t];
+                const int bi = (q * N + i) * 3;
+                if (MODE == kHoDF64) {
+                    df v = df_mul(ldf(Dh, Dl, bi), dfun(Ws[warp][j]));
+                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 1), dfun(Ws[warp][N + j])));
+                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 2), dfun(Ws[warp][2 * N + j])));
+                    v = df_add(v, df_mul(dfun(G[6]), df_mul(ldf(Ph, Pl, q * N + i), ldf(Ph, Pl, q * N + j))));
+                    acc[u] = df_add(acc[u], v);
+                } else {
+                    float v = Dh[bi] * Ws[warp][j].x;
+                    v = fmaf(Dh[bi + 1], Ws[warp][N + j].x, v);
+                    v = fmaf(Dh[bi + 2], Ws[warp][2 * N + j].x, v);
+                    v = fmaf(G[6].x, Ph[q * N + i] * Ph[q * N + j], v);
+                    accf[u] += v;
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = lane + 32 * u;
+            if (t >= NTRI) break;
+            if (MODE == kHoDF64) reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = dfpack(acc[u]);
+            else reinterpret_cast<float*>(kbuf)[e * NTRI + t] = accf[u];
+        }
+        __syncwarp();
+    }
+}
+
+// load vector on curved elements: thread per element, per point the map, J and the physical point
+template <int N>
+__global__ void ho_rhs_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                              const double* __restrict__ ho, int Q, const double* __restrict__ qw, const double* __restrict__ phi,
+                              const double* __restrict__ gd, const double* __restrict__ gp, int fkind, double f0,
+                              double* __restrict__ work, int* __restrict__ status) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+        double X[30];
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) X[3 * v + r] = xyz[3 * (int64_t)tets[4 * e + v] + r];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) X[12 + k] = ho[18 * e + k];
+        double F[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) F[i] = 0.0;
+        for (int q = 0; q < Q; ++q) {
+            double B[9];
+            const double J = fabs(ho_map(X, gd + (size_t)q * 30, B));
+            if (!(J > 0.0) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+            double f = f0;
+            if (fkind == FGPU_RHS_SINE) {
+                double p[3] = {0.0, 0.0, 0.0};
+                for (int g = 0; g < 10; ++g)
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) p[r] = fma(X[3 * g + r], gp[q * 10 + g], p[r]);
+                const double pi = 3.141592653589793;
+                f = 3.0 * pi * pi * sin(pi * p[0]) * sin(pi * p[1]) * sin(pi * p[2]);
+            }
+            const double s = qw[q] * J * f;
+#pragma unroll
+            for (int i = 0; i < N; ++i) F[i] = fma(s, phi[q * N + i], F[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) work[e * N + i] = F[i];
+    }
+}
+
+int ho_qdeg_ok(fgpu_ctx* ctx, int order, int qdeg) {
+    const int lim = order == 1 ? 5 : order == 2 ? 7 : 8;
+    if (qdeg > lim) {
+        ctx->err = "curved elements: quadrature degree above " + std::to_string(lim) + " for this order";
+        return FGPU_ERR_INVALID;
+    }
+    return FGPU_OK;
+}
+
+}  // namespace
+
+int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
+    fgpu_space* V = A->space;
+    const fgpu_mesh* M = V->mesh;
+    if (f->kind != FGPU_FORM_LAPLACE_MASS || V->ncomp != 1) {
+        ctx->err = "curved elements: scalar Laplace/mass forms only";
+        return FGPU_ERR_INVALID;
+    }
+    const int qdeg = f->quad_degree > 0 ? f->quad_degree : std::min(2 * V->order + 2, 8);
+    int rc = ho_qdeg_ok(ctx, V->order, qdeg);
+    if (rc) return rc;
+    HoTables* T = get_ho_tables(ctx, V->order, qdeg);
+    if (!T) return FGPU_ERR_INVALID;
+    const bool f32 = A->precision == FGPU_F32;
+    rc = ensure_two_phase(ctx, A, (size_t)M->nt * T->ntri * (f32 ? 4 : 8));
+    if (rc) return rc;
+    const int64_t warps = M->nt;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4, 152 * 32));
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_elements_ho", ev);
+#define HO_LAUNCH(MODE, NN)                                                                                                   \
+    ho_element_kernel<MODE, NN><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_dh, T->d_dl,  \
+                                                                T->d_ph, T->d_pl, T->d_gd, T->d_qw, T->d_ti, T->d_tj, d_kappa, \
+                                                                f->kappa, f->mass, f->kappa_scale, A->d_kbuf, ctx->d_status)
+    switch (V->n) {
+        case 4: if (f32) HO_LAUNCH(kHoF32, 4); else HO_LAUNCH(kHoDF64, 4); break;
+        case 10: if (f32) HO_LAUNCH(kHoF32, 10); else HO_LAUNCH(kHoDF64, 10); break;
+        default: if (f32) HO_LAUNCH(kHoF32, 20); else HO_LAUNCH(kHoDF64, 20); break;
+    }
+#undef HO_LAUNCH
+    prof_end(ctx, ev);
+    ctx->launches++;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    rc = launch_gather_phase(ctx, A, accumulate);
+    ctx->launches++;
+    return rc;
+}
+
+int launch_rhs_ho(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate) {
+    const fgpu_mesh* M = V->mesh;
+    if (V->ncomp != 1 || (rhs->kind != FGPU_RHS_SINE && rhs->kind != FGPU_RHS_CONST)) {
+        ctx->err = "curved elements: scalar sine or constant sources only";
+        return FGPU_ERR_INVALID;
+    }
+    const int qdeg = rhs->quad_degree > 0 ? rhs->quad_degree : std::min(2 * V->order + 2, 8);
+    int rc = ho_qdeg_ok(ctx, V->order, qdeg);
+    if (rc) return rc;
+    HoTables* T = get_ho_tables(ctx, V->order, qdeg);
+    if (!T) return FGPU_ERR_INVALID;
+    double* work = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&work, std::max<int64_t>(M->nt * V->n, 1) * sizeof(double)));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + 127) / 128, 152 * 32));
+    PendingEvent ev;
+    prof_begin(ctx, "rhs_element_ho", ev);
+    switch (V->n) {
+        case 4: ho_rhs_kernel<4><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
+        case 10: ho_rhs_kernel<10><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
+        default: ho_rhs_kernel<20><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
+    }
+    prof_end(ctx, ev);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) rc = launch_rhs_gather(ctx, V, work, d_out, accumulate);
+    ctx->launches++;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(work);
+    if (e != cudaSuccess) { ctx->err = std::string("curved load vector: ") + cudaGetErrorString(e); return FGPU_ERR_CUDA; }
+    return rc;
+}
+
+}  // namespace fgpu
+
+using namespace fgpu;
+
+extern "C" int fgpu_mesh_set_ho_nodes(fgpu_mesh* M, const double* ho) {
+    if (!M) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = M->ctx;
+    if (ctx->capturing) { ctx->err = "mesh_set_ho_nodes: not capturable"; return FGPU_ERR_INVALID; }
+    if (!ho) {
+        cudaFree(M->d_ho);
+        M->d_ho = nullptr;
+        return FGPU_OK;
+    }
+    const size_t bytes = (size_t)M->nt * 18 * sizeof(double);
+    if (!M->d_ho) FGPU_CUDA_CHECK(ctx, cudaMalloc(&M->d_ho, std::max<size_t>(bytes, 8)));
+    FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(M->d_ho, ho, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    return FGPU_OK;
+}

@@ -833,6 +833,7 @@ extern "C" int fgpu_operator_create(fgpu_ctx* ctx, fgpu_space* V, const fgpu_for
     if (!ctx || !V || !f || !out) return FGPU_ERR_INVALID;
     if (f->kind != FGPU_FORM_LAPLACE_MASS || V->ncomp != 1) { ctx->err = "matrix-free operators support the scalar Laplace/mass form"; return FGPU_ERR_INVALID; }
     if (precision != FGPU_F32 && precision != FGPU_F64 && precision != FGPU_DF64) { ctx->err = "bad operator precision"; return FGPU_ERR_INVALID; }
+    if (V->mesh->d_ho) { ctx->err = "matrix-free operators: affine elements only"; return FGPU_ERR_INVALID; }
     *out = nullptr;
     std::string err;
     DevTables* tab = get_dev_tables(V->order, f->quad_degree > 0 ? f->quad_degree : 2 * V->order, err);

@@ -101,6 +101,7 @@ extern "C" int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_
     if (!V || !rhs || !d_out) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = V->ctx;
     if (rhs->range != FGPU_RANGE_ELEMENTS) { ctx->err = "noalloc: element integrals only"; return FGPU_ERR_INVALID; }
+    if (V->mesh->d_ho) { ctx->err = "noalloc: affine elements only"; return FGPU_ERR_INVALID; }
     const int qdeg = rhs->quad_degree > 0 ? rhs->quad_degree : 2 * V->order;
     if (qdeg < 1 || qdeg > kMaxTetRuleDegree) { ctx->err = "noalloc: quadrature degree must be in [1, 8]"; return FGPU_ERR_INVALID; }
     const int64_t need = V->mesh->nt * (int64_t)V->n * V->ncomp;

@@ -89,9 +89,11 @@ def _ptr(a):
 
 
 class Mesh:
-    """Tetrahedral mesh: vertex coordinates (V x 3) and elements (T x 4) in insertion order."""
+    """Tetrahedral mesh: vertex coordinates (V x 3) and elements (T x 4) in insertion order; with `ho`
+    (T x 6 x 3 edge nodes, local edge order (1,2) (2,0) (0,1) (0,3) (1,3) (2,3)) the elements are curved
+    (P2 geometry, as a gmsh order-2 mesh read with GEOMAP_HO)."""
 
-    def __init__(self, xyz, tets, env=None):
+    def __init__(self, xyz, tets, env=None, ho=None):
         self.env = env or environment()
         self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         self.tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -99,6 +101,18 @@ class Mesh:
         self.env.check(self.env.lib.fgpu_mesh_upload(self.env.h, len(self.xyz), _ptr(self.xyz), len(self.tets),
                                                      _ptr(self.tets), C.byref(h)))
         self.h = h
+        self.ho = None
+        if ho is not None:
+            self.set_ho_nodes(ho)
+
+    def set_ho_nodes(self, ho):
+        """Curved elements from their edge nodes (None: affine again)."""
+        if ho is None:
+            self.ho = None
+            self.env.check(self.env.lib.fgpu_mesh_set_ho_nodes(self.h, None))
+            return
+        self.ho = np.ascontiguousarray(ho, dtype=np.float64).reshape(len(self.tets), 6, 3)
+        self.env.check(self.env.lib.fgpu_mesh_set_ho_nodes(self.h, _ptr(self.ho)))
 
     @property
     def num_elements(self):

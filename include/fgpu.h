@@ -183,6 +183,12 @@ int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, c
                      fgpu_mesh** out);
 /* replace the vertex coordinates (host array, nv x 3): a moved mesh keeps its topology */
 int fgpu_mesh_set_coords(fgpu_mesh* mesh, const double* xyz);
+/* curved (P2-geometry, GEOMAP_HO) elements: ho = T x 6 x 3 coordinates of each element's edge nodes in
+ * the local edge order (1,2) (2,0) (0,1) (0,3) (1,3) (2,3) (host array, copied); NULL makes the mesh
+ * affine again. On a curved mesh the scalar Laplace/mass form and the sine / constant load vector are
+ * integrated with per-point maps (quadrature degree <= 5 / 7 / 8 for P1 / P2 / P3, default 2p + 2);
+ * face integrals, elasticity, matrix-free operators, batches and error norms refuse. */
+int fgpu_mesh_set_ho_nodes(fgpu_mesh* mesh, const double* ho);
 int fgpu_mesh_destroy(fgpu_mesh* mesh);
 
 /* ---- function space Pch<order> (ncomp = 1) / Pchv<order> (ncomp = 3)
