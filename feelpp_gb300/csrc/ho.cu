@@ -8,8 +8,10 @@
 //   K_e(i, j) = sum_q dphi_i(q)^T G_q dphi_j(q) + m_q phi_i(q) phi_j(q),
 //   G_q = w_q |det K_q| kappa B_q^T B_q,  m_q = w_q |det K_q| mass,
 // where dphi are reference gradients. One warp per element: the lanes first
-// take one quadrature point each and form G_q, m_q in binary64 (the map and
-// its inverse), stored in shared memory as double-float pairs; then for every
+// take one quadrature point each and form G_q, m_q (the map, its cofactors,
+// determinant and inverse) in double-float on the FP32 pipes (binary64 runs at
+// 1/71 of the binary32 rate here; binary32 for FP32 matrices), stored in shared
+// memory; then for every
 // q the lanes form W_q = G_q dphi_j(q) for one local dof each, and each lane
 // adds dphi_i . W_j + m_q phi_i phi_j into the upper-triangle entries it owns
 // (double-float on the FP32 pipes for FP64 matrices, binary32 for FP32). The
@@ -47,6 +49,10 @@ struct HoTables {
     double* d_gd = nullptr;    // Q 10 3: reference gradients of the P2 geometric basis
     double* d_gp = nullptr;    // Q 10: P2 geometric basis values
     double* d_qw = nullptr;    // Q
+    float* d_gdh = nullptr;    // Q 10 3: d_gd as double-float (hi)
+    float* d_gdl = nullptr;    //                               (lo)
+    float* d_qwh = nullptr;    // Q: weights as double-float (hi)
+    float* d_qwl = nullptr;    //                            (lo)
     uint8_t* d_ti = nullptr;   // ntri: row of each upper-triangle entry
     uint8_t* d_tj = nullptr;   // ntri: column
 };
@@ -82,6 +88,15 @@ HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg) {
         ph[k] = (float)R.phi[k];
         pl[k] = (float)(R.phi[k] - (double)ph[k]);
     }
+    std::vector<float> gdh(G.dphi.size()), gdl(G.dphi.size()), qwh(R.qw.size()), qwl(R.qw.size());
+    for (size_t k = 0; k < G.dphi.size(); ++k) {
+        gdh[k] = (float)G.dphi[k];
+        gdl[k] = (float)(G.dphi[k] - (double)gdh[k]);
+    }
+    for (size_t k = 0; k < R.qw.size(); ++k) {
+        qwh[k] = (float)R.qw[k];
+        qwl[k] = (float)(R.qw[k] - (double)qwh[k]);
+    }
     std::vector<uint8_t> ti, tj;
     for (int i = 0; i < R.n; ++i)
         for (int j = i; j < R.n; ++j) {
@@ -96,6 +111,10 @@ HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg) {
     if (e == cudaSuccess) e = up(&T->d_gd, G.dphi);
     if (e == cudaSuccess) e = up(&T->d_gp, G.phi);
     if (e == cudaSuccess) e = up(&T->d_qw, R.qw);
+    if (e == cudaSuccess) e = up(&T->d_gdh, gdh);
+    if (e == cudaSuccess) e = up(&T->d_gdl, gdl);
+    if (e == cudaSuccess) e = up(&T->d_qwh, qwh);
+    if (e == cudaSuccess) e = up(&T->d_qwl, qwl);
     if (e == cudaSuccess) e = up(&T->d_ti, ti);
     if (e == cudaSuccess) e = up(&T->d_tj, tj);
     if (e != cudaSuccess) {
@@ -136,8 +155,9 @@ template <int MODE, int N>
 __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
                                                          const double* __restrict__ ho, int Q, const float* __restrict__ Dhg,
                                                          const float* __restrict__ Dlg, const float* __restrict__ Phg,
-                                                         const float* __restrict__ Plg, const double* __restrict__ gd,
-                                                         const double* __restrict__ qw, const uint8_t* __restrict__ tig,
+                                                         const float* __restrict__ Plg, const float* __restrict__ gdh,
+                                                         const float* __restrict__ gdl, const float* __restrict__ qwh,
+                                                         const float* __restrict__ qwl, const uint8_t* __restrict__ tig,
                                                          const uint8_t* __restrict__ tjg, const double* __restrict__ d_kappa,
                                                          double kappa, double mass, const double* __restrict__ kscale,
                                                          void* __restrict__ kbuf, int* __restrict__ status) {
@@ -148,44 +168,102 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
     __shared__ uint8_t ti[NTRI], tj[NTRI];
     __shared__ float2 Gs[4][QM * 7];               // per warp: G_q (00, 11, 22, 01, 02, 12) and m_q
     __shared__ float2 Ws[4][3 * N];                // per warp: W_q = G_q dphi_j
-    __shared__ double Xs[4][30];                   // per warp: the element's 10 nodes
+    __shared__ float2 Xs[4][30];                   // per warp: the element's 10 nodes (double-float)
     for (int k = threadIdx.x; k < Q * N * 3; k += blockDim.x) { Dh[k] = Dhg[k]; Dl[k] = Dlg[k]; }
     for (int k = threadIdx.x; k < Q * N; k += blockDim.x) { Ph[k] = Phg[k]; Pl[k] = Plg[k]; }
     for (int k = threadIdx.x; k < NTRI; k += blockDim.x) { ti[k] = tig[k]; tj[k] = tjg[k]; }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const double ks = kscale ? *kscale : 1.0;
+    const df ksd = d2df(kscale ? *kscale : 1.0), massd = d2df(mass);
     for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; e < nt; e += nw) {
         // the element's nodes: 4 vertices, 6 edge nodes
         if (lane < 12) {
             const int v = lane / 3, r = lane % 3;
-            Xs[warp][lane] = xyz[3 * (int64_t)tets[4 * e + v] + r];
+            Xs[warp][lane] = dfpack(d2df(xyz[3 * (int64_t)tets[4 * e + v] + r]));
         } else if (lane < 30) {
-            Xs[warp][lane] = ho[18 * e + (lane - 12)];
+            Xs[warp][lane] = dfpack(d2df(ho[18 * e + (lane - 12)]));
         }
         __syncwarp();
-        const double kap = (d_kappa ? d_kappa[e] : kappa) * ks;
-        // geometry: one quadrature point per lane, binary64
+        const df kap = df_mul(d2df(d_kappa ? d_kappa[e] : kappa), ksd);
+        // geometry: one quadrature point per lane; double-float on the FP32 pipes (binary32 for FP32
+        // matrices): K = sum_g X_g grad(psi_g)^T, cofactors, det, B = cof / det, G = w J kappa B^T B
         for (int q = lane; q < Q; q += 32) {
-            double B[9];
-            const double det = ho_map(Xs[warp], gd + (size_t)q * 30, B);
-            const double J = fabs(det);
-            if (!(J > 0.0) || !isfinite(J)) atomicOr(status, kStatusBadElement);
-            const double wJ = qw[q] * J, s = wJ * kap;
-            double g[7];
-            g[0] = s * (B[0] * B[0] + B[3] * B[3] + B[6] * B[6]);
-            g[1] = s * (B[1] * B[1] + B[4] * B[4] + B[7] * B[7]);
-            g[2] = s * (B[2] * B[2] + B[5] * B[5] + B[8] * B[8]);
-            g[3] = s * (B[0] * B[1] + B[3] * B[4] + B[6] * B[7]);
-            g[4] = s * (B[0] * B[2] + B[3] * B[5] + B[6] * B[8]);
-            g[5] = s * (B[1] * B[2] + B[4] * B[5] + B[7] * B[8]);
-            g[6] = wJ * mass;
+            const float* gh = gdh + (size_t)q * 30;
+            const float* gl = gdl + (size_t)q * 30;
+            float2 g[7];
+            if (MODE == kHoDF64) {
+                df K[9];
 #pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                const float hi = (float)g[k];
-                Gs[warp][q * 7 + k] = make_float2(hi, (float)(g[k] - (double)hi));
+                for (int k = 0; k < 9; ++k) K[k] = df{0.0f, 0.0f};
+                for (int gg = 0; gg < 10; ++gg) {
+                    const df d0 = df{__ldg(gh + 3 * gg), __ldg(gl + 3 * gg)};
+                    const df d1 = df{__ldg(gh + 3 * gg + 1), __ldg(gl + 3 * gg + 1)};
+                    const df d2 = df{__ldg(gh + 3 * gg + 2), __ldg(gl + 3 * gg + 2)};
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        const df x = dfun(Xs[warp][3 * gg + r]);
+                        K[3 * r] = df_add(K[3 * r], df_mul(x, d0));
+                        K[3 * r + 1] = df_add(K[3 * r + 1], df_mul(x, d1));
+                        K[3 * r + 2] = df_add(K[3 * r + 2], df_mul(x, d2));
+                    }
+                }
+                df C[9];
+                C[0] = df_sub(df_mul(K[4], K[8]), df_mul(K[5], K[7]));
+                C[1] = df_sub(df_mul(K[5], K[6]), df_mul(K[3], K[8]));
+                C[2] = df_sub(df_mul(K[3], K[7]), df_mul(K[4], K[6]));
+                C[3] = df_sub(df_mul(K[2], K[7]), df_mul(K[1], K[8]));
+                C[4] = df_sub(df_mul(K[0], K[8]), df_mul(K[2], K[6]));
+                C[5] = df_sub(df_mul(K[1], K[6]), df_mul(K[0], K[7]));
+                C[6] = df_sub(df_mul(K[1], K[5]), df_mul(K[2], K[4]));
+                C[7] = df_sub(df_mul(K[2], K[3]), df_mul(K[0], K[5]));
+                C[8] = df_sub(df_mul(K[0], K[4]), df_mul(K[1], K[3]));
+                const df det = df_add(df_add(df_mul(K[0], C[0]), df_mul(K[1], C[1])), df_mul(K[2], C[2]));
+                const df J = det.hi < 0.0f ? df_neg(det) : det;
+                if (!(J.hi > 0.0f) || !isfinite(J.hi)) atomicOr(status, kStatusBadElement);
+                const df inv = df_recip(det);
+                df B[9];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) B[k] = df_mul(C[k], inv);
+                const df wJ = df_mul(df{qwh[q], qwl[q]}, J), sc = df_mul(wJ, kap);
+                const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    df t = df_mul(B[pa[k]], B[pb[k]]);
+                    t = df_add(t, df_mul(B[3 + pa[k]], B[3 + pb[k]]));
+                    t = df_add(t, df_mul(B[6 + pa[k]], B[6 + pb[k]]));
+                    g[k] = dfpack(df_mul(sc, t));
+                }
+                g[6] = dfpack(df_mul(wJ, massd));
+            } else {
+                float K[9];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) K[k] = 0.0f;
+                for (int gg = 0; gg < 10; ++gg)
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        const float x = Xs[warp][3 * gg + r].x + Xs[warp][3 * gg + r].y;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) K[3 * r + c] = fmaf(x, __ldg(gh + 3 * gg + c), K[3 * r + c]);
+                    }
+                const float C[9] = {K[4] * K[8] - K[5] * K[7], K[5] * K[6] - K[3] * K[8], K[3] * K[7] - K[4] * K[6],
+                                    K[2] * K[7] - K[1] * K[8], K[0] * K[8] - K[2] * K[6], K[1] * K[6] - K[0] * K[7],
+                                    K[1] * K[5] - K[2] * K[4], K[2] * K[3] - K[0] * K[5], K[0] * K[4] - K[1] * K[3]};
+                const float det = K[0] * C[0] + K[1] * C[1] + K[2] * C[2];
+                const float J = fabsf(det);
+                if (!(J > 0.0f) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+                float B[9];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) B[k] = C[k] / det;
+                const float wJ = qwh[q] * J, sc = wJ * (kap.hi + kap.lo);
+                const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                for (int k = 0; k < 6; ++k)
+                    g[k] = make_float2(sc * (B[pa[k]] * B[pb[k]] + B[3 + pa[k]] * B[3 + pb[k]] + B[6 + pa[k]] * B[6 + pb[k]]), 0.0f);
+                g[6] = make_float2(wJ * (massd.hi + massd.lo), 0.0f);
             }
+#pragma unroll
+            for (int k = 0; k < 7; ++k) Gs[warp][q * 7 + k] = g[k];
         }
         __syncwarp();
         df acc[PER];
@@ -317,7 +395,8 @@ int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, c
     prof_begin(ctx, "assemble_elements_ho", ev);
 #define HO_LAUNCH(MODE, NN)                                                                                                   \
     ho_element_kernel<MODE, NN><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_dh, T->d_dl,  \
-                                                                T->d_ph, T->d_pl, T->d_gd, T->d_qw, T->d_ti, T->d_tj, d_kappa, \
+                                                                T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh, T->d_qwl,      \
+                                                                T->d_ti, T->d_tj, d_kappa,                                     \
                                                                 f->kappa, f->mass, f->kappa_scale, A->d_kbuf, ctx->d_status)
     switch (V->n) {
         case 4: if (f32) HO_LAUNCH(kHoF32, 4); else HO_LAUNCH(kHoDF64, 4); break;
