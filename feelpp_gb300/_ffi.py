@@ -16,7 +16,7 @@ RANGE_ELEMENTS, RANGE_BOUNDARY_FACES, RANGE_MARKED_FACES = 0, 1, 2
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE = 0, 1, 2, 3, 4
 RHS_SINE, RHS_CONST_VEC, RHS_CONST, RHS_FACE = 0, 1, 2, 3
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
-PC_NONE, PC_JACOBI, PC_CHEB_JACOBI, PC_GAMG = 0, 1, 2, 3
+PC_NONE, PC_JACOBI, PC_CHEB_JACOBI, PC_GAMG, PC_PMG = 0, 1, 2, 3, 4
 ARITH_F64, ARITH_DF64 = 0, 1
 
 ERROR_NAMES = {1: "FGPU_ERR_INVALID", 2: "FGPU_ERR_CUDA", 3: "FGPU_ERR_BAD_ELEMENT", 4: "FGPU_ERR_OUT_OF_RANGE",
@@ -55,6 +55,10 @@ class SolverCfg(C.Structure):
 class AmgCfg(C.Structure):
     _fields_ = [("threshold", C.c_double), ("max_levels", C.c_int), ("coarse_eq_lim", C.c_int), ("agg_smooths", C.c_int),
                 ("smoother_degree", C.c_int)]
+
+
+class PmgCfg(C.Structure):
+    _fields_ = [("smoother_degree", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -108,6 +112,10 @@ SIGNATURES = {
     "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),
     "fgpu_amg_destroy": (i32, [P]),
     "fgpu_mesh_set_ho_nodes": (i32, [P, P]),
+    "fgpu_pmg_create": (i32, [P, P, P, P, C.POINTER(PmgCfg), PP]),
+    "fgpu_pmg_info": (i32, [P, DP, P, DP]),
+    "fgpu_pmg_destroy": (i32, [P]),
+    "fgpu_solve_cg_operator_pmg": (i32, [P, P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
     "fgpu_solve_cg_amg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
     "fgpu_amg_host_build": (i32, [i64, P, P, P, C.POINTER(AmgCfg), i32, PP]),
     "fgpu_amg_host_levels": (i32, [P]),

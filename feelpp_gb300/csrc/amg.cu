@@ -351,6 +351,14 @@ int amg_vcycle(fgpu_amg* M, const T* r, const int* stop) {
 }
 
 template int amg_vcycle<double>(fgpu_amg*, const double*, const int*);
+
+int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x) {
+    const int nl = amg_vcycle<float>(M, r, stop);
+    *x = M->L[0].x;
+    return nl;
+}
+
+int64_t amg_rows(const fgpu_amg* M) { return M->L.empty() ? 0 : M->L[0].n; }
 template int amg_vcycle<float2>(fgpu_amg*, const float2*, const int*);
 template int amg_vcycle<float>(fgpu_amg*, const float*, const int*);
 

@@ -375,4 +375,8 @@ static int cg_run(fgpu_ctx* ctx, int64_t n, const CgOperator<PL>& A, const typen
 template <class PL>
 PcHook<PL> amg_pc_hook(fgpu_amg* M);
 
+// the p-multigrid V-cycle of a matrix-free operator as a CG preconditioner (pmg.cu)
+template <class PL>
+PcHook<PL> pmg_pc_hook(fgpu_pmg* P);
+
 }  // namespace fgpu

@@ -285,6 +285,14 @@ int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* ta
 int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec);
 int launch_assemble_elasticity_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);
+int mf_apply_f32_gated(fgpu_ctx* ctx, fgpu_operator* op, const float* x, float* y, const int* stop);
+int64_t operator_nnodes(const fgpu_operator* op);
+int operator_precision(const fgpu_operator* op);
+const fgpu_space* operator_space(const fgpu_operator* op);
+const uint8_t* operator_mask(const fgpu_operator* op);
+const float* operator_diag_f32(fgpu_ctx* ctx, fgpu_operator* op);
+int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x);
+int64_t amg_rows(const fgpu_amg* M);
 int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
 int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);
 int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate);

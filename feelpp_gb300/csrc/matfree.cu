@@ -212,6 +212,34 @@ __global__ void mf_gather_kernel(int64_t nnodes, int64_t nt, const int64_t* __re
     }
 }
 
+// binary32 node gather that returns at once when *stop is set (used inside captured graphs)
+__global__ void mf_gather_f32_stop_kernel(int64_t nnodes, int64_t nt, const int64_t* __restrict__ inc_ptr,
+                                          const int32_t* __restrict__ inc, const float* __restrict__ ye,
+                                          const float* __restrict__ x, const uint8_t* __restrict__ mask, float* __restrict__ y,
+                                          const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        if (mask && mask[m]) {
+            y[m] = x[m];
+            continue;
+        }
+        float s = 0.0f;
+        const int64_t t0 = inc_ptr[m], t1 = inc_ptr[m + 1];
+        for (int64_t t = t0; t < t1; t += 4) {
+            int32_t code[4];
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) code[u] = t + u < t1 ? __ldg(inc + t + u) : 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = t + u < t1 ? __ldg(ye + (int64_t)(code[u] & 31) * nt + (code[u] >> 5)) : 0.0f;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (t + u < t1) s += v[u];
+        }
+        y[m] = s;
+    }
+}
+
 // df64 summation of binary64 element values (keeps ~48 bits in the node sum)
 __global__ void mf_gather_df_kernel(int64_t nnodes, int64_t nt, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                     const double* __restrict__ ye, const double* __restrict__ x, const uint8_t* __restrict__ mask,
@@ -613,13 +641,53 @@ static int mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* x
     return nl;
 }
 
+// y = A x for a binary32 operator with every kernel gated by *stop (for preconditioners that apply
+// the operator inside the CG graph); returns the number of kernels launched
+int mf_apply_f32_gated(fgpu_ctx* ctx, fgpu_operator* op, const float* x, float* y, const int* stop) {
+    const fgpu_space* V = op->space;
+    const int n = V->n;
+    if (op->algo == FGPU_ALGO_COLOUR) return mf_apply_colour_f32(ctx, op, x, y, stop);
+    int nl = 2;
+    const float* xe = x;
+    const uint8_t* me = op->d_mask;
+    if (op->d_mask && op->d_xm) {
+        mask_copy_f32_kernel<<<blocks_for(op->nnodes, 256, 152 * 8), 256, 0, ctx->stream>>>(op->nnodes, x, op->d_mask, op->d_xm, stop);
+        ++nl;
+        xe = op->d_xm;
+        me = nullptr;
+    }
+    const int eb = blocks_for(op->nt, 128, 152 * 16);
+    if (op->use_tc && (n == 10 || n == 20)) {
+        launch_mf_element_tc(ctx, n, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop);
+    } else {
+        switch (n) {
+            case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+            case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+            default: mf_element_f32_gated<20><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+        }
+    }
+    mf_gather_f32_stop_kernel<<<blocks_for(op->nnodes, 256, 152 * 16), 256, 0, ctx->stream>>>(
+        op->nnodes, op->nt, V->d_inc_ptr, V->d_inc, (const float*)op->d_ye, x, op->d_mask, y, stop);
+    return nl;
+}
+
+int64_t operator_nnodes(const fgpu_operator* op) { return op->nnodes; }
+int operator_precision(const fgpu_operator* op) { return op->precision; }
+const fgpu_space* operator_space(const fgpu_operator* op) { return op->space; }
+const uint8_t* operator_mask(const fgpu_operator* op) { return op->d_mask; }
+const float* operator_diag_f32(fgpu_ctx* ctx, fgpu_operator* op) {
+    if (op->precision != FGPU_F32) return nullptr;
+    if (!op->d_diag && operator_diagonal(ctx, op) != FGPU_OK) return nullptr;
+    return (const float*)op->d_diag;
+}
+
 // Matrix-free PCG with Jacobi or Chebyshev-Jacobi (operator diagonal). The
 // binary32 operator's iterations run from a captured graph like the CSR
 // solver; the binary64 ones launch per iteration (their element phase is
 // long, launch overhead is noise, and it is not gated by the stop flag).
 template <class PL>
 static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b, typename PL::S* x, const CgOptions& o, int pc,
-                       CgResult* res, const RefreshFn<PL>* refresh = nullptr) {
+                       CgResult* res, const RefreshFn<PL>* refresh = nullptr, fgpu_pmg* pmg = nullptr) {
     typedef typename PL::S S;
     const int64_t n = op->nnodes;
     const int vb = vec_blocks(n);
@@ -641,7 +709,9 @@ static int mf_pcg_core(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* b
         A.launches = (op->precision == FGPU_F32 && op->d_mask && op->d_xm) ? 3 : 2;
     }
     A.graph = op->precision == FGPU_F32;
-    const int rc = cg_run<PL>(ctx, n, A, dinv, b, x, o, res, refresh);
+    PcHook<PL> hook;
+    if (pmg) hook = pmg_pc_hook<PL>(pmg);
+    const int rc = cg_run<PL>(ctx, n, A, dinv, b, x, o, res, refresh, pmg ? &hook : nullptr);
     cudaFree(dinv);
     return rc;
 }
@@ -674,7 +744,7 @@ static int mf_residual64(fgpu_ctx* ctx, fgpu_operator* op, const double* b, cons
 // binary64 PCG with residual replacement at each convergence claim of the
 // recurrence (q: scratch vector of n doubles)
 static int mf_plain_solve(fgpu_ctx* ctx, fgpu_operator* op, const double* d_b, double* d_x, CgOptions o,
-                          const fgpu_solver_cfg* cfg, double bn, double* q, CgResult* res) {
+                          const fgpu_solver_cfg* cfg, double bn, double* q, CgResult* res, fgpu_pmg* pmg = nullptr) {
     o.delta = 0.0;
     int stagnant = 0;
     double rlast = 0;
@@ -688,11 +758,11 @@ static int mf_plain_solve(fgpu_ctx* ctx, fgpu_operator* op, const double* d_b, d
         if (!*conv && stagnant >= 2) return kRefreshStagnated;
         return FGPU_OK;
     };
-    return mf_pcg_core<PolF64>(ctx, op, d_b, d_x, o, cfg->pc, res, &refresh);
+    return mf_pcg_core<PolF64>(ctx, op, d_b, d_x, o, cfg->pc, res, &refresh, pmg);
 }
 
 int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const double* d_b, double* d_x,
-                      const fgpu_solver_cfg* cfg, fgpu_solve_stats* st) {
+                      const fgpu_solver_cfg* cfg, fgpu_solve_stats* st, fgpu_pmg* pmg) {
     const int64_t n = op->nnodes;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -714,7 +784,7 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
     if (!cfg->mixed) {
         if (op->precision == FGPU_F32) { ctx->err = "the plain matrix-free solve needs a binary64 operator"; rc = FGPU_ERR_INVALID; }
         else {
-            rc = mf_plain_solve(ctx, op, d_b, d_x, opt, cfg, bn, q, &res);
+            rc = mf_plain_solve(ctx, op, d_b, d_x, opt, cfg, bn, q, &res, pmg);
             fail = res.fail == 3 ? 2 : res.fail;
         }
     } else {
@@ -768,7 +838,7 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
             };
             CgOptions o32 = opt;
             o32.rtol = cfg->rtol * bn / rn;   // the binary32 system starts from a unit residual
-            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, o32, cfg->pc, &res, &refresh);
+            rc = mf_pcg_core<PolF32>(ctx, op32, r32, d32, o32, cfg->pc, &res, &refresh, pmg);
             if (rc == FGPU_OK && !res.true_conv) {
                 bool ok = false;
                 if (res.fail != 3) rc = fold(d32, &ok);
@@ -778,7 +848,7 @@ int solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, con
                         CgResult r64;
                         CgOptions o64 = opt;
                         o64.maxit = cfg->maxit - res.iters;
-                        rc = mf_plain_solve(ctx, op, d_b, d_x, o64, cfg, bn, q, &r64);
+                        rc = mf_plain_solve(ctx, op, d_b, d_x, o64, cfg, bn, q, &r64, pmg);
                         fallback = 1;
                         fallback_its = r64.iters;
                         if (rc == FGPU_OK) rc = mf_residual64(ctx, op, d_b, d_x, rbest, q, &rn);
@@ -965,7 +1035,17 @@ extern "C" int fgpu_operator_destroy(fgpu_operator* op) {
 extern "C" int fgpu_solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const fgpu_vector* b, fgpu_vector* x,
                                       const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
     if (!ctx || !op || !b || !x || !cfg || b->n != op->nnodes || x->n != op->nnodes) return FGPU_ERR_INVALID;
-    int rc = solve_cg_operator(ctx, op, op32, b->d, x->d, cfg, stats);
+    if (cfg->pc == FGPU_PC_PMG) { ctx->err = "solve_cg_operator: pc pmg runs through fgpu_solve_cg_operator_pmg"; return FGPU_ERR_INVALID; }
+    int rc = solve_cg_operator(ctx, op, op32, b->d, x->d, cfg, stats, nullptr);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    return rc;
+}
+
+extern "C" int fgpu_solve_cg_operator_pmg(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, fgpu_pmg* pmg, const fgpu_vector* b,
+                                          fgpu_vector* x, const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
+    if (!ctx || !op || !pmg || !b || !x || !cfg || b->n != op->nnodes || x->n != op->nnodes) return FGPU_ERR_INVALID;
+    int rc = solve_cg_operator(ctx, op, op32, b->d, x->d, cfg, stats, pmg);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
     return rc;

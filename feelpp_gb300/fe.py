@@ -621,7 +621,8 @@ class Form1:
         self.vec.zero()
 
 
-_PC = {"none": _ffi.PC_NONE, "jacobi": _ffi.PC_JACOBI, "cheb_jacobi": _ffi.PC_CHEB_JACOBI, "gamg": _ffi.PC_GAMG}
+_PC = {"none": _ffi.PC_NONE, "jacobi": _ffi.PC_JACOBI, "cheb_jacobi": _ffi.PC_CHEB_JACOBI, "gamg": _ffi.PC_GAMG,
+       "pmg": _ffi.PC_PMG}
 
 
 def _solver_cfg(rtol, maxit, pc, mixed, inner_rtol, check_every, arith, cheb_degree, cheb_ratio):
@@ -832,6 +833,33 @@ class AMG:
             self.h = None
 
 
+class PMG:
+    """p-multigrid preconditioner of a matrix-free operator: Chebyshev smoothing on the binary32 operator
+    `smoother`, the P1 Form2 `coarse` (same mesh, Dirichlet rows eliminated) with its AMG hierarchy below."""
+
+    def __init__(self, smoother, coarse, smoother_degree=0):
+        self.env, self.smoother, self.coarse = smoother.env, smoother, coarse
+        self.amg = coarse.gamg()
+        cfg = _ffi.PmgCfg(smoother_degree)
+        h = C.c_void_p()
+        self.env.check(self.env.lib.fgpu_pmg_create(self.env.h, smoother.h, coarse.h, self.amg.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def info(self):
+        lmax, ms = C.c_double(), C.c_double()
+        nc = C.c_int64()
+        self.env.check(self.env.lib.fgpu_pmg_info(self.h, C.byref(lmax), C.byref(nc), C.byref(ms)))
+        return {"lmax": lmax.value, "coarse_rows": nc.value, "setup_ms": ms.value, "coarse_amg": self.amg.info()}
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                self.env.lib.fgpu_pmg_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
 class Operator:
     """Matrix-free operator of a Laplace/mass integral on a scalar space.
 
@@ -870,15 +898,37 @@ class Operator:
         self.env.check(self.env.lib.fgpu_operator_apply(self.env.h, self.h, x.h, y.h))
 
     def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=0.1, check_every=16,
-              cheb_degree=0, cheb_ratio=0.0):
+              cheb_degree=0, cheb_ratio=0.0, coarse=None, smoother=None):
         """Matrix-free PCG; with `inner` (a binary32 Operator) the mixed method is used
-        (binary32 CG with binary64 residual replacement every `inner_rtol` reduction)."""
+        (binary32 CG with binary64 residual replacement every `inner_rtol` reduction).
+        pc="pmg": p-multigrid V-cycle with `coarse` = the assembled P1 Form2 on the same mesh (same
+        coefficients, Dirichlet rows eliminated) and its AMG hierarchy as coarse level; the smoother runs
+        on `smoother` (a binary32 Operator; default `inner`)."""
         cfg = _solver_cfg(rtol, maxit, pc, inner is not None, inner_rtol, check_every, "f64", cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
         vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        if pc == "pmg":
+            pm = self.pmg(coarse, smoother or inner)
+            self.env.check(self.env.lib.fgpu_solve_cg_operator_pmg(self.env.h, self.h, inner.h if inner else None, pm.h, vec.h,
+                                                                   solution.h, C.byref(cfg), C.byref(st)))
+            out = _stats(st)
+            out["pmg"] = pm.info()
+            return out
         self.env.check(self.env.lib.fgpu_solve_cg_operator(self.env.h, self.h, inner.h if inner else None, vec.h,
                                                            solution.h, C.byref(cfg), C.byref(st)))
         return _stats(st)
+
+    def pmg(self, coarse, smoother, smoother_degree=0):
+        """The p-multigrid preconditioner (kept while the coarse matrix is unchanged)."""
+        if coarse is None or smoother is None:
+            raise ValueError("pc='pmg' needs coarse= (the P1 Form2) and a binary32 smoother operator")
+        key = (id(coarse), id(smoother), getattr(coarse, "_version", 0), smoother_degree)
+        pm = getattr(self, "_pmg", None)
+        if pm is None or pm.key != key:
+            pm = PMG(smoother, coarse, smoother_degree)
+            pm.key = key
+            self._pmg = pm
+        return pm
 
     def __del__(self):
         try:

@@ -76,6 +76,9 @@ extern "C" {
 #define FGPU_PC_JACOBI 1
 #define FGPU_PC_CHEB_JACOBI 2     /* degree-K Chebyshev polynomial in D^-1 A (Jacobi-scaled), PETSc
                                      KSPCHEBYSHEV+PCJACOBI used as a fixed preconditioner */
+#define FGPU_PC_PMG 4             /* p-multigrid V-cycle of a matrix-free operator (fgpu_pmg_create): binary32
+                                     Chebyshev smoothing on the order-p operator, the assembled P1 operator
+                                     on the same mesh as coarse level, solved by one AMG V-cycle */
 #define FGPU_PC_GAMG 3            /* smoothed-aggregation AMG V-cycle (pc-type=gamg): fgpu_amg_create,
                                      then fgpu_solve_cg_amg */
 
@@ -87,6 +90,8 @@ typedef struct fgpu_graph fgpu_graph;
 typedef struct fgpu_bc fgpu_bc;
 typedef struct fgpu_batch fgpu_batch;
 typedef struct fgpu_amg fgpu_amg;
+typedef struct fgpu_pmg fgpu_pmg;
+typedef struct fgpu_operator fgpu_operator;
 typedef struct fgpu_mesh fgpu_mesh;
 typedef struct fgpu_space fgpu_space;
 typedef struct fgpu_matrix fgpu_matrix;
@@ -277,6 +282,21 @@ int fgpu_amg_destroy(fgpu_amg* amg);
 int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
                       const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
 
+/* ---- p-multigrid for matrix-free operators (FGPU_PC_PMG): op32 = the binary32 order-p operator (its
+ *      Dirichlet dofs set), A1 = the assembled FP64 P1 form on the same mesh with the same coefficients and
+ *      Dirichlet rows eliminated, amg = fgpu_amg_create(A1). One V-cycle: Chebyshev smoothing of degree
+ *      smoother_degree (0 = 3) on op32, restriction to P1 by the transpose of the P1 -> Pp interpolation, one
+ *      AMG V-cycle, prolongation, post-smoothing. fgpu_solve_cg_operator_pmg runs the matrix-free solve of
+ *      fgpu_solve_cg_operator (plain binary64 or mixed) with it as preconditioner. ---- */
+typedef struct {
+    int smoother_degree;
+} fgpu_pmg_cfg;
+int fgpu_pmg_create(fgpu_ctx* ctx, fgpu_operator* op32, const fgpu_matrix* A1, fgpu_amg* amg, const fgpu_pmg_cfg* cfg,
+                    fgpu_pmg** out);
+/* lambda_max(D^-1 A_p) estimate, coarse rows, set-up time */
+int fgpu_pmg_info(const fgpu_pmg* pmg, double* lmax, int64_t* coarse_rows, double* setup_ms);
+int fgpu_pmg_destroy(fgpu_pmg* pmg);
+
 /* host-only hierarchy (no device): the same set-up from a host CSR, for inspection and tests.
  * fgpu_amg_host_level: rows, nnz of A_l, nnz and columns of P_l (0 on the coarsest), lmax(D^-1 A_l);
  * fgpu_amg_host_export: copies A_l (ia n+1, ja, a), P_l (ia n+1, ja, a) and the aggregate of each
@@ -302,7 +322,6 @@ int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, in
  *      there is no element-level one). precision: FGPU_F32, FGPU_F64 (native) or FGPU_DF64.
  *      Dirichlet dofs are eliminated symmetrically (the operator then equals the assembled
  *      matrix after on(..., elimination_symmetric)). ---- */
-typedef struct fgpu_operator fgpu_operator;
 int fgpu_operator_create(fgpu_ctx* ctx, fgpu_space* V, const fgpu_form_desc* form, int precision, fgpu_operator** out);
 int fgpu_operator_set_dirichlet(fgpu_operator* op, int64_t ndofs, const int32_t* dofs);
 int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_vector* x, fgpu_vector* y);
@@ -321,6 +340,9 @@ int fgpu_tc_selftest(fgpu_ctx* ctx, const float* A, const float* B, float* D);
  * mixed (cfg->mixed) with a binary32 inner operator op32 refined by op's residual */
 int fgpu_solve_cg_operator(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, const fgpu_vector* b, fgpu_vector* x,
                            const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+/* the same with the p-multigrid preconditioner pmg (cfg->pc = FGPU_PC_PMG; see fgpu_pmg_create) */
+int fgpu_solve_cg_operator_pmg(fgpu_ctx* ctx, fgpu_operator* op, fgpu_operator* op32, fgpu_pmg* pmg, const fgpu_vector* b,
+                               fgpu_vector* x, const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
 
 /* ---- host-only queries (no device needed): the dof numbering, the sparsity
  *      pattern and the reference tables the device kernels use ---- */
