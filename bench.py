@@ -526,6 +526,28 @@ def run_matfree(args):
     solve["mixed_fp32_cuda_cores"], _ = mf_solve(ops["f64"], ops["f32_cuda_cores"])
     solve["mixed_fp32_cheb_jacobi"], _ = mf_solve(ops["f64"], ops["f32_cuda_cores"], pc="cheb_jacobi", cheb_degree=3)
     solve["mixed_fp32_colour_scatter"], _ = mf_solve(ops["f64"], ops["f32_colour_scatter"])
+    # p-multigrid: assembled P1 coarse level (with its AMG hierarchy) below the binary32 smoothing
+    V1 = fpp.Pch(M, 1)
+    u1, v1 = V1.element(), V1.element()
+    t0 = time.perf_counter()
+    a1 = fpp.form2(test=V1, trial=V1)
+    a1.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u1), fpp.grad(v1))))
+    l1 = fpp.form1(test=V1)
+    a1 += fpp.on(fpp.boundaryfaces(M), rhs=l1, element=u1, expr=0.0, type="elimination_symmetric")
+    pm = ops["f64"].pmg(a1, ops["f32_cuda_cores"])
+    torch.cuda.synchronize()
+    pmg_setup_ms = (time.perf_counter() - t0) * 1e3
+    wp = V.element()
+    cfgp = fe._solver_cfg(1e-10, 100000, "pmg", True, 0.1, 16, "f64", 0, 0.0)
+    stp = _ffi.SolveStats()
+    rcp = env.lib.fgpu_solve_cg_operator_pmg(env.h, ops["f64"].h, ops["f32_cuda_cores"].h, pm.h, l.vec.h, wp.h, C.byref(cfgp),
+                                              C.byref(stp))
+    sp = fe._stats(stp)
+    sp["status"] = "ok" if rcp == 0 else _ffi.ERROR_NAMES.get(rcp, str(rcp))
+    sp["l2_error"], sp["h1_error"] = wp.errors_sine(qe)
+    sp["setup_ms_p1_assembly_amg_pmg"] = pmg_setup_ms
+    sp["pmg"] = pm.info()
+    solve["mixed_fp32_pmg_amg"] = sp
     if args.with_plain:
         solve["fp64_matfree_df64"], w64 = mf_solve(ops["df64"])
     csr = None
@@ -562,7 +584,8 @@ def run_matfree(args):
         del a
     ref_l2 = solve.get("fp64_matfree_df64", {}).get("l2_error") or (csr["fp64_cg"]["l2_error"] if csr else None)
     if ref_l2:
-        for k in ("mixed_fp32_tensor_cores", "mixed_fp32_cuda_cores", "mixed_fp32_cheb_jacobi", "mixed_fp32_colour_scatter"):
+        for k in ("mixed_fp32_tensor_cores", "mixed_fp32_cuda_cores", "mixed_fp32_cheb_jacobi", "mixed_fp32_colour_scatter",
+                  "mixed_fp32_pmg_amg"):
             solve[k]["l2_error_rel_diff_vs_fp64"] = abs(solve[k]["l2_error"] - ref_l2) / ref_l2
     out = {"metric": "P%d matrix-free operator apply GDOF/s & CG time-to-1e-10 (FP32 inner + FP64 residual)" % args.order,
            "value": applies["f32_cuda_cores"]["gdof_per_s"], "unit": "GDOF/s", "n_gpus": 1,

@@ -311,6 +311,10 @@ int amg_vcycle(fgpu_amg* M, const T* r, const int* stop) {
         fgpu_amg::Level& V = M->L[l];
         const bool coarsest = l == nlev - 1;
         if (coarsest && M->coarse_inv) {
+            if (l == 0) {            // one-level hierarchy: the right-hand side still has to reach V.b
+                amg_start_kernel<T><<<vblocks(V.n), 256, 0, st>>>(V.n, r, V.b, V.dinv, V.inv_theta, V.x, V.w, V.d0, stop);
+                ++nl;
+            }
             const int g = (int)std::max<int64_t>(1, std::min<int64_t>((V.n * 32 + 255) / 256, 152 * 8));
             amg_dense_kernel<<<g, 256, 0, st>>>(V.n, M->coarse_inv, V.b, V.x, stop);
             ++nl;
@@ -523,7 +527,7 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
         for (float** v : vecs) FGPU_CUDA_CHECK(ctx, cudaMalloc(v, std::max<int64_t>(V.n, 1) * sizeof(float)));
         if (coarsest && !H.coarse_inv.empty()) {
             FGPU_CUDA_CHECK(ctx, upload_f32(&M->coarse_inv, H.coarse_inv));
-            nl += 1;
+            nl += l == 0 ? 2 : 1;
         } else if (coarsest) {
             nl += M->coarse_degree;               // start + coarse_degree - 1 steps
         } else {

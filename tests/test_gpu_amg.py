@@ -83,3 +83,12 @@ def test_gamg_rejected_without_hierarchy(env):
     w = V.element()
     rc = env.lib.fgpu_solve_cg(env.h, a.h, None, l.vec.h, w.h, C.byref(cfg), C.byref(st))
     assert _ffi.ERROR_NAMES[rc] == "FGPU_ERR_INVALID"
+
+
+def test_gamg_one_level_dense(env):
+    """Below coarse-eq-lim rows the hierarchy is one dense level: the V-cycle is the (binary32) inverse,
+    and CG converges in a handful of iterations."""
+    M, V, u, v, a, l = poisson(env, 6, 1)
+    w = V.element()
+    st = a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
+    assert st["gamg"]["levels"] == 1 and st["rel_residual"] <= 1e-10 and st["iterations"] <= 6
