@@ -58,7 +58,7 @@ class AmgCfg(C.Structure):
 
 
 class PmgCfg(C.Structure):
-    _fields_ = [("smoother_degree", C.c_int)]
+    _fields_ = [("smoother_degree", C.c_int), ("coarse_cycles", C.c_int)]
 
 
 class SolveStats(C.Structure):

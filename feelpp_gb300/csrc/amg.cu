@@ -67,6 +67,8 @@ struct fgpu_amg {
     double setup_ms = 0;
     int launches_per_cycle = 0;
     fgpu_amg_cfg cfg{};
+    float* xacc = nullptr;           // repeated cycles (amg_vcycle_f32 with cycles > 1): accumulated solution
+    float* tres = nullptr;           //                                                   and residual
 };
 
 namespace fgpu {
@@ -356,9 +358,38 @@ int amg_vcycle(fgpu_amg* M, const T* r, const int* stop) {
 
 template int amg_vcycle<double>(fgpu_amg*, const double*, const int*);
 
-int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x) {
-    const int nl = amg_vcycle<float>(M, r, stop);
+__global__ void amg_add_kernel(int64_t n, const float* __restrict__ a, float* __restrict__ acc, int first,
+                               const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc[i] = first ? a[i] : acc[i] + a[i];
+}
+
+// `cycles` V-cycles for A_0 x = r from x = 0 (each further cycle on the residual of the sum so far)
+int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x, int cycles) {
+    int nl = amg_vcycle<float>(M, r, stop);
     *x = M->L[0].x;
+    if (cycles <= 1) return nl;
+    fgpu_amg::Level& V = M->L[0];
+    cudaStream_t st = M->ctx->stream;
+    if (!M->xacc) {
+        if (cudaMalloc(&M->xacc, V.n * sizeof(float)) != cudaSuccess || cudaMalloc(&M->tres, V.n * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            return nl;                // no room: one cycle
+        }
+    }
+    amg_add_kernel<<<vblocks(V.n), 256, 0, st>>>(V.n, V.x, M->xacc, 1, stop);
+    ++nl;
+    for (int c = 1; c < cycles; ++c) {
+        AmgSweep s;
+        s.n = V.n; s.x = M->xacc; s.b = r; s.out = M->tres;
+        if (M->L.size() > 1 || !M->coarse_inv) sell_sweep<kResid>(st, V, s, stop);
+        else return nl;               // one dense level: the first cycle was already exact
+        nl += 1 + amg_vcycle<float>(M, M->tres, stop);
+        amg_add_kernel<<<vblocks(V.n), 256, 0, st>>>(V.n, V.x, M->xacc, 0, stop);
+        ++nl;
+    }
+    *x = M->xacc;
     return nl;
 }
 
@@ -589,6 +620,8 @@ extern "C" int fgpu_amg_destroy(fgpu_amg* M) {
     if (!M) return FGPU_OK;
     for (auto& V : M->L) free_level(V);
     cudaFree(M->coarse_inv);
+    cudaFree(M->xacc);
+    cudaFree(M->tres);
     delete M;
     return FGPU_OK;
 }

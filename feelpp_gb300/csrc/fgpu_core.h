@@ -291,7 +291,7 @@ int operator_precision(const fgpu_operator* op);
 const fgpu_space* operator_space(const fgpu_operator* op);
 const uint8_t* operator_mask(const fgpu_operator* op);
 const float* operator_diag_f32(fgpu_ctx* ctx, fgpu_operator* op);
-int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x);
+int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x, int cycles);
 int64_t amg_rows(const fgpu_amg* M);
 int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
 int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);

@@ -42,7 +42,8 @@ struct fgpu_pmg {
     int iG = 4, rG = 16;
     float* dinv = nullptr;           // 1 / diag(A_p)
     float *rf = nullptr, *x = nullptr, *w = nullptr, *q = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr, *rc = nullptr;
-    int degree = 3;
+    int degree = 2;
+    int coarse_cycles = 1;           // AMG V-cycles per coarse solve
     double lmax = 0;
     float inv_theta = 1.0f;
     std::vector<float> c1, c2;
@@ -206,7 +207,7 @@ int pmg_vcycle(fgpu_pmg* P, const T* r, const int* stop) {
     csr(st, P->rG, P->nc, P->r_ia, P->r_ja, P->r_a, P->w, P->rc, 0, stop);
     nl += 2;
     const float* xc = nullptr;
-    nl += amg_vcycle_f32(P->amg, P->rc, stop, &xc);
+    nl += amg_vcycle_f32(P->amg, P->rc, stop, &xc, P->coarse_cycles);
     csr(st, P->iG, P->nf, P->i_ia, P->i_ja, P->i_a, xc, P->x, 1, stop);
     ++nl;
     nl += mf_apply_f32_gated(P->ctx, P->op, P->x, P->q, stop);
@@ -368,6 +369,7 @@ extern "C" int fgpu_pmg_create(fgpu_ctx* ctx, fgpu_operator* op32, const fgpu_ma
     P->nf = Vf->ndof;
     P->nc = Vc->ndof;
     if (cfg && cfg->smoother_degree >= 2) P->degree = cfg->smoother_degree;
+    if (cfg && cfg->coarse_cycles >= 1) P->coarse_cycles = std::min(cfg->coarse_cycles, 4);
     const int64_t nt = Vf->mesh->nt;
     const int n = Vf->n;
     // host copies of the dof tables and the fine Dirichlet mask

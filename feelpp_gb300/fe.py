@@ -837,10 +837,10 @@ class PMG:
     """p-multigrid preconditioner of a matrix-free operator: Chebyshev smoothing on the binary32 operator
     `smoother`, the P1 Form2 `coarse` (same mesh, Dirichlet rows eliminated) with its AMG hierarchy below."""
 
-    def __init__(self, smoother, coarse, smoother_degree=0):
+    def __init__(self, smoother, coarse, smoother_degree=0, coarse_cycles=0):
         self.env, self.smoother, self.coarse = smoother.env, smoother, coarse
         self.amg = coarse.gamg()
-        cfg = _ffi.PmgCfg(smoother_degree)
+        cfg = _ffi.PmgCfg(smoother_degree, coarse_cycles)
         h = C.c_void_p()
         self.env.check(self.env.lib.fgpu_pmg_create(self.env.h, smoother.h, coarse.h, self.amg.h, C.byref(cfg), C.byref(h)))
         self.h = h
@@ -898,17 +898,18 @@ class Operator:
         self.env.check(self.env.lib.fgpu_operator_apply(self.env.h, self.h, x.h, y.h))
 
     def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", inner=None, inner_rtol=0.1, check_every=16,
-              cheb_degree=0, cheb_ratio=0.0, coarse=None, smoother=None):
+              cheb_degree=0, cheb_ratio=0.0, coarse=None, smoother=None, smoother_degree=0, coarse_cycles=0):
         """Matrix-free PCG; with `inner` (a binary32 Operator) the mixed method is used
         (binary32 CG with binary64 residual replacement every `inner_rtol` reduction).
         pc="pmg": p-multigrid V-cycle with `coarse` = the assembled P1 Form2 on the same mesh (same
         coefficients, Dirichlet rows eliminated) and its AMG hierarchy as coarse level; the smoother runs
-        on `smoother` (a binary32 Operator; default `inner`)."""
+        on `smoother` (a binary32 Operator; default `inner`), Chebyshev degree `smoother_degree` (0: 2), `coarse_cycles`
+        AMG V-cycles per coarse solve (0: 1)."""
         cfg = _solver_cfg(rtol, maxit, pc, inner is not None, inner_rtol, check_every, "f64", cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
         vec = rhs.vec if isinstance(rhs, Form1) else rhs
         if pc == "pmg":
-            pm = self.pmg(coarse, smoother or inner)
+            pm = self.pmg(coarse, smoother or inner, smoother_degree, coarse_cycles)
             self.env.check(self.env.lib.fgpu_solve_cg_operator_pmg(self.env.h, self.h, inner.h if inner else None, pm.h, vec.h,
                                                                    solution.h, C.byref(cfg), C.byref(st)))
             out = _stats(st)
@@ -918,14 +919,14 @@ class Operator:
                                                            solution.h, C.byref(cfg), C.byref(st)))
         return _stats(st)
 
-    def pmg(self, coarse, smoother, smoother_degree=0):
+    def pmg(self, coarse, smoother, smoother_degree=0, coarse_cycles=0):
         """The p-multigrid preconditioner (kept while the coarse matrix is unchanged)."""
         if coarse is None or smoother is None:
             raise ValueError("pc='pmg' needs coarse= (the P1 Form2) and a binary32 smoother operator")
-        key = (id(coarse), id(smoother), getattr(coarse, "_version", 0), smoother_degree)
+        key = (id(coarse), id(smoother), getattr(coarse, "_version", 0), smoother_degree, coarse_cycles)
         pm = getattr(self, "_pmg", None)
         if pm is None or pm.key != key:
-            pm = PMG(smoother, coarse, smoother_degree)
+            pm = PMG(smoother, coarse, smoother_degree, coarse_cycles)
             pm.key = key
             self._pmg = pm
         return pm

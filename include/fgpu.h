@@ -285,11 +285,12 @@ int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const 
 /* ---- p-multigrid for matrix-free operators (FGPU_PC_PMG): op32 = the binary32 order-p operator (its
  *      Dirichlet dofs set), A1 = the assembled FP64 P1 form on the same mesh with the same coefficients and
  *      Dirichlet rows eliminated, amg = fgpu_amg_create(A1). One V-cycle: Chebyshev smoothing of degree
- *      smoother_degree (0 = 3) on op32, restriction to P1 by the transpose of the P1 -> Pp interpolation, one
+ *      smoother_degree on op32, restriction to P1 by the transpose of the P1 -> Pp interpolation, one
  *      AMG V-cycle, prolongation, post-smoothing. fgpu_solve_cg_operator_pmg runs the matrix-free solve of
  *      fgpu_solve_cg_operator (plain binary64 or mixed) with it as preconditioner. ---- */
 typedef struct {
-    int smoother_degree;
+    int smoother_degree;      /* Chebyshev degree of the order-p smoothing (0 = 2: one operator sweep) */
+    int coarse_cycles;        /* AMG V-cycles per coarse solve (0 = 1) */
 } fgpu_pmg_cfg;
 int fgpu_pmg_create(fgpu_ctx* ctx, fgpu_operator* op32, const fgpu_matrix* A1, fgpu_amg* amg, const fgpu_pmg_cfg* cfg,
                     fgpu_pmg** out);
