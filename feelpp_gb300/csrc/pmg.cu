@@ -42,8 +42,8 @@ struct fgpu_pmg {
     int iG = 4, rG = 16;
     float* dinv = nullptr;           // 1 / diag(A_p)
     float *rf = nullptr, *x = nullptr, *w = nullptr, *q = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr, *rc = nullptr;
-    int degree = 2;
-    int coarse_cycles = 1;           // AMG V-cycles per coarse solve
+    int degree = 3;
+    int coarse_cycles = 2;           // AMG V-cycles per coarse solve
     double lmax = 0;
     float inv_theta = 1.0f;
     std::vector<float> c1, c2;
@@ -162,7 +162,7 @@ int vb_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 2
 
 int lanes(int64_t n, int64_t nnz) {
     const double m = n > 0 ? (double)nnz / (double)n : 1.0;
-    return m <= 6 ? 4 : m <= 12 ? 8 : m <= 24 ? 16 : 32;
+    return m <= 4 ? 1 : m <= 12 ? 8 : m <= 24 ? 16 : 32;     // the prolongation's rows have 1 to 4 entries
 }
 
 void csr(cudaStream_t st, int G, int64_t n, const int64_t* ia, const int32_t* ja, const float* a, const float* x, float* y, int add,
@@ -170,6 +170,7 @@ void csr(cudaStream_t st, int G, int64_t n, const int64_t* ia, const int32_t* ja
     const int per = 256 / G;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + per - 1) / per, 152 * 16));
     switch (G) {
+        case 1: pmg_csr_kernel<1><<<g, 256, 0, st>>>(n, ia, ja, a, x, y, add, stop); break;
         case 4: pmg_csr_kernel<4><<<g, 256, 0, st>>>(n, ia, ja, a, x, y, add, stop); break;
         case 8: pmg_csr_kernel<8><<<g, 256, 0, st>>>(n, ia, ja, a, x, y, add, stop); break;
         case 16: pmg_csr_kernel<16><<<g, 256, 0, st>>>(n, ia, ja, a, x, y, add, stop); break;

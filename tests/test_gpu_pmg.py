@@ -52,7 +52,7 @@ def test_pmg_mixed_matfree(env, order, n):
     assert st["pmg"]["lmax"] > 1.0 and st["pmg"]["coarse_rows"] == (n + 1) ** 3
     w = V.element()
     stj = op64.solve(l, w, rtol=1e-10, inner=op32)
-    assert st["iterations"] <= 0.2 * stj["iterations"]
+    assert st["iterations"] <= 0.35 * stj["iterations"]
     ws = V.element()
     a.solve(rhs=lc, solution=ws, rtol=1e-12)
     assert np.linalg.norm(u.to_numpy() - ws.to_numpy()) <= 1e-8 * np.linalg.norm(ws.to_numpy())
