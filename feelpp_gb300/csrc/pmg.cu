@@ -27,19 +27,19 @@
 #include <vector>
 
 #include "cg_driver.cuh"
+#include "scan.cuh"
 
 struct fgpu_pmg {
     fgpu_ctx* ctx = nullptr;
     fgpu_operator* op = nullptr;     // binary32 order-p operator (Dirichlet rows set)
     fgpu_amg* amg = nullptr;         // hierarchy of the assembled P1 operator
     int64_t nf = 0, nc = 0;
-    int64_t* i_ia = nullptr;         // I: nf x nc
-    int32_t* i_ja = nullptr;
-    float* i_a = nullptr;
-    int64_t* r_ia = nullptr;         // R = I^T: nc x nf
+    int32_t* i_col = nullptr;        // I: nf x nc in ELL form, 4 slots per row (slot-major), columns sorted
+    float* i_val = nullptr;          //    (padding: column 0, value 0)
+    uint32_t* r_ia = nullptr;        // R = I^T: nc x nf, CSR with rows sorted by fine index
     int32_t* r_ja = nullptr;
     float* r_a = nullptr;
-    int iG = 4, rG = 16;
+    int rG = 16;
     float* dinv = nullptr;           // 1 / diag(A_p)
     float *rf = nullptr, *x = nullptr, *w = nullptr, *q = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr, *rc = nullptr;
     int degree = 3;
@@ -117,10 +117,132 @@ __global__ void pmg_resid_kernel(int64_t n, const float* __restrict__ rf, const 
     }
 }
 
+// x += I x_c with I in ELL form (thread per fine row, slots in column order)
+__global__ void pmg_prolong_kernel(int64_t nf, const int32_t* __restrict__ col, const float* __restrict__ val,
+                                   const float* __restrict__ xc, float* __restrict__ x, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
+        float s = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s = fmaf(__ldg(val + k * nf + i), __ldg(xc + __ldg(col + k * nf + i)), s);
+        x[i] += s;
+    }
+}
+
+// ---- device construction of the transfer operators ----
+// coarse Dirichlet vertices: the P1 dofs of masked fine vertex nodes (identical writes only)
+__global__ void pmg_cmask_kernel(int64_t nt, int n, const int32_t* __restrict__ lf, const int32_t* __restrict__ lc,
+                                 const uint8_t* __restrict__ mf, uint8_t* __restrict__ mc) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt * 4; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t >> 2;
+        const int v = (int)(t & 3);
+        if (mf && mf[lf[e * n + v]]) mc[lc[e * 4 + v]] = 1;
+    }
+}
+
+// ELL rows of I: each row is written by the first element of its node's incidence list (one writer,
+// so the weights, which other elements would compute from other local coordinates, are fixed); the
+// entries (P1 dofs of the element's vertices with a nonzero barycentric weight at the node, Dirichlet
+// vertices left out) are sorted by column
+__global__ void pmg_ell_kernel(int64_t nt, int n, const int32_t* __restrict__ lf, const int32_t* __restrict__ lc,
+                               const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                               const uint8_t* __restrict__ mf, const uint8_t* __restrict__ mc, const float* __restrict__ lam,
+                               int64_t nf, int32_t* __restrict__ col, float* __restrict__ val) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt * n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t / n;
+        const int i = (int)(t - e * n);
+        const int64_t row = lf[t];
+        if ((int64_t)(inc[inc_ptr[row]] >> 5) != e) continue;
+        int32_t c[4] = {0, 0, 0, 0};
+        float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        int k = 0;
+        if (!(mf && mf[row])) {
+            for (int v = 0; v < 4; ++v) {
+                const float l = lam[i * 4 + v];
+                const int32_t cv = lc[e * 4 + v];
+                if (l != 0.0f && !mc[cv]) {
+                    int p = k++;
+                    while (p > 0 && c[p - 1] > cv) { c[p] = c[p - 1]; w[p] = w[p - 1]; --p; }
+                    c[p] = cv;
+                    w[p] = l;
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            col[s * nf + row] = c[s];
+            val[s * nf + row] = w[s];
+        }
+    }
+}
+
+__global__ void pmg_rcount_kernel(int64_t nf, const int32_t* __restrict__ col, const float* __restrict__ val, uint32_t* __restrict__ cnt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (val[k * nf + i] != 0.0f) atomicAdd(cnt + col[k * nf + i], 1u);
+}
+
+__global__ void pmg_rfill_kernel(int64_t nf, const int32_t* __restrict__ col, const float* __restrict__ val, uint32_t* __restrict__ fill,
+                                 int32_t* __restrict__ rja, float* __restrict__ ra) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float v = val[k * nf + i];
+            if (v == 0.0f) continue;
+            const uint32_t p = atomicAdd(fill + col[k * nf + i], 1u);
+            rja[p] = (int32_t)i;
+            ra[p] = v;
+        }
+}
+
+// sort every restriction row by fine index (one warp per row, bitonic sort of up to 256 entries in
+// shared memory); longer rows set *status
+__global__ void __launch_bounds__(256) pmg_rsort_kernel(int64_t nc, const uint32_t* __restrict__ ia, int32_t* __restrict__ ja,
+                                                        float* __restrict__ a, int* __restrict__ status) {
+    __shared__ int32_t sk[8][256];
+    __shared__ float sv[8][256];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t r = (int64_t)blockIdx.x * 8 + w; r < nc; r += (int64_t)gridDim.x * 8) {
+        const uint32_t p0 = ia[r], len = ia[r + 1] - p0;
+        if (len > 256) {
+            if (lane == 0) atomicOr(status, 1);
+            continue;
+        }
+        int m = 1;
+        while (m < (int)len) m <<= 1;
+        for (int k = lane; k < m; k += 32) {
+            sk[w][k] = k < (int)len ? ja[p0 + k] : INT32_MAX;
+            sv[w][k] = k < (int)len ? a[p0 + k] : 0.0f;
+        }
+        __syncwarp();
+        for (int size = 2; size <= m; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int k = lane; k < m; k += 32) {
+                    const int partner = k ^ stride;
+                    if (partner > k) {
+                        const bool up = (k & size) == 0;
+                        const int32_t x = sk[w][k], y = sk[w][partner];
+                        if ((x > y) == up) {
+                            sk[w][k] = y; sk[w][partner] = x;
+                            const float t = sv[w][k]; sv[w][k] = sv[w][partner]; sv[w][partner] = t;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int k = lane; k < (int)len; k += 32) {
+            ja[p0 + k] = sk[w][k];
+            a[p0 + k] = sv[w][k];
+        }
+        __syncwarp();
+    }
+}
+
 // y = M x (add = 0) or y += M x (add = 1), G lanes per row; the warp-uniform loop keeps every lane
 // at the shuffles
 template <int G>
-__global__ void __launch_bounds__(256) pmg_csr_kernel(int64_t n, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja,
+__global__ void __launch_bounds__(256) pmg_csr_kernel(int64_t n, const uint32_t* __restrict__ ia, const int32_t* __restrict__ ja,
                                                       const float* __restrict__ a, const float* __restrict__ x, float* __restrict__ y,
                                                       int add, const int* __restrict__ stop) {
     if (stop && *stop) return;
@@ -165,7 +287,7 @@ int lanes(int64_t n, int64_t nnz) {
     return m <= 4 ? 1 : m <= 12 ? 8 : m <= 24 ? 16 : 32;     // the prolongation's rows have 1 to 4 entries
 }
 
-void csr(cudaStream_t st, int G, int64_t n, const int64_t* ia, const int32_t* ja, const float* a, const float* x, float* y, int add,
+void csr(cudaStream_t st, int G, int64_t n, const uint32_t* ia, const int32_t* ja, const float* a, const float* x, float* y, int add,
          const int* stop) {
     const int per = 256 / G;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + per - 1) / per, 152 * 16));
@@ -209,7 +331,7 @@ int pmg_vcycle(fgpu_pmg* P, const T* r, const int* stop) {
     nl += 2;
     const float* xc = nullptr;
     nl += amg_vcycle_f32(P->amg, P->rc, stop, &xc, P->coarse_cycles);
-    csr(st, P->iG, P->nf, P->i_ia, P->i_ja, P->i_a, xc, P->x, 1, stop);
+    pmg_prolong_kernel<<<vb_of(P->nf), 256, 0, st>>>(P->nf, P->i_col, P->i_val, xc, P->x, stop);
     ++nl;
     nl += mf_apply_f32_gated(P->ctx, P->op, P->x, P->q, stop);
     pmg_resid_kernel<<<vb_of(P->nf), 256, 0, st>>>(P->nf, P->rf, P->q, P->w, P->dinv, P->inv_theta, P->d0, P->e, 1, stop);
@@ -266,6 +388,20 @@ __global__ void scale_kernel(int64_t n, const float* __restrict__ x, float s, fl
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = s * x[i];
 }
 
+__global__ void lanczos_init_kernel(int64_t n, const float* __restrict__ dinv, float* __restrict__ s, float* __restrict__ v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        s[i] = sqrtf(fmaxf(dinv[i], 0.0f));
+        uint64_t h = (uint64_t)i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+        h ^= h >> 33; h *= 0xff51afd7ed558ccdull; h ^= h >> 33; h *= 0xc4ceb9fe1a85ec53ull; h ^= h >> 33;
+        v[i] = (float)(h >> 40) * (1.0f / 16777216.0f) - 0.5f;
+    }
+}
+
+__global__ void recip_kernel(int64_t n, const float* __restrict__ d, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = d[i] != 0.0f ? 1.0f / d[i] : 0.0f;
+}
+
 double dot(fgpu_ctx* ctx, int64_t n, const float* a, const float* b, double* d_part, std::vector<double>& h) {
     const int nb = vb_of(n);
     dot_partials_kernel<<<nb, 256, 0, ctx->stream>>>(n, a, b, d_part);
@@ -290,22 +426,11 @@ int lanczos_lmax(fgpu_pmg* P, int m, double* out) {
     if (e == cudaSuccess) e = cudaMalloc(&u, n * 4);
     if (e == cudaSuccess) e = cudaMalloc(&part, h.size() * sizeof(double));
     if (e != cudaSuccess) { cudaGetLastError(); ctx->err = "pmg: allocation failed"; cudaFree(s); cudaFree(v); cudaFree(vold); cudaFree(t); cudaFree(u); cudaFree(part); return FGPU_ERR_ALLOC; }
-    // s = D^-1/2 (from dinv), v0 pseudo-random, normalised
-    std::vector<float> hs(n), hv(n);
-    std::vector<float> hd(n);
-    cudaMemcpy(hd.data(), P->dinv, n * 4, cudaMemcpyDeviceToHost);
-    uint64_t st = 0x9E3779B97F4A7C15ull;
-    double nv = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        hs[i] = std::sqrt(std::max(hd[i], 0.0f));
-        st ^= st >> 33; st *= 0xff51afd7ed558ccdull; st ^= st >> 33;
-        hv[i] = (float)((double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5);
-        nv += (double)hv[i] * hv[i];
-    }
-    for (auto& x : hv) x = (float)(x / std::sqrt(nv));
-    cudaMemcpy(s, hs.data(), n * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(v, hv.data(), n * 4, cudaMemcpyHostToDevice);
-    cudaMemset(vold, 0, n * 4);
+    // s = D^-1/2 (from dinv), v0 pseudo-random (hash of the index), normalised
+    lanczos_init_kernel<<<vb_of(n), 256, 0, ctx->stream>>>(n, P->dinv, s, t);
+    const double nv = std::sqrt(dot(ctx, n, t, t, part, h));
+    scale_kernel<<<vb_of(n), 256, 0, ctx->stream>>>(n, t, (float)(1.0 / nv), v);
+    cudaMemsetAsync(vold, 0, n * 4, ctx->stream);
     std::vector<double> al, be;
     double bprev = 0;
     for (int k = 0; k < m; ++k) {
@@ -338,7 +463,7 @@ cudaError_t upv(T** dst, const std::vector<T>& v) {
 }
 
 void pmg_free(fgpu_pmg* P) {
-    cudaFree(P->i_ia); cudaFree(P->i_ja); cudaFree(P->i_a); cudaFree(P->r_ia); cudaFree(P->r_ja); cudaFree(P->r_a);
+    cudaFree(P->i_col); cudaFree(P->i_val); cudaFree(P->r_ia); cudaFree(P->r_ja); cudaFree(P->r_a);
     cudaFree(P->dinv); cudaFree(P->rf); cudaFree(P->x); cudaFree(P->w); cudaFree(P->q); cudaFree(P->d0); cudaFree(P->d1);
     cudaFree(P->e); cudaFree(P->rc);
 }
@@ -373,72 +498,64 @@ extern "C" int fgpu_pmg_create(fgpu_ctx* ctx, fgpu_operator* op32, const fgpu_ma
     if (cfg && cfg->coarse_cycles >= 1) P->coarse_cycles = std::min(cfg->coarse_cycles, 4);
     const int64_t nt = Vf->mesh->nt;
     const int n = Vf->n;
-    // host copies of the dof tables and the fine Dirichlet mask
-    std::vector<int32_t> lf((size_t)nt * n), lc((size_t)nt * 4);
-    std::vector<uint8_t> mf(P->nf, 0);
-    cudaError_t e = cudaMemcpy(lf.data(), Vf->d_l2n, lf.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(lc.data(), Vc->d_l2n, lc.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && operator_mask(op32)) e = cudaMemcpy(mf.data(), operator_mask(op32), P->nf, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); delete P; return FGPU_ERR_CUDA; }
-    // coarse Dirichlet vertices: the vertex dofs of masked fine vertex nodes
-    std::vector<uint8_t> mc(P->nc, 0);
-    for (int64_t el = 0; el < nt; ++el)
-        for (int v = 0; v < 4; ++v)
-            if (mf[lf[el * n + v]]) mc[lc[el * 4 + v]] = 1;
-    // P1 basis at the order-p reference nodes (barycentric coordinates on [-1,1]^3)
+    // barycentric weights of the P1 vertices at the order-p reference nodes ([-1,1]^3 element)
     std::vector<double> nodes;
     lagrange_nodes(Vf->order, nodes);
-    std::vector<int64_t> rows_ptr(P->nf + 1, 0);
-    std::vector<std::array<int32_t, 4>> rcol(P->nf);
-    std::vector<std::array<float, 4>> rval(P->nf);
-    std::vector<uint8_t> rlen(P->nf, 0), done(P->nf, 0);
-    for (int64_t el = 0; el < nt; ++el)
-        for (int i = 0; i < n; ++i) {
-            const int32_t row = lf[el * n + i];
-            if (done[row]) continue;
-            done[row] = 1;
-            if (mf[row]) continue;
-            const double x = nodes[3 * i], y = nodes[3 * i + 1], z = nodes[3 * i + 2];
-            const double lam[4] = {-0.5 * (1 + x + y + z), 0.5 * (1 + x), 0.5 * (1 + y), 0.5 * (1 + z)};
-            std::array<std::pair<int32_t, float>, 4> ent;
-            int k = 0;
-            for (int v = 0; v < 4; ++v) {
-                const int32_t col = lc[el * 4 + v];
-                if (std::fabs(lam[v]) > 1e-12 && !mc[col]) ent[k++] = {col, (float)lam[v]};
-            }
-            std::sort(ent.begin(), ent.begin() + k);
-            rlen[row] = (uint8_t)k;
-            for (int u = 0; u < k; ++u) { rcol[row][u] = ent[u].first; rval[row][u] = ent[u].second; }
-        }
-    std::vector<int64_t> ia(P->nf + 1, 0);
-    for (int64_t r = 0; r < P->nf; ++r) ia[r + 1] = ia[r] + rlen[r];
-    std::vector<int32_t> ja(ia[P->nf]);
-    std::vector<float> va(ia[P->nf]);
-    for (int64_t r = 0; r < P->nf; ++r)
-        for (int u = 0; u < rlen[r]; ++u) { ja[ia[r] + u] = rcol[r][u]; va[ia[r] + u] = rval[r][u]; }
-    // R = I^T
-    std::vector<int64_t> ria(P->nc + 1, 0);
-    for (int32_t c : ja) ria[c + 1]++;
-    for (int64_t c = 0; c < P->nc; ++c) ria[c + 1] += ria[c];
-    std::vector<int32_t> rja(ja.size());
-    std::vector<float> rva(ja.size());
-    {
-        std::vector<int64_t> fill(ria.begin(), ria.end() - 1);
-        for (int64_t r = 0; r < P->nf; ++r)
-            for (int64_t p = ia[r]; p < ia[r + 1]; ++p) {
-                const int64_t q = fill[ja[p]]++;
-                rja[q] = (int32_t)r;
-                rva[q] = va[p];
-            }
+    std::vector<float> lam((size_t)n * 4);
+    for (int i = 0; i < n; ++i) {
+        const double x = nodes[3 * i], y = nodes[3 * i + 1], z = nodes[3 * i + 2];
+        const double l[4] = {-0.5 * (1 + x + y + z), 0.5 * (1 + x), 0.5 * (1 + y), 0.5 * (1 + z)};
+        for (int v = 0; v < 4; ++v) lam[(size_t)i * 4 + v] = std::fabs(l[v]) > 1e-12 ? (float)l[v] : 0.0f;
     }
-    P->iG = lanes(P->nf, (int64_t)ja.size());
-    P->rG = lanes(P->nc, (int64_t)ja.size());
-    e = upv(&P->i_ia, ia);
-    if (e == cudaSuccess) e = upv(&P->i_ja, ja);
-    if (e == cudaSuccess) e = upv(&P->i_a, va);
-    if (e == cudaSuccess) e = upv(&P->r_ia, ria);
-    if (e == cudaSuccess) e = upv(&P->r_ja, rja);
-    if (e == cudaSuccess) e = upv(&P->r_a, rva);
+    float* d_lam = nullptr;
+    uint8_t* d_mc = nullptr;
+    uint32_t* cnt = nullptr;
+    cudaError_t e = upv(&d_lam, lam);
+    if (e == cudaSuccess) e = cudaMalloc(&d_mc, std::max<int64_t>(P->nc, 1));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_mc, 0, std::max<int64_t>(P->nc, 1), ctx->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&P->i_col, std::max<int64_t>(P->nf, 1) * 4 * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&P->i_val, std::max<int64_t>(P->nf, 1) * 4 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&cnt, (P->nc + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&P->r_ia, (P->nc + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, (P->nc + 1) * sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_lam); cudaFree(d_mc); cudaFree(cnt);
+        ctx->err = "pmg: allocation failed";
+        pmg_free(P); delete P;
+        return FGPU_ERR_ALLOC;
+    }
+    const uint8_t* mf = operator_mask(op32);
+    const int g4 = (int)std::max<int64_t>(1, std::min<int64_t>((nt * 4 + 255) / 256, 152 * 32));
+    const int gn = (int)std::max<int64_t>(1, std::min<int64_t>((nt * n + 255) / 256, 152 * 32));
+    const int gf = (int)std::max<int64_t>(1, std::min<int64_t>((P->nf + 255) / 256, 152 * 32));
+    pmg_cmask_kernel<<<g4, 256, 0, ctx->stream>>>(nt, n, Vf->d_l2n, Vc->d_l2n, mf, d_mc);
+    pmg_ell_kernel<<<gn, 256, 0, ctx->stream>>>(nt, n, Vf->d_l2n, Vc->d_l2n, Vf->d_inc_ptr, Vf->d_inc, mf, d_mc, d_lam, P->nf,
+                                                 P->i_col, P->i_val);
+    pmg_rcount_kernel<<<gf, 256, 0, ctx->stream>>>(P->nf, P->i_col, P->i_val, cnt);
+    ctx->launches += 3;
+    uint64_t nnzr = 0;
+    int rc = scan_u32(ctx, cnt, P->r_ia, P->nc, &nnzr);
+    if (rc == FGPU_OK) {
+        e = cudaMalloc(&P->r_ja, std::max<uint64_t>(nnzr, 1) * sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&P->r_a, std::max<uint64_t>(nnzr, 1) * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, P->r_ia, P->nc * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream);
+        if (e == cudaSuccess) {
+            pmg_rfill_kernel<<<gf, 256, 0, ctx->stream>>>(P->nf, P->i_col, P->i_val, cnt, P->r_ja, P->r_a);
+            const int gr = (int)std::max<int64_t>(1, std::min<int64_t>((P->nc + 7) / 8, 152 * 32));
+            cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+            pmg_rsort_kernel<<<gr, 256, 0, ctx->stream>>>(P->nc, P->r_ia, P->r_ja, P->r_a, ctx->d_status);
+            ctx->launches += 2;
+            int st = 0;
+            e = cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e == cudaSuccess && st) { ctx->err = "pmg: a coarse vertex restricts more than 256 fine dofs"; rc = FGPU_ERR_INVALID; }
+        }
+        if (e != cudaSuccess) { cudaGetLastError(); ctx->err = std::string("pmg: ") + cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    }
+    cudaFree(d_lam); cudaFree(d_mc); cudaFree(cnt);
+    if (rc) { pmg_free(P); delete P; return rc; }
+    P->rG = lanes(P->nc, (int64_t)nnzr);
     float** vecs[8] = {&P->rf, &P->x, &P->w, &P->q, &P->d0, &P->d1, &P->e, &P->dinv};
     for (float** p : vecs)
         if (e == cudaSuccess) e = cudaMalloc(p, std::max<int64_t>(P->nf, 1) * sizeof(float));
@@ -447,13 +564,9 @@ extern "C" int fgpu_pmg_create(fgpu_ctx* ctx, fgpu_operator* op32, const fgpu_ma
     // D^-1 of the binary32 operator (Dirichlet rows: 1)
     const float* diag = operator_diag_f32(ctx, op32);
     if (!diag) { pmg_free(P); delete P; return FGPU_ERR_CUDA; }
-    {
-        std::vector<float> hd(P->nf);
-        cudaMemcpy(hd.data(), diag, P->nf * sizeof(float), cudaMemcpyDeviceToHost);
-        for (auto& d : hd) d = d != 0.0f ? 1.0f / d : 0.0f;
-        cudaMemcpy(P->dinv, hd.data(), P->nf * sizeof(float), cudaMemcpyHostToDevice);
-    }
-    int rc = lanczos_lmax(P, 12, &P->lmax);
+    recip_kernel<<<vb_of(P->nf), 256, 0, ctx->stream>>>(P->nf, diag, P->dinv);
+    ctx->launches++;
+    rc = lanczos_lmax(P, 12, &P->lmax);
     if (rc) { pmg_free(P); delete P; return rc; }
     const double emax = 1.1 * P->lmax, emin = 0.1 * P->lmax;
     const double theta = 0.5 * (emax + emin), delta = 0.5 * (emax - emin), sigma = theta / delta;
