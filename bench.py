@@ -60,10 +60,11 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg"],
+    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "pmg"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
                         "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
-                        "AMG-preconditioned CG solve to 1e-10")
+                        "AMG-preconditioned CG solve to 1e-10; 'pmg' sets up the matrix-free Poisson operators "
+                        "(kappa = 1, perturbation 0.1h) with the P1 coarse level and runs one p-multigrid solve")
     return p.parse_args()
 
 
@@ -448,6 +449,36 @@ def run_probe_gamg(args):
     st = a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
     print(json.dumps({"iterations": st["iterations"], "time_ms": st["time_ms"], "rel_residual": st["rel_residual"],
                       "gamg": st["gamg"]}), flush=True)
+
+
+def run_probe_pmg(args):
+    """One p-multigrid matrix-free solve (mixed binary32 CG, df64 residual replacement, rtol 1e-10) of the
+    P-order Poisson problem of the matfree workload, for kernel profiling; prints iterations and times."""
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    env = fpp.Environment()
+    xyz, tets = meshgen.kuhn_box(args.n, perturb=0.1, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V, V1 = fpp.Pch(M, args.order), fpp.Pch(M, 1)
+    u, v = V.element(), V.element()
+    u1, v1 = V1.element(), V1.element()
+    integral = fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v)))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    bd = V.boundary_dofs()
+    lv = l.to_numpy()
+    lv[bd] = 0.0
+    l.vec.upload(lv)
+    op64, op32 = fpp.operator(V, integral, precision="df64"), fpp.operator(V, integral, precision="f32")
+    op64.set_dirichlet(bd)
+    op32.set_dirichlet(bd)
+    a1 = fpp.form2(test=V1, trial=V1)
+    a1.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u1), fpp.grad(v1))))
+    a1 += fpp.on(fpp.boundaryfaces(M), rhs=fpp.form1(test=V1), element=u1, expr=0.0, type="elimination_symmetric")
+    w = V.element()
+    st = op64.solve(l, w, rtol=1e-10, inner=op32, pc="pmg", coarse=a1)
+    print(json.dumps({"iterations": st["iterations"], "time_ms": st["time_ms"], "rel_residual": st["rel_residual"],
+                      "pmg": st["pmg"]}), flush=True)
 
 
 def run_matfree(args):
@@ -941,6 +972,9 @@ def main():
         return
     if args.probe == "gamg":
         run_probe_gamg(args)
+        return
+    if args.probe == "pmg":
+        run_probe_pmg(args)
         return
     if args.workload == "matfree":
         run_matfree(args)
