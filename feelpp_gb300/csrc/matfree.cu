@@ -33,66 +33,75 @@ namespace fgpu {
 // element phase
 // ---------------------------------------------------------------------------
 // binary32: one thread per element; T (7 n n floats) in shared memory.
-// binary32 element phase, two elements per thread (each reference-tensor value
-// read from shared memory serves both: the loop is bound by shared-memory loads,
-// not FMAs). The warp's 64 elements' l2n rows are staged in shared memory with
-// coalesced loads (row stride N + 1: no bank conflicts); element values are
-// written local-index-major (coalesced).
+// binary32 element phase, EPT elements per thread (each reference-tensor value
+// read from shared memory serves EPT FMAs). The warp's 32 EPT elements' l2n
+// rows are staged in shared memory with coalesced loads (row stride N + 1: no
+// bank conflicts); element values are written local-index-major (coalesced).
+template <int N>
+struct MfF32Shape {                     // elements per thread, warps per block (measured at P3 96³: four
+    static constexpr int EPT = 2;       // elements per thread in 2-warp blocks, 153 registers and 32.7 KB
+    static constexpr int WPB = 4;       // of shared memory per block, took 0.95 ms against 0.81 ms)
+};
+
 template <int N>
 __device__ __forceinline__ void mf_element_f32_body(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
                                                     const float* __restrict__ Tg, const float* __restrict__ x,
                                                     const uint8_t* __restrict__ mask, float* __restrict__ ye) {
     constexpr int NT = 7 * N * N;
-    constexpr int EW = 64;                       // elements per warp pass
+    constexpr int EPT = MfF32Shape<N>::EPT, WPB = MfF32Shape<N>::WPB;
+    constexpr int EW = 32 * EPT;                 // elements per warp pass
     __shared__ float T[NT];
-    __shared__ int32_t sl2n[4][EW * (N + 1)];
+    __shared__ int32_t sl2n[WPB][EW * (N + 1)];
     for (int k = threadIdx.x; k < NT; k += blockDim.x) T[k] = Tg[k];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int32_t* my = sl2n[warp];
-    for (int64_t e0 = ((int64_t)blockIdx.x * 4 + warp) * EW; e0 < nt; e0 += (int64_t)gridDim.x * 4 * EW) {
+    for (int64_t e0 = ((int64_t)blockIdx.x * WPB + warp) * EW; e0 < nt; e0 += (int64_t)gridDim.x * WPB * EW) {
         const int ne = (int)min((int64_t)EW, nt - e0);
         for (int k = lane; k < ne * N; k += 32) {
             const int el = k / N, j = k - el * N;
             my[el * (N + 1) + j] = __ldg(l2n + e0 * N + k);
         }
         __syncwarp();
-        // lane handles elements e0 + lane and e0 + 32 + lane
-        const bool va = lane < ne, vb = lane + 32 < ne;
-        float xa[N], xb[N];
+        // lane handles elements e0 + 32 u + lane, u < EPT
+        bool va[EPT];
+        float xs[EPT][N];
+        float c[EPT][7];
 #pragma unroll
-        for (int j = 0; j < N; ++j) {
-            const int32_t da = va ? my[lane * (N + 1) + j] : 0;
-            const int32_t db = vb ? my[(lane + 32) * (N + 1) + j] : 0;
-            xa[j] = (!va || (mask && mask[da])) ? 0.0f : __ldg(x + da);
-            xb[j] = (!vb || (mask && mask[db])) ? 0.0f : __ldg(x + db);
-        }
-        float ca[7], cb[7];
-        {
-            const int64_t ea = va ? e0 + lane : e0, eb = vb ? e0 + 32 + lane : e0;
-            const float4 a0 = __ldg(rec + 4 * ea), a1 = __ldg(rec + 4 * ea + 1);
-            const float4 b0 = __ldg(rec + 4 * eb), b1 = __ldg(rec + 4 * eb + 1);
-            ca[0] = a0.x; ca[1] = a0.y; ca[2] = a0.z; ca[3] = a0.w; ca[4] = a1.x; ca[5] = a1.y; ca[6] = a1.z;
-            cb[0] = b0.x; cb[1] = b0.y; cb[2] = b0.z; cb[3] = b0.w; cb[4] = b1.x; cb[5] = b1.y; cb[6] = b1.z;
+        for (int u = 0; u < EPT; ++u) {
+            va[u] = lane + 32 * u < ne;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const int32_t d = va[u] ? my[(lane + 32 * u) * (N + 1) + j] : 0;
+                xs[u][j] = (!va[u] || (mask && mask[d])) ? 0.0f : __ldg(x + d);
+            }
+            const int64_t e = va[u] ? e0 + 32 * u + lane : e0;
+            const float4 r0 = __ldg(rec + 4 * e), r1 = __ldg(rec + 4 * e + 1);
+            c[u][0] = r0.x; c[u][1] = r0.y; c[u][2] = r0.z; c[u][3] = r0.w; c[u][4] = r1.x; c[u][5] = r1.y; c[u][6] = r1.z;
         }
 #pragma unroll 1
         for (int i = 0; i < N; ++i) {
-            float acca = 0.0f, accb = 0.0f;
+            float acc[EPT];
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) acc[u] = 0.0f;
 #pragma unroll
             for (int k = 0; k < 7; ++k) {
                 const float* Tk = T + (k * N + i) * N;
-                float sa = 0.0f, sb = 0.0f;
+                float sm[EPT];
+#pragma unroll
+                for (int u = 0; u < EPT; ++u) sm[u] = 0.0f;
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     const float t = Tk[j];
-                    sa = fmaf(t, xa[j], sa);
-                    sb = fmaf(t, xb[j], sb);
+#pragma unroll
+                    for (int u = 0; u < EPT; ++u) sm[u] = fmaf(t, xs[u][j], sm[u]);
                 }
-                acca = fmaf(ca[k], sa, acca);
-                accb = fmaf(cb[k], sb, accb);
+#pragma unroll
+                for (int u = 0; u < EPT; ++u) acc[u] = fmaf(c[u][k], sm[u], acc[u]);
             }
-            if (va) ye[(int64_t)i * nt + e0 + lane] = acca;
-            if (vb) ye[(int64_t)i * nt + e0 + 32 + lane] = accb;
+#pragma unroll
+            for (int u = 0; u < EPT; ++u)
+                if (va[u]) ye[(int64_t)i * nt + e0 + 32 * u + lane] = acc[u];
         }
         __syncwarp();
     }
@@ -103,6 +112,26 @@ __global__ void __launch_bounds__(128) mf_element_f32_kernel(int64_t nt, const i
                                                             const float* __restrict__ Tg, const float* __restrict__ x,
                                                             const uint8_t* __restrict__ mask, float* __restrict__ ye) {
     mf_element_f32_body<N>(nt, l2n, rec, Tg, x, mask, ye);
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) mf_element_f32_gated(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
+                                                           const float* __restrict__ Tg, const float* __restrict__ x,
+                                                           const uint8_t* __restrict__ mask, float* __restrict__ ye,
+                                                           const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    mf_element_f32_body<N>(nt, l2n, rec, Tg, x, mask, ye);
+}
+
+// launch shape of the binary32 element phase: 32 WPB threads per block, enough blocks for one pass
+template <int N>
+static void launch_mf_element_f32(cudaStream_t st, int64_t nt, const int32_t* l2n, const float4* rec, const float* T7f,
+                                  const float* x, const uint8_t* mask, float* ye, const int* stop, bool gated) {
+    constexpr int WPB = MfF32Shape<N>::WPB, EW = 32 * MfF32Shape<N>::EPT;
+    const int64_t per_block = (int64_t)WPB * EW;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nt + per_block - 1) / per_block, 152 * 32));
+    if (gated) mf_element_f32_gated<N><<<blocks, 32 * WPB, 0, st>>>(nt, l2n, rec, T7f, x, mask, ye, stop);
+    else mf_element_f32_kernel<N><<<blocks, 32 * WPB, 0, st>>>(nt, l2n, rec, T7f, x, mask, ye);
 }
 
 // native binary64: one thread per element (FP64 pipe), coefficients from the
@@ -403,9 +432,9 @@ int operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const void* x, void* y) {
         if (rc) return rc;
     } else if (op->precision == FGPU_F32) {
         switch (n) {
-            case 4: mf_element_f32_kernel<4><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye); break;
-            case 10: mf_element_f32_kernel<10><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye); break;
-            case 20: mf_element_f32_kernel<20><<<eb, 128, 0, ctx->stream>>>(nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye); break;
+            case 4: launch_mf_element_f32<4>(ctx->stream, nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, nullptr, false); break;
+            case 10: launch_mf_element_f32<10>(ctx->stream, nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, nullptr, false); break;
+            case 20: launch_mf_element_f32<20>(ctx->stream, nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, nullptr, false); break;
             default: return FGPU_ERR_INVALID;
         }
     } else if (op->precision == FGPU_F64) {
@@ -533,14 +562,7 @@ __global__ void mf_gather_dot_kernel(int64_t nnodes, int64_t nt, const int64_t* 
 }
 
 // element phase gated by the CG stop flag (runs inside the captured graph)
-template <int N>
-__global__ void __launch_bounds__(128) mf_element_f32_gated(int64_t nt, const int32_t* __restrict__ l2n, const float4* __restrict__ rec,
-                                                           const float* __restrict__ Tg, const float* __restrict__ x,
-                                                           const uint8_t* __restrict__ mask, float* __restrict__ ye,
-                                                           const int* __restrict__ stop) {
-    if (stop && *stop) return;
-    mf_element_f32_body<N>(nt, l2n, rec, Tg, x, mask, ye);
-}
+
 
 template <typename T>
 __global__ void copy_cast_kernel(int64_t n, const double* __restrict__ a, T* __restrict__ b) {
@@ -612,9 +634,9 @@ static int mf_apply_cg(fgpu_ctx* ctx, fgpu_operator* op, const typename PL::S* x
         launch_mf_element_tc(ctx, n, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop);
     } else if (op->precision == FGPU_F32) {
         switch (n) {
-            case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
-            case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
-            default: mf_element_f32_gated<20><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+            case 4: launch_mf_element_f32<4>(ctx->stream, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop, true); break;
+            case 10: launch_mf_element_f32<10>(ctx->stream, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop, true); break;
+            default: launch_mf_element_f32<20>(ctx->stream, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop, true); break;
         }
     } else {
         // binary64 element phases (native or df64); not gated: the FP64 matrix-free solve polls every iteration
@@ -661,9 +683,9 @@ int mf_apply_f32_gated(fgpu_ctx* ctx, fgpu_operator* op, const float* x, float* 
         launch_mf_element_tc(ctx, n, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop);
     } else {
         switch (n) {
-            case 4: mf_element_f32_gated<4><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
-            case 10: mf_element_f32_gated<10><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
-            default: mf_element_f32_gated<20><<<eb, 128, 0, ctx->stream>>>(op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop); break;
+            case 4: launch_mf_element_f32<4>(ctx->stream, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop, true); break;
+            case 10: launch_mf_element_f32<10>(ctx->stream, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop, true); break;
+            default: launch_mf_element_f32<20>(ctx->stream, op->nt, V->d_l2n, op->d_rec, op->tab->d_T7f, xe, me, (float*)op->d_ye, stop, true); break;
         }
     }
     mf_gather_f32_stop_kernel<<<blocks_for(op->nnodes, 256, 152 * 16), 256, 0, ctx->stream>>>(
