@@ -9,12 +9,12 @@ from ._ffi import FgpuError  # noqa: F401
 from .fe import (  # noqa: F401
     Environment, Mesh, FunctionSpace, Pch, Pchv, Element, DeviceVector, Form1, Form2, form1, form2, integrate,
     elements, boundaryfaces, markedfaces, gradt, grad, idt, id, inner, stress, on, cst, cst_vec, sine_source,
-    environment, Operator, operator, DeviceScalar, DirichletBC, Graph, capture, Batch, N, hFace, AMG, PMG,
+    environment, Operator, operator, DeviceScalar, DirichletBC, Graph, capture, Batch, N, hFace, AMG, PMG, export_ensight,
 )
 
 __all__ = [
     "Environment", "Mesh", "FunctionSpace", "Pch", "Pchv", "Element", "DeviceVector", "Form1", "Form2", "form1",
     "form2", "integrate", "elements", "boundaryfaces", "markedfaces", "gradt", "grad", "idt", "id", "inner", "stress",
     "on", "cst", "cst_vec", "sine_source", "environment", "meshgen", "FgpuError", "Operator", "operator",
-    "DeviceScalar", "DirichletBC", "Graph", "capture", "Batch", "N", "hFace", "AMG", "PMG",
+    "DeviceScalar", "DirichletBC", "Graph", "capture", "Batch", "N", "hFace", "AMG", "PMG", "export_ensight",
 ]

@@ -939,6 +939,17 @@ class Operator:
             pass
 
 
+def export_ensight(space, prefix, fields):
+    """Write the mesh and nodal fields ({name: Element}) of a scalar space as EnSight Gold files
+    prefix.case, prefix.geo, prefix.<name>.scl (values at the vertices), the reference's default
+    exporter format."""
+    names = list(fields)
+    arr_n = (C.c_char_p * max(len(names), 1))(*[n.encode() for n in names])
+    arr_f = (C.c_void_p * max(len(names), 1))(*[fields[n].h for n in names])
+    space.env.check(space.env.lib.fgpu_export_ensight(space.h, str(prefix).encode(), len(names),
+                                                      C.cast(arr_n, C.c_void_p), C.cast(arr_f, C.c_void_p)))
+
+
 def operator(test, integral, precision="f32"):
     return Operator(test, integral, precision)
 

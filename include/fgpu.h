@@ -313,6 +313,13 @@ int fgpu_amg_host_export(const fgpu_amg_host* h, int level, int64_t* ia, int32_t
 int fgpu_amg_host_coarse_inverse(const fgpu_amg_host* h, double* out);
 int fgpu_amg_host_destroy(fgpu_amg_host* h);
 
+/* ---- EnSight Gold export (the reference's default exporter, feelpp/feel/feelfilters/exporterensightgold.hpp):
+ *      writes prefix.case, prefix.geo (C Binary, one part of tetra4, vertex coordinates) and
+ *      prefix.<name>.scl per field (values at the vertices: the vertex dofs of the scalar space V).
+ *      Field names: 1-19 characters among letters, digits and '_'. ---- */
+int fgpu_export_ensight(const fgpu_space* V, const char* prefix, int nfields, const char* const* names,
+                        const fgpu_vector* const* fields);
+
 /* ---- error norms of a scalar field against u = sin(pi x) sin(pi y) sin(pi z):
  *      normL2(u_h - u) and the H1 seminorm (feelpp/feel/feelvf/norml2.hpp:37, normh1.hpp) ---- */
 int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, int quad_degree, double* l2, double* h1);
