@@ -1217,8 +1217,9 @@ __global__ void __launch_bounds__(256) batch_gather_map_kernel(int nprob, const 
         const int64_t k = g - pz0;
         const uint32_t p0 = __ldg(P.gptr + k), p1 = __ldg(P.gptr + k + 1);
         if (MODE == kModeDF64) {
+            // the single-matrix gather's compensated sum (same bits)
             const float2* kb = reinterpret_cast<const float2*>(P.kbuf);
-            df s{0.0f, 0.0f};
+            float sh = 0.0f, sl = 0.0f;
             for (uint32_t q = p0; q < p1; q += 4) {
                 uint32_t ix[4];
                 float2 v[4];
@@ -1228,8 +1229,13 @@ __global__ void __launch_bounds__(256) batch_gather_map_kernel(int nprob, const 
                 for (int u = 0; u < 4; ++u) v[u] = q + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    if (q + u < p1) s = (q + u == p0) ? df{v[u].x, v[u].y} : df_add(s, df{v[u].x, v[u].y});
+                    if (q + u < p1) {
+                        const df t = two_sum(sh, v[u].x);
+                        sh = t.hi;
+                        sl = f_add(sl, f_add(t.lo, v[u].y));
+                    }
             }
+            df s = two_sum(sh, sl);
             double* out = reinterpret_cast<double*>(P.val) + k;
             if (accumulate) s = df_add(d2df(*out), s);
             *out = df2d(s);
@@ -1393,8 +1399,10 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t p0 = __ldg(gptr + k), p1 = __ldg(gptr + k + 1);
         if (MODE == kModeDF64) {
+            // compensated sum in element order: the high parts through TwoSum, their rounding errors and
+            // the low parts in one binary32 accumulator, normalised once (error ~ (count) u^2 |sum|)
             const float2* kb = reinterpret_cast<const float2*>(kbuf);
-            df s{0.0f, 0.0f};
+            float sh = 0.0f, sl = 0.0f;
             for (uint32_t p = p0; p < p1; p += 4) {
                 uint32_t ix[4];
                 float2 v[4];
@@ -1404,8 +1412,13 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
                 for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    if (p + u < p1) s = (p + u == p0) ? df{v[u].x, v[u].y} : df_add(s, df{v[u].x, v[u].y});
+                    if (p + u < p1) {
+                        const df t = two_sum(sh, v[u].x);
+                        sh = t.hi;
+                        sl = f_add(sl, f_add(t.lo, v[u].y));
+                    }
             }
+            df s = two_sum(sh, sl);
             double* out = reinterpret_cast<double*>(valv) + k;
             if (accumulate) s = df_add(d2df(*out), s);
             *out = df2d(s);
