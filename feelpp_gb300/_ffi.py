@@ -112,6 +112,7 @@ SIGNATURES = {
     "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),
     "fgpu_amg_destroy": (i32, [P]),
     "fgpu_mesh_set_ho_nodes": (i32, [P, P]),
+    "fgpu_assemble_matrix_host": (i32, [P, P, C.POINTER(FormDesc), P]),
     "fgpu_export_ensight": (i32, [P, C.c_char_p, i32, P, P]),
     "fgpu_pmg_create": (i32, [P, P, P, P, C.POINTER(PmgCfg), PP]),
     "fgpu_pmg_info": (i32, [P, DP, P, DP]),

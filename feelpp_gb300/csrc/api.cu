@@ -607,6 +607,48 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     return assemble_impl(ctx, A, f, A->d_kappa_stage, accumulate);
 }
 
+int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, double* host_val) {
+    if (!ctx || !A || !f || !host_val) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix_host: bad arguments");
+    FGPU_NO_CAPTURE(ctx, "assemble_matrix_host");
+    fgpu_space* V = A->space;
+    const int64_t nt = V->mesh->nt;
+    const double* d_kappa = nullptr;
+    if (f->kappa_elem) {
+        if (!A->d_kappa_stage) {
+            int rc = dev_alloc(ctx, &A->d_kappa_stage, nt);
+            if (rc) return rc;
+        }
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(A->d_kappa_stage, f->kappa_elem, nt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        d_kappa = A->d_kappa_stage;
+    }
+    int algo = f->algo;
+    if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(ctx, A);
+    const bool pipelined = f->kind == FGPU_FORM_LAPLACE_MASS && f->range == FGPU_RANGE_ELEMENTS && f->mass_h == 0.0 &&
+                           f->dn_trial == 0.0 && f->dn_test == 0.0 && A->precision == FGPU_F64 && A->ncomp == 1 &&
+                           !V->mesh->d_ho && algo == FGPU_ALGO_TWO_PHASE;
+    if (!pipelined) {
+        int rc = assemble_impl(ctx, A, f, d_kappa, 0);
+        if (rc) return rc;
+        return fgpu_matrix_get_csr(A, nullptr, nullptr, host_val);
+    }
+    std::string err;
+    DevTables* tab = get_dev_tables(V->order, form_qdeg(V, f->quad_degree), err);
+    if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
+    if (A->coef_cap < nt * 8) {
+        cudaFree(A->d_coef);
+        A->d_coef = nullptr;
+        A->coef_cap = 0;
+        int rc = dev_alloc(ctx, &A->d_coef, nt * 8);
+        if (rc) return rc;
+        A->coef_cap = nt * 8;
+    }
+    int rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef), f->kappa_scale);
+    if (rc) return rc;
+    rc = launch_assemble_two_phase_host(ctx, A, tab, reinterpret_cast<const float4*>(A->d_coef), host_val);
+    if (rc) return rc;
+    return finish(ctx);
+}
+
 int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
     return assemble_impl(ctx, A, f, d_kappa, accumulate);
 }

@@ -1539,7 +1539,8 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
 }
 
 template <int MODE, int N>
-static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate,
+                         double* host = nullptr) {
     fgpu_space* V = A->space;
     const int64_t nt = V->mesh->nt;
     constexpr int NTRI = N * (N + 1) / 2;
@@ -1569,6 +1570,7 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     }
+    if (host) return launch_gather_phase_to_host(ctx, A, host, 4);
     const int64_t nnz = A->pattern->nnz;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, (int64_t)sms * 32));
     PendingEvent ev;
@@ -1616,6 +1618,41 @@ int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate) {
     return FGPU_OK;
 }
 
+// Phase 2 in nchunks ranges of CSR entries, each range copied to host memory (pinned for overlap) on
+// its own copy stream as soon as its gather ends: the copies of earlier ranges overlap the gathers of
+// later ones. FP64 matrices.
+int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int nchunks) {
+    fgpu_space* V = A->space;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t nnz = A->pattern->nnz;
+    nchunks = std::max(1, std::min(nchunks, 4));
+    if (!ctx->copy_streams[0]) {
+        for (int i = 0; i < 4; ++i) FGPU_CUDA_CHECK(ctx, cudaStreamCreateWithFlags(&ctx->copy_streams[i], cudaStreamNonBlocking));
+        for (int i = 0; i < 5; ++i) FGPU_CUDA_CHECK(ctx, cudaEventCreateWithFlags(&ctx->copy_events[i], cudaEventDisableTiming));
+    }
+    const int64_t chunk = ((nnz + nchunks - 1) / nchunks + 255) & ~(int64_t)255;
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_gather", ev);
+    for (int c = 0; c < nchunks; ++c) {
+        const int64_t k0 = (int64_t)c * chunk;
+        if (k0 >= nnz) break;
+        const int64_t k1 = std::min(nnz, k0 + chunk);
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((k1 - k0 + 255) / 256, (int64_t)sms * 32));
+        gather_map_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(k1 - k0, V->d_gptr + k0, V->d_gidx, A->d_kbuf,
+                                                                         (double*)A->d_val + k0, 0);
+        ctx->launches++;
+        FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+        FGPU_CUDA_CHECK(ctx, cudaEventRecord(ctx->copy_events[c], ctx->stream));
+        FGPU_CUDA_CHECK(ctx, cudaStreamWaitEvent(ctx->copy_streams[c], ctx->copy_events[c], 0));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(host + k0, (const double*)A->d_val + k0, (k1 - k0) * sizeof(double),
+                                             cudaMemcpyDeviceToHost, ctx->copy_streams[c]));
+    }
+    prof_end(ctx, ev);
+    for (int c = 0; c < nchunks; ++c) FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->copy_streams[c]));
+    return FGPU_OK;
+}
+
 int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate) {
     const int64_t nn = V->topo.nnodes;
     const int64_t gb = std::max<int64_t>(1, std::min<int64_t>((nn + 255) / 256, 152 * 16));
@@ -1625,6 +1662,16 @@ int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, 
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
+}
+
+int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, double* host) {
+    if (A->ncomp != 1 || A->precision != FGPU_F64) { ctx->err = "assemble to host: scalar FP64 matrices"; return FGPU_ERR_INVALID; }
+    switch (A->space->order) {
+        case 1: return run_two_phase<kModeDF64, 4>(ctx, A, tab, rec, 0, host);
+        case 2: return run_two_phase<kModeDF64, 10>(ctx, A, tab, rec, 0, host);
+        case 3: return run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, 0, host);
+        default: ctx->err = "unsupported order"; return FGPU_ERR_INVALID;
+    }
 }
 
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {

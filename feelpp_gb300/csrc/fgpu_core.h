@@ -294,6 +294,8 @@ const float* operator_diag_f32(fgpu_ctx* ctx, fgpu_operator* op);
 int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x, int cycles);
 int64_t amg_rows(const fgpu_amg* M);
 int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
+int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, double* host);
+int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int nchunks);
 int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);
 int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate);
 int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate);

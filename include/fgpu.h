@@ -235,6 +235,11 @@ int fgpu_matrix_destroy(fgpu_matrix* A);
  *      feelpp/feel/feelalg/matrixpetsc.cpp:919-935). accumulate = 0 for '=', 1 for '+='. ---- */
 int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, int accumulate);
 /* same, with the per-element coefficient already on the device (T doubles) */
+/* assemble (accumulate = 0) and write the values to host memory (nnz doubles, CSR order): for the
+ * two-phase FP64 Laplace/mass path the gather runs in four ranges of entries and each range is copied
+ * to the host while the next is gathered (pin host_val for the overlap); other forms assemble, then
+ * copy. The device values are the same as after fgpu_assemble_matrix. */
+int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, double* host_val);
 int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, const double* d_kappa,
                              int accumulate);
 

@@ -231,3 +231,27 @@ def test_elasticity_two_phase_vs_native(env, order, precision):
         got.append(a.values())
     tol = 2e-6 if precision == "f32" else 1e-13
     assert_values_close(got[1], got[0], rtol=tol, atol=tol, what="elasticity two-phase vs gather")
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_assemble_matrix_host(env, precision):
+    """fgpu_assemble_matrix_host (pipelined gather + copies for FP64, assemble-then-copy otherwise) gives the
+    values of fgpu_assemble_matrix followed by a copy."""
+    import ctypes as C
+    from feelpp_gb300 import _ffi, fe
+    xyz, tets = mesh(8, perturb=0.2)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    u, v = V.element(), V.element()
+    integral = fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v))
+    a = fpp.form2(test=V, trial=V, precision=precision)
+    a.assign(integral)
+    ref = a.values().astype(np.float64)
+    d, karr = fe.Form2._desc_of(integral, _ffi.ALGO_AUTO)
+    d.kappa_elem = karr.ctypes.data_as(C.c_void_p)
+    out = np.zeros(a.nnz)
+    a.zero()
+    env.check(env.lib.fgpu_assemble_matrix_host(env.h, a.h, C.byref(d), out.ctypes.data_as(C.c_void_p)))
+    assert np.array_equal(out, ref)
+    assert np.array_equal(a.values().astype(np.float64), ref)
