@@ -1391,7 +1391,8 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 // warp); a split into entries with at most 2 contributions (one unrolled step,
 // 0.21 ms, 70 % of DRAM peak) and the others taken from a list sorted by count
 // (0.30 ms: the sorted list scatters the reads of the element buffer, 1.75 GB
-// of DRAM reads for 5.4 M entries).
+// of DRAM reads for 5.4 M entries). At P2 64^3 two entries per thread (k and
+// k + stride, loads issued together) took 0.90 ms against 0.655 ms.
 template <int MODE>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
