@@ -232,6 +232,7 @@ int fgpu_mesh_set_coords(fgpu_mesh* M, const double* xyz) {
     FGPU_NO_CAPTURE(ctx, "mesh_set_coords");
     FGPU_CUDA_CHECK(ctx, cudaMemcpyAsync(M->d_xyz, xyz, 3 * M->nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     M->h_xyz_stale = true;           // the host copy is refreshed when a host-side query needs it
+    M->coords_version++;
     return FGPU_OK;
 }
 
@@ -320,7 +321,19 @@ int fgpu_space_boundary_dofs(const fgpu_space* V, int xmax_on, double xmax, int6
         FGPU_CUDA_CHECK(V->ctx, cudaStreamSynchronize(V->ctx->stream));
         V->mesh->h_xyz_stale = false;
     }
-    boundary_nodes(V->mesh->nt, V->mesh->h_tets.data(), V->mesh->h_xyz.data(), V->topo, xmax_on, xmax, nodes);
+    // the last result is kept (callers ask for the count, then the list)
+    fgpu_space* W = const_cast<fgpu_space*>(V);
+    if (W->bnd_valid && W->bnd_xmax_on == xmax_on && (!xmax_on || W->bnd_xmax == xmax) && W->bnd_coords == W->mesh->coords_version) {
+        nodes = W->bnd_nodes;
+    } else {
+        if (boundary_nodes_device(V->ctx, V, xmax_on, xmax, nodes) != FGPU_OK)
+            boundary_nodes(V->mesh->nt, V->mesh->h_tets.data(), V->mesh->h_xyz.data(), V->topo, xmax_on, xmax, nodes);
+        W->bnd_nodes = nodes;
+        W->bnd_xmax_on = xmax_on;
+        W->bnd_xmax = xmax;
+        W->bnd_coords = W->mesh->coords_version;
+        W->bnd_valid = true;
+    }
     *count = (int64_t)nodes.size() * V->ncomp;
     if (dofs)
         for (size_t k = 0; k < nodes.size(); ++k)

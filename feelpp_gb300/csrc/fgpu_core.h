@@ -158,6 +158,7 @@ struct fgpu_mesh {
     int64_t nv = 0, nt = 0;
     std::vector<double> h_xyz;       // host copy (refreshed from the device when stale)
     bool h_xyz_stale = false;
+    uint64_t coords_version = 0;     // incremented whenever the coordinates change
     std::vector<int32_t> h_tets;
     double* d_xyz = nullptr;
     int32_t* d_tets = nullptr;
@@ -198,6 +199,11 @@ struct fgpu_space {
         std::vector<int64_t> colour_ptr;
     };
     std::vector<FaceSet> face_sets;
+    std::vector<int32_t> bnd_nodes;  // last boundary-dof query (range, xmax, coordinates version)
+    bool bnd_valid = false;
+    int bnd_xmax_on = 0;
+    double bnd_xmax = 0;
+    uint64_t bnd_coords = 0;
     uint32_t* d_gptr = nullptr;      // two-phase gather map: nnz + 1 offsets into d_gidx
     uint32_t* d_gidx = nullptr;      // T n n element-buffer indices, per CSR entry in element order
 };
@@ -300,6 +306,7 @@ int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);
 int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate);
 int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate);
 int launch_rhs_ho(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate);
+int boundary_nodes_device(fgpu_ctx* ctx, const fgpu_space* V, int xmax_on, double xmax, std::vector<int32_t>& nodes);
 int launch_face_matrix(fgpu_ctx* ctx, fgpu_matrix* A, int range, double xmax, double mass, double mass_h, double dn_trial,
                        double dn_test, int accumulate);
 int launch_face_load(fgpu_ctx* ctx, const fgpu_space* V, int range, double xmax, double g, double g_h, double g_dn,

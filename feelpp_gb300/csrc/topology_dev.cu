@@ -255,21 +255,28 @@ int sort_buffer_size(int64_t need) {
 // Builds V->d_l2n, d_inc_ptr, d_inc and the host copies topo.l2n / nnodes
 // (used by the host queries). Returns FGPU_ERR_INVALID with an empty message
 // when the mesh is outside this path's limits (the caller then uses the host path).
+// reference-element tables in constant memory, once per device
+static int ensure_tables(fgpu_ctx* ctx) {
+    static std::mutex mu;
+    static std::vector<char> done(256, 0);
+    std::lock_guard<std::mutex> lock(mu);
+    if (ctx->device < 0 || ctx->device >= 256) return FGPU_ERR_INVALID;
+    if (!done[ctx->device]) {
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyToSymbol(c_edge_verts, kEdgeVerts, sizeof(int) * 12));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpyToSymbol(c_face_verts, kFaceVerts, sizeof(int) * 12));
+        done[ctx->device] = 1;
+    }
+    return FGPU_OK;
+}
+
 int build_space_device(fgpu_ctx* ctx, fgpu_space* V) {
     const fgpu_mesh* M = V->mesh;
     const int64_t nt = M->nt, nv = M->nv;
     const int order = V->order, n = V->n, ndpe = dofs_per_edge(order), ndpf = dofs_per_face(order);
     if (nv >= ((int64_t)1 << 21) || nt * 14 >= (int64_t)0xFFFFFFFF || nt >= ((int64_t)1 << 26)) return FGPU_ERR_INVALID;
-    {   // reference-element tables, once per device
-        static std::mutex mu;
-        static std::vector<char> done(256, 0);
-        std::lock_guard<std::mutex> lock(mu);
-        if (ctx->device < 0 || ctx->device >= 256) return FGPU_ERR_INVALID;
-        if (!done[ctx->device]) {
-            FGPU_CUDA_CHECK(ctx, cudaMemcpyToSymbol(c_edge_verts, kEdgeVerts, sizeof(int) * 12));
-            FGPU_CUDA_CHECK(ctx, cudaMemcpyToSymbol(c_face_verts, kFaceVerts, sizeof(int) * 12));
-            done[ctx->device] = 1;
-        }
+    {
+        const int rc = ensure_tables(ctx);
+        if (rc) return rc;
     }
     // the host path's input checks: vertex range and repeated vertices
     for (int64_t k = 0; k < nt; ++k) {
@@ -374,6 +381,112 @@ int build_space_device(fgpu_ctx* ctx, fgpu_space* V) {
 
 // Scalar node pattern on the device from the incidence lists (after build_space_device
 // or the host topology upload). Fills P (device ia/ja, nnz, max_row) and the host ia.
+namespace {
+
+// boundary faces: every local face is inserted in a face hash with an occurrence count
+__global__ void face_count_kernel(int64_t nt, const int32_t* __restrict__ tets, unsigned long long* __restrict__ ftab, uint32_t fmask,
+                                  uint32_t* __restrict__ occ, uint32_t* __restrict__ cnt, int* __restrict__ status) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt * 4; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t >> 2;
+        const int f = (int)(t & 3);
+        int a = tets[4 * e + c_face_verts[f][0]], b = tets[4 * e + c_face_verts[f][1]], c = tets[4 * e + c_face_verts[f][2]];
+        if (a > b) { const int x = a; a = b; b = x; }
+        if (b > c) { const int x = b; b = c; c = x; }
+        if (a > b) { const int x = a; a = b; b = x; }
+        const unsigned long long key = ((unsigned long long)a << 42) | ((unsigned long long)b << 21) | (unsigned long long)c;
+        const uint32_t sl = hash_insert(ftab, fmask, key, status);
+        occ[t] = sl;
+        atomicAdd(cnt + sl, 1u);
+    }
+}
+
+// the nodes carried by faces of one element (with xmax_on: whose vertices all have x <= xmax)
+__global__ void boundary_mark_kernel(int64_t nt, const int32_t* __restrict__ tets, const double* __restrict__ xyz, int n,
+                                     const int32_t* __restrict__ l2n, const uint32_t* __restrict__ occ, const uint32_t* __restrict__ cnt,
+                                     const int* __restrict__ fl, int nfl, int xmax_on, double xmax, uint8_t* __restrict__ mark) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt * 4; t += (int64_t)gridDim.x * blockDim.x) {
+        if (cnt[occ[t]] != 1) continue;
+        const int64_t e = t >> 2;
+        const int f = (int)(t & 3);
+        if (xmax_on) {
+            bool ok = true;
+            for (int v = 0; v < 3; ++v) ok = ok && xyz[3 * (int64_t)tets[4 * e + c_face_verts[f][v]]] <= xmax + 1e-12;
+            if (!ok) continue;
+        }
+        for (int k = 0; k < nfl; ++k) mark[l2n[e * n + fl[f * nfl + k]]] = 1;
+    }
+}
+
+}  // namespace
+
+// Boundary dof nodes on the device (the host restatement is topology.cpp boundary_nodes): FGPU_OK, or
+// FGPU_ERR_INVALID when the mesh is too large for the packed face keys (the caller then uses the host).
+int boundary_nodes_device(fgpu_ctx* ctx, const fgpu_space* V, int xmax_on, double xmax, std::vector<int32_t>& nodes) {
+    const fgpu_mesh* M = V->mesh;
+    const int64_t nt = M->nt;
+    if (M->nv >= ((int64_t)1 << 21) || nt == 0) return FGPU_ERR_INVALID;
+    if (ensure_tables(ctx) != FGPU_OK) return FGPU_ERR_INVALID;
+    const int ndpe = dofs_per_edge(V->order), ndpf = dofs_per_face(V->order);
+    std::vector<int> fl;
+    int nfl = 0;
+    for (int f = 0; f < 4; ++f) {
+        std::vector<int> d;
+        for (int v = 0; v < 3; ++v) d.push_back(kFaceVerts[f][v]);
+        for (int j = 0; j < 6; ++j) {
+            const int a = kEdgeVerts[j][0], b = kEdgeVerts[j][1];
+            bool ina = false, inb = false;
+            for (int v = 0; v < 3; ++v) {
+                ina |= kFaceVerts[f][v] == a;
+                inb |= kFaceVerts[f][v] == b;
+            }
+            if (ina && inb)
+                for (int l = 0; l < ndpe; ++l) d.push_back(4 + j * ndpe + l);
+        }
+        for (int l = 0; l < ndpf; ++l) d.push_back(4 + 6 * ndpe + f * ndpf + l);
+        nfl = (int)d.size();
+        fl.insert(fl.end(), d.begin(), d.end());
+    }
+    uint32_t cap = 1;
+    while (cap < (uint32_t)std::min<int64_t>(4 * nt, (int64_t)1 << 31)) cap <<= 1;
+    const int64_t nnodes = V->topo.nnodes;
+    unsigned long long* ftab = nullptr;
+    uint32_t *occ = nullptr, *cnt = nullptr;
+    int* dfl = nullptr;
+    uint8_t* mark = nullptr;
+    auto cleanup = [&]() { cudaFree(ftab); cudaFree(occ); cudaFree(cnt); cudaFree(dfl); cudaFree(mark); };
+    cudaError_t e = cudaMalloc(&ftab, (size_t)cap * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&cnt, (size_t)cap * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&occ, (size_t)nt * 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&dfl, fl.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&mark, std::max<int64_t>(nnodes, 1));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ftab, 0xFF, (size_t)cap * sizeof(unsigned long long), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, (size_t)cap * sizeof(uint32_t), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mark, 0, std::max<int64_t>(nnodes, 1), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dfl, fl.data(), fl.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+    if (e != cudaSuccess) { cudaGetLastError(); cleanup(); return FGPU_ERR_INVALID; }
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nt * 4 + 255) / 256, 152 * 32));
+    face_count_kernel<<<blocks, 256, 0, ctx->stream>>>(nt, M->d_tets, ftab, cap - 1, occ, cnt, ctx->d_status);
+    boundary_mark_kernel<<<blocks, 256, 0, ctx->stream>>>(nt, M->d_tets, M->d_xyz, V->n, V->d_l2n, occ, cnt, dfl, nfl, xmax_on, xmax,
+                                                          mark);
+    ctx->launches += 2;
+    int st = 0;
+    std::vector<uint8_t> hm(nnodes);
+    e = cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hm.data(), mark, nnodes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    if (e != cudaSuccess) { ctx->err = std::string("boundary dofs: ") + cudaGetErrorString(e); return FGPU_ERR_CUDA; }
+    if (st & kStatusTableFull) {
+        cudaMemset(ctx->d_status, 0, sizeof(int));
+        return FGPU_ERR_INVALID;
+    }
+    nodes.clear();
+    for (int64_t r = 0; r < nnodes; ++r)
+        if (hm[r]) nodes.push_back((int32_t)r);
+    return FGPU_OK;
+}
+
 int build_pattern_device(fgpu_ctx* ctx, fgpu_space* V, DevPattern& P, std::vector<int64_t>& h_ia) {
     const int64_t N = V->topo.nnodes;
     const int n = V->n;

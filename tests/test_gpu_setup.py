@@ -74,3 +74,25 @@ def test_device_setup_assembly_matches_oracle_on_shuffled_mesh(env, oracle):
     dia, dja, dval = a.csr()
     assert np.array_equal(dia, ia) and np.array_equal(dja, ja)
     assert_values_close(dval, val)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_boundary_dofs_device_match_oracle(env, oracle, order):
+    """Boundary dofs found on the device (face hash with occurrence counts) equal the oracle's, for the
+    whole boundary and for a marked plane; repeated queries and moved coordinates stay right."""
+    from tests.helpers import mesh
+    xyz, tets = mesh(5, perturb=0.2)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, order)
+    N, l2g = oracle.dof_table(tets, order)
+    for xplane in (None, 0.0):
+        mask = oracle.boundary_mask(order, xyz, tets, l2g, N, xplane=xplane)
+        got = V.boundary_dofs(xplane)
+        assert np.array_equal(got, np.nonzero(mask)[0])
+        assert np.array_equal(V.boundary_dofs(xplane), got)
+    # moving the mesh changes which faces lie on x <= 0
+    xyz2 = xyz.copy()
+    xyz2[:, 0] -= 0.5
+    M.set_coords(xyz2)
+    mask = oracle.boundary_mask(order, xyz2, tets, l2g, N, xplane=0.0)
+    assert np.array_equal(V.boundary_dofs(0.0), np.nonzero(mask)[0])
