@@ -52,6 +52,15 @@ void parallel_rows(int nthreads, int64_t n, const std::function<void(int, int64_
     for (auto& x : th) x.join();
 }
 
+// fn(chunk, r0, r1) over fixed chunks of `chunk` rows, the chunks spread over the threads: per-chunk
+// partial sums combined in chunk order do not depend on the thread count
+void parallel_chunks(int nthreads, int64_t n, int64_t chunk, const std::function<void(int64_t, int64_t, int64_t)>& fn) {
+    const int64_t nc = (n + chunk - 1) / chunk;
+    parallel_rows(nthreads, nc * 4096, [&](int, int64_t c0, int64_t c1) {
+        for (int64_t c = c0 / 4096; c < c1 / 4096; ++c) fn(c, c * chunk, std::min(n, (c + 1) * chunk));
+    });
+}
+
 // C = A * B (rows of A times B), Gustavson with a dense accumulator; columns
 // of every row sorted. Each entry sums its products in (A column, B column) order.
 void spgemm(const HostCsr& A, const HostCsr& B, HostCsr& C, int nthreads) {
@@ -145,30 +154,42 @@ double lmax_estimate(const HostCsr& A, const std::vector<double>& d, int m, int 
     std::vector<double> al, be;
     double bprev = 0;
     const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, (n + 4095) / 4096));
-    std::vector<double> part(T);
+    constexpr int64_t kChunk = 16384;
+    const int64_t nch = (n + kChunk - 1) / kChunk;
+    std::vector<double> pa(nch), pb(nch);
     for (int k = 0; k < m; ++k) {
-        parallel_rows(T, n, [&](int, int64_t r0, int64_t r1) {
+        parallel_chunks(T, n, kChunk, [&](int64_t c, int64_t r0, int64_t r1) {
+            double sa = 0;
             for (int64_t i = r0; i < r1; ++i) {
                 double acc = 0;
                 for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p) acc += A.a[p] * s[A.ja[p]] * v[A.ja[p]];
                 w[i] = s[i] * acc;
+                sa += w[i] * v[i];
             }
+            pa[c] = sa;
         });
         double a = 0;
-        for (int64_t i = 0; i < n; ++i) a += w[i] * v[i];
+        for (int64_t c = 0; c < nch; ++c) a += pa[c];
+        parallel_chunks(T, n, kChunk, [&](int64_t c, int64_t r0, int64_t r1) {
+            double sb = 0;
+            for (int64_t i = r0; i < r1; ++i) {
+                w[i] -= a * v[i] + bprev * vold[i];
+                sb += w[i] * w[i];
+            }
+            pb[c] = sb;
+        });
         double b = 0;
-        for (int64_t i = 0; i < n; ++i) {
-            w[i] -= a * v[i] + bprev * vold[i];
-            b += w[i] * w[i];
-        }
+        for (int64_t c = 0; c < nch; ++c) b += pb[c];
         b = std::sqrt(b);
         al.push_back(a);
         if (b < 1e-14 * std::fabs(a) || k + 1 == m) break;
         be.push_back(b);
-        for (int64_t i = 0; i < n; ++i) {
-            vold[i] = v[i];
-            v[i] = w[i] / b;
-        }
+        parallel_rows(T, n, [&](int, int64_t r0, int64_t r1) {
+            for (int64_t i = r0; i < r1; ++i) {
+                vold[i] = v[i];
+                v[i] = w[i] / b;
+            }
+        });
         bprev = b;
     }
     // largest eigenvalue of the tridiagonal (al, be) by Sturm bisection
@@ -200,7 +221,8 @@ double lmax_estimate(const HostCsr& A, const std::vector<double>& d, int m, int 
 }
 
 // strong neighbours (symmetrised, without the diagonal) as a CSR graph
-void strength(const HostCsr& A, const std::vector<double>& d, double theta, std::vector<int64_t>& sp, std::vector<int32_t>& sj) {
+void strength(const HostCsr& A, const std::vector<double>& d, double theta, std::vector<int64_t>& sp, std::vector<int32_t>& sj,
+              int nthreads) {
     const int64_t n = A.nrows;
     std::vector<int64_t> cnt(n + 1, 0);
     auto strong = [&](int64_t i, int64_t p) {
@@ -208,20 +230,24 @@ void strength(const HostCsr& A, const std::vector<double>& d, double theta, std:
         if (j == i || A.a[p] == 0.0) return false;
         return std::fabs(A.a[p]) > theta * std::sqrt(std::fabs(d[i] * d[j]));
     };
-    for (int64_t i = 0; i < n; ++i)
-        for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
-            if (strong(i, p)) cnt[i + 1]++;
+    parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1) {
+        for (int64_t i = r0; i < r1; ++i)
+            for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
+                if (strong(i, p)) cnt[i + 1]++;
+    });
     // symmetrise: a coupling counts when either direction is strong
     sp.assign(n + 1, 0);
     std::vector<int32_t> tmpj;
     std::vector<int64_t> tp(n + 1, 0);
     for (int64_t i = 0; i < n; ++i) tp[i + 1] = tp[i] + cnt[i + 1];
     tmpj.resize(tp[n]);
-    for (int64_t i = 0; i < n; ++i) {
-        int64_t q = tp[i];
-        for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
-            if (strong(i, p)) tmpj[q++] = A.ja[p];
-    }
+    parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1) {
+        for (int64_t i = r0; i < r1; ++i) {
+            int64_t q = tp[i];
+            for (int64_t p = A.ia[i]; p < A.ia[i + 1]; ++p)
+                if (strong(i, p)) tmpj[q++] = A.ja[p];
+        }
+    });
     // transpose of the strong graph, merged with it (sorted, unique)
     std::vector<int64_t> tc(n + 1, 0);
     for (int64_t q = 0; q < tp[n]; ++q) tc[tmpj[q] + 1]++;
@@ -232,20 +258,29 @@ void strength(const HostCsr& A, const std::vector<double>& d, double theta, std:
         for (int64_t i = 0; i < n; ++i)
             for (int64_t q = tp[i]; q < tp[i + 1]; ++q) tj[f[tmpj[q]]++] = (int32_t)i;
     }
-    sj.clear();
-    sj.reserve(tp[n] + tp[n] / 8);
-    for (int64_t i = 0; i < n; ++i) {
-        int64_t a = tp[i], b = tc[i];
+    // merge of the two sorted lists per row: count, offsets, fill (rows in parallel)
+    auto merge_row = [&](int64_t i, int32_t* out) {
+        int64_t a = tp[i], b = tc[i], k = 0;
         const int64_t ae = tp[i + 1], bend = tc[i + 1];
         while (a < ae || b < bend) {
             int32_t v;
             if (b >= bend || (a < ae && tmpj[a] < tj[b])) v = tmpj[a++];
             else if (a >= ae || tj[b] < tmpj[a]) v = tj[b++];
             else { v = tmpj[a++]; ++b; }
-            sj.push_back(v);
+            if (out) out[k] = v;
+            ++k;
         }
-        sp[i + 1] = (int64_t)sj.size();
-    }
+        return k;
+    };
+    std::vector<int64_t> len(n + 1, 0);
+    parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1) {
+        for (int64_t i = r0; i < r1; ++i) len[i + 1] = merge_row(i, nullptr);
+    });
+    for (int64_t i = 0; i < n; ++i) sp[i + 1] = sp[i] + len[i + 1];
+    sj.assign(sp[n], 0);
+    parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1) {
+        for (int64_t i = r0; i < r1; ++i) merge_row(i, sj.data() + sp[i]);
+    });
 }
 
 // greedy aggregation; returns the number of aggregates, agg[i] = -1 for nodes left out
@@ -303,28 +338,37 @@ void smoothed_prolongator(const HostCsr& A, const std::vector<double>& d, const 
     if (nsmooth <= 0) { P = std::move(P0); return; }
     HostCsr AP;
     spgemm(A, P0, AP, nthreads);
-    // P = P0 - omega D^-1 (A P0): merge the sorted rows
+    // P = P0 - omega D^-1 (A P0): merge the sorted rows (count, offsets, fill; rows in parallel)
     P.nrows = A.nrows;
     P.ncols = nagg;
     P.ia.assign(A.nrows + 1, 0);
-    P.ja.clear();
-    P.a.clear();
-    P.ja.reserve(AP.ja.size() + P0.ja.size());
-    P.a.reserve(AP.ja.size() + P0.ja.size());
-    for (int64_t i = 0; i < A.nrows; ++i) {
+    auto merge_row = [&](int64_t i, int32_t* oj, double* oa) {
         const double f = d[i] != 0.0 ? omega / d[i] : 0.0;
-        int64_t p = P0.ia[i];
+        int64_t p = P0.ia[i], k = 0;
         const int64_t pe = P0.ia[i + 1];
+        auto put = [&](int32_t j, double v) {
+            if (oj) { oj[k] = j; oa[k] = v; }
+            ++k;
+        };
         for (int64_t q = AP.ia[i]; q < AP.ia[i + 1]; ++q) {
-            while (p < pe && P0.ja[p] < AP.ja[q]) { P.ja.push_back(P0.ja[p]); P.a.push_back(P0.a[p]); ++p; }
+            while (p < pe && P0.ja[p] < AP.ja[q]) { put(P0.ja[p], P0.a[p]); ++p; }
             double v = -f * AP.a[q];
             if (p < pe && P0.ja[p] == AP.ja[q]) { v += P0.a[p]; ++p; }
-            P.ja.push_back(AP.ja[q]);
-            P.a.push_back(v);
+            put(AP.ja[q], v);
         }
-        while (p < pe) { P.ja.push_back(P0.ja[p]); P.a.push_back(P0.a[p]); ++p; }
-        P.ia[i + 1] = (int64_t)P.ja.size();
-    }
+        while (p < pe) { put(P0.ja[p], P0.a[p]); ++p; }
+        return k;
+    };
+    std::vector<int64_t> len(A.nrows + 1, 0);
+    parallel_rows(nthreads, A.nrows, [&](int, int64_t r0, int64_t r1) {
+        for (int64_t i = r0; i < r1; ++i) len[i + 1] = merge_row(i, nullptr, nullptr);
+    });
+    for (int64_t i = 0; i < A.nrows; ++i) P.ia[i + 1] = P.ia[i] + len[i + 1];
+    P.ja.assign(P.ia[A.nrows], 0);
+    P.a.assign(P.ia[A.nrows], 0.0);
+    parallel_rows(nthreads, A.nrows, [&](int, int64_t r0, int64_t r1) {
+        for (int64_t i = r0; i < r1; ++i) merge_row(i, P.ja.data() + P.ia[i], P.a.data() + P.ia[i]);
+    });
 }
 
 // dense inverse of a symmetric positive definite matrix (Cholesky); false when not SPD
@@ -380,7 +424,7 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
         L.lmax = lmax_estimate(A, d, 12, nthreads);
         std::vector<int64_t> sp;
         std::vector<int32_t> sj;
-        strength(A, d, cfg.threshold, sp, sj);
+        strength(A, d, cfg.threshold, sp, sj, nthreads);
         const int64_t nagg = aggregate(A.nrows, sp, sj, L.agg);
         if (nagg == 0 || nagg >= A.nrows) break;              // nothing to coarsen
         const double omega = 4.0 / (3.0 * L.lmax);
