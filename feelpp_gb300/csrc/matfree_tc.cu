@@ -145,10 +145,8 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem_d, const unsigned char* A
     tc_commit(mbar);
 }
 
-// ---------------------------------------------------------------------------
-// Element phase: ye[i][e] = sum_k c_{e,k} (T_k x_e)_i for all elements.
-// Shared memory: Bh, Bl (NMMA x KPAD tf32), Ah, Al (128 x KPAD tf32).
-// ---------------------------------------------------------------------------
+// Operand shapes of the element phase: B = [T_0; ...; T_6] as NMMA x KPAD, A = a tile of x_e as
+// 128 x KPAD (tf32 hi and lo parts of each).
 template <int N>
 struct TcDims {
     static constexpr int KPAD = (N + 7) / 8 * 8;
@@ -158,24 +156,72 @@ struct TcDims {
     static constexpr int SMEM = 1024 + 2 * BBYTES + 2 * ABYTES + 64;
 };
 
+
+// ---------------------------------------------------------------------------
+// Pipelined element phase (one CTA per SM, 256 threads): warps 0-3 gather the
+// x_e of a tile into one of two A buffers (one thread per element row) while
+// thread 0 issues the MMAs of the previous tile into one of two TMEM
+// accumulators and warps 4-7 (one thread per TMEM lane) combine the finished
+// accumulator with the coefficients and write the element values. Three
+// mbarriers per buffer: full (128 producer arrivals), mma (the commit of the
+// MMAs that read the buffer and fill the accumulator), free (128 consumer
+// arrivals, the accumulator may be overwritten). Tile it uses buffer it & 1
+// for the (it >> 1)-th time: every wait is on a phase that cannot be overtaken.
+// Every wait is bounded; a timeout sets a status bit and a shared flag that
+// makes every role leave its loop, and the tensor memory is freed at the end.
+// ---------------------------------------------------------------------------
+struct TcPipeShared {
+    uint64_t full[2], mma[2], freeb[2];
+    uint32_t tmem_base;
+    volatile int bad;
+};
+
+__device__ __forceinline__ void mbar_init(void* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(void* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// bounded wait that also gives up when another role has flagged a failure
+__device__ __forceinline__ bool mbar_wait_or_bad(void* b, uint32_t phase, int budget, volatile int* bad) {
+    uint32_t done = 0;
+    for (int it = 0; it < budget; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(smem_u32(b)), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if ((it & 63) == 63 && *bad) return false;
+    }
+    return false;
+}
+
 template <int N>
-__global__ void __launch_bounds__(kTcThreads) mf_element_tc_kernel(int64_t nt, const int32_t* __restrict__ l2n,
-                                                                   const float4* __restrict__ rec, const float* __restrict__ Tg,
-                                                                   const float* __restrict__ x, const uint8_t* __restrict__ mask,
-                                                                   float* __restrict__ ye, const int* __restrict__ stop,
-                                                                   int* __restrict__ status, int wait_budget) {
-    typedef TcDims<N> D;
+struct TcPipeDims {
+    static constexpr int KPAD = TcDims<N>::KPAD, NMMA = TcDims<N>::NMMA;
+    static constexpr int BBYTES = NMMA * KPAD * 4, ABYTES = kTcTile * KPAD * 4;
+    static constexpr int USED = 1024 + 2 * BBYTES + 4 * ABYTES + 256;
+    static constexpr int SMEM = USED > 118 * 1024 ? USED : 118 * 1024;   // one CTA per SM (its 512 TMEM columns)
+    static constexpr int ACC_STRIDE = 256;                                // TMEM columns between the two accumulators
+};
+
+template <int N>
+__global__ void __launch_bounds__(256) mf_element_tc_pipe_kernel(int64_t nt, const int32_t* __restrict__ l2n,
+                                                                 const float4* __restrict__ rec, const float* __restrict__ Tg,
+                                                                 const float* __restrict__ x, const uint8_t* __restrict__ mask,
+                                                                 float* __restrict__ ye, const int* __restrict__ stop,
+                                                                 int* __restrict__ status, int wait_budget) {
+    typedef TcPipeDims<N> D;
     if (stop && *stop) return;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
     unsigned char* Bh = base;
     unsigned char* Bl = Bh + D::BBYTES;
-    unsigned char* Ah = Bl + D::BBYTES;
-    unsigned char* Al = Ah + D::ABYTES;
-    TcShared* ts = reinterpret_cast<TcShared*>(Al + D::ABYTES);
+    unsigned char* A0 = Bl + D::BBYTES;                     // buffer b: hi at A0 + 2 b ABYTES, lo after it
+    TcPipeShared* ps = reinterpret_cast<TcPipeShared*>(A0 + 4 * D::ABYTES);
     const int t = threadIdx.x;
-    // B = [T_0; ...; T_6] as NMMA x KPAD: row n = k N + i, column j -> T_k[i][j]
-    for (int idx = t; idx < D::NMMA * D::KPAD; idx += kTcThreads) {
+    for (int idx = t; idx < D::NMMA * D::KPAD; idx += blockDim.x) {
         const int n = idx / D::KPAD, j = idx - n * D::KPAD;
         float v = 0.0f;
         if (n < 7 * N && j < N) {
@@ -186,67 +232,105 @@ __global__ void __launch_bounds__(kTcThreads) mf_element_tc_kernel(int64_t nt, c
         *reinterpret_cast<float*>(Bh + core_off(n, j, D::KPAD)) = h;
         *reinterpret_cast<float*>(Bl + core_off(n, j, D::KPAD)) = v - h;
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tc_setup(ts);
-    const uint32_t tmem = ts->tmem_base;
-    const uint32_t my_lane_addr = tmem + ((uint32_t)(32 * (t >> 5)) << 16);
-    uint32_t phase = 0;
-    const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t e = tile * kTcTile + t;
-        float c[7] = {0, 0, 0, 0, 0, 0, 0};
-        // gather x_e into A (hi / lo), zero padding
-#pragma unroll
-        for (int j = 0; j < D::KPAD; ++j) {
-            float v = 0.0f;
-            if (e < nt && j < N) {
-                const int32_t d = l2n[e * N + j];
-                v = (mask && mask[d]) ? 0.0f : x[d];
-            }
-            const float h = tf32_hi(v);
-            *reinterpret_cast<float*>(Ah + core_off(t, j, D::KPAD)) = h;
-            *reinterpret_cast<float*>(Al + core_off(t, j, D::KPAD)) = v - h;
+    if (t == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&ps->full[b], 128);
+            mbar_init(&ps->mma[b], 1);
+            mbar_init(&ps->freeb[b], 128);
         }
-        if (e < nt) {
-            const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
-            c[0] = h0.x; c[1] = h0.y; c[2] = h0.z; c[3] = h0.w; c[4] = h1.x; c[5] = h1.y; c[6] = h1.z;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (t == 0) tc_issue<D::KPAD, D::NMMA>(tmem, Ah, Al, Bh, Bl, &ts->mbar);
-        const bool ok = mbar_wait(&ts->mbar, phase, wait_budget);
-        phase ^= 1u;
-        if (!ok) {
-            if (t == 0) atomicOr(status, kStatusTcTimeout);
-            ts->bad = 1;
-        }
-        __syncthreads();
-        if (ts->bad) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // epilogue: y_i = sum_k c_k Z[k N + i]
-        float y[N];
-#pragma unroll
-        for (int i = 0; i < N; ++i) y[i] = 0.0f;
-#pragma unroll
-        for (int cb = 0; cb < D::NMMA; cb += 16) {
-            float z[16];
-            tmem_ld16(my_lane_addr + cb, z);
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int n = cb + q;
-                if (n < 7 * N) y[n % N] = fmaf(c[n / N], z[q], y[n % N]);
-            }
-        }
-        if (e < nt) {
-#pragma unroll
-            for (int i = 0; i < N; ++i) ye[(int64_t)i * nt + e] = y[i];
-        }
-        // all TMEM reads and smem A reads done before the next tile overwrites them
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        ps->bad = 0;
     }
-    tc_teardown(ts);
+    if ((t >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ps->tmem_base)), "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = ps->tmem_base;
+    const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
+    if (t < 128) {
+        // producers; thread 0 also issues the MMAs
+        for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; ++it, tile += gridDim.x) {
+            const int b = (int)(it & 1);
+            const uint32_t u = (uint32_t)(it >> 1);
+            unsigned char* Ahb = A0 + 2 * b * D::ABYTES;
+            unsigned char* Alb = Ahb + D::ABYTES;
+            if (u > 0 && !mbar_wait_or_bad(&ps->mma[b], (u - 1) & 1u, wait_budget, &ps->bad)) { ps->bad = 1; break; }
+            const int64_t e = tile * kTcTile + t;
+            float v[D::KPAD];
+#pragma unroll
+            for (int j = 0; j < D::KPAD; ++j) {
+                v[j] = 0.0f;
+                if (e < nt && j < N) {
+                    const int32_t d = __ldg(l2n + e * N + j);
+                    v[j] = (mask && mask[d]) ? 0.0f : __ldg(x + d);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < D::KPAD; ++j) {
+                const float h = tf32_hi(v[j]);
+                *reinterpret_cast<float*>(Ahb + core_off(t, j, D::KPAD)) = h;
+                *reinterpret_cast<float*>(Alb + core_off(t, j, D::KPAD)) = v[j] - h;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&ps->full[b]);
+            if (t == 0) {
+                bool ok = mbar_wait_or_bad(&ps->full[b], u & 1u, wait_budget, &ps->bad);
+                if (ok && u > 0) ok = mbar_wait_or_bad(&ps->freeb[b], (u - 1) & 1u, wait_budget, &ps->bad);
+                if (!ok) { ps->bad = 1; atomicOr(status, kStatusTcTimeout); break; }
+                tc_issue<D::KPAD, D::NMMA>(tmem + (uint32_t)(b * D::ACC_STRIDE), Ahb, Alb, Bh, Bl, &ps->mma[b]);
+            }
+            if (ps->bad) break;
+        }
+    } else {
+        // consumers: one thread per TMEM lane / element row
+        const int r = t - 128;
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * ((t >> 5) & 3)) << 16);
+        for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; ++it, tile += gridDim.x) {
+            const int b = (int)(it & 1);
+            const uint32_t u = (uint32_t)(it >> 1);
+            const int64_t e = tile * kTcTile + r;
+            float c[7] = {0, 0, 0, 0, 0, 0, 0};
+            if (e < nt) {
+                const float4 h0 = __ldg(rec + 4 * e), h1 = __ldg(rec + 4 * e + 1);
+                c[0] = h0.x; c[1] = h0.y; c[2] = h0.z; c[3] = h0.w; c[4] = h1.x; c[5] = h1.y; c[6] = h1.z;
+            }
+            if (!mbar_wait_or_bad(&ps->mma[b], u & 1u, wait_budget, &ps->bad)) {
+                ps->bad = 1;
+                if (r == 0) atomicOr(status, kStatusTcTimeout);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            float y[N];
+#pragma unroll
+            for (int i = 0; i < N; ++i) y[i] = 0.0f;
+#pragma unroll
+            for (int cb = 0; cb < D::NMMA; cb += 16) {
+                float z[16];
+                tmem_ld16(lane_addr + (uint32_t)(b * D::ACC_STRIDE + cb), z);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int n = cb + q;
+                    if (n < 7 * N) y[n % N] = fmaf(c[n / N], z[q], y[n % N]);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(&ps->freeb[b]);
+            if (e < nt) {
+#pragma unroll
+                for (int i = 0; i < N; ++i) ye[(int64_t)i * nt + e] = y[i];
+            }
+            if (ps->bad) break;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if ((t >> 5) == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -302,17 +386,17 @@ int launch_mf_element_tc(fgpu_ctx* ctx, int n, int64_t nt, const int32_t* l2n, c
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, 2 * (int64_t)sms));
+    const int pgrid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)sms));
     if (n == 20) {
-        auto k = mf_element_tc_kernel<20>;
-        constexpr int sm = TcDims<20>::SMEM;
+        auto k = mf_element_tc_pipe_kernel<20>;
+        constexpr int sm = TcPipeDims<20>::SMEM;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        k<<<grid, kTcThreads, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
+        k<<<pgrid, 256, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
     } else if (n == 10) {
-        auto k = mf_element_tc_kernel<10>;
-        constexpr int sm = TcDims<10>::SMEM;
+        auto k = mf_element_tc_pipe_kernel<10>;
+        constexpr int sm = TcPipeDims<10>::SMEM;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        k<<<grid, kTcThreads, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
+        k<<<pgrid, 256, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
     } else {
         ctx->err = "tensor-core element phase supports P2 and P3";
         return FGPU_ERR_INVALID;

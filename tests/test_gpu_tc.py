@@ -25,8 +25,10 @@ def test_tc_selftest_gemm(env):
     assert np.all(np.abs(D - ref) <= 4e-6 * scale), np.abs(D - ref).max()
 
 
-@pytest.mark.parametrize("order,n", [(2, 6), (3, 4), (3, 7)])
+@pytest.mark.parametrize("order,n", [(2, 6), (3, 4), (3, 7), (2, 24), (3, 20)])
 def test_operator_apply_tensor_cores(env, order, n):
+    """(the larger meshes give every CTA of the pipelined kernel three or more tiles, so both buffers are
+    reused)"""
     xyz, tets, M, V, integral, a, l = system(env, n, order)
     op = fpp.operator(V, integral, precision="f32")
     op.use_tensor_cores(True)
