@@ -158,12 +158,13 @@ struct TcDims {
 
 
 // ---------------------------------------------------------------------------
-// Pipelined element phase (one CTA per SM, 256 threads): warps 0-3 gather the
-// x_e of a tile into one of two A buffers (one thread per element row) while
-// thread 0 issues the MMAs of the previous tile into one of two TMEM
-// accumulators and warps 4-7 (one thread per TMEM lane) combine the finished
-// accumulator with the coefficients and write the element values. Three
-// mbarriers per buffer: full (128 producer arrivals), mma (the commit of the
+// Pipelined element phase (one CTA per SM, 384 threads): warps 0-7 stage the
+// tile's dof indices with coalesced loads, then gather its x values (all 256
+// threads over the 128 x KPAD entries, many independent loads in flight) into
+// one of two A buffers, while thread 0 issues the MMAs of the previous tile
+// into one of two TMEM accumulators and warps 8-11 (one thread per TMEM lane)
+// combine the finished accumulator with the coefficients and write the element
+// values. Three mbarriers per buffer: full (256 producer arrivals), mma (the commit of the
 // MMAs that read the buffer and fill the accumulator), free (128 consumer
 // arrivals, the accumulator may be overwritten). Tile it uses buffer it & 1
 // for the (it >> 1)-th time: every wait is on a phase that cannot be overtaken.
@@ -201,13 +202,17 @@ template <int N>
 struct TcPipeDims {
     static constexpr int KPAD = TcDims<N>::KPAD, NMMA = TcDims<N>::NMMA;
     static constexpr int BBYTES = NMMA * KPAD * 4, ABYTES = kTcTile * KPAD * 4;
-    static constexpr int USED = 1024 + 2 * BBYTES + 4 * ABYTES + 256;
+    static constexpr int IDXBYTES = kTcTile * N * 4;
+    static constexpr int USED = 1024 + 2 * BBYTES + 4 * ABYTES + IDXBYTES + 256;
     static constexpr int SMEM = USED > 118 * 1024 ? USED : 118 * 1024;   // one CTA per SM (its 512 TMEM columns)
     static constexpr int ACC_STRIDE = 256;                                // TMEM columns between the two accumulators
 };
 
+constexpr int kTcProducers = 256;
+constexpr int kTcPipeThreads = kTcProducers + 128;
+
 template <int N>
-__global__ void __launch_bounds__(256) mf_element_tc_pipe_kernel(int64_t nt, const int32_t* __restrict__ l2n,
+__global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int64_t nt, const int32_t* __restrict__ l2n,
                                                                  const float4* __restrict__ rec, const float* __restrict__ Tg,
                                                                  const float* __restrict__ x, const uint8_t* __restrict__ mask,
                                                                  float* __restrict__ ye, const int* __restrict__ stop,
@@ -219,7 +224,8 @@ __global__ void __launch_bounds__(256) mf_element_tc_pipe_kernel(int64_t nt, con
     unsigned char* Bh = base;
     unsigned char* Bl = Bh + D::BBYTES;
     unsigned char* A0 = Bl + D::BBYTES;                     // buffer b: hi at A0 + 2 b ABYTES, lo after it
-    TcPipeShared* ps = reinterpret_cast<TcPipeShared*>(A0 + 4 * D::ABYTES);
+    int32_t* sidx = reinterpret_cast<int32_t*>(A0 + 4 * D::ABYTES);   // the tile's dof indices (128 x N)
+    TcPipeShared* ps = reinterpret_cast<TcPipeShared*>(A0 + 4 * D::ABYTES + D::IDXBYTES);
     const int t = threadIdx.x;
     for (int idx = t; idx < D::NMMA * D::KPAD; idx += blockDim.x) {
         const int n = idx / D::KPAD, j = idx - n * D::KPAD;
@@ -234,7 +240,7 @@ __global__ void __launch_bounds__(256) mf_element_tc_pipe_kernel(int64_t nt, con
     }
     if (t == 0) {
         for (int b = 0; b < 2; ++b) {
-            mbar_init(&ps->full[b], 128);
+            mbar_init(&ps->full[b], kTcProducers);
             mbar_init(&ps->mma[b], 1);
             mbar_init(&ps->freeb[b], 128);
         }
@@ -252,43 +258,55 @@ __global__ void __launch_bounds__(256) mf_element_tc_pipe_kernel(int64_t nt, con
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = ps->tmem_base;
     const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
-    if (t < 128) {
+    if (t < kTcProducers) {
         // producers; thread 0 also issues the MMAs
         for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; ++it, tile += gridDim.x) {
             const int b = (int)(it & 1);
             const uint32_t u = (uint32_t)(it >> 1);
             unsigned char* Ahb = A0 + 2 * b * D::ABYTES;
             unsigned char* Alb = Ahb + D::ABYTES;
-            if (u > 0 && !mbar_wait_or_bad(&ps->mma[b], (u - 1) & 1u, wait_budget, &ps->bad)) { ps->bad = 1; break; }
-            const int64_t e = tile * kTcTile + t;
-            float v[D::KPAD];
-#pragma unroll
-            for (int j = 0; j < D::KPAD; ++j) {
-                v[j] = 0.0f;
-                if (e < nt && j < N) {
-                    const int32_t d = __ldg(l2n + e * N + j);
-                    v[j] = (mask && mask[d]) ? 0.0f : __ldg(x + d);
+            const int64_t e0 = tile * kTcTile;
+            const int rows = (int)min((int64_t)kTcTile, nt - e0);
+            // the tile's dof indices: one contiguous block of rows * N ints
+            asm volatile("bar.sync 1, %0;" ::"r"(kTcProducers) : "memory");
+            for (int k = t; k < rows * N; k += kTcProducers) sidx[k] = __ldg(l2n + e0 * N + k);
+            uint32_t mybad = 0;
+            if (u > 0 && !mbar_wait_or_bad(&ps->mma[b], (u - 1) & 1u, wait_budget, &ps->bad)) mybad = 1;
+            mybad |= (uint32_t)(ps->bad != 0);
+            // barrier over the producers that also ORs their failure flags: all leave together or none
+            uint32_t anybad = 0;
+            asm volatile("{\n\t.reg .pred pin, pout;\n\tsetp.ne.u32 pin, %1, 0;\n\tbar.red.or.pred pout, 1, %2, pin;\n\t"
+                         "selp.u32 %0, 1, 0, pout;\n\t}\n"
+                         : "=r"(anybad)
+                         : "r"(mybad), "r"(kTcProducers)
+                         : "memory");
+            if (anybad) { ps->bad = 1; break; }
+            // x values, all producer threads over the 128 x KPAD entries
+            for (int p = t; p < kTcTile * D::KPAD; p += kTcProducers) {
+                const int row = p / D::KPAD, j = p - row * D::KPAD;
+                float v = 0.0f;
+                if (row < rows && j < N) {
+                    const int32_t d = sidx[row * N + j];
+                    v = (mask && mask[d]) ? 0.0f : __ldg(x + d);
                 }
-            }
-#pragma unroll
-            for (int j = 0; j < D::KPAD; ++j) {
-                const float h = tf32_hi(v[j]);
-                *reinterpret_cast<float*>(Ahb + core_off(t, j, D::KPAD)) = h;
-                *reinterpret_cast<float*>(Alb + core_off(t, j, D::KPAD)) = v[j] - h;
+                const float h = tf32_hi(v);
+                *reinterpret_cast<float*>(Ahb + core_off(row, j, D::KPAD)) = h;
+                *reinterpret_cast<float*>(Alb + core_off(row, j, D::KPAD)) = v - h;
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&ps->full[b]);
             if (t == 0) {
+                // the issuer does not leave the loop on a timeout: it flags it, and the producers' barrier
+                // at the next tile takes everyone out together
                 bool ok = mbar_wait_or_bad(&ps->full[b], u & 1u, wait_budget, &ps->bad);
                 if (ok && u > 0) ok = mbar_wait_or_bad(&ps->freeb[b], (u - 1) & 1u, wait_budget, &ps->bad);
-                if (!ok) { ps->bad = 1; atomicOr(status, kStatusTcTimeout); break; }
-                tc_issue<D::KPAD, D::NMMA>(tmem + (uint32_t)(b * D::ACC_STRIDE), Ahb, Alb, Bh, Bl, &ps->mma[b]);
+                if (ok) tc_issue<D::KPAD, D::NMMA>(tmem + (uint32_t)(b * D::ACC_STRIDE), Ahb, Alb, Bh, Bl, &ps->mma[b]);
+                else { ps->bad = 1; atomicOr(status, kStatusTcTimeout); }
             }
-            if (ps->bad) break;
         }
     } else {
         // consumers: one thread per TMEM lane / element row
-        const int r = t - 128;
+        const int r = t - kTcProducers;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * ((t >> 5) & 3)) << 16);
         for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; ++it, tile += gridDim.x) {
             const int b = (int)(it & 1);
@@ -391,12 +409,12 @@ int launch_mf_element_tc(fgpu_ctx* ctx, int n, int64_t nt, const int32_t* l2n, c
         auto k = mf_element_tc_pipe_kernel<20>;
         constexpr int sm = TcPipeDims<20>::SMEM;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        k<<<pgrid, 256, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
+        k<<<pgrid, kTcPipeThreads, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
     } else if (n == 10) {
         auto k = mf_element_tc_pipe_kernel<10>;
         constexpr int sm = TcPipeDims<10>::SMEM;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        k<<<pgrid, 256, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
+        k<<<pgrid, kTcPipeThreads, sm, ctx->stream>>>(nt, l2n, rec, T7f, x, mask, ye, stop, ctx->d_status, kTcWaitBudget);
     } else {
         ctx->err = "tensor-core element phase supports P2 and P3";
         return FGPU_ERR_INVALID;
