@@ -382,7 +382,8 @@ struct fgpu_operator {
     void* d_ye = nullptr;            // element buffer T x n (float or double)
     uint8_t* d_mask = nullptr;       // Dirichlet mask (nnodes) or null
     void* d_diag = nullptr;          // operator diagonal (float or double)
-    float* d_xf = nullptr;           // binary32 work vectors for the F32 solve
+    float* d_xf = nullptr;           // binary32 copies of x and y for fgpu_operator_apply on binary64 vectors
+    float* d_yf = nullptr;
     float* d_xm = nullptr;           // binary32 x with the Dirichlet entries zeroed (element phase input)
     int64_t nt = 0, nnodes = 0;
     int use_tc = 0;                  // binary32 element phase on the tensor cores (tcgen05, P2/P3)
@@ -987,25 +988,31 @@ extern "C" int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_
     if (!ctx || !op || !x || !y || x->n != op->nnodes || y->n != op->nnodes) return FGPU_ERR_INVALID;
     int rc;
     if (op->precision == FGPU_F32) {
-        float *xf = nullptr, *yf = nullptr;
-        if (cudaMalloc(&xf, op->nnodes * 4) != cudaSuccess || cudaMalloc(&yf, op->nnodes * 4) != cudaSuccess) {
-            cudaFree(xf);
+        // the binary32 copies stay with the operator (no allocation per apply)
+        if (!op->d_xf && (cudaMalloc(&op->d_xf, op->nnodes * 4) != cudaSuccess ||
+                          cudaMalloc(&op->d_yf, op->nnodes * 4) != cudaSuccess)) {
+            cudaFree(op->d_xf);
+            op->d_xf = nullptr;
             ctx->err = "apply: allocation failed";
             return FGPU_ERR_ALLOC;
         }
         const int vb = vec_blocks(op->nnodes);
-        copy_cast_kernel<float><<<vb, 256, 0, ctx->stream>>>(op->nnodes, x->d, xf);
-        rc = operator_apply(ctx, op, xf, yf);
-        cast_back_kernel<float><<<vb, 256, 0, ctx->stream>>>(op->nnodes, yf, y->d);
+        copy_cast_kernel<float><<<vb, 256, 0, ctx->stream>>>(op->nnodes, x->d, op->d_xf);
+        rc = operator_apply(ctx, op, op->d_xf, op->d_yf);
+        cast_back_kernel<float><<<vb, 256, 0, ctx->stream>>>(op->nnodes, op->d_yf, y->d);
         ctx->launches += 2;
-        cudaError_t e = cudaStreamSynchronize(ctx->stream);
-        cudaFree(xf);
-        cudaFree(yf);
-        if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
     } else {
         rc = operator_apply(ctx, op, x->d, y->d);
-        cudaError_t e = cudaStreamSynchronize(ctx->stream);
-        if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    }
+    // completion and the device status word (bounded tensor-core waits report through it)
+    int hst = 0;
+    cudaError_t e = cudaMemcpyAsync(&hst, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (!rc && e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = FGPU_ERR_CUDA; }
+    if (e == cudaSuccess && hst) {
+        cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        if (!rc) { ctx->err = "apply: device status " + std::to_string(hst); rc = FGPU_ERR_CUDA; }
     }
     return rc;
 }
@@ -1048,6 +1055,7 @@ extern "C" int fgpu_operator_destroy(fgpu_operator* op) {
     cudaFree(op->d_mask);
     cudaFree(op->d_diag);
     cudaFree(op->d_xf);
+    cudaFree(op->d_yf);
     cudaFree(op->d_xm);
     cudaFree(op->d_xs);
     delete op;

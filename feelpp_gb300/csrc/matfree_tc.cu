@@ -82,6 +82,16 @@ __device__ __forceinline__ bool mbar_wait(void* mbar, uint32_t phase, int budget
     return false;
 }
 
+// x16 load without the wait (the caller waits once for several loads)
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
     asm volatile(
@@ -158,9 +168,9 @@ struct TcDims {
 
 
 // ---------------------------------------------------------------------------
-// Pipelined element phase (one CTA per SM, 384 threads): warps 0-7 stage the
-// tile's dof indices with coalesced loads, then gather its x values (all 256
-// threads over the 128 x KPAD entries, many independent loads in flight) into
+// Pipelined element phase (one CTA per SM, 384 threads): warps 0-7 gather the
+// tile's x values (all 256 threads over the 128 x KPAD entries, many independent
+// loads in flight; the dof indices of the next tile are loaded meanwhile) into
 // one of two A buffers, while thread 0 issues the MMAs of the previous tile
 // into one of two TMEM accumulators and warps 8-11 (one thread per TMEM lane)
 // combine the finished accumulator with the coefficients and write the element
@@ -202,8 +212,7 @@ template <int N>
 struct TcPipeDims {
     static constexpr int KPAD = TcDims<N>::KPAD, NMMA = TcDims<N>::NMMA;
     static constexpr int BBYTES = NMMA * KPAD * 4, ABYTES = kTcTile * KPAD * 4;
-    static constexpr int IDXBYTES = kTcTile * N * 4;
-    static constexpr int USED = 1024 + 2 * BBYTES + 4 * ABYTES + IDXBYTES + 256;
+    static constexpr int USED = 1024 + 2 * BBYTES + 4 * ABYTES + 256;
     static constexpr int SMEM = USED > 118 * 1024 ? USED : 118 * 1024;   // one CTA per SM (its 512 TMEM columns)
     static constexpr int ACC_STRIDE = 256;                                // TMEM columns between the two accumulators
 };
@@ -224,8 +233,7 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
     unsigned char* Bh = base;
     unsigned char* Bl = Bh + D::BBYTES;
     unsigned char* A0 = Bl + D::BBYTES;                     // buffer b: hi at A0 + 2 b ABYTES, lo after it
-    int32_t* sidx = reinterpret_cast<int32_t*>(A0 + 4 * D::ABYTES);   // the tile's dof indices (128 x N)
-    TcPipeShared* ps = reinterpret_cast<TcPipeShared*>(A0 + 4 * D::ABYTES + D::IDXBYTES);
+    TcPipeShared* ps = reinterpret_cast<TcPipeShared*>(A0 + 4 * D::ABYTES);
     const int t = threadIdx.x;
     for (int idx = t; idx < D::NMMA * D::KPAD; idx += blockDim.x) {
         const int n = idx / D::KPAD, j = idx - n * D::KPAD;
@@ -259,17 +267,26 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
     const uint32_t tmem = ps->tmem_base;
     const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
     if (t < kTcProducers) {
-        // producers; thread 0 also issues the MMAs
+        // producers; thread 0 also issues the MMAs. Entry p = t + q * 256 of a tile is (row, j) =
+        // (p / KPAD, p % KPAD): consecutive threads read consecutive ints of the tile's l2n block
+        constexpr int ITER = kTcTile * D::KPAD / kTcProducers;
+        static_assert(ITER * kTcProducers == kTcTile * D::KPAD, "tile entries split evenly");
+        auto load_tile_idx = [&](int64_t tl, int32_t* d) {
+            const int64_t e0 = tl * kTcTile;
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) {
+                const int p = t + q * kTcProducers;
+                const int row = p / D::KPAD, j = p - row * D::KPAD;
+                d[q] = (tl < ntiles && e0 + row < nt && j < N) ? __ldg(l2n + (e0 + row) * N + j) : -1;
+            }
+        };
+        int32_t dn[ITER];
+        load_tile_idx(blockIdx.x, dn);
         for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; ++it, tile += gridDim.x) {
             const int b = (int)(it & 1);
             const uint32_t u = (uint32_t)(it >> 1);
             unsigned char* Ahb = A0 + 2 * b * D::ABYTES;
             unsigned char* Alb = Ahb + D::ABYTES;
-            const int64_t e0 = tile * kTcTile;
-            const int rows = (int)min((int64_t)kTcTile, nt - e0);
-            // the tile's dof indices: one contiguous block of rows * N ints
-            asm volatile("bar.sync 1, %0;" ::"r"(kTcProducers) : "memory");
-            for (int k = t; k < rows * N; k += kTcProducers) sidx[k] = __ldg(l2n + e0 * N + k);
             uint32_t mybad = 0;
             if (u > 0 && !mbar_wait_or_bad(&ps->mma[b], (u - 1) & 1u, wait_budget, &ps->bad)) mybad = 1;
             mybad |= (uint32_t)(ps->bad != 0);
@@ -281,17 +298,27 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
                          : "r"(mybad), "r"(kTcProducers)
                          : "memory");
             if (anybad) { ps->bad = 1; break; }
-            // x values, all producer threads over the 128 x KPAD entries
-            for (int p = t; p < kTcTile * D::KPAD; p += kTcProducers) {
+            // this tile's indices arrived during the previous tile; ask for the next tile's now
+            int32_t dd[ITER];
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) dd[q] = dn[q];
+            load_tile_idx(tile + gridDim.x, dn);
+            // x values, all producer threads over the 128 x KPAD entries, ITER independent loads each
+            float v[ITER];
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) v[q] = dd[q] >= 0 ? __ldg(x + dd[q]) : 0.0f;
+            if (mask) {
+#pragma unroll
+                for (int q = 0; q < ITER; ++q)
+                    if (dd[q] >= 0 && mask[dd[q]]) v[q] = 0.0f;
+            }
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) {
+                const int p = t + q * kTcProducers;
                 const int row = p / D::KPAD, j = p - row * D::KPAD;
-                float v = 0.0f;
-                if (row < rows && j < N) {
-                    const int32_t d = sidx[row * N + j];
-                    v = (mask && mask[d]) ? 0.0f : __ldg(x + d);
-                }
-                const float h = tf32_hi(v);
+                const float h = tf32_hi(v[q]);
                 *reinterpret_cast<float*>(Ahb + core_off(row, j, D::KPAD)) = h;
-                *reinterpret_cast<float*>(Alb + core_off(row, j, D::KPAD)) = v - h;
+                *reinterpret_cast<float*>(Alb + core_off(row, j, D::KPAD)) = v[q] - h;
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&ps->full[b]);
@@ -326,15 +353,22 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
             float y[N];
 #pragma unroll
             for (int i = 0; i < N; ++i) y[i] = 0.0f;
+            // the accumulator row in groups of three x16 loads, one wait per group
+            constexpr int NB = D::NMMA / 16;
 #pragma unroll
-            for (int cb = 0; cb < D::NMMA; cb += 16) {
-                float z[16];
-                tmem_ld16(lane_addr + (uint32_t)(b * D::ACC_STRIDE + cb), z);
+            for (int g0 = 0; g0 < NB; g0 += 3) {
+                uint32_t z[3][16];
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int n = cb + q;
-                    if (n < 7 * N) y[n % N] = fmaf(c[n / N], z[q], y[n % N]);
-                }
+                for (int g = 0; g < 3; ++g)
+                    if (g0 + g < NB) tmem_ld16_nowait(lane_addr + (uint32_t)(b * D::ACC_STRIDE + (g0 + g) * 16), z[g]);
+                tmem_wait_ld();
+#pragma unroll
+                for (int g = 0; g < 3; ++g)
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int n = (g0 + g) * 16 + q;
+                        if (g0 + g < NB && n < 7 * N) y[n % N] = fmaf(c[n / N], __uint_as_float(z[g][q]), y[n % N]);
+                    }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             mbar_arrive(&ps->freeb[b]);
