@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "pmg"],
+    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "pmg", "apply"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
                         "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
                         "AMG-preconditioned CG solve to 1e-10; 'pmg' sets up the matrix-free Poisson operators "
@@ -480,6 +480,34 @@ def run_probe_pmg(args):
     st = op64.solve(l, w, rtol=1e-10, inner=op32, pc="pmg", coarse=a1)
     print(json.dumps({"iterations": st["iterations"], "time_ms": st["time_ms"], "rel_residual": st["rel_residual"],
                       "pmg": st["pmg"]}), flush=True)
+
+
+def run_probe_apply(args):
+    """Binary32 matrix-free applies of the P-order Laplace operator (Dirichlet dofs masked), CUDA-core and
+    tcgen05 element phases, 5 applies each, for kernel profiling; prints the element/node phase times."""
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    env = fpp.Environment(profile=True)
+    xyz, tets = meshgen.kuhn_box(args.n, perturb=0.1, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, args.order)
+    u, v = V.element(), V.element()
+    integral = fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v)))
+    bd = V.boundary_dofs()
+    x, y = V.element(), V.element()
+    x.upload(np.random.default_rng(0).standard_normal(V.ndof))
+    out = {"ndof": V.ndof, "elements": len(tets)}
+    for name, tc in (("f32_cuda_cores", False), ("f32_tensor_cores", True)):
+        op = fpp.operator(V, integral, precision="f32")
+        op.use_tensor_cores(tc)
+        op.set_dirichlet(bd)
+        env.prof_reset()
+        for _ in range(5):
+            op.apply(x, y)
+        ne, te = env.prof("matfree_element")
+        ng, tg = env.prof("matfree_gather")
+        out[name] = {"element_phase_ms": te / max(ne, 1), "node_phase_ms": tg / max(ng, 1)}
+    print(json.dumps(out), flush=True)
 
 
 def run_matfree(args):
@@ -973,6 +1001,9 @@ def main():
         return
     if args.probe == "gamg":
         run_probe_gamg(args)
+        return
+    if args.probe == "apply":
+        run_probe_apply(args)
         return
     if args.probe == "pmg":
         run_probe_pmg(args)

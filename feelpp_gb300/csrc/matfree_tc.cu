@@ -168,9 +168,9 @@ struct TcDims {
 
 
 // ---------------------------------------------------------------------------
-// Pipelined element phase (one CTA per SM, 384 threads): warps 0-7 gather the
-// tile's x values (all 256 threads over the 128 x KPAD entries, many independent
-// loads in flight; the dof indices of the next tile are loaded meanwhile) into
+// Pipelined element phase (one CTA per SM, 384 threads): warps 0-7 write the
+// tile's x values (all 256 threads over the 128 x KPAD entries, gathered into
+// registers during the previous tile while the next tile's loads are in flight) into
 // one of two A buffers, while thread 0 issues the MMAs of the previous tile
 // into one of two TMEM accumulators and warps 8-11 (one thread per TMEM lane)
 // combine the finished accumulator with the coefficients and write the element
@@ -280,8 +280,22 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
                 d[q] = (tl < ntiles && e0 + row < nt && j < N) ? __ldg(l2n + (e0 + row) * N + j) : -1;
             }
         };
+        // x values (and Dirichlet mask bytes) of the entries with indices d; -1 reads nothing
+        auto gather = [&](const int32_t* d, float* v, uint32_t* m) {
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) v[q] = d[q] >= 0 ? __ldg(x + d[q]) : 0.0f;
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) m[q] = (mask && d[q] >= 0) ? (uint32_t)mask[d[q]] : 0u;
+        };
+        // three-stage register pipeline: while tile it is written to shared memory from the values
+        // gathered during tile it - 1, the x values of tile it + 1 and the indices of tile it + 2 are
+        // in flight
         int32_t dn[ITER];
+        float vc[ITER];
+        uint32_t mc[ITER];
         load_tile_idx(blockIdx.x, dn);
+        gather(dn, vc, mc);
+        load_tile_idx(blockIdx.x + gridDim.x, dn);
         for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; ++it, tile += gridDim.x) {
             const int b = (int)(it & 1);
             const uint32_t u = (uint32_t)(it >> 1);
@@ -298,28 +312,26 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
                          : "r"(mybad), "r"(kTcProducers)
                          : "memory");
             if (anybad) { ps->bad = 1; break; }
-            // this tile's indices arrived during the previous tile; ask for the next tile's now
+            // start the next tile's gathers and the indices of the one after
             int32_t dd[ITER];
 #pragma unroll
             for (int q = 0; q < ITER; ++q) dd[q] = dn[q];
-            load_tile_idx(tile + gridDim.x, dn);
-            // x values, all producer threads over the 128 x KPAD entries, ITER independent loads each
-            float v[ITER];
-#pragma unroll
-            for (int q = 0; q < ITER; ++q) v[q] = dd[q] >= 0 ? __ldg(x + dd[q]) : 0.0f;
-            if (mask) {
-#pragma unroll
-                for (int q = 0; q < ITER; ++q)
-                    if (dd[q] >= 0 && mask[dd[q]]) v[q] = 0.0f;
-            }
+            float vn[ITER];
+            uint32_t mn[ITER];
+            gather(dd, vn, mn);
+            load_tile_idx(tile + 2 * (int64_t)gridDim.x, dn);
+            // this tile's values, all producer threads over the 128 x KPAD entries
 #pragma unroll
             for (int q = 0; q < ITER; ++q) {
                 const int p = t + q * kTcProducers;
                 const int row = p / D::KPAD, j = p - row * D::KPAD;
-                const float h = tf32_hi(v[q]);
+                const float val = mc[q] ? 0.0f : vc[q];
+                const float h = tf32_hi(val);
                 *reinterpret_cast<float*>(Ahb + core_off(row, j, D::KPAD)) = h;
-                *reinterpret_cast<float*>(Alb + core_off(row, j, D::KPAD)) = v[q] - h;
+                *reinterpret_cast<float*>(Alb + core_off(row, j, D::KPAD)) = val - h;
             }
+#pragma unroll
+            for (int q = 0; q < ITER; ++q) { vc[q] = vn[q]; mc[q] = mn[q]; }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&ps->full[b]);
             if (t == 0) {
