@@ -594,13 +594,13 @@ def run_matfree(args):
     a1.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u1), fpp.grad(v1))))
     l1 = fpp.form1(test=V1)
     a1 += fpp.on(fpp.boundaryfaces(M), rhs=l1, element=u1, expr=0.0, type="elimination_symmetric")
-    pm = ops["df64"].pmg(a1, ops["f32_cuda_cores"])
+    pm = ops["df64"].pmg(a1, ops["f32_tensor_cores"])
     torch.cuda.synchronize()
     pmg_setup_ms = (time.perf_counter() - t0) * 1e3
     wp = V.element()
     cfgp = fe._solver_cfg(1e-10, 100000, "pmg", True, 0.1, 16, "f64", 0, 0.0)
     stp = _ffi.SolveStats()
-    rcp = env.lib.fgpu_solve_cg_operator_pmg(env.h, ops["df64"].h, ops["f32_cuda_cores"].h, pm.h, l.vec.h, wp.h, C.byref(cfgp),
+    rcp = env.lib.fgpu_solve_cg_operator_pmg(env.h, ops["df64"].h, ops["f32_tensor_cores"].h, pm.h, l.vec.h, wp.h, C.byref(cfgp),
                                               C.byref(stp))
     sp = fe._stats(stp)
     sp["status"] = "ok" if rcp == 0 else _ffi.ERROR_NAMES.get(rcp, str(rcp))

@@ -289,7 +289,8 @@ __global__ void __launch_bounds__(kTcPipeThreads) mf_element_tc_pipe_kernel(int6
         };
         // three-stage register pipeline: while tile it is written to shared memory from the values
         // gathered during tile it - 1, the x values of tile it + 1 and the indices of tile it + 2 are
-        // in flight
+        // in flight. (4-byte cp.async copies into shared-memory slots, three tiles ahead, measured
+        // slower: 0.74 vs 0.64 ms for the P3 96^3 element phase.)
         int32_t dn[ITER];
         float vc[ITER];
         uint32_t mc[ITER];
