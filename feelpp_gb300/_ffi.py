@@ -14,6 +14,7 @@ F64, F32, DF64 = 0, 1, 2
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
 RANGE_ELEMENTS, RANGE_BOUNDARY_FACES, RANGE_MARKED_FACES = 0, 1, 2
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE = 0, 1, 2, 3, 4
+HOST_TRANSFER_AUTO, HOST_TRANSFER_COPY, HOST_TRANSFER_DIRECT = 0, 1, 2
 RHS_SINE, RHS_CONST_VEC, RHS_CONST, RHS_FACE = 0, 1, 2, 3
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2
 PC_NONE, PC_JACOBI, PC_CHEB_JACOBI, PC_GAMG, PC_PMG = 0, 1, 2, 3, 4
@@ -113,6 +114,7 @@ SIGNATURES = {
     "fgpu_amg_destroy": (i32, [P]),
     "fgpu_mesh_set_ho_nodes": (i32, [P, P]),
     "fgpu_assemble_matrix_host": (i32, [P, P, C.POINTER(FormDesc), P]),
+    "fgpu_set_host_transfer": (i32, [P, i32]),
     "fgpu_export_ensight": (i32, [P, C.c_char_p, i32, P, P]),
     "fgpu_pmg_create": (i32, [P, P, P, P, C.POINTER(PmgCfg), PP]),
     "fgpu_pmg_info": (i32, [P, DP, P, DP]),

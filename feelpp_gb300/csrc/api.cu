@@ -620,6 +620,14 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     return assemble_impl(ctx, A, f, A->d_kappa_stage, accumulate);
 }
 
+int fgpu_set_host_transfer(fgpu_ctx* ctx, int mode) {
+    if (!ctx) return FGPU_ERR_INVALID;
+    if (mode != FGPU_HOST_TRANSFER_AUTO && mode != FGPU_HOST_TRANSFER_COPY && mode != FGPU_HOST_TRANSFER_DIRECT)
+        return set_err(ctx, FGPU_ERR_INVALID, "host transfer mode: AUTO, COPY or DIRECT");
+    ctx->host_transfer = mode;
+    return FGPU_OK;
+}
+
 int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, double* host_val) {
     if (!ctx || !A || !f || !host_val) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix_host: bad arguments");
     FGPU_NO_CAPTURE(ctx, "assemble_matrix_host");

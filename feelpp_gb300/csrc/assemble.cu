@@ -1396,7 +1396,8 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 template <int MODE>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
-                                                         void* __restrict__ valv, int accumulate) {
+                                                         void* __restrict__ valv, int accumulate, double* __restrict__ hout) {
+    // hout (binary64 results only): a mapped page-locked host buffer that receives a copy of each value
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t p0 = __ldg(gptr + k), p1 = __ldg(gptr + k + 1);
         if (MODE == kModeDF64) {
@@ -1422,7 +1423,9 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
             df s = two_sum(sh, sl);
             double* out = reinterpret_cast<double*>(valv) + k;
             if (accumulate) s = df_add(d2df(*out), s);
-            *out = df2d(s);
+            const double r = df2d(s);
+            *out = r;
+            if (hout) hout[k] = r;
         } else {
             const float* kb = reinterpret_cast<const float*>(kbuf);
             float s = 0.0f;
@@ -1576,7 +1579,7 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, (int64_t)sms * 32));
     PendingEvent ev;
     prof_begin(ctx, "assemble_gather", ev);
-    gather_map_kernel<MODE><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
+    gather_map_kernel<MODE><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, nullptr);
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
@@ -1611,9 +1614,9 @@ int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate) {
     PendingEvent ev;
     prof_begin(ctx, "assemble_gather", ev);
     if (A->precision == FGPU_F32)
-        gather_map_kernel<kModeF32><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
+        gather_map_kernel<kModeF32><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, nullptr);
     else
-        gather_map_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate);
+        gather_map_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, nullptr);
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
@@ -1632,6 +1635,30 @@ int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int
         for (int i = 0; i < 4; ++i) FGPU_CUDA_CHECK(ctx, cudaStreamCreateWithFlags(&ctx->copy_streams[i], cudaStreamNonBlocking));
         for (int i = 0; i < 5; ++i) FGPU_CUDA_CHECK(ctx, cudaEventCreateWithFlags(&ctx->copy_events[i], cudaEventDisableTiming));
     }
+    // direct stores: the gather writes every value to device memory and to the mapped host buffer
+    double* hdev = nullptr;
+    if (ctx->host_transfer != FGPU_HOST_TRANSFER_COPY) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            hdev = static_cast<double*>(pa.devicePointer);
+        else
+            cudaGetLastError();
+        if (!hdev && ctx->host_transfer == FGPU_HOST_TRANSFER_DIRECT) {
+            ctx->err = "direct host transfer: the host buffer is not page-locked and mapped";
+            return FGPU_ERR_INVALID;
+        }
+    }
+    if (hdev) {
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, (int64_t)sms * 32));
+        PendingEvent ev;
+        prof_begin(ctx, "assemble_gather", ev);
+        gather_map_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, 0, hdev);
+        prof_end(ctx, ev);
+        ctx->launches++;
+        FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+        FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+        return FGPU_OK;
+    }
     const int64_t chunk = ((nnz + nchunks - 1) / nchunks + 255) & ~(int64_t)255;
     PendingEvent ev;
     prof_begin(ctx, "assemble_gather", ev);
@@ -1641,7 +1668,7 @@ int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int
         const int64_t k1 = std::min(nnz, k0 + chunk);
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((k1 - k0 + 255) / 256, (int64_t)sms * 32));
         gather_map_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(k1 - k0, V->d_gptr + k0, V->d_gidx, A->d_kbuf,
-                                                                         (double*)A->d_val + k0, 0);
+                                                                         (double*)A->d_val + k0, 0, nullptr);
         ctx->launches++;
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
         FGPU_CUDA_CHECK(ctx, cudaEventRecord(ctx->copy_events[c], ctx->stream));

@@ -137,6 +137,7 @@ struct fgpu_ctx {
     int64_t capture_launches0 = 0;
     cudaStream_t copy_streams[4] = {nullptr, nullptr, nullptr, nullptr};   // large host<->device copies in chunks
     cudaEvent_t copy_events[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int host_transfer = 0;         // FGPU_HOST_TRANSFER_*: how results reach host buffers
 };
 
 struct fgpu_graph {

@@ -48,6 +48,12 @@ class Environment:
     def launches(self):
         return int(self.lib.fgpu_launch_count(self.h))
 
+    def set_host_transfer(self, mode="auto"):
+        """How host-output assembly moves values: "auto", "copy" (copy engines) or "direct" (kernel stores
+        into the page-locked host buffer)."""
+        m = {"auto": _ffi.HOST_TRANSFER_AUTO, "copy": _ffi.HOST_TRANSFER_COPY, "direct": _ffi.HOST_TRANSFER_DIRECT}[mode]
+        self.check(self.lib.fgpu_set_host_transfer(self.h, m))
+
     def prof(self, name):
         n = C.c_int64()
         ms = C.c_double()

@@ -57,6 +57,12 @@ extern "C" {
                                      built once per space. AUTO picks it when its buffers fit in device
                                      memory, else FGPU_ALGO_GATHER (elasticity: native FP64 / binary32) */
 
+/* how fgpu_assemble_matrix_host moves the values to host memory */
+#define FGPU_HOST_TRANSFER_AUTO 0   /* DIRECT when the host buffer is page-locked and mapped, else COPY */
+#define FGPU_HOST_TRANSFER_COPY 1   /* copy-engine transfers of ranges of entries, overlapping the gather */
+#define FGPU_HOST_TRANSFER_DIRECT 2 /* the gather kernel stores each value to device and host memory
+                                       (page-locked buffers only; over NVLink-C2C on Grace hosts) */
+
 #define FGPU_RANGE_ELEMENTS 0       /* _range=elements(mesh) */
 #define FGPU_RANGE_BOUNDARY_FACES 1 /* _range=boundaryfaces(mesh): faces of one element */
 #define FGPU_RANGE_MARKED_FACES 2   /* boundary faces whose vertices all have x <= range_xmax
@@ -240,6 +246,8 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* fo
  * to the host while the next is gathered (pin host_val for the overlap); other forms assemble, then
  * copy. The device values are the same as after fgpu_assemble_matrix. */
 int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, double* host_val);
+/* FGPU_HOST_TRANSFER_* for later fgpu_assemble_matrix_host calls (default AUTO) */
+int fgpu_set_host_transfer(fgpu_ctx* ctx, int mode);
 int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, const double* d_kappa,
                              int accumulate);
 

@@ -255,3 +255,38 @@ def test_assemble_matrix_host(env, precision):
     env.check(env.lib.fgpu_assemble_matrix_host(env.h, a.h, C.byref(d), out.ctypes.data_as(C.c_void_p)))
     assert np.array_equal(out, ref)
     assert np.array_equal(a.values().astype(np.float64), ref)
+
+
+@pytest.mark.parametrize("mode", ["auto", "direct", "copy"])
+def test_assemble_matrix_host_transfer_modes(env, mode):
+    """Host-output assembly into a page-locked buffer: direct stores from the gather kernel and copy-engine
+    ranges give the device values bit for bit; direct stores refuse a pageable buffer."""
+    import ctypes as C
+    import torch
+    from feelpp_gb300 import _ffi, fe
+    xyz, tets = mesh(10, perturb=0.2)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    u, v = V.element(), V.element()
+    integral = fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v))
+    a = fpp.form2(test=V, trial=V)
+    a.assign(integral)
+    ref = a.values()
+    d, karr = fe.Form2._desc_of(integral, _ffi.ALGO_AUTO)
+    d.kappa_elem = karr.ctypes.data_as(C.c_void_p)
+    pinned = torch.zeros(a.nnz, dtype=torch.float64).pin_memory()
+    env.set_host_transfer(mode)
+    try:
+        a.zero()
+        env.check(env.lib.fgpu_assemble_matrix_host(env.h, a.h, C.byref(d), C.c_void_p(pinned.data_ptr())))
+        assert np.array_equal(pinned.numpy(), ref)
+        assert np.array_equal(a.values(), ref)
+        pageable = np.zeros(a.nnz)
+        rc = env.lib.fgpu_assemble_matrix_host(env.h, a.h, C.byref(d), pageable.ctypes.data_as(C.c_void_p))
+        if mode == "direct":
+            assert _ffi.ERROR_NAMES.get(rc) == "FGPU_ERR_INVALID"
+        else:
+            assert rc == 0 and np.array_equal(pageable, ref)
+    finally:
+        env.set_host_transfer("auto")
