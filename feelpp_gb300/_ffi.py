@@ -81,6 +81,10 @@ SIGNATURES = {
     "fgpu_sync": (i32, [P]),
     "fgpu_launch_count": (i64, [P]),
     "fgpu_mesh_upload": (i32, [P, i64, P, i64, P, PP]),
+    "fgpu_mesh_upload_hex": (i32, [P, i64, P, i64, P, PP]),
+    "fgpu_host_hex_dof_table": (i32, [i64, i64, P, i32, P, C.POINTER(i64)]),
+    "fgpu_host_hex_ref_tables": (i32, [i32, i32, P, P, P, P, P, C.POINTER(i32)]),
+    "fgpu_mesh_cell_vertices": (i32, [P, C.POINTER(i32)]),
     "fgpu_mesh_set_coords": (i32, [P, P]),
     "fgpu_mesh_destroy": (i32, [P]),
     "fgpu_space_create": (i32, [P, P, i32, i32, PP]),

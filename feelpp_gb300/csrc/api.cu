@@ -226,6 +226,40 @@ int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, c
     return FGPU_OK;
 }
 
+int fgpu_mesh_upload_hex(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nh, const int32_t* hexes, fgpu_mesh** out) {
+    FGPU_NO_CAPTURE(ctx, "mesh_upload_hex");
+    if (!ctx || !out || !xyz || !hexes || nv <= 0 || nh <= 0) return set_err(ctx, FGPU_ERR_INVALID, "mesh_upload_hex: bad arguments");
+    *out = nullptr;
+    for (int64_t k = 0; k < 8 * nh; ++k)
+        if (hexes[k] < 0 || hexes[k] >= nv) return set_err(ctx, FGPU_ERR_OUT_OF_RANGE, "hexahedron vertex index out of range");
+    fgpu_mesh* M = new (std::nothrow) fgpu_mesh();
+    if (!M) return set_err(ctx, FGPU_ERR_ALLOC, "host allocation");
+    M->ctx = ctx;
+    M->cv = 8;
+    M->nv = nv;
+    M->nt = nh;
+    M->h_xyz.assign(xyz, xyz + 3 * nv);
+    M->h_tets.assign(hexes, hexes + 8 * nh);
+    int rc = dev_alloc(ctx, &M->d_xyz, 3 * nv);
+    if (!rc) rc = dev_alloc(ctx, &M->d_tets, 8 * nh);
+    if (rc) { cudaFree(M->d_xyz); delete M; return rc; }
+    cudaMemcpyAsync(M->d_xyz, xyz, 3 * nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(M->d_tets, hexes, 8 * nh * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(M->d_xyz); cudaFree(M->d_tets); delete M;
+        return set_err(ctx, FGPU_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = M;
+    return FGPU_OK;
+}
+
+int fgpu_mesh_cell_vertices(const fgpu_mesh* M, int* nverts) {
+    if (!M || !nverts) return FGPU_ERR_INVALID;
+    *nverts = M->cv;
+    return FGPU_OK;
+}
+
 int fgpu_mesh_set_coords(fgpu_mesh* M, const double* xyz) {
     if (!M || !xyz) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = M->ctx;
@@ -252,6 +286,7 @@ int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* M, int order, int ncomp, fgpu_sp
     if (!ctx || !M || !out) return set_err(ctx, FGPU_ERR_INVALID, "space_create: bad arguments");
     if (order < 1 || order > 3) return set_err(ctx, FGPU_ERR_INVALID, "order must be 1, 2 or 3");
     if (ncomp != 1 && ncomp != 3) return set_err(ctx, FGPU_ERR_INVALID, "ncomp must be 1 or 3");
+    if (M->cv == 8 && (order > 2 || ncomp != 1)) return set_err(ctx, FGPU_ERR_INVALID, "hexahedra: scalar Q1 and Q2 spaces");
     *out = nullptr;
     fgpu_space* V = new (std::nothrow) fgpu_space();
     if (!V) return set_err(ctx, FGPU_ERR_ALLOC, "host allocation");
@@ -259,9 +294,14 @@ int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* M, int order, int ncomp, fgpu_sp
     V->mesh = M;
     V->order = order;
     V->ncomp = ncomp;
-    V->n = nloc_of(order);
+    V->n = M->cv == 8 ? hex_nloc(order) : nloc_of(order);
     std::string err;
-    if (!ctx->host_setup) {
+    if (M->cv == 8) {
+        if (!build_hex_topology(M->nv, M->nt, M->h_tets.data(), order, V->topo, err)) {
+            delete V;
+            return set_err(ctx, FGPU_ERR_INVALID, err);
+        }
+    } else if (!ctx->host_setup) {
         // dof table and incidence on the device; the host path takes the meshes it cannot handle
         ctx->err.clear();
         const int rcd = build_space_device(ctx, V);
@@ -277,7 +317,7 @@ int fgpu_space_create(fgpu_ctx* ctx, fgpu_mesh* M, int order, int ncomp, fgpu_sp
         if (rcd != FGPU_ERR_INVALID) { delete V; return rcd; }   // bad input or a device error
         ctx->err.clear();                                          // outside the device path's limits
     }
-    if (!build_topology(M->nv, M->nt, M->h_tets.data(), order, V->topo, err)) {
+    if (M->cv == 4 && !build_topology(M->nv, M->nt, M->h_tets.data(), order, V->topo, err)) {
         delete V;
         return set_err(ctx, FGPU_ERR_INVALID, err);
     }
@@ -326,7 +366,9 @@ int fgpu_space_boundary_dofs(const fgpu_space* V, int xmax_on, double xmax, int6
     if (W->bnd_valid && W->bnd_xmax_on == xmax_on && (!xmax_on || W->bnd_xmax == xmax) && W->bnd_coords == W->mesh->coords_version) {
         nodes = W->bnd_nodes;
     } else {
-        if (boundary_nodes_device(V->ctx, V, xmax_on, xmax, nodes) != FGPU_OK)
+        if (V->mesh->cv == 8)
+            hex_boundary_nodes(V->mesh->nt, V->mesh->h_tets.data(), V->mesh->h_xyz.data(), V->topo, xmax_on, xmax, nodes);
+        else if (boundary_nodes_device(V->ctx, V, xmax_on, xmax, nodes) != FGPU_OK)
             boundary_nodes(V->mesh->nt, V->mesh->h_tets.data(), V->mesh->h_xyz.data(), V->topo, xmax_on, xmax, nodes);
         W->bnd_nodes = nodes;
         W->bnd_xmax_on = xmax_on;
@@ -537,6 +579,13 @@ static int auto_assembly_algo(fgpu_ctx* ctx, const fgpu_matrix* A) {
 
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
     if (!ctx || !A || !f) return set_err(ctx, FGPU_ERR_INVALID, "assemble_matrix: bad arguments");
+    if (A->space->mesh->cv == 8) {   // hexahedra: quadrature element kernel (trilinear map) + gather map
+        if (f->algo != FGPU_ALGO_AUTO && f->algo != FGPU_ALGO_TWO_PHASE)
+            return set_err(ctx, FGPU_ERR_INVALID, "hexahedra: two-phase assembly only");
+        const int rc = launch_assemble_hex(ctx, A, f, d_kappa, accumulate);
+        if (rc) return rc;
+        return finish(ctx);
+    }
     if (f->range == FGPU_RANGE_BOUNDARY_FACES || f->range == FGPU_RANGE_MARKED_FACES) {
         if (A->space->mesh->d_ho) return set_err(ctx, FGPU_ERR_INVALID, "face integrals: flat faces only (the mesh has curved elements)");
         if (f->kind != FGPU_FORM_LAPLACE_MASS || f->kappa != 0.0 || d_kappa || f->kappa_scale)
@@ -646,7 +695,7 @@ int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_des
     if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(ctx, A);
     const bool pipelined = f->kind == FGPU_FORM_LAPLACE_MASS && f->range == FGPU_RANGE_ELEMENTS && f->mass_h == 0.0 &&
                            f->dn_trial == 0.0 && f->dn_test == 0.0 && A->precision == FGPU_F64 && A->ncomp == 1 &&
-                           !V->mesh->d_ho && algo == FGPU_ALGO_TWO_PHASE;
+                           !V->mesh->d_ho && V->mesh->cv == 4 && algo == FGPU_ALGO_TWO_PHASE;
     if (!pipelined) {
         int rc = assemble_impl(ctx, A, f, d_kappa, 0);
         if (rc) return rc;
@@ -720,6 +769,12 @@ int fgpu_vector_destroy(fgpu_vector* v) {
 int fgpu_assemble_vector(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, fgpu_vector* out, int accumulate) {
     FGPU_NO_CAPTURE(ctx, "assemble_vector");
     if (!ctx || !V || !rhs || !out || out->n != V->ndof) return set_err(ctx, FGPU_ERR_INVALID, "assemble_vector: bad arguments");
+    if (V->mesh->cv == 8) {
+        if (rhs->range != FGPU_RANGE_ELEMENTS) return set_err(ctx, FGPU_ERR_INVALID, "hexahedra: load vectors over elements(mesh) only");
+        const int rc = launch_rhs_hex(ctx, V, rhs, out->d, accumulate);
+        const int rc2 = finish(ctx);
+        return rc ? rc : rc2;
+    }
     if (rhs->range == FGPU_RANGE_BOUNDARY_FACES || rhs->range == FGPU_RANGE_MARKED_FACES) {
         if (V->mesh->d_ho) return set_err(ctx, FGPU_ERR_INVALID, "face integrals: flat faces only (the mesh has curved elements)");
         if (rhs->kind != FGPU_RHS_CONST && rhs->kind != FGPU_RHS_FACE)
@@ -953,6 +1008,31 @@ int fgpu_host_dof_table(int64_t nv, int64_t nt, const int32_t* tets, int order, 
     return FGPU_OK;
 }
 
+int fgpu_host_hex_dof_table(int64_t nv, int64_t nh, const int32_t* hexes, int order, int32_t* l2g, int64_t* ndof) {
+    if (!hexes || nv <= 0 || nh <= 0) return FGPU_ERR_INVALID;
+    for (int64_t k = 0; k < 8 * nh; ++k)
+        if (hexes[k] < 0 || hexes[k] >= nv) return FGPU_ERR_OUT_OF_RANGE;
+    Topology topo;
+    std::string err;
+    if (!build_hex_topology(nv, nh, hexes, order, topo, err)) return FGPU_ERR_INVALID;
+    if (ndof) *ndof = topo.nnodes;
+    if (l2g) std::copy(topo.l2n.begin(), topo.l2n.end(), l2g);
+    return FGPU_OK;
+}
+
+int fgpu_host_hex_ref_tables(int order, int qdeg, double* nodes, double* qx, double* qw, double* phi, double* dphi, int* nq) {
+    RefTables R;
+    std::string err;
+    if (!build_hex_ref_tables(order, qdeg, R, err)) return FGPU_ERR_INVALID;
+    if (nq) *nq = R.Q;
+    if (nodes) std::copy(R.nodes.begin(), R.nodes.end(), nodes);
+    if (qx) std::copy(R.qx.begin(), R.qx.end(), qx);
+    if (qw) std::copy(R.qw.begin(), R.qw.end(), qw);
+    if (phi) std::copy(R.phi.begin(), R.phi.end(), phi);
+    if (dphi) std::copy(R.dphi.begin(), R.dphi.end(), dphi);
+    return FGPU_OK;
+}
+
 int fgpu_host_pattern(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int64_t* ia, int32_t* ja,
                       int64_t* nnz) {
     if (!tets || !ia || nv <= 0 || nt <= 0 || (ncomp != 1 && ncomp != 3)) return FGPU_ERR_INVALID;
@@ -1016,7 +1096,7 @@ int fgpu_host_df64_ops(int op, int64_t n, const double* a, const double* b, doub
 int fgpu_norms_sine(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_vector* u, int quad_degree, double* l2, double* h1) {
     FGPU_NO_CAPTURE(ctx, "norms_sine");
     if (!ctx || !V || !u || !l2 || !h1 || u->n != V->ndof || V->ncomp != 1) return set_err(ctx, FGPU_ERR_INVALID, "norms: bad arguments");
-    if (V->mesh->d_ho) return set_err(ctx, FGPU_ERR_INVALID, "norms: affine elements only");
+    if (V->mesh->d_ho || V->mesh->cv != 4) return set_err(ctx, FGPU_ERR_INVALID, "norms: affine tetrahedra only");
     std::string err;
     DevTables* tab = get_dev_tables(V->order, quad_degree > 0 ? quad_degree : 2 * V->order, err);
     if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);

@@ -190,6 +190,7 @@ __global__ void geometry_kernel(int64_t nt, const double* __restrict__ xyz, cons
 int launch_geometry(fgpu_ctx* ctx, const fgpu_mesh* mesh, int kind, const double* d_kappa, double kappa,
                     double mass, double lam, double mu, double* d_coef) {
     (void)lam; (void)mu;
+    if (mesh->cv != 4) { ctx->err = "this operation takes tetrahedral meshes"; return FGPU_ERR_INVALID; }
     int threads = 256;
     int64_t blocks = (mesh->nt + threads - 1) / threads;
     if (blocks > 152 * 64) blocks = 152 * 64;
@@ -754,6 +755,7 @@ __global__ void geometry_df_kernel(int64_t nt, const double* __restrict__ xyz, c
 
 int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
                        float4* d_rec, const double* d_kscale) {
+    if (mesh->cv != 4) { ctx->err = "this operation takes tetrahedral meshes"; return FGPU_ERR_INVALID; }
     int threads = 256;
     int64_t blocks = std::min<int64_t>((mesh->nt + threads - 1) / threads, 152 * 16);
     if (blocks < 1) blocks = 1;
@@ -1466,7 +1468,7 @@ __global__ void __launch_bounds__(256) map_fill_kernel(int64_t nrows, int n, int
                                                        const uint32_t* __restrict__ gptr, uint32_t* __restrict__ gidx,
                                                        int* __restrict__ status) {
     __shared__ uint32_t cur[8][256];
-    __shared__ uint16_t tri[400];
+    __shared__ uint16_t tri[32 * 32];   // n <= 32 (checked by the launcher)
     for (int k = threadIdx.x; k < n * n; k += blockDim.x) tri[k] = trig[k];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1506,16 +1508,24 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
         return FGPU_ERR_INVALID;
     }
     if (!V->d_pos) { ctx->err = "gather map: no position table"; return FGPU_ERR_INVALID; }
-    std::string err;
-    DevTables* tab = get_dev_tables(V->order, 2 * V->order, err);
-    if (!tab) { ctx->err = err; return FGPU_ERR_INVALID; }
+    if (n > 32) { ctx->err = "gather map: more than 32 local dofs"; return FGPU_ERR_INVALID; }
+    // upper-triangle index of (min(i,j), max(i,j)) in the element buffer's row-major (i <= j) order
+    std::vector<uint16_t> htri((size_t)n * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const int a = std::min(i, j), b = std::max(i, j);
+            htri[(size_t)i * n + j] = (uint16_t)(a * n - a * (a - 1) / 2 + (b - a));
+        }
+    uint16_t* d_tri = nullptr;
     uint32_t *cnt = nullptr, *gptr = nullptr, *gidx = nullptr;
-    cudaError_t e = cudaMalloc(&cnt, nnz * sizeof(uint32_t));
+    cudaError_t e = cudaMalloc(&d_tri, htri.size() * sizeof(uint16_t));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_tri, htri.data(), htri.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&cnt, nnz * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&gptr, (nnz + 1) * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&gidx, contrib * sizeof(uint32_t));
     if (e != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(cnt); cudaFree(gptr); cudaFree(gidx);
+        cudaFree(d_tri); cudaFree(cnt); cudaFree(gptr); cudaFree(gidx);
         ctx->err = "gather map: allocation failed";
         return FGPU_ERR_ALLOC;
     }
@@ -1525,13 +1535,14 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
     map_count_kernel<<<sms * 16, 256, 0, ctx->stream>>>(nt, n, V->d_l2n, P.d_ia, V->d_pos, cnt);
     uint64_t total = 0;
     int rcs = scan_u32(ctx, cnt, gptr, nnz, &total);
-    if (rcs) { cudaFree(cnt); cudaFree(gptr); cudaFree(gidx); return rcs; }
+    if (rcs) { cudaFree(d_tri); cudaFree(cnt); cudaFree(gptr); cudaFree(gidx); return rcs; }
     map_fill_kernel<<<sms * 8, 256, 0, ctx->stream>>>(P.nrows, n, n * (n + 1) / 2, P.d_ia, V->d_inc_ptr, V->d_inc, V->d_pos,
-                                                      tab->d_tri, gptr, gidx, ctx->d_status);
+                                                      d_tri, gptr, gidx, ctx->d_status);
     ctx->launches += 2;
     e = cudaGetLastError();
     cudaStreamSynchronize(ctx->stream);
     cudaFree(cnt);
+    cudaFree(d_tri);
     if (e != cudaSuccess) {
         cudaFree(gptr); cudaFree(gidx);
         ctx->err = std::string("gather map: ") + cudaGetErrorString(e);

@@ -139,7 +139,8 @@ int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const 
         const fgpu_form_desc& f = descs[k];
         if (!A) return batch_err(ctx, FGPU_ERR_INVALID, "batch_create: null matrix");
         if (A->ctx != ctx) return batch_err(ctx, FGPU_ERR_INVALID, "batch_create: matrix of another context");
-        if (A->space->mesh->d_ho) return batch_err(ctx, FGPU_ERR_INVALID, "batch_create: affine elements only");
+        if (A->space->mesh->d_ho || A->space->mesh->cv != 4)
+            return batch_err(ctx, FGPU_ERR_INVALID, "batch_create: affine tetrahedra only");
         const fgpu_space* V = A->space;
         if (f.kind != FGPU_FORM_LAPLACE_MASS || A->ncomp != 1)
             return batch_err(ctx, FGPU_ERR_INVALID, "batch_create: batches hold scalar Laplace/mass forms");

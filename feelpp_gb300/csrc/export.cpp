@@ -1,6 +1,6 @@
 // EnSight Gold export of device results (the reference's default exporter
 // format, feelpp/feel/feelfilters/exporterensightgold.hpp): the mesh as one
-// part of 4-node tetrahedra and nodal scalar fields, in "C Binary" files
+// part of 4-node tetrahedra (or 8-node hexahedra) and nodal scalar fields, in "C Binary" files
 // written on the host after one copy of each field from the device.
 //
 // Files for prefix P: P.case (text), P.geo, and P.<name>.scl per field. The
@@ -59,7 +59,7 @@ extern "C" int fgpu_export_ensight(const fgpu_space* V, const char* prefix, int 
     FGPU_CUDA_CHECK(ctx, cudaMemcpy(l2n.data(), V->d_l2n, l2n.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
     std::vector<int64_t> vdof(nv, -1);
     for (int64_t e = 0; e < nt; ++e)
-        for (int v = 0; v < 4; ++v) vdof[M->h_tets[4 * e + v]] = l2n[(size_t)e * n + v];
+        for (int v = 0; v < M->cv; ++v) vdof[M->h_tets[(size_t)M->cv * e + v]] = l2n[(size_t)e * n + v];
     const std::string base(prefix);
     std::string stem = base;
     const size_t slash = stem.find_last_of('/');
@@ -70,7 +70,7 @@ extern "C" int fgpu_export_ensight(const fgpu_space* V, const char* prefix, int 
         if (!f) { ctx->err = "export: cannot write " + base + ".geo"; return FGPU_ERR_INVALID; }
         put80(f, "C Binary");
         put80(f, "feelpp_gb300 export");
-        put80(f, "tetrahedral mesh");
+        put80(f, M->cv == 8 ? "hexahedral mesh" : "tetrahedral mesh");
         put80(f, "node id off");
         put80(f, "element id off");
         put80(f, "part");
@@ -83,9 +83,11 @@ extern "C" int fgpu_export_ensight(const fgpu_space* V, const char* prefix, int 
             for (int64_t i = 0; i < nv; ++i) c[i] = (float)M->h_xyz[3 * i + d];
             std::fwrite(c.data(), sizeof(float), nv, f);
         }
-        put80(f, "tetra4");
+        // EnSight's hexa8 numbers the bottom face counter-clockwise, then the top face: the reference
+        // hexahedron's vertex order
+        put80(f, M->cv == 8 ? "hexa8" : "tetra4");
         put_i32(f, (int32_t)nt);
-        std::vector<int32_t> conn((size_t)nt * 4);
+        std::vector<int32_t> conn((size_t)nt * M->cv);
         for (size_t k = 0; k < conn.size(); ++k) conn[k] = M->h_tets[k] + 1;
         std::fwrite(conn.data(), sizeof(int32_t), conn.size(), f);
         const bool ok = std::ferror(f) == 0;

@@ -61,6 +61,16 @@ struct Topology {
 };
 bool build_topology(int64_t nv, int64_t nt, const int32_t* tets, int order, Topology& topo, std::string& err);
 
+// hexahedral meshes (Q1 geometry; Q1/Q2 spaces)
+extern const int kHexEdgeVerts[12][2];
+extern const int kHexFaceVerts[6][4];
+int hex_nloc(int order);
+void hex_dof_points(int order, std::vector<double>& pts);
+bool build_hex_ref_tables(int order, int qdeg, RefTables& out, std::string& err);
+bool build_hex_topology(int64_t nv, int64_t nh, const int32_t* hexes, int order, Topology& topo, std::string& err);
+bool hex_boundary_nodes(int64_t nh, const int32_t* hexes, const double* xyz, const Topology& topo, int xmax_on, double xmax,
+                        std::vector<int32_t>& nodes);
+
 struct NodePattern {                 // scalar node-to-node pattern (COUPLED + diagonal)
     int64_t nrows = 0, nnz = 0;
     int max_row = 0;
@@ -160,7 +170,8 @@ struct fgpu_mesh {
     std::vector<double> h_xyz;       // host copy (refreshed from the device when stale)
     bool h_xyz_stale = false;
     uint64_t coords_version = 0;     // incremented whenever the coordinates change
-    std::vector<int32_t> h_tets;
+    int cv = 4;                      // vertices per element: 4 (tetrahedra) or 8 (hexahedra)
+    std::vector<int32_t> h_tets;     // T x cv element vertices
     double* d_xyz = nullptr;
     int32_t* d_tets = nullptr;
     double* d_ho = nullptr;          // curved (P2-geometry) elements: T x 6 x 3 edge nodes (e2p order), or null
@@ -307,6 +318,8 @@ int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);
 int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate);
 int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate);
 int launch_rhs_ho(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate);
+int launch_assemble_hex(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate);
+int launch_rhs_hex(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate);
 int boundary_nodes_device(fgpu_ctx* ctx, const fgpu_space* V, int xmax_on, double xmax, std::vector<int32_t>& nodes);
 int launch_face_matrix(fgpu_ctx* ctx, fgpu_matrix* A, int range, double xmax, double mass, double mass_h, double dn_trial,
                        double dn_test, int accumulate);

@@ -34,9 +34,11 @@ namespace {
 
 enum HoMode { kHoF32 = 0, kHoDF64 = 1 };
 
-template <int N>
+// G geometric nodes per element: 10 (P2-geometry tetrahedra) or 8 (Q1 hexahedra)
+template <int N, int G>
 struct HoLimits {
-    static constexpr int QMAX = N == 4 ? 14 : N == 10 ? 31 : 43;   // quadrature degree <= 5 / 7 / 8
+    // tetrahedra: quadrature degree <= 5 / 7 / 8; hexahedra: m^3 Gauss points, m <= 4 (Q1) / 3 (Q2)
+    static constexpr int QMAX = G == 8 ? (N == 8 ? 64 : 27) : N == 4 ? 14 : N == 10 ? 31 : 43;
 };
 
 struct HoTables {
@@ -46,8 +48,9 @@ struct HoTables {
     float* d_ph = nullptr;     // Q n: basis values (df64 hi)
     float* d_pl = nullptr;     //      (df64 lo)
     double* d_phi = nullptr;   // Q n (binary64, load vector)
-    double* d_gd = nullptr;    // Q 10 3: reference gradients of the P2 geometric basis
-    double* d_gp = nullptr;    // Q 10: P2 geometric basis values
+    int G = 10;                // geometric nodes per element
+    double* d_gd = nullptr;    // Q G 3: reference gradients of the geometric basis (P2 tet / Q1 hex)
+    double* d_gp = nullptr;    // Q G: geometric basis values
     double* d_qw = nullptr;    // Q
     float* d_gdh = nullptr;    // Q 10 3: d_gd as double-float (hi)
     float* d_gdl = nullptr;    //                               (lo)
@@ -67,15 +70,19 @@ cudaError_t up(T** dst, const std::vector<T>& v) {
     return e;
 }
 
-HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg) {
+// hex: Q1/Q2 hexahedra (geometry Q1), else P-order tetrahedra with P2 geometry
+HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg, bool hex = false) {
     std::lock_guard<std::mutex> lock(g_ho_mutex);
-    const auto key = std::make_tuple(ctx->device, order, qdeg);
+    const auto key = std::make_tuple(ctx->device, order + (hex ? 100 : 0), qdeg);
     auto it = g_ho_tabs.find(key);
     if (it != g_ho_tabs.end()) return it->second;
     RefTables R, G;
     std::string err;
-    if (!build_ref_tables(order, qdeg, R, err) || !build_ref_tables(2, qdeg, G, err)) { ctx->err = err; return nullptr; }
+    const bool ok = hex ? build_hex_ref_tables(order, qdeg, R, err) && build_hex_ref_tables(1, qdeg, G, err)
+                        : build_ref_tables(order, qdeg, R, err) && build_ref_tables(2, qdeg, G, err);
+    if (!ok) { ctx->err = err; return nullptr; }
     HoTables* T = new HoTables();
+    T->G = G.n;
     T->n = R.n;
     T->Q = R.Q;
     T->ntri = R.n * (R.n + 1) / 2;
@@ -128,11 +135,12 @@ HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg) {
 }
 
 // K = sum_g X_g grad(psi_g)^T at one point, then |det K| and B = K^-T (cofactors / det)
-__device__ __forceinline__ double ho_map(const double* X /* 10 x 3 */, const double* gd /* 10 x 3 */, double B[9]) {
+template <int GN>
+__device__ __forceinline__ double ho_map(const double* X /* GN x 3 */, const double* gd /* GN x 3 */, double B[9]) {
     double K[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) K[k] = 0.0;
-    for (int g = 0; g < 10; ++g)
+    for (int g = 0; g < GN; ++g)
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -151,7 +159,7 @@ __device__ __forceinline__ df ldf(const float* h, const float* l, int k) { retur
 __device__ __forceinline__ df dfun(float2 v) { return df{v.x, v.y}; }
 __device__ __forceinline__ float2 dfpack(df v) { return make_float2(v.hi, v.lo); }
 
-template <int MODE, int N>
+template <int MODE, int N, int GN>
 __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
                                                          const double* __restrict__ ho, int Q, const float* __restrict__ Dhg,
                                                          const float* __restrict__ Dlg, const float* __restrict__ Phg,
@@ -162,13 +170,13 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                                                          double kappa, double mass, const double* __restrict__ kscale,
                                                          void* __restrict__ kbuf, int* __restrict__ status) {
     constexpr int NTRI = N * (N + 1) / 2;
-    constexpr int QM = HoLimits<N>::QMAX;
+    constexpr int QM = HoLimits<N, GN>::QMAX;
     constexpr int PER = (NTRI + 31) / 32;          // entries per lane
     __shared__ float Dh[QM * N * 3], Dl[QM * N * 3], Ph[QM * N], Pl[QM * N];
     __shared__ uint8_t ti[NTRI], tj[NTRI];
     __shared__ float2 Gs[4][QM * 7];               // per warp: G_q (00, 11, 22, 01, 02, 12) and m_q
     __shared__ float2 Ws[4][3 * N];                // per warp: W_q = G_q dphi_j
-    __shared__ float2 Xs[4][30];                   // per warp: the element's 10 nodes (double-float)
+    __shared__ float2 Xs[4][3 * GN];               // per warp: the element's geometric nodes (double-float)
     for (int k = threadIdx.x; k < Q * N * 3; k += blockDim.x) { Dh[k] = Dhg[k]; Dl[k] = Dlg[k]; }
     for (int k = threadIdx.x; k < Q * N; k += blockDim.x) { Ph[k] = Phg[k]; Pl[k] = Plg[k]; }
     for (int k = threadIdx.x; k < NTRI; k += blockDim.x) { ti[k] = tig[k]; tj[k] = tjg[k]; }
@@ -177,8 +185,10 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     const df ksd = d2df(kscale ? *kscale : 1.0), massd = d2df(mass);
     for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; e < nt; e += nw) {
-        // the element's nodes: 4 vertices, 6 edge nodes
-        if (lane < 12) {
+        // the element's nodes: tetrahedra 4 vertices and 6 edge nodes, hexahedra 8 vertices
+        if (GN == 8) {
+            if (lane < 24) Xs[warp][lane] = dfpack(d2df(xyz[3 * (int64_t)tets[8 * e + lane / 3] + lane % 3]));
+        } else if (lane < 12) {
             const int v = lane / 3, r = lane % 3;
             Xs[warp][lane] = dfpack(d2df(xyz[3 * (int64_t)tets[4 * e + v] + r]));
         } else if (lane < 30) {
@@ -189,14 +199,14 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
         // geometry: one quadrature point per lane; double-float on the FP32 pipes (binary32 for FP32
         // matrices): K = sum_g X_g grad(psi_g)^T, cofactors, det, B = cof / det, G = w J kappa B^T B
         for (int q = lane; q < Q; q += 32) {
-            const float* gh = gdh + (size_t)q * 30;
-            const float* gl = gdl + (size_t)q * 30;
+            const float* gh = gdh + (size_t)q * 3 * GN;
+            const float* gl = gdl + (size_t)q * 3 * GN;
             float2 g[7];
             if (MODE == kHoDF64) {
                 df K[9];
 #pragma unroll
                 for (int k = 0; k < 9; ++k) K[k] = df{0.0f, 0.0f};
-                for (int gg = 0; gg < 10; ++gg) {
+                for (int gg = 0; gg < GN; ++gg) {
                     const df d0 = df{__ldg(gh + 3 * gg), __ldg(gl + 3 * gg)};
                     const df d1 = df{__ldg(gh + 3 * gg + 1), __ldg(gl + 3 * gg + 1)};
                     const df d2 = df{__ldg(gh + 3 * gg + 2), __ldg(gl + 3 * gg + 2)};
@@ -239,7 +249,7 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                 float K[9];
 #pragma unroll
                 for (int k = 0; k < 9; ++k) K[k] = 0.0f;
-                for (int gg = 0; gg < 10; ++gg)
+                for (int gg = 0; gg < GN; ++gg)
 #pragma unroll
                     for (int r = 0; r < 3; ++r) {
                         const float x = Xs[warp][3 * gg + r].x + Xs[warp][3 * gg + r].y;
@@ -325,32 +335,39 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
 }
 
 // load vector on curved elements: thread per element, per point the map, J and the physical point
-template <int N>
+template <int N, int GN>
 __global__ void ho_rhs_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
                               const double* __restrict__ ho, int Q, const double* __restrict__ qw, const double* __restrict__ phi,
                               const double* __restrict__ gd, const double* __restrict__ gp, int fkind, double f0,
                               double* __restrict__ work, int* __restrict__ status) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
-        double X[30];
+        double X[3 * GN];
+        if (GN == 8) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v)
+            for (int v = 0; v < 8; ++v)
 #pragma unroll
-            for (int r = 0; r < 3; ++r) X[3 * v + r] = xyz[3 * (int64_t)tets[4 * e + v] + r];
+                for (int r = 0; r < 3; ++r) X[3 * v + r] = xyz[3 * (int64_t)tets[8 * e + v] + r];
+        } else {
 #pragma unroll
-        for (int k = 0; k < 18; ++k) X[12 + k] = ho[18 * e + k];
+            for (int v = 0; v < 4; ++v)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) X[3 * v + r] = xyz[3 * (int64_t)tets[4 * e + v] + r];
+#pragma unroll
+            for (int k = 0; k < 3 * GN - 12; ++k) X[12 + k] = ho[18 * e + k];
+        }
         double F[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) F[i] = 0.0;
         for (int q = 0; q < Q; ++q) {
             double B[9];
-            const double J = fabs(ho_map(X, gd + (size_t)q * 30, B));
+            const double J = fabs(ho_map<GN>(X, gd + (size_t)q * 3 * GN, B));
             if (!(J > 0.0) || !isfinite(J)) atomicOr(status, kStatusBadElement);
             double f = f0;
             if (fkind == FGPU_RHS_SINE) {
                 double p[3] = {0.0, 0.0, 0.0};
-                for (int g = 0; g < 10; ++g)
+                for (int g = 0; g < GN; ++g)
 #pragma unroll
-                    for (int r = 0; r < 3; ++r) p[r] = fma(X[3 * g + r], gp[q * 10 + g], p[r]);
+                    for (int r = 0; r < 3; ++r) p[r] = fma(X[3 * g + r], gp[q * GN + g], p[r]);
                 const double pi = 3.141592653589793;
                 f = 3.0 * pi * pi * sin(pi * p[0]) * sin(pi * p[1]) * sin(pi * p[2]);
             }
@@ -372,7 +389,86 @@ int ho_qdeg_ok(fgpu_ctx* ctx, int order, int qdeg) {
     return FGPU_OK;
 }
 
+int hex_qdeg_ok(fgpu_ctx* ctx, int order, int qdeg) {
+    const int lim = order == 1 ? 6 : 4;   // 4^3 / 3^3 Gauss points
+    if (qdeg > lim) {
+        ctx->err = "hexahedra: quadrature degree above " + std::to_string(lim) + " for this order";
+        return FGPU_ERR_INVALID;
+    }
+    return FGPU_OK;
+}
+
 }  // namespace
+
+// Q1/Q2 hexahedra: the curved-element kernels with the trilinear (Q1) map and tensor Gauss rules
+int launch_assemble_hex(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
+    fgpu_space* V = A->space;
+    const fgpu_mesh* M = V->mesh;
+    if (f->kind != FGPU_FORM_LAPLACE_MASS || V->ncomp != 1 || f->range != FGPU_RANGE_ELEMENTS || f->mass_h != 0.0 ||
+        f->dn_trial != 0.0 || f->dn_test != 0.0) {
+        ctx->err = "hexahedra: scalar Laplace/mass forms over elements(mesh) only";
+        return FGPU_ERR_INVALID;
+    }
+    const int qdeg = f->quad_degree > 0 ? f->quad_degree : 2 * V->order;
+    int rc = hex_qdeg_ok(ctx, V->order, qdeg);
+    if (rc) return rc;
+    HoTables* T = get_ho_tables(ctx, V->order, qdeg, true);
+    if (!T) return FGPU_ERR_INVALID;
+    const bool f32 = A->precision == FGPU_F32;
+    rc = ensure_two_phase(ctx, A, (size_t)M->nt * T->ntri * (f32 ? 4 : 8));
+    if (rc) return rc;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + 3) / 4, 152 * 32));
+    PendingEvent ev;
+    prof_begin(ctx, "assemble_elements_hex", ev);
+#define HEX_LAUNCH(MODE, NN)                                                                                                  \
+    ho_element_kernel<MODE, NN, 8><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, nullptr, T->Q, T->d_dh,       \
+                                                                   T->d_dl, T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh,    \
+                                                                   T->d_qwl, T->d_ti, T->d_tj, d_kappa, f->kappa, f->mass,     \
+                                                                   f->kappa_scale, A->d_kbuf, ctx->d_status)
+    if (V->n == 8) {
+        if (f32) HEX_LAUNCH(kHoF32, 8); else HEX_LAUNCH(kHoDF64, 8);
+    } else {
+        if (f32) HEX_LAUNCH(kHoF32, 27); else HEX_LAUNCH(kHoDF64, 27);
+    }
+#undef HEX_LAUNCH
+    prof_end(ctx, ev);
+    ctx->launches++;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    rc = launch_gather_phase(ctx, A, accumulate);
+    ctx->launches++;
+    return rc;
+}
+
+int launch_rhs_hex(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate) {
+    const fgpu_mesh* M = V->mesh;
+    if (V->ncomp != 1 || (rhs->kind != FGPU_RHS_SINE && rhs->kind != FGPU_RHS_CONST)) {
+        ctx->err = "hexahedra: scalar sine or constant sources only";
+        return FGPU_ERR_INVALID;
+    }
+    const int qdeg = rhs->quad_degree > 0 ? rhs->quad_degree : 2 * V->order;
+    int rc = hex_qdeg_ok(ctx, V->order, qdeg);
+    if (rc) return rc;
+    HoTables* T = get_ho_tables(ctx, V->order, qdeg, true);
+    if (!T) return FGPU_ERR_INVALID;
+    double* work = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&work, std::max<int64_t>(M->nt * V->n, 1) * sizeof(double)));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + 127) / 128, 152 * 32));
+    PendingEvent ev;
+    prof_begin(ctx, "rhs_element_hex", ev);
+    if (V->n == 8)
+        ho_rhs_kernel<8, 8><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, nullptr, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status);
+    else
+        ho_rhs_kernel<27, 8><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, nullptr, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status);
+    prof_end(ctx, ev);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) rc = launch_rhs_gather(ctx, V, work, d_out, accumulate);
+    ctx->launches++;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(work);
+    if (e != cudaSuccess) { ctx->err = std::string("hexahedral load vector: ") + cudaGetErrorString(e); return FGPU_ERR_CUDA; }
+    return rc;
+}
 
 int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
     fgpu_space* V = A->space;
@@ -394,7 +490,7 @@ int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, c
     PendingEvent ev;
     prof_begin(ctx, "assemble_elements_ho", ev);
 #define HO_LAUNCH(MODE, NN)                                                                                                   \
-    ho_element_kernel<MODE, NN><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_dh, T->d_dl,  \
+    ho_element_kernel<MODE, NN, 10><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_dh, T->d_dl,  \
                                                                 T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh, T->d_qwl,      \
                                                                 T->d_ti, T->d_tj, d_kappa,                                     \
                                                                 f->kappa, f->mass, f->kappa_scale, A->d_kbuf, ctx->d_status)
@@ -429,9 +525,9 @@ int launch_rhs_ho(fgpu_ctx* ctx, const fgpu_space* V, const fgpu_rhs_desc* rhs, 
     PendingEvent ev;
     prof_begin(ctx, "rhs_element_ho", ev);
     switch (V->n) {
-        case 4: ho_rhs_kernel<4><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
-        case 10: ho_rhs_kernel<10><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
-        default: ho_rhs_kernel<20><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
+        case 4: ho_rhs_kernel<4, 10><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
+        case 10: ho_rhs_kernel<10, 10><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
+        default: ho_rhs_kernel<20, 10><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_qw, T->d_phi, T->d_gd, T->d_gp, rhs->kind, rhs->c[0], work, ctx->d_status); break;
     }
     prof_end(ctx, ev);
     ctx->launches++;
@@ -452,6 +548,7 @@ extern "C" int fgpu_mesh_set_ho_nodes(fgpu_mesh* M, const double* ho) {
     if (!M) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = M->ctx;
     if (ctx->capturing) { ctx->err = "mesh_set_ho_nodes: not capturable"; return FGPU_ERR_INVALID; }
+    if (M->cv != 4) { ctx->err = "mesh_set_ho_nodes: tetrahedral meshes only"; return FGPU_ERR_INVALID; }
     if (!ho) {
         cudaFree(M->d_ho);
         M->d_ho = nullptr;

@@ -273,6 +273,7 @@ int build_space_device(fgpu_ctx* ctx, fgpu_space* V) {
     const fgpu_mesh* M = V->mesh;
     const int64_t nt = M->nt, nv = M->nv;
     const int order = V->order, n = V->n, ndpe = dofs_per_edge(order), ndpf = dofs_per_face(order);
+    if (M->cv != 4) return FGPU_ERR_INVALID;
     if (nv >= ((int64_t)1 << 21) || nt * 14 >= (int64_t)0xFFFFFFFF || nt >= ((int64_t)1 << 26)) return FGPU_ERR_INVALID;
     {
         const int rc = ensure_tables(ctx);
@@ -424,7 +425,7 @@ __global__ void boundary_mark_kernel(int64_t nt, const int32_t* __restrict__ tet
 int boundary_nodes_device(fgpu_ctx* ctx, const fgpu_space* V, int xmax_on, double xmax, std::vector<int32_t>& nodes) {
     const fgpu_mesh* M = V->mesh;
     const int64_t nt = M->nt;
-    if (M->nv >= ((int64_t)1 << 21) || nt == 0) return FGPU_ERR_INVALID;
+    if (M->cv != 4 || M->nv >= ((int64_t)1 << 21) || nt == 0) return FGPU_ERR_INVALID;
     if (ensure_tables(ctx) != FGPU_OK) return FGPU_ERR_INVALID;
     const int ndpe = dofs_per_edge(V->order), ndpf = dofs_per_face(V->order);
     std::vector<int> fl;

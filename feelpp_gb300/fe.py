@@ -97,15 +97,20 @@ def _ptr(a):
 class Mesh:
     """Tetrahedral mesh: vertex coordinates (V x 3) and elements (T x 4) in insertion order; with `ho`
     (T x 6 x 3 edge nodes, local edge order (1,2) (2,0) (0,1) (0,3) (1,3) (2,3)) the elements are curved
-    (P2 geometry, as a gmsh order-2 mesh read with GEOMAP_HO)."""
+    (P2 geometry, as a gmsh order-2 mesh read with GEOMAP_HO). Elements given as T x 8 vertex ids make a
+    hexahedral mesh (Mesh<Hypercube<3,1>>, reference vertex order: the z = -1 face counter-clockwise from
+    (-1,-1,-1), then the z = +1 face); its spaces are scalar Q1/Q2."""
 
     def __init__(self, xyz, tets, env=None, ho=None):
         self.env = env or environment()
         self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         self.tets = np.ascontiguousarray(tets, dtype=np.int32)
+        if self.tets.ndim != 2 or self.tets.shape[1] not in (4, 8):
+            raise ValueError("elements: T x 4 (tetrahedra) or T x 8 (hexahedra) vertex ids")
+        self.cell = "hex" if self.tets.shape[1] == 8 else "tet"
+        upload = self.env.lib.fgpu_mesh_upload_hex if self.cell == "hex" else self.env.lib.fgpu_mesh_upload
         h = C.c_void_p()
-        self.env.check(self.env.lib.fgpu_mesh_upload(self.env.h, len(self.xyz), _ptr(self.xyz), len(self.tets),
-                                                     _ptr(self.tets), C.byref(h)))
+        self.env.check(upload(self.env.h, len(self.xyz), _ptr(self.xyz), len(self.tets), _ptr(self.tets), C.byref(h)))
         self.h = h
         self.ho = None
         if ho is not None:

@@ -48,6 +48,32 @@ def kuhn_box(nx, ny=None, nz=None, lengths=(1.0, 1.0, 1.0), perturb=0.0, seed=12
     return xyz, tets.reshape(-1, 4).astype(np.int32)
 
 
+def hex_box(nx, ny=None, nz=None, lengths=(1.0, 1.0, 1.0), perturb=0.0, seed=1234):
+    """Structured hexahedral mesh of [0,Lx]x[0,Ly]x[0,Lz] (the grid of MeshStructured): the vertices and
+    their interior perturbation as in kuhn_box, one hexahedron per cell in the reference vertex order
+    (z = -1 face (0,0,0) (1,0,0) (1,1,0) (0,1,0), then the z = +1 face)."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    Lx, Ly, Lz = lengths
+    ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    hx, hy, hz = Lx / nx, Ly / ny, Lz / nz
+    xyz = np.stack([ii * hx, jj * hy, kk * hz], axis=-1).reshape(-1, 3).astype(np.float64)
+    if perturb > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-1.0, 1.0, size=xyz.shape) * (perturb * np.array([hx, hy, hz]))
+        interior = ((ii > 0) & (ii < nx) & (jj > 0) & (jj < ny) & (kk > 0) & (kk < nz)).reshape(-1)
+        xyz[interior] += d[interior]
+
+    def vid(i, j, k):
+        return (i * (ny + 1) + j) * (nz + 1) + k
+
+    ci, cj, ck = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ci, cj, ck = ci.reshape(-1), cj.reshape(-1), ck.reshape(-1)
+    corners = ((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1))
+    hexes = np.stack([vid(ci + a, cj + b, ck + c) for a, b, c in corners], axis=1)
+    return xyz, hexes.astype(np.int32)
+
+
 def lognormal_kappa(nt, seed=5678):
     rng = np.random.default_rng(seed)
     return rng.lognormal(0.0, 1.0, size=nt)

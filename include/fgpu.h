@@ -194,6 +194,14 @@ int fgpu_mesh_upload(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nt, c
                      fgpu_mesh** out);
 /* replace the vertex coordinates (host array, nv x 3): a moved mesh keeps its topology */
 int fgpu_mesh_set_coords(fgpu_mesh* mesh, const double* xyz);
+/* Hexahedral mesh (Mesh<Hypercube<3,1>>, e.g. from MeshStructured, feelpp/feel/feeldiscr/meshstructured.hpp):
+ * nh x 8 vertex ids in the reference hexahedron's order (feelpp/feel/feelmesh/refhypercube.hpp:148-183:
+ * the z = -1 face counter-clockwise from (-1,-1,-1), then the z = +1 face). Spaces: scalar Q1/Q2
+ * (fgpu_space_create order 1 or 2); forms: Laplace/mass over elements(mesh) with the trilinear map at
+ * every point of the tensor Gauss rule of feelpp/feel/feelpoly/gausshypercube.cpp; load vectors; on()
+ * through fgpu_space_boundary_dofs; CG/AMG on the assembled matrix; EnSight export. */
+int fgpu_mesh_upload_hex(fgpu_ctx* ctx, int64_t nv, const double* xyz, int64_t nh, const int32_t* hexes, fgpu_mesh** out);
+int fgpu_mesh_cell_vertices(const fgpu_mesh* mesh, int* nverts);   /* 4 or 8 */
 /* curved (P2-geometry, GEOMAP_HO) elements: ho = T x 6 x 3 coordinates of each element's edge nodes in
  * the local edge order (1,2) (2,0) (0,1) (0,3) (1,3) (2,3) (host array, copied); NULL makes the mesh
  * affine again. On a curved mesh the scalar Laplace/mass form and the sine / constant load vector are
@@ -375,6 +383,11 @@ int fgpu_host_dof_table(int64_t nv, int64_t nt, const int32_t* tets, int order, 
  * ja == NULL to fill ia (ndof + 1) and get *nnz, then again with ja (nnz). */
 int fgpu_host_pattern(int64_t nv, int64_t nt, const int32_t* tets, int order, int ncomp, int64_t* ia, int32_t* ja,
                       int64_t* nnz);
+/* Q1/Q2 on hexahedra: first-encounter dof table (nh x 8 or nh x 27) and the reference tables (local dof
+ * points n x 3, Gauss points Q x 3 and weights, basis values Q x n and reference gradients Q x n x 3;
+ * call with NULL arrays to get Q) */
+int fgpu_host_hex_dof_table(int64_t nv, int64_t nh, const int32_t* hexes, int order, int32_t* l2g, int64_t* ndof);
+int fgpu_host_hex_ref_tables(int order, int qdeg, double* nodes, double* qx, double* qw, double* phi, double* dphi, int* nq);
 /* Lagrange node set (nloc x 3), basis values (Q x nloc) and reference gradients
  * (Q x nloc x 3) at the degree-qdeg rule, and the reference tensors
  * S (9 x nloc x nloc) and M (nloc x nloc); any output may be NULL. Returns Q in *npts. */
