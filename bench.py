@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--nprob", type=int, default=512, help="batch: number of independent problems")
     p.add_argument("--nmax", type=int, default=40, help="batch: largest cube resolution")
     p.add_argument("--heat-steps", type=int, default=100, help="heat: backward-Euler steps")
-    p.add_argument("--workload", default="assembly", choices=["assembly", "matfree", "elasticity", "batch", "heat", "curved"],
+    p.add_argument("--workload", default="assembly", choices=["assembly", "matfree", "elasticity", "batch", "heat", "curved", "hex"],
                    help="assembly: the headline P2 assembly + CG line; matfree: P3 matrix-free operator and CG; "
                         "elasticity: vector P2 linear elasticity assembly (FP64, FP32) and CG; batch: many independent "
                         "problems in one persistent launch; heat: graph-replayed reassembly for backward Euler; "
@@ -902,6 +902,72 @@ def run_curved(args):
     print(json.dumps(res), flush=True)
 
 
+def run_hex(args):
+    """Hexahedral mesh (the structured grid of MeshStructured, interior vertices perturbed 0.15 h): Q-order
+    kappa grad.grad + mass assembly (lognormal kappa, tensor Gauss rule of degree 2 order) in FP64 and
+    FP32; CG + AMG to 1e-10 on the Poisson problem (sine source, homogeneous Dirichlet); the numpy oracle
+    times the same assembly on an 8^3 sample."""
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    from oracle import hexoracle
+
+    env = fpp.Environment(device=0, profile=True)
+    xyz, hexes = meshgen.hex_box(args.n, perturb=0.15, seed=1234)
+    kappa = meshgen.lognormal_kappa(len(hexes), seed=5678)
+    M = fpp.Mesh(xyz, hexes, env=env)
+    V = fpp.Pch(M, args.order)
+    u, v = V.element(), V.element()
+    it = fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    with ClockSampler(0) as clk:
+        for name, prec in (("fp64", "f64"), ("fp32", "f32")):
+            a = fpp.form2(test=V, trial=V, precision=prec)
+            for _ in range(max(args.warmup, 1)):
+                a.assign(it)
+            env.prof_reset()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(args.steps):
+                a.assign(it)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            ne, te = env.prof("assemble_elements_hex")
+            ng, tg = env.prof("assemble_gather")
+            out[name] = {"ms": ms, "gnnz_per_s": a.nnz / (ms / 1e3) / 1e9, "element_ms": te / max(ne, 1),
+                         "gather_ms": tg / max(ng, 1)}
+        nnz = a.nnz
+        a = fpp.form2(test=V, trial=V)
+        a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.gradt(u), fpp.grad(v))))
+        l = fpp.form1(test=V)
+        l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+        a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+        w = V.element()
+        sol = a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
+    cpu = None
+    if not args.no_cpu:
+        from oracle import pyoracle
+        xs, hs = meshgen.hex_box(8, perturb=0.15, seed=1234)
+        ks = meshgen.lognormal_kappa(len(hs), seed=5678)
+        Ns, l2s = hexoracle.dof_table(hs, args.order)
+        ias, jas = pyoracle.pattern(Ns, l2s)
+        t0 = time.perf_counter()
+        hexoracle.assemble(args.order, xs, hs, l2s, ias, jas, kappa=ks, mass=1.0)
+        dt = time.perf_counter() - t0
+        cpu = {"value": len(jas) / dt / 1e9, "unit": "Gnnz/s", "cores": 1, "kind": "port",
+               "sample": "numpy oracle (element matrices by einsum, scatter per element row) on the 8^3 hexahedral "
+                         "mesh, Q%d, nnz %d" % (args.order, len(jas))}
+    res = {"metric": "Q%d hexahedral assembly Gnnz/s" % args.order,
+           "value": out["fp64"]["gnnz_per_s"], "unit": "Gnnz/s", "n_gpus": 1, "steps": args.steps,
+           "higher_is_better": True, "dtype": "f64 (df64 entries)", "data": "synthetic",
+           "config": {"workload": "Q%d Laplace + mass on the %d^3 hexahedral grid, interior vertices perturbed 0.15 h "
+                                  "(T = %d, N = %d, nnz = %d)" % (args.order, args.n, len(hexes), V.ndof, nnz)},
+           "assembly": out, "gamg_solve": sol, "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(res), flush=True)
+
+
 def run_heat(args):
     """P2 heat equation on the 64^3 Kuhn cube: backward Euler, (M + dt kappa(t) K) u^{n+1}
     = M u^n + dt F with kappa(t) = 1 + 0.5 sin t and homogeneous Dirichlet rows. Each step
@@ -997,6 +1063,9 @@ def main():
         return
     if args.workload == "curved":
         run_curved(args)
+        return
+    if args.workload == "hex":
+        run_hex(args)
         return
     if args.workload == "heat":
         run_heat(args)
