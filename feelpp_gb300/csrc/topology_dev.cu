@@ -341,8 +341,18 @@ int build_space_device(fgpu_ctx* ctx, fgpu_space* V) {
     l2n_kernel<<<eb, 256, 0, s>>>(nt, M->d_tets, n, ndpe, ndpf, kv, ke, kf, occ_e, occ_f, off, V->d_l2n);
     ctx->launches++;
     // incidence
-    if (N > nt * 14) { cleanup(); ctx->err = "device dof table: internal size check"; return FGPU_ERR_CUDA; }
-    uint32_t* cptr = off;                 // reuse: N + 1 <= 14 T + 1 entries
+    // the list offsets reuse `off` (14 T + 1 entries); very small meshes (a P3 element alone carries 20
+    // nodes) get their own buffer
+    uint32_t* cptr = off;
+    if (N > nt * 14) {
+        cudaStreamSynchronize(s);         // l2n_kernel has read the entity offsets
+        cudaFree(off);
+        off = nullptr;
+        if (cudaMalloc(&off, (size_t)(N + 1) * sizeof(uint32_t)) != cudaSuccess) {
+            cudaGetLastError(); cleanup(); ctx->err = "device dof table: allocation failed"; return FGPU_ERR_ALLOC;
+        }
+        cptr = off;
+    }
     cudaMemsetAsync(cnt, 0, (size_t)(N + 1) * sizeof(uint32_t), s);
     const int64_t tn = nt * n;
     const int cb = (int)std::max<int64_t>(1, std::min<int64_t>((tn + 255) / 256, (int64_t)sms * 16));
