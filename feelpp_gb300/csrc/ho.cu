@@ -159,7 +159,8 @@ __device__ __forceinline__ df ldf(const float* h, const float* l, int k) { retur
 __device__ __forceinline__ df dfun(float2 v) { return df{v.x, v.y}; }
 __device__ __forceinline__ float2 dfpack(df v) { return make_float2(v.hi, v.lo); }
 
-template <int MODE, int N, int GN>
+// LPG lanes per element (32: one element per warp; 8: four elements per warp, for at most 8 points)
+template <int MODE, int N, int GN, int LPG = 32>
 __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
                                                          const double* __restrict__ ho, int Q, const float* __restrict__ Dhg,
                                                          const float* __restrict__ Dlg, const float* __restrict__ Phg,
@@ -170,35 +171,39 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                                                          double kappa, double mass, const double* __restrict__ kscale,
                                                          void* __restrict__ kbuf, int* __restrict__ status) {
     constexpr int NTRI = N * (N + 1) / 2;
-    constexpr int QM = HoLimits<N, GN>::QMAX;
-    constexpr int PER = (NTRI + 31) / 32;          // entries per lane
+    constexpr int EPW = 32 / LPG;                  // elements per warp
+    constexpr int QM = LPG == 32 ? HoLimits<N, GN>::QMAX : LPG;
+    constexpr int PER = (NTRI + LPG - 1) / LPG;    // entries per lane
     __shared__ float Dh[QM * N * 3], Dl[QM * N * 3], Ph[QM * N], Pl[QM * N];
     __shared__ uint8_t ti[NTRI], tj[NTRI];
-    __shared__ float2 Gs[4][QM * 7];               // per warp: G_q (00, 11, 22, 01, 02, 12) and m_q
-    __shared__ float2 Ws[4][3 * N];                // per warp: W_q = G_q dphi_j
-    __shared__ float2 Xs[4][3 * GN];               // per warp: the element's geometric nodes (double-float)
+    __shared__ float2 Gs[4][EPW][QM * 7];          // per element: G_q (00, 11, 22, 01, 02, 12) and m_q
+    __shared__ float2 Ws[4][EPW][3 * N];           // per element: W_q = G_q dphi_j
+    __shared__ float2 Xs[4][EPW][3 * GN];          // per element: its geometric nodes (double-float)
     for (int k = threadIdx.x; k < Q * N * 3; k += blockDim.x) { Dh[k] = Dhg[k]; Dl[k] = Dlg[k]; }
     for (int k = threadIdx.x; k < Q * N; k += blockDim.x) { Ph[k] = Phg[k]; Pl[k] = Plg[k]; }
     for (int k = threadIdx.x; k < NTRI; k += blockDim.x) { ti[k] = tig[k]; tj[k] = tjg[k]; }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = lane / LPG, gl = lane % LPG;
+    float2* XsG = Xs[warp][grp];
+    float2* GsG = Gs[warp][grp];
+    float2* WsG = Ws[warp][grp];
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     const df ksd = d2df(kscale ? *kscale : 1.0), massd = d2df(mass);
-    for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; e < nt; e += nw) {
+    for (int64_t e0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * EPW; e0 < nt; e0 += nw * EPW) {
+        const int64_t e = e0 + grp;
+        const bool live = e < nt;                  // the warp's loops stay uniform; a dead slot writes nothing
         // the element's nodes: tetrahedra 4 vertices and 6 edge nodes, hexahedra 8 vertices
-        if (GN == 8) {
-            if (lane < 24) Xs[warp][lane] = dfpack(d2df(xyz[3 * (int64_t)tets[8 * e + lane / 3] + lane % 3]));
-        } else if (lane < 12) {
-            const int v = lane / 3, r = lane % 3;
-            Xs[warp][lane] = dfpack(d2df(xyz[3 * (int64_t)tets[4 * e + v] + r]));
-        } else if (lane < 30) {
-            Xs[warp][lane] = dfpack(d2df(ho[18 * e + (lane - 12)]));
+        for (int k = gl; k < 3 * GN && live; k += LPG) {
+            if (GN == 8) XsG[k] = dfpack(d2df(xyz[3 * (int64_t)tets[8 * e + k / 3] + k % 3]));
+            else if (k < 12) XsG[k] = dfpack(d2df(xyz[3 * (int64_t)tets[4 * e + k / 3] + k % 3]));
+            else XsG[k] = dfpack(d2df(ho[18 * e + (k - 12)]));
         }
         __syncwarp();
-        const df kap = df_mul(d2df(d_kappa ? d_kappa[e] : kappa), ksd);
+        const df kap = live ? df_mul(d2df(d_kappa ? d_kappa[e] : kappa), ksd) : df{0.0f, 0.0f};
         // geometry: one quadrature point per lane; double-float on the FP32 pipes (binary32 for FP32
         // matrices): K = sum_g X_g grad(psi_g)^T, cofactors, det, B = cof / det, G = w J kappa B^T B
-        for (int q = lane; q < Q; q += 32) {
+        for (int q = gl; q < Q; q += LPG) {
             const float* gh = gdh + (size_t)q * 3 * GN;
             const float* gl = gdl + (size_t)q * 3 * GN;
             float2 g[7];
@@ -212,7 +217,7 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                     const df d2 = df{__ldg(gh + 3 * gg + 2), __ldg(gl + 3 * gg + 2)};
 #pragma unroll
                     for (int r = 0; r < 3; ++r) {
-                        const df x = dfun(Xs[warp][3 * gg + r]);
+                        const df x = live ? dfun(XsG[3 * gg + r]) : df{(float)(gg == r + 1), 0.0f};
                         K[3 * r] = df_add(K[3 * r], df_mul(x, d0));
                         K[3 * r + 1] = df_add(K[3 * r + 1], df_mul(x, d1));
                         K[3 * r + 2] = df_add(K[3 * r + 2], df_mul(x, d2));
@@ -230,7 +235,7 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                 C[8] = df_sub(df_mul(K[0], K[4]), df_mul(K[1], K[3]));
                 const df det = df_add(df_add(df_mul(K[0], C[0]), df_mul(K[1], C[1])), df_mul(K[2], C[2]));
                 const df J = det.hi < 0.0f ? df_neg(det) : det;
-                if (!(J.hi > 0.0f) || !isfinite(J.hi)) atomicOr(status, kStatusBadElement);
+                if (live && (!(J.hi > 0.0f) || !isfinite(J.hi))) atomicOr(status, kStatusBadElement);
                 const df inv = df_recip(det);
                 df B[9];
 #pragma unroll
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                 for (int gg = 0; gg < GN; ++gg)
 #pragma unroll
                     for (int r = 0; r < 3; ++r) {
-                        const float x = Xs[warp][3 * gg + r].x + Xs[warp][3 * gg + r].y;
+                        const float x = live ? XsG[3 * gg + r].x + XsG[3 * gg + r].y : (float)(gg == r + 1);
 #pragma unroll
                         for (int c = 0; c < 3; ++c) K[3 * r + c] = fmaf(x, __ldg(gh + 3 * gg + c), K[3 * r + c]);
                     }
@@ -261,7 +266,7 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                                     K[1] * K[5] - K[2] * K[4], K[2] * K[3] - K[0] * K[5], K[0] * K[4] - K[1] * K[3]};
                 const float det = K[0] * C[0] + K[1] * C[1] + K[2] * C[2];
                 const float J = fabsf(det);
-                if (!(J > 0.0f) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+                if (live && (!(J > 0.0f) || !isfinite(J))) atomicOr(status, kStatusBadElement);
                 float B[9];
 #pragma unroll
                 for (int k = 0; k < 9; ++k) B[k] = C[k] / det;
@@ -273,7 +278,7 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                 g[6] = make_float2(wJ * (massd.hi + massd.lo), 0.0f);
             }
 #pragma unroll
-            for (int k = 0; k < 7; ++k) Gs[warp][q * 7 + k] = g[k];
+            for (int k = 0; k < 7; ++k) GsG[q * 7 + k] = g[k];
         }
         __syncwarp();
         df acc[PER];
@@ -281,42 +286,42 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
 #pragma unroll
         for (int u = 0; u < PER; ++u) { acc[u] = df{0.0f, 0.0f}; accf[u] = 0.0f; }
         for (int q = 0; q < Q; ++q) {
-            const float2* G = &Gs[warp][q * 7];
-            if (lane < N) {
-                const int b0 = (q * N + lane) * 3;
+            const float2* G = &GsG[q * 7];
+            for (int jl = gl; jl < N; jl += LPG) {
+                const int b0 = (q * N + jl) * 3;
                 if (MODE == kHoDF64) {
                     const df d0 = ldf(Dh, Dl, b0), d1 = ldf(Dh, Dl, b0 + 1), d2 = ldf(Dh, Dl, b0 + 2);
                     const df g00 = dfun(G[0]), g11 = dfun(G[1]), g22 = dfun(G[2]), g01 = dfun(G[3]), g02 = dfun(G[4]), g12 = dfun(G[5]);
                     const df w0 = df_add(df_add(df_mul(g00, d0), df_mul(g01, d1)), df_mul(g02, d2));
                     const df w1 = df_add(df_add(df_mul(g01, d0), df_mul(g11, d1)), df_mul(g12, d2));
                     const df w2 = df_add(df_add(df_mul(g02, d0), df_mul(g12, d1)), df_mul(g22, d2));
-                    Ws[warp][lane] = dfpack(w0);
-                    Ws[warp][N + lane] = dfpack(w1);
-                    Ws[warp][2 * N + lane] = dfpack(w2);
+                    WsG[jl] = dfpack(w0);
+                    WsG[N + jl] = dfpack(w1);
+                    WsG[2 * N + jl] = dfpack(w2);
                 } else {
                     const float d0 = Dh[b0], d1 = Dh[b0 + 1], d2 = Dh[b0 + 2];
-                    Ws[warp][lane] = make_float2(fmaf(G[0].x, d0, fmaf(G[3].x, d1, G[4].x * d2)), 0.0f);
-                    Ws[warp][N + lane] = make_float2(fmaf(G[3].x, d0, fmaf(G[1].x, d1, G[5].x * d2)), 0.0f);
-                    Ws[warp][2 * N + lane] = make_float2(fmaf(G[4].x, d0, fmaf(G[5].x, d1, G[2].x * d2)), 0.0f);
+                    WsG[jl] = make_float2(fmaf(G[0].x, d0, fmaf(G[3].x, d1, G[4].x * d2)), 0.0f);
+                    WsG[N + jl] = make_float2(fmaf(G[3].x, d0, fmaf(G[1].x, d1, G[5].x * d2)), 0.0f);
+                    WsG[2 * N + jl] = make_float2(fmaf(G[4].x, d0, fmaf(G[5].x, d1, G[2].x * d2)), 0.0f);
                 }
             }
             __syncwarp();
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
-                const int t = lane + 32 * u;
+                const int t = gl + LPG * u;
                 if (t >= NTRI) break;
                 const int i = ti[t], j = tj[t];
                 const int bi = (q * N + i) * 3;
                 if (MODE == kHoDF64) {
-                    df v = df_mul(ldf(Dh, Dl, bi), dfun(Ws[warp][j]));
-                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 1), dfun(Ws[warp][N + j])));
-                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 2), dfun(Ws[warp][2 * N + j])));
+                    df v = df_mul(ldf(Dh, Dl, bi), dfun(WsG[j]));
+                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 1), dfun(WsG[N + j])));
+                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 2), dfun(WsG[2 * N + j])));
                     v = df_add(v, df_mul(dfun(G[6]), df_mul(ldf(Ph, Pl, q * N + i), ldf(Ph, Pl, q * N + j))));
                     acc[u] = df_add(acc[u], v);
                 } else {
-                    float v = Dh[bi] * Ws[warp][j].x;
-                    v = fmaf(Dh[bi + 1], Ws[warp][N + j].x, v);
-                    v = fmaf(Dh[bi + 2], Ws[warp][2 * N + j].x, v);
+                    float v = Dh[bi] * WsG[j].x;
+                    v = fmaf(Dh[bi + 1], WsG[N + j].x, v);
+                    v = fmaf(Dh[bi + 2], WsG[2 * N + j].x, v);
                     v = fmaf(G[6].x, Ph[q * N + i] * Ph[q * N + j], v);
                     accf[u] += v;
                 }
@@ -324,8 +329,8 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
             __syncwarp();
         }
 #pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int t = lane + 32 * u;
+        for (int u = 0; u < PER && live; ++u) {
+            const int t = gl + LPG * u;
             if (t >= NTRI) break;
             if (MODE == kHoDF64) reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = dfpack(acc[u]);
             else reinterpret_cast<float*>(kbuf)[e * NTRI + t] = accf[u];
@@ -420,15 +425,19 @@ int launch_assemble_hex(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, 
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + 3) / 4, 152 * 32));
     PendingEvent ev;
     prof_begin(ctx, "assemble_elements_hex", ev);
-#define HEX_LAUNCH(MODE, NN)                                                                                                  \
-    ho_element_kernel<MODE, NN, 8><<<blocks, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, nullptr, T->Q, T->d_dh,       \
-                                                                   T->d_dl, T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh,    \
-                                                                   T->d_qwl, T->d_ti, T->d_tj, d_kappa, f->kappa, f->mass,     \
-                                                                   f->kappa_scale, A->d_kbuf, ctx->d_status)
-    if (V->n == 8) {
-        if (f32) HEX_LAUNCH(kHoF32, 8); else HEX_LAUNCH(kHoDF64, 8);
+#define HEX_LAUNCH(MODE, NN, LPG, NB)                                                                                         \
+    ho_element_kernel<MODE, NN, 8, LPG><<<NB, 128, 0, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, nullptr, T->Q, T->d_dh,      \
+                                                                    T->d_dl, T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh,   \
+                                                                    T->d_qwl, T->d_ti, T->d_tj, d_kappa, f->kappa, f->mass,    \
+                                                                    f->kappa_scale, A->d_kbuf, ctx->d_status)
+    if (V->n == 8 && T->Q <= 8) {
+        // Q1 with the 2^3 rule: four elements per warp, one point and one dof per lane
+        const int nb4 = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + 15) / 16, 152 * 32));
+        if (f32) HEX_LAUNCH(kHoF32, 8, 8, nb4); else HEX_LAUNCH(kHoDF64, 8, 8, nb4);
+    } else if (V->n == 8) {
+        if (f32) HEX_LAUNCH(kHoF32, 8, 32, blocks); else HEX_LAUNCH(kHoDF64, 8, 32, blocks);
     } else {
-        if (f32) HEX_LAUNCH(kHoF32, 27); else HEX_LAUNCH(kHoDF64, 27);
+        if (f32) HEX_LAUNCH(kHoF32, 27, 32, blocks); else HEX_LAUNCH(kHoDF64, 27, 32, blocks);
     }
 #undef HEX_LAUNCH
     prof_end(ctx, ev);
