@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "pmg", "apply"],
+    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "pmg", "apply", "gmres"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
                         "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
                         "AMG-preconditioned CG solve to 1e-10; 'pmg' sets up the matrix-free Poisson operators "
@@ -493,6 +493,30 @@ def run_probe_pmg(args):
     st = op64.solve(l, w, rtol=1e-10, inner=op32, pc="pmg", coarse=a1)
     print(json.dumps({"iterations": st["iterations"], "time_ms": st["time_ms"], "rel_residual": st["rel_residual"],
                       "pmg": st["pmg"]}), flush=True)
+
+
+def run_probe_gmres(args):
+    """GMRES(30) (the reference's default ksp-type) on the P-order Poisson problem of the assembly
+    workload with the default non-symmetric on() elimination, Jacobi and AMG right preconditioning, to
+    1e-10; CG + AMG on the symmetric elimination for comparison."""
+    import feelpp_gb300 as fpp
+    env = fpp.Environment()
+    out = {}
+    for on_type in ("elimination", "elimination_symmetric"):
+        fpp_, xyz, tets, kappa, M, V = build_workload(args.n, args.order, env)
+        u, v = V.element(), V.element()
+        a = fpp.form2(test=V, trial=V)
+        a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v))))
+        l = fpp.form1(test=V)
+        l.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+        a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type=on_type)
+        runs = [("gmres", "jacobi"), ("gmres", "gamg")] if on_type == "elimination" else [("cg", "gamg"), ("gmres", "gamg")]
+        for ksp, pc in runs:
+            w = V.element()
+            st = a.solve(rhs=l, solution=w, rtol=1e-10, ksp=ksp, pc=pc)
+            out["%s_%s_%s" % (on_type, ksp, pc)] = {k: st[k] for k in ("iterations", "outer", "rel_residual", "time_ms")}
+    print(json.dumps({"workload": "P%d Poisson, %d^3 Kuhn mesh, lognormal kappa" % (args.order, args.n), "solves": out}),
+          flush=True)
 
 
 def run_probe_apply(args):
@@ -1086,6 +1110,9 @@ def main():
         return
     if args.probe == "apply":
         run_probe_apply(args)
+        return
+    if args.probe == "gmres":
+        run_probe_gmres(args)
         return
     if args.probe == "pmg":
         run_probe_pmg(args)

@@ -394,6 +394,7 @@ int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x
 }
 
 int64_t amg_rows(const fgpu_amg* M) { return M->L.empty() ? 0 : M->L[0].n; }
+const fgpu_ctx* amg_context(const fgpu_amg* M) { return M->ctx; }
 template int amg_vcycle<float2>(fgpu_amg*, const float2*, const int*);
 template int amg_vcycle<float>(fgpu_amg*, const float*, const int*);
 

@@ -840,6 +840,19 @@ int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, 
     return finish(ctx);
 }
 
+int fgpu_solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
+                     const fgpu_solver_cfg* cfg, int restart, fgpu_solve_stats* stats) {
+    if (!ctx || !A || !b || !x || !cfg || b->n != A->nrows || x->n != A->nrows)
+        return set_err(ctx, FGPU_ERR_INVALID, "solve_gmres: bad arguments");
+    FGPU_NO_CAPTURE(ctx, "solve_gmres");
+    int rc = finish(ctx);
+    if (rc) return rc;
+    if (A->ncomp != 1 && A->ncomp != 3) return set_err(ctx, FGPU_ERR_INVALID, "solve_gmres: bad matrix");
+    rc = solve_gmres(ctx, A, amg, b->d, x->d, cfg, restart, stats);
+    const int rc2 = finish(ctx);
+    return rc ? rc : rc2;
+}
+
 int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats) {
     if (!ctx || !A || !b || !x || !cfg || b->n != A->nrows || x->n != A->nrows)

@@ -311,6 +311,9 @@ const uint8_t* operator_mask(const fgpu_operator* op);
 const float* operator_diag_f32(fgpu_ctx* ctx, fgpu_operator* op);
 int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x, int cycles);
 int64_t amg_rows(const fgpu_amg* M);
+const fgpu_ctx* amg_context(const fgpu_amg* M);
+int solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const double* b, double* x, const fgpu_solver_cfg* cfg,
+                int restart, fgpu_solve_stats* st);
 int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
 int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, double* host);
 int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int nchunks);

@@ -766,15 +766,24 @@ class Form2:
         self.env.check(self.env.lib.fgpu_matrix_mult(self.env.h, self.h, x.h, y.h))
 
     def solve(self, rhs, solution, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False, inner_rtol=0.1,
-              check_every=16, arith="f64", cheb_degree=0, cheb_ratio=0.0, gamg=None):
+              check_every=16, arith="f64", cheb_degree=0, cheb_ratio=0.0, gamg=None, ksp="cg", restart=30):
         """CG + Jacobi (ksp-type=cg, pc-type=jacobi). mixed=True: binary32 CG whose iterate is folded
         into the binary64 solution, and its residual replaced by the binary64 one, each time the
         recurrence residual has dropped by `inner_rtol`; arith="df64": double-float arithmetic for
         the plain solve. pc="gamg": smoothed-aggregation AMG V-cycle, the hierarchy built on first use
-        (options in `gamg`, see AMG) and rebuilt when the matrix changed since."""
+        (options in `gamg`, see AMG) and rebuilt when the matrix changed since. ksp="gmres": restarted
+        GMRES(restart) with right preconditioning (pc "none", "jacobi" or "gamg"), for non-symmetric
+        matrices."""
         cfg = _solver_cfg(rtol, maxit, pc, mixed, inner_rtol, check_every, arith, cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
         vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        if ksp == "gmres":
+            amg = self.gamg(**(gamg or {})) if pc == "gamg" else None
+            self.env.check(self.env.lib.fgpu_solve_gmres(self.env.h, self.h, amg.h if amg else None, vec.h, solution.h,
+                                                         C.byref(cfg), int(restart), C.byref(st)))
+            return _stats(st)
+        if ksp != "cg":
+            raise ValueError("ksp: 'cg' or 'gmres'")
         if pc == "gamg":
             amg = self.gamg(**(gamg or {}))
             self.env.check(self.env.lib.fgpu_solve_cg_amg(self.env.h, self.h, amg.h, vec.h, solution.h, C.byref(cfg),

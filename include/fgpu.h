@@ -286,6 +286,13 @@ int fgpu_matrix_mult(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_vector* x, 
  *      feelpp/feel/feelvf/bilinearformbase.hpp:447-466, feelpp/feel/feelalg/
  *      solverlinearpetsc.cpp:490-570). A32 is used by the mixed solver (may be
  *      NULL: then it is made from A). x is the initial guess and the solution. ---- */
+/* ---- KSPGMRES, the reference's default ksp-type (feelpp/feel/feelalg/backend.cpp:56, 733 -> PETSc
+ *      KSPSolve, solverlinearpetsc.cpp:490-570): restarted GMRES(restart; 0 = 30) with right
+ *      preconditioning (pc NONE, JACOBI, or GAMG with `amg` from fgpu_amg_create on A), stopping when
+ *      ||b - A x||_2 <= rtol ||b||_2; for non-symmetric matrices (elimination without symmetric
+ *      column zeroing, non-symmetric Nitsche terms). x holds the initial guess. ---- */
+int fgpu_solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
+                     const fgpu_solver_cfg* cfg, int restart, fgpu_solve_stats* stats);
 int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
 
