@@ -403,7 +403,7 @@ def run_gb300(args, rank, world, local):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "P2 Lagrange Laplacian+mass FP64 assembly, %d^3-hex Kuhn cube (%d tets, N=%d, nnz=%d), perturb 0.15h, lognormal kappa, quad degree 4" % (args.n, T, N, nnz),
+           "config": {"workload": "P%d Lagrange Laplacian+mass FP64 assembly, %d^3-hex Kuhn cube (%d tets, N=%d, nnz=%d), perturb 0.15h, lognormal kappa, quad degree %d" % (args.order, args.n, T, N, nnz, 2 * args.order),
                       "order": args.order, "mesh_n": args.n, "l2": "inputs larger than L2 (CSR values %.0f MB)" % (nnz * 8 / 1e6),
                       "parallelism": "replicas" if world > 1 else "single"},
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
