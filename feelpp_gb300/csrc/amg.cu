@@ -494,6 +494,49 @@ cudaError_t upload_sell(fgpu_amg::Level& V, const HostCsr& A) {
     return e;
 }
 
+// level 0 from the device matrix: binary32 SELL values through the layout's CSR positions, and
+// binary32 1 / a_ii (the same roundings as the host path: (float)a, (float)(1.0 / a))
+__global__ void amg_sell_values_kernel(int64_t nstored, const int32_t* __restrict__ src, const double* __restrict__ csr,
+                                       float* __restrict__ out) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nstored; j += (int64_t)gridDim.x * blockDim.x)
+        out[j] = src[j] >= 0 ? (float)csr[src[j]] : 0.0f;
+}
+
+__global__ void amg_dinv_kernel(int64_t n, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja,
+                                const double* __restrict__ val, float* __restrict__ dinv) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = ia[r], hi = ia[r + 1];
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (ja[mid] < r) lo = mid + 1; else hi = mid;
+        }
+        dinv[r] = (lo < ia[r + 1] && ja[lo] == r) ? (float)(1.0 / val[lo]) : 0.0f;
+    }
+}
+
+// the fine level's SELL operator and diagonal built on the device from A (the host path's layout:
+// C = 32, sigma = 256, rows sorted by length descending then index, padding columns = the row)
+int upload_level0_device(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg::Level& V) {
+    std::shared_ptr<SellLayout> L;
+    int rc = build_sell(ctx, A, L);
+    if (rc) return rc;
+    V.nslices = L->nslices;
+    V.s_ptr = L->d_slice_ptr; L->d_slice_ptr = nullptr;
+    V.s_len = L->d_slice_len; L->d_slice_len = nullptr;
+    V.s_perm = L->d_perm; L->d_perm = nullptr;
+    V.s_col = L->d_col; L->d_col = nullptr;
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&V.s_val, std::max<int64_t>(L->nstored, 1) * sizeof(float)));
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(&V.dinv, std::max<int64_t>(V.n, 1) * sizeof(float)));
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((L->nstored + 255) / 256, 152 * 32));
+    amg_sell_values_kernel<<<g, 256, 0, ctx->stream>>>(L->nstored, L->d_src, (const double*)A->d_val, V.s_val);
+    const int gd = (int)std::max<int64_t>(1, std::min<int64_t>((V.n + 255) / 256, 152 * 16));
+    amg_dinv_kernel<<<gd, 256, 0, ctx->stream>>>(V.n, A->d_ia, A->d_ja, (const double*)A->d_val, V.dinv);
+    ctx->launches += 2;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));   // the layout's d_src is freed on return
+    return FGPU_OK;
+}
+
 cudaError_t upload_f32(float** dst, const std::vector<double>& v) {
     std::vector<float> f(v.size());
     for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
@@ -537,12 +580,17 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
         V.lmax = hl.lmax;
         const bool coarsest = l == nlev - 1;
         cheb_coefs(V, coarsest ? M->coarse_degree : M->degree);
-        std::vector<double> dinv(V.n, 0.0);
-        for (int64_t i = 0; i < V.n; ++i)
-            for (int64_t p = hl.A.ia[i]; p < hl.A.ia[i + 1]; ++p)
-                if (hl.A.ja[p] == i) dinv[i] = 1.0 / hl.A.a[p];
-        FGPU_CUDA_CHECK(ctx, upload_f32(&V.dinv, dinv));
-        FGPU_CUDA_CHECK(ctx, upload_sell(V, hl.A));
+        if (l == 0 && A->nnz < ((int64_t)1 << 31)) {
+            const int rc0 = upload_level0_device(ctx, A, V);
+            if (rc0) return rc0;
+        } else {
+            std::vector<double> dinv(V.n, 0.0);
+            for (int64_t i = 0; i < V.n; ++i)
+                for (int64_t p = hl.A.ia[i]; p < hl.A.ia[i + 1]; ++p)
+                    if (hl.A.ja[p] == i) dinv[i] = 1.0 / hl.A.a[p];
+            FGPU_CUDA_CHECK(ctx, upload_f32(&V.dinv, dinv));
+            FGPU_CUDA_CHECK(ctx, upload_sell(V, hl.A));
+        }
         if (!coarsest) {
             V.p_nnz = (int64_t)hl.P.ja.size();
             V.r_nnz = (int64_t)hl.R.ja.size();

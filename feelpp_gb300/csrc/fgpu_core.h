@@ -312,6 +312,7 @@ const float* operator_diag_f32(fgpu_ctx* ctx, fgpu_operator* op);
 int amg_vcycle_f32(fgpu_amg* M, const float* r, const int* stop, const float** x, int cycles);
 int64_t amg_rows(const fgpu_amg* M);
 const fgpu_ctx* amg_context(const fgpu_amg* M);
+int build_sell(fgpu_ctx* ctx, const fgpu_matrix* A, std::shared_ptr<SellLayout>& out);
 int solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const double* b, double* x, const fgpu_solver_cfg* cfg,
                 int restart, fgpu_solve_stats* st);
 int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
