@@ -924,7 +924,7 @@ class Operator:
         pc="pmg": p-multigrid V-cycle with `coarse` = the assembled P1 Form2 on the same mesh (same
         coefficients, Dirichlet rows eliminated) and its AMG hierarchy as coarse level; the smoother runs
         on `smoother` (a binary32 Operator; default `inner`), Chebyshev degree `smoother_degree` (0: 3), `coarse_cycles`
-        AMG V-cycles per coarse solve (0: 2)."""
+        AMG V-cycles per coarse solve (0: 4)."""
         cfg = _solver_cfg(rtol, maxit, pc, inner is not None, inner_rtol, check_every, "f64", cheb_degree, cheb_ratio)
         st = _ffi.SolveStats()
         vec = rhs.vec if isinstance(rhs, Form1) else rhs

@@ -318,7 +318,7 @@ int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const 
  *      fgpu_solve_cg_operator (plain binary64 or mixed) with it as preconditioner. ---- */
 typedef struct {
     int smoother_degree;      /* Chebyshev degree of the order-p smoothing (0 = 3: two operator sweeps) */
-    int coarse_cycles;        /* AMG V-cycles per coarse solve (0 = 2) */
+    int coarse_cycles;        /* AMG V-cycles per coarse solve (0 = 4, at most 4) */
 } fgpu_pmg_cfg;
 int fgpu_pmg_create(fgpu_ctx* ctx, fgpu_operator* op32, const fgpu_matrix* A1, fgpu_amg* amg, const fgpu_pmg_cfg* cfg,
                     fgpu_pmg** out);
