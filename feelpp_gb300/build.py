@@ -74,16 +74,5 @@ def build(force=False, verbose=False, extra_flags=()):
     return LIB
 
 
-def build_probe():
-    """Compile the arithmetic-throughput probe (FP64/FP32 FMA, conversions) to _lib/probe_peaks."""
-    os.makedirs(OUT_DIR, exist_ok=True)
-    exe = os.path.join(OUT_DIR, "probe_peaks")
-    src = os.path.join(CSRC, "probe_peaks.cu")
-    if os.path.exists(exe) and os.path.getmtime(exe) >= os.path.getmtime(src):
-        return exe
-    subprocess.check_call([NVCC] + ARCH + ["-O3", "-o", exe, src])
-    return exe
-
-
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))

@@ -559,9 +559,12 @@ int launch_rhs(fgpu_ctx* ctx, const fgpu_space* V, const DevTables* tab, int fki
 }
 
 // Same two load-vector kernels launched on an explicit stream with caller-given
-// tables and work buffer (used by the allocation-free entry point).
+// tables and work buffer (used by the allocation-free entry point). Tetrahedral
+// P1-P3 spaces only; on failure `err` says why (the CUDA error of the launch, or
+// the unsupported local size).
 int launch_rhs_raw(cudaStream_t stream, const fgpu_space* V, int Q, const double* qx, const double* qw,
-                   const double* phi, int fkind, const double* fc, double* d_out, int accumulate, double* d_work) {
+                   const double* phi, int fkind, const double* fc, double* d_out, int accumulate, double* d_work,
+                   std::string& err) {
     const fgpu_mesh* M = V->mesh;
     int threads = 128;
     int64_t blocks = std::min<int64_t>((M->nt + threads - 1) / threads, 152 * 32);
@@ -570,13 +573,19 @@ int launch_rhs_raw(cudaStream_t stream, const fgpu_space* V, int Q, const double
         case 4: rhs_element_kernel<4><<<(int)blocks, threads, 0, stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, Q, qx, qw, phi, fkind, fc[0], fc[1], fc[2], d_work); break;
         case 10: rhs_element_kernel<10><<<(int)blocks, threads, 0, stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, Q, qx, qw, phi, fkind, fc[0], fc[1], fc[2], d_work); break;
         case 20: rhs_element_kernel<20><<<(int)blocks, threads, 0, stream>>>(M->nt, M->d_xyz, M->d_tets, V->ncomp, Q, qx, qw, phi, fkind, fc[0], fc[1], fc[2], d_work); break;
-        default: return FGPU_ERR_INVALID;
+        default:
+            err = "load vector: " + std::to_string(V->n) + " local dofs per component (P1-P3 tetrahedra have 4, 10 or 20)";
+            return FGPU_ERR_INVALID;
     }
+    cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) { err = std::string("load-vector element kernel: ") + cudaGetErrorString(ce); return FGPU_ERR_CUDA; }
     int64_t nn = V->topo.nnodes;
     int64_t gb = std::min<int64_t>((nn + 255) / 256, 152 * 16);
     if (gb < 1) gb = 1;
     rhs_gather_kernel<<<(int)gb, 256, 0, stream>>>(nn, V->n, V->ncomp, V->d_inc_ptr, V->d_inc, d_work, d_out, accumulate);
-    return cudaGetLastError() == cudaSuccess ? FGPU_OK : FGPU_ERR_CUDA;
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) { err = std::string("load-vector gather kernel: ") + cudaGetErrorString(ce); return FGPU_ERR_CUDA; }
+    return FGPU_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -135,6 +135,23 @@ struct GmWork {
     }
 };
 
+// Timing events and the launch count of one solve: released and booked on every
+// exit of solve_gmres, the early error returns included.
+struct GmScope {
+    fgpu_ctx* ctx;
+    const int64_t* launches;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    GmScope(fgpu_ctx* c, const int64_t* l) : ctx(c), launches(l) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+    }
+    ~GmScope() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        ctx->launches += *launches;
+    }
+};
+
 }  // namespace
 
 int solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const double* b, double* x, const fgpu_solver_cfg* cfg,
@@ -203,9 +220,8 @@ int solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const double
         FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(s));
         return FGPU_OK;
     };
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    GmScope scope(ctx, &launches);
+    cudaEvent_t e0 = scope.e0, e1 = scope.e1;
     cudaEventRecord(e0, s);
     double bb = 0.0;
     dots(1, b, b, ww, 0);
@@ -302,10 +318,7 @@ int solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const double
     cudaEventSynchronize(e1);
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
-    ctx->launches += launches;
     if (st) {
         *st = fgpu_solve_stats{};
         st->iterations = it;

@@ -36,7 +36,8 @@
 
 namespace fgpu {
 int launch_rhs_raw(cudaStream_t stream, const fgpu_space* V, int Q, const double* qx, const double* qw,
-                   const double* phi, int fkind, const double* fc, double* d_out, int accumulate, double* d_work);
+                   const double* phi, int fkind, const double* fc, double* d_out, int accumulate, double* d_work,
+                   std::string& err);
 }
 
 using namespace fgpu;
@@ -101,7 +102,12 @@ extern "C" int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_
     if (!V || !rhs || !d_out) return FGPU_ERR_INVALID;
     fgpu_ctx* ctx = V->ctx;
     if (rhs->range != FGPU_RANGE_ELEMENTS) { ctx->err = "noalloc: element integrals only"; return FGPU_ERR_INVALID; }
+    if (V->mesh->cv != 4) { ctx->err = "noalloc: tetrahedral meshes only (the space is on hexahedra)"; return FGPU_ERR_INVALID; }
     if (V->mesh->d_ho) { ctx->err = "noalloc: affine elements only"; return FGPU_ERR_INVALID; }
+    if (rhs->kind != FGPU_RHS_SINE && rhs->kind != FGPU_RHS_CONST && rhs->kind != FGPU_RHS_CONST_VEC) {
+        ctx->err = "noalloc: sources FGPU_RHS_SINE, FGPU_RHS_CONST and FGPU_RHS_CONST_VEC only (FGPU_RHS_FACE is a face-range load)";
+        return FGPU_ERR_INVALID;
+    }
     const int qdeg = rhs->quad_degree > 0 ? rhs->quad_degree : 2 * V->order;
     if (qdeg < 1 || qdeg > kMaxTetRuleDegree) { ctx->err = "noalloc: quadrature degree must be in [1, 8]"; return FGPU_ERR_INVALID; }
     const int64_t need = V->mesh->nt * (int64_t)V->n * V->ncomp;
@@ -119,9 +125,9 @@ extern "C" int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_
     if (rc == FGPU_OK) {
         const TableSlot& s = st->slot[V->order][qdeg];
         rc = launch_rhs_raw((cudaStream_t)stream, V, s.Q, st->tables + s.qx, st->tables + s.qw, st->tables + s.phi,
-                            rhs->kind, rhs->c, d_out, accumulate, st->scratch);
-        if (rc != FGPU_OK) err = std::string("noalloc launch: ") + cudaGetErrorString(cudaGetLastError());
-        ctx->launches += 2;
+                            rhs->kind, rhs->c, d_out, accumulate, st->scratch, err);
+        if (rc != FGPU_OK) err = "noalloc: " + err;
+        else ctx->launches += 2;
     }
     if (prev != ctx->device) cudaSetDevice(prev);
     if (rc != FGPU_OK) ctx->err = err;

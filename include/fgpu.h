@@ -411,7 +411,10 @@ int fgpu_host_ref_tables(int order, int qdeg, double* nodes, double* phi, double
  *      exceed it (else FGPU_ERR_INVALID). The first call on a device sets it up
  *      (symbol lookup + table copy) and must come before any stream capture. All
  *      calls share the scratch: calls that overlap on the GPU race. d_out is a
- *      device array of ndof doubles; stream is a cudaStream_t (NULL = default). ---- */
+ *      device array of ndof doubles; stream is a cudaStream_t (NULL = default),
+ *      which the caller orders after the context's stream (the space's arrays are
+ *      uploaded there). Tetrahedral P1-P3 spaces and the element sources SINE,
+ *      CONST and CONST_VEC only; anything else is refused with a message. ---- */
 #define FGPU_NOALLOC_MAX_ELEMENT_VALUES (1 << 21)
 int fgpu_assemble_vector_noalloc(const fgpu_space* V, const fgpu_rhs_desc* rhs, double* d_out, int accumulate,
                                  void* stream);

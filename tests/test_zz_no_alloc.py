@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import feelpp_gb300 as fpp
-from feelpp_gb300 import _ffi
+from feelpp_gb300 import _ffi, meshgen
 from tests.helpers import assert_values_close, mesh
 
 pytestmark = pytest.mark.gpu
@@ -38,12 +38,18 @@ def _noalloc(env, V, desc, out):
     import torch
     dptr = C.c_void_p()
     env.check(env.lib.fgpu_vector_device(out.h, C.byref(dptr)))
-    env.sync()                                   # the output vector was created on the context's stream
+    env.sync()                                   # the caller's stream must come after the context's work
     s = torch.cuda.Stream()
     rc = env.lib.fgpu_assemble_vector_noalloc(V.h, C.byref(desc), dptr, 0, C.c_void_p(s.cuda_stream))
     env.check(rc)
     torch.cuda.synchronize()
     return out.to_numpy()
+
+
+def _device_ptr(env, out):
+    dptr = C.c_void_p()
+    env.check(env.lib.fgpu_vector_device(out.h, C.byref(dptr)))
+    return dptr
 
 
 @pytest.mark.parametrize("order", [1, 2, 3])
@@ -82,3 +88,42 @@ def test_noalloc_rejects_oversized(env):
     rc = env.lib.fgpu_assemble_vector_noalloc(V.h, C.byref(_desc(_ffi.RHS_SINE)), dptr, 0, None)
     assert rc == 1
     assert b"FGPU_NOALLOC_MAX_ELEMENT_VALUES" in env.lib.fgpu_last_error(env.h)
+
+
+def test_noalloc_allocates_no_device_memory(env):
+    """The property the entry point exists for: once the first call has set the
+    device up, further calls leave the device's free memory unchanged."""
+    import torch
+    xyz, tets = mesh(8, perturb=0.2)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    out = fpp.DeviceVector(env, V.ndof)
+    ref = _regular(V, fpp.sine_source())
+    _noalloc(env, V, _desc(_ffi.RHS_SINE), out)             # first call: set-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    got = _noalloc(env, V, _desc(_ffi.RHS_SINE), out)
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "the call changed free device memory by %d bytes" % (free0 - free1)
+    assert_values_close(got, ref, what="no-alloc load vector after set-up")
+
+
+def test_noalloc_refuses_hexahedra(env):
+    xyz, hexes = meshgen.hex_box(3, 3, 3, perturb=0.1)
+    M = fpp.Mesh(xyz, hexes, env=env)
+    V = fpp.Pch(M, 1)
+    out = fpp.DeviceVector(env, V.ndof)
+    rc = env.lib.fgpu_assemble_vector_noalloc(V.h, C.byref(_desc(_ffi.RHS_SINE)), _device_ptr(env, out), 0, None)
+    assert rc == 1
+    assert b"tetrahedral meshes only" in env.lib.fgpu_last_error(env.h)
+
+
+def test_noalloc_refuses_face_source(env):
+    xyz, tets = mesh(3)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 1)
+    out = fpp.DeviceVector(env, V.ndof)
+    rc = env.lib.fgpu_assemble_vector_noalloc(V.h, C.byref(_desc(_ffi.RHS_FACE, (1.0, 0.0, 0.0))),
+                                              _device_ptr(env, out), 0, None)
+    assert rc == 1
+    assert b"FGPU_RHS_FACE" in env.lib.fgpu_last_error(env.h)
