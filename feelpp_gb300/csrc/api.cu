@@ -68,6 +68,7 @@ int finish(fgpu_ctx* ctx, bool sync = true) {
         if (hst & kStatusBadElement) return set_err(ctx, FGPU_ERR_BAD_ELEMENT, "degenerate element: |det K| <= 0 or non-finite");
         if (hst & kStatusMissingEntry) return set_err(ctx, FGPU_ERR_PATTERN, "element column absent from the pattern");
         if (hst & kStatusRowOverflow) return set_err(ctx, FGPU_ERR_INVALID, "pattern row longer than the staging buffer");
+        if (hst & kStatusStreamTimeout) return set_err(ctx, FGPU_ERR_CUDA, "streamed assembly: a wait for another task timed out");
         return set_err(ctx, FGPU_ERR_CUDA, "device status " + std::to_string(hst));
     }
     return FGPU_OK;
@@ -392,6 +393,7 @@ int fgpu_space_destroy(fgpu_space* V) {
     cudaFree(V->d_pos);
     cudaFree(V->d_gptr);
     cudaFree(V->d_gidx);
+    stream_plan_free(V->stream_plan);
     delete V;
     return FGPU_OK;
 }
@@ -557,24 +559,19 @@ int fgpu_matrix_destroy(fgpu_matrix* A) {
 }
 
 // ---------------------------------------------------------------------------
-// Algorithm choice for FGPU_ALGO_AUTO: the two-phase assembly (element
-// buffer + gather map) when its buffers exist or fit in free device memory
-// with a 10 % margin, else the fused gather (no extra memory). The choice
-// depends on memory only, never on timings, so AUTO results are reproducible.
+// Algorithm choice for FGPU_ALGO_AUTO, from the form and the mesh only (never
+// from free device memory or the capture state), so that AUTO gives the same
+// bits whoever else uses the device: the streamed assembly for scalar
+// Laplace/mass forms on affine tetrahedra with a position table (pattern rows
+// of at most 256 entries), the two-phase assembly for elasticity, the fused
+// gather otherwise. A buffer the chosen path cannot allocate is an error.
 // ---------------------------------------------------------------------------
-static int auto_assembly_algo(fgpu_ctx* ctx, const fgpu_matrix* A) {
+static int auto_assembly_algo(const fgpu_matrix* A, int kind) {
     const fgpu_space* V = A->space;
-    const int64_t nt = V->mesh->nt;
-    const int n = V->n, ntri = n * (n + 1) / 2;
-    size_t need = 0;
-    const size_t kb = (size_t)nt * ntri * (A->ncomp == 3 ? 9 : 1) * (A->precision == FGPU_F64 ? 8 : 4);
-    if (A->kbuf_bytes < kb) need += kb;
-    if (!V->d_gptr) need += ((size_t)nt * n * n + (size_t)A->pattern->nnz * 2 + 1) * sizeof(uint32_t);
-    if (need == 0) return FGPU_ALGO_TWO_PHASE;
-    if (ctx->capturing) return FGPU_ALGO_GATHER;
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return FGPU_ALGO_GATHER; }
-    return need + need / 10 < free_b ? FGPU_ALGO_TWO_PHASE : FGPU_ALGO_GATHER;
+    if (!V->d_pos) return FGPU_ALGO_GATHER;
+    if (kind == FGPU_FORM_ELASTICITY) return FGPU_ALGO_TWO_PHASE;
+    if (A->ncomp == 1 && V->mesh->cv == 4 && !V->mesh->d_ho) return FGPU_ALGO_STREAMED;
+    return FGPU_ALGO_TWO_PHASE;
 }
 
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
@@ -608,6 +605,16 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     std::string err;
     DevTables* tab = get_dev_tables(V->order, qdeg, err);
     if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
+    int algo = f->algo;
+    if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(A, f->kind);
+    if (algo == FGPU_ALGO_STREAMED) {
+        if (f->kind != FGPU_FORM_LAPLACE_MASS || A->ncomp != 1)
+            return set_err(ctx, FGPU_ERR_INVALID, "FGPU_ALGO_STREAMED: scalar Laplace/mass forms only");
+        // geometry fused into the kernel: no coefficient records in device memory
+        const int rc = launch_assemble_streamed(ctx, A, tab, d_kappa, f->kappa, f->mass, f->kappa_scale, accumulate, nullptr);
+        if (rc) return rc;
+        return finish(ctx);
+    }
     const int64_t nt = V->mesh->nt;
     const int rec = f->kind == FGPU_FORM_ELASTICITY ? 16 : 8;
     if (A->coef_cap < nt * rec && ctx->capturing)
@@ -621,21 +628,18 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
         A->coef_cap = nt * rec;
     }
     int rc = FGPU_OK;
-    if (f->kind == FGPU_FORM_LAPLACE_MASS && !(f->algo == FGPU_ALGO_GATHER_NATIVE_F64 && A->precision == FGPU_F64)) {
+    if (f->kind == FGPU_FORM_LAPLACE_MASS && !(algo == FGPU_ALGO_GATHER_NATIVE_F64 && A->precision == FGPU_F64)) {
         // FP64 matrices: df64 arithmetic on the FP32 pipes; FP32 matrices: binary32
         rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef), f->kappa_scale);
         if (rc) return rc;
         const float4* recs = reinterpret_cast<const float4*>(A->d_coef);
-        int algo = f->algo;
-        if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(ctx, A);
         rc = algo == FGPU_ALGO_TWO_PHASE ? launch_assemble_two_phase(ctx, A, tab, recs, accumulate)
                                          : launch_assemble_gather_df(ctx, A, tab, recs, accumulate);
         if (rc) return rc;
         return finish(ctx);
     }
     if (f->kappa_scale) return set_err(ctx, FGPU_ERR_INVALID, "kappa_scale: Laplace/mass forms on the default path only");
-    if (f->kind == FGPU_FORM_ELASTICITY && (f->algo == FGPU_ALGO_TWO_PHASE ||
-                                            (f->algo == FGPU_ALGO_AUTO && auto_assembly_algo(ctx, A) == FGPU_ALGO_TWO_PHASE))) {
+    if (f->kind == FGPU_FORM_ELASTICITY && algo == FGPU_ALGO_TWO_PHASE) {
         // df64 (FP64 matrices) or binary32 element blocks, then the gather map
         rc = launch_geometry_el_df(ctx, V->mesh, f->lambda, f->mu, reinterpret_cast<float4*>(A->d_coef));
         if (rc) return rc;
@@ -692,10 +696,10 @@ int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_des
         d_kappa = A->d_kappa_stage;
     }
     int algo = f->algo;
-    if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(ctx, A);
+    if (algo == FGPU_ALGO_AUTO) algo = auto_assembly_algo(A, f->kind);
     const bool pipelined = f->kind == FGPU_FORM_LAPLACE_MASS && f->range == FGPU_RANGE_ELEMENTS && f->mass_h == 0.0 &&
                            f->dn_trial == 0.0 && f->dn_test == 0.0 && A->precision == FGPU_F64 && A->ncomp == 1 &&
-                           !V->mesh->d_ho && V->mesh->cv == 4 && algo == FGPU_ALGO_TWO_PHASE;
+                           !V->mesh->d_ho && V->mesh->cv == 4 && (algo == FGPU_ALGO_TWO_PHASE || algo == FGPU_ALGO_STREAMED);
     if (!pipelined) {
         int rc = assemble_impl(ctx, A, f, d_kappa, 0);
         if (rc) return rc;
@@ -704,6 +708,24 @@ int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_des
     std::string err;
     DevTables* tab = get_dev_tables(V->order, form_qdeg(V, f->quad_degree), err);
     if (!tab) return set_err(ctx, FGPU_ERR_INVALID, err);
+    if (algo == FGPU_ALGO_STREAMED && ctx->host_transfer != FGPU_HOST_TRANSFER_COPY) {
+        // the streamed kernel stores every value to device memory and to the mapped host buffer
+        cudaPointerAttributes pa{};
+        double* hdev = nullptr;
+        if (cudaPointerGetAttributes(&pa, host_val) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            hdev = static_cast<double*>(pa.devicePointer);
+        else
+            cudaGetLastError();
+        if (hdev) {
+            int rc = launch_assemble_streamed(ctx, A, tab, d_kappa, f->kappa, f->mass, f->kappa_scale, 0, hdev);
+            if (rc) return rc;
+            return finish(ctx);
+        }
+        if (ctx->host_transfer == FGPU_HOST_TRANSFER_DIRECT)
+            return set_err(ctx, FGPU_ERR_INVALID, "direct host transfer: the host buffer is not page-locked and mapped");
+    }
+    // copy-engine transfers of ranges of entries overlapping the gather of later ranges (two-phase
+    // kernels; the streamed path gives the same bits)
     if (A->coef_cap < nt * 8) {
         cudaFree(A->d_coef);
         A->d_coef = nullptr;

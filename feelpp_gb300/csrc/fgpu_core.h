@@ -12,6 +12,9 @@
 
 namespace fgpu {
 
+struct StreamPlan;                   // schedule of the streamed assembly (stream_asm.cu)
+void stream_plan_free(StreamPlan* p);
+
 // ---------------------------------------------------------------------------
 // Reference tetrahedron conventions (Feel++: feelpp/feel/feelmesh/refsimplex.hpp:151-165,
 // feelpp/feel/feelmesh/simplexordering.hpp:284-293 edges, :341-347 faces).
@@ -218,6 +221,7 @@ struct fgpu_space {
     uint64_t bnd_coords = 0;
     uint32_t* d_gptr = nullptr;      // two-phase gather map: nnz + 1 offsets into d_gidx
     uint32_t* d_gidx = nullptr;      // T n n element-buffer indices, per CSR entry in element order
+    fgpu::StreamPlan* stream_plan = nullptr;   // streamed assembly: task order and waits (built on first use)
 };
 
 struct SellLayout {                  // SELL-C-sigma (C = 32, sigma = 256) copy of a CSR pattern
@@ -265,6 +269,7 @@ enum StatusBits : int {
     kStatusRowOverflow = 2,    // a pattern row longer than the kernel's staging buffer
     kStatusMissingEntry = 4,   // an element column absent from its row (pattern mismatch)
     kStatusBreakdown = 8,      // CG breakdown (p.Ap <= 0)
+    kStatusStreamTimeout = 256,// streamed assembly: a wait for another task gave up
 };
 
 struct DevTables {                     // device copies of the reference tables
@@ -300,6 +305,8 @@ int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kap
                        float4* d_rec, const double* d_kscale = nullptr);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+int launch_assemble_streamed(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const double* d_kappa, double kappa,
+                             double mass, const double* kscale, int accumulate, double* hout);
 int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec);
 int launch_assemble_elasticity_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V);

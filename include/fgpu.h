@@ -54,8 +54,16 @@ extern "C" {
 #define FGPU_ALGO_TWO_PHASE 4     /* element matrices (upper triangles; 3x3 blocks for elasticity) into
                                      a device buffer in df64 (FP64 matrices) or binary32, then each CSR
                                      entry sums its contributions in element order through a gather map
-                                     built once per space. AUTO picks it when its buffers fit in device
-                                     memory, else FGPU_ALGO_GATHER (elasticity: native FP64 / binary32) */
+                                     built once per space */
+#define FGPU_ALGO_STREAMED 5      /* scalar Laplace/mass forms on affine tetrahedra: the arithmetic and
+                                     summation order of FGPU_ALGO_TWO_PHASE (bit-identical values) in one
+                                     persistent launch, element matrices through a ring of element slots
+                                     that stays in L2, each pattern row summed once its elements are done;
+                                     no element buffer, no gather map.
+   FGPU_ALGO_AUTO picks by the form and the mesh only, never by free memory or capture state, so its
+   values do not depend on other users of the device: STREAMED for scalar Laplace/mass forms on affine
+   tetrahedra (pattern rows of at most 256 entries), TWO_PHASE for elasticity and for curved or
+   hexahedral meshes, GATHER otherwise. A buffer it cannot allocate is an error (FGPU_ERR_ALLOC). */
 
 /* how fgpu_assemble_matrix_host moves the values to host memory */
 #define FGPU_HOST_TRANSFER_AUTO 0   /* DIRECT when the host buffer is page-locked and mapped, else COPY */
