@@ -561,17 +561,16 @@ int fgpu_matrix_destroy(fgpu_matrix* A) {
 // ---------------------------------------------------------------------------
 // Algorithm choice for FGPU_ALGO_AUTO, from the form and the mesh only (never
 // from free device memory or the capture state), so that AUTO gives the same
-// bits whoever else uses the device: the streamed assembly for scalar
-// Laplace/mass forms on affine tetrahedra with a position table (pattern rows
-// of at most 256 entries), the two-phase assembly for elasticity, the fused
-// gather otherwise. A buffer the chosen path cannot allocate is an error.
+// bits whoever else uses the device: the two-phase assembly whenever the space
+// has a position table (pattern rows of at most 256 entries), the fused gather
+// otherwise. A buffer the chosen path cannot allocate is an error. (The
+// streamed assembly gives the two-phase bits with a third of the memory
+// traffic, but measured slower at P2/P3 64^3: 2.10 against 1.14 ms, 11.7
+// against 4.3 ms; it is latency- and issue-bound, so it is not the default.)
 // ---------------------------------------------------------------------------
 static int auto_assembly_algo(const fgpu_matrix* A, int kind) {
-    const fgpu_space* V = A->space;
-    if (!V->d_pos) return FGPU_ALGO_GATHER;
-    if (kind == FGPU_FORM_ELASTICITY) return FGPU_ALGO_TWO_PHASE;
-    if (A->ncomp == 1 && V->mesh->cv == 4 && !V->mesh->d_ho) return FGPU_ALGO_STREAMED;
-    return FGPU_ALGO_TWO_PHASE;
+    (void)kind;
+    return A->space->d_pos ? FGPU_ALGO_TWO_PHASE : FGPU_ALGO_GATHER;
 }
 
 static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, const double* d_kappa, int accumulate) {
@@ -612,8 +611,14 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
             return set_err(ctx, FGPU_ERR_INVALID, "FGPU_ALGO_STREAMED: scalar Laplace/mass forms only");
         // geometry fused into the kernel: no coefficient records in device memory
         const int rc = launch_assemble_streamed(ctx, A, tab, d_kappa, f->kappa, f->mass, f->kappa_scale, accumulate, nullptr);
-        if (rc) return rc;
-        return finish(ctx);
+        if (rc == kStreamedUnsupported && f->algo == FGPU_ALGO_AUTO) {
+            algo = FGPU_ALGO_TWO_PHASE;             // same values (same arithmetic and order)
+        } else {
+            if (rc == kStreamedUnsupported)
+                return set_err(ctx, FGPU_ERR_INVALID, "FGPU_ALGO_STREAMED: a dof belongs to more elements than a gather task stages");
+            if (rc) return rc;
+            return finish(ctx);
+        }
     }
     const int64_t nt = V->mesh->nt;
     const int rec = f->kind == FGPU_FORM_ELASTICITY ? 16 : 8;
@@ -718,8 +723,8 @@ int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_des
             cudaGetLastError();
         if (hdev) {
             int rc = launch_assemble_streamed(ctx, A, tab, d_kappa, f->kappa, f->mass, f->kappa_scale, 0, hdev);
-            if (rc) return rc;
-            return finish(ctx);
+            if (rc == FGPU_OK) return finish(ctx);
+            if (rc != kStreamedUnsupported) return rc;
         }
         if (ctx->host_transfer == FGPU_HOST_TRANSFER_DIRECT)
             return set_err(ctx, FGPU_ERR_INVALID, "direct host transfer: the host buffer is not page-locked and mapped");

@@ -763,7 +763,9 @@ __global__ void positions_kernel(int64_t nt, int n, const int32_t* __restrict__ 
 int launch_build_positions(fgpu_ctx* ctx, fgpu_space* V) {
     if (V->d_pos) return FGPU_OK;
     const int64_t total = V->mesh->nt * (int64_t)V->n * V->n;
-    cudaError_t e = cudaMalloc(&V->d_pos, total);
+    // 64 bytes of padding: the streamed assembly copies the table in aligned 4-byte words that
+    // may run up to 12 bytes past an element's last row
+    cudaError_t e = cudaMalloc(&V->d_pos, total + 64);
     if (e != cudaSuccess) { ctx->err = "position table allocation failed"; V->d_pos = nullptr; return FGPU_ERR_ALLOC; }
     int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 64);
     PendingEvent ev;

@@ -305,6 +305,7 @@ int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kap
                        float4* d_rec, const double* d_kscale = nullptr);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
 int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+constexpr int kStreamedUnsupported = -1;   // launch_assemble_streamed: use the two-phase path
 int launch_assemble_streamed(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const double* d_kappa, double kappa,
                              double mass, const double* kscale, int accumulate, double* hout);
 int launch_geometry_el_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, double lam, double mu, float4* d_rec);

@@ -61,9 +61,8 @@ extern "C" {
                                      that stays in L2, each pattern row summed once its elements are done;
                                      no element buffer, no gather map.
    FGPU_ALGO_AUTO picks by the form and the mesh only, never by free memory or capture state, so its
-   values do not depend on other users of the device: STREAMED for scalar Laplace/mass forms on affine
-   tetrahedra (pattern rows of at most 256 entries), TWO_PHASE for elasticity and for curved or
-   hexahedral meshes, GATHER otherwise. A buffer it cannot allocate is an error (FGPU_ERR_ALLOC). */
+   values do not depend on other users of the device: TWO_PHASE when the pattern rows have at most
+   256 entries, GATHER otherwise. A buffer it cannot allocate is an error (FGPU_ERR_ALLOC). */
 
 /* how fgpu_assemble_matrix_host moves the values to host memory */
 #define FGPU_HOST_TRANSFER_AUTO 0   /* DIRECT when the host buffer is page-locked and mapped, else COPY */

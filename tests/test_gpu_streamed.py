@@ -1,5 +1,5 @@
-"""Streamed assembly (FGPU_ALGO_STREAMED, the AUTO choice for scalar Laplace/mass forms on affine
-tetrahedra) on a GB300: the same arithmetic and summation order as the two-phase assembly, so the
+"""Streamed assembly (FGPU_ALGO_STREAMED: scalar Laplace/mass forms on affine tetrahedra in one
+persistent launch) on a GB300: the same arithmetic and summation order as the two-phase assembly, so the
 values must be bit-identical to it, and within the FP64 parity tolerance of the oracle. Long thin
 meshes make the ring of element slots wrap many times (element tasks waiting for the gather tasks
 that still read the slots they overwrite)."""
@@ -65,7 +65,7 @@ def test_streamed_fp32_and_accumulate_equal_two_phase(env, order):
         assert np.array_equal(s.values(), t.values()), precision
 
 
-def test_auto_picks_streamed_and_matches_explicit(env):
+def test_auto_is_two_phase_and_matches_streamed(env):
     xyz, tets = meshgen.kuhn_box(10, perturb=0.2, seed=3)
     kappa = meshgen.lognormal_kappa(len(tets), seed=4)
     M = fpp.Mesh(xyz, tets, env=env)
@@ -74,7 +74,7 @@ def test_auto_picks_streamed_and_matches_explicit(env):
     u, v = V.element(), V.element()
     l0 = env.launches()
     a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + 0.7 * fpp.idt(u) * fpp.id(v)))
-    assert env.launches() - l0 == 1          # one persistent launch (two-phase: geometry, elements, gather)
+    assert env.launches() - l0 == 3          # geometry, element matrices, gather
     s = _assemble(env, M, V, kappa, _ffi.ALGO_STREAMED)
     assert np.array_equal(a.values(), s.values())
 
@@ -115,3 +115,22 @@ def test_streamed_host_transfer_equals_device_values(env):
         env.check(env.lib.fgpu_assemble_matrix_host(env.h, a.h, C.byref(d), C.c_void_p(h.data_ptr())))
         assert np.array_equal(h.numpy(), ref), mode
     env.set_host_transfer("auto")
+
+
+def test_auto_bits_same_eager_and_captured(env):
+    """AUTO never switches algorithm inside a graph capture: replayed values equal eager ones."""
+    xyz, tets = meshgen.kuhn_box(9, perturb=0.2, seed=12)
+    kappa = meshgen.lognormal_kappa(len(tets), seed=13)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 3)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    kt = fpp.DeviceScalar(env, 1.0)
+    integral = fpp.integrate(fpp.elements(M), kt * fpp.inner(fpp.gradt(u), fpp.grad(v)) + 0.7 * fpp.idt(u) * fpp.id(v))
+    a.assign(integral)
+    eager = a.values()
+    with fpp.capture(env) as g:
+        a.assign(integral)
+    a.zero()
+    g.launch()
+    assert np.array_equal(a.values(), eager)
