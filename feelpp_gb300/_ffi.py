@@ -96,6 +96,7 @@ SIGNATURES = {
     "fgpu_matrix_create_like": (i32, [P, i32, PP]),
     "fgpu_matrix_info": (i32, [P, I64P, I64P, IP]),
     "fgpu_matrix_get_csr": (i32, [P, P, P, P]),
+    "fgpu_matrix_get_csr32": (i32, [P, P, P, P]),
     "fgpu_matrix_values_device": (i32, [P, PP]),
     "fgpu_matrix_zero": (i32, [P]),
     "fgpu_matrix_convert": (i32, [P, P]),
@@ -112,6 +113,7 @@ SIGNATURES = {
     "fgpu_dirichlet": (i32, [P, P, P, i64, P, P, i32, f64]),
     "fgpu_matrix_mult": (i32, [P, P, P, P]),
     "fgpu_solve_cg": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), C.POINTER(SolveStats)]),
+    "fgpu_solve_cg_refine_dd": (i32, [P, P, P, P, P, P, C.POINTER(SolverCfg), C.c_double, C.POINTER(SolveStats)]),
     "fgpu_amg_create": (i32, [P, P, C.POINTER(AmgCfg), PP]),
     "fgpu_amg_update": (i32, [P]),
     "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),

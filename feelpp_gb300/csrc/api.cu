@@ -525,6 +525,21 @@ int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* 
     return FGPU_OK;
 }
 
+int fgpu_matrix_get_csr32(const fgpu_matrix* A, int32_t* ia, int32_t* ja, double* val) {
+    if (A) FGPU_NO_CAPTURE(A->ctx, "matrix_get_csr32");
+    if (!A) return FGPU_ERR_INVALID;
+    if (A->nnz > (int64_t)INT32_MAX || A->nrows >= (int64_t)INT32_MAX)
+        return set_err(A->ctx, FGPU_ERR_INVALID, "matrix_get_csr32: " + std::to_string(A->nnz) +
+                                                     " nonzeros do not fit 32-bit row offsets (use fgpu_matrix_get_csr)");
+    if (ia) {
+        std::vector<int64_t> ia64(A->nrows + 1);
+        int rc = fgpu_matrix_get_csr(A, ia64.data(), nullptr, nullptr);
+        if (rc) return rc;
+        for (int64_t r = 0; r <= A->nrows; ++r) ia[r] = (int32_t)ia64[r];
+    }
+    return fgpu_matrix_get_csr(A, nullptr, ja, val);
+}
+
 int fgpu_matrix_values_device(const fgpu_matrix* A, void** dptr) {
     if (!A || !dptr) return FGPU_ERR_INVALID;
     *dptr = A->d_val;
@@ -902,6 +917,31 @@ int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, c
     rc = solve_pcg_mixed(ctx, A, a32, b->d, x->d, cfg, stats);
     if (tmp) fgpu_matrix_destroy(tmp);
     int rc2 = finish(ctx);
+    return rc ? rc : rc2;
+}
+
+int fgpu_solve_cg_refine_dd(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
+                            fgpu_vector* x_lo, const fgpu_solver_cfg* cfg, double inner_reduction, fgpu_solve_stats* stats) {
+    if (!ctx || !A || !b || !x || !cfg || b->n != A->nrows || x->n != A->nrows || (x_lo && x_lo->n != A->nrows))
+        return set_err(ctx, FGPU_ERR_INVALID, "solve_cg_refine_dd: bad arguments");
+    FGPU_NO_CAPTURE(ctx, "solve_cg_refine_dd");
+    if (A->precision != FGPU_F64) return set_err(ctx, FGPU_ERR_INVALID, "solve_cg_refine_dd: FP64 matrices");
+    if (cfg->pc == FGPU_PC_GAMG && (!amg || cfg->mixed))
+        return set_err(ctx, FGPU_ERR_INVALID, "solve_cg_refine_dd: pc gamg needs an AMG of A and a non-mixed inner solve");
+    if (cfg->pc != FGPU_PC_GAMG && amg) return set_err(ctx, FGPU_ERR_INVALID, "solve_cg_refine_dd: an AMG is given but pc is not gamg");
+    int rc = finish(ctx);
+    if (rc) return rc;
+    fgpu_matrix* tmp = nullptr;
+    if (cfg->mixed) {
+        rc = fgpu_matrix_create_like(A, FGPU_F32, &tmp);
+        if (rc) return rc;
+        rc = launch_convert_values(ctx, A, tmp);
+        if (rc) { fgpu_matrix_destroy(tmp); return rc; }
+    }
+    rc = solve_refine_dd(ctx, A, tmp, cfg->pc == FGPU_PC_GAMG ? amg : nullptr, b->d, x->d, x_lo ? x_lo->d : nullptr, cfg,
+                         inner_reduction, stats);
+    if (tmp) fgpu_matrix_destroy(tmp);
+    const int rc2 = finish(ctx);
     return rc ? rc : rc2;
 }
 

@@ -386,6 +386,8 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
               fgpu_solve_stats* st, fgpu_amg* amg = nullptr);
 int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A32, const double* d_b, double* d_x,
                     const fgpu_solver_cfg* cfg, fgpu_solve_stats* st);
+int solve_refine_dd(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, fgpu_amg* amg, const double* b, double* xh,
+                    double* xl_out, const fgpu_solver_cfg* cfg, double inner_reduction, fgpu_solve_stats* st);
 
 }  // namespace fgpu
 

@@ -795,6 +795,23 @@ class Form2:
                                                   C.byref(st)))
         return _stats(st)
 
+    def solve_refined(self, rhs, solution, solution_lo=None, rtol=1e-10, maxit=100000, pc="jacobi", mixed=False,
+                      inner_reduction=1e-6, gamg=None, cheb_degree=0):
+        """CG with iterative refinement in double-double: the solution is solution + solution_lo (two
+        binary64 vectors, about 106 bits) and the outer residual b - A (solution + solution_lo) is formed
+        in double-double, so rtol may lie below the binary64 floor of a stiff system. Each outer step
+        solves for the correction with CG (pc "jacobi", "cheb_jacobi", "none" or "gamg"; mixed allowed
+        without gamg) to the relative reduction inner_reduction. The returned rel_residual is the
+        double-double one; "outer" counts the outer steps."""
+        cfg = _solver_cfg(rtol, maxit, pc, mixed, 0.1, 16, "f64", cheb_degree, 0.0)
+        st = _ffi.SolveStats()
+        vec = rhs.vec if isinstance(rhs, Form1) else rhs
+        amg = self.gamg(**(gamg or {})) if pc == "gamg" else None
+        self.env.check(self.env.lib.fgpu_solve_cg_refine_dd(self.env.h, self.h, amg.h if amg else None, vec.h, solution.h,
+                                                            solution_lo.h if solution_lo is not None else None,
+                                                            C.byref(cfg), float(inner_reduction), C.byref(st)))
+        return _stats(st)
+
     def gamg(self, **opts):
         """The AMG hierarchy of this matrix (built, or rebuilt when the values changed since)."""
         amg = getattr(self, "_amg", None)

@@ -241,6 +241,10 @@ int fgpu_matrix_create_like(const fgpu_matrix* A, int precision, fgpu_matrix** o
 int fgpu_matrix_info(const fgpu_matrix* A, int64_t* nrows, int64_t* nnz, int* precision);
 /* host copies of the CSR arrays; any pointer may be NULL (values as double) */
 int fgpu_matrix_get_csr(const fgpu_matrix* A, int64_t* ia, int32_t* ja, double* val);
+/* the same with 32-bit row offsets, the PetscInt width of a default PETSc build that
+ * MatSeqAIJSetPreallocationCSR takes (MatrixPetsc::init, feelpp/feel/feelalg/matrixpetsc.hpp:625,
+ * matrixpetsc.cpp:405-413); FGPU_ERR_INVALID when nnz does not fit in int32 */
+int fgpu_matrix_get_csr32(const fgpu_matrix* A, int32_t* ia, int32_t* ja, double* val);
 /* device pointer of the value array (double or float per precision) */
 int fgpu_matrix_values_device(const fgpu_matrix* A, void** dptr);
 /* MatrixPetsc::zero (MatZeroEntries, matrixpetsc.cpp:617-627) */
@@ -302,6 +306,16 @@ int fgpu_solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const f
                      const fgpu_solver_cfg* cfg, int restart, fgpu_solve_stats* stats);
 int fgpu_solve_cg(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, const fgpu_vector* b, fgpu_vector* x,
                   const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
+/* ---- the same solve to tolerances below the binary64 floor of stiff systems (the reference's
+ *      KSPSolve with rtol 1e-10 on the clamped elasticity beam): iterative refinement whose solution is
+ *      the unevaluated double-double sum x + x_lo and whose outer residual b - A (x + x_lo) is formed in
+ *      double-double arithmetic; each outer step solves for the correction with the solver of cfg
+ *      (pc JACOBI / CHEB_JACOBI / NONE, or GAMG with `amg` of A; mixed allowed without GAMG) to a
+ *      relative reduction inner_reduction (0 = 1e-6). Stops when the double-double residual reaches
+ *      cfg->rtol ||b||; stats->rel_residual is that residual, stats->outer the outer steps, stats->iterations
+ *      the inner iterations. x holds the initial guess; x_lo (may be NULL) receives the low part. ---- */
+int fgpu_solve_cg_refine_dd(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
+                            fgpu_vector* x_lo, const fgpu_solver_cfg* cfg, double inner_reduction, fgpu_solve_stats* stats);
 
 /* ---- --pc-type=gamg (PCGAMG smoothed aggregation, feelpp/feel/feelalg/preconditionerpetsc.cpp:2229-2330):
  *      fgpu_amg_create builds the hierarchy from the FP64 matrix A as it is now (host set-up: strength
