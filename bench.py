@@ -295,6 +295,19 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def read_tune_picks(path):
+    """{key: [params]} of an autotuner cache file (last line of a key wins)."""
+    out = {}
+    try:
+        for ln in open(path):
+            parts = ln.split()
+            if len(parts) > 1:
+                out[parts[0]] = [int(x) for x in parts[1:]]
+    except OSError:
+        pass
+    return out
+
+
 def timed_region(stream, local, fn, reps):
     """ms per call of fn (CUDA events on the launch stream, synchronized on both sides) and the
     clock record of that region."""
@@ -419,7 +432,10 @@ def run_gb300(args, rank, world, local):
     # events below are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    env = fpp.Environment(device=local, stream=C.c_void_p(stream.cuda_stream), profile=True)
+    import tempfile
+    tune_dir = tempfile.mkdtemp(prefix="fgpu_tune_")
+    tune_file = os.path.join(tune_dir, "picks.txt")        # the autotuner's picks of this run, reported below
+    env = fpp.Environment(device=local, stream=C.c_void_p(stream.cuda_stream), profile=True, tune_cache=tune_file)
     fpp_, xyz, tets, kappa, M, V = build_workload(args.n, args.order, env)
     u, v = V.element(), V.element()
     a = fpp.form2(test=V, trial=V)
@@ -637,6 +653,7 @@ def run_gb300(args, rank, world, local):
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
            "clocks": clk.summary(), "fp32_assembly": fp32, "native_fp64_assembly": native, "solve": solve,
            "extras": extras,
+           "autotune": read_tune_picks(tune_file),
            "arith": "FP64-accurate: double-float (binary32 pairs) on the FP32 pipes, binary64 storage"}
     print(json.dumps(out), flush=True)
 

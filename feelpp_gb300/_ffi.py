@@ -32,7 +32,7 @@ class FgpuError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("profile", C.c_int), ("host_threads", C.c_int),
-                ("host_setup", C.c_int)]
+                ("host_setup", C.c_int), ("tune", C.c_int), ("tune_cache", C.c_char_p)]
 
 
 class FormDesc(C.Structure):

@@ -151,6 +151,11 @@ int fgpu_create(const fgpu_config* cfg, fgpu_ctx** out) {
     if (ht <= 0) ht = (int)std::max(1u, std::thread::hardware_concurrency());
     ctx->host_threads = ht;
     ctx->host_setup = cfg ? cfg->host_setup : 0;
+    ctx->tune = cfg ? cfg->tune : 0;
+    if (cfg && cfg->tune_cache) {
+        ctx->tune_file = cfg->tune_cache;
+        tune_load_cache_file(ctx->tune_file);
+    }
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) {
         delete ctx;

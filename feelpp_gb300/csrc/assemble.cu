@@ -18,6 +18,7 @@
 // copy of the row; the row is then written once, coalesced. Every entry is
 // summed in element insertion order, the order the reference adds into PETSc;
 // no float atomics, deterministic.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -1311,9 +1312,10 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
     }
 }
 
-// One thread per CSR entry, its contributions in batches of 4 (the index and
+// One thread per CSR entry, its contributions in batches of B (the index and
 // value loads of a batch are issued together; the sum stays in element
-// order). Measured against three alternatives at P2 48^3 (this: 0.32 ms):
+// order, so B, like the launch shape, does not change the result; the tuner
+// picks it). Measured against three alternatives at P2 48^3 (this: 0.32 ms):
 // entries sorted by contribution count within 256-entry windows (0.50 ms: the
 // permuted writes lose their coalescing); a warp-flat load of the 32 entries'
 // contributions staged in shared memory (0.39 ms: fewer loads in flight per
@@ -1322,7 +1324,7 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 // (0.30 ms: the sorted list scatters the reads of the element buffer, 1.75 GB
 // of DRAM reads for 5.4 M entries). At P2 64^3 two entries per thread (k and
 // k + stride, loads issued together) took 0.90 ms against 0.655 ms.
-template <int MODE>
+template <int MODE, int B = 4>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
                                                          void* __restrict__ valv, int accumulate, double* __restrict__ hout) {
@@ -1334,15 +1336,15 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
             // the low parts in one binary32 accumulator, normalised once (error ~ (count) u^2 |sum|)
             const float2* kb = reinterpret_cast<const float2*>(kbuf);
             float sh = 0.0f, sl = 0.0f;
-            for (uint32_t p = p0; p < p1; p += 4) {
-                uint32_t ix[4];
-                float2 v[4];
+            for (uint32_t p = p0; p < p1; p += B) {
+                uint32_t ix[B];
+                float2 v[B];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
+                for (int u = 0; u < B; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
+                for (int u = 0; u < B; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                for (int u = 0; u < B; ++u)
                     if (p + u < p1) {
                         const df t = two_sum(sh, v[u].x);
                         sh = t.hi;
@@ -1358,15 +1360,15 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
         } else {
             const float* kb = reinterpret_cast<const float*>(kbuf);
             float s = 0.0f;
-            for (uint32_t p = p0; p < p1; p += 4) {
-                uint32_t ix[4];
-                float v[4];
+            for (uint32_t p = p0; p < p1; p += B) {
+                uint32_t ix[B];
+                float v[B];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
+                for (int u = 0; u < B; ++u) ix[u] = p + u < p1 ? __ldg(gidx + p + u) : 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : 0.0f;
+                for (int u = 0; u < B; ++u) v[u] = p + u < p1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : 0.0f;
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                for (int u = 0; u < B; ++u)
                     if (p + u < p1) s = (p + u == p0) ? v[u] : f_add(s, v[u]);
             }
             float* out = reinterpret_cast<float*>(valv) + k;
@@ -1480,6 +1482,82 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
     return FGPU_OK;
 }
 
+// Launch shape of the two-phase kernels: threads per block and blocks per SM of the element kernel
+// and of the gather, and the gather's contributions per load batch. None changes the values.
+struct TwoPhaseShape {
+    int el_threads = 256, el_bpsm = 16, g_threads = 256, g_bpsm = 32, g_batch = 4;
+};
+
+template <int MODE, int N>
+static void launch_element_tri(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int sms,
+                               const TwoPhaseShape& sh) {
+    constexpr int NTRI = N * (N + 1) / 2;
+    constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;
+    const int64_t nt = A->space->mesh->nt;
+    const int64_t warps = (nt + EPW - 1) / EPW, wpb = sh.el_threads / 32;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((warps + wpb - 1) / wpb, (int64_t)sms * sh.el_bpsm));
+    element_tri_kernel<MODE, N><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
+}
+
+template <int MODE>
+static void launch_gather_map(fgpu_ctx* ctx, fgpu_matrix* A, int sms, const TwoPhaseShape& sh, int accumulate, double* hout) {
+    const fgpu_space* V = A->space;
+    const int64_t nnz = A->pattern->nnz;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + sh.g_threads - 1) / sh.g_threads, (int64_t)sms * sh.g_bpsm));
+    switch (sh.g_batch) {
+        case 2: gather_map_kernel<MODE, 2><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
+        case 8: gather_map_kernel<MODE, 8><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
+        default: gather_map_kernel<MODE, 4><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
+    }
+}
+
+// median of 5 timed launches (after one warm-up) of fn on the context's stream, in ms
+template <class F>
+static float median_ms(fgpu_ctx* ctx, F&& fn) {
+    cudaEvent_t ev[6];
+    for (auto& e : ev) cudaEventCreate(&e);
+    fn();
+    for (int r = 0; r < 5; ++r) {
+        cudaEventRecord(ev[r], ctx->stream);
+        fn();
+    }
+    cudaEventRecord(ev[5], ctx->stream);
+    cudaEventSynchronize(ev[5]);
+    float t[5];
+    for (int r = 0; r < 5; ++r) cudaEventElapsedTime(&t[r], ev[r], ev[r + 1]);
+    for (auto& e : ev) cudaEventDestroy(e);
+    std::sort(t, t + 5);
+    ctx->launches += 6;
+    return t[2];
+}
+
+// Time the candidate shapes on the real inputs (the element buffer and the values are written by the
+// candidates; the assembly that follows overwrites both).
+template <int MODE, int N>
+static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int sms, TwoPhaseShape& best) {
+    float best_ms = 1e30f;
+    TwoPhaseShape s = best;
+    for (int th : {128, 256})
+        for (int bp : {4, 8, 16, 32}) {
+            s.el_threads = th;
+            s.el_bpsm = bp;
+            const float ms = median_ms(ctx, [&] { launch_element_tri<MODE, N>(ctx, A, tab, rec, sms, s); });
+            if (ms < best_ms) { best_ms = ms; best.el_threads = th; best.el_bpsm = bp; }
+        }
+    best_ms = 1e30f;
+    for (int th : {128, 256})
+        for (int bp : {8, 16, 32, 64})
+            for (int b : {2, 4, 8}) {
+                s.g_threads = th;
+                s.g_bpsm = bp;
+                s.g_batch = b;
+                const float ms = median_ms(ctx, [&] { launch_gather_map<MODE>(ctx, A, sms, s, 0, nullptr); });
+                if (ms < best_ms) { best_ms = ms; best.g_threads = th; best.g_bpsm = bp; best.g_batch = b; }
+            }
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    return FGPU_OK;
+}
+
 template <int MODE, int N>
 static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate,
                          double* host = nullptr) {
@@ -1502,22 +1580,29 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t nnz = A->pattern->nnz;
+    TwoPhaseShape shape;
+    const std::string key = "two_phase|" + tune_device_key(ctx->device) + "|P" + std::to_string(V->order) + "|" +
+                            (MODE == kModeDF64 ? "f64" : "f32") + "|n2^" + std::to_string(tune_size_class(nnz));
+    std::vector<int> tv;
+    if (ctx->tune == 0 && tune_lookup(ctx->tune_file, key, tv) && tv.size() == 5) {
+        shape = TwoPhaseShape{tv[0], tv[1], tv[2], tv[3], tv[4]};
+    } else if (ctx->tune == 0 && !ctx->capturing && accumulate == 0 && !host) {
+        int rc = tune_two_phase<MODE, N>(ctx, A, tab, rec, sms, shape);
+        if (rc) return rc;
+        tune_record(ctx->tune_file, key, {shape.el_threads, shape.el_bpsm, shape.g_threads, shape.g_bpsm, shape.g_batch});
+    }
     {
-        constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;
-        const int64_t warps = (nt + EPW - 1) / EPW;
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)sms * 16));
         PendingEvent ev;
         prof_begin(ctx, "assemble_elements", ev);
-        element_tri_kernel<MODE, N><<<(int)blocks, 256, 0, ctx->stream>>>(nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
+        launch_element_tri<MODE, N>(ctx, A, tab, rec, sms, shape);
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     }
     if (host) return launch_gather_phase_to_host(ctx, A, host, 4);
-    const int64_t nnz = A->pattern->nnz;
-    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, (int64_t)sms * 32));
     PendingEvent ev;
     prof_begin(ctx, "assemble_gather", ev);
-    gather_map_kernel<MODE><<<(int)blocks, 256, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, nullptr);
+    launch_gather_map<MODE>(ctx, A, sms, shape, accumulate, nullptr);
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;

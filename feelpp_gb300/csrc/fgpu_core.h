@@ -151,6 +151,8 @@ struct fgpu_ctx {
     cudaStream_t copy_streams[4] = {nullptr, nullptr, nullptr, nullptr};   // large host<->device copies in chunks
     cudaEvent_t copy_events[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int host_transfer = 0;         // FGPU_HOST_TRANSFER_*: how results reach host buffers
+    int tune = 0;                  // 0: time launch shapes on first use; -1: fixed default shapes
+    std::string tune_file;         // cache file of the picks ("" = none)
 };
 
 struct fgpu_graph {
@@ -386,6 +388,13 @@ int solve_pcg(fgpu_ctx* ctx, const fgpu_matrix* A, const double* d_b, double* d_
               fgpu_solve_stats* st, fgpu_amg* amg = nullptr);
 int solve_pcg_mixed(fgpu_ctx* ctx, const fgpu_matrix* A64, const fgpu_matrix* A32, const double* d_b, double* d_x,
                     const fgpu_solver_cfg* cfg, fgpu_solve_stats* st);
+// launch-shape autotuner store (tune.cpp)
+void tune_load_cache_file(const std::string& path);
+bool tune_lookup(const std::string& file, const std::string& key, std::vector<int>& vals);
+void tune_record(const std::string& file, const std::string& key, const std::vector<int>& vals);
+std::string tune_device_key(int device);
+int tune_size_class(int64_t n);
+
 int solve_refine_dd(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32, fgpu_amg* amg, const double* b, double* xh,
                     double* xl_out, const fgpu_solver_cfg* cfg, double inner_reduction, fgpu_solve_stats* st);
 

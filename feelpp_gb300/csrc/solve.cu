@@ -21,6 +21,7 @@
 // results are bitwise reproducible. A device flag stops the iteration once
 // ||r|| <= rtol ||b||; the host replays a captured CUDA graph of `check_every`
 // iterations and polls the flag between replays.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -259,7 +260,7 @@ static int sell_blocks(const SellLayout& L) {
 // nonzeros) combination is solved; the choice is cached (0 = SELL, else G).
 // ---------------------------------------------------------------------------
 static std::mutex g_tune_mutex;
-static std::map<std::tuple<int, int, int64_t, int64_t>, int> g_spmv_tune;
+static std::map<std::tuple<std::string, int, int, int64_t, int64_t>, int> g_spmv_tune;
 
 template <class PL>
 struct SpmvPlan {
@@ -283,13 +284,18 @@ struct SpmvPlan {
 template <class PL>
 static int plan_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* val, const typename PL::S* x,
                      typename PL::S* y, SpmvPlan<PL>& plan) {
-    const auto key = std::make_tuple(ctx->device, PL::id, A->nrows, A->nnz);
+    const auto key = std::make_tuple(ctx->tune_file, ctx->device, PL::id, A->nrows, A->nnz);
+    const std::string skey = "spmv|" + tune_device_key(ctx->device) + "|pol" + std::to_string(PL::id) + "|" +
+                             std::to_string(A->nrows) + "x" + std::to_string(A->nnz);
     int choice = -1;
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_spmv_tune.find(key);
         if (it != g_spmv_tune.end()) choice = it->second;
     }
+    std::vector<int> tv;
+    if (choice == -1 && tune_lookup(ctx->tune_file, skey, tv) && tv.size() == 1) choice = tv[0];
+    if (choice == -1 && ctx->tune != 0) choice = spmv_group(A);
     // SELL layout and values (needed to time it, and to use it)
     bool have_sell = false;
     if (choice == -1 || choice == 0) {
@@ -309,9 +315,10 @@ static int plan_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* 
         }
     }
     if (choice == -1) {
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
+        // median of 5 individually timed products per candidate (a sum of a few products let one slow
+        // repetition on a shared GPU decide)
+        cudaEvent_t ev[6];
+        for (auto& e : ev) cudaEventCreate(&e);
         float best_ms = 1e30f;
         int best = spmv_group(A);
         const int cands[5] = {4, 8, 16, 32, 0};
@@ -322,19 +329,24 @@ static int plan_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const typename PL::V* 
             trial.sell = plan.sell;
             trial.sval = plan.sval;
             trial.launch(ctx->stream, A, val, x, y, 0, nullptr, nullptr, nullptr, nullptr);
-            cudaEventRecord(e0, ctx->stream);
-            for (int rep = 0; rep < 3; ++rep) trial.launch(ctx->stream, A, val, x, y, 0, nullptr, nullptr, nullptr, nullptr);
-            cudaEventRecord(e1, ctx->stream);
-            cudaEventSynchronize(e1);
+            for (int rep = 0; rep < 5; ++rep) {
+                cudaEventRecord(ev[rep], ctx->stream);
+                trial.launch(ctx->stream, A, val, x, y, 0, nullptr, nullptr, nullptr, nullptr);
+            }
+            cudaEventRecord(ev[5], ctx->stream);
+            cudaEventSynchronize(ev[5]);
             trial.sval = nullptr;  // not owned by the trial
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ctx->launches += 4;
-            if (ms < best_ms) { best_ms = ms; best = c; }
+            float t[5];
+            for (int rep = 0; rep < 5; ++rep) cudaEventElapsedTime(&t[rep], ev[rep], ev[rep + 1]);
+            std::sort(t, t + 5);
+            ctx->launches += 6;
+            if (t[2] < best_ms) { best_ms = t[2]; best = c; }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        for (auto& e : ev) cudaEventDestroy(e);
         choice = best;
+        tune_record(ctx->tune_file, skey, {choice});
+    }
+    {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_spmv_tune[key] = choice;
     }

@@ -30,9 +30,10 @@ from ._ffi import check
 class Environment:
     """Owns an ``fgpu_ctx`` (device, launch stream, profiling)."""
 
-    def __init__(self, device=0, stream=None, profile=False, host_threads=0, host_setup=False):
+    def __init__(self, device=0, stream=None, profile=False, host_threads=0, host_setup=False, tune=True, tune_cache=None):
         self.lib = _ffi.load()
-        cfg = _ffi.Config(device, stream, 1 if profile else 0, host_threads, 1 if host_setup else 0)
+        cfg = _ffi.Config(device, stream, 1 if profile else 0, host_threads, 1 if host_setup else 0, 0 if tune else -1,
+                          tune_cache.encode() if tune_cache else None)
         h = C.c_void_p()
         rc = self.lib.fgpu_create(C.byref(cfg), C.byref(h))
         if rc != 0:

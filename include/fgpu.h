@@ -118,6 +118,11 @@ typedef struct {
     int host_setup;    /* 1: build dof tables, incidence and patterns on the host (topology.cpp);
                           0 (default): on the device (topology_dev.cu; same arrays), with the host
                           path used automatically for meshes of 2^21 vertices or more */
+    int tune;          /* 0 (default): launch shapes that do not change results (threads per block,
+                          blocks per SM, loads per batch of the two-phase assembly kernels; the CG's
+                          SpMV layout) are timed on the first use of a (device, kernel, order, precision,
+                          size class) key and the fastest kept; -1: fixed default shapes */
+    const char* tune_cache; /* file the picks are appended to and read from at creation (NULL: none) */
 } fgpu_config;
 
 typedef struct {
