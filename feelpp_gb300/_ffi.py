@@ -122,6 +122,7 @@ SIGNATURES = {
     "fgpu_assemble_matrix_host": (i32, [P, P, C.POINTER(FormDesc), P]),
     "fgpu_solve_gmres": (i32, [P, P, P, P, P, C.POINTER(SolverCfg), i32, C.POINTER(SolveStats)]),
     "fgpu_set_host_transfer": (i32, [P, i32]),
+    "fgpu_set_tensor_cores": (i32, [P, i32]),
     "fgpu_export_ensight": (i32, [P, C.c_char_p, i32, P, P]),
     "fgpu_pmg_create": (i32, [P, P, P, P, C.POINTER(PmgCfg), PP]),
     "fgpu_pmg_info": (i32, [P, DP, P, DP]),

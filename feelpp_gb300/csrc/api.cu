@@ -698,6 +698,12 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     return assemble_impl(ctx, A, f, A->d_kappa_stage, accumulate);
 }
 
+int fgpu_set_tensor_cores(fgpu_ctx* ctx, int on) {
+    if (!ctx) return FGPU_ERR_INVALID;
+    ctx->tensor_cores = on ? 1 : 0;
+    return FGPU_OK;
+}
+
 int fgpu_set_host_transfer(fgpu_ctx* ctx, int mode) {
     if (!ctx) return FGPU_ERR_INVALID;
     if (mode != FGPU_HOST_TRANSFER_AUTO && mode != FGPU_HOST_TRANSFER_COPY && mode != FGPU_HOST_TRANSFER_DIRECT)

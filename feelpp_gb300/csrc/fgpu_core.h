@@ -153,6 +153,7 @@ struct fgpu_ctx {
     int host_transfer = 0;         // FGPU_HOST_TRANSFER_*: how results reach host buffers
     int tune = 0;                  // 0: time launch shapes on first use; -1: fixed default shapes
     std::string tune_file;         // cache file of the picks ("" = none)
+    int tensor_cores = 1;          // binary32 quadrature-form element matrices on tcgen05 (fgpu_set_tensor_cores)
 };
 
 struct fgpu_graph {

@@ -19,6 +19,7 @@
 // them per CSR entry in element order, as for affine elements.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
@@ -27,6 +28,7 @@
 
 #include "df64.h"
 #include "fgpu_core.h"
+#include "tc_ptx.cuh"
 
 namespace fgpu {
 
@@ -58,6 +60,8 @@ struct HoTables {
     float* d_qwl = nullptr;    //                            (lo)
     uint8_t* d_ti = nullptr;   // ntri: row of each upper-triangle entry
     uint8_t* d_tj = nullptr;   // ntri: column
+    float* d_tcB = nullptr;    // tensor-core B operand: per chunk of points, per accumulator, tf32 hi / lo
+    std::vector<double> dphi, phi;   // Q n 3, Q n (host copies for building d_tcB)
 };
 
 std::mutex g_ho_mutex;
@@ -130,6 +134,8 @@ HoTables* get_ho_tables(fgpu_ctx* ctx, int order, int qdeg, bool hex = false) {
         delete T;
         return nullptr;
     }
+    T->dphi = R.dphi;
+    T->phi = R.phi;
     g_ho_tabs[key] = T;
     return T;
 }
@@ -339,6 +345,246 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
     }
 }
 
+// ---------------------------------------------------------------------------
+// Binary32 element matrices on the tensor cores (tcgen05, kind::tf32).
+//
+// With the per-point coefficients g_q = (G00, G11, G22, G01, G02, G12, m, 0) of an
+// element (G_q = w_q |det K_q| kappa B_q^T B_q, m = w_q |det K_q| mass) the
+// upper triangle of its matrix is one row of a dense product:
+//     K_e(t) = sum_q sum_r g_{q,r}(e) T_{q,r}(t),   t = (i, j), i <= j,
+//     T_{q,0..2}(t) = d_a,i d_a,j,  T_{q,3}(t) = d0_i d1_j + d1_i d0_j,  (02, 12 likewise),
+//     T_{q,6}(t) = phi_i phi_j,  T_{q,7} = 0  (d: reference gradients at point q),
+// i.e. for a tile of 128 elements D (128 x NTRI) = A (128 x 8Q) * B^T (8Q x NTRI),
+// with K = 8 per quadrature point: one tf32 MMA k-step per point. B is the same for
+// every element (built once on the host, split into tf32 high and low parts in the
+// shared-memory core-matrix layout of each chunk of QC points) and is staged per
+// chunk with a bulk asynchronous copy (cp.async.bulk, completion counted on an
+// mbarrier); A is formed by the CTA's 128 threads (one element each: the map, its
+// cofactors, determinant and B = K^-T at the chunk's points, in binary32) into one
+// of two stages while the tensor cores run the previous chunk's 3xTF32 products
+// (hi*hi + hi*lo + lo*hi into the FP32 accumulator in tensor memory). The
+// epilogue reads each element's row back with tcgen05.ld and stores it into the
+// two-phase element buffer. NACC accumulators of NP columns cover NTRI (two for
+// Q2 hexahedra, 378 entries). Every mbarrier wait is bounded: a timeout sets a
+// status bit and a shared flag, every thread leaves at the next barrier, and the
+// tensor memory is freed.
+// ---------------------------------------------------------------------------
+constexpr int kHoTcThreads = 128;
+constexpr int kHoTcQC = 2;                       // quadrature points per chunk (K = 16)
+constexpr int kStatusHoTcTimeout = 512;
+
+template <int N, int GN>
+struct HoTcDims {
+    static constexpr int NTRI = N * (N + 1) / 2;
+    static constexpr int NACC = NTRI > 256 ? 2 : 1;
+    static constexpr int NP = ((NTRI + NACC - 1) / NACC + 15) / 16 * 16;     // MMA N per accumulator
+    static constexpr int ACC_STRIDE = NACC == 2 ? 256 : NP;                   // tensor-memory columns between accumulators
+    static constexpr int NCOLS_USED = (NACC - 1) * ACC_STRIDE + NP;
+    static constexpr int NCOLS = NCOLS_USED <= 32 ? 32 : NCOLS_USED <= 64 ? 64 : NCOLS_USED <= 128 ? 128
+                                 : NCOLS_USED <= 256 ? 256 : 512;            // tensor-memory allocation
+    static constexpr int KC = 8 * kHoTcQC;
+    static constexpr int ABYTES = kTcTile * KC * 4;                           // one part (hi or lo) of A
+    static constexpr int BPART = NP * KC * 4;                                 // one part of one accumulator's B
+    static constexpr int BSTAGE = NACC * 2 * BPART;
+    static constexpr int QM = HoLimits<N, GN>::QMAX;
+    static constexpr int SMEM_USED = 1024 + 2 * BSTAGE + 2 * 2 * ABYTES + QM * GN * 3 * 4 + QM * 4 + 16 + 128;
+    // at most 512 / NCOLS blocks per SM, so that their tensor-memory allocations always fit
+    static constexpr int MAXCTA = 512 / NCOLS;
+    static constexpr int SMEM_MIN = 228 * 1024 / (MAXCTA + 1) + 1024;
+    static constexpr int SMEM = SMEM_USED > SMEM_MIN ? SMEM_USED : SMEM_MIN;
+};
+
+struct HoTcShared {
+    uint64_t bfull[2], mma[2];
+    uint32_t tmem;
+    int bad;
+};
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, void* mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+                 : "memory");
+}
+
+template <int N, int GN>
+__global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt, const double* __restrict__ xyz,
+                                                                    const int32_t* __restrict__ tets, const double* __restrict__ ho,
+                                                                    int Q, const float* __restrict__ Bg, const float* __restrict__ gdh,
+                                                                    const float* __restrict__ qwh, const double* __restrict__ d_kappa,
+                                                                    double kappa, double mass, const double* __restrict__ kscale,
+                                                                    float* __restrict__ kbuf, int* __restrict__ status, int budget) {
+    typedef HoTcDims<N, GN> D;
+    extern __shared__ __align__(1024) unsigned char ho_smem[];
+    unsigned char* base = (unsigned char*)(((uintptr_t)ho_smem + 1023) & ~(uintptr_t)1023);
+    unsigned char* Bs = base;                                   // 2 stages of B
+    unsigned char* As = Bs + 2 * D::BSTAGE;                     // 2 stages of (A hi, A lo)
+    float* gds = reinterpret_cast<float*>(As + 4 * D::ABYTES);  // Q GN 3 geometric reference gradients
+    float* qws = gds + D::QM * GN * 3;
+    HoTcShared* sh = reinterpret_cast<HoTcShared*>(((uintptr_t)(qws + D::QM) + 15) & ~(uintptr_t)15);   // mbarriers: 8-byte aligned
+    const int t = threadIdx.x;
+    for (int k = t; k < Q * GN * 3; k += kHoTcThreads) gds[k] = gdh[k];
+    for (int k = t; k < Q; k += kHoTcThreads) qws[k] = qwh[k];
+    if (t == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&sh->bfull[s], 1);
+            mbar_init(&sh->mma[s], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sh->bad = 0;
+    }
+    if ((t >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem)),
+                     "r"(D::NCOLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = sh->tmem;
+    const uint32_t lane_addr = tmem + ((uint32_t)((t >> 5) * 32) << 16);
+    const float ksc = kscale ? (float)*kscale : 1.0f;
+    const int nchunks = (Q + kHoTcQC - 1) / kHoTcQC;
+    const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
+    constexpr uint32_t idesc = make_idesc_tf32(D::NP);
+    constexpr uint32_t lbo = 128, sbo = (D::KC / 4) * 128;
+    uint32_t c = 0;                                             // chunk counter over all tiles
+    bool quit = false;
+    for (int64_t tile = blockIdx.x; tile < ntiles && !quit; tile += gridDim.x) {
+        const int64_t e = tile * kTcTile + t;
+        const bool live = e < nt;
+        float X[3 * GN];
+        float kap = 0.0f;
+        if (live) {
+#pragma unroll
+            for (int k = 0; k < 3 * GN; ++k) {
+                if (GN == 8) X[k] = (float)xyz[3 * (int64_t)tets[8 * e + k / 3] + k % 3];
+                else if (k < 12) X[k] = (float)xyz[3 * (int64_t)tets[4 * e + k / 3] + k % 3];
+                else X[k] = (float)ho[18 * e + (k - 12)];
+            }
+            kap = (float)(d_kappa ? d_kappa[e] : kappa) * ksc;
+        }
+        for (int ch = 0; ch < nchunks; ++ch, ++c) {
+            const int s = (int)(c & 1u);
+            const uint32_t u = c >> 1;
+            unsigned char* Ah = As + 2 * s * D::ABYTES;
+            unsigned char* Al = Ah + D::ABYTES;
+            unsigned char* Bst = Bs + s * D::BSTAGE;
+            // the stage is free once the products of chunk c - 2 are done
+            if (u > 0 && !mbar_wait(&sh->mma[s], (u - 1) & 1u, budget)) sh->bad = 1;
+            if (t == 0 && u > 0) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (t == 0) bulk_g2s(Bst, Bg + (size_t)ch * (D::BSTAGE / 4), D::BSTAGE, &sh->bfull[s]);
+            // this element's coefficients at the chunk's points (zero past the last point or element)
+#pragma unroll
+            for (int ql = 0; ql < kHoTcQC; ++ql) {
+                const int q = ch * kHoTcQC + ql;
+                float g[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) g[r] = 0.0f;
+                if (live && q < Q) {
+                    const float* gq = gds + q * GN * 3;
+                    float K[9];
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) K[k] = 0.0f;
+#pragma unroll
+                    for (int gg = 0; gg < GN; ++gg)
+#pragma unroll
+                        for (int r = 0; r < 3; ++r)
+#pragma unroll
+                            for (int cc = 0; cc < 3; ++cc) K[3 * r + cc] = fmaf(X[3 * gg + r], gq[3 * gg + cc], K[3 * r + cc]);
+                    const float C[9] = {K[4] * K[8] - K[5] * K[7], K[5] * K[6] - K[3] * K[8], K[3] * K[7] - K[4] * K[6],
+                                        K[2] * K[7] - K[1] * K[8], K[0] * K[8] - K[2] * K[6], K[1] * K[6] - K[0] * K[7],
+                                        K[1] * K[5] - K[2] * K[4], K[2] * K[3] - K[0] * K[5], K[0] * K[4] - K[1] * K[3]};
+                    const float det = K[0] * C[0] + K[1] * C[1] + K[2] * C[2];
+                    const float J = fabsf(det);
+                    if (!(J > 0.0f) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+                    float B[9];
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) B[k] = C[k] / det;
+                    const float wJ = qws[q] * J, sc = wJ * kap;
+                    const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                    for (int k = 0; k < 6; ++k)
+                        g[k] = sc * (B[pa[k]] * B[pb[k]] + B[3 + pa[k]] * B[3 + pb[k]] + B[6 + pa[k]] * B[6 + pb[k]]);
+                    g[6] = wJ * (float)mass;
+                }
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const float h = tf32_hi(g[r]);
+                    *reinterpret_cast<float*>(Ah + core_off(t, 8 * ql + r, D::KC)) = h;
+                    *reinterpret_cast<float*>(Al + core_off(t, 8 * ql + r, D::KC)) = g[r] - h;
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (sh->bad) { quit = true; break; }
+            if (t == 0) {
+                if (!mbar_wait(&sh->bfull[s], u & 1u, budget)) {
+                    sh->bad = 1;
+                    atomicOr(status, kStatusHoTcTimeout);
+                } else {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                    for (int a = 0; a < D::NACC; ++a) {
+                        const unsigned char* Bh = Bst + (2 * a) * D::BPART;
+                        const unsigned char* Bl = Bh + D::BPART;
+#pragma unroll
+                        for (int ks = 0; ks < kHoTcQC; ++ks) {
+                            const uint64_t ah = make_sdesc(smem_u32(Ah) + ks * 256, lbo, sbo);
+                            const uint64_t al = make_sdesc(smem_u32(Al) + ks * 256, lbo, sbo);
+                            const uint64_t bh = make_sdesc(smem_u32(Bh) + ks * 256, lbo, sbo);
+                            const uint64_t bl = make_sdesc(smem_u32(Bl) + ks * 256, lbo, sbo);
+                            const uint32_t dst = tmem + (uint32_t)(a * D::ACC_STRIDE);
+                            tc_mma(dst, ah, bh, idesc, (ch > 0 || ks > 0) ? 1u : 0u);
+                            tc_mma(dst, ah, bl, idesc, 1u);
+                            tc_mma(dst, al, bh, idesc, 1u);
+                        }
+                    }
+                    tc_commit(&sh->mma[s]);
+                }
+            }
+        }
+        if (quit) break;
+        // epilogue: the last chunk's commit completes the accumulator
+        const uint32_t cl = c - 1;
+        if (!mbar_wait(&sh->mma[cl & 1u], (cl >> 1) & 1u, budget)) {
+            sh->bad = 1;
+            atomicOr(status, kStatusHoTcTimeout);
+        }
+        __syncthreads();
+        if (sh->bad) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+        for (int a = 0; a < D::NACC; ++a)
+            for (int col = 0; col < D::NP; col += 16) {
+                uint32_t r[16];
+                tmem_ld16_nowait(lane_addr + (uint32_t)(a * D::ACC_STRIDE + col), r);
+                tmem_wait_ld();
+                if (live) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int tt = a * D::NP + col + i;   // accumulator a holds entries a NP .. a NP + NP - 1
+                        if (tt < D::NTRI) kbuf[e * D::NTRI + tt] = __uint_as_float(r[i]);
+                    }
+                }
+            }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    // after a failure, wait (bounded) for the products and copies this block issued last before the
+    // tensor memory and the shared memory go away
+    if (t == 0 && sh->bad && c > 0) {
+        const uint32_t cl = c - 1;
+        mbar_wait(&sh->mma[cl & 1u], (cl >> 1) & 1u, budget);
+        mbar_wait(&sh->bfull[cl & 1u], (cl >> 1) & 1u, budget);
+        if (c > 1) mbar_wait(&sh->bfull[(cl - 1) & 1u], ((cl - 1) >> 1) & 1u, budget);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if ((t >> 5) == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(D::NCOLS) : "memory");
+}
+
 // load vector on curved elements: thread per element, per point the map, J and the physical point
 template <int N, int GN>
 __global__ void ho_rhs_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
@@ -383,6 +629,90 @@ __global__ void ho_rhs_kernel(int64_t nt, const double* __restrict__ xyz, const 
 #pragma unroll
         for (int i = 0; i < N; ++i) work[e * N + i] = F[i];
     }
+}
+
+
+// ---- host side of the tensor-core element kernel ----
+// B operand of HoTcDims<N, GN> from the reference tables: per chunk of kHoTcQC points, per accumulator,
+// the tf32 high then low parts of T_{q,r}(t) in the shared-memory core-matrix layout (row = entry,
+// K index = 8 (point in chunk) + r).
+template <int N, int GN>
+static int ho_tc_tables(fgpu_ctx* ctx, HoTables* T) {
+    typedef HoTcDims<N, GN> D;
+    std::lock_guard<std::mutex> lock(g_ho_mutex);
+    if (T->d_tcB) return FGPU_OK;
+    const int Q = T->Q, nch = (Q + kHoTcQC - 1) / kHoTcQC;
+    std::vector<float> B((size_t)nch * (D::BSTAGE / 4), 0.0f);
+    std::vector<int> ti, tj;
+    for (int i = 0; i < N; ++i)
+        for (int j = i; j < N; ++j) {
+            ti.push_back(i);
+            tj.push_back(j);
+        }
+    auto tf32_hi_host = [](float x) {
+        uint32_t u;
+        std::memcpy(&u, &x, 4);
+        u = (u + 0x1000u) & 0xFFFFE000u;
+        float h;
+        std::memcpy(&h, &u, 4);
+        return h;
+    };
+    auto off = [](int row, int k) { return (size_t)((row >> 3) * (D::KC / 4) * 128 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4) / 4; };
+    for (int ch = 0; ch < nch; ++ch)
+        for (int a = 0; a < D::NACC; ++a)
+            for (int n = 0; n < D::NP; ++n) {
+                const int t = a * D::NP + n;
+                for (int ql = 0; ql < kHoTcQC; ++ql) {
+                    const int q = ch * kHoTcQC + ql;
+                    for (int r = 0; r < 8; ++r) {
+                        double v = 0.0;
+                        if (t < D::NTRI && q < Q && r < 7) {
+                            const int i = ti[t], j = tj[t];
+                            const double* di = &T->dphi[((size_t)q * N + i) * 3];
+                            const double* dj = &T->dphi[((size_t)q * N + j) * 3];
+                            switch (r) {
+                                case 0: v = di[0] * dj[0]; break;
+                                case 1: v = di[1] * dj[1]; break;
+                                case 2: v = di[2] * dj[2]; break;
+                                case 3: v = di[0] * dj[1] + di[1] * dj[0]; break;
+                                case 4: v = di[0] * dj[2] + di[2] * dj[0]; break;
+                                case 5: v = di[1] * dj[2] + di[2] * dj[1]; break;
+                                default: v = T->phi[(size_t)q * N + i] * T->phi[(size_t)q * N + j]; break;
+                            }
+                        }
+                        const float h = tf32_hi_host((float)v);
+                        const size_t base = (size_t)ch * (D::BSTAGE / 4) + (size_t)(2 * a) * (D::BPART / 4);
+                        B[base + off(n, 8 * ql + r)] = h;
+                        B[base + D::BPART / 4 + off(n, 8 * ql + r)] = (float)(v - (double)h);
+                    }
+                }
+            }
+    cudaError_t e = up(&T->d_tcB, B);
+    if (e != cudaSuccess) { cudaGetLastError(); ctx->err = "tensor-core element tables: upload failed"; return FGPU_ERR_CUDA; }
+    return FGPU_OK;
+}
+
+constexpr int kHoTcWaitBudget = 1 << 22;
+
+template <int N, int GN>
+static int launch_ho_tc(fgpu_ctx* ctx, fgpu_matrix* A, HoTables* T, const double* d_kappa, const fgpu_form_desc* f) {
+    typedef HoTcDims<N, GN> D;
+    const fgpu_mesh* M = A->space->mesh;
+    if (T->Q > D::QM) { ctx->err = "tensor-core element kernel: too many quadrature points"; return FGPU_ERR_INVALID; }
+    int rc = ho_tc_tables<N, GN>(ctx, T);
+    if (rc) return rc;
+    auto kern = ho_element_tc_kernel<N, GN>;
+    FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, D::SMEM));
+    int per_sm = 0, sms = 0;
+    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kHoTcThreads, D::SMEM));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    per_sm = std::max(1, std::min(per_sm, D::MAXCTA));
+    const int64_t ntiles = (M->nt + kTcTile - 1) / kTcTile;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)per_sm * sms));
+    kern<<<blocks, kHoTcThreads, D::SMEM, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_tcB, T->d_gdh, T->d_qwh,
+                                                         d_kappa, f->kappa, f->mass, f->kappa_scale, (float*)A->d_kbuf,
+                                                         ctx->d_status, kHoTcWaitBudget);
+    return FGPU_OK;
 }
 
 int ho_qdeg_ok(fgpu_ctx* ctx, int order, int qdeg) {
@@ -430,7 +760,10 @@ int launch_assemble_hex(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, 
                                                                     T->d_dl, T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh,   \
                                                                     T->d_qwl, T->d_ti, T->d_tj, d_kappa, f->kappa, f->mass,    \
                                                                     f->kappa_scale, A->d_kbuf, ctx->d_status)
-    if (V->n == 8 && T->Q <= 8) {
+    if (f32 && ctx->tensor_cores) {
+        rc = V->n == 8 ? launch_ho_tc<8, 8>(ctx, A, T, d_kappa, f) : launch_ho_tc<27, 8>(ctx, A, T, d_kappa, f);
+        if (rc) return rc;
+    } else if (V->n == 8 && T->Q <= 8) {
         // Q1 with the 2^3 rule: four elements per warp, one point and one dof per lane
         const int nb4 = (int)std::max<int64_t>(1, std::min<int64_t>((M->nt + 15) / 16, 152 * 32));
         if (f32) HEX_LAUNCH(kHoF32, 8, 8, nb4); else HEX_LAUNCH(kHoDF64, 8, 8, nb4);
@@ -503,10 +836,16 @@ int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, c
                                                                 T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh, T->d_qwl,      \
                                                                 T->d_ti, T->d_tj, d_kappa,                                     \
                                                                 f->kappa, f->mass, f->kappa_scale, A->d_kbuf, ctx->d_status)
-    switch (V->n) {
-        case 4: if (f32) HO_LAUNCH(kHoF32, 4); else HO_LAUNCH(kHoDF64, 4); break;
-        case 10: if (f32) HO_LAUNCH(kHoF32, 10); else HO_LAUNCH(kHoDF64, 10); break;
-        default: if (f32) HO_LAUNCH(kHoF32, 20); else HO_LAUNCH(kHoDF64, 20); break;
+    if (f32 && ctx->tensor_cores) {
+        rc = V->n == 4 ? launch_ho_tc<4, 10>(ctx, A, T, d_kappa, f)
+             : V->n == 10 ? launch_ho_tc<10, 10>(ctx, A, T, d_kappa, f) : launch_ho_tc<20, 10>(ctx, A, T, d_kappa, f);
+        if (rc) return rc;
+    } else {
+        switch (V->n) {
+            case 4: if (f32) HO_LAUNCH(kHoF32, 4); else HO_LAUNCH(kHoDF64, 4); break;
+            case 10: if (f32) HO_LAUNCH(kHoF32, 10); else HO_LAUNCH(kHoDF64, 10); break;
+            default: if (f32) HO_LAUNCH(kHoF32, 20); else HO_LAUNCH(kHoDF64, 20); break;
+        }
     }
 #undef HO_LAUNCH
     prof_end(ctx, ev);

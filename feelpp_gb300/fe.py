@@ -49,6 +49,11 @@ class Environment:
     def launches(self):
         return int(self.lib.fgpu_launch_count(self.h))
 
+    def set_tensor_cores(self, on=True):
+        """Binary32 quadrature-form element matrices (curved tetrahedra, hexahedra) on the tensor cores
+        (default) or on the CUDA cores."""
+        self.check(self.lib.fgpu_set_tensor_cores(self.h, 1 if on else 0))
+
     def set_host_transfer(self, mode="auto"):
         """How host-output assembly moves values: "auto", "copy" (copy engines) or "direct" (kernel stores
         into the page-locked host buffer)."""

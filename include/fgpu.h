@@ -270,6 +270,11 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* fo
  * to the host while the next is gathered (pin host_val for the overlap); other forms assemble, then
  * copy. The device values are the same as after fgpu_assemble_matrix. */
 int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, double* host_val);
+/* binary32 element matrices of the quadrature form (curved tetrahedra, hexahedra: the per-point
+ * contraction K_e = sum_q dphi^T G_q dphi + m_q phi phi^T of BilinearForm::Context::integrate,
+ * feelpp/feel/feelvf/bilinearformcontext.hpp:585-589) on the tensor cores (tcgen05 kind::tf32,
+ * 3xTF32 products, FP32 accumulation in tensor memory): 1 (default) or 0 (CUDA cores) */
+int fgpu_set_tensor_cores(fgpu_ctx* ctx, int on);
 /* FGPU_HOST_TRANSFER_* for later fgpu_assemble_matrix_host calls (default AUTO) */
 int fgpu_set_host_transfer(fgpu_ctx* ctx, int mode);
 int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, const double* d_kappa,
