@@ -370,7 +370,8 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
 // tensor memory is freed.
 // ---------------------------------------------------------------------------
 constexpr int kHoTcThreads = 128;
-constexpr int kHoTcQC = 2;                       // quadrature points per chunk (K = 16)
+constexpr int kHoTcQC = 1;                       // quadrature points per chunk (K = 8: one MMA k-step)
+constexpr int kHoTcBStages = 4;                  // table stages; the copy for chunk c + 2 starts at chunk c
 constexpr int kStatusHoTcTimeout = 512;
 
 template <int N, int GN>
@@ -387,7 +388,7 @@ struct HoTcDims {
     static constexpr int BPART = NP * KC * 4;                                 // one part of one accumulator's B
     static constexpr int BSTAGE = NACC * 2 * BPART;
     static constexpr int QM = HoLimits<N, GN>::QMAX;
-    static constexpr int SMEM_USED = 1024 + 2 * BSTAGE + 2 * 2 * ABYTES + QM * GN * 3 * 4 + QM * 4 + 16 + 128;
+    static constexpr int SMEM_USED = 1024 + kHoTcBStages * BSTAGE + 2 * 2 * ABYTES + QM * GN * 3 * 4 + QM * 4 + 16 + 256;
     // at most 512 / NCOLS blocks per SM, so that their tensor-memory allocations always fit
     static constexpr int MAXCTA = 512 / NCOLS;
     static constexpr int SMEM_MIN = 228 * 1024 / (MAXCTA + 1) + 1024;
@@ -395,7 +396,7 @@ struct HoTcDims {
 };
 
 struct HoTcShared {
-    uint64_t bfull[2], mma[2];
+    uint64_t bfull[kHoTcBStages], mma[kHoTcBStages];
     uint32_t tmem;
     int bad;
 };
@@ -415,23 +416,33 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
                                                                     double kappa, double mass, const double* __restrict__ kscale,
                                                                     float* __restrict__ kbuf, int* __restrict__ status, int budget) {
     typedef HoTcDims<N, GN> D;
+    constexpr int NB = kHoTcBStages;
     extern __shared__ __align__(1024) unsigned char ho_smem[];
     unsigned char* base = (unsigned char*)(((uintptr_t)ho_smem + 1023) & ~(uintptr_t)1023);
-    unsigned char* Bs = base;                                   // 2 stages of B
-    unsigned char* As = Bs + 2 * D::BSTAGE;                     // 2 stages of (A hi, A lo)
+    unsigned char* Bs = base;                                   // NB stages of B
+    unsigned char* As = Bs + NB * D::BSTAGE;                    // 2 stages of (A hi, A lo)
     float* gds = reinterpret_cast<float*>(As + 4 * D::ABYTES);  // Q GN 3 geometric reference gradients
     float* qws = gds + D::QM * GN * 3;
     HoTcShared* sh = reinterpret_cast<HoTcShared*>(((uintptr_t)(qws + D::QM) + 15) & ~(uintptr_t)15);   // mbarriers: 8-byte aligned
     const int t = threadIdx.x;
     for (int k = t; k < Q * GN * 3; k += kHoTcThreads) gds[k] = gdh[k];
     for (int k = t; k < Q; k += kHoTcThreads) qws[k] = qwh[k];
+    const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
+    const int nchunks = (Q + kHoTcQC - 1) / kHoTcQC;
+    const int64_t mytiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const uint32_t total = (uint32_t)(mytiles * nchunks);       // chunks this block runs
+    // table chunk of chunk c (every tile runs the same sequence of chunks)
+    auto copy_chunk = [&](uint32_t c) {
+        bulk_g2s(Bs + (c % NB) * D::BSTAGE, Bg + (size_t)(c % (uint32_t)nchunks) * (D::BSTAGE / 4), D::BSTAGE, &sh->bfull[c % NB]);
+    };
     if (t == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < NB; ++s) {
             mbar_init(&sh->bfull[s], 1);
             mbar_init(&sh->mma[s], 1);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         sh->bad = 0;
+        for (uint32_t c = 0; c < 2 && c < total; ++c) copy_chunk(c);
     }
     if ((t >> 5) == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem)),
@@ -444,8 +455,6 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
     const uint32_t tmem = sh->tmem;
     const uint32_t lane_addr = tmem + ((uint32_t)((t >> 5) * 32) << 16);
     const float ksc = kscale ? (float)*kscale : 1.0f;
-    const int nchunks = (Q + kHoTcQC - 1) / kHoTcQC;
-    const int64_t ntiles = (nt + kTcTile - 1) / kTcTile;
     constexpr uint32_t idesc = make_idesc_tf32(D::NP);
     constexpr uint32_t lbo = 128, sbo = (D::KC / 4) * 128;
     uint32_t c = 0;                                             // chunk counter over all tiles
@@ -465,15 +474,11 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
             kap = (float)(d_kappa ? d_kappa[e] : kappa) * ksc;
         }
         for (int ch = 0; ch < nchunks; ++ch, ++c) {
-            const int s = (int)(c & 1u);
-            const uint32_t u = c >> 1;
-            unsigned char* Ah = As + 2 * s * D::ABYTES;
+            unsigned char* Ah = As + 2 * (c & 1u) * D::ABYTES;
             unsigned char* Al = Ah + D::ABYTES;
-            unsigned char* Bst = Bs + s * D::BSTAGE;
-            // the stage is free once the products of chunk c - 2 are done
-            if (u > 0 && !mbar_wait(&sh->mma[s], (u - 1) & 1u, budget)) sh->bad = 1;
-            if (t == 0 && u > 0) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            if (t == 0) bulk_g2s(Bst, Bg + (size_t)ch * (D::BSTAGE / 4), D::BSTAGE, &sh->bfull[s]);
+            // chunk c - 2 done: its A stage and its table stage are free
+            if (c >= 2 && !mbar_wait(&sh->mma[(c - 2) % NB], ((c - 2) / NB) & 1u, budget)) sh->bad = 1;
+            if (t == 0 && c + 2 < total && !sh->bad) copy_chunk(c + 2);
             // this element's coefficients at the chunk's points (zero past the last point or element)
 #pragma unroll
             for (int ql = 0; ql < kHoTcQC; ++ql) {
@@ -498,9 +503,10 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
                     const float det = K[0] * C[0] + K[1] * C[1] + K[2] * C[2];
                     const float J = fabsf(det);
                     if (!(J > 0.0f) || !isfinite(J)) atomicOr(status, kStatusBadElement);
+                    const float id = 1.0f / det;
                     float B[9];
 #pragma unroll
-                    for (int k = 0; k < 9; ++k) B[k] = C[k] / det;
+                    for (int k = 0; k < 9; ++k) B[k] = C[k] * id;
                     const float wJ = qws[q] * J, sc = wJ * kap;
                     const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
@@ -519,11 +525,12 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
             __syncthreads();
             if (sh->bad) { quit = true; break; }
             if (t == 0) {
-                if (!mbar_wait(&sh->bfull[s], u & 1u, budget)) {
+                if (!mbar_wait(&sh->bfull[c % NB], (c / NB) & 1u, budget)) {
                     sh->bad = 1;
                     atomicOr(status, kStatusHoTcTimeout);
                 } else {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const unsigned char* Bst = Bs + (c % NB) * D::BSTAGE;
 #pragma unroll
                     for (int a = 0; a < D::NACC; ++a) {
                         const unsigned char* Bh = Bst + (2 * a) * D::BPART;
@@ -540,14 +547,14 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
                             tc_mma(dst, al, bh, idesc, 1u);
                         }
                     }
-                    tc_commit(&sh->mma[s]);
+                    tc_commit(&sh->mma[c % NB]);
                 }
             }
         }
         if (quit) break;
         // epilogue: the last chunk's commit completes the accumulator
         const uint32_t cl = c - 1;
-        if (!mbar_wait(&sh->mma[cl & 1u], (cl >> 1) & 1u, budget)) {
+        if (!mbar_wait(&sh->mma[cl % NB], (cl / NB) & 1u, budget)) {
             sh->bad = 1;
             atomicOr(status, kStatusHoTcTimeout);
         }
@@ -571,13 +578,11 @@ __global__ void __launch_bounds__(kHoTcThreads) ho_element_tc_kernel(int64_t nt,
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
     }
-    // after a failure, wait (bounded) for the products and copies this block issued last before the
-    // tensor memory and the shared memory go away
-    if (t == 0 && sh->bad && c > 0) {
-        const uint32_t cl = c - 1;
-        mbar_wait(&sh->mma[cl & 1u], (cl >> 1) & 1u, budget);
-        mbar_wait(&sh->bfull[cl & 1u], (cl >> 1) & 1u, budget);
-        if (c > 1) mbar_wait(&sh->bfull[(cl - 1) & 1u], ((cl - 1) >> 1) & 1u, budget);
+    // after a failure, wait (bounded) for the products and copies this block issued before the tensor
+    // memory and the shared memory go away
+    if (t == 0 && sh->bad) {
+        for (uint32_t k = (c > 2 ? c - 2 : 0); k < c; ++k) mbar_wait(&sh->mma[k % NB], (k / NB) & 1u, budget);
+        for (uint32_t k = (c > 2 ? c - 2 : 0); k < c + 2 && k < total; ++k) mbar_wait(&sh->bfull[k % NB], (k / NB) & 1u, budget);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -703,10 +708,18 @@ static int launch_ho_tc(fgpu_ctx* ctx, fgpu_matrix* A, HoTables* T, const double
     if (rc) return rc;
     auto kern = ho_element_tc_kernel<N, GN>;
     FGPU_CUDA_CHECK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, D::SMEM));
-    int per_sm = 0, sms = 0;
-    FGPU_CUDA_CHECK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kHoTcThreads, D::SMEM));
+    // resident blocks per SM from the registers and the shared memory (the occupancy calculator gives 1
+    // for kernels that allocate tensor memory; the blocks here never wait for one another, so more blocks
+    // than fit only queue), and at most 512 / NCOLS so that their tensor-memory allocations fit
+    cudaFuncAttributes fa{};
+    FGPU_CUDA_CHECK(ctx, cudaFuncGetAttributes(&fa, kern));
+    int sms = 0, smem_sm = 0, regs_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    per_sm = std::max(1, std::min(per_sm, D::MAXCTA));
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, ctx->device);
+    const int by_smem = smem_sm / (D::SMEM + 1024);
+    const int by_regs = regs_sm / (((fa.numRegs + 7) & ~7) * kHoTcThreads);
+    const int per_sm = std::max(1, std::min(std::min(by_smem, by_regs), D::MAXCTA));
     const int64_t ntiles = (M->nt + kTcTile - 1) / kTcTile;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)per_sm * sms));
     kern<<<blocks, kHoTcThreads, D::SMEM, ctx->stream>>>(M->nt, M->d_xyz, M->d_tets, M->d_ho, T->Q, T->d_tcB, T->d_gdh, T->d_qwh,
