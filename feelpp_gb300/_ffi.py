@@ -55,7 +55,7 @@ class SolverCfg(C.Structure):
 
 class AmgCfg(C.Structure):
     _fields_ = [("threshold", C.c_double), ("max_levels", C.c_int), ("coarse_eq_lim", C.c_int), ("agg_smooths", C.c_int),
-                ("smoother_degree", C.c_int)]
+                ("smoother_degree", C.c_int), ("setup_on_host", C.c_int)]
 
 
 class PmgCfg(C.Structure):
@@ -117,6 +117,7 @@ SIGNATURES = {
     "fgpu_amg_create": (i32, [P, P, C.POINTER(AmgCfg), PP]),
     "fgpu_amg_update": (i32, [P]),
     "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),
+    "fgpu_amg_setup_info": (i32, [P, C.POINTER(C.c_int), DP, DP]),
     "fgpu_amg_destroy": (i32, [P]),
     "fgpu_mesh_set_ho_nodes": (i32, [P, P]),
     "fgpu_assemble_matrix_host": (i32, [P, P, C.POINTER(FormDesc), P]),
@@ -135,6 +136,8 @@ SIGNATURES = {
     "fgpu_amg_host_export": (i32, [P, i32, P, P, P, P, P, P, P]),
     "fgpu_amg_host_coarse_inverse": (i32, [P, P]),
     "fgpu_amg_host_destroy": (i32, [P]),
+    "fgpu_amg_device_build": (i32, [P, P, C.POINTER(AmgCfg), PP]),
+    "fgpu_amg_host_device_levels": (i32, [P]),
     "fgpu_norms_sine": (i32, [P, P, P, i32, DP, DP]),
     "fgpu_operator_create": (i32, [P, P, C.POINTER(FormDesc), i32, PP]),
     "fgpu_operator_set_dirichlet": (i32, [P, i64, P]),

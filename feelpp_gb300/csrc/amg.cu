@@ -65,6 +65,9 @@ struct fgpu_amg {
     int degree = 3;                  // Chebyshev degree of the level smoothers
     int coarse_degree = 12;          // coarsest-level smoothing degree without a dense inverse
     double setup_ms = 0;
+    int device_levels = 0;           // levels whose set-up ran on the device
+    double aggregate_ms = 0;         // host aggregation inside the device set-up
+    double tail_ms = 0;              // host set-up of the levels below the device ones
     int launches_per_cycle = 0;
     fgpu_amg_cfg cfg{};
     float* xacc = nullptr;           // repeated cycles (amg_vcycle_f32 with cycles > 1): accumulated solution
@@ -547,63 +550,110 @@ cudaError_t upload_f32(float** dst, const std::vector<double>& v) {
 
 }  // namespace
 
+// binary32 copy of device FP64 values
+static __global__ void amg_f32_kernel(int64_t n, const double* __restrict__ a, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = (float)a[i];
+}
+
+// prolongator / restriction of a device-built level: the CSR index arrays are taken over, the values
+// rounded to binary32 (the host path's (float)a)
+static int take_transfer(fgpu_ctx* ctx, AmgDevCsr& D, int64_t** ia, int32_t** ja, float** a) {
+    FGPU_CUDA_CHECK(ctx, cudaMalloc(a, std::max<int64_t>(D.nnz, 1) * sizeof(float)));
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((D.nnz + 255) / 256, 152 * 16));
+    amg_f32_kernel<<<g, 256, 0, ctx->stream>>>(D.nnz, D.a, *a);
+    ctx->launches++;
+    FGPU_CUDA_CHECK(ctx, cudaGetLastError());
+    *ia = D.ia;
+    *ja = D.ja;
+    D.ia = nullptr;
+    D.ja = nullptr;
+    return FGPU_OK;
+}
+
 int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg* M) {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = A->nrows, nnz = A->nnz;
-    HostCsr H0;
-    H0.nrows = H0.ncols = n;
-    H0.ia.resize(n + 1);
-    H0.ja.resize(nnz);
-    H0.a.resize(nnz);
-    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
-    FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ia.data(), A->d_ia, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
-    FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ja.data(), A->d_ja, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.a.data(), A->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
-    AmgHostCfg hc;
-    if (cfg) {
-        hc.threshold = cfg->threshold;
-        if (cfg->max_levels > 0) hc.max_levels = cfg->max_levels;
-        if (cfg->coarse_eq_lim > 0) hc.coarse_eq_lim = cfg->coarse_eq_lim;
-        hc.agg_smooths = cfg->agg_smooths == 0 ? 1 : cfg->agg_smooths < 0 ? 0 : cfg->agg_smooths;
-        if (cfg->smoother_degree >= 2) M->degree = cfg->smoother_degree;
+    if (cfg && cfg->smoother_degree >= 2) M->degree = cfg->smoother_degree;
+    const AmgHostCfg hc = amg_host_cfg(cfg, ctx->host_threads);
+    // levels 0 .. ndev-1 built on the device (D), the rest on the host (H)
+    AmgDevHierarchy D;
+    AmgHierarchy& H = D.tail;
+    if (!cfg || !cfg->setup_on_host) {
+        const int rc = amg_build_device(ctx, A, hc, D);
+        if (rc) return rc;
+    } else {
+        HostCsr H0;
+        H0.nrows = H0.ncols = n;
+        H0.ia.resize(n + 1);
+        H0.ja.resize(nnz);
+        H0.a.resize(nnz);
+        FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ia.data(), A->d_ia, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ja.data(), A->d_ja, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.a.data(), A->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
+        std::string err;
+        if (!amg_build_host(std::move(H0), hc, H, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
     }
-    hc.nthreads = ctx->host_threads;
-    AmgHierarchy H;
-    std::string err;
-    if (!amg_build_host(std::move(H0), hc, H, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
-    const int nlev = (int)H.levels.size();
+    const int ndev = (int)D.levels.size();
+    const int nlev = ndev + (int)H.levels.size();
     M->L.assign(nlev, fgpu_amg::Level());
     int nl = 0;
     for (int l = 0; l < nlev; ++l) {
-        AmgHostLevel& hl = H.levels[l];
         fgpu_amg::Level& V = M->L[l];
-        V.n = hl.A.nrows;
-        V.nnz = (int64_t)hl.A.ja.size();
-        V.lmax = hl.lmax;
         const bool coarsest = l == nlev - 1;
+        const bool dev = l < ndev;
+        AmgHostLevel* hl = dev ? nullptr : &H.levels[l - ndev];
+        V.n = dev ? D.levels[l].A.nrows : hl->A.nrows;
+        V.nnz = dev ? D.levels[l].A.nnz : (int64_t)hl->A.ja.size();
+        V.lmax = dev ? D.levels[l].lmax : hl->lmax;
         cheb_coefs(V, coarsest ? M->coarse_degree : M->degree);
         if (l == 0 && A->nnz < ((int64_t)1 << 31)) {
             const int rc0 = upload_level0_device(ctx, A, V);
             if (rc0) return rc0;
+        } else if (dev && V.nnz < ((int64_t)1 << 31)) {
+            fgpu_matrix view;                       // the level operator's device arrays (not owned)
+            view.ctx = ctx;
+            view.nrows = V.n;
+            view.nnz = V.nnz;
+            view.d_ia = D.levels[l].A.ia;
+            view.d_ja = D.levels[l].A.ja;
+            view.d_val = D.levels[l].A.a;
+            const int rc0 = upload_level0_device(ctx, &view, V);
+            if (rc0) return rc0;
         } else {
+            HostCsr copy;
+            if (dev) {
+                const int rc0 = amg_copy_to_host(ctx, D.levels[l].A, copy);
+                if (rc0) return rc0;
+            }
+            const HostCsr& HA = dev ? copy : hl->A;
             std::vector<double> dinv(V.n, 0.0);
             for (int64_t i = 0; i < V.n; ++i)
-                for (int64_t p = hl.A.ia[i]; p < hl.A.ia[i + 1]; ++p)
-                    if (hl.A.ja[p] == i) dinv[i] = 1.0 / hl.A.a[p];
+                for (int64_t p = HA.ia[i]; p < HA.ia[i + 1]; ++p)
+                    if (HA.ja[p] == i) dinv[i] = 1.0 / HA.a[p];
             FGPU_CUDA_CHECK(ctx, upload_f32(&V.dinv, dinv));
-            FGPU_CUDA_CHECK(ctx, upload_sell(V, hl.A));
+            FGPU_CUDA_CHECK(ctx, upload_sell(V, HA));
         }
-        if (!coarsest) {
-            V.p_nnz = (int64_t)hl.P.ja.size();
-            V.r_nnz = (int64_t)hl.R.ja.size();
-            V.pG = lanes_for(hl.P.nrows, V.p_nnz);
-            V.rG = lanes_for(hl.R.nrows, V.r_nnz);
-            FGPU_CUDA_CHECK(ctx, upload(&V.p_ia, hl.P.ia.data(), hl.P.ia.size()));
-            FGPU_CUDA_CHECK(ctx, upload(&V.p_ja, hl.P.ja.data(), hl.P.ja.size()));
-            FGPU_CUDA_CHECK(ctx, upload_f32(&V.p_a, hl.P.a));
-            FGPU_CUDA_CHECK(ctx, upload(&V.r_ia, hl.R.ia.data(), hl.R.ia.size()));
-            FGPU_CUDA_CHECK(ctx, upload(&V.r_ja, hl.R.ja.data(), hl.R.ja.size()));
-            FGPU_CUDA_CHECK(ctx, upload_f32(&V.r_a, hl.R.a));
+        if (!coarsest && dev) {
+            AmgDevLevel& dl = D.levels[l];
+            V.p_nnz = dl.P.nnz;
+            V.r_nnz = dl.R.nnz;
+            V.pG = lanes_for(dl.P.nrows, V.p_nnz);
+            V.rG = lanes_for(dl.R.nrows, V.r_nnz);
+            int rc0 = take_transfer(ctx, dl.P, &V.p_ia, &V.p_ja, &V.p_a);
+            if (!rc0) rc0 = take_transfer(ctx, dl.R, &V.r_ia, &V.r_ja, &V.r_a);
+            if (rc0) return rc0;
+        } else if (!coarsest) {
+            V.p_nnz = (int64_t)hl->P.ja.size();
+            V.r_nnz = (int64_t)hl->R.ja.size();
+            V.pG = lanes_for(hl->P.nrows, V.p_nnz);
+            V.rG = lanes_for(hl->R.nrows, V.r_nnz);
+            FGPU_CUDA_CHECK(ctx, upload(&V.p_ia, hl->P.ia.data(), hl->P.ia.size()));
+            FGPU_CUDA_CHECK(ctx, upload(&V.p_ja, hl->P.ja.data(), hl->P.ja.size()));
+            FGPU_CUDA_CHECK(ctx, upload_f32(&V.p_a, hl->P.a));
+            FGPU_CUDA_CHECK(ctx, upload(&V.r_ia, hl->R.ia.data(), hl->R.ia.size()));
+            FGPU_CUDA_CHECK(ctx, upload(&V.r_ja, hl->R.ja.data(), hl->R.ja.size()));
+            FGPU_CUDA_CHECK(ctx, upload_f32(&V.r_a, hl->R.a));
         }
         float** vecs[6] = {&V.x, &V.b, &V.w, &V.d0, &V.d1, &V.e};
         for (float** v : vecs) FGPU_CUDA_CHECK(ctx, cudaMalloc(v, std::max<int64_t>(V.n, 1) * sizeof(float)));
@@ -617,7 +667,10 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
         }
     }
     M->launches_per_cycle = nl;
-    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+    FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));   // the device levels' FP64 values are freed on return
+    M->device_levels = ndev;
+    M->aggregate_ms = D.ms_aggregate;
+    M->tail_ms = cfg && cfg->setup_on_host ? 0.0 : D.ms_tail;
     M->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return FGPU_OK;
 }
@@ -664,6 +717,14 @@ extern "C" int fgpu_amg_info(const fgpu_amg* M, int* nlevels, int64_t* rows, int
         if (nnz) nnz[l] = M->L[l].nnz;
     }
     if (setup_ms) *setup_ms = M->setup_ms;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_amg_setup_info(const fgpu_amg* M, int* device_levels, double* aggregate_ms, double* host_tail_ms) {
+    if (!M) return FGPU_ERR_INVALID;
+    if (device_levels) *device_levels = M->device_levels;
+    if (aggregate_ms) *aggregate_ms = M->aggregate_ms;
+    if (host_tail_ms) *host_tail_ms = M->tail_ms;
     return FGPU_OK;
 }
 

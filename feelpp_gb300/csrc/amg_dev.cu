@@ -1,0 +1,943 @@
+// Device set-up of the smoothed-aggregation hierarchy (the default of fgpu_amg_create).
+//
+// The construction of the host set-up (amg_setup.cpp: Vanek, Mandel, Brezina 1996; PETSc PCGAMG "agg"
+// options of the reference, feelpp/feel/feelalg/preconditionerpetsc.cpp:2229-2330), with every step but
+// the greedy aggregation on the device, and every floating-point result formed in the host set-up's
+// order with the same roundings, so that the device levels equal the host levels bit for bit:
+//   * diagonal and strength graph: a row kernel marks |a_ij| > theta sqrt(|a_ii a_jj|) (j != i,
+//     a_ij != 0); its transpose is built by counting, a scan and a fill, each row sorted, and the two
+//     sorted lists merged per row (the symmetrised graph);
+//   * greedy aggregation: the host set-up's three passes over the copied graph (sequential by nature);
+//   * lambda_max(D^-1 A): 12 Lanczos steps on D^-1/2 A D^-1/2 from the host set-up's start vector, the
+//     products one thread per row in column order, the dot products as sequential sums over chunks of
+//     16384 rows combined in chunk order (the host's partition), the tridiagonal's largest eigenvalue
+//     by the host's Sturm bisection;
+//   * P0(i, agg(i)) = 1/sqrt(|agg|), A P0, and P = P0 - omega D^-1 (A P0) merged row by row;
+//   * R = P^T by counting, a scan, a fill and a per-row sort;
+//   * sparse products A P0, A P and R (A P): one warp per row of the left factor. The row's products
+//     are enumerated in (left column, right column) order 32 at a time; lanes holding the same output
+//     column form a group whose lowest lane inserts the column into a shared-memory hash table and adds
+//     the group's products to its running sum one by one in lane order, so every output entry is the
+//     host's sequential sum. Rows with more distinct columns than the small table holds are listed and
+//     redone with a larger table; the row is then sorted by column in shared memory (bitonic sort of
+//     the table's slot list) and written out.
+// Levels of at most 16384 rows, and any level with a row beyond the kernels' staging capacity, go to
+// the host set-up for the rest of the hierarchy (the results are the same either way).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fgpu_core.h"
+#include "scan.cuh"
+
+namespace fgpu {
+
+AmgDevCsr::AmgDevCsr(AmgDevCsr&& o) noexcept { *this = std::move(o); }
+AmgDevCsr& AmgDevCsr::operator=(AmgDevCsr&& o) noexcept {
+    if (this != &o) {
+        std::swap(nrows, o.nrows); std::swap(ncols, o.ncols); std::swap(nnz, o.nnz);
+        std::swap(ia, o.ia); std::swap(ja, o.ja); std::swap(a, o.a); std::swap(own, o.own);
+    }
+    return *this;
+}
+AmgDevCsr::~AmgDevCsr() {
+    if (own) { cudaFree(ia); cudaFree(ja); cudaFree(a); }
+}
+
+namespace {
+
+constexpr int kStOverflow = 1;               // a row beyond a kernel's staging capacity
+constexpr int kStDiag = 2;                   // a non-positive diagonal entry
+constexpr int64_t kLanczosChunk = 16384;     // rows per partial sum (the host set-up's partition)
+constexpr int kLanczosSteps = 12;
+constexpr int64_t kHandoffRows = 16384;      // levels this small continue on the host
+constexpr int kSortMax = 2048;               // longest row sorted by seg_sort_kernel
+constexpr int kSortWarps = 4;
+constexpr int kMaxLeft = 4096;               // longest left-factor row of a sparse product
+constexpr int kBins[3] = {256, 2048, 8192};  // hash table sizes (at most half full)
+constexpr int kBinLog[3] = {8, 11, 13};
+
+int grid_rows(int64_t n, int per_block, int cap = 152 * 16) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + per_block - 1) / per_block, cap));
+}
+
+struct Work {                                // device scratch freed at scope exit
+    std::vector<void*> ptrs;
+    Work() = default;
+    Work(const Work&) = delete;
+    Work& operator=(const Work&) = delete;
+    ~Work() { for (void* p : ptrs) cudaFree(p); }
+    template <typename T>
+    T* get(int64_t n) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, std::max<int64_t>(n, 1) * sizeof(T)) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
+
+#define DEV_TRY(call)                                                                                         \
+    do {                                                                                                      \
+        const cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) { ctx->err = std::string("gamg device set-up: ") + cudaGetErrorString(e_); return FGPU_ERR_CUDA; } \
+    } while (0)
+#define DEV_ALLOC(ok)                                                                                         \
+    do {                                                                                                      \
+        if (!(ok)) { ctx->err = "gamg device set-up: device allocation failed"; return FGPU_ERR_ALLOC; }    \
+    } while (0)
+
+int alloc_csr(fgpu_ctx* ctx, AmgDevCsr& C, int64_t nrows, int64_t ncols, int64_t nnz) {
+    C = AmgDevCsr();
+    C.nrows = nrows;
+    C.ncols = ncols;
+    C.nnz = nnz;
+    DEV_TRY(cudaMalloc(&C.ia, (nrows + 1) * sizeof(int64_t)));
+    DEV_TRY(cudaMalloc(&C.ja, std::max<int64_t>(nnz, 1) * sizeof(int32_t)));
+    DEV_TRY(cudaMalloc(&C.a, std::max<int64_t>(nnz, 1) * sizeof(double)));
+    return FGPU_OK;
+}
+
+int read_status(fgpu_ctx* ctx, const int* d_status, int* h) {
+    DEV_TRY(cudaMemcpyAsync(h, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));
+    return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------------------------------
+
+// diagonal (the last stored (i, i) entry, as the host's `diagonal`); flags a non-positive one
+__global__ void diag_kernel(int64_t n, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja, const double* __restrict__ a,
+                            double* __restrict__ d, int* __restrict__ status) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        for (int64_t p = ia[i]; p < ia[i + 1]; ++p)
+            if (ja[p] == i) v = a[p];
+        d[i] = v;
+        if (!(v > 0.0)) atomicOr(status, kStDiag);
+    }
+}
+
+// strong couplings of each row: counts (out == nullptr) or columns in row order at off[i]
+__global__ void strong_kernel(int64_t n, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja, const double* __restrict__ a,
+                              const double* __restrict__ d, double theta, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
+                              int32_t* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t k = 0;
+        for (int64_t p = ia[i]; p < ia[i + 1]; ++p) {
+            const int32_t j = ja[p];
+            const double v = a[p];
+            if (j == i || v == 0.0) continue;
+            if (fabs(v) > theta * sqrt(fabs(__dmul_rn(d[i], d[j])))) {
+                if (out) out[off[i] + k] = j;
+                ++k;
+            }
+        }
+        if (cnt) cnt[i] = k;
+    }
+}
+
+// column counts of a list of column indices
+__global__ void col_count_kernel(int64_t nnz, const int32_t* __restrict__ col, uint32_t* __restrict__ cnt) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(cnt + col[q], 1u);
+}
+
+// transpose fill: entry (i, col[q]) goes to row col[q] of the transpose (positions by cursors; the
+// rows are sorted afterwards). Row pointers of the source in 32-bit (off32) or 64-bit (off64) form.
+__global__ void transpose_fill_kernel(int64_t n, const uint32_t* __restrict__ off32, const int64_t* __restrict__ off64,
+                                      const int32_t* __restrict__ col, const double* __restrict__ val, uint32_t* __restrict__ cursor,
+                                      int32_t* __restrict__ oj, double* __restrict__ oa) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = off64 ? off64[i] : off32[i], e = off64 ? off64[i + 1] : off32[i + 1];
+        for (int64_t q = b; q < e; ++q) {
+            const uint32_t t = atomicAdd(cursor + col[q], 1u);
+            oj[t] = (int32_t)i;
+            if (val) oa[t] = val[q];
+        }
+    }
+}
+
+// each row's keys (and values) sorted by key: one warp per row, bitonic sort in shared memory
+__global__ void __launch_bounds__(kSortWarps * 32) seg_sort_kernel(int64_t n, const uint32_t* __restrict__ off32,
+                                                                  const int64_t* __restrict__ off64, int32_t* __restrict__ key,
+                                                                  double* __restrict__ val, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char ss_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* sv = reinterpret_cast<double*>(ss_smem) + warp * kSortMax;
+    int32_t* sk = reinterpret_cast<int32_t*>(ss_smem + (val ? kSortWarps * kSortMax * 8 : 0)) + warp * kSortMax;
+    for (int64_t r = (int64_t)blockIdx.x * kSortWarps + warp; r < n; r += (int64_t)gridDim.x * kSortWarps) {
+        const int64_t b = off64 ? off64[r] : off32[r], e = off64 ? off64[r + 1] : off32[r + 1];
+        const int len = (int)(e - b);
+        if (len <= 1) continue;
+        if (len > kSortMax) {
+            if (lane == 0) atomicOr(status, kStOverflow);
+            continue;
+        }
+        int P = 1;
+        while (P < len) P <<= 1;
+        for (int k = lane; k < P; k += 32) {
+            sk[k] = k < len ? key[b + k] : INT32_MAX;
+            if (val) sv[k] = k < len ? val[b + k] : 0.0;
+        }
+        __syncwarp();
+        for (int size = 2; size <= P; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int k = lane; k < P; k += 32) {
+                    const int l = k ^ stride;
+                    if (l > k) {
+                        const bool up = (k & size) == 0;
+                        const int32_t x = sk[k], y = sk[l];
+                        if ((x > y) == up) {
+                            sk[k] = y;
+                            sk[l] = x;
+                            if (val) {
+                                const double t = sv[k];
+                                sv[k] = sv[l];
+                                sv[l] = t;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int k = lane; k < len; k += 32) {
+            key[b + k] = sk[k];
+            if (val) val[b + k] = sv[k];
+        }
+        __syncwarp();
+    }
+}
+
+// union of two sorted rows (count when out == nullptr)
+__global__ void merge_kernel(int64_t n, const uint32_t* __restrict__ pa, const int32_t* __restrict__ ja_, const uint32_t* __restrict__ pb,
+                             const int32_t* __restrict__ jb, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
+                             int32_t* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t a = pa[i], b = pb[i], k = 0;
+        const uint32_t ae = pa[i + 1], be = pb[i + 1];
+        while (a < ae || b < be) {
+            int32_t v;
+            if (b >= be || (a < ae && ja_[a] < jb[b])) v = ja_[a++];
+            else if (a >= ae || jb[b] < ja_[a]) v = jb[b++];
+            else { v = ja_[a++]; ++b; }
+            if (out) out[off[i] + k] = v;
+            ++k;
+        }
+        if (cnt) cnt[i] = k;
+    }
+}
+
+// Lanczos: w_i = s_i sum_p (a_p s_j) v_j, the row summed in column order (one thread per row)
+__global__ void lanczos_spmv_kernel(int64_t n, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja, const double* __restrict__ a,
+                                    const double* __restrict__ s, const double* __restrict__ v, double* __restrict__ w) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int64_t p = ia[i]; p < ia[i + 1]; ++p) {
+            const int32_t j = ja[p];
+            acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(a[p], s[j]), v[j]));
+        }
+        w[i] = __dmul_rn(s[i], acc);
+    }
+}
+// partial[c] = sum over the rows of chunk c of x_i y_i, in row order (one thread per chunk)
+__global__ void chunk_dot_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ partial) {
+    const int64_t nch = (n + kLanczosChunk - 1) / kLanczosChunk;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nch; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r1 = min(n, (c + 1) * kLanczosChunk);
+        double t = 0.0;
+        for (int64_t i = c * kLanczosChunk; i < r1; ++i) t = __dadd_rn(t, __dmul_rn(x[i], y[i]));
+        partial[c] = t;
+    }
+}
+// w_i -= a v_i + b vold_i
+__global__ void lanczos_update_kernel(int64_t n, double a, double b, const double* __restrict__ v, const double* __restrict__ vold,
+                                      double* __restrict__ w) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        w[i] = __dsub_rn(w[i], __dadd_rn(__dmul_rn(a, v[i]), __dmul_rn(b, vold[i])));
+}
+// vold = v; v = w / b
+__global__ void lanczos_next_kernel(int64_t n, double b, const double* __restrict__ w, double* __restrict__ v, double* __restrict__ vold) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        vold[i] = v[i];
+        v[i] = __ddiv_rn(w[i], b);
+    }
+}
+__global__ void inv_sqrt_kernel(int64_t n, const double* __restrict__ d, double* __restrict__ s) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s[i] = d[i] > 0.0 ? __ddiv_rn(1.0, __dsqrt_rn(d[i])) : 0.0;
+}
+
+// tentative prolongator rows: one entry (agg_i, s0[agg_i]) where agg_i >= 0
+__global__ void p0_count_kernel(int64_t n, const int32_t* __restrict__ agg, uint32_t* __restrict__ cnt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        cnt[i] = agg[i] >= 0 ? 1u : 0u;
+}
+__global__ void p0_fill_kernel(int64_t n, const int32_t* __restrict__ agg, const double* __restrict__ s0, const uint32_t* __restrict__ off,
+                               int64_t* __restrict__ ia, int32_t* __restrict__ ja, double* __restrict__ a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
+        ia[i] = off[i];
+        if (i < n && agg[i] >= 0) {
+            ja[off[i]] = agg[i];
+            a[off[i]] = s0[agg[i]];
+        }
+    }
+}
+
+// P = P0 - omega D^-1 (A P0), the two sorted rows merged (count when oj == nullptr)
+__global__ void prolong_merge_kernel(int64_t n, const int64_t* __restrict__ p0i, const int32_t* __restrict__ p0j,
+                                     const double* __restrict__ p0a, const int64_t* __restrict__ qi, const int32_t* __restrict__ qj,
+                                     const double* __restrict__ qa, const double* __restrict__ d, double omega, uint32_t* __restrict__ cnt,
+                                     const uint32_t* __restrict__ off, int32_t* __restrict__ oj, double* __restrict__ oa) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double f = d[i] != 0.0 ? __ddiv_rn(omega, d[i]) : 0.0;
+        int64_t p = p0i[i];
+        const int64_t pe = p0i[i + 1];
+        uint32_t k = 0;
+        const int64_t o = oj ? (int64_t)off[i] : 0;
+        for (int64_t q = qi[i]; q < qi[i + 1]; ++q) {
+            const int32_t c = qj[q];
+            for (; p < pe && p0j[p] < c; ++p, ++k)
+                if (oj) { oj[o + k] = p0j[p]; oa[o + k] = p0a[p]; }
+            double v = __dmul_rn(-f, qa[q]);
+            if (p < pe && p0j[p] == c) { v = __dadd_rn(v, p0a[p]); ++p; }
+            if (oj) { oj[o + k] = c; oa[o + k] = v; }
+            ++k;
+        }
+        for (; p < pe; ++p, ++k)
+            if (oj) { oj[o + k] = p0j[p]; oa[o + k] = p0a[p]; }
+        if (cnt) cnt[i] = k;
+    }
+}
+
+__global__ void u32_to_i64_kernel(int64_t n1, const uint32_t* __restrict__ a, int64_t* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n1; i += (int64_t)gridDim.x * blockDim.x) b[i] = a[i];
+}
+
+// longest row and largest product count of a sparse product's rows (left factor A, right factor B)
+__global__ void row_stats_kernel(int64_t n, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja, const int64_t* __restrict__ ib,
+                                 unsigned long long* __restrict__ out) {
+    unsigned long long mlen = 0, mprod = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        unsigned long long pr = 0;
+        for (int64_t p = ia[i]; p < ia[i + 1]; ++p) pr += (unsigned long long)(ib[ja[p] + 1] - ib[ja[p]]);
+        mlen = max(mlen, (unsigned long long)(ia[i + 1] - ia[i]));
+        mprod = max(mprod, pr);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mlen = max(mlen, __shfl_xor_sync(0xffffffffu, mlen, o));
+        mprod = max(mprod, __shfl_xor_sync(0xffffffffu, mprod, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, mlen);
+        atomicMax(out + 1, mprod);
+    }
+}
+
+// Sparse product C = A B, one warp per row of A (see the file comment). Count pass (oj == nullptr):
+// cnt[i] = distinct columns of row i, or row i appended to `ovf` when it holds more than tsize / 2
+// (status overflow when ovf is null). Fill pass: rows whose count exceeds tsize / 2 are left to a
+// larger table; the others are written sorted at off[i].
+struct SpgemmArgs {
+    int64_t nrows = 0;
+    const int32_t* rows = nullptr;   // row list (null: rows 0..nrows-1)
+    const int64_t* ia = nullptr;
+    const int32_t* ja = nullptr;
+    const double* a = nullptr;
+    const int64_t* ib = nullptr;
+    const int32_t* jb = nullptr;
+    const double* b = nullptr;
+    int tsize = 256;                 // hash slots per warp (power of two, >= 64)
+    int tshift = 24;                 // 32 - log2(tsize)
+    int pre_cap = 0;                 // longest row of A
+    int warps = 8;                   // warps per block
+    int wbytes = 0;                  // shared memory per warp
+    uint32_t* cnt = nullptr;
+    int32_t* ovf = nullptr;
+    uint32_t* novf = nullptr;
+    const int64_t* off = nullptr;
+    int32_t* oj = nullptr;
+    double* oa = nullptr;
+    int* status = nullptr;
+};
+
+int spgemm_warp_bytes(int tsize, int pre_cap) {
+    const int b = tsize * 8 + 32 * 8 + tsize * 4 + (tsize / 2) * 4 + (pre_cap + 1) * 4;
+    return (b + 15) & ~15;
+}
+
+__global__ void __launch_bounds__(256) spgemm_kernel(SpgemmArgs g) {
+    extern __shared__ __align__(16) unsigned char sg_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* base = sg_smem + (size_t)warp * g.wbytes;
+    double* hv = reinterpret_cast<double*>(base);                               // tsize values
+    double* stage = hv + g.tsize;                                               // 32 products
+    int32_t* hk = reinterpret_cast<int32_t*>(stage + 32);                       // tsize keys (-1: empty)
+    int32_t* list = hk + g.tsize;                                               // tsize / 2 used slots
+    int32_t* pre = list + g.tsize / 2;                                          // pre_cap + 1 product offsets
+    const int T = g.tsize, half = g.tsize / 2;
+    const bool fill = g.oj != nullptr;
+    for (int k = lane; k < T; k += 32) hk[k] = -1;
+    __syncwarp();
+    for (int64_t r = (int64_t)blockIdx.x * g.warps + warp; r < g.nrows; r += (int64_t)gridDim.x * g.warps) {
+        const int64_t i = g.rows ? (int64_t)g.rows[r] : r;
+        if (fill && g.off[i + 1] - g.off[i] > half) continue;        // a larger table's row
+        const int64_t a0 = g.ia[i];
+        const int na = (int)(g.ia[i + 1] - a0);
+        // product offsets: exclusive scan of the lengths of the B rows named by row i of A
+        int run = 0;
+        for (int k0 = 0; k0 < na; k0 += 32) {
+            const int k = k0 + lane;
+            int len = 0;
+            if (k < na) {
+                const int32_t c = g.ja[a0 + k];
+                len = (int)(g.ib[c + 1] - g.ib[c]);
+            }
+            int x = len;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (k < na) pre[k] = run + x - len;
+            run += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        const int nprod = run;
+        int nuniq = 0;
+        bool over = false;
+        for (int s0 = 0; s0 < nprod; s0 += 32) {
+            const int pidx = s0 + lane;
+            const bool act = pidx < nprod;
+            int32_t col = -1;
+            double val = 0.0;
+            if (act) {
+                int lo = 0, hi = na - 1;                         // the A entry of product pidx
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (pre[mid] <= pidx) lo = mid; else hi = mid - 1;
+                }
+                const int64_t q = g.ib[g.ja[a0 + lo]] + (pidx - pre[lo]);
+                col = g.jb[q];
+                if (fill) val = __dmul_rn(g.a[a0 + lo], g.b[q]);
+            }
+            const unsigned grp = __match_any_sync(0xffffffffu, col);
+            const bool leader = act && lane == __ffs(grp) - 1;
+            int slot = -1;
+            bool newkey = false;
+            if (leader) {
+                uint32_t h = ((uint32_t)col * 2654435761u) >> g.tshift;
+                for (int probe = 0; probe < T; ++probe) {
+                    const int32_t old = atomicCAS(hk + h, -1, col);
+                    if (old == -1) { newkey = true; slot = (int)h; break; }
+                    if (old == col) { slot = (int)h; break; }
+                    h = (h + 1) & (uint32_t)(T - 1);
+                }
+                if (slot < 0) over = true;
+            }
+            const unsigned nb = __ballot_sync(0xffffffffu, newkey);
+            if (newkey) {
+                const int pos = nuniq + __popc(nb & ((1u << lane) - 1u));
+                if (pos < half) list[pos] = slot;
+            }
+            nuniq += __popc(nb);
+            if (fill) {
+                stage[lane] = val;
+                __syncwarp();
+                if (leader && slot >= 0) {
+                    double v = newkey ? 0.0 : hv[slot];
+                    for (unsigned m = grp; m; m &= m - 1u) v = __dadd_rn(v, stage[__ffs(m) - 1]);
+                    hv[slot] = v;
+                }
+            }
+            __syncwarp();
+            if (__any_sync(0xffffffffu, over) || nuniq > half) { over = true; break; }
+        }
+        if (over) {
+            for (int k = lane; k < T; k += 32) hk[k] = -1;
+            __syncwarp();
+            if (lane == 0) {
+                if (!fill && g.ovf) {
+                    g.ovf[atomicAdd(g.novf, 1u)] = (int32_t)i;
+                    g.cnt[i] = 0;
+                } else {
+                    atomicOr(g.status, kStOverflow);
+                    if (!fill) g.cnt[i] = 0;
+                }
+            }
+            continue;
+        }
+        if (!fill) {
+            if (lane == 0) g.cnt[i] = (uint32_t)nuniq;
+        } else {
+            // sort the used slots by key (padding slots -1 sort last), then write the row
+            int P = 1;
+            while (P < nuniq) P <<= 1;
+            for (int k = nuniq + lane; k < P; k += 32) list[k] = -1;
+            __syncwarp();
+            for (int size = 2; size <= P; size <<= 1)
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int k = lane; k < P; k += 32) {
+                        const int l = k ^ stride;
+                        if (l > k) {
+                            const bool up = (k & size) == 0;
+                            const int32_t sa = list[k], sb = list[l];
+                            const int32_t ka = sa < 0 ? INT32_MAX : hk[sa], kb = sb < 0 ? INT32_MAX : hk[sb];
+                            if ((ka > kb) == up) {
+                                list[k] = sb;
+                                list[l] = sa;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            const int64_t ob = g.off[i];
+            for (int k = lane; k < nuniq; k += 32) {
+                const int32_t s = list[k];
+                g.oj[ob + k] = hk[s];
+                g.oa[ob + k] = hv[s];
+            }
+        }
+        __syncwarp();
+        for (int k = lane; k < nuniq; k += 32) hk[list[k]] = -1;
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// host drivers
+// ---------------------------------------------------------------------------------------------------
+
+int launch_spgemm(fgpu_ctx* ctx, SpgemmArgs g, int bin) {
+    g.tsize = kBins[bin];
+    g.tshift = 32 - kBinLog[bin];
+    g.wbytes = spgemm_warp_bytes(g.tsize, g.pre_cap);
+    g.warps = std::max(1, std::min(8, (110 * 1024) / g.wbytes));
+    const int smem = g.warps * g.wbytes;
+    if (smem > 227 * 1024) { ctx->err = "gamg device set-up: product row too long for shared memory"; return FGPU_ERR_INVALID; }
+    DEV_TRY(cudaFuncSetAttribute(spgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int per_sm = std::max(1, std::min(2048 / (32 * g.warps), (228 * 1024) / (smem + 1024)));
+    const int blocks = grid_rows(g.nrows, g.warps, 152 * per_sm);
+    spgemm_kernel<<<blocks, 32 * g.warps, smem, ctx->stream>>>(g);
+    ctx->launches++;
+    DEV_TRY(cudaGetLastError());
+    return FGPU_OK;
+}
+
+// C = A B (rows sorted by column). *overflow: a row beyond the largest table or the staging capacity.
+int spgemm_dev(fgpu_ctx* ctx, const AmgDevCsr& A, const AmgDevCsr& B, AmgDevCsr& C, int* d_status, bool* overflow) {
+    *overflow = false;
+    const int64_t n = A.nrows;
+    Work w;
+    unsigned long long* stats = w.get<unsigned long long>(2);
+    uint32_t* cnt = w.get<uint32_t>(n + 1);
+    uint32_t* off32 = w.get<uint32_t>(n + 1);
+    int32_t* ovf1 = w.get<int32_t>(n);
+    int32_t* ovf2 = w.get<int32_t>(n);
+    uint32_t* novf = w.get<uint32_t>(2);
+    DEV_ALLOC(stats && cnt && off32 && ovf1 && ovf2 && novf);
+    DEV_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    DEV_TRY(cudaMemsetAsync(novf, 0, 2 * sizeof(uint32_t), ctx->stream));
+    row_stats_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, B.ia, stats);
+    ctx->launches++;
+    unsigned long long hs[2] = {0, 0};
+    DEV_TRY(cudaMemcpyAsync(hs, stats, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));
+    if (hs[0] > (unsigned long long)kMaxLeft || hs[1] > 0x7fffffffull) { *overflow = true; return FGPU_OK; }
+    SpgemmArgs g;
+    g.ia = A.ia; g.ja = A.ja; g.a = A.a;
+    g.ib = B.ia; g.jb = B.ja; g.b = B.a;
+    g.pre_cap = (int)hs[0];
+    g.status = d_status;
+    // count: all rows with the small table, the rows it cannot hold with the larger ones
+    uint32_t hn[2] = {0, 0};
+    {
+        SpgemmArgs c = g;
+        c.nrows = n; c.cnt = cnt; c.ovf = ovf1; c.novf = novf;
+        int rc = launch_spgemm(ctx, c, 0);
+        if (rc) return rc;
+        DEV_TRY(cudaMemcpyAsync(hn, novf, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));
+        if (hn[0]) {
+            c.nrows = hn[0]; c.rows = ovf1; c.ovf = ovf2; c.novf = novf + 1;
+            rc = launch_spgemm(ctx, c, 1);
+            if (rc) return rc;
+            DEV_TRY(cudaMemcpyAsync(hn + 1, novf + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+            DEV_TRY(cudaStreamSynchronize(ctx->stream));
+            if (hn[1]) {
+                c.nrows = hn[1]; c.rows = ovf2; c.ovf = nullptr; c.novf = nullptr;
+                rc = launch_spgemm(ctx, c, 2);
+                if (rc) return rc;
+            }
+        }
+    }
+    int st = 0;
+    int rc = read_status(ctx, d_status, &st);
+    if (rc) return rc;
+    if (st & kStOverflow) { *overflow = true; return FGPU_OK; }
+    uint64_t total = 0;
+    rc = scan_u32(ctx, cnt, off32, n, &total);
+    if (rc) return rc;
+    rc = alloc_csr(ctx, C, n, B.ncols, (int64_t)total);
+    if (rc) return rc;
+    u32_to_i64_kernel<<<grid_rows(n + 1, 256), 256, 0, ctx->stream>>>(n + 1, off32, C.ia);
+    ctx->launches++;
+    g.off = C.ia; g.oj = C.ja; g.oa = C.a;
+    {
+        SpgemmArgs f = g;
+        f.nrows = n;
+        rc = launch_spgemm(ctx, f, 0);
+        if (rc) return rc;
+        if (hn[0]) {
+            f.nrows = hn[0]; f.rows = ovf1;
+            rc = launch_spgemm(ctx, f, 1);
+            if (rc) return rc;
+        }
+        if (hn[1]) {
+            f.nrows = hn[1]; f.rows = ovf2;
+            rc = launch_spgemm(ctx, f, 2);
+            if (rc) return rc;
+        }
+    }
+    rc = read_status(ctx, d_status, &st);
+    if (rc) return rc;
+    *overflow = (st & kStOverflow) != 0;
+    return FGPU_OK;
+}
+
+int seg_sort(fgpu_ctx* ctx, int64_t n, const uint32_t* off32, const int64_t* off64, int32_t* key, double* val, int* d_status) {
+    const int smem = kSortWarps * kSortMax * (val ? 12 : 4);
+    DEV_TRY(cudaFuncSetAttribute(seg_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    seg_sort_kernel<<<grid_rows(n, kSortWarps, 152 * 4), kSortWarps * 32, smem, ctx->stream>>>(n, off32, off64, key, val, d_status);
+    ctx->launches++;
+    DEV_TRY(cudaGetLastError());
+    return FGPU_OK;
+}
+
+// T = M^T of an n x m device CSR (rows of T sorted by column of M)
+int transpose_dev(fgpu_ctx* ctx, const AmgDevCsr& M, AmgDevCsr& T, int* d_status) {
+    const int64_t m = M.ncols;
+    Work w;
+    uint32_t* tcnt = w.get<uint32_t>(m + 1);
+    uint32_t* toff = w.get<uint32_t>(m + 1);
+    uint32_t* cur = w.get<uint32_t>(m + 1);
+    DEV_ALLOC(tcnt && toff && cur);
+    DEV_TRY(cudaMemsetAsync(tcnt, 0, (m + 1) * sizeof(uint32_t), ctx->stream));
+    col_count_kernel<<<grid_rows(M.nnz, 256), 256, 0, ctx->stream>>>(M.nnz, M.ja, tcnt);
+    ctx->launches++;
+    int rc = scan_u32(ctx, tcnt, toff, m, nullptr);
+    if (rc) return rc;
+    rc = alloc_csr(ctx, T, m, M.nrows, M.nnz);
+    if (rc) return rc;
+    DEV_TRY(cudaMemcpyAsync(cur, toff, (m + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
+    transpose_fill_kernel<<<grid_rows(M.nrows, 256), 256, 0, ctx->stream>>>(M.nrows, nullptr, M.ia, M.ja, M.a, cur, T.ja, T.a);
+    u32_to_i64_kernel<<<grid_rows(m + 1, 256), 256, 0, ctx->stream>>>(m + 1, toff, T.ia);
+    ctx->launches += 2;
+    rc = seg_sort(ctx, m, nullptr, T.ia, T.ja, T.a, d_status);
+    if (rc) return rc;
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));     // the scratch above is freed on return
+    return FGPU_OK;
+}
+
+// One level on the device: lambda_max, strength graph, aggregation (host), P, R, A_c = R (A P).
+// *handoff: the level goes to the host set-up instead (a row beyond a kernel's capacity, or nothing
+// to coarsen); *last: the coarsening stagnates and A_c is the coarsest operator.
+int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_status, AmgDevCsr& Ac, bool* handoff, bool* last,
+              double* host_ms) {
+    *handoff = false;
+    *last = false;
+    const AmgDevCsr& A = L.A;
+    const int64_t n = A.nrows;
+    // the Lanczos start vector is made on the host while the device forms the diagonal and the graph
+    std::vector<double> hv0;
+    std::thread starter([&hv0, n] { amg_lanczos_start(n, hv0); });
+    struct Join {
+        std::thread& t;
+        ~Join() { if (t.joinable()) t.join(); }
+    } join{starter};
+    Work w;
+    double* d = w.get<double>(n);
+    uint32_t* cnt = w.get<uint32_t>(n + 1);
+    uint32_t* tp = w.get<uint32_t>(n + 1);
+    DEV_ALLOC(d && cnt && tp);
+    diag_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, d_status);
+    strong_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, cfg.threshold, cnt, nullptr, nullptr);
+    ctx->launches += 2;
+    uint64_t ns = 0;
+    int rc = scan_u32(ctx, cnt, tp, n, &ns);
+    if (rc) return rc;
+    int st = 0;
+    rc = read_status(ctx, d_status, &st);
+    if (rc) return rc;
+    if (st & kStDiag) { ctx->err = "gamg: the diagonal must be positive (SPD matrix)"; return FGPU_ERR_INVALID; }
+    // symmetrised strength graph
+    int32_t* tmpj = w.get<int32_t>((int64_t)ns);
+    uint32_t* tcnt = w.get<uint32_t>(n + 1);
+    uint32_t* tc = w.get<uint32_t>(n + 1);
+    uint32_t* cur = w.get<uint32_t>(n + 1);
+    int32_t* tj = w.get<int32_t>((int64_t)ns);
+    uint32_t* sp32 = w.get<uint32_t>(n + 1);
+    DEV_ALLOC(tmpj && tcnt && tc && cur && tj && sp32);
+    strong_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, cfg.threshold, nullptr, tp, tmpj);
+    DEV_TRY(cudaMemsetAsync(tcnt, 0, (n + 1) * sizeof(uint32_t), ctx->stream));
+    col_count_kernel<<<grid_rows((int64_t)ns, 256), 256, 0, ctx->stream>>>((int64_t)ns, tmpj, tcnt);
+    ctx->launches += 2;
+    rc = scan_u32(ctx, tcnt, tc, n, nullptr);
+    if (rc) return rc;
+    DEV_TRY(cudaMemcpyAsync(cur, tc, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
+    transpose_fill_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, tp, nullptr, tmpj, nullptr, cur, tj, nullptr);
+    ctx->launches++;
+    rc = seg_sort(ctx, n, tc, nullptr, tj, nullptr, d_status);
+    if (rc) return rc;
+    merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, tp, tmpj, tc, tj, cnt, nullptr, nullptr);
+    ctx->launches++;
+    uint64_t nsg = 0;
+    rc = scan_u32(ctx, cnt, sp32, n, &nsg);
+    if (rc) return rc;
+    int32_t* sj = w.get<int32_t>((int64_t)nsg);
+    DEV_ALLOC(sj);
+    merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, tp, tmpj, tc, tj, nullptr, sp32, sj);
+    ctx->launches++;
+    rc = read_status(ctx, d_status, &st);
+    if (rc) return rc;
+    if (st & kStOverflow) { *handoff = true; return FGPU_OK; }
+    std::vector<uint32_t> hsp32(n + 1);
+    std::vector<int32_t> hsj(nsg);
+    DEV_TRY(cudaMemcpyAsync(hsp32.data(), sp32, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (nsg) DEV_TRY(cudaMemcpyAsync(hsj.data(), sj, nsg * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    // lambda_max(D^-1 A) by Lanczos: the first product is queued behind the graph copies and runs
+    // while the host aggregates
+    double* s = w.get<double>(n);
+    double* v = w.get<double>(n);
+    double* vold = w.get<double>(n);
+    double* wv = w.get<double>(n);
+    const int64_t nch = (n + kLanczosChunk - 1) / kLanczosChunk;
+    double* part = w.get<double>(nch);
+    DEV_ALLOC(s && v && vold && wv && part);
+    starter.join();
+    DEV_TRY(cudaMemcpyAsync(v, hv0.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    DEV_TRY(cudaMemsetAsync(vold, 0, n * sizeof(double), ctx->stream));
+    inv_sqrt_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, d, s);
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));              // the graph is on the host
+    lanczos_spmv_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, s, v, wv);
+    ctx->launches += 2;
+    const auto th0 = std::chrono::steady_clock::now();
+    std::vector<int64_t> hsp(n + 1);
+    for (int64_t i = 0; i <= n; ++i) hsp[i] = hsp32[i];
+    const int64_t nagg = amg_aggregate(n, hsp, hsj, L.agg);
+    *host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
+    {
+        std::vector<double> al, be, hp(nch);
+        double bprev = 0.0;
+        auto dot = [&](const double* x, const double* y, double* out) -> int {
+            chunk_dot_kernel<<<grid_rows(nch, 128), 128, 0, ctx->stream>>>(n, x, y, part);
+            ctx->launches++;
+            DEV_TRY(cudaMemcpyAsync(hp.data(), part, nch * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            DEV_TRY(cudaStreamSynchronize(ctx->stream));
+            double t = 0.0;
+            for (int64_t c = 0; c < nch; ++c) t += hp[c];
+            *out = t;
+            return FGPU_OK;
+        };
+        for (int k = 0; k < kLanczosSteps; ++k) {
+            if (k > 0) {
+                lanczos_spmv_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, s, v, wv);
+                ctx->launches++;
+            }
+            double a = 0.0, b2 = 0.0;
+            rc = dot(wv, v, &a);
+            if (rc) return rc;
+            lanczos_update_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, a, bprev, v, vold, wv);
+            ctx->launches++;
+            rc = dot(wv, wv, &b2);
+            if (rc) return rc;
+            const double b = std::sqrt(b2);
+            al.push_back(a);
+            if (b < 1e-14 * std::fabs(a) || k + 1 == kLanczosSteps) break;
+            be.push_back(b);
+            lanczos_next_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, b, wv, v, vold);
+            ctx->launches++;
+            bprev = b;
+        }
+        L.lmax = amg_tridiag_lmax(al, be);
+    }
+    if (nagg == 0 || nagg >= n) { *handoff = true; return FGPU_OK; }
+    // tentative prolongator and A P0
+    std::vector<double> sz(nagg, 0.0), hs0(nagg);
+    for (int64_t i = 0; i < n; ++i)
+        if (L.agg[i] >= 0) sz[L.agg[i]] += 1.0;
+    for (int64_t c = 0; c < nagg; ++c) hs0[c] = 1.0 / std::sqrt(sz[c]);
+    int32_t* dagg = w.get<int32_t>(n);
+    double* ds0 = w.get<double>(nagg);
+    DEV_ALLOC(dagg && ds0);
+    DEV_TRY(cudaMemcpyAsync(dagg, L.agg.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    DEV_TRY(cudaMemcpyAsync(ds0, hs0.data(), nagg * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    p0_count_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, dagg, cnt);
+    ctx->launches++;
+    uint64_t n0 = 0;
+    rc = scan_u32(ctx, cnt, tp, n, &n0);
+    if (rc) return rc;
+    AmgDevCsr P0;
+    rc = alloc_csr(ctx, P0, n, nagg, (int64_t)n0);
+    if (rc) return rc;
+    p0_fill_kernel<<<grid_rows(n + 1, 256), 256, 0, ctx->stream>>>(n, dagg, ds0, tp, P0.ia, P0.ja, P0.a);
+    ctx->launches++;
+    bool ovf = false;
+    if (cfg.agg_smooths <= 0) {
+        L.P = std::move(P0);
+    } else {
+        AmgDevCsr AP0;
+        rc = spgemm_dev(ctx, A, P0, AP0, d_status, &ovf);
+        if (rc) return rc;
+        if (ovf) { *handoff = true; return FGPU_OK; }
+        const double omega = 4.0 / (3.0 * L.lmax);
+        prolong_merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, P0.ia, P0.ja, P0.a, AP0.ia, AP0.ja, AP0.a, d, omega, cnt,
+                                                                        nullptr, nullptr, nullptr);
+        ctx->launches++;
+        uint64_t pn = 0;
+        rc = scan_u32(ctx, cnt, tp, n, &pn);
+        if (rc) return rc;
+        rc = alloc_csr(ctx, L.P, n, nagg, (int64_t)pn);
+        if (rc) return rc;
+        prolong_merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, P0.ia, P0.ja, P0.a, AP0.ia, AP0.ja, AP0.a, d, omega, nullptr,
+                                                                        tp, L.P.ja, L.P.a);
+        u32_to_i64_kernel<<<grid_rows(n + 1, 256), 256, 0, ctx->stream>>>(n + 1, tp, L.P.ia);
+        ctx->launches += 2;
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));         // P0 and A P0 are freed on leaving this block
+    }
+    rc = transpose_dev(ctx, L.P, L.R, d_status);
+    if (rc) return rc;
+    rc = read_status(ctx, d_status, &st);
+    if (rc) return rc;
+    if (st & kStOverflow) { *handoff = true; return FGPU_OK; }
+    // Galerkin product A_c = R (A P)
+    AmgDevCsr AP;
+    rc = spgemm_dev(ctx, A, L.P, AP, d_status, &ovf);
+    if (rc) return rc;
+    if (ovf) { *handoff = true; return FGPU_OK; }
+    rc = spgemm_dev(ctx, L.R, AP, Ac, d_status, &ovf);
+    if (rc) return rc;
+    if (ovf) { *handoff = true; return FGPU_OK; }
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));             // the scratch of this level is freed on return
+    if ((double)nagg > 0.9 * (double)n) *last = true;
+    return FGPU_OK;
+}
+
+}  // namespace
+
+int amg_copy_to_host(fgpu_ctx* ctx, const AmgDevCsr& D, HostCsr& H) {
+    H.nrows = D.nrows;
+    H.ncols = D.ncols;
+    H.ia.assign(D.nrows + 1, 0);
+    H.ja.resize(D.nnz);
+    H.a.resize(D.nnz);
+    if (!D.ia) return FGPU_OK;
+    DEV_TRY(cudaMemcpyAsync(H.ia.data(), D.ia, (D.nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (D.nnz) {
+        DEV_TRY(cudaMemcpyAsync(H.ja.data(), D.ja, D.nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        DEV_TRY(cudaMemcpyAsync(H.a.data(), D.a, D.nnz * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));
+    return FGPU_OK;
+}
+
+int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg, AmgDevHierarchy& H) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int max_levels = cfg.max_levels > 0 ? cfg.max_levels : 10;
+    const int64_t coarse_lim = cfg.coarse_eq_lim > 0 ? cfg.coarse_eq_lim : 800;
+    H.levels.clear();
+    H.tail = AmgHierarchy();
+    int* d_status = nullptr;
+    DEV_TRY(cudaMalloc(&d_status, sizeof(int)));
+    struct StatusFree {
+        int* p;
+        ~StatusFree() { cudaFree(p); }
+    } status_free{d_status};
+    DEV_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
+    H.levels.emplace_back();
+    {
+        AmgDevCsr& A0 = H.levels[0].A;               // a view of the matrix's own arrays
+        A0.own = false;
+        A0.nrows = A0.ncols = Am->nrows;
+        A0.nnz = Am->nnz;
+        A0.ia = Am->d_ia;
+        A0.ja = Am->d_ja;
+        A0.a = static_cast<double*>(Am->d_val);
+    }
+    double host_ms = 0;
+    bool last = false;
+    int l = 0;
+    for (; l + 1 < max_levels && !last; ++l) {
+        AmgDevLevel& L = H.levels[l];
+        if (L.A.nrows <= coarse_lim || L.A.nrows <= kHandoffRows || L.A.nnz >= ((int64_t)1 << 32)) break;
+        AmgDevCsr Ac;
+        bool handoff = false;
+        const int rc = level_dev(ctx, L, cfg, d_status, Ac, &handoff, &last, &host_ms);
+        if (rc) return rc;
+        if (handoff) {
+            DEV_TRY(cudaStreamSynchronize(ctx->stream));
+            L.P = AmgDevCsr();
+            L.R = AmgDevCsr();
+            L.agg.clear();
+            L.lmax = 0;
+            DEV_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
+            last = false;
+            break;
+        }
+        H.levels.emplace_back();
+        H.levels.back().A = std::move(Ac);
+    }
+    // the rest on the host, from level l (its operator copied)
+    const auto t1 = std::chrono::steady_clock::now();
+    HostCsr Al;
+    int rc = amg_copy_to_host(ctx, H.levels[l].A, Al);
+    if (rc) return rc;
+    AmgHostCfg tc = cfg;
+    tc.max_levels = last ? 1 : max_levels - l;
+    std::string err;
+    if (!amg_build_host(std::move(Al), tc, H.tail, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
+    H.levels.resize(l);
+    const auto t2 = std::chrono::steady_clock::now();
+    H.ms_total = std::chrono::duration<double, std::milli>(t2 - t0).count();
+    H.ms_tail = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    H.ms_aggregate = host_ms;
+    return FGPU_OK;
+}
+
+}  // namespace fgpu
+
+// ---------------------------------------------------------------------------------------------------
+// The device-built hierarchy copied into the host set-up's inspection object (fgpu_amg_host_*), so
+// that it can be compared with fgpu_amg_host_build's level by level.
+// ---------------------------------------------------------------------------------------------------
+extern "C" int fgpu_amg_device_build(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg_host** out) {
+    using namespace fgpu;
+    if (!ctx || !A || !out) return FGPU_ERR_INVALID;
+    *out = nullptr;
+    if (A->precision != FGPU_F64) { ctx->err = "gamg: FP64 matrices only"; return FGPU_ERR_INVALID; }
+    if (ctx->capturing) { ctx->err = "gamg: set-up is not capturable"; return FGPU_ERR_INVALID; }
+    const AmgHostCfg hc = amg_host_cfg(cfg, ctx->host_threads);
+    AmgDevHierarchy D;
+    int rc = amg_build_device(ctx, A, hc, D);
+    if (rc) return rc;
+    fgpu_amg_host* h = new fgpu_amg_host();
+    for (auto& dl : D.levels) {
+        h->H.levels.emplace_back();
+        AmgHostLevel& hl = h->H.levels.back();
+        if ((rc = amg_copy_to_host(ctx, dl.A, hl.A)) || (rc = amg_copy_to_host(ctx, dl.P, hl.P)) ||
+            (rc = amg_copy_to_host(ctx, dl.R, hl.R))) {
+            delete h;
+            return rc;
+        }
+        hl.agg = dl.agg;
+        hl.lmax = dl.lmax;
+    }
+    for (auto& tl : D.tail.levels) h->H.levels.push_back(std::move(tl));
+    h->H.coarse_inv.swap(D.tail.coarse_inv);
+    h->device_levels = (int)D.levels.size();
+    *out = h;
+    return FGPU_OK;
+}

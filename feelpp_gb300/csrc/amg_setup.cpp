@@ -140,17 +140,9 @@ std::vector<double> diagonal(const HostCsr& A) {
 double lmax_estimate(const HostCsr& A, const std::vector<double>& d, int m, int nthreads) {
     const int64_t n = A.nrows;
     if (n == 0) return 1.0;
-    std::vector<double> s(n), v(n), vold(n, 0.0), w(n);
+    std::vector<double> s(n), v, vold(n, 0.0), w(n);
     for (int64_t i = 0; i < n; ++i) s[i] = d[i] > 0 ? 1.0 / std::sqrt(d[i]) : 0.0;
-    uint64_t h = 0x9E3779B97F4A7C15ull;
-    double nv = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        h ^= h >> 33; h *= 0xff51afd7ed558ccdull; h ^= h >> 33;
-        v[i] = (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
-        nv += v[i] * v[i];
-    }
-    nv = std::sqrt(nv);
-    for (auto& x : v) x /= nv;
+    amg_lanczos_start(n, v);
     std::vector<double> al, be;
     double bprev = 0;
     const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, (n + 4095) / 4096));
@@ -192,32 +184,7 @@ double lmax_estimate(const HostCsr& A, const std::vector<double>& d, int m, int 
         });
         bprev = b;
     }
-    // largest eigenvalue of the tridiagonal (al, be) by Sturm bisection
-    const int mm = (int)al.size();
-    double hi = 0;
-    for (int j = 0; j < mm; ++j) {
-        double g = std::fabs(al[j]);
-        if (j > 0) g += std::fabs(be[j - 1]);
-        if (j + 1 < mm) g += std::fabs(be[j]);
-        hi = std::max(hi, g);
-    }
-    double lo = 0;
-    auto below = [&](double x) {
-        int c = 0;
-        double q = 1.0;
-        for (int j = 0; j < mm; ++j) {
-            q = al[j] - x - (j > 0 ? be[j - 1] * be[j - 1] / q : 0.0);
-            if (q == 0.0) q = -1e-300;
-            if (q < 0) ++c;
-        }
-        return c;
-    };
-    for (int it = 0; it < 200 && hi - lo > 1e-10 * hi; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        if (below(mid) == mm) hi = mid;
-        else lo = mid;
-    }
-    return hi > 0 ? hi : 1.0;
+    return amg_tridiag_lmax(al, be);
 }
 
 // strong neighbours (symmetrised, without the diagonal) as a CSR graph
@@ -406,6 +373,65 @@ bool spd_inverse(int64_t n, std::vector<double>& M) {
 
 }  // namespace
 
+// fixed pseudo-random start of the Lanczos estimate, normalised
+void amg_lanczos_start(int64_t n, std::vector<double>& v) {
+    v.assign(n, 0.0);
+    uint64_t h = 0x9E3779B97F4A7C15ull;
+    double nv = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        h ^= h >> 33; h *= 0xff51afd7ed558ccdull; h ^= h >> 33;
+        v[i] = (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+        nv += v[i] * v[i];
+    }
+    nv = std::sqrt(nv);
+    for (auto& x : v) x /= nv;
+}
+
+// largest eigenvalue of the symmetric tridiagonal (al, be) by Sturm bisection
+double amg_tridiag_lmax(const std::vector<double>& al, const std::vector<double>& be) {
+    const int mm = (int)al.size();
+    double hi = 0;
+    for (int j = 0; j < mm; ++j) {
+        double g = std::fabs(al[j]);
+        if (j > 0) g += std::fabs(be[j - 1]);
+        if (j + 1 < mm) g += std::fabs(be[j]);
+        hi = std::max(hi, g);
+    }
+    double lo = 0;
+    auto below = [&](double x) {
+        int c = 0;
+        double q = 1.0;
+        for (int j = 0; j < mm; ++j) {
+            q = al[j] - x - (j > 0 ? be[j - 1] * be[j - 1] / q : 0.0);
+            if (q == 0.0) q = -1e-300;
+            if (q < 0) ++c;
+        }
+        return c;
+    };
+    for (int it = 0; it < 200 && hi - lo > 1e-10 * hi; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (below(mid) == mm) hi = mid;
+        else lo = mid;
+    }
+    return hi > 0 ? hi : 1.0;
+}
+
+int64_t amg_aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg) {
+    return aggregate(n, sp, sj, agg);
+}
+
+AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads) {
+    AmgHostCfg hc;
+    if (cfg) {
+        hc.threshold = cfg->threshold;
+        if (cfg->max_levels > 0) hc.max_levels = cfg->max_levels;
+        if (cfg->coarse_eq_lim > 0) hc.coarse_eq_lim = cfg->coarse_eq_lim;
+        hc.agg_smooths = cfg->agg_smooths == 0 ? 1 : cfg->agg_smooths < 0 ? 0 : cfg->agg_smooths;
+    }
+    hc.nthreads = nthreads;
+    return hc;
+}
+
 bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err) {
     const int nthreads = cfg.nthreads > 0 ? cfg.nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
     const int max_levels = cfg.max_levels > 0 ? cfg.max_levels : 10;
@@ -460,9 +486,6 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
 // Host-only entry points: build and inspect a hierarchy from a host CSR (no
 // device needed), for checking the set-up against its definition.
 // ---------------------------------------------------------------------------
-struct fgpu_amg_host {
-    fgpu::AmgHierarchy H;
-};
 
 extern "C" int fgpu_amg_host_build(int64_t n, const int64_t* ia, const int32_t* ja, const double* a, const fgpu_amg_cfg* cfg,
                                    int nthreads, fgpu_amg_host** out) {
@@ -473,14 +496,7 @@ extern "C" int fgpu_amg_host_build(int64_t n, const int64_t* ia, const int32_t* 
     A.ia.assign(ia, ia + n + 1);
     A.ja.assign(ja, ja + ia[n]);
     A.a.assign(a, a + ia[n]);
-    fgpu::AmgHostCfg hc;
-    if (cfg) {
-        hc.threshold = cfg->threshold;
-        if (cfg->max_levels > 0) hc.max_levels = cfg->max_levels;
-        if (cfg->coarse_eq_lim > 0) hc.coarse_eq_lim = cfg->coarse_eq_lim;
-        hc.agg_smooths = cfg->agg_smooths == 0 ? 1 : cfg->agg_smooths < 0 ? 0 : cfg->agg_smooths;
-    }
-    hc.nthreads = nthreads;
+    const fgpu::AmgHostCfg hc = fgpu::amg_host_cfg(cfg, nthreads);
     fgpu_amg_host* h = new fgpu_amg_host();
     std::string err;
     if (!fgpu::amg_build_host(std::move(A), hc, h->H, err)) {
@@ -492,6 +508,8 @@ extern "C" int fgpu_amg_host_build(int64_t n, const int64_t* ia, const int32_t* 
 }
 
 extern "C" int fgpu_amg_host_levels(const fgpu_amg_host* h) { return h ? (int)h->H.levels.size() : 0; }
+
+extern "C" int fgpu_amg_host_device_levels(const fgpu_amg_host* h) { return h ? h->device_levels : 0; }
 
 extern "C" int fgpu_amg_host_level(const fgpu_amg_host* h, int l, int64_t* n, int64_t* nnz, int64_t* p_nnz, int64_t* p_cols,
                                    double* lmax) {

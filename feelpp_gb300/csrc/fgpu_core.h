@@ -113,6 +113,39 @@ struct AmgHierarchy {
 };
 constexpr int64_t kAmgDenseCoarse = 2048;   // largest coarsest level inverted densely
 bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err);
+AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads);
+// pieces of the host set-up shared with the device set-up (amg_dev.cu)
+int64_t amg_aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg);
+void amg_lanczos_start(int64_t n, std::vector<double>& v);
+double amg_tridiag_lmax(const std::vector<double>& al, const std::vector<double>& be);
+
+// The hierarchy built on the device (amg_dev.cu): device CSR levels down to the first level handed to
+// the host set-up; `tail` holds that level and the ones below it.
+struct AmgDevCsr {
+    int64_t nrows = 0, ncols = 0, nnz = 0;
+    int64_t* ia = nullptr;
+    int32_t* ja = nullptr;
+    double* a = nullptr;
+    bool own = true;                 // false: a view of arrays owned elsewhere
+    AmgDevCsr() = default;
+    AmgDevCsr(const AmgDevCsr&) = delete;
+    AmgDevCsr& operator=(const AmgDevCsr&) = delete;
+    AmgDevCsr(AmgDevCsr&& o) noexcept;
+    AmgDevCsr& operator=(AmgDevCsr&& o) noexcept;
+    ~AmgDevCsr();
+};
+struct AmgDevLevel {
+    AmgDevCsr A, P, R;               // level operator (level 0: a view of the matrix), prolongator, R = P^T
+    std::vector<int32_t> agg;
+    double lmax = 0;
+};
+struct AmgDevHierarchy {
+    std::vector<AmgDevLevel> levels;
+    AmgHierarchy tail;
+    double ms_total = 0, ms_aggregate = 0, ms_tail = 0;
+};
+int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* A, const AmgHostCfg& cfg, AmgDevHierarchy& H);
+int amg_copy_to_host(fgpu_ctx* ctx, const AmgDevCsr& D, HostCsr& H);
 
 // Boundary dof nodes: the nodes carried by faces owned by one element; when
 // `xmax_on` only the faces whose three vertices satisfy x <= xmax (+1e-12).
@@ -409,3 +442,10 @@ int solve_refine_dd(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_matrix* A32,
             return FGPU_ERR_CUDA;                                                         \
         }                                                                                 \
     } while (0)
+
+// A hierarchy held for inspection (fgpu_amg_host_*): built on the host, or on the device and copied
+// (device_levels = the levels the device set-up built).
+struct fgpu_amg_host {
+    fgpu::AmgHierarchy H;
+    int device_levels = 0;
+};

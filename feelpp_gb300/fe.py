@@ -821,7 +821,9 @@ class Form2:
     def gamg(self, **opts):
         """The AMG hierarchy of this matrix (built, or rebuilt when the values changed since)."""
         amg = getattr(self, "_amg", None)
-        if amg is not None and amg.opts != opts:
+        full = dict(threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0, setup_on_host=False)
+        full.update(opts)
+        if amg is not None and amg.opts != full:
             amg = None
         if amg is None:
             amg = AMG(self, **opts)
@@ -844,13 +846,15 @@ class AMG:
     """Smoothed-aggregation AMG hierarchy of an assembled FP64 form (pc-type=gamg; PETSc PCGAMG "agg"
     options of the reference: threshold (pc-gamg-threshold), max_levels (pc-mg-levels), coarse_eq_lim
     (pc-gamg-coarse-eq-lim), agg_smooths (pc-gamg-nsmooths; -1 = unsmoothed), smoother_degree
-    (Chebyshev degree of the level smoothers). 0 selects the default."""
+    (Chebyshev degree of the level smoothers). 0 selects the default. setup_on_host: build the hierarchy
+    on the host instead of the device (the same hierarchy bit for bit)."""
 
-    def __init__(self, form, threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0):
+    def __init__(self, form, threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0,
+                 setup_on_host=False):
         self.env, self.form = form.env, form
         self.opts = dict(threshold=threshold, max_levels=max_levels, coarse_eq_lim=coarse_eq_lim, agg_smooths=agg_smooths,
-                         smoother_degree=smoother_degree)
-        cfg = _ffi.AmgCfg(float(threshold), max_levels, coarse_eq_lim, agg_smooths, smoother_degree)
+                         smoother_degree=smoother_degree, setup_on_host=setup_on_host)
+        cfg = _ffi.AmgCfg(float(threshold), max_levels, coarse_eq_lim, agg_smooths, smoother_degree, int(bool(setup_on_host)))
         h = C.c_void_p()
         self.env.check(self.env.lib.fgpu_amg_create(self.env.h, form.h, C.byref(cfg), C.byref(h)))
         self.h = h
@@ -864,8 +868,11 @@ class AMG:
         nnz = np.zeros(16, dtype=np.int64)
         ms = C.c_double()
         self.env.check(self.env.lib.fgpu_amg_info(self.h, C.byref(nl), _ptr(rows), _ptr(nnz), C.byref(ms)))
+        dl, agg_ms, tail_ms = C.c_int(), C.c_double(), C.c_double()
+        self.env.check(self.env.lib.fgpu_amg_setup_info(self.h, C.byref(dl), C.byref(agg_ms), C.byref(tail_ms)))
         return {"levels": nl.value, "rows": rows[:nl.value].tolist(), "nnz": nnz[:nl.value].tolist(),
-                "setup_ms": ms.value}
+                "setup_ms": ms.value, "device_levels": dl.value, "setup_aggregate_ms": agg_ms.value,
+                "setup_host_tail_ms": tail_ms.value}
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -178,6 +178,8 @@ typedef struct {              /* smoothed-aggregation AMG (PETSc PCGAMG "agg" op
     int coarse_eq_lim;        /* pc-gamg-coarse-eq-lim (0 = 800) */
     int agg_smooths;          /* pc-gamg-nsmooths: 0 = default 1 (smoothed aggregation); -1 = none */
     int smoother_degree;      /* Chebyshev degree of the level smoothers (0 = 3, i.e. 2 operator sweeps) */
+    int setup_on_host;        /* 0: hierarchy built on the device (levels of at most 16384 rows on the host);
+                                 1: built on the host. Both give the same hierarchy bit for bit. */
 } fgpu_amg_cfg;
 
 typedef struct {
@@ -335,8 +337,11 @@ int fgpu_solve_cg_refine_dd(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, 
  *      iteration (Chebyshev level smoothers, dense coarsest solve). A must outlive the hierarchy. ---- */
 int fgpu_amg_create(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg** out);
 int fgpu_amg_update(fgpu_amg* amg);
-/* levels, rows[level], nnz[level] (arrays of at least 16 entries or NULL), host set-up time in ms */
+/* levels, rows[level], nnz[level] (arrays of at least 16 entries or NULL), set-up time in ms */
 int fgpu_amg_info(const fgpu_amg* amg, int* nlevels, int64_t* rows, int64_t* nnz, double* setup_ms);
+/* levels whose set-up ran on the device, and the host parts of the set-up time: the greedy aggregation
+ * of the device levels and the host set-up of the levels below them (ms) */
+int fgpu_amg_setup_info(const fgpu_amg* amg, int* device_levels, double* aggregate_ms, double* host_tail_ms);
 int fgpu_amg_destroy(fgpu_amg* amg);
 int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
                       const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
@@ -371,6 +376,11 @@ int fgpu_amg_host_export(const fgpu_amg_host* h, int level, int64_t* ia, int32_t
                          double* pa, int32_t* agg);
 int fgpu_amg_host_coarse_inverse(const fgpu_amg_host* h, double* out);
 int fgpu_amg_host_destroy(fgpu_amg_host* h);
+/* the device set-up's hierarchy of an assembled FP64 matrix, copied into a host inspection object
+ * (replaces the host set-up of fgpu_amg_create; amg_setup.cpp's construction, same bits);
+ * fgpu_amg_host_device_levels: how many of its levels the device built (0 for fgpu_amg_host_build) */
+int fgpu_amg_device_build(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg_host** out);
+int fgpu_amg_host_device_levels(const fgpu_amg_host* h);
 
 /* ---- EnSight Gold export (the reference's default exporter, feelpp/feel/feelfilters/exporterensightgold.hpp):
  *      writes prefix.case, prefix.geo (C Binary, one part of tetra4, vertex coordinates) and
