@@ -117,7 +117,7 @@ SIGNATURES = {
     "fgpu_amg_create": (i32, [P, P, C.POINTER(AmgCfg), PP]),
     "fgpu_amg_update": (i32, [P]),
     "fgpu_amg_info": (i32, [P, C.POINTER(C.c_int), P, P, DP]),
-    "fgpu_amg_setup_info": (i32, [P, C.POINTER(C.c_int), DP, DP]),
+    "fgpu_amg_setup_info": (i32, [P, C.POINTER(C.c_int), P]),
     "fgpu_amg_destroy": (i32, [P]),
     "fgpu_mesh_set_ho_nodes": (i32, [P, P]),
     "fgpu_assemble_matrix_host": (i32, [P, P, C.POINTER(FormDesc), P]),

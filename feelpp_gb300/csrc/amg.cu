@@ -66,8 +66,7 @@ struct fgpu_amg {
     int coarse_degree = 12;          // coarsest-level smoothing degree without a dense inverse
     double setup_ms = 0;
     int device_levels = 0;           // levels whose set-up ran on the device
-    double aggregate_ms = 0;         // host aggregation inside the device set-up
-    double tail_ms = 0;              // host set-up of the levels below the device ones
+    fgpu::AmgSetupTimes times;       // set-up phases (device set-up; the host set-up reports tail and layout)
     int launches_per_cycle = 0;
     fgpu_amg_cfg cfg{};
     float* xacc = nullptr;           // repeated cycles (amg_vcycle_f32 with cycles > 1): accumulated solution
@@ -594,6 +593,7 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
         std::string err;
         if (!amg_build_host(std::move(H0), hc, H, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
     }
+    const auto t_layout = std::chrono::steady_clock::now();
     const int ndev = (int)D.levels.size();
     const int nlev = ndev + (int)H.levels.size();
     M->L.assign(nlev, fgpu_amg::Level());
@@ -669,9 +669,11 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
     M->launches_per_cycle = nl;
     FGPU_CUDA_CHECK(ctx, cudaStreamSynchronize(ctx->stream));   // the device levels' FP64 values are freed on return
     M->device_levels = ndev;
-    M->aggregate_ms = D.ms_aggregate;
-    M->tail_ms = cfg && cfg->setup_on_host ? 0.0 : D.ms_tail;
     M->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    M->times = D.times;
+    M->times.layout = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_layout).count();
+    if (cfg && cfg->setup_on_host) M->times.tail = M->setup_ms - M->times.layout;
+    M->times.total = M->setup_ms;
     return FGPU_OK;
 }
 
@@ -720,11 +722,14 @@ extern "C" int fgpu_amg_info(const fgpu_amg* M, int* nlevels, int64_t* rows, int
     return FGPU_OK;
 }
 
-extern "C" int fgpu_amg_setup_info(const fgpu_amg* M, int* device_levels, double* aggregate_ms, double* host_tail_ms) {
+extern "C" int fgpu_amg_setup_info(const fgpu_amg* M, int* device_levels, double* phases_ms) {
     if (!M) return FGPU_ERR_INVALID;
     if (device_levels) *device_levels = M->device_levels;
-    if (aggregate_ms) *aggregate_ms = M->aggregate_ms;
-    if (host_tail_ms) *host_tail_ms = M->tail_ms;
+    if (phases_ms) {
+        const AmgSetupTimes& t = M->times;
+        const double v[8] = {t.graph, t.aggregate, t.lanczos, t.prolong, t.galerkin, t.tail, t.layout, t.total};
+        for (int k = 0; k < 8; ++k) phases_ms[k] = v[k];
+    }
     return FGPU_OK;
 }
 

@@ -24,8 +24,10 @@
 // Levels of at most 16384 rows, and any level with a row beyond the kernels' staging capacity, go to
 // the host set-up for the rest of the hierarchy (the results are the same either way).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -244,15 +246,24 @@ __global__ void lanczos_spmv_kernel(int64_t n, const int64_t* __restrict__ ia, c
         w[i] = __dmul_rn(s[i], acc);
     }
 }
-// partial[c] = sum over the rows of chunk c of x_i y_i, in row order (one thread per chunk)
-__global__ void chunk_dot_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ partial) {
-    const int64_t nch = (n + kLanczosChunk - 1) / kLanczosChunk;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nch; c += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r1 = min(n, (c + 1) * kLanczosChunk);
-        double t = 0.0;
-        for (int64_t i = c * kLanczosChunk; i < r1; ++i) t = __dadd_rn(t, __dmul_rn(x[i], y[i]));
-        partial[c] = t;
+// partial[c] = sum over the rows of chunk c of x_i y_i, in row order: one block per chunk; the block
+// forms a tile's products in shared memory, one thread adds them in order
+constexpr int kDotTile = 2048;
+__global__ void __launch_bounds__(128) chunk_dot_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                                                        double* __restrict__ partial) {
+    __shared__ double buf[kDotTile];
+    const int64_t c = blockIdx.x;
+    const int64_t r0 = c * kLanczosChunk, r1 = min(n, r0 + kLanczosChunk);
+    double t = 0.0;
+    for (int64_t b = r0; b < r1; b += kDotTile) {
+        const int m = (int)min((int64_t)kDotTile, r1 - b);
+        for (int k = threadIdx.x; k < m; k += blockDim.x) buf[k] = __dmul_rn(x[b + k], y[b + k]);
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int k = 0; k < m; ++k) t = __dadd_rn(t, buf[k]);
+        __syncthreads();
     }
+    if (threadIdx.x == 0) partial[c] = t;
 }
 // w_i -= a v_i + b vold_i
 __global__ void lanczos_update_kernel(int64_t n, double a, double b, const double* __restrict__ v, const double* __restrict__ vold,
@@ -642,30 +653,113 @@ int transpose_dev(fgpu_ctx* ctx, const AmgDevCsr& M, AmgDevCsr& T, int* d_status
     return FGPU_OK;
 }
 
+// lambda_max(D^-1 A) by Lanczos on its own stream, driven by its own host thread (it runs while the
+// host aggregates); the same arithmetic as the host set-up's estimate
+struct LanczosJob {
+    int64_t n = 0;
+    const int64_t* ia = nullptr;
+    const int32_t* ja = nullptr;
+    const double* a = nullptr;
+    const double* d = nullptr;
+    double *s = nullptr, *v = nullptr, *vold = nullptr, *wv = nullptr, *part = nullptr;
+    cudaStream_t st = nullptr;
+    double lmax = 0;
+    int launches = 0;
+    cudaError_t err = cudaSuccess;
+
+    bool ok(cudaError_t e) {
+        if (e != cudaSuccess && err == cudaSuccess) err = e;
+        return e == cudaSuccess;
+    }
+    int device = 0;
+    void run() {
+        if (!ok(cudaSetDevice(device))) return;
+        std::vector<double> hv0;
+        amg_lanczos_start(n, hv0);
+        const int64_t nch = (n + kLanczosChunk - 1) / kLanczosChunk;
+        if (!ok(cudaMemcpyAsync(v, hv0.data(), n * sizeof(double), cudaMemcpyHostToDevice, st))) return;
+        if (!ok(cudaMemsetAsync(vold, 0, n * sizeof(double), st))) return;
+        inv_sqrt_kernel<<<grid_rows(n, 256), 256, 0, st>>>(n, d, s);
+        ++launches;
+        std::vector<double> al, be, hp(nch);
+        double bprev = 0.0;
+        auto dot = [&](const double* x, const double* y, double* out) {
+            chunk_dot_kernel<<<(int)nch, 128, 0, st>>>(n, x, y, part);
+            ++launches;
+            if (!ok(cudaMemcpyAsync(hp.data(), part, nch * sizeof(double), cudaMemcpyDeviceToHost, st)) || !ok(cudaStreamSynchronize(st)))
+                return false;
+            double t = 0.0;
+            for (int64_t c = 0; c < nch; ++c) t += hp[c];
+            *out = t;
+            return true;
+        };
+        for (int k = 0; k < kLanczosSteps; ++k) {
+            lanczos_spmv_kernel<<<grid_rows(n, 256), 256, 0, st>>>(n, ia, ja, a, s, v, wv);
+            ++launches;
+            double al_k = 0.0, b2 = 0.0;
+            if (!dot(wv, v, &al_k)) return;
+            lanczos_update_kernel<<<grid_rows(n, 256), 256, 0, st>>>(n, al_k, bprev, v, vold, wv);
+            ++launches;
+            if (!dot(wv, wv, &b2)) return;
+            const double b = std::sqrt(b2);
+            al.push_back(al_k);
+            if (b < 1e-14 * std::fabs(al_k) || k + 1 == kLanczosSteps) break;
+            be.push_back(b);
+            lanczos_next_kernel<<<grid_rows(n, 256), 256, 0, st>>>(n, b, wv, v, vold);
+            ++launches;
+            bprev = b;
+        }
+        ok(cudaGetLastError());
+        lmax = amg_tridiag_lmax(al, be);
+    }
+};
+
 // One level on the device: lambda_max, strength graph, aggregation (host), P, R, A_c = R (A P).
 // *handoff: the level goes to the host set-up instead (a row beyond a kernel's capacity, or nothing
 // to coarsen); *last: the coarsening stagnates and A_c is the coarsest operator.
 int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_status, AmgDevCsr& Ac, bool* handoff, bool* last,
-              double* host_ms) {
+              AmgSetupTimes& tm) {
+    using clock = std::chrono::steady_clock;
+    auto ms_since = [](clock::time_point t) { return std::chrono::duration<double, std::milli>(clock::now() - t).count(); };
+    auto tphase = clock::now();
     *handoff = false;
     *last = false;
     const AmgDevCsr& A = L.A;
     const int64_t n = A.nrows;
-    // the Lanczos start vector is made on the host while the device forms the diagonal and the graph
-    std::vector<double> hv0;
-    std::thread starter([&hv0, n] { amg_lanczos_start(n, hv0); });
-    struct Join {
-        std::thread& t;
-        ~Join() { if (t.joinable()) t.join(); }
-    } join{starter};
+    const int64_t nch = (n + kLanczosChunk - 1) / kLanczosChunk;
     Work w;
     double* d = w.get<double>(n);
     uint32_t* cnt = w.get<uint32_t>(n + 1);
     uint32_t* tp = w.get<uint32_t>(n + 1);
-    DEV_ALLOC(d && cnt && tp);
+    LanczosJob lz;
+    lz.n = n; lz.ia = A.ia; lz.ja = A.ja; lz.a = A.a; lz.d = d; lz.device = ctx->device;
+    lz.s = w.get<double>(n);
+    lz.v = w.get<double>(n);
+    lz.vold = w.get<double>(n);
+    lz.wv = w.get<double>(n);
+    lz.part = w.get<double>(nch);
+    DEV_ALLOC(d && cnt && tp && lz.s && lz.v && lz.vold && lz.wv && lz.part);
     diag_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, d_status);
+    ctx->launches++;
+    // the Lanczos thread and stream: started once the diagonal is formed, joined before any return
+    cudaEvent_t d_ready = nullptr;
+    DEV_TRY(cudaEventCreateWithFlags(&d_ready, cudaEventDisableTiming));
+    DEV_TRY(cudaEventRecord(d_ready, ctx->stream));
+    DEV_TRY(cudaStreamCreateWithFlags(&lz.st, cudaStreamNonBlocking));
+    DEV_TRY(cudaStreamWaitEvent(lz.st, d_ready, 0));
+    std::thread lanczos([&lz] { lz.run(); });
+    struct LanczosGuard {
+        std::thread& t;
+        LanczosJob& job;
+        cudaEvent_t ev;
+        ~LanczosGuard() {
+            if (t.joinable()) t.join();
+            cudaStreamDestroy(job.st);
+            cudaEventDestroy(ev);
+        }
+    } lanczos_guard{lanczos, lz, d_ready};
     strong_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, cfg.threshold, cnt, nullptr, nullptr);
-    ctx->launches += 2;
+    ctx->launches++;
     uint64_t ns = 0;
     int rc = scan_u32(ctx, cnt, tp, n, &ns);
     if (rc) return rc;
@@ -701,69 +795,45 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     DEV_ALLOC(sj);
     merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, tp, tmpj, tc, tj, nullptr, sp32, sj);
     ctx->launches++;
+    std::vector<uint32_t> hsp32(n + 1);
+    DEV_TRY(cudaMemcpyAsync(hsp32.data(), sp32, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     rc = read_status(ctx, d_status, &st);
     if (rc) return rc;
     if (st & kStOverflow) { *handoff = true; return FGPU_OK; }
-    std::vector<uint32_t> hsp32(n + 1);
-    std::vector<int32_t> hsj(nsg);
-    DEV_TRY(cudaMemcpyAsync(hsp32.data(), sp32, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    if (nsg) DEV_TRY(cudaMemcpyAsync(hsj.data(), sj, nsg * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    // lambda_max(D^-1 A) by Lanczos: the first product is queued behind the graph copies and runs
-    // while the host aggregates
-    double* s = w.get<double>(n);
-    double* v = w.get<double>(n);
-    double* vold = w.get<double>(n);
-    double* wv = w.get<double>(n);
-    const int64_t nch = (n + kLanczosChunk - 1) / kLanczosChunk;
-    double* part = w.get<double>(nch);
-    DEV_ALLOC(s && v && vold && wv && part);
-    starter.join();
-    DEV_TRY(cudaMemcpyAsync(v, hv0.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    DEV_TRY(cudaMemsetAsync(vold, 0, n * sizeof(double), ctx->stream));
-    inv_sqrt_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, d, s);
-    DEV_TRY(cudaStreamSynchronize(ctx->stream));              // the graph is on the host
-    lanczos_spmv_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, s, v, wv);
-    ctx->launches += 2;
-    const auto th0 = std::chrono::steady_clock::now();
-    std::vector<int64_t> hsp(n + 1);
-    for (int64_t i = 0; i <= n; ++i) hsp[i] = hsp32[i];
-    const int64_t nagg = amg_aggregate(n, hsp, hsj, L.agg);
-    *host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
-    {
-        std::vector<double> al, be, hp(nch);
-        double bprev = 0.0;
-        auto dot = [&](const double* x, const double* y, double* out) -> int {
-            chunk_dot_kernel<<<grid_rows(nch, 128), 128, 0, ctx->stream>>>(n, x, y, part);
-            ctx->launches++;
-            DEV_TRY(cudaMemcpyAsync(hp.data(), part, nch * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-            DEV_TRY(cudaStreamSynchronize(ctx->stream));
-            double t = 0.0;
-            for (int64_t c = 0; c < nch; ++c) t += hp[c];
-            *out = t;
-            return FGPU_OK;
-        };
-        for (int k = 0; k < kLanczosSteps; ++k) {
-            if (k > 0) {
-                lanczos_spmv_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, s, v, wv);
-                ctx->launches++;
+    tm.graph += ms_since(tphase);
+    tphase = clock::now();
+    // greedy aggregation on the host; its first pass follows the graph's copy in chunks of rows
+    std::unique_ptr<int32_t[]> hsj(new int32_t[std::max<uint64_t>(nsg, 1)]);
+    std::atomic<int64_t> rows_ready{0};
+    std::atomic<int> copy_failed{0};
+    cudaError_t copy_err = cudaSuccess;
+    std::thread copier([&] {
+        cudaSetDevice(ctx->device);
+        constexpr uint32_t kChunk = 1u << 22;            // entries per copy
+        int64_t r = 0;
+        while (r < n) {
+            const uint64_t target = (uint64_t)hsp32[r] + kChunk;
+            int64_t r1 = std::upper_bound(hsp32.begin() + r + 1, hsp32.end(), target,
+                                          [](uint64_t t, uint32_t x) { return t < (uint64_t)x; }) - hsp32.begin() - 1;
+            r1 = std::min<int64_t>(n, std::max<int64_t>(r1, r + 1));
+            const uint32_t b = hsp32[r], e = hsp32[r1];
+            if (e > b) {
+                copy_err = cudaMemcpyAsync(hsj.get() + b, sj + b, (size_t)(e - b) * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+                if (copy_err == cudaSuccess) copy_err = cudaStreamSynchronize(ctx->stream);
+                if (copy_err != cudaSuccess) { copy_failed.store(1, std::memory_order_release); return; }
             }
-            double a = 0.0, b2 = 0.0;
-            rc = dot(wv, v, &a);
-            if (rc) return rc;
-            lanczos_update_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, a, bprev, v, vold, wv);
-            ctx->launches++;
-            rc = dot(wv, wv, &b2);
-            if (rc) return rc;
-            const double b = std::sqrt(b2);
-            al.push_back(a);
-            if (b < 1e-14 * std::fabs(a) || k + 1 == kLanczosSteps) break;
-            be.push_back(b);
-            lanczos_next_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, b, wv, v, vold);
-            ctx->launches++;
-            bprev = b;
+            rows_ready.store(r1, std::memory_order_release);
+            r = r1;
         }
-        L.lmax = amg_tridiag_lmax(al, be);
+    });
+    const int64_t nagg = amg_aggregate_streamed(n, hsp32.data(), hsj.get(), rows_ready, copy_failed, L.agg);
+    copier.join();
+    if (copy_err != cudaSuccess || nagg < 0) {
+        ctx->err = std::string("gamg device set-up: graph copy: ") + cudaGetErrorString(copy_err);
+        return FGPU_ERR_CUDA;
     }
+    tm.aggregate += ms_since(tphase);
+    tphase = clock::now();
     if (nagg == 0 || nagg >= n) { *handoff = true; return FGPU_OK; }
     // tentative prolongator and A P0
     std::vector<double> sz(nagg, 0.0), hs0(nagg);
@@ -786,13 +856,28 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     p0_fill_kernel<<<grid_rows(n + 1, 256), 256, 0, ctx->stream>>>(n, dagg, ds0, tp, P0.ia, P0.ja, P0.a);
     ctx->launches++;
     bool ovf = false;
+    // lambda_max: wait for the Lanczos thread (A P0 does not need it)
+    auto join_lanczos = [&]() -> int {
+        const auto tw = clock::now();
+        if (lanczos.joinable()) lanczos.join();
+        ctx->launches += lz.launches;
+        lz.launches = 0;
+        tm.lanczos += ms_since(tw);
+        if (lz.err != cudaSuccess) { ctx->err = std::string("gamg device set-up: lambda_max: ") + cudaGetErrorString(lz.err); return FGPU_ERR_CUDA; }
+        L.lmax = lz.lmax;
+        return FGPU_OK;
+    };
     if (cfg.agg_smooths <= 0) {
         L.P = std::move(P0);
+        rc = join_lanczos();
+        if (rc) return rc;
     } else {
         AmgDevCsr AP0;
         rc = spgemm_dev(ctx, A, P0, AP0, d_status, &ovf);
         if (rc) return rc;
         if (ovf) { *handoff = true; return FGPU_OK; }
+        rc = join_lanczos();
+        if (rc) return rc;
         const double omega = 4.0 / (3.0 * L.lmax);
         prolong_merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, P0.ia, P0.ja, P0.a, AP0.ia, AP0.ja, AP0.a, d, omega, cnt,
                                                                         nullptr, nullptr, nullptr);
@@ -813,6 +898,8 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     rc = read_status(ctx, d_status, &st);
     if (rc) return rc;
     if (st & kStOverflow) { *handoff = true; return FGPU_OK; }
+    tm.prolong += ms_since(tphase);
+    tphase = clock::now();
     // Galerkin product A_c = R (A P)
     AmgDevCsr AP;
     rc = spgemm_dev(ctx, A, L.P, AP, d_status, &ovf);
@@ -822,6 +909,7 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     if (rc) return rc;
     if (ovf) { *handoff = true; return FGPU_OK; }
     DEV_TRY(cudaStreamSynchronize(ctx->stream));             // the scratch of this level is freed on return
+    tm.galerkin += ms_since(tphase);
     if ((double)nagg > 0.9 * (double)n) *last = true;
     return FGPU_OK;
 }
@@ -867,7 +955,7 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
         A0.ja = Am->d_ja;
         A0.a = static_cast<double*>(Am->d_val);
     }
-    double host_ms = 0;
+    H.times = AmgSetupTimes();
     bool last = false;
     int l = 0;
     for (; l + 1 < max_levels && !last; ++l) {
@@ -875,7 +963,7 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
         if (L.A.nrows <= coarse_lim || L.A.nrows <= kHandoffRows || L.A.nnz >= ((int64_t)1 << 32)) break;
         AmgDevCsr Ac;
         bool handoff = false;
-        const int rc = level_dev(ctx, L, cfg, d_status, Ac, &handoff, &last, &host_ms);
+        const int rc = level_dev(ctx, L, cfg, d_status, Ac, &handoff, &last, H.times);
         if (rc) return rc;
         if (handoff) {
             DEV_TRY(cudaStreamSynchronize(ctx->stream));
@@ -901,9 +989,8 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
     if (!amg_build_host(std::move(Al), tc, H.tail, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
     H.levels.resize(l);
     const auto t2 = std::chrono::steady_clock::now();
-    H.ms_total = std::chrono::duration<double, std::milli>(t2 - t0).count();
-    H.ms_tail = std::chrono::duration<double, std::milli>(t2 - t1).count();
-    H.ms_aggregate = host_ms;
+    H.times.total = std::chrono::duration<double, std::milli>(t2 - t0).count();
+    H.times.tail = std::chrono::duration<double, std::milli>(t2 - t1).count();
     return FGPU_OK;
 }
 

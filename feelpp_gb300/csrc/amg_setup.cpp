@@ -28,6 +28,7 @@
 // each output entry is accumulated in a fixed order and rows keep sorted
 // columns, so the hierarchy does not depend on the thread count.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -250,36 +251,46 @@ void strength(const HostCsr& A, const std::vector<double>& d, double theta, std:
     });
 }
 
-// greedy aggregation; returns the number of aggregates, agg[i] = -1 for nodes left out
-int64_t aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg) {
+// greedy aggregation; returns the number of aggregates, agg[i] = -1 for nodes left out. Every pass
+// visits the rows in order and reads only the visited row's neighbour list, so the first pass can run
+// while the lists are still arriving: ready(r) returns once rows [0, r) are present (false: they never
+// will be, and the aggregation returns -1).
+template <typename Off, typename Ready>
+int64_t aggregate_rows(int64_t n, const Off* sp, const int32_t* sj, std::vector<int32_t>& agg, Ready ready) {
     agg.assign(n, -1);
     int64_t nagg = 0;
+    constexpr int64_t kStep = 4096;
     // pass 1: roots whose whole strong neighbourhood is free
     for (int64_t i = 0; i < n; ++i) {
+        if (i % kStep == 0 && !ready(std::min(n, i + kStep))) return -1;
         if (agg[i] != -1 || sp[i + 1] == sp[i]) continue;
         bool free = true;
-        for (int64_t q = sp[i]; q < sp[i + 1] && free; ++q) free = agg[sj[q]] == -1;
+        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1] && free; ++q) free = agg[sj[q]] == -1;
         if (!free) continue;
         agg[i] = (int32_t)nagg;
-        for (int64_t q = sp[i]; q < sp[i + 1]; ++q) agg[sj[q]] = (int32_t)nagg;
+        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1]; ++q) agg[sj[q]] = (int32_t)nagg;
         ++nagg;
     }
     // pass 2: free nodes join the aggregate of their first aggregated neighbour (pass-1 state)
     std::vector<int32_t> snap(agg);
     for (int64_t i = 0; i < n; ++i) {
         if (snap[i] != -1 || sp[i + 1] == sp[i]) continue;
-        for (int64_t q = sp[i]; q < sp[i + 1]; ++q)
+        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1]; ++q)
             if (snap[sj[q]] != -1) { agg[i] = snap[sj[q]]; break; }
     }
     // pass 3: the rest form aggregates with their free neighbours
     for (int64_t i = 0; i < n; ++i) {
         if (agg[i] != -1 || sp[i + 1] == sp[i]) continue;
         agg[i] = (int32_t)nagg;
-        for (int64_t q = sp[i]; q < sp[i + 1]; ++q)
+        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1]; ++q)
             if (agg[sj[q]] == -1) agg[sj[q]] = (int32_t)nagg;
         ++nagg;
     }
     return nagg;
+}
+
+int64_t aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg) {
+    return aggregate_rows(n, sp.data(), sj.data(), agg, [](int64_t) { return true; });
 }
 
 // P = (I - omega D^-1 A) P0 with P0(i, agg(i)) = 1/sqrt(|agg|)
@@ -338,8 +349,9 @@ void smoothed_prolongator(const HostCsr& A, const std::vector<double>& d, const 
     });
 }
 
-// dense inverse of a symmetric positive definite matrix (Cholesky); false when not SPD
-bool spd_inverse(int64_t n, std::vector<double>& M) {
+// dense inverse of a symmetric positive definite matrix (Cholesky); false when not SPD. The columns of
+// the inverse are independent solves, split among the threads.
+bool spd_inverse(int64_t n, std::vector<double>& M, int nthreads) {
     std::vector<double> L(M);
     for (int64_t j = 0; j < n; ++j) {
         double s = L[j * n + j];
@@ -354,19 +366,23 @@ bool spd_inverse(int64_t n, std::vector<double>& M) {
         }
     }
     // columns of the inverse: solve L L^T x = e_c
-    std::vector<double> inv((size_t)n * n), y(n);
-    for (int64_t c = 0; c < n; ++c) {
-        for (int64_t i = 0; i < n; ++i) {
-            double t = i == c ? 1.0 : 0.0;
-            for (int64_t k = 0; k < i; ++k) t -= L[i * n + k] * y[k];
-            y[i] = t / L[i * n + i];
+    std::vector<double> inv((size_t)n * n);
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, n / 16));
+    parallel_rows(T, n * 4096, [&](int, int64_t c0, int64_t c1) {
+        std::vector<double> y(n);
+        for (int64_t c = (c0 + 4095) / 4096; c < (c1 + 4095) / 4096; ++c) {
+            for (int64_t i = 0; i < n; ++i) {
+                double t = i == c ? 1.0 : 0.0;
+                for (int64_t k = 0; k < i; ++k) t -= L[i * n + k] * y[k];
+                y[i] = t / L[i * n + i];
+            }
+            for (int64_t i = n - 1; i >= 0; --i) {
+                double t = y[i];
+                for (int64_t k = i + 1; k < n; ++k) t -= L[k * n + i] * inv[k * n + c];
+                inv[i * n + c] = t / L[i * n + i];
+            }
         }
-        for (int64_t i = n - 1; i >= 0; --i) {
-            double t = y[i];
-            for (int64_t k = i + 1; k < n; ++k) t -= L[k * n + i] * inv[k * n + c];
-            inv[i * n + c] = t / L[i * n + i];
-        }
-    }
+    });
     M.swap(inv);
     return true;
 }
@@ -416,8 +432,15 @@ double amg_tridiag_lmax(const std::vector<double>& al, const std::vector<double>
     return hi > 0 ? hi : 1.0;
 }
 
-int64_t amg_aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg) {
-    return aggregate(n, sp, sj, agg);
+int64_t amg_aggregate_streamed(int64_t n, const uint32_t* sp, const int32_t* sj, const std::atomic<int64_t>& rows_ready,
+                               const std::atomic<int>& failed, std::vector<int32_t>& agg) {
+    return aggregate_rows(n, sp, sj, agg, [&](int64_t r) {
+        while (rows_ready.load(std::memory_order_acquire) < r) {
+            if (failed.load(std::memory_order_acquire)) return false;
+            std::this_thread::yield();
+        }
+        return !failed.load(std::memory_order_acquire);
+    });
 }
 
 AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads) {
@@ -475,7 +498,7 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
         std::vector<double> M((size_t)n * n, 0.0);
         for (int64_t i = 0; i < n; ++i)
             for (int64_t p = C.A.ia[i]; p < C.A.ia[i + 1]; ++p) M[i * n + C.A.ja[p]] = C.A.a[p];
-        if (spd_inverse(n, M)) H.coarse_inv.swap(M);
+        if (spd_inverse(n, M, nthreads)) H.coarse_inv.swap(M);
     }
     return true;
 }

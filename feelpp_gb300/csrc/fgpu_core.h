@@ -1,5 +1,6 @@
 // Internal declarations of the GB300 assembly backend (not part of the C-ABI).
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <map>
 #include <memory>
@@ -115,7 +116,10 @@ constexpr int64_t kAmgDenseCoarse = 2048;   // largest coarsest level inverted d
 bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err);
 AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads);
 // pieces of the host set-up shared with the device set-up (amg_dev.cu)
-int64_t amg_aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg);
+// the host set-up's greedy aggregation over a graph copied in row order: rows [0, rows_ready) present;
+// returns -1 when `failed` is raised before all rows arrive
+int64_t amg_aggregate_streamed(int64_t n, const uint32_t* sp, const int32_t* sj, const std::atomic<int64_t>& rows_ready,
+                               const std::atomic<int>& failed, std::vector<int32_t>& agg);
 void amg_lanczos_start(int64_t n, std::vector<double>& v);
 double amg_tridiag_lmax(const std::vector<double>& al, const std::vector<double>& be);
 
@@ -139,10 +143,20 @@ struct AmgDevLevel {
     std::vector<int32_t> agg;
     double lmax = 0;
 };
+struct AmgSetupTimes {                // wall times of the set-up phases (ms), summed over the levels
+    double graph = 0;                // diagonal, strength graph and its copy to the host
+    double aggregate = 0;            // greedy aggregation (host)
+    double lanczos = 0;              // lambda_max estimate
+    double prolong = 0;              // P0, A P0, P, R = P^T
+    double galerkin = 0;             // A P and R (A P)
+    double tail = 0;                 // host set-up of the levels below the device ones
+    double layout = 0;               // level layouts (SELL-C-sigma, binary32 copies) and uploads
+    double total = 0;
+};
 struct AmgDevHierarchy {
     std::vector<AmgDevLevel> levels;
     AmgHierarchy tail;
-    double ms_total = 0, ms_aggregate = 0, ms_tail = 0;
+    AmgSetupTimes times;
 };
 int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* A, const AmgHostCfg& cfg, AmgDevHierarchy& H);
 int amg_copy_to_host(fgpu_ctx* ctx, const AmgDevCsr& D, HostCsr& H);

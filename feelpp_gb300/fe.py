@@ -868,11 +868,13 @@ class AMG:
         nnz = np.zeros(16, dtype=np.int64)
         ms = C.c_double()
         self.env.check(self.env.lib.fgpu_amg_info(self.h, C.byref(nl), _ptr(rows), _ptr(nnz), C.byref(ms)))
-        dl, agg_ms, tail_ms = C.c_int(), C.c_double(), C.c_double()
-        self.env.check(self.env.lib.fgpu_amg_setup_info(self.h, C.byref(dl), C.byref(agg_ms), C.byref(tail_ms)))
+        dl = C.c_int()
+        ph = np.zeros(8)
+        self.env.check(self.env.lib.fgpu_amg_setup_info(self.h, C.byref(dl), _ptr(ph)))
+        names = ("graph", "aggregate", "lanczos", "prolong", "galerkin", "host_levels", "layout", "total")
         return {"levels": nl.value, "rows": rows[:nl.value].tolist(), "nnz": nnz[:nl.value].tolist(),
-                "setup_ms": ms.value, "device_levels": dl.value, "setup_aggregate_ms": agg_ms.value,
-                "setup_host_tail_ms": tail_ms.value}
+                "setup_ms": ms.value, "device_levels": dl.value,
+                "setup_phases_ms": {k: round(float(x), 3) for k, x in zip(names, ph)}}
 
     def __del__(self):
         if getattr(self, "h", None):

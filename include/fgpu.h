@@ -339,9 +339,11 @@ int fgpu_amg_create(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg
 int fgpu_amg_update(fgpu_amg* amg);
 /* levels, rows[level], nnz[level] (arrays of at least 16 entries or NULL), set-up time in ms */
 int fgpu_amg_info(const fgpu_amg* amg, int* nlevels, int64_t* rows, int64_t* nnz, double* setup_ms);
-/* levels whose set-up ran on the device, and the host parts of the set-up time: the greedy aggregation
- * of the device levels and the host set-up of the levels below them (ms) */
-int fgpu_amg_setup_info(const fgpu_amg* amg, int* device_levels, double* aggregate_ms, double* host_tail_ms);
+/* levels whose set-up ran on the device, and the set-up's phases in ms (8 entries or NULL): strength
+ * graph, greedy aggregation (host), lambda_max, prolongator and restriction, Galerkin products, host
+ * set-up of the levels below the device ones (all levels with setup_on_host), level layouts and
+ * uploads, total */
+int fgpu_amg_setup_info(const fgpu_amg* amg, int* device_levels, double* phases_ms);
 int fgpu_amg_destroy(fgpu_amg* amg);
 int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
                       const fgpu_solver_cfg* cfg, fgpu_solve_stats* stats);
