@@ -1323,7 +1323,12 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 // 0.21 ms, 70 % of DRAM peak) and the others taken from a list sorted by count
 // (0.30 ms: the sorted list scatters the reads of the element buffer, 1.75 GB
 // of DRAM reads for 5.4 M entries). At P2 64^3 two entries per thread (k and
-// k + stride, loads issued together) took 0.90 ms against 0.655 ms.
+// k + stride, loads issued together) took 0.90 ms against 0.655 ms. A symmetric
+// map (entries j >= i only, each thread also storing its value at the transpose's
+// position) halves the map and the buffer reads on paper but took 0.785 ms
+// against 0.64 ms: at 48^3 its DRAM reads stayed at 888 MB (the transposes'
+// second reads of the buffer hit L2 here), with more warp instructions (half the
+// lanes idle) and scattered stores.
 template <int MODE, int B = 4>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
