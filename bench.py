@@ -1015,11 +1015,14 @@ def run_elasticity(args):
         x64, xmx = u.to_numpy(), u2.to_numpy()
         # double-double refinement: the rtol 1e-10 target below the binary64 residual floor
         refined = {}
-        for name, kw in (("jacobi", {}), ("mixed_fp32_inner", {"mixed": True}), ("gamg", {"pc": "gamg"})):
+        for name, kw in (("jacobi", {}), ("mixed_fp32_inner", {"mixed": True}), ("gamg", {"pc": "gamg"}),
+                         ("gamg_rigid_body", {"pc": "gamg", "gamg": {"near_null_space": "rigid"}})):
             w, wl = V.element(), V.element()
             try:
                 refined[name] = a.solve_refined(rhs=l, solution=w, solution_lo=wl, rtol=1e-10, **kw)
                 refined[name]["status"] = "ok"
+                if kw.get("pc") == "gamg":
+                    refined[name]["gamg"] = a.gamg(**kw.get("gamg", {})).info()
             except fpp.FgpuError as e:
                 refined[name] = {"status": str(e)}
             refined[name]["displacement_rel_diff_vs_fp64"] = float(np.linalg.norm(w.to_numpy() - x64) / np.linalg.norm(x64))

@@ -55,7 +55,8 @@ class SolverCfg(C.Structure):
 
 class AmgCfg(C.Structure):
     _fields_ = [("threshold", C.c_double), ("max_levels", C.c_int), ("coarse_eq_lim", C.c_int), ("agg_smooths", C.c_int),
-                ("smoother_degree", C.c_int), ("setup_on_host", C.c_int)]
+                ("smoother_degree", C.c_int), ("setup_on_host", C.c_int), ("block_size", C.c_int), ("nns_count", C.c_int),
+                ("nns", C.c_void_p), ("nns_host", C.c_void_p)]
 
 
 class PmgCfg(C.Structure):
@@ -138,6 +139,7 @@ SIGNATURES = {
     "fgpu_amg_host_destroy": (i32, [P]),
     "fgpu_amg_device_build": (i32, [P, P, C.POINTER(AmgCfg), PP]),
     "fgpu_amg_host_device_levels": (i32, [P]),
+    "fgpu_space_rigid_body_modes": (i32, [P, P]),
     "fgpu_norms_sine": (i32, [P, P, P, i32, DP, DP]),
     "fgpu_operator_create": (i32, [P, P, C.POINTER(FormDesc), i32, PP]),
     "fgpu_operator_set_dirichlet": (i32, [P, i64, P]),

@@ -68,7 +68,8 @@ struct fgpu_amg {
     int device_levels = 0;           // levels whose set-up ran on the device
     fgpu::AmgSetupTimes times;       // set-up phases (device set-up; the host set-up reports tail and layout)
     int launches_per_cycle = 0;
-    fgpu_amg_cfg cfg{};
+    fgpu_amg_cfg cfg{};              // (its vector pointers cleared: the near null space is kept below)
+    fgpu::AmgNns nns;                // near null space (m = 0: none)
     float* xacc = nullptr;           // repeated cycles (amg_vcycle_f32 with cycles > 1): accumulated solution
     float* tres = nullptr;           //                                                   and residual
 };
@@ -577,8 +578,9 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
     // levels 0 .. ndev-1 built on the device (D), the rest on the host (H)
     AmgDevHierarchy D;
     AmgHierarchy& H = D.tail;
+    const AmgNns* nns = M->nns.m > 0 ? &M->nns : nullptr;
     if (!cfg || !cfg->setup_on_host) {
-        const int rc = amg_build_device(ctx, A, hc, D);
+        const int rc = amg_build_device(ctx, A, hc, D, nns);
         if (rc) return rc;
     } else {
         HostCsr H0;
@@ -591,7 +593,7 @@ int amg_setup(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu
         FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.ja.data(), A->d_ja, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
         FGPU_CUDA_CHECK(ctx, cudaMemcpy(H0.a.data(), A->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
         std::string err;
-        if (!amg_build_host(std::move(H0), hc, H, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
+        if (!amg_build_host(std::move(H0), hc, H, err, nns)) { ctx->err = err; return FGPU_ERR_INVALID; }
     }
     const auto t_layout = std::chrono::steady_clock::now();
     const int ndev = (int)D.levels.size();
@@ -690,7 +692,15 @@ extern "C" int fgpu_amg_create(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_a
     M->ctx = ctx;
     M->A = A;
     if (cfg) M->cfg = *cfg;
-    const int rc = amg_setup(ctx, A, &M->cfg, M);
+    bool has_nns = false;
+    int rc = amg_nns_from_cfg(ctx, cfg, A->nrows, M->nns, &has_nns);
+    if (rc) {
+        delete M;
+        return rc;
+    }
+    M->cfg.nns = nullptr;
+    M->cfg.nns_host = nullptr;
+    rc = amg_setup(ctx, A, &M->cfg, M);
     if (rc) {
         for (auto& V : M->L) free_level(V);
         cudaFree(M->coarse_inv);
@@ -727,8 +737,8 @@ extern "C" int fgpu_amg_setup_info(const fgpu_amg* M, int* device_levels, double
     if (device_levels) *device_levels = M->device_levels;
     if (phases_ms) {
         const AmgSetupTimes& t = M->times;
-        const double v[8] = {t.graph, t.aggregate, t.lanczos, t.prolong, t.galerkin, t.tail, t.layout, t.total};
-        for (int k = 0; k < 8; ++k) phases_ms[k] = v[k];
+        const double v[9] = {t.graph, t.aggregate, t.lanczos, t.prolong, t.galerkin, t.tail, t.layout, t.total, (double)t.handoff};
+        for (int k = 0; k < 9; ++k) phases_ms[k] = v[k];
     }
     return FGPU_OK;
 }

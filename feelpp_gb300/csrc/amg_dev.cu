@@ -56,11 +56,10 @@ constexpr int kStDiag = 2;                   // a non-positive diagonal entry
 constexpr int64_t kLanczosChunk = 16384;     // rows per partial sum (the host set-up's partition)
 constexpr int kLanczosSteps = 12;
 constexpr int64_t kHandoffRows = 16384;      // levels this small continue on the host
-constexpr int kSortMax = 2048;               // longest row sorted by seg_sort_kernel
-constexpr int kSortWarps = 4;
-constexpr int kMaxLeft = 4096;               // longest left-factor row of a sparse product
-constexpr int kBins[3] = {256, 2048, 8192};  // hash table sizes (at most half full)
-constexpr int kBinLog[3] = {8, 11, 13};
+constexpr int kSortMax = 16384;              // longest row sorted by seg_sort_kernel
+constexpr int kMaxLeft = 8192;               // longest left-factor row of a sparse product
+constexpr int kBins[3] = {256, 1024, 8192};  // hash table sizes (at most half full)
+constexpr int kBinLog[3] = {8, 10, 13};
 
 int grid_rows(int64_t n, int per_block, int cap = 152 * 16) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + per_block - 1) / per_block, cap));
@@ -164,19 +163,20 @@ __global__ void transpose_fill_kernel(int64_t n, const uint32_t* __restrict__ of
     }
 }
 
-// each row's keys (and values) sorted by key: one warp per row, bitonic sort in shared memory
-__global__ void __launch_bounds__(kSortWarps * 32) seg_sort_kernel(int64_t n, const uint32_t* __restrict__ off32,
-                                                                  const int64_t* __restrict__ off64, int32_t* __restrict__ key,
-                                                                  double* __restrict__ val, int* __restrict__ status) {
+// each row's keys (and values) sorted by key: one warp per row, bitonic sort in shared memory (cap
+// entries per warp)
+__global__ void __launch_bounds__(128) seg_sort_kernel(int64_t n, const uint32_t* __restrict__ off32, const int64_t* __restrict__ off64,
+                                                       int cap, int32_t* __restrict__ key, double* __restrict__ val,
+                                                       int* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char ss_smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* sv = reinterpret_cast<double*>(ss_smem) + warp * kSortMax;
-    int32_t* sk = reinterpret_cast<int32_t*>(ss_smem + (val ? kSortWarps * kSortMax * 8 : 0)) + warp * kSortMax;
-    for (int64_t r = (int64_t)blockIdx.x * kSortWarps + warp; r < n; r += (int64_t)gridDim.x * kSortWarps) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    double* sv = reinterpret_cast<double*>(ss_smem) + (size_t)warp * cap;
+    int32_t* sk = reinterpret_cast<int32_t*>(ss_smem + (val ? (size_t)warps * cap * 8 : 0)) + (size_t)warp * cap;
+    for (int64_t r = (int64_t)blockIdx.x * warps + warp; r < n; r += (int64_t)gridDim.x * warps) {
         const int64_t b = off64 ? off64[r] : off32[r], e = off64 ? off64[r + 1] : off32[r + 1];
         const int len = (int)(e - b);
         if (len <= 1) continue;
-        if (len > kSortMax) {
+        if (len > cap) {
             if (lane == 0) atomicOr(status, kStOverflow);
             continue;
         }
@@ -213,6 +213,16 @@ __global__ void __launch_bounds__(kSortWarps * 32) seg_sort_kernel(int64_t n, co
         }
         __syncwarp();
     }
+}
+
+// longest row of a CSR offset array (32- or 64-bit)
+__global__ void max_row_kernel(int64_t n, const uint32_t* __restrict__ off32, const int64_t* __restrict__ off64,
+                               unsigned long long* __restrict__ out) {
+    unsigned long long m = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, (unsigned long long)(off64 ? off64[r + 1] - off64[r] : off32[r + 1] - off32[r]));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 // union of two sorted rows (count when out == nullptr)
@@ -346,6 +356,111 @@ __global__ void row_stats_kernel(int64_t n, const int64_t* __restrict__ ia, cons
     if ((threadIdx.x & 31) == 0) {
         atomicMax(out, mlen);
         atomicMax(out + 1, mprod);
+    }
+}
+
+// node of each dof (near null space levels: nodes are consecutive dof ranges)
+__global__ void node_of_kernel(int64_t nn, const int64_t* __restrict__ node_ptr, int32_t* __restrict__ node_of) {
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nn; I += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t i = node_ptr[I]; i < node_ptr[I + 1]; ++i) node_of[i] = (int32_t)I;
+}
+
+// node graph of the dof graph (sp, sj): one warp per node, the nodes of its dofs' neighbours gathered in
+// shared memory (cap entries per warp), sorted (bitonic), duplicates and the node itself removed; count
+// (out == nullptr) or fill
+constexpr int kCollapseMax = 16384;
+__global__ void __launch_bounds__(128) collapse_kernel(int64_t nn, const int64_t* __restrict__ node_ptr, const uint32_t* __restrict__ sp,
+                                                       const int32_t* __restrict__ sj, const int32_t* __restrict__ node_of, int cap,
+                                                       uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
+                                                       int32_t* __restrict__ out, int* __restrict__ status) {
+    extern __shared__ __align__(16) int32_t cbuf[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    int32_t* b = cbuf + (size_t)warp * cap;
+    for (int64_t I = (int64_t)blockIdx.x * warps + warp; I < nn; I += (int64_t)gridDim.x * warps) {
+        const uint32_t q0 = sp[node_ptr[I]], q1 = sp[node_ptr[I + 1]];
+        const int len = (int)(q1 - q0);
+        if (len > cap) {
+            if (lane == 0) {
+                atomicOr(status, kStOverflow);
+                if (cnt) cnt[I] = 0;
+            }
+            continue;
+        }
+        int P = 1;
+        while (P < len) P <<= 1;
+        for (int k = lane; k < P; k += 32) {
+            const int32_t J = k < len ? node_of[sj[q0 + k]] : INT32_MAX;
+            b[k] = (J == (int32_t)I) ? INT32_MAX : J;
+        }
+        __syncwarp();
+        for (int size = 2; size <= P; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int k = lane; k < P; k += 32) {
+                    const int l = k ^ stride;
+                    if (l > k) {
+                        const bool up = (k & size) == 0;
+                        const int32_t x = b[k], y = b[l];
+                        if ((x > y) == up) { b[k] = y; b[l] = x; }
+                    }
+                }
+                __syncwarp();
+            }
+        // distinct values: a position k counts when b[k] is real and differs from b[k - 1]
+        uint32_t run = 0;
+        for (int k0 = 0; k0 < P; k0 += 32) {
+            const int k = k0 + lane;
+            const bool keep = k < P && b[k] != INT32_MAX && (k == 0 || b[k] != b[k - 1]);
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep && out) out[off[I] + run + __popc(m & ((1u << lane) - 1u))] = b[k];
+            run += __popc(m);
+        }
+        if (cnt && lane == 0) cnt[I] = run;
+        __syncwarp();
+    }
+}
+
+// longest gathered list of collapse_kernel: max over nodes of the node's dof rows' total length
+__global__ void node_len_kernel(int64_t nn, const int64_t* __restrict__ node_ptr, const uint32_t* __restrict__ sp,
+                                unsigned long long* __restrict__ out) {
+    unsigned long long m = 0;
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nn; I += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, (unsigned long long)(sp[node_ptr[I + 1]] - sp[node_ptr[I]]));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// rigid body modes at the dof nodes: node coordinates from the first incident element's affine map
+// (barycentric weights of the local node), then the six modes about the centroid c
+__global__ void node_coords_kernel(int64_t nnodes, int n, const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                   const int32_t* __restrict__ tets, const double* __restrict__ xyz, const double* __restrict__ lam,
+                                   double* __restrict__ out) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        double x[3] = {0.0, 0.0, 0.0};
+        if (inc_ptr[m + 1] > inc_ptr[m]) {
+            const int32_t code = inc[inc_ptr[m]];
+            const int64_t e = code >> 5;
+            const int a = code & 31;
+            for (int v = 0; v < 4; ++v) {
+                const double w = lam[a * 4 + v];
+                const int64_t g = tets[e * 4 + v];
+                for (int d = 0; d < 3; ++d) x[d] = fma(w, xyz[g * 3 + d], x[d]);
+            }
+        }
+        for (int d = 0; d < 3; ++d) out[m * 3 + d] = x[d];
+    }
+}
+__global__ void rbm_kernel(int64_t nnodes, const double* __restrict__ xn, double cx, double cy, double cz, double* __restrict__ m0,
+                           double* __restrict__ m1, double* __restrict__ m2, double* __restrict__ m3, double* __restrict__ m4,
+                           double* __restrict__ m5) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nnodes; m += (int64_t)gridDim.x * blockDim.x) {
+        const double x = xn[m * 3] - cx, y = xn[m * 3 + 1] - cy, z = xn[m * 3 + 2] - cz;
+        const int64_t r = m * 3;
+        m0[r] = 1.0; m0[r + 1] = 0.0; m0[r + 2] = 0.0;
+        m1[r] = 0.0; m1[r + 1] = 1.0; m1[r + 2] = 0.0;
+        m2[r] = 0.0; m2[r + 1] = 0.0; m2[r + 2] = 1.0;
+        m3[r] = -y; m3[r + 1] = x; m3[r + 2] = 0.0;
+        m4[r] = 0.0; m4[r + 1] = -z; m4[r + 2] = y;
+        m5[r] = z; m5[r + 1] = 0.0; m5[r + 2] = -x;
     }
 }
 
@@ -620,9 +735,24 @@ int spgemm_dev(fgpu_ctx* ctx, const AmgDevCsr& A, const AmgDevCsr& B, AmgDevCsr&
 }
 
 int seg_sort(fgpu_ctx* ctx, int64_t n, const uint32_t* off32, const int64_t* off64, int32_t* key, double* val, int* d_status) {
-    const int smem = kSortWarps * kSortMax * (val ? 12 : 4);
+    unsigned long long* dmax = nullptr;
+    DEV_TRY(cudaMalloc(&dmax, sizeof(unsigned long long)));
+    struct Free { unsigned long long* p; ~Free() { cudaFree(p); } } fr{dmax};
+    DEV_TRY(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), ctx->stream));
+    max_row_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, off32, off64, dmax);
+    unsigned long long hmax = 0;
+    DEV_TRY(cudaMemcpyAsync(&hmax, dmax, sizeof(hmax), cudaMemcpyDeviceToHost, ctx->stream));
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->launches++;
+    if (hmax <= 1) return FGPU_OK;
+    int cap = 32;
+    while (cap < (int)std::min<unsigned long long>(hmax, (unsigned long long)kSortMax + 1)) cap <<= 1;
+    cap = std::min(cap, kSortMax);              // longer rows raise the overflow status
+    const int bytes = val ? 12 : 4;
+    const int warps = std::max(1, std::min(4, (96 * 1024) / (cap * bytes)));
+    const int smem = warps * cap * bytes;
     DEV_TRY(cudaFuncSetAttribute(seg_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    seg_sort_kernel<<<grid_rows(n, kSortWarps, 152 * 4), kSortWarps * 32, smem, ctx->stream>>>(n, off32, off64, key, val, d_status);
+    seg_sort_kernel<<<grid_rows(n, warps, 152 * 8), warps * 32, smem, ctx->stream>>>(n, off32, off64, cap, key, val, d_status);
     ctx->launches++;
     DEV_TRY(cudaGetLastError());
     return FGPU_OK;
@@ -717,8 +847,8 @@ struct LanczosJob {
 // One level on the device: lambda_max, strength graph, aggregation (host), P, R, A_c = R (A P).
 // *handoff: the level goes to the host set-up instead (a row beyond a kernel's capacity, or nothing
 // to coarsen); *last: the coarsening stagnates and A_c is the coarsest operator.
-int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_status, AmgDevCsr& Ac, bool* handoff, bool* last,
-              AmgSetupTimes& tm) {
+int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, const AmgNns* nns, AmgNns* next, int* d_status, AmgDevCsr& Ac,
+              bool* handoff, bool* last, AmgSetupTimes& tm) {
     using clock = std::chrono::steady_clock;
     auto ms_since = [](clock::time_point t) { return std::chrono::duration<double, std::milli>(clock::now() - t).count(); };
     auto tphase = clock::now();
@@ -795,15 +925,55 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     DEV_ALLOC(sj);
     merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, tp, tmpj, tc, tj, nullptr, sp32, sj);
     ctx->launches++;
-    std::vector<uint32_t> hsp32(n + 1);
-    DEV_TRY(cudaMemcpyAsync(hsp32.data(), sp32, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    // the graph to aggregate: the dof graph, or (near null space) its node graph
+    int64_t ng = n;
+    const uint32_t* gp32 = sp32;
+    const int32_t* gj = sj;
+    uint64_t ngj = nsg;
+    if (nns) {
+        ng = (int64_t)nns->node_ptr.size() - 1;
+        int64_t* dnp = w.get<int64_t>(ng + 1);
+        int32_t* node_of = w.get<int32_t>(n);
+        uint32_t* ncnt = w.get<uint32_t>(ng + 1);
+        uint32_t* np32 = w.get<uint32_t>(ng + 1);
+        DEV_ALLOC(dnp && node_of && ncnt && np32);
+        unsigned long long* dmax = w.get<unsigned long long>(1);
+        DEV_ALLOC(dmax);
+        DEV_TRY(cudaMemcpyAsync(dnp, nns->node_ptr.data(), (ng + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        DEV_TRY(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), ctx->stream));
+        node_of_kernel<<<grid_rows(ng, 256), 256, 0, ctx->stream>>>(ng, dnp, node_of);
+        node_len_kernel<<<grid_rows(ng, 256), 256, 0, ctx->stream>>>(ng, dnp, sp32, dmax);
+        unsigned long long hmax = 0;
+        DEV_TRY(cudaMemcpyAsync(&hmax, dmax, sizeof(hmax), cudaMemcpyDeviceToHost, ctx->stream));
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));
+        if (hmax > (unsigned long long)kCollapseMax) { *handoff = true; tm.handoff = 2; return FGPU_OK; }
+        int cap = 32;
+        while (cap < (int)hmax) cap <<= 1;
+        const int cwarps = std::max(1, std::min(4, (96 * 1024) / (cap * 4)));
+        const int csmem = cwarps * cap * 4;
+        DEV_TRY(cudaFuncSetAttribute(collapse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, csmem));
+        collapse_kernel<<<grid_rows(ng, cwarps, 152 * 8), cwarps * 32, csmem, ctx->stream>>>(ng, dnp, sp32, sj, node_of, cap, ncnt, nullptr,
+                                                                                            nullptr, d_status);
+        ctx->launches += 3;
+        rc = scan_u32(ctx, ncnt, np32, ng, &ngj);
+        if (rc) return rc;
+        int32_t* nj = w.get<int32_t>((int64_t)ngj);
+        DEV_ALLOC(nj);
+        collapse_kernel<<<grid_rows(ng, cwarps, 152 * 8), cwarps * 32, csmem, ctx->stream>>>(ng, dnp, sp32, sj, node_of, cap, nullptr, np32,
+                                                                                            nj, d_status);
+        ctx->launches++;
+        gp32 = np32;
+        gj = nj;
+    }
+    std::vector<uint32_t> hsp32(ng + 1);
+    DEV_TRY(cudaMemcpyAsync(hsp32.data(), gp32, (ng + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     rc = read_status(ctx, d_status, &st);
     if (rc) return rc;
-    if (st & kStOverflow) { *handoff = true; return FGPU_OK; }
+    if (st & kStOverflow) { *handoff = true; tm.handoff = nns ? 2 : 1; return FGPU_OK; }
     tm.graph += ms_since(tphase);
     tphase = clock::now();
     // greedy aggregation on the host; its first pass follows the graph's copy in chunks of rows
-    std::unique_ptr<int32_t[]> hsj(new int32_t[std::max<uint64_t>(nsg, 1)]);
+    std::unique_ptr<int32_t[]> hsj(new int32_t[std::max<uint64_t>(ngj, 1)]);
     std::atomic<int64_t> rows_ready{0};
     std::atomic<int> copy_failed{0};
     cudaError_t copy_err = cudaSuccess;
@@ -811,14 +981,14 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
         cudaSetDevice(ctx->device);
         constexpr uint32_t kChunk = 1u << 22;            // entries per copy
         int64_t r = 0;
-        while (r < n) {
+        while (r < ng) {
             const uint64_t target = (uint64_t)hsp32[r] + kChunk;
             int64_t r1 = std::upper_bound(hsp32.begin() + r + 1, hsp32.end(), target,
                                           [](uint64_t t, uint32_t x) { return t < (uint64_t)x; }) - hsp32.begin() - 1;
-            r1 = std::min<int64_t>(n, std::max<int64_t>(r1, r + 1));
+            r1 = std::min<int64_t>(ng, std::max<int64_t>(r1, r + 1));
             const uint32_t b = hsp32[r], e = hsp32[r1];
             if (e > b) {
-                copy_err = cudaMemcpyAsync(hsj.get() + b, sj + b, (size_t)(e - b) * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+                copy_err = cudaMemcpyAsync(hsj.get() + b, gj + b, (size_t)(e - b) * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
                 if (copy_err == cudaSuccess) copy_err = cudaStreamSynchronize(ctx->stream);
                 if (copy_err != cudaSuccess) { copy_failed.store(1, std::memory_order_release); return; }
             }
@@ -826,7 +996,8 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
             r = r1;
         }
     });
-    const int64_t nagg = amg_aggregate_streamed(n, hsp32.data(), hsj.get(), rows_ready, copy_failed, L.agg);
+    std::vector<int32_t> agg_node;
+    const int64_t nagg = amg_aggregate_streamed(ng, hsp32.data(), hsj.get(), rows_ready, copy_failed, nns ? agg_node : L.agg);
     copier.join();
     if (copy_err != cudaSuccess || nagg < 0) {
         ctx->err = std::string("gamg device set-up: graph copy: ") + cudaGetErrorString(copy_err);
@@ -834,7 +1005,30 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     }
     tm.aggregate += ms_since(tphase);
     tphase = clock::now();
-    if (nagg == 0 || nagg >= n) { *handoff = true; return FGPU_OK; }
+    if (nagg == 0 || nagg >= ng) { *handoff = true; tm.handoff = 3; return FGPU_OK; }
+    AmgDevCsr P0;
+    int64_t ncoarse = nagg;
+    if (nns) {
+        // tentative prolongator from the near null space (host QR per aggregate, the host set-up's code)
+        HostCsr hP0;
+        if (amg_tentative_nns(*nns, agg_node, nagg, cfg.nthreads > 0 ? cfg.nthreads : 1, hP0, *next)) {
+            ctx->err = "gamg: coarse level too large";
+            return FGPU_ERR_INVALID;
+        }
+        if (hP0.ncols == 0 || hP0.ncols >= n) { *handoff = true; tm.handoff = 3; return FGPU_OK; }
+        ncoarse = hP0.ncols;
+        L.agg.assign(n, -1);
+        for (int64_t I = 0; I < ng; ++I)
+            for (int64_t i = nns->node_ptr[I]; i < nns->node_ptr[I + 1]; ++i) L.agg[i] = agg_node[I];
+        rc = alloc_csr(ctx, P0, n, hP0.ncols, (int64_t)hP0.ja.size());
+        if (rc) return rc;
+        DEV_TRY(cudaMemcpyAsync(P0.ia, hP0.ia.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        if (!hP0.ja.empty()) {
+            DEV_TRY(cudaMemcpyAsync(P0.ja, hP0.ja.data(), hP0.ja.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+            DEV_TRY(cudaMemcpyAsync(P0.a, hP0.a.data(), hP0.a.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));            // hP0 is freed on leaving this block
+    } else {
     // tentative prolongator and A P0
     std::vector<double> sz(nagg, 0.0), hs0(nagg);
     for (int64_t i = 0; i < n; ++i)
@@ -850,11 +1044,11 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     uint64_t n0 = 0;
     rc = scan_u32(ctx, cnt, tp, n, &n0);
     if (rc) return rc;
-    AmgDevCsr P0;
     rc = alloc_csr(ctx, P0, n, nagg, (int64_t)n0);
     if (rc) return rc;
     p0_fill_kernel<<<grid_rows(n + 1, 256), 256, 0, ctx->stream>>>(n, dagg, ds0, tp, P0.ia, P0.ja, P0.a);
     ctx->launches++;
+    }
     bool ovf = false;
     // lambda_max: wait for the Lanczos thread (A P0 does not need it)
     auto join_lanczos = [&]() -> int {
@@ -875,7 +1069,7 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
         AmgDevCsr AP0;
         rc = spgemm_dev(ctx, A, P0, AP0, d_status, &ovf);
         if (rc) return rc;
-        if (ovf) { *handoff = true; return FGPU_OK; }
+        if (ovf) { *handoff = true; tm.handoff = 4; return FGPU_OK; }
         rc = join_lanczos();
         if (rc) return rc;
         const double omega = 4.0 / (3.0 * L.lmax);
@@ -885,7 +1079,7 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
         uint64_t pn = 0;
         rc = scan_u32(ctx, cnt, tp, n, &pn);
         if (rc) return rc;
-        rc = alloc_csr(ctx, L.P, n, nagg, (int64_t)pn);
+        rc = alloc_csr(ctx, L.P, n, ncoarse, (int64_t)pn);
         if (rc) return rc;
         prolong_merge_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, P0.ia, P0.ja, P0.a, AP0.ia, AP0.ja, AP0.a, d, omega, nullptr,
                                                                         tp, L.P.ja, L.P.a);
@@ -897,20 +1091,20 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, int* d_statu
     if (rc) return rc;
     rc = read_status(ctx, d_status, &st);
     if (rc) return rc;
-    if (st & kStOverflow) { *handoff = true; return FGPU_OK; }
+    if (st & kStOverflow) { *handoff = true; tm.handoff = 5; return FGPU_OK; }
     tm.prolong += ms_since(tphase);
     tphase = clock::now();
     // Galerkin product A_c = R (A P)
     AmgDevCsr AP;
     rc = spgemm_dev(ctx, A, L.P, AP, d_status, &ovf);
     if (rc) return rc;
-    if (ovf) { *handoff = true; return FGPU_OK; }
+    if (ovf) { *handoff = true; tm.handoff = 6; return FGPU_OK; }
     rc = spgemm_dev(ctx, L.R, AP, Ac, d_status, &ovf);
     if (rc) return rc;
-    if (ovf) { *handoff = true; return FGPU_OK; }
+    if (ovf) { *handoff = true; tm.handoff = 7; return FGPU_OK; }
     DEV_TRY(cudaStreamSynchronize(ctx->stream));             // the scratch of this level is freed on return
     tm.galerkin += ms_since(tphase);
-    if ((double)nagg > 0.9 * (double)n) *last = true;
+    if ((double)ncoarse > 0.9 * (double)n) *last = true;
     return FGPU_OK;
 }
 
@@ -932,7 +1126,7 @@ int amg_copy_to_host(fgpu_ctx* ctx, const AmgDevCsr& D, HostCsr& H) {
     return FGPU_OK;
 }
 
-int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg, AmgDevHierarchy& H) {
+int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg, AmgDevHierarchy& H, const AmgNns* nns) {
     const auto t0 = std::chrono::steady_clock::now();
     const int max_levels = cfg.max_levels > 0 ? cfg.max_levels : 10;
     const int64_t coarse_lim = cfg.coarse_eq_lim > 0 ? cfg.coarse_eq_lim : 800;
@@ -956,14 +1150,17 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
         A0.a = static_cast<double*>(Am->d_val);
     }
     H.times = AmgSetupTimes();
+    AmgNns cur;
+    if (nns) cur = *nns;
     bool last = false;
     int l = 0;
     for (; l + 1 < max_levels && !last; ++l) {
         AmgDevLevel& L = H.levels[l];
         if (L.A.nrows <= coarse_lim || L.A.nrows <= kHandoffRows || L.A.nnz >= ((int64_t)1 << 32)) break;
         AmgDevCsr Ac;
+        AmgNns next;
         bool handoff = false;
-        const int rc = level_dev(ctx, L, cfg, d_status, Ac, &handoff, &last, H.times);
+        const int rc = level_dev(ctx, L, cfg, nns ? &cur : nullptr, &next, d_status, Ac, &handoff, &last, H.times);
         if (rc) return rc;
         if (handoff) {
             DEV_TRY(cudaStreamSynchronize(ctx->stream));
@@ -977,6 +1174,7 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
         }
         H.levels.emplace_back();
         H.levels.back().A = std::move(Ac);
+        if (nns) cur = std::move(next);
     }
     // the rest on the host, from level l (its operator copied)
     const auto t1 = std::chrono::steady_clock::now();
@@ -986,7 +1184,7 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
     AmgHostCfg tc = cfg;
     tc.max_levels = last ? 1 : max_levels - l;
     std::string err;
-    if (!amg_build_host(std::move(Al), tc, H.tail, err)) { ctx->err = err; return FGPU_ERR_INVALID; }
+    if (!amg_build_host(std::move(Al), tc, H.tail, err, nns ? &cur : nullptr)) { ctx->err = err; return FGPU_ERR_INVALID; }
     H.levels.resize(l);
     const auto t2 = std::chrono::steady_clock::now();
     H.times.total = std::chrono::duration<double, std::milli>(t2 - t0).count();
@@ -995,6 +1193,68 @@ int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* Am, const AmgHostCfg& cfg
 }
 
 }  // namespace fgpu
+
+namespace fgpu {
+
+int amg_nns_from_cfg(fgpu_ctx* ctx, const fgpu_amg_cfg* cfg, int64_t n, AmgNns& nns, bool* has) {
+    *has = false;
+    if (!cfg || cfg->nns_count <= 0) return FGPU_OK;
+    if (!cfg->nns || amg_nns_layout(cfg, n, nns)) { ctx->err = "gamg: invalid near null space (count, block size or vectors)"; return FGPU_ERR_INVALID; }
+    std::vector<double> col(n);
+    for (int j = 0; j < nns.m; ++j) {
+        const fgpu_vector* v = cfg->nns[j];
+        if (!v || v->n != n) { ctx->err = "gamg: a near null space vector does not match the matrix"; return FGPU_ERR_INVALID; }
+        DEV_TRY(cudaMemcpyAsync(col.data(), v->d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));
+        for (int64_t i = 0; i < n; ++i) nns.B[(size_t)i * nns.m + j] = col[i];
+    }
+    *has = true;
+    return FGPU_OK;
+}
+
+}  // namespace fgpu
+
+extern "C" int fgpu_space_rigid_body_modes(const fgpu_space* V, fgpu_vector* const* out) {
+    using namespace fgpu;
+    if (!V || !out) return FGPU_ERR_INVALID;
+    fgpu_ctx* ctx = V->ctx;
+    if (V->ncomp != 3 || V->mesh->cv != 4) { ctx->err = "rigid body modes: Pchv spaces on tetrahedral meshes only"; return FGPU_ERR_INVALID; }
+    const int64_t nn = V->ndof / 3;
+    for (int k = 0; k < 6; ++k)
+        if (!out[k] || out[k]->n != V->ndof) { ctx->err = "rigid body modes: six vectors of the space's size"; return FGPU_ERR_INVALID; }
+    std::vector<double> ref;
+    if (!lagrange_nodes(V->order, ref) || (int)ref.size() != 3 * V->n) { ctx->err = "rigid body modes: orders 1-3"; return FGPU_ERR_INVALID; }
+    std::vector<double> lam((size_t)V->n * 4);
+    for (int a = 0; a < V->n; ++a) {                // barycentrics of the reference nodes ([-1, 1] reference tetrahedron)
+        const double l1 = 0.5 * (1.0 + ref[a * 3]), l2 = 0.5 * (1.0 + ref[a * 3 + 1]), l3 = 0.5 * (1.0 + ref[a * 3 + 2]);
+        lam[a * 4] = 1.0 - l1 - l2 - l3;
+        lam[a * 4 + 1] = l1;
+        lam[a * 4 + 2] = l2;
+        lam[a * 4 + 3] = l3;
+    }
+    fgpu_mesh* M = V->mesh;
+    if (M->h_xyz_stale) {
+        DEV_TRY(cudaMemcpyAsync(M->h_xyz.data(), M->d_xyz, M->h_xyz.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));
+        M->h_xyz_stale = false;
+    }
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int64_t v = 0; v < M->nv; ++v)
+        for (int d = 0; d < 3; ++d) c[d] += M->h_xyz[v * 3 + d];
+    for (int d = 0; d < 3; ++d) c[d] /= (double)std::max<int64_t>(M->nv, 1);
+    double *dlam = nullptr, *xn = nullptr;
+    DEV_TRY(cudaMalloc(&dlam, lam.size() * sizeof(double)));
+    struct Free { double*& a; double*& b; ~Free() { cudaFree(a); cudaFree(b); } } fr{dlam, xn};
+    DEV_TRY(cudaMalloc(&xn, std::max<int64_t>(nn, 1) * 3 * sizeof(double)));
+    DEV_TRY(cudaMemcpyAsync(dlam, lam.data(), lam.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    node_coords_kernel<<<grid_rows(nn, 256), 256, 0, ctx->stream>>>(nn, V->n, V->d_inc_ptr, V->d_inc, M->d_tets, M->d_xyz, dlam, xn);
+    rbm_kernel<<<grid_rows(nn, 256), 256, 0, ctx->stream>>>(nn, xn, c[0], c[1], c[2], out[0]->d, out[1]->d, out[2]->d, out[3]->d,
+                                                           out[4]->d, out[5]->d);
+    ctx->launches += 2;
+    DEV_TRY(cudaGetLastError());
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));
+    return FGPU_OK;
+}
 
 // ---------------------------------------------------------------------------------------------------
 // The device-built hierarchy copied into the host set-up's inspection object (fgpu_amg_host_*), so
@@ -1007,8 +1267,12 @@ extern "C" int fgpu_amg_device_build(fgpu_ctx* ctx, const fgpu_matrix* A, const 
     if (A->precision != FGPU_F64) { ctx->err = "gamg: FP64 matrices only"; return FGPU_ERR_INVALID; }
     if (ctx->capturing) { ctx->err = "gamg: set-up is not capturable"; return FGPU_ERR_INVALID; }
     const AmgHostCfg hc = amg_host_cfg(cfg, ctx->host_threads);
+    AmgNns nns;
+    bool has_nns = false;
+    int rc = amg_nns_from_cfg(ctx, cfg, A->nrows, nns, &has_nns);
+    if (rc) return rc;
     AmgDevHierarchy D;
-    int rc = amg_build_device(ctx, A, hc, D);
+    rc = amg_build_device(ctx, A, hc, D, has_nns ? &nns : nullptr);
     if (rc) return rc;
     fgpu_amg_host* h = new fgpu_amg_host();
     for (auto& dl : D.levels) {

@@ -293,32 +293,35 @@ int64_t aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<i
     return aggregate_rows(n, sp.data(), sj.data(), agg, [](int64_t) { return true; });
 }
 
-// P = (I - omega D^-1 A) P0 with P0(i, agg(i)) = 1/sqrt(|agg|)
-void smoothed_prolongator(const HostCsr& A, const std::vector<double>& d, const std::vector<int32_t>& agg, int64_t nagg, double omega,
-                          int nsmooth, HostCsr& P, int nthreads) {
+// P0(i, agg(i)) = 1/sqrt(|agg|): the constant near null space
+void tentative_constant(int64_t n, const std::vector<int32_t>& agg, int64_t nagg, HostCsr& P0) {
     std::vector<double> sz(nagg, 0.0);
-    for (int64_t i = 0; i < A.nrows; ++i)
+    for (int64_t i = 0; i < n; ++i)
         if (agg[i] >= 0) sz[agg[i]] += 1.0;
     std::vector<double> s0(nagg);
     for (int64_t c = 0; c < nagg; ++c) s0[c] = 1.0 / std::sqrt(sz[c]);
-    HostCsr P0;
-    P0.nrows = A.nrows;
+    P0.nrows = n;
     P0.ncols = nagg;
-    P0.ia.assign(A.nrows + 1, 0);
-    for (int64_t i = 0; i < A.nrows; ++i) P0.ia[i + 1] = P0.ia[i] + (agg[i] >= 0 ? 1 : 0);
-    P0.ja.resize(P0.ia[A.nrows]);
-    P0.a.resize(P0.ia[A.nrows]);
-    for (int64_t i = 0; i < A.nrows; ++i)
+    P0.ia.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) P0.ia[i + 1] = P0.ia[i] + (agg[i] >= 0 ? 1 : 0);
+    P0.ja.resize(P0.ia[n]);
+    P0.a.resize(P0.ia[n]);
+    for (int64_t i = 0; i < n; ++i)
         if (agg[i] >= 0) {
             P0.ja[P0.ia[i]] = agg[i];
             P0.a[P0.ia[i]] = s0[agg[i]];
         }
+}
+
+// P = (I - omega D^-1 A) P0 (nsmooth > 0) or P0
+void smooth_prolongator(const HostCsr& A, const std::vector<double>& d, HostCsr&& P0, double omega, int nsmooth, HostCsr& P,
+                        int nthreads) {
     if (nsmooth <= 0) { P = std::move(P0); return; }
     HostCsr AP;
     spgemm(A, P0, AP, nthreads);
     // P = P0 - omega D^-1 (A P0): merge the sorted rows (count, offsets, fill; rows in parallel)
     P.nrows = A.nrows;
-    P.ncols = nagg;
+    P.ncols = P0.ncols;
     P.ia.assign(A.nrows + 1, 0);
     auto merge_row = [&](int64_t i, int32_t* oj, double* oa) {
         const double f = d[i] != 0.0 ? omega / d[i] : 0.0;
@@ -443,6 +446,17 @@ int64_t amg_aggregate_streamed(int64_t n, const uint32_t* sp, const int32_t* sj,
     });
 }
 
+// node layout and storage of a near null space (values filled by the caller); nonzero when invalid
+int amg_nns_layout(const fgpu_amg_cfg* cfg, int64_t n, AmgNns& nns) {
+    const int bs = cfg->block_size > 0 ? cfg->block_size : 1;
+    if (cfg->nns_count <= 0 || cfg->nns_count > 64 || n % bs != 0) return FGPU_ERR_INVALID;
+    nns.m = cfg->nns_count;
+    nns.node_ptr.resize(n / bs + 1);
+    for (int64_t I = 0; I <= n / bs; ++I) nns.node_ptr[I] = I * bs;
+    nns.B.assign((size_t)n * nns.m, 0.0);
+    return FGPU_OK;
+}
+
 AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads) {
     AmgHostCfg hc;
     if (cfg) {
@@ -455,7 +469,140 @@ AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads) {
     return hc;
 }
 
-bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err) {
+void amg_collapse_graph(const std::vector<int64_t>& node_ptr, const std::vector<int64_t>& sp, const int32_t* sj, int nthreads,
+                        std::vector<int64_t>& np, std::vector<int32_t>& nj) {
+    const int64_t nn = (int64_t)node_ptr.size() - 1;
+    const int64_t nd = node_ptr[nn];
+    std::vector<int32_t> node_of(nd);
+    for (int64_t I = 0; I < nn; ++I)
+        for (int64_t i = node_ptr[I]; i < node_ptr[I + 1]; ++i) node_of[i] = (int32_t)I;
+    auto row = [&](int64_t I, std::vector<int32_t>& tmp) {
+        tmp.clear();
+        for (int64_t i = node_ptr[I]; i < node_ptr[I + 1]; ++i)
+            for (int64_t q = sp[i]; q < sp[i + 1]; ++q) {
+                const int32_t J = node_of[sj[q]];
+                if (J != I) tmp.push_back(J);
+            }
+        std::sort(tmp.begin(), tmp.end());
+        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    };
+    std::vector<int64_t> len(nn + 1, 0);
+    parallel_rows(nthreads, nn, [&](int, int64_t r0, int64_t r1) {
+        std::vector<int32_t> tmp;
+        for (int64_t I = r0; I < r1; ++I) { row(I, tmp); len[I + 1] = (int64_t)tmp.size(); }
+    });
+    np.assign(nn + 1, 0);
+    for (int64_t I = 0; I < nn; ++I) np[I + 1] = np[I] + len[I + 1];
+    nj.assign(np[nn], 0);
+    parallel_rows(nthreads, nn, [&](int, int64_t r0, int64_t r1) {
+        std::vector<int32_t> tmp;
+        for (int64_t I = r0; I < r1; ++I) {
+            row(I, tmp);
+            std::copy(tmp.begin(), tmp.end(), nj.begin() + np[I]);
+        }
+    });
+}
+
+// Per aggregate (its nodes in increasing order, their dofs in increasing order): B restricted to the
+// aggregate's k dofs (k x m) = Q R by modified Gram-Schmidt; a column whose orthogonal part is below
+// 1e-12 of its norm is dropped, so the aggregate gets r <= m coarse dofs. P0 holds Q (rows: the dofs,
+// columns: the aggregate's coarse dofs); the coarse level's vectors are the rows of R.
+int amg_tentative_nns(const AmgNns& nns, const std::vector<int32_t>& agg_node, int64_t nagg, int nthreads, HostCsr& P0,
+                      AmgNns& coarse) {
+    const int m = nns.m;
+    const int64_t nn = (int64_t)nns.node_ptr.size() - 1;
+    const int64_t nd = nns.node_ptr[nn];
+    // nodes of each aggregate (counting sort, increasing node order)
+    std::vector<int64_t> aptr(nagg + 1, 0);
+    for (int64_t I = 0; I < nn; ++I)
+        if (agg_node[I] >= 0) aptr[agg_node[I] + 1]++;
+    for (int64_t c = 0; c < nagg; ++c) aptr[c + 1] += aptr[c];
+    std::vector<int32_t> anodes(aptr[nagg]);
+    {
+        std::vector<int64_t> f(aptr.begin(), aptr.end() - 1);
+        for (int64_t I = 0; I < nn; ++I)
+            if (agg_node[I] >= 0) anodes[f[agg_node[I]]++] = (int32_t)I;
+    }
+    // QR of each aggregate
+    std::vector<std::vector<double>> Q(nagg), R(nagg);
+    std::vector<int> rank(nagg, 0);
+    parallel_rows(nthreads, nagg, [&](int, int64_t c0, int64_t c1) {
+        for (int64_t c = c0; c < c1; ++c) {
+            std::vector<int64_t> dofs;
+            for (int64_t t = aptr[c]; t < aptr[c + 1]; ++t)
+                for (int64_t i = nns.node_ptr[anodes[t]]; i < nns.node_ptr[anodes[t] + 1]; ++i) dofs.push_back(i);
+            const int64_t k = (int64_t)dofs.size();
+            std::vector<double>& q = Q[c];               // k x m, column-major (kept columns first)
+            std::vector<double>& r = R[c];               // m x m, row-major (rows: kept columns)
+            q.assign((size_t)k * m, 0.0);
+            r.assign((size_t)m * m, 0.0);
+            int kept = 0;
+            std::vector<double> v(k);
+            for (int j = 0; j < m; ++j) {
+                double n0 = 0.0;
+                for (int64_t t = 0; t < k; ++t) {
+                    v[t] = nns.B[(size_t)dofs[t] * m + j];
+                    n0 += v[t] * v[t];
+                }
+                n0 = std::sqrt(n0);
+                for (int l = 0; l < kept; ++l) {
+                    double dot = 0.0;
+                    for (int64_t t = 0; t < k; ++t) dot += q[(size_t)l * k + t] * v[t];
+                    r[(size_t)l * m + j] = dot;
+                    for (int64_t t = 0; t < k; ++t) v[t] -= dot * q[(size_t)l * k + t];
+                }
+                double nv = 0.0;
+                for (int64_t t = 0; t < k; ++t) nv += v[t] * v[t];
+                nv = std::sqrt(nv);
+                if (nv > 1e-12 * n0 && nv > 1e-300) {
+                    for (int64_t t = 0; t < k; ++t) q[(size_t)kept * k + t] = v[t] / nv;
+                    r[(size_t)kept * m + j] = nv;
+                    ++kept;
+                }
+            }
+            rank[c] = kept;
+        }
+    });
+    std::vector<int64_t> cptr(nagg + 1, 0);
+    for (int64_t c = 0; c < nagg; ++c) cptr[c + 1] = cptr[c] + rank[c];
+    if (cptr[nagg] >= ((int64_t)1 << 31)) return FGPU_ERR_INVALID;
+    // P0 rows: a dof of aggregate c holds the c's Q row at columns cptr[c] ..
+    std::vector<int32_t> agg_dof(nd, -1);
+    std::vector<int64_t> pos_in_agg(nd, 0);
+    for (int64_t c = 0; c < nagg; ++c) {
+        int64_t t = 0;
+        for (int64_t a = aptr[c]; a < aptr[c + 1]; ++a)
+            for (int64_t i = nns.node_ptr[anodes[a]]; i < nns.node_ptr[anodes[a] + 1]; ++i) {
+                agg_dof[i] = (int32_t)c;
+                pos_in_agg[i] = t++;
+            }
+    }
+    P0.nrows = nd;
+    P0.ncols = cptr[nagg];
+    P0.ia.assign(nd + 1, 0);
+    for (int64_t i = 0; i < nd; ++i) P0.ia[i + 1] = P0.ia[i] + (agg_dof[i] >= 0 ? rank[agg_dof[i]] : 0);
+    P0.ja.resize(P0.ia[nd]);
+    P0.a.resize(P0.ia[nd]);
+    for (int64_t i = 0; i < nd; ++i) {
+        const int32_t c = agg_dof[i];
+        if (c < 0) continue;
+        const int64_t k = (int64_t)Q[c].size() / m;
+        for (int l = 0; l < rank[c]; ++l) {
+            P0.ja[P0.ia[i] + l] = (int32_t)(cptr[c] + l);
+            P0.a[P0.ia[i] + l] = Q[c][(size_t)l * k + pos_in_agg[i]];
+        }
+    }
+    // next level: node c = aggregate c, its dofs the rank[c] coarse dofs, its vectors the rows of R
+    coarse.m = m;
+    coarse.node_ptr = cptr;
+    coarse.B.assign((size_t)cptr[nagg] * m, 0.0);
+    for (int64_t c = 0; c < nagg; ++c)
+        for (int l = 0; l < rank[c]; ++l)
+            for (int j = 0; j < m; ++j) coarse.B[(size_t)(cptr[c] + l) * m + j] = R[c][(size_t)l * m + j];
+    return FGPU_OK;
+}
+
+bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err, const AmgNns* nns) {
     const int nthreads = cfg.nthreads > 0 ? cfg.nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
     const int max_levels = cfg.max_levels > 0 ? cfg.max_levels : 10;
     const int64_t coarse_lim = cfg.coarse_eq_lim > 0 ? cfg.coarse_eq_lim : 800;
@@ -463,6 +610,15 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
     H.coarse_inv.clear();
     H.levels.emplace_back();
     H.levels[0].A = std::move(A0);
+    AmgNns cur;
+    if (nns) {
+        cur = *nns;
+        if (cur.m <= 0 || cur.node_ptr.empty() || cur.node_ptr.back() != H.levels[0].A.nrows ||
+            (int64_t)cur.B.size() != H.levels[0].A.nrows * cur.m) {
+            err = "gamg: near null space does not match the matrix";
+            return false;
+        }
+    }
     for (int l = 0; l + 1 < max_levels; ++l) {
         AmgHostLevel& L = H.levels[l];
         const HostCsr& A = L.A;
@@ -474,17 +630,37 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
         std::vector<int64_t> sp;
         std::vector<int32_t> sj;
         strength(A, d, cfg.threshold, sp, sj, nthreads);
-        const int64_t nagg = aggregate(A.nrows, sp, sj, L.agg);
-        if (nagg == 0 || nagg >= A.nrows) break;              // nothing to coarsen
+        HostCsr P0;
+        AmgNns next;
+        int64_t nagg = 0;
+        if (!nns) {
+            nagg = aggregate(A.nrows, sp, sj, L.agg);
+            if (nagg == 0 || nagg >= A.nrows) break;          // nothing to coarsen
+            tentative_constant(A.nrows, L.agg, nagg, P0);
+        } else {
+            std::vector<int64_t> np;
+            std::vector<int32_t> nj, agg_node;
+            amg_collapse_graph(cur.node_ptr, sp, sj.data(), nthreads, np, nj);
+            const int64_t nn = (int64_t)cur.node_ptr.size() - 1;
+            nagg = aggregate(nn, np, nj, agg_node);
+            if (nagg == 0 || nagg >= nn) break;
+            if (amg_tentative_nns(cur, agg_node, nagg, nthreads, P0, next)) { err = "gamg: coarse level too large"; return false; }
+            if (P0.ncols == 0 || P0.ncols >= A.nrows) break;
+            L.agg.assign(A.nrows, -1);
+            for (int64_t I = 0; I < nn; ++I)
+                for (int64_t i = cur.node_ptr[I]; i < cur.node_ptr[I + 1]; ++i) L.agg[i] = agg_node[I];
+        }
         const double omega = 4.0 / (3.0 * L.lmax);
-        smoothed_prolongator(A, d, L.agg, nagg, omega, cfg.agg_smooths, L.P, nthreads);
+        smooth_prolongator(A, d, std::move(P0), omega, cfg.agg_smooths, L.P, nthreads);
         transpose(L.P, L.R);
         HostCsr AP, Ac;
         spgemm(A, L.P, AP, nthreads);
         spgemm(L.R, AP, Ac, nthreads);
+        const int64_t nc = Ac.nrows;
         H.levels.emplace_back();
         H.levels.back().A = std::move(Ac);
-        if ((double)nagg > 0.9 * (double)H.levels[l].A.nrows) break;   // stagnating coarsening
+        if (nns) cur = std::move(next);
+        if ((double)nc > 0.9 * (double)H.levels[l].A.nrows) break;   // stagnating coarsening
     }
     AmgHostLevel& C = H.levels.back();
     {
@@ -520,9 +696,15 @@ extern "C" int fgpu_amg_host_build(int64_t n, const int64_t* ia, const int32_t* 
     A.ja.assign(ja, ja + ia[n]);
     A.a.assign(a, a + ia[n]);
     const fgpu::AmgHostCfg hc = fgpu::amg_host_cfg(cfg, nthreads);
+    fgpu::AmgNns nns;
+    if (cfg && cfg->nns_count > 0) {
+        if (!cfg->nns_host || fgpu::amg_nns_layout(cfg, n, nns)) return FGPU_ERR_INVALID;
+        for (int64_t i = 0; i < n; ++i)
+            for (int j = 0; j < nns.m; ++j) nns.B[(size_t)i * nns.m + j] = cfg->nns_host[(size_t)j * n + i];
+    }
     fgpu_amg_host* h = new fgpu_amg_host();
     std::string err;
-    if (!fgpu::amg_build_host(std::move(A), hc, h->H, err)) {
+    if (!fgpu::amg_build_host(std::move(A), hc, h->H, err, nns.m ? &nns : nullptr)) {
         delete h;
         return FGPU_ERR_INVALID;
     }

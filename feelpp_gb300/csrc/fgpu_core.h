@@ -113,8 +113,24 @@ struct AmgHierarchy {
     std::vector<double> coarse_inv;  // dense inverse of the coarsest operator (row-major), or empty
 };
 constexpr int64_t kAmgDenseCoarse = 2048;   // largest coarsest level inverted densely
-bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err);
+// Near null space of a level (PETSc's MatNullSpace given to GAMG, e.g. the rigid body modes of an
+// elasticity space): m vectors on the level's dofs, the dofs grouped in nodes (consecutive ranges).
+// Aggregation then runs on the nodes and each aggregate's tentative prolongator is the Q of the QR
+// factorisation of the vectors restricted to its dofs; R gives the next level's vectors.
+struct AmgNns {
+    int m = 0;
+    std::vector<int64_t> node_ptr;   // nodes + 1 dof offsets
+    std::vector<double> B;           // ndof x m, row-major
+};
+bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::string& err, const AmgNns* nns = nullptr);
+// node graph of a dof graph: nodes I, J coupled when a dof of I and a dof of J are (no self loops)
+void amg_collapse_graph(const std::vector<int64_t>& node_ptr, const std::vector<int64_t>& sp, const int32_t* sj, int nthreads,
+                        std::vector<int64_t>& np, std::vector<int32_t>& nj);
+// tentative prolongator of node aggregates from the near null space; `coarse` receives the next level's
+int amg_tentative_nns(const AmgNns& nns, const std::vector<int32_t>& agg_node, int64_t nagg, int nthreads, HostCsr& P0,
+                      AmgNns& coarse);
 AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads);
+int amg_nns_layout(const fgpu_amg_cfg* cfg, int64_t n, AmgNns& nns);
 // pieces of the host set-up shared with the device set-up (amg_dev.cu)
 // the host set-up's greedy aggregation over a graph copied in row order: rows [0, rows_ready) present;
 // returns -1 when `failed` is raised before all rows arrive
@@ -152,13 +168,18 @@ struct AmgSetupTimes {                // wall times of the set-up phases (ms), s
     double tail = 0;                 // host set-up of the levels below the device ones
     double layout = 0;               // level layouts (SELL-C-sigma, binary32 copies) and uploads
     double total = 0;
+    int handoff = 0;                 // why the device set-up handed a level of more than 16384 rows to the host:
+                                     // 0 none, 1 strength graph, 2 node graph, 3 nothing to coarsen, 4 A P0,
+                                     // 5 R = P^T, 6 A P, 7 R (A P) (a row beyond the kernels' staging)
 };
 struct AmgDevHierarchy {
     std::vector<AmgDevLevel> levels;
     AmgHierarchy tail;
     AmgSetupTimes times;
 };
-int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* A, const AmgHostCfg& cfg, AmgDevHierarchy& H);
+int amg_build_device(fgpu_ctx* ctx, const fgpu_matrix* A, const AmgHostCfg& cfg, AmgDevHierarchy& H, const AmgNns* nns = nullptr);
+// the near null space of fgpu_amg_cfg (device vectors) for a matrix of n rows; *has = false without one
+int amg_nns_from_cfg(fgpu_ctx* ctx, const fgpu_amg_cfg* cfg, int64_t n, AmgNns& nns, bool* has);
 int amg_copy_to_host(fgpu_ctx* ctx, const AmgDevCsr& D, HostCsr& H);
 
 // Boundary dof nodes: the nodes carried by faces owned by one element; when

@@ -184,6 +184,14 @@ class FunctionSpace:
     def element(self, name="u"):
         return Element(self, name)
 
+    def rigid_body_modes(self):
+        """The six rigid body modes of a Pchv space at its dof nodes (translations x, y, z; rotations
+        (-y, x, 0), (0, -z, y), (z, 0, -x) about the vertex centroid): the elasticity near null space."""
+        vs = [DeviceVector(self.env, self.ndof) for _ in range(6)]
+        arr = (C.c_void_p * 6)(*[v.h.value for v in vs])
+        self.env.check(self.env.lib.fgpu_space_rigid_body_modes(self.h, arr))
+        return vs
+
     def __del__(self):
         try:
             if self.h:
@@ -821,7 +829,8 @@ class Form2:
     def gamg(self, **opts):
         """The AMG hierarchy of this matrix (built, or rebuilt when the values changed since)."""
         amg = getattr(self, "_amg", None)
-        full = dict(threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0, setup_on_host=False)
+        full = dict(threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0, setup_on_host=False,
+                    near_null_space=None, block_size=0)
         full.update(opts)
         if amg is not None and amg.opts != full:
             amg = None
@@ -847,14 +856,29 @@ class AMG:
     options of the reference: threshold (pc-gamg-threshold), max_levels (pc-mg-levels), coarse_eq_lim
     (pc-gamg-coarse-eq-lim), agg_smooths (pc-gamg-nsmooths; -1 = unsmoothed), smoother_degree
     (Chebyshev degree of the level smoothers). 0 selects the default. setup_on_host: build the hierarchy
-    on the host instead of the device (the same hierarchy bit for bit)."""
+    on the host instead of the device (the same hierarchy bit for bit). near_null_space: None (the
+    constant vector), "rigid" (the rigid body modes of the form's Pchv space, block size 3) or a list of
+    DeviceVectors with block_size rows per node (PETSc MatSetNearNullSpace)."""
 
     def __init__(self, form, threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0,
-                 setup_on_host=False):
+                 setup_on_host=False, near_null_space=None, block_size=0):
         self.env, self.form = form.env, form
         self.opts = dict(threshold=threshold, max_levels=max_levels, coarse_eq_lim=coarse_eq_lim, agg_smooths=agg_smooths,
-                         smoother_degree=smoother_degree, setup_on_host=setup_on_host)
+                         smoother_degree=smoother_degree, setup_on_host=setup_on_host, near_null_space=near_null_space,
+                         block_size=block_size)
         cfg = _ffi.AmgCfg(float(threshold), max_levels, coarse_eq_lim, agg_smooths, smoother_degree, int(bool(setup_on_host)))
+        self._nns = None
+        if near_null_space is not None:
+            if isinstance(near_null_space, str):
+                if near_null_space != "rigid":
+                    raise ValueError("near_null_space: 'rigid' or a list of DeviceVectors")
+                vecs, block_size = form.space.rigid_body_modes(), 3
+            else:
+                vecs = list(near_null_space)
+            arr = (C.c_void_p * len(vecs))(*[v.h.value for v in vecs])
+            self._nns = (vecs, arr)
+            cfg.block_size, cfg.nns_count = int(block_size), len(vecs)
+            cfg.nns = C.cast(arr, C.c_void_p)
         h = C.c_void_p()
         self.env.check(self.env.lib.fgpu_amg_create(self.env.h, form.h, C.byref(cfg), C.byref(h)))
         self.h = h
@@ -869,12 +893,12 @@ class AMG:
         ms = C.c_double()
         self.env.check(self.env.lib.fgpu_amg_info(self.h, C.byref(nl), _ptr(rows), _ptr(nnz), C.byref(ms)))
         dl = C.c_int()
-        ph = np.zeros(8)
+        ph = np.zeros(9)
         self.env.check(self.env.lib.fgpu_amg_setup_info(self.h, C.byref(dl), _ptr(ph)))
         names = ("graph", "aggregate", "lanczos", "prolong", "galerkin", "host_levels", "layout", "total")
         return {"levels": nl.value, "rows": rows[:nl.value].tolist(), "nnz": nnz[:nl.value].tolist(),
                 "setup_ms": ms.value, "device_levels": dl.value,
-                "setup_phases_ms": {k: round(float(x), 3) for k, x in zip(names, ph)}}
+                "setup_phases_ms": {k: round(float(x), 3) for k, x in zip(names, ph[:8])}, "handoff": int(ph[8])}
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -180,6 +180,15 @@ typedef struct {              /* smoothed-aggregation AMG (PETSc PCGAMG "agg" op
     int smoother_degree;      /* Chebyshev degree of the level smoothers (0 = 3, i.e. 2 operator sweeps) */
     int setup_on_host;        /* 0: hierarchy built on the device (levels of at most 16384 rows on the host);
                                  1: built on the host. Both give the same hierarchy bit for bit. */
+    /* near null space (PETSc MatSetNearNullSpace, which the reference attaches on solve:
+     * feelpp/feel/feelalg/backend.hpp:1074-1088; e.g. the six rigid body modes of an elasticity space,
+     * fgpu_space_rigid_body_modes). nns_count = 0: the constant vector per aggregate. Otherwise the
+     * aggregation runs on nodes of block_size consecutive rows and each aggregate's tentative
+     * prolongator is the Q of the QR factorisation of the vectors restricted to its rows. */
+    int block_size;           /* rows per node (0 = 1) */
+    int nns_count;            /* number of vectors */
+    const fgpu_vector* const* nns;   /* fgpu_amg_create / fgpu_amg_device_build: device vectors of the matrix's size */
+    const double* nns_host;   /* fgpu_amg_host_build: nns_count x n values, vector after vector */
 } fgpu_amg_cfg;
 
 typedef struct {
@@ -339,10 +348,11 @@ int fgpu_amg_create(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg
 int fgpu_amg_update(fgpu_amg* amg);
 /* levels, rows[level], nnz[level] (arrays of at least 16 entries or NULL), set-up time in ms */
 int fgpu_amg_info(const fgpu_amg* amg, int* nlevels, int64_t* rows, int64_t* nnz, double* setup_ms);
-/* levels whose set-up ran on the device, and the set-up's phases in ms (8 entries or NULL): strength
+/* levels whose set-up ran on the device, and the set-up's phases in ms (9 entries or NULL): strength
  * graph, greedy aggregation (host), lambda_max, prolongator and restriction, Galerkin products, host
  * set-up of the levels below the device ones (all levels with setup_on_host), level layouts and
- * uploads, total */
+ * uploads, total; then the code of the step that handed a level of more than 16384 rows to the host
+ * (0 none, 1 strength graph, 2 node graph, 3 nothing to coarsen, 4 A P0, 5 R = P^T, 6 A P, 7 R (A P)) */
 int fgpu_amg_setup_info(const fgpu_amg* amg, int* device_levels, double* phases_ms);
 int fgpu_amg_destroy(fgpu_amg* amg);
 int fgpu_solve_cg_amg(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const fgpu_vector* b, fgpu_vector* x,
@@ -382,6 +392,10 @@ int fgpu_amg_host_destroy(fgpu_amg_host* h);
  * (replaces the host set-up of fgpu_amg_create; amg_setup.cpp's construction, same bits);
  * fgpu_amg_host_device_levels: how many of its levels the device built (0 for fgpu_amg_host_build) */
 int fgpu_amg_device_build(fgpu_ctx* ctx, const fgpu_matrix* A, const fgpu_amg_cfg* cfg, fgpu_amg_host** out);
+/* the six rigid body modes of a Pchv (ncomp = 3) space at its dof nodes (affine element maps): the
+ * translations along x, y, z and the rotations (-y, x, 0), (0, -z, y), (z, 0, -x) about the centroid
+ * of the mesh vertices; out: six vectors of the space's size (created by the caller) */
+int fgpu_space_rigid_body_modes(const fgpu_space* V, fgpu_vector* const* out);
 int fgpu_amg_host_device_levels(const fgpu_amg_host* h);
 
 /* ---- EnSight Gold export (the reference's default exporter, feelpp/feel/feelfilters/exporterensightgold.hpp):

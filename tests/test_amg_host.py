@@ -135,3 +135,59 @@ def test_unsmoothed_and_threshold(fgpu_lib, oracle):
     A1 = Ht.level(1)[0]
     G = (P0.T @ A0 @ P0).tocsr()
     assert abs(A1 - G).max() <= 1e-12 * abs(G).max()
+
+
+def _elasticity_beam(oracle, n):
+    """clamped P1 elasticity beam of [0,4]x[0,1]^2 (lambda 1, mu 0.5), its rigid body modes at the nodes"""
+    xyz, tets = mesh(n, perturb=0.1, lengths=(4.0, 1.0, 1.0))
+    N, l2g, ia, ja, val = oracle_system(oracle, xyz, tets, 1, ncomp=3, kind=1, lam=1.0, mu=0.5)
+    # P1 nodes are the mesh vertices: node coordinates through the scalar dof table
+    Ns, l2s = oracle.dof_table(tets, 1)
+    X = np.zeros((Ns, 3))
+    X[l2s.ravel()] = xyz[tets.ravel()]
+    mask = np.zeros(N, dtype=np.uint8)
+    mask[(3 * np.nonzero(X[:, 0] <= 1e-12)[0][:, None] + np.arange(3)).ravel()] = 1
+    oracle.dirichlet(ia, ja, val, np.zeros(N), mask, mode=1)
+    c = X.mean(axis=0)
+    x, y, z = (X - c).T
+    o, one = np.zeros(Ns), np.ones(Ns)
+    modes = [(one, o, o), (o, one, o), (o, o, one), (-y, x, o), (o, -z, y), (z, o, -x)]
+    B = np.stack([np.stack(m, axis=1).ravel() for m in modes])        # 6 x N, node-major dofs
+    return ia, ja, val, B, mask
+
+
+def _nns_hier(lib, ia, ja, a, B, **cfg):
+    c = _ffi.AmgCfg(cfg.get("threshold", 0.0), cfg.get("max_levels", 0), cfg.get("coarse_eq_lim", 0), cfg.get("agg_smooths", 0), 0)
+    Bc = np.ascontiguousarray(B, np.float64)
+    c.block_size, c.nns_count, c.nns_host = 3, len(B), Bc.ctypes.data
+    h = C.c_void_p()
+    ia, ja, a = np.ascontiguousarray(ia, np.int64), np.ascontiguousarray(ja, np.int32), np.ascontiguousarray(a, np.float64)
+    assert lib.fgpu_amg_host_build(len(ia) - 1, _p(ia), _p(ja), _p(a), C.byref(c), 2, C.byref(h)) == 0
+    H = Hier.__new__(Hier)
+    H.lib, H.h = lib, h
+    return H
+
+
+def test_rigid_body_near_null_space(fgpu_lib, oracle):
+    """Aggregation by nodes, the tentative prolongator spans the rigid body modes on each aggregate
+    (orthonormal columns), and the Galerkin identity holds on every level."""
+    ia, ja, val, B, mask = _elasticity_beam(oracle, 6)
+    Hu = _nns_hier(fgpu_lib, ia, ja, val, B, agg_smooths=-1, coarse_eq_lim=60)
+    A, P, agg, _ = Hu.level(0)
+    assert np.array_equal(agg[0::3], agg[1::3]) and np.array_equal(agg[0::3], agg[2::3])     # whole nodes
+    assert np.allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-13)
+    rows = agg >= 0
+    Bt = B.T * rows[:, None]
+    assert np.abs(Bt - P @ (P.T @ Bt)).max() <= 1e-10 * np.abs(Bt).max()
+    nagg = agg.max() + 1
+    assert 3 * nagg <= P.shape[1] <= 6 * nagg
+    H = _nns_hier(fgpu_lib, ia, ja, val, B, coarse_eq_lim=60)
+    prev = None
+    for l in range(H.nlevels()):
+        A, P, agg, lmax = H.level(l)
+        if prev is not None:
+            Ap, Pp = prev
+            G = (Pp.T @ Ap @ Pp).tocsr()
+            assert abs(A - G).max() <= 1e-12 * abs(G).max()
+        prev = (A, P)
+    assert H.nlevels() >= 2
