@@ -61,7 +61,7 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "pmg", "apply", "gmres"],
+    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "gamg_rigid", "pmg", "apply", "gmres"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
                         "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
                         "AMG-preconditioned CG solve to 1e-10; 'pmg' sets up the matrix-free Poisson operators "
@@ -709,6 +709,25 @@ def run_probe_gamg(args):
     st = a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
     print(json.dumps({"iterations": st["iterations"], "time_ms": st["time_ms"], "rel_residual": st["rel_residual"],
                       "gamg": st["gamg"]}), flush=True)
+
+
+def run_probe_gamg_rigid(args):
+    """The AMG hierarchy of the clamped vector P2 elasticity beam of [0,4]x[0,1]^2 (n^3 Kuhn mesh,
+    lambda 1, mu 0.5) with the rigid body near null space, built on the device, for kernel profiling;
+    prints the levels and the set-up phases."""
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    env = fpp.Environment()
+    xyz, tets = meshgen.kuhn_box(args.n, lengths=(4.0, 1.0, 1.0), perturb=0.1, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, 2)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    a.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, 1.0, 0.5), fpp.grad(v))))
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.cst_vec(0, 0, -1), fpp.id(v))))
+    a += fpp.on(fpp.markedfaces(M, 0.0), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    print(json.dumps({"gamg": a.gamg(near_null_space="rigid").info()}), flush=True)
 
 
 def run_probe_pmg(args):
@@ -1366,6 +1385,9 @@ def main():
         return
     if args.probe == "gamg":
         run_probe_gamg(args)
+        return
+    if args.probe == "gamg_rigid":
+        run_probe_gamg_rigid(args)
         return
     if args.probe == "apply":
         run_probe_apply(args)

@@ -57,9 +57,9 @@ constexpr int64_t kLanczosChunk = 16384;     // rows per partial sum (the host s
 constexpr int kLanczosSteps = 12;
 constexpr int64_t kHandoffRows = 16384;      // levels this small continue on the host
 constexpr int kSortMax = 16384;              // longest row sorted by seg_sort_kernel
-constexpr int kMaxLeft = 8192;               // longest left-factor row of a sparse product
-constexpr int kBins[3] = {256, 1024, 8192};  // hash table sizes (at most half full)
-constexpr int kBinLog[3] = {8, 10, 13};
+constexpr int kNumBins = 4;
+constexpr int kBins[kNumBins] = {256, 1024, 2048, 8192};  // hash table sizes (at most half full)
+constexpr int kBinLog[kNumBins] = {8, 10, 11, 13};
 
 int grid_rows(int64_t n, int per_block, int cap = 152 * 16) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + per_block - 1) / per_block, cap));
@@ -479,7 +479,6 @@ struct SpgemmArgs {
     const double* b = nullptr;
     int tsize = 256;                 // hash slots per warp (power of two, >= 64)
     int tshift = 24;                 // 32 - log2(tsize)
-    int pre_cap = 0;                 // longest row of A
     int warps = 8;                   // warps per block
     int wbytes = 0;                  // shared memory per warp
     uint32_t* cnt = nullptr;
@@ -491,8 +490,8 @@ struct SpgemmArgs {
     int* status = nullptr;
 };
 
-int spgemm_warp_bytes(int tsize, int pre_cap) {
-    const int b = tsize * 8 + 32 * 8 + tsize * 4 + (tsize / 2) * 4 + (pre_cap + 1) * 4;
+int spgemm_warp_bytes(int tsize) {
+    const int b = tsize * 8 + 32 * 8 + tsize * 4 + (tsize / 2) * 4;
     return (b + 15) & ~15;
 }
 
@@ -504,7 +503,6 @@ __global__ void __launch_bounds__(256) spgemm_kernel(SpgemmArgs g) {
     double* stage = hv + g.tsize;                                               // 32 products
     int32_t* hk = reinterpret_cast<int32_t*>(stage + 32);                       // tsize keys (-1: empty)
     int32_t* list = hk + g.tsize;                                               // tsize / 2 used slots
-    int32_t* pre = list + g.tsize / 2;                                          // pre_cap + 1 product offsets
     const int T = g.tsize, half = g.tsize / 2;
     const bool fill = g.oj != nullptr;
     for (int k = lane; k < T; k += 32) hk[k] = -1;
@@ -514,73 +512,80 @@ __global__ void __launch_bounds__(256) spgemm_kernel(SpgemmArgs g) {
         if (fill && g.off[i + 1] - g.off[i] > half) continue;        // a larger table's row
         const int64_t a0 = g.ia[i];
         const int na = (int)(g.ia[i + 1] - a0);
-        // product offsets: exclusive scan of the lengths of the B rows named by row i of A
-        int run = 0;
-        for (int k0 = 0; k0 < na; k0 += 32) {
-            const int k = k0 + lane;
+        int nuniq = 0;
+        bool over = false;
+        // the row of A in chunks of 32 entries (one per lane: its B row's start, length and the A value);
+        // the chunk's products in (A column, B column) order, 32 at a time
+        for (int c0 = 0; c0 < na && !over; c0 += 32) {
+            const int cn = min(32, na - c0);
             int len = 0;
-            if (k < na) {
-                const int32_t c = g.ja[a0 + k];
-                len = (int)(g.ib[c + 1] - g.ib[c]);
+            int64_t bstart = 0;
+            double av = 0.0;
+            if (lane < cn) {
+                const int32_t c = g.ja[a0 + c0 + lane];
+                bstart = g.ib[c];
+                len = (int)(g.ib[c + 1] - bstart);
+                if (fill) av = g.a[a0 + c0 + lane];
             }
             int x = len;
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= o) x += y;
             }
-            if (k < na) pre[k] = run + x - len;
-            run += __shfl_sync(0xffffffffu, x, 31);
-        }
-        __syncwarp();
-        const int nprod = run;
-        int nuniq = 0;
-        bool over = false;
-        for (int s0 = 0; s0 < nprod; s0 += 32) {
-            const int pidx = s0 + lane;
-            const bool act = pidx < nprod;
-            int32_t col = -1;
-            double val = 0.0;
-            if (act) {
-                int lo = 0, hi = na - 1;                         // the A entry of product pidx
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (pre[mid] <= pidx) lo = mid; else hi = mid - 1;
+            const int excl = x - len;
+            const int ctot = __shfl_sync(0xffffffffu, x, 31);
+            for (int s0 = 0; s0 < ctot; s0 += 32) {
+                const int pidx = s0 + lane;
+                const bool act = pidx < ctot;
+                // the chunk entry of product pidx: the last lane e < cn with excl_e <= pidx (fixed 5 steps)
+                int lo = 0;
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int cand = lo + step;
+                    const int ec = __shfl_sync(0xffffffffu, excl, cand & 31);
+                    if (cand < cn && ec <= pidx) lo = cand;
                 }
-                const int64_t q = g.ib[g.ja[a0 + lo]] + (pidx - pre[lo]);
-                col = g.jb[q];
-                if (fill) val = __dmul_rn(g.a[a0 + lo], g.b[q]);
-            }
-            const unsigned grp = __match_any_sync(0xffffffffu, col);
-            const bool leader = act && lane == __ffs(grp) - 1;
-            int slot = -1;
-            bool newkey = false;
-            if (leader) {
-                uint32_t h = ((uint32_t)col * 2654435761u) >> g.tshift;
-                for (int probe = 0; probe < T; ++probe) {
-                    const int32_t old = atomicCAS(hk + h, -1, col);
-                    if (old == -1) { newkey = true; slot = (int)h; break; }
-                    if (old == col) { slot = (int)h; break; }
-                    h = (h + 1) & (uint32_t)(T - 1);
+                const int e_excl = __shfl_sync(0xffffffffu, excl, lo);
+                const int64_t e_start = __shfl_sync(0xffffffffu, bstart, lo);
+                const double e_a = __shfl_sync(0xffffffffu, av, lo);
+                int32_t col = -1;
+                double val = 0.0;
+                if (act) {
+                    const int64_t q = e_start + (pidx - e_excl);
+                    col = g.jb[q];
+                    if (fill) val = __dmul_rn(e_a, g.b[q]);
                 }
-                if (slot < 0) over = true;
-            }
-            const unsigned nb = __ballot_sync(0xffffffffu, newkey);
-            if (newkey) {
-                const int pos = nuniq + __popc(nb & ((1u << lane) - 1u));
-                if (pos < half) list[pos] = slot;
-            }
-            nuniq += __popc(nb);
-            if (fill) {
-                stage[lane] = val;
+                const unsigned grp = __match_any_sync(0xffffffffu, col);
+                const bool leader = act && lane == __ffs(grp) - 1;
+                int slot = -1;
+                bool newkey = false;
+                if (leader) {
+                    uint32_t h = ((uint32_t)col * 2654435761u) >> g.tshift;
+                    for (int probe = 0; probe < T; ++probe) {
+                        const int32_t old = atomicCAS(hk + h, -1, col);
+                        if (old == -1) { newkey = true; slot = (int)h; break; }
+                        if (old == col) { slot = (int)h; break; }
+                        h = (h + 1) & (uint32_t)(T - 1);
+                    }
+                    if (slot < 0) over = true;
+                }
+                const unsigned nb = __ballot_sync(0xffffffffu, newkey);
+                if (newkey) {
+                    const int pos = nuniq + __popc(nb & ((1u << lane) - 1u));
+                    if (pos < half) list[pos] = slot;
+                }
+                nuniq += __popc(nb);
+                if (fill) {
+                    stage[lane] = val;
+                    __syncwarp();
+                    if (leader && slot >= 0) {
+                        double v = newkey ? 0.0 : hv[slot];
+                        for (unsigned m = grp; m; m &= m - 1u) v = __dadd_rn(v, stage[__ffs(m) - 1]);
+                        hv[slot] = v;
+                    }
+                }
                 __syncwarp();
-                if (leader && slot >= 0) {
-                    double v = newkey ? 0.0 : hv[slot];
-                    for (unsigned m = grp; m; m &= m - 1u) v = __dadd_rn(v, stage[__ffs(m) - 1]);
-                    hv[slot] = v;
-                }
+                if (__any_sync(0xffffffffu, over) || nuniq > half) { over = true; break; }
             }
-            __syncwarp();
-            if (__any_sync(0xffffffffu, over) || nuniq > half) { over = true; break; }
         }
         if (over) {
             for (int k = lane; k < T; k += 32) hk[k] = -1;
@@ -640,10 +645,9 @@ __global__ void __launch_bounds__(256) spgemm_kernel(SpgemmArgs g) {
 int launch_spgemm(fgpu_ctx* ctx, SpgemmArgs g, int bin) {
     g.tsize = kBins[bin];
     g.tshift = 32 - kBinLog[bin];
-    g.wbytes = spgemm_warp_bytes(g.tsize, g.pre_cap);
+    g.wbytes = spgemm_warp_bytes(g.tsize);
     g.warps = std::max(1, std::min(8, (110 * 1024) / g.wbytes));
     const int smem = g.warps * g.wbytes;
-    if (smem > 227 * 1024) { ctx->err = "gamg device set-up: product row too long for shared memory"; return FGPU_ERR_INVALID; }
     DEV_TRY(cudaFuncSetAttribute(spgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     const int per_sm = std::max(1, std::min(2048 / (32 * g.warps), (228 * 1024) / (smem + 1024)));
     const int blocks = grid_rows(g.nrows, g.warps, 152 * per_sm);
@@ -653,7 +657,7 @@ int launch_spgemm(fgpu_ctx* ctx, SpgemmArgs g, int bin) {
     return FGPU_OK;
 }
 
-// C = A B (rows sorted by column). *overflow: a row beyond the largest table or the staging capacity.
+// C = A B (rows sorted by column). *overflow: a row with more distinct columns than the largest table.
 int spgemm_dev(fgpu_ctx* ctx, const AmgDevCsr& A, const AmgDevCsr& B, AmgDevCsr& C, int* d_status, bool* overflow) {
     *overflow = false;
     const int64_t n = A.nrows;
@@ -661,42 +665,39 @@ int spgemm_dev(fgpu_ctx* ctx, const AmgDevCsr& A, const AmgDevCsr& B, AmgDevCsr&
     unsigned long long* stats = w.get<unsigned long long>(2);
     uint32_t* cnt = w.get<uint32_t>(n + 1);
     uint32_t* off32 = w.get<uint32_t>(n + 1);
-    int32_t* ovf1 = w.get<int32_t>(n);
-    int32_t* ovf2 = w.get<int32_t>(n);
-    uint32_t* novf = w.get<uint32_t>(2);
-    DEV_ALLOC(stats && cnt && off32 && ovf1 && ovf2 && novf);
+    int32_t* ovf[kNumBins] = {nullptr, w.get<int32_t>(n), w.get<int32_t>(n), w.get<int32_t>(n)};
+    uint32_t* novf = w.get<uint32_t>(kNumBins);
+    DEV_ALLOC(stats && cnt && off32 && ovf[1] && ovf[2] && ovf[3] && novf);
     DEV_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
-    DEV_TRY(cudaMemsetAsync(novf, 0, 2 * sizeof(uint32_t), ctx->stream));
+    DEV_TRY(cudaMemsetAsync(novf, 0, kNumBins * sizeof(uint32_t), ctx->stream));
     row_stats_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, B.ia, stats);
     ctx->launches++;
     unsigned long long hs[2] = {0, 0};
     DEV_TRY(cudaMemcpyAsync(hs, stats, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
     DEV_TRY(cudaStreamSynchronize(ctx->stream));
-    if (hs[0] > (unsigned long long)kMaxLeft || hs[1] > 0x7fffffffull) { *overflow = true; return FGPU_OK; }
+    if (hs[1] > 0x7fffffffull) { *overflow = true; return FGPU_OK; }
     SpgemmArgs g;
     g.ia = A.ia; g.ja = A.ja; g.a = A.a;
     g.ib = B.ia; g.jb = B.ja; g.b = B.a;
-    g.pre_cap = (int)hs[0];
     g.status = d_status;
-    // count: all rows with the small table, the rows it cannot hold with the larger ones
-    uint32_t hn[2] = {0, 0};
+    // count: all rows with the smallest table, the rows it cannot hold with the next ones in turn
+    int64_t rows_in[kNumBins] = {n, 0, 0, 0};
     {
-        SpgemmArgs c = g;
-        c.nrows = n; c.cnt = cnt; c.ovf = ovf1; c.novf = novf;
-        int rc = launch_spgemm(ctx, c, 0);
-        if (rc) return rc;
-        DEV_TRY(cudaMemcpyAsync(hn, novf, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-        DEV_TRY(cudaStreamSynchronize(ctx->stream));
-        if (hn[0]) {
-            c.nrows = hn[0]; c.rows = ovf1; c.ovf = ovf2; c.novf = novf + 1;
-            rc = launch_spgemm(ctx, c, 1);
+        for (int bin = 0; bin < kNumBins; ++bin) {
+            if (bin > 0 && rows_in[bin] == 0) break;
+            SpgemmArgs c = g;
+            c.nrows = rows_in[bin];
+            c.rows = ovf[bin];
+            c.cnt = cnt;
+            c.ovf = bin + 1 < kNumBins ? ovf[bin + 1] : nullptr;
+            c.novf = bin + 1 < kNumBins ? novf + bin + 1 : nullptr;
+            int rc = launch_spgemm(ctx, c, bin);
             if (rc) return rc;
-            DEV_TRY(cudaMemcpyAsync(hn + 1, novf + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-            DEV_TRY(cudaStreamSynchronize(ctx->stream));
-            if (hn[1]) {
-                c.nrows = hn[1]; c.rows = ovf2; c.ovf = nullptr; c.novf = nullptr;
-                rc = launch_spgemm(ctx, c, 2);
-                if (rc) return rc;
+            if (bin + 1 < kNumBins) {
+                uint32_t hn = 0;
+                DEV_TRY(cudaMemcpyAsync(&hn, novf + bin + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+                DEV_TRY(cudaStreamSynchronize(ctx->stream));
+                rows_in[bin + 1] = hn;
             }
         }
     }
@@ -712,21 +713,13 @@ int spgemm_dev(fgpu_ctx* ctx, const AmgDevCsr& A, const AmgDevCsr& B, AmgDevCsr&
     u32_to_i64_kernel<<<grid_rows(n + 1, 256), 256, 0, ctx->stream>>>(n + 1, off32, C.ia);
     ctx->launches++;
     g.off = C.ia; g.oj = C.ja; g.oa = C.a;
-    {
+    for (int bin = 0; bin < kNumBins; ++bin) {
+        if (rows_in[bin] == 0) continue;
         SpgemmArgs f = g;
-        f.nrows = n;
-        rc = launch_spgemm(ctx, f, 0);
+        f.nrows = rows_in[bin];
+        f.rows = ovf[bin];
+        rc = launch_spgemm(ctx, f, bin);
         if (rc) return rc;
-        if (hn[0]) {
-            f.nrows = hn[0]; f.rows = ovf1;
-            rc = launch_spgemm(ctx, f, 1);
-            if (rc) return rc;
-        }
-        if (hn[1]) {
-            f.nrows = hn[1]; f.rows = ovf2;
-            rc = launch_spgemm(ctx, f, 2);
-            if (rc) return rc;
-        }
     }
     rc = read_status(ctx, d_status, &st);
     if (rc) return rc;
