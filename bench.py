@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the P3 / streamed / Poisson-error / p-multigrid extras")
     p.add_argument("--pmg-n", type=int, default=96, help="extras: mesh of the config-5 p-multigrid solve (0: skip)")
+    p.add_argument("--elasticity-n", type=int, default=48, help="extras: mesh of the config-3 elasticity beam (0: skip)")
     p.add_argument("--nprob", type=int, default=512, help="batch: number of independent problems")
     p.add_argument("--nmax", type=int, default=40, help="batch: largest cube resolution")
     p.add_argument("--heat-steps", type=int, default=100, help="heat: backward-Euler steps")
@@ -420,6 +421,49 @@ def extra_pmg(fpp, _ffi, fe, n, local):
     return out
 
 
+def extra_elasticity(fpp, env_unused, n, local, steps=5):
+    """Config 3: clamped vector P2 elasticity beam of [0,4]x[0,1]^2 (n^3 Kuhn mesh perturbed 0.1h,
+    lambda 1, mu 0.5, body force (0,0,-1)): FP64 assembly rate, then CG with double-double iterative
+    refinement to 1e-10 preconditioned by AMG with the rigid body near null space."""
+    from feelpp_gb300 import meshgen
+    env = fpp.Environment(device=local)
+    xyz, tets = meshgen.kuhn_box(n, lengths=(4.0, 1.0, 1.0), perturb=0.1, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pchv(M, 2)
+    u, v = V.element(), V.element()
+    a = fpp.form2(test=V, trial=V)
+    integral = fpp.integrate(fpp.elements(M), fpp.inner(fpp.stress(u, 1.0, 0.5), fpp.grad(v)))
+    for _ in range(3):
+        a.assign(integral)
+    env.sync()
+    with NvmlSampler(local) as clk_a:            # wall time of the synchronised loop (launches included)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            a.assign(integral)
+        env.sync()
+        asm_ms = (time.perf_counter() - t0) * 1e3 / steps
+    l = fpp.form1(test=V)
+    l.assign(fpp.integrate(fpp.elements(M), fpp.inner(fpp.cst_vec(0, 0, -1), fpp.id(v))))
+    a += fpp.on(fpp.markedfaces(M, 0.0), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    w, wl = V.element(), V.element()
+    with NvmlSampler(local) as clk_s:
+        t0 = time.perf_counter()
+        amg = a.gamg(near_null_space="rigid")
+        setup_ms = (time.perf_counter() - t0) * 1e3
+        try:
+            st = a.solve_refined(rhs=l, solution=w, solution_lo=wl, rtol=1e-10, pc="gamg", gamg={"near_null_space": "rigid"})
+            st["status"] = "ok"
+        except fpp.FgpuError as e:
+            st = {"status": str(e)}
+    x = w.to_numpy().reshape(-1, 3)
+    return {"workload": "vector P2 elasticity, %d^3 Kuhn mesh of [0,4]x[0,1]^2 (%d tets, %d dofs, nnz %d), perturb 0.1h"
+                        % (n, len(tets), V.ndof, a.nnz),
+            "assembly_f64": {"ms_per_step": asm_ms, "value": a.nnz / (asm_ms / 1e3) / 1e6, "unit": "Mnnz/s",
+                             "clocks": clk_a.summary()},
+            "solve_refined_dd_gamg_rigid_body": st, "amg_setup_ms": setup_ms, "amg": amg.info(),
+            "min_uz": float(x[:, 2].min()), "clocks": clk_s.summary()}
+
+
 def run_gb300(args, rank, world, local):
     import ctypes as C
 
@@ -628,6 +672,8 @@ def run_gb300(args, rank, world, local):
         extras["streamed_assembly"] = streamed
         if args.pmg_n > 0:
             extras["config5_pmg_p3"] = extra_pmg(fpp, _ffi, fe, args.pmg_n, local)
+        if args.elasticity_n > 0:
+            extras["config3_elasticity_p2"] = extra_elasticity(fpp, None, args.elasticity_n, local)
     if rank != 0:
         return
     cpu = None
