@@ -865,22 +865,23 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, const AmgNns
     diag_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, d_status);
     ctx->launches++;
     // the Lanczos thread and stream: started once the diagonal is formed, joined before any return
+    std::thread lanczos;
     cudaEvent_t d_ready = nullptr;
+    struct LanczosGuard {
+        std::thread& t;
+        LanczosJob& job;
+        cudaEvent_t& ev;
+        ~LanczosGuard() {
+            if (t.joinable()) t.join();
+            if (job.st) cudaStreamDestroy(job.st);
+            if (ev) cudaEventDestroy(ev);
+        }
+    } lanczos_guard{lanczos, lz, d_ready};
     DEV_TRY(cudaEventCreateWithFlags(&d_ready, cudaEventDisableTiming));
     DEV_TRY(cudaEventRecord(d_ready, ctx->stream));
     DEV_TRY(cudaStreamCreateWithFlags(&lz.st, cudaStreamNonBlocking));
     DEV_TRY(cudaStreamWaitEvent(lz.st, d_ready, 0));
-    std::thread lanczos([&lz] { lz.run(); });
-    struct LanczosGuard {
-        std::thread& t;
-        LanczosJob& job;
-        cudaEvent_t ev;
-        ~LanczosGuard() {
-            if (t.joinable()) t.join();
-            cudaStreamDestroy(job.st);
-            cudaEventDestroy(ev);
-        }
-    } lanczos_guard{lanczos, lz, d_ready};
+    lanczos = std::thread([&lz] { lz.run(); });
     strong_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, A.ia, A.ja, A.a, d, cfg.threshold, cnt, nullptr, nullptr);
     ctx->launches++;
     uint64_t ns = 0;
