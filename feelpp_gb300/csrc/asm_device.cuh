@@ -86,6 +86,26 @@ __device__ __forceinline__ df coef_entry_df(const float* ch, const float* cl, co
     }
     return quick_two_sum(s, err);
 }
+// the same sum with the entry's table values already in registers (th[k], tl[k])
+__device__ __forceinline__ df coef_entry_df_reg(const float* ch, const float* cl, const float* th, const float* tl) {
+    float s = 0.0f, err = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        const float p = f_mul(ch[k], th[k]);
+        const float pe = f_fma(ch[k], th[k], -p);
+        err = f_fma(ch[k], tl[k], err);
+        err = f_fma(cl[k], th[k], err);
+        err = f_add(err, pe);
+        if (k == 0) {
+            s = p;
+        } else {
+            df t = two_sum(s, p);
+            s = t.hi;
+            err = f_add(err, t.lo);
+        }
+    }
+    return quick_two_sum(s, err);
+}
 __device__ __forceinline__ float coef_entry_f(const float* ch, const float* __restrict__ Th, int stride, int tix) {
     float v = 0.0f;
 #pragma unroll

@@ -1296,6 +1296,53 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
     const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
     const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    if (NTRI <= 64) {
+        // at most two entries per lane, the same ones for every element: their table values stay in
+        // registers across the element loop
+        constexpr int TS = EPW > 1 ? NTRI : 32;
+        const int t1 = t0 + TS;
+        float th0[7], tl0[7], th1[7], tl1[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const bool ok0 = sub < EPW && t0 < NTRI, ok1 = sub < EPW && t1 < NTRI;
+            th0[k] = ok0 ? Th[k * NTRI + t0] : 0.0f;
+            th1[k] = ok1 ? Th[k * NTRI + t1] : 0.0f;
+            tl0[k] = (MODE == kModeDF64 && ok0) ? Tl[k * NTRI + t0] : 0.0f;
+            tl1[k] = (MODE == kModeDF64 && ok1) ? Tl[k * NTRI + t1] : 0.0f;
+        }
+        for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
+            const int64_t e = e0 + sub;
+            if (sub >= EPW || e >= nt) continue;
+            float ch[7], cl[7];
+            load_record(rec + 4 * e, ch, cl, MODE == kModeDF64);
+            if (MODE == kModeDF64) {
+                float2* kb = reinterpret_cast<float2*>(kbuf) + e * NTRI;
+                if (t0 < NTRI) {
+                    const df v = coef_entry_df_reg(ch, cl, th0, tl0);
+                    kb[t0] = make_float2(v.hi, v.lo);
+                }
+                if (t1 < NTRI) {
+                    const df v = coef_entry_df_reg(ch, cl, th1, tl1);
+                    kb[t1] = make_float2(v.hi, v.lo);
+                }
+            } else {
+                float* kb = reinterpret_cast<float*>(kbuf) + e * NTRI;
+                if (t0 < NTRI) {
+                    float v = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th0[k], v);
+                    kb[t0] = v;
+                }
+                if (t1 < NTRI) {
+                    float v = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th1[k], v);
+                    kb[t1] = v;
+                }
+            }
+        }
+        return;
+    }
     for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
         const int64_t e = e0 + sub;
         if (sub >= EPW || e >= nt) continue;
