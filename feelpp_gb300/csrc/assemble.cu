@@ -1713,7 +1713,8 @@ int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int
     // direct stores: the gather writes every value to device memory and to the mapped host buffer.
     // (Element kernel and gather in eight ranges each, a range of entries gathered on a side stream
     // once the element ranges it reads were done, measured slower: 16.4 against 19.2 Gnnz/s end to
-    // end at P2 64^3.)
+    // end at P2 64^3; so was a variant with the elements ordered by the first of four row chunks that
+    // reads them: 16.8-16.9 against 19.7 Gnnz/s, with a gather grid of 4 or 32 blocks per SM.)
     double* hdev = nullptr;
     if (ctx->host_transfer != FGPU_HOST_TRANSFER_COPY) {
         cudaPointerAttributes pa{};
