@@ -826,8 +826,11 @@ class Form2:
                                                             C.byref(cfg), float(inner_reduction), C.byref(st)))
         return _stats(st)
 
-    def gamg(self, **opts):
-        """The AMG hierarchy of this matrix (built, or rebuilt when the values changed since)."""
+    def gamg(self, reuse=False, **opts):
+        """The AMG hierarchy of this matrix (built, or rebuilt when the values changed since). reuse=True
+        keeps an existing hierarchy after the values changed (PETSc's -pc_gamg_reuse_interpolation /
+        a preconditioner kept across time steps): the V-cycle then acts with the older operator, the CG
+        with the current one."""
         amg = getattr(self, "_amg", None)
         full = dict(threshold=0.0, max_levels=0, coarse_eq_lim=0, agg_smooths=0, smoother_degree=0, setup_on_host=False,
                     near_null_space=None, block_size=0)
@@ -838,7 +841,7 @@ class Form2:
             amg = AMG(self, **opts)
             self._amg = amg
             self._amg_version = self._version
-        elif self._amg_version != self._version:
+        elif self._amg_version != self._version and not reuse:
             amg.update()
             self._amg_version = self._version
         return amg

@@ -92,3 +92,21 @@ def test_gamg_one_level_dense(env):
     w = V.element()
     st = a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
     assert st["gamg"]["levels"] == 1 and st["rel_residual"] <= 1e-10 and st["iterations"] <= 6
+
+
+def test_gamg_hierarchy_kept_across_reassembly(env):
+    """reuse=True keeps the hierarchy of the first assembly as the preconditioner of later ones (time
+    stepping): CG still converges to the current matrix's solution"""
+    xyz, tets = mesh(10, perturb=0.15)
+    kappa = meshgen.lognormal_kappa(len(tets))
+    M, V, u, v, a, l = poisson(env, 10, 2, kappa=kappa)
+    w = V.element()
+    a.solve(rhs=l, solution=w, rtol=1e-10, pc="gamg")
+    amg0 = a.gamg()
+    a.assign(fpp.integrate(fpp.elements(M), (1.5 * kappa) * fpp.inner(fpp.gradt(u), fpp.grad(v))))
+    a += fpp.on(fpp.boundaryfaces(M), rhs=l, element=u, expr=0.0, type="elimination_symmetric")
+    w2 = V.element()
+    st = a.solve(rhs=l, solution=w2, rtol=1e-10, pc="gamg", gamg={"reuse": True})
+    assert a.gamg(reuse=True) is amg0
+    assert st["rel_residual"] <= 1e-10
+    assert np.linalg.norm(w2.to_numpy() - w.to_numpy() / 1.5) <= 1e-8 * np.linalg.norm(w.to_numpy())
