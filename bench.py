@@ -518,8 +518,8 @@ def run_gb300(args, rank, world, local):
     geo_cnt, geo_ms = env.prof("geometry")
     value = nnz * args.steps * world / (ms_max / 1e3) / 1e6
 
-    # roofline of the dominant kernel and of the whole assembly step, in SURVEY-8(d) algorithmic
-    # bytes of one assembly: B_asm = CSR values written once, ja / ia read once, coordinates,
+    # roofline of the dominant kernel and of the whole assembly step, in the algorithmic bytes of one
+    # assembly: B_asm = CSR values written once, ja / ia read once, coordinates,
     # l2g and kappa read once (no load vector in this step)
     hbm_peak, peak_kind = load_peaks()
     n_loc = (args.order + 1) * (args.order + 2) * (args.order + 3) // 6
