@@ -1375,7 +1375,11 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 // position) halves the map and the buffer reads on paper but took 0.785 ms
 // against 0.64 ms: at 48^3 its DRAM reads stayed at 888 MB (the transposes'
 // second reads of the buffer hit L2 here), with more warp instructions (half the
-// lanes idle) and scattered stores.
+// lanes idle) and scattered stores. One batch of 6 per entry with the entries of
+// more than 6 contributions (the vertex-row diagonals, 0.5 % of the entries) left
+// to a second kernel over their list: timed by the tuner against B = 2, 4, 8 and
+// never picked at P2 or P3 64^3 (the warps' longest entries are not what bounds
+// the kernel).
 template <int MODE, int B = 4>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
