@@ -1,16 +1,17 @@
 // Device set-up of the smoothed-aggregation hierarchy (the default of fgpu_amg_create).
 //
 // The construction of the host set-up (amg_setup.cpp: Vanek, Mandel, Brezina 1996; PETSc PCGAMG "agg"
-// options of the reference, feelpp/feel/feelalg/preconditionerpetsc.cpp:2229-2330), with every step but
-// the greedy aggregation on the device, and every floating-point result formed in the host set-up's
-// order with the same roundings, so that the device levels equal the host levels bit for bit:
+// options of the reference, feelpp/feel/feelalg/preconditionerpetsc.cpp:2229-2330), every step on the
+// device (but the QR of a near null space's aggregates), and every floating-point result formed in the
+// host set-up's order with the same roundings, so that the device levels equal the host levels bit for bit:
 //   * diagonal and strength graph: a row kernel marks |a_ij| > theta sqrt(|a_ii a_jj|) (j != i,
 //     a_ij != 0); its transpose is built by counting, a scan and a fill, each row sorted, and the two
 //     sorted lists merged per row (the symmetrised graph);
-//   * greedy aggregation: the host set-up's three passes over the copied graph (sequential by nature);
+//   * aggregation: the host set-up's rounds of a distance-2 independent set (roots), then roots'
+//     neighbours, then the rest by their first aggregated neighbour, each step a kernel over the nodes;
 //   * lambda_max(D^-1 A): 12 Lanczos steps on D^-1/2 A D^-1/2 from the host set-up's start vector, the
 //     products one thread per row in column order, the dot products as sequential sums over chunks of
-//     16384 rows combined in chunk order (the host's partition), the tridiagonal's largest eigenvalue
+//     1024 rows combined in chunk order (the host's partition), the tridiagonal's largest eigenvalue
 //     by the host's Sturm bisection;
 //   * P0(i, agg(i)) = 1/sqrt(|agg|), A P0, and P = P0 - omega D^-1 (A P0) merged row by row;
 //   * R = P^T by counting, a scan, a fill and a per-row sort;
@@ -53,7 +54,7 @@ namespace {
 
 constexpr int kStOverflow = 1;               // a row beyond a kernel's staging capacity
 constexpr int kStDiag = 2;                   // a non-positive diagonal entry
-constexpr int64_t kLanczosChunk = 16384;     // rows per partial sum (the host set-up's partition)
+constexpr int64_t kLanczosChunk = 1024;      // rows per partial sum (the host set-up's partition)
 constexpr int kLanczosSteps = 12;
 constexpr int64_t kHandoffRows = 16384;      // levels this small continue on the host
 constexpr int kSortMax = 16384;              // longest row sorted by seg_sort_kernel
@@ -258,7 +259,7 @@ __global__ void lanczos_spmv_kernel(int64_t n, const int64_t* __restrict__ ia, c
 }
 // partial[c] = sum over the rows of chunk c of x_i y_i, in row order: one block per chunk; the block
 // forms a tile's products in shared memory, one thread adds them in order
-constexpr int kDotTile = 2048;
+constexpr int kDotTile = 1024;
 __global__ void __launch_bounds__(128) chunk_dot_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
                                                         double* __restrict__ partial) {
     __shared__ double buf[kDotTile];
@@ -462,6 +463,129 @@ __global__ void rbm_kernel(int64_t nnodes, const double* __restrict__ xn, double
         m4[r] = 0.0; m4[r + 1] = -z; m4[r + 2] = y;
         m5[r] = z; m5[r + 1] = 0.0; m5[r + 2] = -x;
     }
+}
+
+// Aggregation rounds (the host set-up's aggregate_mis2, amg_setup.cpp): states 0 undecided, 1 root,
+// 2 out, 3 no strong neighbours; each kernel reads the previous step's arrays only.
+__global__ void mis_init_kernel(int64_t n, const uint32_t* __restrict__ sp, int8_t* __restrict__ state) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        state[i] = sp[i + 1] > sp[i] ? 0 : 3;
+}
+// largest undecided key and any root in the closed neighbourhood (8 lanes per node, reductions by
+// shuffles: max and or do not depend on the order)
+constexpr int kMisLanes = 8;
+__global__ void __launch_bounds__(256) mis_pass1_kernel(int64_t n, const uint32_t* __restrict__ sp, const int32_t* __restrict__ sj,
+                                                        const int8_t* __restrict__ state, uint64_t* __restrict__ m1,
+                                                        uint8_t* __restrict__ r1) {
+    const int sub = threadIdx.x & (kMisLanes - 1);
+    const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kMisLanes);
+    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kMisLanes;; i += groups) {
+        const bool live = i < n;
+        uint64_t m = 0;
+        unsigned r = 0;
+        if (live) {
+            if (sub == 0) {
+                m = state[i] == 0 ? amg_mis_key(i) : 0;
+                r = state[i] == 1;
+            }
+            for (uint32_t q = sp[i] + sub; q < sp[i + 1]; q += kMisLanes) {
+                const int32_t j = sj[q];
+                const int8_t sjs = state[j];
+                if (sjs == 0) m = max(m, amg_mis_key(j));
+                r |= sjs == 1;
+            }
+        }
+        for (int o = kMisLanes / 2; o > 0; o >>= 1) {
+            m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+            r |= __shfl_xor_sync(0xffffffffu, r, o);
+        }
+        if (live && sub == 0) {
+            m1[i] = m;
+            r1[i] = (uint8_t)r;
+        }
+        // all lanes of the warp leave together (the shuffles above need them)
+        if (__all_sync(0xffffffffu, i >= n)) break;
+    }
+}
+// the same over distance 2, and the new state; counts the nodes left undecided
+__global__ void __launch_bounds__(256) mis_pass2_kernel(int64_t n, const uint32_t* __restrict__ sp, const int32_t* __restrict__ sj,
+                                                        const int8_t* __restrict__ state, const uint64_t* __restrict__ m1,
+                                                        const uint8_t* __restrict__ r1, int8_t* __restrict__ nstate,
+                                                        unsigned long long* __restrict__ undecided) {
+    const int sub = threadIdx.x & (kMisLanes - 1);
+    const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kMisLanes);
+    unsigned long long c = 0;
+    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kMisLanes;; i += groups) {
+        const bool live = i < n;
+        const int8_t s0 = live ? state[i] : (int8_t)3;
+        uint64_t m = 0;
+        unsigned r = 0;
+        if (live && s0 == 0) {
+            if (sub == 0) {
+                m = m1[i];
+                r = r1[i];
+            }
+            for (uint32_t q = sp[i] + sub; q < sp[i + 1]; q += kMisLanes) {
+                m = max(m, m1[sj[q]]);
+                r |= r1[sj[q]];
+            }
+        }
+        for (int o = kMisLanes / 2; o > 0; o >>= 1) {
+            m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+            r |= __shfl_xor_sync(0xffffffffu, r, o);
+        }
+        if (live && sub == 0) {
+            int8_t ns = s0;
+            if (s0 == 0) {
+                if (r) ns = 2;
+                else if (m == amg_mis_key(i)) ns = 1;
+                else ++c;
+            }
+            nstate[i] = ns;
+        }
+        // all lanes of the warp leave together (the shuffles above need them)
+        if (__all_sync(0xffffffffu, i >= n)) break;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(undecided, c);
+}
+__global__ void mis_root_flag_kernel(int64_t n, const int8_t* __restrict__ state, uint32_t* __restrict__ flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = state[i] == 1 ? 1u : 0u;
+}
+// roots and their neighbours (a node has at most one root neighbour)
+__global__ void mis_assign1_kernel(int64_t n, const uint32_t* __restrict__ sp, const int32_t* __restrict__ sj,
+                                   const int8_t* __restrict__ state, const uint32_t* __restrict__ rank, int32_t* __restrict__ a1) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t a = -1;
+        if (state[i] == 1) {
+            a = (int32_t)rank[i];
+        } else {
+            for (uint32_t q = sp[i]; q < sp[i + 1]; ++q)
+                if (state[sj[q]] == 1) { a = (int32_t)rank[sj[q]]; break; }
+        }
+        a1[i] = a;
+    }
+}
+// the other coupled nodes join the aggregate of their first neighbour (column order) aggregated above
+__global__ void mis_assign2_kernel(int64_t n, const uint32_t* __restrict__ sp, const int32_t* __restrict__ sj,
+                                   const int8_t* __restrict__ state, const int32_t* __restrict__ a1, int32_t* __restrict__ agg) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t a = a1[i];
+        if (a < 0 && state[i] != 3)
+            for (uint32_t q = sp[i]; q < sp[i + 1]; ++q)
+                if (a1[sj[q]] >= 0) { a = a1[sj[q]]; break; }
+        agg[i] = a;
+    }
+}
+// tentative scaling of the constant vector: aggregate sizes, then 1/sqrt(size)
+__global__ void agg_size_kernel(int64_t n, const int32_t* __restrict__ agg, unsigned int* __restrict__ sz) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (agg[i] >= 0) atomicAdd(sz + agg[i], 1u);
+}
+__global__ void agg_scale_kernel(int64_t nagg, const unsigned int* __restrict__ sz, double* __restrict__ s0) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nagg; c += (int64_t)gridDim.x * blockDim.x)
+        s0[c] = __ddiv_rn(1.0, __dsqrt_rn((double)sz[c]));
 }
 
 // Sparse product C = A B, one warp per row of A (see the file comment). Count pass (oj == nullptr):
@@ -959,44 +1083,52 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, const AmgNns
         gp32 = np32;
         gj = nj;
     }
-    std::vector<uint32_t> hsp32(ng + 1);
-    DEV_TRY(cudaMemcpyAsync(hsp32.data(), gp32, (ng + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     rc = read_status(ctx, d_status, &st);
     if (rc) return rc;
     if (st & kStOverflow) { *handoff = true; tm.handoff = nns ? 2 : 1; return FGPU_OK; }
     tm.graph += ms_since(tphase);
     tphase = clock::now();
-    // greedy aggregation on the host; its first pass follows the graph's copy in chunks of rows
-    std::unique_ptr<int32_t[]> hsj(new int32_t[std::max<uint64_t>(ngj, 1)]);
-    std::atomic<int64_t> rows_ready{0};
-    std::atomic<int> copy_failed{0};
-    cudaError_t copy_err = cudaSuccess;
-    std::thread copier([&] {
-        cudaSetDevice(ctx->device);
-        constexpr uint32_t kChunk = 1u << 22;            // entries per copy
-        int64_t r = 0;
-        while (r < ng) {
-            const uint64_t target = (uint64_t)hsp32[r] + kChunk;
-            int64_t r1 = std::upper_bound(hsp32.begin() + r + 1, hsp32.end(), target,
-                                          [](uint64_t t, uint32_t x) { return t < (uint64_t)x; }) - hsp32.begin() - 1;
-            r1 = std::min<int64_t>(ng, std::max<int64_t>(r1, r + 1));
-            const uint32_t b = hsp32[r], e = hsp32[r1];
-            if (e > b) {
-                copy_err = cudaMemcpyAsync(hsj.get() + b, gj + b, (size_t)(e - b) * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
-                if (copy_err == cudaSuccess) copy_err = cudaStreamSynchronize(ctx->stream);
-                if (copy_err != cudaSuccess) { copy_failed.store(1, std::memory_order_release); return; }
-            }
-            rows_ready.store(r1, std::memory_order_release);
-            r = r1;
-        }
-    });
-    std::vector<int32_t> agg_node;
-    const int64_t nagg = amg_aggregate_streamed(ng, hsp32.data(), hsj.get(), rows_ready, copy_failed, nns ? agg_node : L.agg);
-    copier.join();
-    if (copy_err != cudaSuccess || nagg < 0) {
-        ctx->err = std::string("gamg device set-up: graph copy: ") + cudaGetErrorString(copy_err);
-        return FGPU_ERR_CUDA;
+    // aggregation: rounds of the distance-2 independent set, then the two assignment steps
+    int8_t* mstate = w.get<int8_t>(ng);
+    int8_t* mnext = w.get<int8_t>(ng);
+    uint64_t* m1 = w.get<uint64_t>(ng);
+    uint8_t* r1 = w.get<uint8_t>(ng);
+    unsigned long long* dund = w.get<unsigned long long>(1);
+    uint32_t* rflag = w.get<uint32_t>(ng + 1);
+    uint32_t* rank = w.get<uint32_t>(ng + 1);
+    int32_t* a1 = w.get<int32_t>(ng);
+    int32_t* dagg_node = w.get<int32_t>(ng);
+    DEV_ALLOC(mstate && mnext && m1 && r1 && dund && rflag && rank && a1 && dagg_node);
+    const int gg = grid_rows(ng, 256);
+    const int gm = grid_rows(ng, 256 / kMisLanes, 152 * 16);
+    mis_init_kernel<<<gg, 256, 0, ctx->stream>>>(ng, gp32, mstate);
+    ctx->launches++;
+    for (int round = 0;; ++round) {
+        if (round > 1000) { ctx->err = "gamg device set-up: aggregation did not converge"; return FGPU_ERR_INVALID; }
+        DEV_TRY(cudaMemsetAsync(dund, 0, sizeof(unsigned long long), ctx->stream));
+        mis_pass1_kernel<<<gm, 256, 0, ctx->stream>>>(ng, gp32, gj, mstate, m1, r1);
+        mis_pass2_kernel<<<gm, 256, 0, ctx->stream>>>(ng, gp32, gj, mstate, m1, r1, mnext, dund);
+        ctx->launches += 2;
+        std::swap(mstate, mnext);
+        unsigned long long hund = 0;
+        DEV_TRY(cudaMemcpyAsync(&hund, dund, sizeof(hund), cudaMemcpyDeviceToHost, ctx->stream));
+        DEV_TRY(cudaStreamSynchronize(ctx->stream));
+        if (hund == 0) break;
     }
+    mis_root_flag_kernel<<<gg, 256, 0, ctx->stream>>>(ng, mstate, rflag);
+    ctx->launches++;
+    uint64_t nroots = 0;
+    rc = scan_u32(ctx, rflag, rank, ng, &nroots);
+    if (rc) return rc;
+    mis_assign1_kernel<<<gg, 256, 0, ctx->stream>>>(ng, gp32, gj, mstate, rank, a1);
+    mis_assign2_kernel<<<gg, 256, 0, ctx->stream>>>(ng, gp32, gj, mstate, a1, dagg_node);
+    ctx->launches += 2;
+    const int64_t nagg = (int64_t)nroots;
+    std::vector<int32_t> agg_node;
+    std::vector<int32_t>& hagg = nns ? agg_node : L.agg;
+    hagg.resize(ng);
+    DEV_TRY(cudaMemcpyAsync(hagg.data(), dagg_node, ng * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    DEV_TRY(cudaStreamSynchronize(ctx->stream));
     tm.aggregate += ms_since(tphase);
     tphase = clock::now();
     if (nagg == 0 || nagg >= ng) { *handoff = true; tm.handoff = 3; return FGPU_OK; }
@@ -1023,18 +1155,16 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, const AmgNns
         }
         DEV_TRY(cudaStreamSynchronize(ctx->stream));            // hP0 is freed on leaving this block
     } else {
-    // tentative prolongator and A P0
-    std::vector<double> sz(nagg, 0.0), hs0(nagg);
-    for (int64_t i = 0; i < n; ++i)
-        if (L.agg[i] >= 0) sz[L.agg[i]] += 1.0;
-    for (int64_t c = 0; c < nagg; ++c) hs0[c] = 1.0 / std::sqrt(sz[c]);
-    int32_t* dagg = w.get<int32_t>(n);
+    // tentative prolongator (1/sqrt(|agg|), the host's 1.0 / std::sqrt of the exact size) and A P0
+    const int32_t* dagg = dagg_node;
+    unsigned int* dsz = w.get<unsigned int>(nagg);
     double* ds0 = w.get<double>(nagg);
-    DEV_ALLOC(dagg && ds0);
-    DEV_TRY(cudaMemcpyAsync(dagg, L.agg.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    DEV_TRY(cudaMemcpyAsync(ds0, hs0.data(), nagg * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    DEV_ALLOC(dsz && ds0);
+    DEV_TRY(cudaMemsetAsync(dsz, 0, nagg * sizeof(unsigned int), ctx->stream));
+    agg_size_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, dagg, dsz);
+    agg_scale_kernel<<<grid_rows(nagg, 256), 256, 0, ctx->stream>>>(nagg, dsz, ds0);
     p0_count_kernel<<<grid_rows(n, 256), 256, 0, ctx->stream>>>(n, dagg, cnt);
-    ctx->launches++;
+    ctx->launches += 3;
     uint64_t n0 = 0;
     rc = scan_u32(ctx, cnt, tp, n, &n0);
     if (rc) return rc;

@@ -10,9 +10,9 @@
 //   1. strength graph: j is a strong neighbour of i when
 //      |a_ij| > theta sqrt(|a_ii a_jj|) (theta = 0: every stored coupling),
 //      symmetrised;
-//   2. greedy aggregation in three passes (root aggregates of whole free
-//      neighbourhoods; leftovers join a neighbouring root aggregate; the rest
-//      form aggregates of their free neighbourhoods); nodes without strong
+//   2. aggregation: roots form a maximal distance-2 independent set (rounds
+//      with hashed priorities, order-independent), their neighbours join them,
+//      the other nodes join a neighbouring aggregate; nodes without strong
 //      neighbours (rows eliminated by on(), decoupled) are left out: their
 //      prolongator rows are zero and the smoother solves them exactly;
 //   3. tentative prolongator: P0(i, agg(i)) = 1/sqrt(|agg|) (the constant near
@@ -147,7 +147,7 @@ double lmax_estimate(const HostCsr& A, const std::vector<double>& d, int m, int 
     std::vector<double> al, be;
     double bprev = 0;
     const int T = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads, (n + 4095) / 4096));
-    constexpr int64_t kChunk = 16384;
+    constexpr int64_t kChunk = 1024;
     const int64_t nch = (n + kChunk - 1) / kChunk;
     std::vector<double> pa(nch), pb(nch);
     for (int k = 0; k < m; ++k) {
@@ -251,46 +251,89 @@ void strength(const HostCsr& A, const std::vector<double>& d, double theta, std:
     });
 }
 
-// greedy aggregation; returns the number of aggregates, agg[i] = -1 for nodes left out. Every pass
-// visits the rows in order and reads only the visited row's neighbour list, so the first pass can run
-// while the lists are still arriving: ready(r) returns once rows [0, r) are present (false: they never
-// will be, and the aggregation returns -1).
-template <typename Off, typename Ready>
-int64_t aggregate_rows(int64_t n, const Off* sp, const int32_t* sj, std::vector<int32_t>& agg, Ready ready) {
+// Aggregation (returns the number of aggregates; agg[i] = -1 for nodes without strong neighbours):
+//   1. roots: a maximal distance-2 independent set (no two roots within two edges), found in rounds: an
+//      undecided node becomes a root when its key is the largest among the undecided nodes within
+//      distance 2 and no root lies within distance 2 of it; a node with a root within distance 2 is
+//      out. Keys: a hash of the node index in the high 32 bits, the index in the low ones (distinct);
+//   2. a root's neighbours join its aggregate (a node has at most one root neighbour);
+//   3. every other coupled node (within distance 2 of a root, as the set is maximal) joins the
+//      aggregate of its first neighbour, in column order, that step 2 aggregated.
+// Aggregates are numbered by root index. Every step reads the previous step's arrays only, so the
+// result does not depend on the order in which nodes are visited: the device set-up runs the same
+// rounds as kernels and gets the same aggregates.
+void aggregate_mis2(int64_t n, const int64_t* sp, const int32_t* sj, std::vector<int32_t>& agg, int nthreads) {
+    std::vector<int8_t> state(n), nstate(n);     // 0 undecided, 1 root, 2 out, 3 no strong neighbours
+    std::vector<uint64_t> m1(n);
+    std::vector<uint8_t> r1(n);
+    int64_t undecided = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        state[i] = sp[i + 1] > sp[i] ? 0 : 3;
+        undecided += state[i] == 0;
+    }
+    while (undecided > 0) {
+        parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1_) {
+            for (int64_t i = r0; i < r1_; ++i) {
+                uint64_t m = state[i] == 0 ? amg_mis_key(i) : 0;
+                uint8_t r = state[i] == 1;
+                for (int64_t q = sp[i]; q < sp[i + 1]; ++q) {
+                    const int32_t j = sj[q];
+                    if (state[j] == 0) m = std::max(m, amg_mis_key(j));
+                    r |= state[j] == 1;
+                }
+                m1[i] = m;
+                r1[i] = r;
+            }
+        });
+        std::vector<int64_t> cnt(std::max(1, nthreads), 0);
+        parallel_rows(nthreads, n, [&](int t, int64_t r0, int64_t r1_) {
+            int64_t c = 0;
+            for (int64_t i = r0; i < r1_; ++i) {
+                nstate[i] = state[i];
+                if (state[i] != 0) continue;
+                uint64_t m = m1[i];
+                uint8_t r = r1[i];
+                for (int64_t q = sp[i]; q < sp[i + 1]; ++q) {
+                    m = std::max(m, m1[sj[q]]);
+                    r |= r1[sj[q]];
+                }
+                if (r) nstate[i] = 2;
+                else if (m == amg_mis_key(i)) nstate[i] = 1;
+                else ++c;
+            }
+            cnt[t] += c;
+        });
+        state.swap(nstate);
+        undecided = 0;
+        for (int64_t c : cnt) undecided += c;
+    }
+    std::vector<int32_t> rank(n, -1);
+    int32_t nroots = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (state[i] == 1) rank[i] = nroots++;
+    std::vector<int32_t> a1(n, -1);
+    parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1_) {
+        for (int64_t i = r0; i < r1_; ++i) {
+            if (state[i] == 1) { a1[i] = rank[i]; continue; }
+            for (int64_t q = sp[i]; q < sp[i + 1]; ++q)
+                if (state[sj[q]] == 1) { a1[i] = rank[sj[q]]; break; }
+        }
+    });
     agg.assign(n, -1);
-    int64_t nagg = 0;
-    constexpr int64_t kStep = 4096;
-    // pass 1: roots whose whole strong neighbourhood is free
-    for (int64_t i = 0; i < n; ++i) {
-        if (i % kStep == 0 && !ready(std::min(n, i + kStep))) return -1;
-        if (agg[i] != -1 || sp[i + 1] == sp[i]) continue;
-        bool free = true;
-        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1] && free; ++q) free = agg[sj[q]] == -1;
-        if (!free) continue;
-        agg[i] = (int32_t)nagg;
-        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1]; ++q) agg[sj[q]] = (int32_t)nagg;
-        ++nagg;
-    }
-    // pass 2: free nodes join the aggregate of their first aggregated neighbour (pass-1 state)
-    std::vector<int32_t> snap(agg);
-    for (int64_t i = 0; i < n; ++i) {
-        if (snap[i] != -1 || sp[i + 1] == sp[i]) continue;
-        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1]; ++q)
-            if (snap[sj[q]] != -1) { agg[i] = snap[sj[q]]; break; }
-    }
-    // pass 3: the rest form aggregates with their free neighbours
-    for (int64_t i = 0; i < n; ++i) {
-        if (agg[i] != -1 || sp[i + 1] == sp[i]) continue;
-        agg[i] = (int32_t)nagg;
-        for (int64_t q = sp[i]; q < (int64_t)sp[i + 1]; ++q)
-            if (agg[sj[q]] == -1) agg[sj[q]] = (int32_t)nagg;
-        ++nagg;
-    }
-    return nagg;
+    parallel_rows(nthreads, n, [&](int, int64_t r0, int64_t r1_) {
+        for (int64_t i = r0; i < r1_; ++i) {
+            if (a1[i] >= 0 || state[i] == 3) { agg[i] = a1[i]; continue; }
+            for (int64_t q = sp[i]; q < sp[i + 1]; ++q)
+                if (a1[sj[q]] >= 0) { agg[i] = a1[sj[q]]; break; }
+        }
+    });
 }
 
-int64_t aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg) {
-    return aggregate_rows(n, sp.data(), sj.data(), agg, [](int64_t) { return true; });
+int64_t aggregate(int64_t n, const std::vector<int64_t>& sp, const std::vector<int32_t>& sj, std::vector<int32_t>& agg, int nthreads) {
+    aggregate_mis2(n, sp.data(), sj.data(), agg, nthreads);
+    int64_t nagg = 0;
+    for (int64_t i = 0; i < n; ++i) nagg = std::max<int64_t>(nagg, agg[i] + 1);
+    return nagg;
 }
 
 // P0(i, agg(i)) = 1/sqrt(|agg|): the constant near null space
@@ -435,16 +478,6 @@ double amg_tridiag_lmax(const std::vector<double>& al, const std::vector<double>
     return hi > 0 ? hi : 1.0;
 }
 
-int64_t amg_aggregate_streamed(int64_t n, const uint32_t* sp, const int32_t* sj, const std::atomic<int64_t>& rows_ready,
-                               const std::atomic<int>& failed, std::vector<int32_t>& agg) {
-    return aggregate_rows(n, sp, sj, agg, [&](int64_t r) {
-        while (rows_ready.load(std::memory_order_acquire) < r) {
-            if (failed.load(std::memory_order_acquire)) return false;
-            std::this_thread::yield();
-        }
-        return !failed.load(std::memory_order_acquire);
-    });
-}
 
 // node layout and storage of a near null space (values filled by the caller); nonzero when invalid
 int amg_nns_layout(const fgpu_amg_cfg* cfg, int64_t n, AmgNns& nns) {
@@ -634,7 +667,7 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
         AmgNns next;
         int64_t nagg = 0;
         if (!nns) {
-            nagg = aggregate(A.nrows, sp, sj, L.agg);
+            nagg = aggregate(A.nrows, sp, sj, L.agg, nthreads);
             if (nagg == 0 || nagg >= A.nrows) break;          // nothing to coarsen
             tentative_constant(A.nrows, L.agg, nagg, P0);
         } else {
@@ -642,7 +675,7 @@ bool amg_build_host(HostCsr&& A0, const AmgHostCfg& cfg, AmgHierarchy& H, std::s
             std::vector<int32_t> nj, agg_node;
             amg_collapse_graph(cur.node_ptr, sp, sj.data(), nthreads, np, nj);
             const int64_t nn = (int64_t)cur.node_ptr.size() - 1;
-            nagg = aggregate(nn, np, nj, agg_node);
+            nagg = aggregate(nn, np, nj, agg_node, nthreads);
             if (nagg == 0 || nagg >= nn) break;
             if (amg_tentative_nns(cur, agg_node, nagg, nthreads, P0, next)) { err = "gamg: coarse level too large"; return false; }
             if (P0.ncols == 0 || P0.ncols >= A.nrows) break;

@@ -132,10 +132,14 @@ int amg_tentative_nns(const AmgNns& nns, const std::vector<int32_t>& agg_node, i
 AmgHostCfg amg_host_cfg(const fgpu_amg_cfg* cfg, int nthreads);
 int amg_nns_layout(const fgpu_amg_cfg* cfg, int64_t n, AmgNns& nns);
 // pieces of the host set-up shared with the device set-up (amg_dev.cu)
-// the host set-up's greedy aggregation over a graph copied in row order: rows [0, rows_ready) present;
-// returns -1 when `failed` is raised before all rows arrive
-int64_t amg_aggregate_streamed(int64_t n, const uint32_t* sp, const int32_t* sj, const std::atomic<int64_t>& rows_ready,
-                               const std::atomic<int>& failed, std::vector<int32_t>& agg);
+// key of a node in the aggregation's independent-set rounds: a hash of the index above the index
+__host__ __device__ inline uint64_t amg_mis_key(int64_t i) {
+    uint64_t z = (uint64_t)i + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return ((z >> 32) << 32) | (uint64_t)(uint32_t)i;
+}
 void amg_lanczos_start(int64_t n, std::vector<double>& v);
 double amg_tridiag_lmax(const std::vector<double>& al, const std::vector<double>& be);
 
@@ -161,7 +165,7 @@ struct AmgDevLevel {
 };
 struct AmgSetupTimes {                // wall times of the set-up phases (ms), summed over the levels
     double graph = 0;                // diagonal, strength graph and its copy to the host
-    double aggregate = 0;            // greedy aggregation (host)
+    double aggregate = 0;            // aggregation
     double lanczos = 0;              // lambda_max estimate
     double prolong = 0;              // P0, A P0, P, R = P^T
     double galerkin = 0;             // A P and R (A P)
