@@ -134,7 +134,9 @@ __global__ void strong_kernel(int64_t n, const int64_t* __restrict__ ia, const i
             const int32_t j = ja[p];
             const double v = a[p];
             if (j == i || v == 0.0) continue;
-            if (fabs(v) > theta * sqrt(fabs(__dmul_rn(d[i], d[j])))) {
+            // theta = 0 (the default): every nonzero coupling is strong (0 * sqrt of the positive, finite
+            // diagonal product is 0), without the diagonal loads and the square root
+            if (theta == 0.0 || fabs(v) > theta * sqrt(fabs(__dmul_rn(d[i], d[j])))) {
                 if (out) out[off[i] + k] = j;
                 ++k;
             }
