@@ -885,8 +885,8 @@ def run_matfree(args):
     for name, prec, tc in [("f32_tensor_cores", "f32", True), ("f32_cuda_cores", "f32", False),
                            ("f32_colour_scatter", "f32", False), ("df64", "df64", False), ("f64", "f64", False)]:
         op = fpp.operator(V, integral, precision=prec)
-        if tc:
-            op.use_tensor_cores(True)
+        if prec == "f32" and name != "f32_colour_scatter":
+            op.use_tensor_cores(tc)
         if name == "f32_colour_scatter":
             op.set_algo("colour")
         op.set_dirichlet(bd)

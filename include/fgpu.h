@@ -420,7 +420,8 @@ int fgpu_operator_set_dirichlet(fgpu_operator* op, int64_t ndofs, const int32_t*
 int fgpu_operator_apply(fgpu_ctx* ctx, fgpu_operator* op, const fgpu_vector* x, fgpu_vector* y);
 int fgpu_operator_destroy(fgpu_operator* op);
 /* run the binary32 element phase on the tensor cores (tcgen05.mma kind::tf32, 3xTF32 split,
- * accumulator in tensor memory); P2 / P3 binary32 operators */
+ * accumulator in tensor memory); P2 / P3 binary32 operators (default: on for P3, off for P2, the
+ * faster of the two for each order) */
 int fgpu_operator_set_tensor_cores(fgpu_operator* op, int on);
 /* binary32 operators: FGPU_ALGO_GATHER (element buffer, then one node-ordered gather; default) or
  * FGPU_ALGO_COLOUR (elements coloured so that a colour shares no vertex, one launch per colour
