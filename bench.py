@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-extras", action="store_true", help="skip the P3 / streamed / Poisson-error / p-multigrid extras")
     p.add_argument("--pmg-n", type=int, default=96, help="extras: mesh of the config-5 p-multigrid solve (0: skip)")
     p.add_argument("--elasticity-n", type=int, default=48, help="extras: mesh of the config-3 elasticity beam (0: skip)")
+    p.add_argument("--no-config4", action="store_true",
+                   help="extras: skip the config-4 batch (512 uneven problems) and the P2 heat time loop")
     p.add_argument("--nprob", type=int, default=512, help="batch: number of independent problems")
     p.add_argument("--nmax", type=int, default=40, help="batch: largest cube resolution")
     p.add_argument("--heat-steps", type=int, default=100, help="heat: backward-Euler steps")
@@ -674,6 +676,16 @@ def run_gb300(args, rank, world, local):
             extras["config5_pmg_p3"] = extra_pmg(fpp, _ffi, fe, args.pmg_n, local)
         if args.elasticity_n > 0:
             extras["config3_elasticity_p2"] = extra_elasticity(fpp, None, args.elasticity_n, local)
+        if not args.no_config4 and world == 1:
+            # the config-4 workloads on this process's GPU, each on its own stream and environment
+            prev = torch.cuda.current_stream()
+            a4 = argparse.Namespace(**vars(args))
+            a4.steps, a4.warmup, a4.nprob, a4.nmax = 10, 3, 512, 40
+            extras["config4_batch"] = run_batch(a4, emit=False)
+            a5 = argparse.Namespace(**vars(args))
+            a5.n, a5.heat_steps = 64, 100
+            extras["config4_heat"] = run_heat(a5, emit=False, jacobi=False)
+            torch.cuda.set_stream(prev)
     if rank != 0:
         return
     cpu = None
@@ -1104,7 +1116,7 @@ def run_elasticity(args):
     print(json.dumps(out), flush=True)
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     """Independent Poisson problems (cube resolution n ~ U{8..nmax}, order ~ U{1,2,3},
     lognormal kappa, all seeded) assembled in FP64 by one geometry launch and one
     persistent gather launch; compared with a loop of per-problem assemblies and
@@ -1197,7 +1209,9 @@ def run_batch(args):
            "loop_of_single_assemblies": {"ms_per_step": ms_loop, "host_wall_ms": wall_loop,
                                          "launches_per_step": 2 * args.nprob},
            "graph_replay_ms_per_step": ms_graph, "setup_s": setup_s, "clocks": clk.summary()}
-    print(json.dumps(out), flush=True)
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def run_curved(args):
@@ -1321,7 +1335,7 @@ def run_hex(args):
     print(json.dumps(res), flush=True)
 
 
-def run_heat(args):
+def run_heat(args, emit=True, jacobi=True):
     """P2 heat equation on the 64^3 Kuhn cube: backward Euler, (M + dt kappa(t) K) u^{n+1}
     = M u^n + dt F with kappa(t) = 1 + 0.5 sin t and homogeneous Dirichlet rows. Each step
     replays one captured CUDA graph (reassembly, right-hand side, Dirichlet rows) after
@@ -1381,24 +1395,28 @@ def run_heat(args):
     torch.cuda.synchronize()
     ms_eager = e0.elapsed_time(e1) / 20
     wall_eager = (time.perf_counter() - t0) / 20 * 1e3
-    # the time loop
-    un.zero()
-    its, solve_ms = [], []
-    with ClockSampler(0) as clk:
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k in range(args.heat_steps):
-            kt.set(1.0 + 0.5 * math.sin((k + 1) * dt))
-            g.launch()
-            st = A.solve(rhs=b, solution=un, rtol=1e-10)
-            its.append(st["iterations"])
-            solve_ms.append(st["time_ms"])
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    l2, h1 = un.errors_sine(4)
+    # the time loop with Jacobi-preconditioned CG
+    time_loop, x1, clk = None, None, None
+    if jacobi:
+        un.zero()
+        its, solve_ms = [], []
+        with ClockSampler(0) as clk:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(args.heat_steps):
+                kt.set(1.0 + 0.5 * math.sin((k + 1) * dt))
+                g.launch()
+                st = A.solve(rhs=b, solution=un, rtol=1e-10)
+                its.append(st["iterations"])
+                solve_ms.append(st["time_ms"])
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        l2, h1 = un.errors_sine(4)
+        time_loop = {"wall_s": wall, "cg_iterations_mean": float(np.mean(its)), "cg_ms_mean": float(np.mean(solve_ms)),
+                     "final_l2_norm_diff_to_sine": l2, "pc": "jacobi"}
+        x1 = un.to_numpy()
     # the same time loop with CG + AMG, the hierarchy built at the first step and kept (the V-cycle
     # acts with the first step's operator, the CG with each step's); the captured step reads un
-    x1 = un.to_numpy()
     un.zero()
     its2, solve_ms2 = [], []
     with ClockSampler(0) as clk2:
@@ -1412,7 +1430,13 @@ def run_heat(args):
             solve_ms2.append(st["time_ms"])
         torch.cuda.synchronize()
         wall2 = time.perf_counter() - t0
+    l2g, _ = un.errors_sine(4)
     x2 = un.to_numpy()
+    gamg_loop = {"wall_s": wall2, "cg_iterations_mean": float(np.mean(its2)),
+                 "cg_ms_mean": float(np.mean(solve_ms2)), "pc": "gamg, hierarchy of the first step kept",
+                 "final_l2_norm_diff_to_sine": l2g, "clocks": clk2.summary()}
+    if x1 is not None:
+        gamg_loop["final_solution_rel_diff_vs_jacobi"] = float(np.linalg.norm(x2 - x1) / np.linalg.norm(x1))
     out = {"metric": "P2 heat equation: graph-replayed reassembly ms/step and backward-Euler s/100 steps",
            "value": ms_graph, "unit": "ms/reassembly", "n_gpus": 1, "steps": args.heat_steps,
            "higher_is_better": False, "dtype": "f64", "data": "synthetic",
@@ -1420,14 +1444,11 @@ def run_heat(args):
                       % (n, len(tets), V.ndof, A.nnz, dt)},
            "reassembly": {"graph_ms": ms_graph, "eager_ms": ms_eager, "eager_host_wall_ms": wall_eager,
                           "mnnz_per_s_graph": A.nnz / (ms_graph / 1e3) / 1e6},
-           "time_loop": {"wall_s": wall, "cg_iterations_mean": float(np.mean(its)), "cg_ms_mean": float(np.mean(solve_ms)),
-                         "final_l2_norm_diff_to_sine": l2, "pc": "jacobi"},
-           "time_loop_gamg_kept": {"wall_s": wall2, "cg_iterations_mean": float(np.mean(its2)),
-                                   "cg_ms_mean": float(np.mean(solve_ms2)), "pc": "gamg, hierarchy of the first step kept",
-                                   "final_solution_rel_diff_vs_jacobi": float(np.linalg.norm(x2 - x1) / np.linalg.norm(x1)),
-                                   "clocks": clk2.summary()},
-           "clocks": clk.summary()}
-    print(json.dumps(out), flush=True)
+           "time_loop": time_loop, "time_loop_gamg_kept": gamg_loop,
+           "clocks": clk.summary() if clk is not None else None}
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def main():
