@@ -14,6 +14,7 @@ F64, F32, DF64 = 0, 1, 2
 FORM_LAPLACE_MASS, FORM_ELASTICITY = 0, 1
 RANGE_ELEMENTS, RANGE_BOUNDARY_FACES, RANGE_MARKED_FACES = 0, 1, 2
 ALGO_AUTO, ALGO_GATHER, ALGO_COLOUR, ALGO_GATHER_NATIVE_F64, ALGO_TWO_PHASE, ALGO_STREAMED = 0, 1, 2, 3, 4, 5
+TC_F32, TC_DF64 = 1, 2
 HOST_TRANSFER_AUTO, HOST_TRANSFER_COPY, HOST_TRANSFER_DIRECT = 0, 1, 2
 RHS_SINE, RHS_CONST_VEC, RHS_CONST, RHS_FACE = 0, 1, 2, 3
 ON_ELIMINATION, ON_ELIMINATION_SYMMETRIC, ON_ELIMINATION_KEEP_DIAGONAL = 0, 1, 2

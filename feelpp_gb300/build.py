@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
-SOURCES = ["basis.cpp", "topology.cpp", "assemble.cu", "solve.cu", "matfree.cu", "matfree_tc.cu", "api.cu", "noalloc.cu", "batch.cu", "topology_dev.cu", "faces.cu", "amg_setup.cpp", "amg.cu", "amg_dev.cu", "ho.cu", "pmg.cu", "export.cpp", "hex.cpp", "gmres.cu", "stream_asm.cu", "refine.cu", "tune.cpp"]
+SOURCES = ["basis.cpp", "topology.cpp", "assemble.cu", "solve.cu", "matfree.cu", "matfree_tc.cu", "api.cu", "noalloc.cu", "batch.cu", "topology_dev.cu", "faces.cu", "amg_setup.cpp", "amg.cu", "amg_dev.cu", "ho.cu", "pmg.cu", "export.cpp", "hex.cpp", "gmres.cu", "stream_asm.cu", "refine.cu", "tune.cpp", "element_tc.cu"]
 
 
 def _digest(paths):

@@ -698,9 +698,9 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     return assemble_impl(ctx, A, f, A->d_kappa_stage, accumulate);
 }
 
-int fgpu_set_tensor_cores(fgpu_ctx* ctx, int on) {
-    if (!ctx) return FGPU_ERR_INVALID;
-    ctx->tensor_cores = on ? 1 : 0;
+int fgpu_set_tensor_cores(fgpu_ctx* ctx, int mask) {
+    if (!ctx || (mask & ~(FGPU_TC_F32 | FGPU_TC_DF64))) return FGPU_ERR_INVALID;
+    ctx->tensor_cores = mask;
     return FGPU_OK;
 }
 

@@ -1379,7 +1379,14 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
 // more than 6 contributions (the vertex-row diagonals, 0.5 % of the entries) left
 // to a second kernel over their list: timed by the tuner against B = 2, 4, 8 and
 // never picked at P2 or P3 64^3 (the warps' longest entries are not what bounds
-// the kernel).
+// the kernel). L2 eviction hints (map and values evict-first, element buffer
+// evict-last) raised the DRAM reads at P2 48^3 from 900 to 1010 MB and the time
+// from 0.275 to 0.295 ms. The grid matters for the reads: with more blocks than
+// fit at once, each wave of resident blocks strides over the whole matrix and an
+// entry and its transpose are read in different waves (900 MB); one entry per
+// thread sweeps the entries in order and reads exactly the design bytes (660 MB)
+// but took 0.30 ms: the kernel is bound by issue and by the latency of its three
+// dependent loads, not by DRAM.
 template <int MODE, int B = 4>
 __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
                                                          const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
@@ -1430,6 +1437,120 @@ __global__ void __launch_bounds__(256) gather_map_kernel(int64_t nnz, const uint
             float* out = reinterpret_cast<float*>(valv) + k;
             *out = accumulate ? f_add(*out, s) : s;
         }
+    }
+}
+
+// The same gather software-pipelined over a thread's grid-stride entries. One entry costs three
+// dependent loads (its gptr range, then its gidx indices, then the element-buffer values), so the
+// plain kernel keeps one round trip of DRAM latency per load level in flight per thread. Here
+// iteration i issues the element-buffer loads of entry k (indices already in registers), the gidx
+// loads of entry k + S and the gptr loads of entry k + 2S together, then sums entry k: one latency
+// per entry instead of three. Entries with more than B contributions load their further batches
+// in place. The sum of every entry is the same sequence of operations as in gather_map_kernel, so
+// the values are the same bits. Measured at 64^3 (tuned shapes): binary32 P3 1.87 against 2.12 ms,
+// P2 0.43 against 0.46 ms; df64 P2 0.66 against 0.64 ms (more registers, and the three entries in
+// flight widen the window of element-buffer lines: 880 against 803 MB of DRAM reads at 48^3). The
+// tuner times both.
+template <int MODE, int B = 4>
+__global__ void __launch_bounds__(256) gather_map_pipe_kernel(int64_t nnz, const uint32_t* __restrict__ gptr,
+                                                              const uint32_t* __restrict__ gidx, const void* __restrict__ kbuf,
+                                                              void* __restrict__ valv, int accumulate, double* __restrict__ hout) {
+    const int64_t S = (int64_t)gridDim.x * blockDim.x;
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    uint32_t a0 = __ldg(gptr + k), a1 = __ldg(gptr + k + 1);          // entry k
+    int64_t kn = k + S;
+    uint32_t b0 = 0, b1 = 0;                                            // entry k + S
+    if (kn < nnz) {
+        b0 = __ldg(gptr + kn);
+        b1 = __ldg(gptr + kn + 1);
+    }
+    uint32_t ix[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) ix[u] = a0 + u < a1 ? __ldg(gidx + a0 + u) : 0u;
+    for (;;) {
+        // loads of three entries in flight together
+        uint32_t nx[B];
+        uint32_t c0 = 0, c1 = 0;
+        const int64_t knn = kn + S;
+        if (MODE == kModeDF64) {
+            const float2* kb = reinterpret_cast<const float2*>(kbuf);
+            float2 v[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) v[u] = a0 + u < a1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int u = 0; u < B; ++u) nx[u] = b0 + u < b1 ? __ldg(gidx + b0 + u) : 0u;
+            if (knn < nnz) {
+                c0 = __ldg(gptr + knn);
+                c1 = __ldg(gptr + knn + 1);
+            }
+            float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (a0 + u < a1) {
+                    const df t = two_sum(sh, v[u].x);
+                    sh = t.hi;
+                    sl = f_add(sl, f_add(t.lo, v[u].y));
+                }
+            for (uint32_t p = a0 + B; p < a1; p += B) {
+                uint32_t jx[B];
+                float2 w[B];
+#pragma unroll
+                for (int u = 0; u < B; ++u) jx[u] = p + u < a1 ? __ldg(gidx + p + u) : 0u;
+#pragma unroll
+                for (int u = 0; u < B; ++u) w[u] = p + u < a1 ? __ldg(kb + (jx[u] & 0x7FFFFFFFu)) : make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int u = 0; u < B; ++u)
+                    if (p + u < a1) {
+                        const df t = two_sum(sh, w[u].x);
+                        sh = t.hi;
+                        sl = f_add(sl, f_add(t.lo, w[u].y));
+                    }
+            }
+            df sum = two_sum(sh, sl);
+            double* out = reinterpret_cast<double*>(valv) + k;
+            if (accumulate) sum = df_add(d2df(*out), sum);
+            const double r = df2d(sum);
+            *out = r;
+            if (hout) hout[k] = r;
+        } else {
+            const float* kb = reinterpret_cast<const float*>(kbuf);
+            float v[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) v[u] = a0 + u < a1 ? __ldg(kb + (ix[u] & 0x7FFFFFFFu)) : 0.0f;
+#pragma unroll
+            for (int u = 0; u < B; ++u) nx[u] = b0 + u < b1 ? __ldg(gidx + b0 + u) : 0u;
+            if (knn < nnz) {
+                c0 = __ldg(gptr + knn);
+                c1 = __ldg(gptr + knn + 1);
+            }
+            float sum = 0.0f;
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (a0 + u < a1) sum = (u == 0) ? v[u] : f_add(sum, v[u]);
+            for (uint32_t p = a0 + B; p < a1; p += B) {
+                uint32_t jx[B];
+                float w[B];
+#pragma unroll
+                for (int u = 0; u < B; ++u) jx[u] = p + u < a1 ? __ldg(gidx + p + u) : 0u;
+#pragma unroll
+                for (int u = 0; u < B; ++u) w[u] = p + u < a1 ? __ldg(kb + (jx[u] & 0x7FFFFFFFu)) : 0.0f;
+#pragma unroll
+                for (int u = 0; u < B; ++u)
+                    if (p + u < a1) sum = f_add(sum, w[u]);
+            }
+            float* out = reinterpret_cast<float*>(valv) + k;
+            *out = accumulate ? f_add(*out, sum) : sum;
+        }
+        if (kn >= nnz) break;
+        k = kn;
+        kn = knn;
+        a0 = b0;
+        a1 = b1;
+        b0 = c0;
+        b1 = c1;
+#pragma unroll
+        for (int u = 0; u < B; ++u) ix[u] = nx[u];
     }
 }
 
@@ -1541,7 +1662,7 @@ int launch_build_gather_map(fgpu_ctx* ctx, fgpu_space* V) {
 // Launch shape of the two-phase kernels: threads per block and blocks per SM of the element kernel
 // and of the gather, and the gather's contributions per load batch. None changes the values.
 struct TwoPhaseShape {
-    int el_threads = 256, el_bpsm = 16, g_threads = 256, g_bpsm = 32, g_batch = 4;
+    int el_threads = 256, el_bpsm = 16, g_threads = 256, g_bpsm = 32, g_batch = 4, g_pipe = 0;
 };
 
 template <int MODE, int N>
@@ -1560,6 +1681,14 @@ static void launch_gather_map(fgpu_ctx* ctx, fgpu_matrix* A, int sms, const TwoP
     const fgpu_space* V = A->space;
     const int64_t nnz = A->pattern->nnz;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((nnz + sh.g_threads - 1) / sh.g_threads, (int64_t)sms * sh.g_bpsm));
+    if (sh.g_pipe) {
+        switch (sh.g_batch) {
+            case 2: gather_map_pipe_kernel<MODE, 2><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
+            case 8: gather_map_pipe_kernel<MODE, 8><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
+            default: gather_map_pipe_kernel<MODE, 4><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
+        }
+        return;
+    }
     switch (sh.g_batch) {
         case 2: gather_map_kernel<MODE, 2><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
         case 8: gather_map_kernel<MODE, 8><<<(int)blocks, sh.g_threads, 0, ctx->stream>>>(nnz, V->d_gptr, V->d_gidx, A->d_kbuf, A->d_val, accumulate, hout); break;
@@ -1610,6 +1739,17 @@ static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, c
                 const float ms = median_ms(ctx, [&] { launch_gather_map<MODE>(ctx, A, sms, s, 0, nullptr); });
                 if (ms < best_ms) { best_ms = ms; best.g_threads = th; best.g_bpsm = bp; best.g_batch = b; }
             }
+    // the software-pipelined gather, its grid at most the resident blocks (a sweep over the entries)
+    for (int th : {128, 256})
+        for (int bp : {2, 4, 6, 8})
+            for (int b : {2, 4}) {
+                s.g_threads = th;
+                s.g_bpsm = bp * (256 / th);
+                s.g_batch = b;
+                s.g_pipe = 1;
+                const float ms = median_ms(ctx, [&] { launch_gather_map<MODE>(ctx, A, sms, s, 0, nullptr); });
+                if (ms < best_ms) { best_ms = ms; best.g_threads = th; best.g_bpsm = s.g_bpsm; best.g_batch = b; best.g_pipe = 1; }
+            }
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;
 }
@@ -1641,17 +1781,23 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     const std::string key = "two_phase|" + tune_device_key(ctx->device) + "|P" + std::to_string(V->order) + "|" +
                             (MODE == kModeDF64 ? "f64" : "f32") + "|n2^" + std::to_string(tune_size_class(nnz));
     std::vector<int> tv;
-    if (ctx->tune == 0 && tune_lookup(ctx->tune_file, key, tv) && tv.size() == 5) {
-        shape = TwoPhaseShape{tv[0], tv[1], tv[2], tv[3], tv[4]};
+    if (ctx->tune == 0 && tune_lookup(ctx->tune_file, key, tv) && (tv.size() == 5 || tv.size() == 6)) {
+        shape = TwoPhaseShape{tv[0], tv[1], tv[2], tv[3], tv[4], tv.size() == 6 ? tv[5] : 0};
     } else if (ctx->tune == 0 && !ctx->capturing && accumulate == 0 && !host) {
         int rc = tune_two_phase<MODE, N>(ctx, A, tab, rec, sms, shape);
         if (rc) return rc;
-        tune_record(ctx->tune_file, key, {shape.el_threads, shape.el_bpsm, shape.g_threads, shape.g_bpsm, shape.g_batch});
+        tune_record(ctx->tune_file, key, {shape.el_threads, shape.el_bpsm, shape.g_threads, shape.g_bpsm, shape.g_batch, shape.g_pipe});
     }
     {
         PendingEvent ev;
         prof_begin(ctx, "assemble_elements", ev);
-        launch_element_tri<MODE, N>(ctx, A, tab, rec, sms, shape);
+        if (MODE == kModeDF64 && (ctx->tensor_cores & FGPU_TC_DF64)) {
+            // the df64 element matrices on the tensor cores (bf16 slices, exact level sums)
+            const int rc = launch_element_tri_tc(ctx, V->order, nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
+            if (rc) return rc;
+        } else {
+            launch_element_tri<MODE, N>(ctx, A, tab, rec, sms, shape);
+        }
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     }

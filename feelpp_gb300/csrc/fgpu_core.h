@@ -225,7 +225,7 @@ struct fgpu_ctx {
     int host_transfer = 0;         // FGPU_HOST_TRANSFER_*: how results reach host buffers
     int tune = 0;                  // 0: time launch shapes on first use; -1: fixed default shapes
     std::string tune_file;         // cache file of the picks ("" = none)
-    int tensor_cores = 1;          // binary32 quadrature-form element matrices on tcgen05 (fgpu_set_tensor_cores)
+    int tensor_cores = FGPU_TC_F32; // element kernels on tcgen05 (fgpu_set_tensor_cores mask)
 };
 
 struct fgpu_graph {
@@ -345,7 +345,11 @@ enum StatusBits : int {
     kStatusMissingEntry = 4,   // an element column absent from its row (pattern mismatch)
     kStatusBreakdown = 8,      // CG breakdown (p.Ap <= 0)
     kStatusStreamTimeout = 256,// streamed assembly: a wait for another task gave up
+    kStatusOzTimeout = 1024,   // tensor-core df64 element kernel: a wait for its products gave up
 };
+
+// element_tc.cu: df64 element buffer of the affine Laplace/mass form on the tensor cores (orders 1-3)
+int launch_element_tri_tc(fgpu_ctx* ctx, int order, int64_t nt, const float4* rec, const float* Th, const float* Tl, void* kbuf);
 
 struct DevTables {                     // device copies of the reference tables
     int order = 0, n = 0, Q = 0, qdeg = 0;

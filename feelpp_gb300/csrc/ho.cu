@@ -773,7 +773,7 @@ int launch_assemble_hex(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, 
                                                                     T->d_dl, T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh,   \
                                                                     T->d_qwl, T->d_ti, T->d_tj, d_kappa, f->kappa, f->mass,    \
                                                                     f->kappa_scale, A->d_kbuf, ctx->d_status)
-    if (f32 && ctx->tensor_cores) {
+    if (f32 && (ctx->tensor_cores & FGPU_TC_F32)) {
         rc = V->n == 8 ? launch_ho_tc<8, 8>(ctx, A, T, d_kappa, f) : launch_ho_tc<27, 8>(ctx, A, T, d_kappa, f);
         if (rc) return rc;
     } else if (V->n == 8 && T->Q <= 8) {
@@ -849,7 +849,7 @@ int launch_assemble_ho(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f, c
                                                                 T->d_ph, T->d_pl, T->d_gdh, T->d_gdl, T->d_qwh, T->d_qwl,      \
                                                                 T->d_ti, T->d_tj, d_kappa,                                     \
                                                                 f->kappa, f->mass, f->kappa_scale, A->d_kbuf, ctx->d_status)
-    if (f32 && ctx->tensor_cores) {
+    if (f32 && (ctx->tensor_cores & FGPU_TC_F32)) {
         rc = V->n == 4 ? launch_ho_tc<4, 10>(ctx, A, T, d_kappa, f)
              : V->n == 10 ? launch_ho_tc<10, 10>(ctx, A, T, d_kappa, f) : launch_ho_tc<20, 10>(ctx, A, T, d_kappa, f);
         if (rc) return rc;

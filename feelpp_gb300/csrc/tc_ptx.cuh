@@ -1,6 +1,6 @@
-// tcgen05 / mbarrier helpers shared by the tensor-core kernels (matfree_tc.cu, ho.cu):
-// shared-memory matrix descriptors for K-major operands without swizzle (8-row x
-// 16-byte core matrices), the tf32 instruction descriptor, MMA issue and commit,
+// tcgen05 / mbarrier helpers shared by the tensor-core kernels (matfree_tc.cu, ho.cu,
+// element_tc.cu): shared-memory matrix descriptors for K-major operands without swizzle
+// (8-row x 16-byte core matrices), the tf32 and bf16 instruction descriptors, MMA issue and commit,
 // bounded mbarrier waits and tensor-memory loads.
 #pragma once
 #include <cstdint>
@@ -28,6 +28,11 @@ __host__ __device__ constexpr uint32_t make_idesc_tf32(int nmma) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(nmma >> 3) << 17) | ((uint32_t)(kTcTile >> 4) << 24);
 }
 
+// Instruction descriptor: D f32, A and B bf16 (kind::f16), both K-major, M = 128, N = nmma.
+__host__ __device__ constexpr uint32_t make_idesc_bf16(int nmma) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nmma >> 3) << 17) | ((uint32_t)(kTcTile >> 4) << 24);
+}
+
 __device__ __forceinline__ float tf32_hi(float x) {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
@@ -41,6 +46,13 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 

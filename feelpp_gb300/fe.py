@@ -49,10 +49,12 @@ class Environment:
     def launches(self):
         return int(self.lib.fgpu_launch_count(self.h))
 
-    def set_tensor_cores(self, on=True):
+    def set_tensor_cores(self, on=True, df64=False):
         """Binary32 quadrature-form element matrices (curved tetrahedra, hexahedra) on the tensor cores
-        (default) or on the CUDA cores."""
-        self.check(self.lib.fgpu_set_tensor_cores(self.h, 1 if on else 0))
+        (on, the default) or on the CUDA cores; df64: the FP64-accurate affine Laplace/mass element
+        matrices of the two-phase assembly on the tensor cores too (exact bf16 slices; default off,
+        the CUDA-core df64 kernel is faster)."""
+        self.check(self.lib.fgpu_set_tensor_cores(self.h, (_ffi.TC_F32 if on else 0) | (_ffi.TC_DF64 if df64 else 0)))
 
     def set_host_transfer(self, mode="auto"):
         """How host-output assembly moves values: "auto", "copy" (copy engines) or "direct" (kernel stores

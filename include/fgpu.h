@@ -281,11 +281,20 @@ int fgpu_assemble_matrix(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* fo
  * to the host while the next is gathered (pin host_val for the overlap); other forms assemble, then
  * copy. The device values are the same as after fgpu_assemble_matrix. */
 int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, double* host_val);
-/* binary32 element matrices of the quadrature form (curved tetrahedra, hexahedra: the per-point
- * contraction K_e = sum_q dphi^T G_q dphi + m_q phi phi^T of BilinearForm::Context::integrate,
- * feelpp/feel/feelvf/bilinearformcontext.hpp:585-589) on the tensor cores (tcgen05 kind::tf32,
- * 3xTF32 products, FP32 accumulation in tensor memory): 1 (default) or 0 (CUDA cores) */
-int fgpu_set_tensor_cores(fgpu_ctx* ctx, int on);
+/* element matrices on the tensor cores, a mask of
+ *   FGPU_TC_F32 (default on): binary32 element matrices of the quadrature form (curved tetrahedra,
+ *     hexahedra: the per-point contraction K_e = sum_q dphi^T G_q dphi + m_q phi phi^T of
+ *     BilinearForm::Context::integrate, feelpp/feel/feelvf/bilinearformcontext.hpp:585-589) with
+ *     tcgen05 kind::tf32, 3xTF32 products, FP32 accumulation in tensor memory;
+ *   FGPU_TC_DF64 (default off): FP64-accurate element matrices of the affine Laplace/mass form in the
+ *     two-phase assembly with tcgen05 kind::f16 on exact bf16 slices of the coefficients and the
+ *     reference tensors (levels of slice products summed exactly in FP32); values within ~3e-14 of
+ *     sum_k |c_k T_k| of the CUDA-core df64 kernel's, not the same bits, and slower than it on GB300
+ *     (0.42 against 0.33 ms for the P2 64^3 element phase).
+ * 0 keeps every element kernel on the CUDA cores. */
+#define FGPU_TC_F32 1
+#define FGPU_TC_DF64 2
+int fgpu_set_tensor_cores(fgpu_ctx* ctx, int mask);
 /* FGPU_HOST_TRANSFER_* for later fgpu_assemble_matrix_host calls (default AUTO) */
 int fgpu_set_host_transfer(fgpu_ctx* ctx, int mode);
 int fgpu_assemble_matrix_dev(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* form, const double* d_kappa,

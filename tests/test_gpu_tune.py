@@ -42,15 +42,27 @@ def test_tuned_shapes_keep_the_bits_and_persist(order, n):
         assert any("|P%d|f64|" % order in k for k in keys) and any("|P%d|f32|" % order in k for k in keys)
         for ln in lines:
             if ln.startswith("two_phase|"):
-                th, bp, gth, gbp, batch = map(int, ln.split()[1:])
-                assert th in (128, 256) and bp in (4, 8, 16, 32) and gth in (128, 256) and gbp in (8, 16, 32, 64)
-                assert batch in (2, 4, 8)
+                th, bp, gth, gbp, batch, pipe = map(int, ln.split()[1:])
+                assert th in (128, 256) and bp in (4, 8, 16, 32) and gth in (128, 256)
+                assert gbp in ((2, 4, 6, 8, 12, 16) if pipe else (8, 16, 32, 64))
+                assert batch in (2, 4, 8) and pipe in (0, 1)
         # a later context reads the picks: no timing on its first assembly
         later = fpp.Environment(tune=True, tune_cache=cache)
         l0 = later.launches()
         again = _assemble(later, xyz, tets, kappa, order, "f64").values()
         assert later.launches() - l0 < 50
         assert np.array_equal(again, _assemble(fixed, xyz, tets, kappa, order, "f64").values())
+        # the plain and the software-pipelined gather, whichever the tuner picked: the same bits
+        for pipe in (0, 1):
+            forced = os.path.join(d, "forced%d.txt" % pipe)
+            with open(forced, "w") as f:
+                for ln in lines:
+                    if ln.startswith("two_phase|"):
+                        f.write(" ".join(ln.split()[:6] + [str(pipe)]) + "\n")
+            env_h = fpp.Environment(tune=True, tune_cache=forced)
+            for precision in ("f64", "f32"):
+                got = _assemble(env_h, xyz, tets, kappa, order, precision).values()
+                assert np.array_equal(got, _assemble(fixed, xyz, tets, kappa, order, precision).values())
 
 
 def test_cg_spmv_pick_is_recorded():
