@@ -64,11 +64,13 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "gamg_rigid", "pmg", "apply", "gmres"],
+    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "gamg_rigid", "pmg", "apply", "gmres", "elements_tc"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
                         "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
                         "AMG-preconditioned CG solve to 1e-10; 'pmg' sets up the matrix-free Poisson operators "
-                        "(kappa = 1, perturbation 0.1h) with the P1 coarse level and runs one p-multigrid solve")
+                        "(kappa = 1, perturbation 0.1h) with the P1 coarse level and runs one p-multigrid solve; "
+                        "'elements_tc' times the FP64 two-phase element phase with the CUDA-core df64 kernel and "
+                        "with the tensor-core (bf16 slices) kernel, --steps assemblies each")
     return p.parse_args()
 
 
@@ -870,6 +872,41 @@ def run_probe_apply(args):
     print(json.dumps(out), flush=True)
 
 
+def run_probe_elements_tc(args):
+    """FP64 (df64) two-phase assemblies of the P-order Laplace+mass form (lognormal kappa, perturbation
+    0.15h) with the element matrices on the CUDA cores and on the tensor cores (FGPU_TC_DF64: exact bf16
+    slices), --steps each after 3 warm-ups; prints the element and gather phase times and the largest
+    difference of the two matrices."""
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    env = fpp.Environment(profile=True)
+    xyz, tets = meshgen.kuhn_box(args.n, perturb=0.15, seed=1234)
+    kappa = meshgen.lognormal_kappa(len(tets), seed=5678)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, args.order)
+    u, v = V.element(), V.element()
+    expr = fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v))
+    out = {"order": args.order, "mesh_n": args.n, "elements": len(tets)}
+    vals = {}
+    for name, tc in (("cuda_cores", False), ("tensor_cores", True)):
+        env.set_tensor_cores(True, df64=tc)
+        a = fpp.form2(test=V, trial=V)
+        for _ in range(3):
+            a.assign(expr)
+        env.prof_reset()
+        for _ in range(args.steps):
+            a.assign(expr)
+        ne, te = env.prof("assemble_elements")
+        ng, tg = env.prof("assemble_gather")
+        out[name] = {"element_phase_ms": te / max(ne, 1), "gather_ms": tg / max(ng, 1)}
+        vals[name] = a.values()
+        del a
+    env.set_tensor_cores(True)
+    ref = vals["cuda_cores"]
+    out["max_abs_diff_over_max"] = float(np.abs(vals["tensor_cores"] - ref).max() / np.abs(ref).max())
+    print(json.dumps(out), flush=True)
+
+
 def run_matfree(args):
     """Mixed-precision matrix-free P3 Poisson (unit cube, perturbed 0.1h, kappa = 1, homogeneous
     Dirichlet): operator applies in FP32 (CUDA cores and tcgen05 tensor cores), df64 and native
@@ -1482,6 +1519,9 @@ def main():
         return
     if args.probe == "gmres":
         run_probe_gmres(args)
+        return
+    if args.probe == "elements_tc":
+        run_probe_elements_tc(args)
         return
     if args.probe == "pmg":
         run_probe_pmg(args)
