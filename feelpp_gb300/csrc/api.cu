@@ -655,11 +655,16 @@ static int assemble_impl(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_desc* f,
     int rc = FGPU_OK;
     if (f->kind == FGPU_FORM_LAPLACE_MASS && !(algo == FGPU_ALGO_GATHER_NATIVE_F64 && A->precision == FGPU_F64)) {
         // FP64 matrices: df64 arithmetic on the FP32 pipes; FP32 matrices: binary32
+        if (algo == FGPU_ALGO_TWO_PHASE) {
+            // the coefficient records are formed inside the element kernel
+            const GeoIn geo{V->mesh->d_xyz, V->mesh->d_tets, d_kappa, f->kappa, f->mass, f->kappa_scale};
+            rc = launch_assemble_two_phase(ctx, A, tab, nullptr, &geo, accumulate);
+            if (rc) return rc;
+            return finish(ctx);
+        }
         rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef), f->kappa_scale);
         if (rc) return rc;
-        const float4* recs = reinterpret_cast<const float4*>(A->d_coef);
-        rc = algo == FGPU_ALGO_TWO_PHASE ? launch_assemble_two_phase(ctx, A, tab, recs, accumulate)
-                                         : launch_assemble_gather_df(ctx, A, tab, recs, accumulate);
+        rc = launch_assemble_gather_df(ctx, A, tab, reinterpret_cast<const float4*>(A->d_coef), accumulate);
         if (rc) return rc;
         return finish(ctx);
     }
@@ -765,9 +770,8 @@ int fgpu_assemble_matrix_host(fgpu_ctx* ctx, fgpu_matrix* A, const fgpu_form_des
         if (rc) return rc;
         A->coef_cap = nt * 8;
     }
-    int rc = launch_geometry_df(ctx, V->mesh, d_kappa, f->kappa, f->mass, reinterpret_cast<float4*>(A->d_coef), f->kappa_scale);
-    if (rc) return rc;
-    rc = launch_assemble_two_phase_host(ctx, A, tab, reinterpret_cast<const float4*>(A->d_coef), host_val);
+    const GeoIn geo{V->mesh->d_xyz, V->mesh->d_tets, d_kappa, f->kappa, f->mass, f->kappa_scale};
+    int rc = launch_assemble_two_phase_host(ctx, A, tab, nullptr, &geo, host_val);
     if (rc) return rc;
     return finish(ctx);
 }

@@ -120,4 +120,13 @@ __device__ __forceinline__ void load_record(const float4* __restrict__ rp, float
         cl[0] = l0.x; cl[1] = l0.y; cl[2] = l0.z; cl[3] = l0.w; cl[4] = l1.x; cl[5] = l1.y; cl[6] = l1.z;
     }
 }
+// the same record from shared memory
+__device__ __forceinline__ void load_record_shared(const float4* rp, float* ch, float* cl, bool lo) {
+    const float4 h0 = rp[0], h1 = rp[1];
+    ch[0] = h0.x; ch[1] = h0.y; ch[2] = h0.z; ch[3] = h0.w; ch[4] = h1.x; ch[5] = h1.y; ch[6] = h1.z;
+    if (lo) {
+        const float4 l0 = rp[2], l1 = rp[3];
+        cl[0] = l0.x; cl[1] = l0.y; cl[2] = l0.z; cl[3] = l0.w; cl[4] = l1.x; cl[5] = l1.y; cl[6] = l1.z;
+    }
+}
 }  // namespace fgpu

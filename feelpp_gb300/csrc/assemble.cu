@@ -1278,14 +1278,18 @@ int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, c
 //   No float atomics; the gather is a streaming pass over gptr, gidx and the
 //   CSR values.
 // ---------------------------------------------------------------------------
-template <int MODE, int N>
-__global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const float4* __restrict__ rec,
+// GEO: the geometry runs in the kernel (no coefficient records in device memory): each warp forms the
+// records of 32 consecutive elements, one per lane (geometry_df_record, the same arithmetic as
+// geometry_df_kernel), into shared memory, then their element matrices as below.
+template <int MODE, int N, bool GEO>
+__global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const float4* __restrict__ rec, GeoIn geo,
                                                           const float* __restrict__ Thg, const float* __restrict__ Tlg,
-                                                          void* __restrict__ kbuf) {
+                                                          void* __restrict__ kbuf, int* __restrict__ status) {
     constexpr int NTRI = N * (N + 1) / 2;
     constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;      // elements per warp pass (P1: 3)
     __shared__ float Th[7 * NTRI];
     __shared__ float Tl[MODE == kModeDF64 ? 7 * NTRI : 1];
+    __shared__ float4 srec[GEO ? 8 * 32 * 4 : 1];        // per warp: the records of 32 elements
     for (int k = threadIdx.x; k < 7 * NTRI; k += blockDim.x) {
         Th[k] = Thg[k];
         if (MODE == kModeDF64) Tl[k] = Tlg[k];
@@ -1296,12 +1300,12 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
     const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
     const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    // at most two entries per lane when NTRI <= 64, the same ones for every element: their table values
+    // stay in registers across the element loop
+    constexpr int TS = EPW > 1 ? NTRI : 32;
+    const int t1 = t0 + TS;
+    float th0[7], tl0[7], th1[7], tl1[7];
     if (NTRI <= 64) {
-        // at most two entries per lane, the same ones for every element: their table values stay in
-        // registers across the element loop
-        constexpr int TS = EPW > 1 ? NTRI : 32;
-        const int t1 = t0 + TS;
-        float th0[7], tl0[7], th1[7], tl1[7];
 #pragma unroll
         for (int k = 0; k < 7; ++k) {
             const bool ok0 = sub < EPW && t0 < NTRI, ok1 = sub < EPW && t1 < NTRI;
@@ -1310,11 +1314,10 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
             tl0[k] = (MODE == kModeDF64 && ok0) ? Tl[k * NTRI + t0] : 0.0f;
             tl1[k] = (MODE == kModeDF64 && ok1) ? Tl[k * NTRI + t1] : 0.0f;
         }
-        for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
-            const int64_t e = e0 + sub;
-            if (sub >= EPW || e >= nt) continue;
-            float ch[7], cl[7];
-            load_record(rec + 4 * e, ch, cl, MODE == kModeDF64);
+    }
+    // the entries of element e held by this lane
+    auto entries = [&](int64_t e, const float* ch, const float* cl) {
+        if (NTRI <= 64) {
             if (MODE == kModeDF64) {
                 float2* kb = reinterpret_cast<float2*>(kbuf) + e * NTRI;
                 if (t0 < NTRI) {
@@ -1340,22 +1343,43 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
                     kb[t1] = v;
                 }
             }
+        } else {
+            for (int t = t0; t < NTRI; t += (EPW > 1 ? NTRI : 32)) {
+                if (MODE == kModeDF64) {
+                    const df v = coef_entry_df(ch, cl, Th, Tl, NTRI, t);
+                    reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = make_float2(v.hi, v.lo);
+                } else {
+                    reinterpret_cast<float*>(kbuf)[e * NTRI + t] = coef_entry_f(ch, Th, NTRI, t);
+                }
+            }
+        }
+    };
+    if (!GEO) {
+        for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
+            const int64_t e = e0 + sub;
+            if (sub >= EPW || e >= nt) continue;
+            float ch[7], cl[7];
+            load_record(rec + 4 * e, ch, cl, MODE == kModeDF64);      // once per element and lane
+            entries(e, ch, cl);
         }
         return;
     }
-    for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
-        const int64_t e = e0 + sub;
-        if (sub >= EPW || e >= nt) continue;
-        float ch[7], cl[7];
-        load_record(rec + 4 * e, ch, cl, MODE == kModeDF64);      // once per element and lane
-        for (int t = t0; t < NTRI; t += (EPW > 1 ? NTRI : 32)) {
-            if (MODE == kModeDF64) {
-                const df v = coef_entry_df(ch, cl, Th, Tl, NTRI, t);
-                reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = make_float2(v.hi, v.lo);
-            } else {
-                reinterpret_cast<float*>(kbuf)[e * NTRI + t] = coef_entry_f(ch, Th, NTRI, t);
+    const df kc = d2df(geo.kc), mc = d2df(geo.mc);
+    const df ksc = geo.kscale ? d2df(*geo.kscale) : df{1.0f, 0.0f};
+    float4* wrec = srec + (threadIdx.x >> 5) * 32 * 4;
+    for (int64_t g0 = wid * 32; g0 < nt; g0 += nw * 32) {
+        if (g0 + lane < nt) geometry_df_record(g0 + lane, geo.xyz, geo.tets, geo.kappa, kc, mc, ksc, wrec + 4 * lane, status);
+        __syncwarp();
+        const int cnt = (int)(nt - g0 < 32 ? nt - g0 : 32);
+        for (int j0 = 0; j0 < cnt; j0 += EPW) {
+            const int j = j0 + sub;
+            if (sub < EPW && j < cnt) {
+                float ch[7], cl[7];
+                load_record_shared(wrec + 4 * j, ch, cl, MODE == kModeDF64);
+                entries(g0 + j, ch, cl);
             }
         }
+        __syncwarp();
     }
 }
 
@@ -1666,14 +1690,19 @@ struct TwoPhaseShape {
 };
 
 template <int MODE, int N>
-static void launch_element_tri(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int sms,
-                               const TwoPhaseShape& sh) {
+static void launch_element_tri(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo,
+                               int sms, const TwoPhaseShape& sh) {
     constexpr int NTRI = N * (N + 1) / 2;
     constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;
     const int64_t nt = A->space->mesh->nt;
-    const int64_t warps = (nt + EPW - 1) / EPW, wpb = sh.el_threads / 32;
+    const int64_t warps = rec ? (nt + EPW - 1) / EPW : (nt + 31) / 32, wpb = sh.el_threads / 32;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((warps + wpb - 1) / wpb, (int64_t)sms * sh.el_bpsm));
-    element_tri_kernel<MODE, N><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
+    if (rec)
+        element_tri_kernel<MODE, N, false><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, rec, GeoIn{}, tab->d_T7th, tab->d_T7tl,
+                                                                                        A->d_kbuf, ctx->d_status);
+    else
+        element_tri_kernel<MODE, N, true><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, nullptr, *geo, tab->d_T7th, tab->d_T7tl,
+                                                                                       A->d_kbuf, ctx->d_status);
 }
 
 template <int MODE>
@@ -1719,14 +1748,15 @@ static float median_ms(fgpu_ctx* ctx, F&& fn) {
 // Time the candidate shapes on the real inputs (the element buffer and the values are written by the
 // candidates; the assembly that follows overwrites both).
 template <int MODE, int N>
-static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int sms, TwoPhaseShape& best) {
+static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo, int sms,
+                          TwoPhaseShape& best) {
     float best_ms = 1e30f;
     TwoPhaseShape s = best;
     for (int th : {128, 256})
         for (int bp : {4, 8, 16, 32}) {
             s.el_threads = th;
             s.el_bpsm = bp;
-            const float ms = median_ms(ctx, [&] { launch_element_tri<MODE, N>(ctx, A, tab, rec, sms, s); });
+            const float ms = median_ms(ctx, [&] { launch_element_tri<MODE, N>(ctx, A, tab, rec, geo, sms, s); });
             if (ms < best_ms) { best_ms = ms; best.el_threads = th; best.el_bpsm = bp; }
         }
     best_ms = 1e30f;
@@ -1755,11 +1785,18 @@ static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, c
 }
 
 template <int MODE, int N>
-static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate,
-                         double* host = nullptr) {
+static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo,
+                         int accumulate, double* host = nullptr) {
     fgpu_space* V = A->space;
     const int64_t nt = V->mesh->nt;
     constexpr int NTRI = N * (N + 1) / 2;
+    const bool tc = MODE == kModeDF64 && (ctx->tensor_cores & FGPU_TC_DF64);
+    if (!rec && tc) {
+        // the tensor-core element kernel reads the coefficient records from device memory
+        const int rc = launch_geometry_df(ctx, V->mesh, geo->kappa, geo->kc, geo->mc, reinterpret_cast<float4*>(A->d_coef), geo->kscale);
+        if (rc) return rc;
+        rec = reinterpret_cast<const float4*>(A->d_coef);
+    }
     if (!V->d_gptr) {
         if (ctx->capturing) { ctx->err = "two-phase assembly: assemble once before capturing (gather map)"; return FGPU_ERR_INVALID; }
         int rc = launch_build_gather_map(ctx, V);
@@ -1784,19 +1821,19 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     if (ctx->tune == 0 && tune_lookup(ctx->tune_file, key, tv) && (tv.size() == 5 || tv.size() == 6)) {
         shape = TwoPhaseShape{tv[0], tv[1], tv[2], tv[3], tv[4], tv.size() == 6 ? tv[5] : 0};
     } else if (ctx->tune == 0 && !ctx->capturing && accumulate == 0 && !host) {
-        int rc = tune_two_phase<MODE, N>(ctx, A, tab, rec, sms, shape);
+        int rc = tune_two_phase<MODE, N>(ctx, A, tab, rec, geo, sms, shape);
         if (rc) return rc;
         tune_record(ctx->tune_file, key, {shape.el_threads, shape.el_bpsm, shape.g_threads, shape.g_bpsm, shape.g_batch, shape.g_pipe});
     }
     {
         PendingEvent ev;
         prof_begin(ctx, "assemble_elements", ev);
-        if (MODE == kModeDF64 && (ctx->tensor_cores & FGPU_TC_DF64)) {
+        if (tc) {
             // the df64 element matrices on the tensor cores (bf16 slices, exact level sums)
             const int rc = launch_element_tri_tc(ctx, V->order, nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
             if (rc) return rc;
         } else {
-            launch_element_tri<MODE, N>(ctx, A, tab, rec, sms, shape);
+            launch_element_tri<MODE, N>(ctx, A, tab, rec, geo, sms, shape);
         }
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
@@ -1921,26 +1958,27 @@ int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, 
     return FGPU_OK;
 }
 
-int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, double* host) {
+int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo,
+                                   double* host) {
     if (A->ncomp != 1 || A->precision != FGPU_F64) { ctx->err = "assemble to host: scalar FP64 matrices"; return FGPU_ERR_INVALID; }
     switch (A->space->order) {
-        case 1: return run_two_phase<kModeDF64, 4>(ctx, A, tab, rec, 0, host);
-        case 2: return run_two_phase<kModeDF64, 10>(ctx, A, tab, rec, 0, host);
-        case 3: return run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, 0, host);
+        case 1: return run_two_phase<kModeDF64, 4>(ctx, A, tab, rec, geo, 0, host);
+        case 2: return run_two_phase<kModeDF64, 10>(ctx, A, tab, rec, geo, 0, host);
+        case 3: return run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, geo, 0, host);
         default: ctx->err = "unsupported order"; return FGPU_ERR_INVALID;
     }
 }
 
-int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate) {
+int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo, int accumulate) {
     const int order = A->space->order;
     const bool f32 = A->precision == FGPU_F32;
     if (A->ncomp != 1) { ctx->err = "Laplace/mass form needs a scalar space"; return FGPU_ERR_INVALID; }
-    if (order == 1) return f32 ? run_two_phase<kModeF32, 4>(ctx, A, tab, rec, accumulate)
-                               : run_two_phase<kModeDF64, 4>(ctx, A, tab, rec, accumulate);
-    if (order == 2) return f32 ? run_two_phase<kModeF32, 10>(ctx, A, tab, rec, accumulate)
-                               : run_two_phase<kModeDF64, 10>(ctx, A, tab, rec, accumulate);
-    if (order == 3) return f32 ? run_two_phase<kModeF32, 20>(ctx, A, tab, rec, accumulate)
-                               : run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, accumulate);
+    if (order == 1) return f32 ? run_two_phase<kModeF32, 4>(ctx, A, tab, rec, geo, accumulate)
+                               : run_two_phase<kModeDF64, 4>(ctx, A, tab, rec, geo, accumulate);
+    if (order == 2) return f32 ? run_two_phase<kModeF32, 10>(ctx, A, tab, rec, geo, accumulate)
+                               : run_two_phase<kModeDF64, 10>(ctx, A, tab, rec, geo, accumulate);
+    if (order == 3) return f32 ? run_two_phase<kModeF32, 20>(ctx, A, tab, rec, geo, accumulate)
+                               : run_two_phase<kModeDF64, 20>(ctx, A, tab, rec, geo, accumulate);
     ctx->err = "unsupported order";
     return FGPU_ERR_INVALID;
 }

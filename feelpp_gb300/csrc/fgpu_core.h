@@ -383,7 +383,17 @@ int launch_assemble_colour(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, 
 int launch_geometry_df(fgpu_ctx* ctx, const fgpu_mesh* mesh, const double* d_kappa, double kappa, double mass,
                        float4* d_rec, const double* d_kscale = nullptr);
 int launch_assemble_gather_df(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
-int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, int accumulate);
+// inputs of the element coefficient records when the geometry runs inside the element kernel
+struct GeoIn {
+    const double* xyz = nullptr;
+    const int32_t* tets = nullptr;
+    const double* kappa = nullptr;     // per element, or null: kc
+    double kc = 0.0, mc = 0.0;
+    const double* kscale = nullptr;    // device factor of kappa, or null
+};
+// two-phase Laplace/mass assembly from coefficient records (rec) or with the geometry fused into the
+// element kernel (rec null, geo given)
+int launch_assemble_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo, int accumulate);
 constexpr int kStreamedUnsupported = -1;   // launch_assemble_streamed: use the two-phase path
 int launch_assemble_streamed(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const double* d_kappa, double kappa,
                              double mass, const double* kscale, int accumulate, double* hout);
@@ -403,7 +413,8 @@ int build_sell(fgpu_ctx* ctx, const fgpu_matrix* A, std::shared_ptr<SellLayout>&
 int solve_gmres(fgpu_ctx* ctx, const fgpu_matrix* A, fgpu_amg* amg, const double* b, double* x, const fgpu_solver_cfg* cfg,
                 int restart, fgpu_solve_stats* st);
 int ensure_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, size_t need);
-int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, double* host);
+int launch_assemble_two_phase_host(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo,
+                                   double* host);
 int launch_gather_phase_to_host(fgpu_ctx* ctx, fgpu_matrix* A, double* host, int nchunks);
 int launch_gather_phase(fgpu_ctx* ctx, fgpu_matrix* A, int accumulate);
 int launch_rhs_gather(fgpu_ctx* ctx, const fgpu_space* V, const double* d_work, double* d_out, int accumulate);

@@ -74,7 +74,7 @@ def test_auto_is_two_phase_and_matches_streamed(env):
     u, v = V.element(), V.element()
     l0 = env.launches()
     a.assign(fpp.integrate(fpp.elements(M), kappa * fpp.inner(fpp.gradt(u), fpp.grad(v)) + 0.7 * fpp.idt(u) * fpp.id(v)))
-    assert env.launches() - l0 == 3          # geometry, element matrices, gather
+    assert env.launches() - l0 == 2          # element matrices (geometry inside), gather
     s = _assemble(env, M, V, kappa, _ffi.ALGO_STREAMED)
     assert np.array_equal(a.values(), s.values())
 
