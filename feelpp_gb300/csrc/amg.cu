@@ -166,6 +166,36 @@ __global__ void __launch_bounds__(256) amg_sell_kernel(AmgSweep s, AmgSell m, co
     }
 }
 
+// the same sweep for levels with few rows: a block of W warps per slice, warp w summing the entries
+// k = w, w + W, ... of the slice's 32 rows (coalesced like the one-thread-per-row kernel), the W
+// partial sums of a row then added in warp order; a level of 25 K rows has ~800 slices, so the
+// one-thread-per-row kernel would run 25 K threads through rows of ~60 dependent loads each
+template <int MODE, int W>
+__global__ void __launch_bounds__(32 * W) amg_sell_split_kernel(AmgSweep s, AmgSell m, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    __shared__ float part[W][32];
+    const int r = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t sl = blockIdx.x; sl < m.nslices; sl += gridDim.x) {
+        const int L = __ldg(m.len + sl);
+        const int64_t base = __ldg(m.ptr + sl) + r;
+        float acc = 0.0f;
+        for (int k = w; k < L; k += W) {
+            const int64_t j = base + (int64_t)k * 32;
+            acc = fmaf(__ldg(m.val + j), __ldg(s.x + __ldg(m.col + j)), acc);
+        }
+        part[w][r] = acc;
+        __syncthreads();
+        if (w == 0) {
+            float t = part[0][r];
+#pragma unroll
+            for (int q = 1; q < W; ++q) t += part[q][r];
+            const int64_t i = sl * 32 + r;
+            if (i < s.n) amg_epilogue<MODE>(s, __ldg(m.perm + i), t);
+        }
+        __syncthreads();
+    }
+}
+
 // one sweep of a CSR operator (the prolongators and restrictions): s_i = sum_j a_ij x_j with G lanes
 // per row, then the mode's epilogue
 template <int G, int MODE>
@@ -264,6 +294,10 @@ void sweep(cudaStream_t st, int G, const AmgSweep& s, const int* stop) {
     }
 }
 
+// levels with fewer rows than this run the split-slice sweep (152 SMs x 1024 threads: the one-thread-
+// per-row kernel would not fill the GPU once)
+constexpr int64_t kSellSplitRows = 152 * 1024;
+
 template <int MODE>
 void sell_sweep(cudaStream_t st, const fgpu_amg::Level& V, const AmgSweep& s, const int* stop) {
     AmgSell m;
@@ -273,6 +307,11 @@ void sell_sweep(cudaStream_t st, const fgpu_amg::Level& V, const AmgSweep& s, co
     m.perm = V.s_perm;
     m.col = V.s_col;
     m.val = V.s_val;
+    if (V.nslices * 32 < kSellSplitRows) {
+        // few rows: eight warps per slice (the rows are long on the coarse levels)
+        amg_sell_split_kernel<MODE, 8><<<(int)std::max<int64_t>(1, V.nslices), 256, 0, st>>>(s, m, stop);
+        return;
+    }
     // one thread per slot, no grid-stride loop: slices differ in length, and many short-lived blocks
     // keep the SMs fuller than a few long-lived ones (measured: 46 % warps active with two waves)
     const int g = (int)std::max<int64_t>(1, (V.nslices * 32 + 255) / 256);
