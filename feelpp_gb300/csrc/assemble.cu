@@ -1278,21 +1278,24 @@ int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, c
 //   No float atomics; the gather is a streaming pass over gptr, gidx and the
 //   CSR values.
 // ---------------------------------------------------------------------------
-// GEO: the geometry runs in the kernel (no coefficient records in device memory): each warp forms the
+// The coefficient records are formed in the kernel (none in device memory): each warp forms the
 // records of 32 consecutive elements, one per lane (geometry_df_record, the same arithmetic as
-// geometry_df_kernel), into shared memory, then their element matrices as below.
-template <int MODE, int N, bool GEO>
-__global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const float4* __restrict__ rec, GeoIn geo,
-                                                          const float* __restrict__ Thg, const float* __restrict__ Tlg,
-                                                          void* __restrict__ kbuf, int* __restrict__ status) {
+// geometry_df_kernel), into shared memory, then their element matrices. With NTRI <= 64 each lane keeps
+// the table values of its (at most two) entries in registers across the elements; with more entries
+// (P3) two elements share each table value read from shared memory.
+template <int MODE, int N>
+__global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, GeoIn geo, const float* __restrict__ Thg,
+                                                          const float* __restrict__ Tlg, void* __restrict__ kbuf,
+                                                          int* __restrict__ status) {
     constexpr int NTRI = N * (N + 1) / 2;
     constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;      // elements per warp pass (P1: 3)
+    constexpr bool DF = MODE == kModeDF64;
     __shared__ float Th[7 * NTRI];
-    __shared__ float Tl[MODE == kModeDF64 ? 7 * NTRI : 1];
-    __shared__ float4 srec[GEO ? 8 * 32 * 4 : 1];        // per warp: the records of 32 elements
+    __shared__ float Tl[DF ? 7 * NTRI : 1];
+    __shared__ float4 srec[8 * 32 * 4];                  // per warp: the records of 32 elements
     for (int k = threadIdx.x; k < 7 * NTRI; k += blockDim.x) {
         Th[k] = Thg[k];
-        if (MODE == kModeDF64) Tl[k] = Tlg[k];
+        if (DF) Tl[k] = Tlg[k];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -1300,8 +1303,6 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
     const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
     const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    // at most two entries per lane when NTRI <= 64, the same ones for every element: their table values
-    // stay in registers across the element loop
     constexpr int TS = EPW > 1 ? NTRI : 32;
     const int t1 = t0 + TS;
     float th0[7], tl0[7], th1[7], tl1[7];
@@ -1311,58 +1312,9 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
             const bool ok0 = sub < EPW && t0 < NTRI, ok1 = sub < EPW && t1 < NTRI;
             th0[k] = ok0 ? Th[k * NTRI + t0] : 0.0f;
             th1[k] = ok1 ? Th[k * NTRI + t1] : 0.0f;
-            tl0[k] = (MODE == kModeDF64 && ok0) ? Tl[k * NTRI + t0] : 0.0f;
-            tl1[k] = (MODE == kModeDF64 && ok1) ? Tl[k * NTRI + t1] : 0.0f;
+            tl0[k] = (DF && ok0) ? Tl[k * NTRI + t0] : 0.0f;
+            tl1[k] = (DF && ok1) ? Tl[k * NTRI + t1] : 0.0f;
         }
-    }
-    // the entries of element e held by this lane
-    auto entries = [&](int64_t e, const float* ch, const float* cl) {
-        if (NTRI <= 64) {
-            if (MODE == kModeDF64) {
-                float2* kb = reinterpret_cast<float2*>(kbuf) + e * NTRI;
-                if (t0 < NTRI) {
-                    const df v = coef_entry_df_reg(ch, cl, th0, tl0);
-                    kb[t0] = make_float2(v.hi, v.lo);
-                }
-                if (t1 < NTRI) {
-                    const df v = coef_entry_df_reg(ch, cl, th1, tl1);
-                    kb[t1] = make_float2(v.hi, v.lo);
-                }
-            } else {
-                float* kb = reinterpret_cast<float*>(kbuf) + e * NTRI;
-                if (t0 < NTRI) {
-                    float v = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th0[k], v);
-                    kb[t0] = v;
-                }
-                if (t1 < NTRI) {
-                    float v = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th1[k], v);
-                    kb[t1] = v;
-                }
-            }
-        } else {
-            for (int t = t0; t < NTRI; t += (EPW > 1 ? NTRI : 32)) {
-                if (MODE == kModeDF64) {
-                    const df v = coef_entry_df(ch, cl, Th, Tl, NTRI, t);
-                    reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = make_float2(v.hi, v.lo);
-                } else {
-                    reinterpret_cast<float*>(kbuf)[e * NTRI + t] = coef_entry_f(ch, Th, NTRI, t);
-                }
-            }
-        }
-    };
-    if (!GEO) {
-        for (int64_t e0 = wid * EPW; e0 < nt; e0 += nw * EPW) {
-            const int64_t e = e0 + sub;
-            if (sub >= EPW || e >= nt) continue;
-            float ch[7], cl[7];
-            load_record(rec + 4 * e, ch, cl, MODE == kModeDF64);      // once per element and lane
-            entries(e, ch, cl);
-        }
-        return;
     }
     const df kc = d2df(geo.kc), mc = d2df(geo.mc);
     const df ksc = geo.kscale ? d2df(*geo.kscale) : df{1.0f, 0.0f};
@@ -1371,12 +1323,73 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, const floa
         if (g0 + lane < nt) geometry_df_record(g0 + lane, geo.xyz, geo.tets, geo.kappa, kc, mc, ksc, wrec + 4 * lane, status);
         __syncwarp();
         const int cnt = (int)(nt - g0 < 32 ? nt - g0 : 32);
-        for (int j0 = 0; j0 < cnt; j0 += EPW) {
-            const int j = j0 + sub;
-            if (sub < EPW && j < cnt) {
+        if (NTRI <= 64) {
+            for (int j0 = 0; j0 < cnt; j0 += EPW) {
+                const int j = j0 + sub;
+                if (sub >= EPW || j >= cnt) continue;
                 float ch[7], cl[7];
-                load_record_shared(wrec + 4 * j, ch, cl, MODE == kModeDF64);
-                entries(g0 + j, ch, cl);
+                load_record_shared(wrec + 4 * j, ch, cl, DF);
+                const int64_t e = g0 + j;
+                if (DF) {
+                    float2* kb = reinterpret_cast<float2*>(kbuf) + e * NTRI;
+                    if (t0 < NTRI) {
+                        const df v = coef_entry_df_reg(ch, cl, th0, tl0);
+                        kb[t0] = make_float2(v.hi, v.lo);
+                    }
+                    if (t1 < NTRI) {
+                        const df v = coef_entry_df_reg(ch, cl, th1, tl1);
+                        kb[t1] = make_float2(v.hi, v.lo);
+                    }
+                } else {
+                    float* kb = reinterpret_cast<float*>(kbuf) + e * NTRI;
+                    if (t0 < NTRI) {
+                        float v = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th0[k], v);
+                        kb[t0] = v;
+                    }
+                    if (t1 < NTRI) {
+                        float v = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th1[k], v);
+                        kb[t1] = v;
+                    }
+                }
+            }
+        } else {
+            for (int j = 0; j < cnt; j += 2) {
+                const bool two = j + 1 < cnt;
+                float ch0[7], cl0[7], ch1[7], cl1[7];
+                load_record_shared(wrec + 4 * j, ch0, cl0, DF);
+                load_record_shared(wrec + 4 * (two ? j + 1 : j), ch1, cl1, DF);
+                const int64_t e = g0 + j;
+                for (int t = lane; t < NTRI; t += 32) {
+                    float th[7], tl[7];
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) {
+                        th[k] = Th[k * NTRI + t];
+                        tl[k] = DF ? Tl[k * NTRI + t] : 0.0f;
+                    }
+                    if (DF) {
+                        float2* kb = reinterpret_cast<float2*>(kbuf);
+                        const df v0 = coef_entry_df_reg(ch0, cl0, th, tl);
+                        kb[e * NTRI + t] = make_float2(v0.hi, v0.lo);
+                        if (two) {
+                            const df v1 = coef_entry_df_reg(ch1, cl1, th, tl);
+                            kb[(e + 1) * NTRI + t] = make_float2(v1.hi, v1.lo);
+                        }
+                    } else {
+                        float* kb = reinterpret_cast<float*>(kbuf);
+                        float v0 = 0.0f, v1 = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) {
+                            v0 = fmaf(ch0[k], th[k], v0);
+                            v1 = fmaf(ch1[k], th[k], v1);
+                        }
+                        kb[e * NTRI + t] = v0;
+                        if (two) kb[(e + 1) * NTRI + t] = v1;
+                    }
+                }
             }
         }
         __syncwarp();
@@ -1690,19 +1703,13 @@ struct TwoPhaseShape {
 };
 
 template <int MODE, int N>
-static void launch_element_tri(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo,
-                               int sms, const TwoPhaseShape& sh) {
-    constexpr int NTRI = N * (N + 1) / 2;
-    constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;
+static void launch_element_tri(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const GeoIn* geo, int sms,
+                               const TwoPhaseShape& sh) {
     const int64_t nt = A->space->mesh->nt;
-    const int64_t warps = rec ? (nt + EPW - 1) / EPW : (nt + 31) / 32, wpb = sh.el_threads / 32;
+    const int64_t warps = (nt + 31) / 32, wpb = sh.el_threads / 32;       // 32 elements per warp
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((warps + wpb - 1) / wpb, (int64_t)sms * sh.el_bpsm));
-    if (rec)
-        element_tri_kernel<MODE, N, false><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, rec, GeoIn{}, tab->d_T7th, tab->d_T7tl,
-                                                                                        A->d_kbuf, ctx->d_status);
-    else
-        element_tri_kernel<MODE, N, true><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, nullptr, *geo, tab->d_T7th, tab->d_T7tl,
-                                                                                       A->d_kbuf, ctx->d_status);
+    element_tri_kernel<MODE, N><<<(int)blocks, sh.el_threads, 0, ctx->stream>>>(nt, *geo, tab->d_T7th, tab->d_T7tl, A->d_kbuf,
+                                                                             ctx->d_status);
 }
 
 template <int MODE>
@@ -1748,15 +1755,16 @@ static float median_ms(fgpu_ctx* ctx, F&& fn) {
 // Time the candidate shapes on the real inputs (the element buffer and the values are written by the
 // candidates; the assembly that follows overwrites both).
 template <int MODE, int N>
-static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const float4* rec, const GeoIn* geo, int sms,
+static int tune_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, const GeoIn* geo, bool elements, int sms,
                           TwoPhaseShape& best) {
     float best_ms = 1e30f;
     TwoPhaseShape s = best;
     for (int th : {128, 256})
         for (int bp : {4, 8, 16, 32}) {
+            if (!elements) break;                  // the tensor-core element kernel has its own shape
             s.el_threads = th;
             s.el_bpsm = bp;
-            const float ms = median_ms(ctx, [&] { launch_element_tri<MODE, N>(ctx, A, tab, rec, geo, sms, s); });
+            const float ms = median_ms(ctx, [&] { launch_element_tri<MODE, N>(ctx, A, tab, geo, sms, s); });
             if (ms < best_ms) { best_ms = ms; best.el_threads = th; best.el_bpsm = bp; }
         }
     best_ms = 1e30f;
@@ -1821,7 +1829,7 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
     if (ctx->tune == 0 && tune_lookup(ctx->tune_file, key, tv) && (tv.size() == 5 || tv.size() == 6)) {
         shape = TwoPhaseShape{tv[0], tv[1], tv[2], tv[3], tv[4], tv.size() == 6 ? tv[5] : 0};
     } else if (ctx->tune == 0 && !ctx->capturing && accumulate == 0 && !host) {
-        int rc = tune_two_phase<MODE, N>(ctx, A, tab, rec, geo, sms, shape);
+        int rc = tune_two_phase<MODE, N>(ctx, A, tab, geo, !tc, sms, shape);
         if (rc) return rc;
         tune_record(ctx->tune_file, key, {shape.el_threads, shape.el_bpsm, shape.g_threads, shape.g_bpsm, shape.g_batch, shape.g_pipe});
     }
@@ -1833,7 +1841,7 @@ static int run_two_phase(fgpu_ctx* ctx, fgpu_matrix* A, const DevTables* tab, co
             const int rc = launch_element_tri_tc(ctx, V->order, nt, rec, tab->d_T7th, tab->d_T7tl, A->d_kbuf);
             if (rc) return rc;
         } else {
-            launch_element_tri<MODE, N>(ctx, A, tab, rec, geo, sms, shape);
+            launch_element_tri<MODE, N>(ctx, A, tab, geo, sms, shape);
         }
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
