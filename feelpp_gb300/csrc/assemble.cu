@@ -1088,6 +1088,111 @@ static int batch_tables(fgpu_ctx* ctx, float** h, float** l) {
     return FGPU_OK;
 }
 
+// The two-phase element phase works on groups of 32 consecutive elements: each warp forms the
+// coefficient records of a group, one per lane (geometry_df_record, the same arithmetic as
+// geometry_df_kernel), into shared memory, then the group's element matrices. With NTRI <= 64 each lane
+// holds the table values of its (at most two) entries in registers (tri_lane_tables); with more entries
+// (P3) two elements share each table value read from shared memory.
+template <int MODE, int N>
+__device__ __forceinline__ void tri_lane_tables(const float* Th, const float* Tl, int lane, float* th0, float* tl0, float* th1,
+                                                float* tl1) {
+    constexpr int NTRI = N * (N + 1) / 2;
+    constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;
+    const int sub = lane / NTRI < EPW ? lane / NTRI : EPW;
+    const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
+    const int t1 = t0 + (EPW > 1 ? NTRI : 32);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        const bool ok0 = sub < EPW && t0 < NTRI, ok1 = sub < EPW && t1 < NTRI;
+        th0[k] = ok0 ? Th[k * NTRI + t0] : 0.0f;
+        th1[k] = ok1 ? Th[k * NTRI + t1] : 0.0f;
+        tl0[k] = (MODE == kModeDF64 && ok0) ? Tl[k * NTRI + t0] : 0.0f;
+        tl1[k] = (MODE == kModeDF64 && ok1) ? Tl[k * NTRI + t1] : 0.0f;
+    }
+}
+
+// the upper triangles of elements e0 .. e0 + cnt - 1 from their records in wrec (shared memory)
+template <int MODE, int N>
+__device__ __forceinline__ void tri_group_entries(void* __restrict__ kbuf, int64_t e0, int cnt, const float4* wrec, const float* Th,
+                                                  const float* Tl, int lane, const float* th0, const float* tl0, const float* th1,
+                                                  const float* tl1) {
+    constexpr int NTRI = N * (N + 1) / 2;
+    constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;      // elements per warp pass (P1: 3)
+    constexpr bool DF = MODE == kModeDF64;
+    if (NTRI <= 64) {
+        const int sub = lane / NTRI < EPW ? lane / NTRI : EPW;
+        const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
+        const int t1 = t0 + (EPW > 1 ? NTRI : 32);
+        for (int j0 = 0; j0 < cnt; j0 += EPW) {
+            const int j = j0 + sub;
+            if (sub >= EPW || j >= cnt) continue;
+            float ch[7], cl[7];
+            load_record_shared(wrec + 4 * j, ch, cl, DF);
+            const int64_t e = e0 + j;
+            if (DF) {
+                float2* kb = reinterpret_cast<float2*>(kbuf) + e * NTRI;
+                if (t0 < NTRI) {
+                    const df v = coef_entry_df_reg(ch, cl, th0, tl0);
+                    kb[t0] = make_float2(v.hi, v.lo);
+                }
+                if (t1 < NTRI) {
+                    const df v = coef_entry_df_reg(ch, cl, th1, tl1);
+                    kb[t1] = make_float2(v.hi, v.lo);
+                }
+            } else {
+                float* kb = reinterpret_cast<float*>(kbuf) + e * NTRI;
+                if (t0 < NTRI) {
+                    float v = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th0[k], v);
+                    kb[t0] = v;
+                }
+                if (t1 < NTRI) {
+                    float v = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th1[k], v);
+                    kb[t1] = v;
+                }
+            }
+        }
+    } else {
+        for (int j = 0; j < cnt; j += 2) {
+            const bool two = j + 1 < cnt;
+            float ch0[7], cl0[7], ch1[7], cl1[7];
+            load_record_shared(wrec + 4 * j, ch0, cl0, DF);
+            load_record_shared(wrec + 4 * (two ? j + 1 : j), ch1, cl1, DF);
+            const int64_t e = e0 + j;
+            for (int t = lane; t < NTRI; t += 32) {
+                float th[7], tl[7];
+#pragma unroll
+                for (int k = 0; k < 7; ++k) {
+                    th[k] = Th[k * NTRI + t];
+                    tl[k] = DF ? Tl[k * NTRI + t] : 0.0f;
+                }
+                if (DF) {
+                    float2* kb = reinterpret_cast<float2*>(kbuf);
+                    const df v0 = coef_entry_df_reg(ch0, cl0, th, tl);
+                    kb[e * NTRI + t] = make_float2(v0.hi, v0.lo);
+                    if (two) {
+                        const df v1 = coef_entry_df_reg(ch1, cl1, th, tl);
+                        kb[(e + 1) * NTRI + t] = make_float2(v1.hi, v1.lo);
+                    }
+                } else {
+                    float* kb = reinterpret_cast<float*>(kbuf);
+                    float v0 = 0.0f, v1 = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) {
+                        v0 = fmaf(ch0[k], th[k], v0);
+                        v1 = fmaf(ch1[k], th[k], v1);
+                    }
+                    kb[e * NTRI + t] = v0;
+                    if (two) kb[(e + 1) * NTRI + t] = v1;
+                }
+            }
+        }
+    }
+}
+
 // ---- two-phase batches: the element kernel and the gather-map kernel of the
 // single-problem path over all problems (same per-entry arithmetic and order,
 // so each matrix gets the bits FGPU_ALGO_TWO_PHASE gives it alone) ----
@@ -1097,10 +1202,12 @@ constexpr int kBatchTriFloats = 7 * 10 + 7 * 55 + 7 * 210;
 
 template <int MODE>
 __global__ void __launch_bounds__(256) batch_element_kernel(int nprob, const BatchProblem* __restrict__ probs,
-                                                            const int64_t* __restrict__ elem_off, int64_t total,
-                                                            const float* __restrict__ Thg, const float* __restrict__ Tlg) {
+                                                            const int64_t* __restrict__ grp_off, int64_t total_groups,
+                                                            const float* __restrict__ Thg, const float* __restrict__ Tlg,
+                                                            int* __restrict__ status) {
     __shared__ float Th[kBatchTriFloats];
     __shared__ float Tl[MODE == kModeDF64 ? kBatchTriFloats : 1];
+    __shared__ float4 srec[8 * 32 * 4];                  // per warp: the records of 32 elements
     for (int k = threadIdx.x; k < kBatchTriFloats; k += blockDim.x) {
         Th[k] = Thg[k];
         if (MODE == kModeDF64) Tl[k] = Tlg[k];
@@ -1108,27 +1215,35 @@ __global__ void __launch_bounds__(256) batch_element_kernel(int nprob, const Bat
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    float4* wrec = srec + (threadIdx.x >> 5) * 32 * 4;
     int p = -1;
-    int64_t pe0 = 0, pe1 = 0;
-    for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < total; g += nw) {   // one warp per element
-        if (g < pe0 || g >= pe1) {
-            p = batch_find(elem_off, nprob, g);
-            pe0 = elem_off[p];
-            pe1 = elem_off[p + 1];
+    int64_t pg0 = 0, pg1 = 0;
+    // one warp per group of 32 consecutive elements of one problem (the single-problem kernel's groups)
+    for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < total_groups; g += nw) {
+        if (g < pg0 || g >= pg1) {
+            p = batch_find(grp_off, nprob, g);
+            pg0 = grp_off[p];
+            pg1 = grp_off[p + 1];
         }
         const BatchProblem& P = probs[p];
-        const int64_t e = g - pe0;
-        const int n = P.n, ntri = n * (n + 1) / 2, to = batch_tri_off(P.order);
-        float ch[7], cl[7];
-        load_record(P.rec + 4 * e, ch, cl, MODE == kModeDF64);
-        for (int t = lane; t < ntri; t += 32) {
-            if (MODE == kModeDF64) {
-                const df v = coef_entry_df(ch, cl, Th + to, Tl + to, ntri, t);
-                reinterpret_cast<float2*>(P.kbuf)[e * ntri + t] = make_float2(v.hi, v.lo);
-            } else {
-                reinterpret_cast<float*>(P.kbuf)[e * ntri + t] = coef_entry_f(ch, Th + to, ntri, t);
-            }
+        const int64_t e0 = (g - pg0) * 32;
+        const int cnt = (int)(P.nt - e0 < 32 ? P.nt - e0 : 32);
+        if (lane < cnt)
+            geometry_df_record(e0 + lane, P.xyz, P.tets, P.kappa, d2df(P.kappa_c), d2df(P.mass), df{1.0f, 0.0f}, wrec + 4 * lane,
+                               status);
+        __syncwarp();
+        float th0[7], tl0[7], th1[7], tl1[7];
+        const int to = batch_tri_off(P.order);
+        if (P.order == 1) {
+            tri_lane_tables<MODE, 4>(Th + to, Tl + to, lane, th0, tl0, th1, tl1);
+            tri_group_entries<MODE, 4>(P.kbuf, e0, cnt, wrec, Th + to, Tl + to, lane, th0, tl0, th1, tl1);
+        } else if (P.order == 2) {
+            tri_lane_tables<MODE, 10>(Th + to, Tl + to, lane, th0, tl0, th1, tl1);
+            tri_group_entries<MODE, 10>(P.kbuf, e0, cnt, wrec, Th + to, Tl + to, lane, th0, tl0, th1, tl1);
+        } else {
+            tri_group_entries<MODE, 20>(P.kbuf, e0, cnt, wrec, Th + to, Tl + to, lane, th0, tl0, th1, tl1);
         }
+        __syncwarp();
     }
 }
 
@@ -1211,8 +1326,8 @@ static int batch_tri_tables(fgpu_ctx* ctx, float** h, float** l) {
     return FGPU_OK;
 }
 
-int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
-                           int64_t total_elems, const int64_t* d_nz_off, int64_t total_nnz, int f32, int threads,
+int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_grp_off,
+                           int64_t total_groups, const int64_t* d_nz_off, int64_t total_nnz, int f32, int threads,
                            int accumulate) {
     float *Th = nullptr, *Tl = nullptr;
     int rc = batch_tri_tables(ctx, &Th, &Tl);
@@ -1220,11 +1335,15 @@ int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     {
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((total_elems + 7) / 8, (int64_t)sms * 16));
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((total_groups + 7) / 8, (int64_t)sms * 16));
         PendingEvent ev;
         prof_begin(ctx, "batch_elements", ev);
-        if (f32) batch_element_kernel<kModeF32><<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_elem_off, total_elems, Th, Tl);
-        else batch_element_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_elem_off, total_elems, Th, Tl);
+        if (f32)
+            batch_element_kernel<kModeF32><<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_grp_off, total_groups, Th, Tl,
+                                                                                 ctx->d_status);
+        else
+            batch_element_kernel<kModeDF64><<<(int)blocks, 256, 0, ctx->stream>>>(nprob, d_probs, d_grp_off, total_groups, Th, Tl,
+                                                                                  ctx->d_status);
         prof_end(ctx, ev);
         FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     }
@@ -1278,17 +1397,11 @@ int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, c
 //   No float atomics; the gather is a streaming pass over gptr, gidx and the
 //   CSR values.
 // ---------------------------------------------------------------------------
-// The coefficient records are formed in the kernel (none in device memory): each warp forms the
-// records of 32 consecutive elements, one per lane (geometry_df_record, the same arithmetic as
-// geometry_df_kernel), into shared memory, then their element matrices. With NTRI <= 64 each lane keeps
-// the table values of its (at most two) entries in registers across the elements; with more entries
-// (P3) two elements share each table value read from shared memory.
 template <int MODE, int N>
 __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, GeoIn geo, const float* __restrict__ Thg,
                                                           const float* __restrict__ Tlg, void* __restrict__ kbuf,
                                                           int* __restrict__ status) {
     constexpr int NTRI = N * (N + 1) / 2;
-    constexpr int EPW = NTRI >= 32 ? 1 : 32 / NTRI;      // elements per warp pass (P1: 3)
     constexpr bool DF = MODE == kModeDF64;
     __shared__ float Th[7 * NTRI];
     __shared__ float Tl[DF ? 7 * NTRI : 1];
@@ -1299,23 +1412,10 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, GeoIn geo,
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int sub = lane / NTRI < EPW ? lane / NTRI : EPW;  // element slot of this lane (EPW: idle)
-    const int t0 = EPW > 1 ? lane - sub * NTRI : lane;
     const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    constexpr int TS = EPW > 1 ? NTRI : 32;
-    const int t1 = t0 + TS;
     float th0[7], tl0[7], th1[7], tl1[7];
-    if (NTRI <= 64) {
-#pragma unroll
-        for (int k = 0; k < 7; ++k) {
-            const bool ok0 = sub < EPW && t0 < NTRI, ok1 = sub < EPW && t1 < NTRI;
-            th0[k] = ok0 ? Th[k * NTRI + t0] : 0.0f;
-            th1[k] = ok1 ? Th[k * NTRI + t1] : 0.0f;
-            tl0[k] = (DF && ok0) ? Tl[k * NTRI + t0] : 0.0f;
-            tl1[k] = (DF && ok1) ? Tl[k * NTRI + t1] : 0.0f;
-        }
-    }
+    if (NTRI <= 64) tri_lane_tables<MODE, N>(Th, Tl, lane, th0, tl0, th1, tl1);   // the same for every element
     const df kc = d2df(geo.kc), mc = d2df(geo.mc);
     const df ksc = geo.kscale ? d2df(*geo.kscale) : df{1.0f, 0.0f};
     float4* wrec = srec + (threadIdx.x >> 5) * 32 * 4;
@@ -1323,75 +1423,7 @@ __global__ void __launch_bounds__(256) element_tri_kernel(int64_t nt, GeoIn geo,
         if (g0 + lane < nt) geometry_df_record(g0 + lane, geo.xyz, geo.tets, geo.kappa, kc, mc, ksc, wrec + 4 * lane, status);
         __syncwarp();
         const int cnt = (int)(nt - g0 < 32 ? nt - g0 : 32);
-        if (NTRI <= 64) {
-            for (int j0 = 0; j0 < cnt; j0 += EPW) {
-                const int j = j0 + sub;
-                if (sub >= EPW || j >= cnt) continue;
-                float ch[7], cl[7];
-                load_record_shared(wrec + 4 * j, ch, cl, DF);
-                const int64_t e = g0 + j;
-                if (DF) {
-                    float2* kb = reinterpret_cast<float2*>(kbuf) + e * NTRI;
-                    if (t0 < NTRI) {
-                        const df v = coef_entry_df_reg(ch, cl, th0, tl0);
-                        kb[t0] = make_float2(v.hi, v.lo);
-                    }
-                    if (t1 < NTRI) {
-                        const df v = coef_entry_df_reg(ch, cl, th1, tl1);
-                        kb[t1] = make_float2(v.hi, v.lo);
-                    }
-                } else {
-                    float* kb = reinterpret_cast<float*>(kbuf) + e * NTRI;
-                    if (t0 < NTRI) {
-                        float v = 0.0f;
-#pragma unroll
-                        for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th0[k], v);
-                        kb[t0] = v;
-                    }
-                    if (t1 < NTRI) {
-                        float v = 0.0f;
-#pragma unroll
-                        for (int k = 0; k < 7; ++k) v = fmaf(ch[k], th1[k], v);
-                        kb[t1] = v;
-                    }
-                }
-            }
-        } else {
-            for (int j = 0; j < cnt; j += 2) {
-                const bool two = j + 1 < cnt;
-                float ch0[7], cl0[7], ch1[7], cl1[7];
-                load_record_shared(wrec + 4 * j, ch0, cl0, DF);
-                load_record_shared(wrec + 4 * (two ? j + 1 : j), ch1, cl1, DF);
-                const int64_t e = g0 + j;
-                for (int t = lane; t < NTRI; t += 32) {
-                    float th[7], tl[7];
-#pragma unroll
-                    for (int k = 0; k < 7; ++k) {
-                        th[k] = Th[k * NTRI + t];
-                        tl[k] = DF ? Tl[k * NTRI + t] : 0.0f;
-                    }
-                    if (DF) {
-                        float2* kb = reinterpret_cast<float2*>(kbuf);
-                        const df v0 = coef_entry_df_reg(ch0, cl0, th, tl);
-                        kb[e * NTRI + t] = make_float2(v0.hi, v0.lo);
-                        if (two) {
-                            const df v1 = coef_entry_df_reg(ch1, cl1, th, tl);
-                            kb[(e + 1) * NTRI + t] = make_float2(v1.hi, v1.lo);
-                        }
-                    } else {
-                        float* kb = reinterpret_cast<float*>(kbuf);
-                        float v0 = 0.0f, v1 = 0.0f;
-#pragma unroll
-                        for (int k = 0; k < 7; ++k) {
-                            v0 = fmaf(ch0[k], th[k], v0);
-                            v1 = fmaf(ch1[k], th[k], v1);
-                        }
-                        kb[e * NTRI + t] = v0;
-                        if (two) kb[(e + 1) * NTRI + t] = v1;
-                    }
-                }
-            }
-        }
+        tri_group_entries<MODE, N>(kbuf, g0, cnt, wrec, Th, Tl, lane, th0, tl0, th1, tl1);
         __syncwarp();
     }
 }

@@ -28,11 +28,12 @@ struct fgpu_batch {
     int nprob = 0;
     int f32 = 0;
     int acc_floats = 0;              // per-warp staging floats (max over problems of EPB * maxrow * width)
-    int64_t total_rows = 0, total_elems = 0, total_nnz = 0;
+    int64_t total_rows = 0, total_elems = 0, total_nnz = 0, total_groups = 0;
     bool two_phase = false;          // element buffers + gather maps (else the fused row-owner gather)
     BatchProblem* d_probs = nullptr;
     int64_t* d_row_off = nullptr;
     int64_t* d_elem_off = nullptr;
+    int64_t* d_grp_off = nullptr;    // groups of 32 elements per problem (two-phase element kernel)
     int64_t* d_nz_off = nullptr;
     unsigned long long* d_counter = nullptr;
     BatchLaunch launch;
@@ -69,15 +70,17 @@ int batch_finish(fgpu_ctx* ctx) {
 int run_gather(fgpu_batch* b, const BatchLaunch& cfg, int accumulate) {
     fgpu_ctx* ctx = b->ctx;
     if (b->two_phase)
-        return launch_batch_two_phase(ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems, b->d_nz_off, b->total_nnz, b->f32,
+        return launch_batch_two_phase(ctx, b->nprob, b->d_probs, b->d_grp_off, b->total_groups, b->d_nz_off, b->total_nnz, b->f32,
                                       cfg.threads, accumulate);
     return launch_batch_gather(ctx, b->nprob, b->d_probs, b->d_row_off, b->total_rows, b->f32, b->acc_floats, b->d_counter, cfg,
                                accumulate);
 }
 
 int run(fgpu_batch* b, const BatchLaunch& cfg, int accumulate) {
-    int rc = launch_batch_geometry(b->ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems);
-    if (rc) return rc;
+    if (!b->two_phase) {             // the two-phase element kernel forms the coefficient records itself
+        int rc = launch_batch_geometry(b->ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems);
+        if (rc) return rc;
+    }
     return run_gather(b, cfg, accumulate);
 }
 
@@ -132,7 +135,7 @@ int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const 
     if (!ctx || nprob <= 0 || !mats || !descs || !out) return batch_err(ctx, FGPU_ERR_INVALID, "batch_create: bad arguments");
     *out = nullptr;
     std::vector<BatchProblem> probs(nprob);
-    std::vector<int64_t> row_off(nprob + 1, 0), elem_off(nprob + 1, 0);
+    std::vector<int64_t> row_off(nprob + 1, 0), elem_off(nprob + 1, 0), grp_off(nprob + 1, 0);
     int f32 = -1, acc = 0;
     for (int k = 0; k < nprob; ++k) {
         const fgpu_matrix* A = mats[k];
@@ -183,6 +186,7 @@ int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const 
         P.val = A->d_val;
         row_off[k + 1] = row_off[k] + A->nrows;
         elem_off[k + 1] = elem_off[k] + V->mesh->nt;
+        grp_off[k + 1] = grp_off[k] + (V->mesh->nt + 31) / 32;
         acc = std::max(acc, epb_of(V->order) * P.maxrow * (mf32 ? 1 : 2));
     }
     // two-phase when every space's gather map and every matrix's element buffer exist or fit
@@ -234,16 +238,19 @@ int fgpu_batch_create(fgpu_ctx* ctx, int nprob, fgpu_matrix* const* mats, const 
     b->acc_floats = (acc + 3) & ~3;
     b->total_rows = row_off[nprob];
     b->total_elems = elem_off[nprob];
+    b->total_groups = grp_off[nprob];
     b->mats.assign(mats, mats + nprob);
     cudaError_t e = cudaMalloc(&b->d_probs, nprob * sizeof(BatchProblem));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_row_off, (nprob + 1) * sizeof(int64_t));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_elem_off, (nprob + 1) * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_grp_off, (nprob + 1) * sizeof(int64_t));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_nz_off, (nprob + 1) * sizeof(int64_t));
     if (e == cudaSuccess) e = cudaMemcpy(b->d_nz_off, nz_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_probs, probs.data(), nprob * sizeof(BatchProblem), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_row_off, row_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_elem_off, elem_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_grp_off, grp_off.data(), (nprob + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         ctx->err = std::string("batch_create: ") + cudaGetErrorString(e);
         fgpu_batch_destroy(b);
@@ -257,7 +264,7 @@ int fgpu_batch_assemble(fgpu_ctx* ctx, fgpu_batch* b, int accumulate) {
     if (!ctx || !b || b->ctx != ctx) return batch_err(ctx, FGPU_ERR_INVALID, "batch_assemble: bad arguments");
     if (!b->tuned && !accumulate && !ctx->capturing) {
         // the candidates overwrite the values ('='), so tuning runs only on '=' calls
-        int rc = launch_batch_geometry(ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems);
+        int rc = b->two_phase ? FGPU_OK : launch_batch_geometry(ctx, b->nprob, b->d_probs, b->d_elem_off, b->total_elems);
         if (!rc) rc = tune(b);
         if (rc) return rc;
     }
@@ -301,6 +308,7 @@ int fgpu_batch_destroy(fgpu_batch* b) {
     cudaFree(b->d_probs);
     cudaFree(b->d_row_off);
     cudaFree(b->d_elem_off);
+    cudaFree(b->d_grp_off);
     cudaFree(b->d_counter);
     cudaFree(b->d_nz_off);
     delete b;

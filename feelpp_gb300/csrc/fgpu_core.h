@@ -458,8 +458,8 @@ struct BatchLaunch {                 // launch configuration picked by the batch
 };
 int launch_batch_geometry(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
                           int64_t total_elems);
-int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_elem_off,
-                           int64_t total_elems, const int64_t* d_nz_off, int64_t total_nnz, int f32, int threads,
+int launch_batch_two_phase(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_grp_off,
+                           int64_t total_groups, const int64_t* d_nz_off, int64_t total_nnz, int f32, int threads,
                            int accumulate);
 int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, const int64_t* d_row_off,
                         int64_t total_rows, int f32, int acc_floats, unsigned long long* d_counter,
