@@ -135,35 +135,40 @@ struct AmgSell {
     const float* val = nullptr;
 };
 
+// row i (in sorted order) of a SELL sweep: the entries of its slice column, four loads issued together
+// (memory-level parallelism), summed in entry order, then the epilogue on the original row
+template <int MODE>
+__device__ __forceinline__ void sell_row(const AmgSweep& s, const AmgSell& m, int64_t i) {
+    const int64_t sl = i >> 5;
+    const int L = __ldg(m.len + sl);
+    const int64_t base = __ldg(m.ptr + sl) + (i & 31);
+    float acc = 0.0f;
+    int k = 0;
+    for (; k + 4 <= L; k += 4) {
+        const int64_t j = base + (int64_t)k * 32;
+        const int32_t c0 = __ldg(m.col + j), c1 = __ldg(m.col + j + 32), c2 = __ldg(m.col + j + 64), c3 = __ldg(m.col + j + 96);
+        const float v0 = __ldg(m.val + j), v1 = __ldg(m.val + j + 32), v2 = __ldg(m.val + j + 64), v3 = __ldg(m.val + j + 96);
+        const float x0 = __ldg(s.x + c0), x1 = __ldg(s.x + c1), x2 = __ldg(s.x + c2), x3 = __ldg(s.x + c3);
+        acc = fmaf(v0, x0, acc);
+        acc = fmaf(v1, x1, acc);
+        acc = fmaf(v2, x2, acc);
+        acc = fmaf(v3, x3, acc);
+    }
+    for (; k < L; ++k) {
+        const int64_t j = base + (int64_t)k * 32;
+        acc = fmaf(__ldg(m.val + j), __ldg(s.x + __ldg(m.col + j)), acc);
+    }
+    if (i < s.n) amg_epilogue<MODE>(s, __ldg(m.perm + i), acc);
+}
+
 // one sweep of a level operator in SELL form: thread per (sorted) row, then the epilogue on the
 // original row; every lane of a warp belongs to one slice, so the entry loop is warp-uniform
 template <int MODE>
 __global__ void __launch_bounds__(128) amg_sell_kernel(AmgSweep s, AmgSell m, const int* __restrict__ stop) {
     if (stop && *stop) return;
     const int64_t total = m.nslices * 32;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t sl = i >> 5;
-        const int L = __ldg(m.len + sl);
-        const int64_t base = __ldg(m.ptr + sl) + (i & 31);
-        // four entries' loads issued together (memory-level parallelism), summed in entry order
-        float acc = 0.0f;
-        int k = 0;
-        for (; k + 4 <= L; k += 4) {
-            const int64_t j = base + (int64_t)k * 32;
-            const int32_t c0 = __ldg(m.col + j), c1 = __ldg(m.col + j + 32), c2 = __ldg(m.col + j + 64), c3 = __ldg(m.col + j + 96);
-            const float v0 = __ldg(m.val + j), v1 = __ldg(m.val + j + 32), v2 = __ldg(m.val + j + 64), v3 = __ldg(m.val + j + 96);
-            const float x0 = __ldg(s.x + c0), x1 = __ldg(s.x + c1), x2 = __ldg(s.x + c2), x3 = __ldg(s.x + c3);
-            acc = fmaf(v0, x0, acc);
-            acc = fmaf(v1, x1, acc);
-            acc = fmaf(v2, x2, acc);
-            acc = fmaf(v3, x3, acc);
-        }
-        for (; k < L; ++k) {
-            const int64_t j = base + (int64_t)k * 32;
-            acc = fmaf(__ldg(m.val + j), __ldg(s.x + __ldg(m.col + j)), acc);
-        }
-        if (i < s.n) amg_epilogue<MODE>(s, __ldg(m.perm + i), acc);
-    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        sell_row<MODE>(s, m, i);
 }
 
 // the same sweep for levels with few rows: a block of W warps per slice, warp w summing the entries
@@ -315,7 +320,8 @@ void sell_sweep(cudaStream_t st, const fgpu_amg::Level& V, const AmgSweep& s, co
     // one thread per slot, no grid-stride loop: slices differ in length, and many short-lived blocks
     // keep the SMs fuller than a few long-lived ones (measured: 46 % warps active with two waves). Blocks
     // of 128 threads (4 slices): CG + AMG iterations 1.21 / 6.45 ms at P2 / P3 64^3, against 1.28 / 6.86 ms
-    // with 256 and 1.29 / 6.68 ms with 64
+    // with 256 and 1.29 / 6.68 ms with 64; persistent warps taking four slices at a time from an atomic
+    // counter: 1.35 / 6.93 ms
     const int g = (int)std::max<int64_t>(1, (V.nslices * 32 + 127) / 128);
     amg_sell_kernel<MODE><<<g, 128, 0, st>>>(s, m, stop);
 }
