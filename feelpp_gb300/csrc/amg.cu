@@ -283,9 +283,12 @@ int lanes_for(int64_t n, int64_t nnz) {
     return m <= 6 ? 4 : m <= 12 ? 8 : m <= 24 ? 16 : 32;
 }
 
+// grid cap of the CSR sweeps (prolongators, restrictions); one thread group per row without a cap took
+// 1.225 against 1.214 ms per P2 64^3 CG + AMG iteration
+constexpr int64_t kAmgSweepCap = 152 * 16;
 int grid_for(int64_t rows, int G) {
     const int64_t per = 256 / G;
-    return (int)std::max<int64_t>(1, std::min<int64_t>((rows + per - 1) / per, 152 * 16));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((rows + per - 1) / per, kAmgSweepCap));
 }
 
 template <int MODE>

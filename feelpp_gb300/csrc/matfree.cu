@@ -124,12 +124,14 @@ __global__ void __launch_bounds__(128) mf_element_f32_gated(int64_t nt, const in
 }
 
 // launch shape of the binary32 element phase: 32 WPB threads per block, enough blocks for one pass
+// grid cap of the binary32 element phase (without it: P2 96^3 0.266 against 0.252 ms, P3 0.784 against 0.793)
+constexpr int64_t kMfElemCap = 152 * 32;
 template <int N>
 static void launch_mf_element_f32(cudaStream_t st, int64_t nt, const int32_t* l2n, const float4* rec, const float* T7f,
                                   const float* x, const uint8_t* mask, float* ye, const int* stop, bool gated) {
     constexpr int WPB = MfF32Shape<N>::WPB, EW = 32 * MfF32Shape<N>::EPT;
     const int64_t per_block = (int64_t)WPB * EW;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nt + per_block - 1) / per_block, 152 * 32));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nt + per_block - 1) / per_block, kMfElemCap));
     if (gated) mf_element_f32_gated<N><<<blocks, 32 * WPB, 0, st>>>(nt, l2n, rec, T7f, x, mask, ye, stop);
     else mf_element_f32_kernel<N><<<blocks, 32 * WPB, 0, st>>>(nt, l2n, rec, T7f, x, mask, ye);
 }
