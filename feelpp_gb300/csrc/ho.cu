@@ -162,6 +162,17 @@ __device__ __forceinline__ double ho_map(const double* X /* GN x 3 */, const dou
 }
 
 __device__ __forceinline__ df ldf(const float* h, const float* l, int k) { return df{h[k], l[k]}; }
+// s + e += a b: the exact product of the high parts (FMA) split into its rounded value, added to s by
+// TwoSum, and its error; the cross terms a.hi b.lo + a.lo b.hi and the TwoSum error go to e
+__device__ __forceinline__ void ho_dot_term(df a, df b, float& s, float& e) {
+    const float p = f_mul(a.hi, b.hi);
+    e = f_fma(a.hi, b.lo, e);
+    e = f_fma(a.lo, b.hi, e);
+    e = f_add(e, f_fma(a.hi, b.hi, -p));
+    const df t = two_sum(s, p);
+    s = t.hi;
+    e = f_add(e, t.lo);
+}
 __device__ __forceinline__ df dfun(float2 v) { return df{v.x, v.y}; }
 __device__ __forceinline__ float2 dfpack(df v) { return make_float2(v.hi, v.lo); }
 
@@ -287,10 +298,12 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
             for (int k = 0; k < 7; ++k) GsG[q * 7 + k] = g[k];
         }
         __syncwarp();
-        df acc[PER];
-        float accf[PER];
+        // double-float entries as a compensated dot product over the points: the high parts of the exact
+        // products through TwoSum, their errors, the cross terms and the low parts in a binary32
+        // accumulator (the arithmetic of the affine kernel's coef_entry_df); binary32: plain sums
+        float acs[PER], ace[PER];
 #pragma unroll
-        for (int u = 0; u < PER; ++u) { acc[u] = df{0.0f, 0.0f}; accf[u] = 0.0f; }
+        for (int u = 0; u < PER; ++u) { acs[u] = 0.0f; ace[u] = 0.0f; }
         for (int q = 0; q < Q; ++q) {
             const float2* G = &GsG[q * 7];
             for (int jl = gl; jl < N; jl += LPG) {
@@ -319,17 +332,16 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
                 const int i = ti[t], j = tj[t];
                 const int bi = (q * N + i) * 3;
                 if (MODE == kHoDF64) {
-                    df v = df_mul(ldf(Dh, Dl, bi), dfun(WsG[j]));
-                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 1), dfun(WsG[N + j])));
-                    v = df_add(v, df_mul(ldf(Dh, Dl, bi + 2), dfun(WsG[2 * N + j])));
-                    v = df_add(v, df_mul(dfun(G[6]), df_mul(ldf(Ph, Pl, q * N + i), ldf(Ph, Pl, q * N + j))));
-                    acc[u] = df_add(acc[u], v);
+                    ho_dot_term(ldf(Dh, Dl, bi), dfun(WsG[j]), acs[u], ace[u]);
+                    ho_dot_term(ldf(Dh, Dl, bi + 1), dfun(WsG[N + j]), acs[u], ace[u]);
+                    ho_dot_term(ldf(Dh, Dl, bi + 2), dfun(WsG[2 * N + j]), acs[u], ace[u]);
+                    ho_dot_term(dfun(G[6]), df_mul(ldf(Ph, Pl, q * N + i), ldf(Ph, Pl, q * N + j)), acs[u], ace[u]);
                 } else {
                     float v = Dh[bi] * WsG[j].x;
                     v = fmaf(Dh[bi + 1], WsG[N + j].x, v);
                     v = fmaf(Dh[bi + 2], WsG[2 * N + j].x, v);
                     v = fmaf(G[6].x, Ph[q * N + i] * Ph[q * N + j], v);
-                    accf[u] += v;
+                    acs[u] += v;
                 }
             }
             __syncwarp();
@@ -338,8 +350,8 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
         for (int u = 0; u < PER && live; ++u) {
             const int t = gl + LPG * u;
             if (t >= NTRI) break;
-            if (MODE == kHoDF64) reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = dfpack(acc[u]);
-            else reinterpret_cast<float*>(kbuf)[e * NTRI + t] = accf[u];
+            if (MODE == kHoDF64) reinterpret_cast<float2*>(kbuf)[e * NTRI + t] = dfpack(two_sum(acs[u], ace[u]));
+            else reinterpret_cast<float*>(kbuf)[e * NTRI + t] = acs[u];
         }
         __syncwarp();
     }
