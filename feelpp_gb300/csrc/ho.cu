@@ -225,6 +225,9 @@ __global__ void __launch_bounds__(128) ho_element_kernel(int64_t nt, const doubl
             const float* gl = gdl + (size_t)q * 3 * GN;
             float2 g[7];
             if (MODE == kHoDF64) {
+                // (the map's entries keep double-float multiply-adds: sum_g X_g grad(psi_g) cancels heavily,
+                // since the gradients sum to zero, and a compensated dot product with one binary32 error
+                // term missed the 1e-12 parity on curved P2 elements)
                 df K[9];
 #pragma unroll
                 for (int k = 0; k < 9; ++k) K[k] = df{0.0f, 0.0f};
