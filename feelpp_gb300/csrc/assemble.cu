@@ -2203,6 +2203,8 @@ __global__ void __launch_bounds__(256) gather_el_kernel(int64_t nrows, const int
         for (int pos = lane; pos < len; pos += 32) {
             const int64_t ks = s0 + pos;
             const uint32_t p0 = __ldg(gptr + ks), p1 = __ldg(gptr + ks + 1);
+            // (a compensated sum per component, as in gather_map_kernel, took 4.71 against 4.25 ms for the
+            // P2 48^3 elasticity assembly: the nine components' two accumulators)
             df acc[9];
             float accf[9];
 #pragma unroll
