@@ -1387,8 +1387,9 @@ int launch_batch_gather(fgpu_ctx* ctx, int nprob, const BatchProblem* d_probs, c
 // Two-phase assembly.
 //   Phase 1 (element_tri_kernel): each element matrix is computed once, as its
 //   upper triangle (NTRI = n (n + 1) / 2 entries; the reference tensors are
-//   exactly symmetric), into a device buffer; one warp per element, lanes over
-//   entries, the element's record loaded once per lane, contiguous writes.
+//   exactly symmetric), into a device buffer; each warp forms the coefficient
+//   records of 32 elements (one per lane, in shared memory), then their
+//   matrices with lanes over entries, contiguous writes.
 //   Phase 2 (gather_map_kernel): one thread per CSR entry sums its
 //   contributions in element order through a gather map built once per space
 //   (gptr: nnz + 1 offsets, gidx: buffer index of each contribution), which is
