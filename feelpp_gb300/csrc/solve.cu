@@ -73,6 +73,12 @@ static int spmv_blocks(const fgpu_matrix* A, int G) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(need, 152 * 16));
 }
 
+// without per-block partial sums the grid does not change the result: one block per 256 / G rows
+// (P2 64^3 y = A x: 0.40 against 0.43 ms with the capped grid; 8 lanes per row took 0.48 ms)
+static int spmv_blocks_uncapped(const fgpu_matrix* A, int G) {
+    return (int)std::max<int64_t>(1, (A->nrows + (256 / G) - 1) / (256 / G));
+}
+
 
 int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y, double alpha_b, const double* b) {
     (void)alpha_b;
@@ -84,7 +90,7 @@ int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y,
     PendingEvent ev;
     prof_begin(ctx, "spmv", ev);
     launch_spmv_t<PolF64>(ctx->stream, A, (const double*)A->d_val, G, x, y, b ? 1 : 0, b, nullptr, nullptr, nullptr,
-                          spmv_blocks(A, G));
+                          spmv_blocks_uncapped(A, G));
     prof_end(ctx, ev);
     FGPU_CUDA_CHECK(ctx, cudaGetLastError());
     return FGPU_OK;

@@ -144,6 +144,42 @@ def test_dirichlet_modes(env, oracle, mode_name, mode):
     assert_values_close(l.to_numpy(), b, what="rhs after on()")
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("order,n,frac,precision", [(2, 8, 0.2, "f64"), (1, 20, 0.05, "f64"), (3, 5, 0.5, "f64"),
+                                                    (2, 8, 0.2, "f32")])
+def test_dirichlet_scattered_rows(env, oracle, mode, order, n, frac, precision):
+    """on() over a seeded random subset of the dofs (rows eliminated anywhere in the numbering, groups of
+    32 rows with none, some or all of them eliminated, rows longer than 32 entries), random values g, a
+    random right-hand side and diag = 2.5, on FP64 and FP32 matrices."""
+    xyz, tets = mesh(n, perturb=0.2)
+    M, V, a = device_matrix(env, xyz, tets, order, kappa=1.0, mass=0.5, precision=precision)
+    ia, ja, val = a.csr()
+    N = len(ia) - 1
+    rng = np.random.default_rng(100 + mode + 10 * order)
+    dofs = np.sort(rng.choice(N, size=max(1, int(frac * N)), replace=False)).astype(np.int32)
+    dofs[: min(64, len(dofs))] = np.arange(min(64, len(dofs)), dtype=np.int32)   # the first two groups eliminated
+    dofs = np.unique(dofs)
+    g = rng.standard_normal(len(dofs))
+    b0 = rng.standard_normal(N)
+    rhs = V.element()
+    rhs.upload(b0)
+    bc = fpp.DirichletBC(V, dofs, g)
+    a.apply_bc(bc, rhs=rhs, type={0: "elimination", 1: "elimination_symmetric", 2: "elimination_keep_diagonal"}[mode],
+               diag=2.5)
+    mask = np.zeros(N, np.uint8)
+    mask[dofs] = 1
+    gg = np.zeros(N)
+    gg[dofs] = g
+    b = b0.copy()
+    oracle.dirichlet(ia, ja, val, b, mask, g=gg, mode=mode, diag=2.5)
+    got = a.values()
+    if precision == "f32":
+        val = val.astype(np.float32).astype(np.float64)
+    assert np.array_equal(got == 0.0, val == 0.0)
+    assert_values_close(got, val, what="matrix after on()")
+    assert_values_close(rhs.to_numpy(), b, what="rhs after on()")
+
+
 def test_bad_element_reported(env):
     xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [0, 0, 1]], dtype=float)
     tets = np.array([[0, 1, 2, 3], [0, 1, 2, 4]], dtype=np.int32)   # first tet is flat (det K = 0)
