@@ -64,13 +64,15 @@ def parse():
     p.add_argument("--with-plain", action="store_true", help="matfree: also time the plain df64 matrix-free CG")
     p.add_argument("--with-csr", action="store_true", help="matfree: also assemble the FP64 CSR and solve with it")
     p.add_argument("--with-gamg", action="store_true", help="assembly / matfree --with-csr: also solve with pc=gamg")
-    p.add_argument("--probe", default=None, choices=[None, "cg", "gamg", "gamg_rigid", "pmg", "apply", "gmres", "elements_tc"],
+    p.add_argument("--probe", default=None,
+                   choices=[None, "cg", "gamg", "gamg_rigid", "pmg", "apply", "gmres", "elements_tc", "heat_ops"],
                    help="profiling aid: 'cg' assembles the P2 system and runs 48 CG iterations (FP64 and mixed); "
                         "'gamg' builds the AMG hierarchy of the Poisson system (kappa = 1) and runs one "
                         "AMG-preconditioned CG solve to 1e-10; 'pmg' sets up the matrix-free Poisson operators "
                         "(kappa = 1, perturbation 0.1h) with the P1 coarse level and runs one p-multigrid solve; "
                         "'elements_tc' times the FP64 two-phase element phase with the CUDA-core df64 kernel and "
-                        "with the tensor-core (bf16 slices) kernel, --steps assemblies each")
+                        "with the tensor-core (bf16 slices) kernel, --steps assemblies each; 'heat_ops' times each "
+                        "operation of one P2 backward-Euler step (reassembly, M u, axpby, Dirichlet rows) on its own")
     return p.parse_args()
 
 
@@ -872,6 +874,54 @@ def run_probe_apply(args):
     print(json.dumps(out), flush=True)
 
 
+def run_probe_heat_ops(args):
+    """The operations of one P2 heat step (reassembly of M + dt kappa(t) K, b = M u^n, b += dt F, Dirichlet
+    rows in the symmetric mode) on the n^3 Kuhn cube, each timed alone over 20 calls with CUDA events
+    after 3 warm-up calls, with the library's per-kernel times; prints one JSON line."""
+    import ctypes as C
+    import torch
+    import feelpp_gb300 as fpp
+    from feelpp_gb300 import meshgen
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    env = fpp.Environment(device=0, stream=C.c_void_p(stream.cuda_stream), profile=True)
+    xyz, tets = meshgen.kuhn_box(args.n, perturb=0.15, seed=1234)
+    M = fpp.Mesh(xyz, tets, env=env)
+    V = fpp.Pch(M, 2)
+    u, v = V.element(), V.element()
+    dt = 0.01
+    kt = fpp.DeviceScalar(env, 1.0)
+    mass = fpp.form2(test=V, trial=V)
+    mass.assign(fpp.integrate(fpp.elements(M), fpp.idt(u) * fpp.id(v)))
+    F = fpp.form1(test=V)
+    F.assign(fpp.integrate(fpp.elements(M), fpp.sine_source() * fpp.id(v)))
+    bc = fpp.DirichletBC(V, V.boundary_dofs())
+    A = fpp.form2(test=V, trial=V)
+    integral = fpp.integrate(fpp.elements(M), dt * kt * fpp.inner(fpp.gradt(u), fpp.grad(v)) + fpp.idt(u) * fpp.id(v))
+    b, un = V.element(), V.element()
+    ops = {"reassembly": lambda: A.assign(integral), "mass_mult": lambda: mass.mult(un, b),
+           "axpby": lambda: b.axpby(dt, F.vec, 1.0), "dirichlet": lambda: A.apply_bc(bc, rhs=b)}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"workload": "P2 heat step operations, %d^3 Kuhn cube (N=%d, nnz=%d)" % (args.n, V.ndof, A.nnz)}
+    for name, f in ops.items():
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        env.prof_reset()
+        e0.record(stream)
+        for _ in range(20):
+            f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"ms": e0.elapsed_time(e1) / 20}
+        for kname in ("assemble_elements", "assemble_gather", "spmv", "dirichlet"):
+            cnt, ms = env.prof(kname)
+            if cnt:
+                out[name]["kernel_ms_" + kname] = ms / cnt
+    print(json.dumps(out), flush=True)
+
+
 def run_probe_elements_tc(args):
     """FP64 (df64) two-phase assemblies of the P-order Laplace+mass form (lognormal kappa, perturbation
     0.15h) with the element matrices on the CUDA cores and on the tensor cores (FGPU_TC_DF64: exact bf16
@@ -1522,6 +1572,9 @@ def main():
         return
     if args.probe == "elements_tc":
         run_probe_elements_tc(args)
+        return
+    if args.probe == "heat_ops":
+        run_probe_heat_ops(args)
         return
     if args.probe == "pmg":
         run_probe_pmg(args)
