@@ -53,6 +53,7 @@ static void launch_spmv_t(cudaStream_t s, const fgpu_matrix* A, const typename P
                           typename PL::S* y, int mode, const typename PL::S* b, const typename PL::S* wdot,
                           typename PL::D* partial, const CGScalars<PL>* sc, int blocks) {
     switch (G) {
+        case 2: spmv_kernel<PL, 2><<<blocks, 256, 0, s>>>(A->nrows, A->d_ia, A->d_ja, val, x, y, mode, b, wdot, partial, sc); break;
         case 4: spmv_kernel<PL, 4><<<blocks, 256, 0, s>>>(A->nrows, A->d_ia, A->d_ja, val, x, y, mode, b, wdot, partial, sc); break;
         case 8: spmv_kernel<PL, 8><<<blocks, 256, 0, s>>>(A->nrows, A->d_ia, A->d_ja, val, x, y, mode, b, wdot, partial, sc); break;
         case 16: spmv_kernel<PL, 16><<<blocks, 256, 0, s>>>(A->nrows, A->d_ia, A->d_ja, val, x, y, mode, b, wdot, partial, sc); break;
@@ -80,6 +81,13 @@ static int spmv_blocks_uncapped(const fgpu_matrix* A, int G) {
     return (int)std::max<int64_t>(1, (A->nrows + (256 / G) - 1) / (256 / G));
 }
 
+// lanes per row of y = A x: two for rows of up to 40 entries (one FP64 shuffle-add per lane; P2 64^3:
+// 0.36 against 0.40 ms with four), else as in the solver
+static int mult_group(const fgpu_matrix* A) {
+    const double avg = A->nrows ? (double)A->nnz / (double)A->nrows : 1.0;
+    return avg <= 40 ? 2 : spmv_group(A);
+}
+
 
 int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y, double alpha_b, const double* b) {
     (void)alpha_b;
@@ -87,7 +95,7 @@ int launch_spmv(fgpu_ctx* ctx, const fgpu_matrix* A, const double* x, double* y,
         ctx->err = "y = A x with binary64 vectors needs an FP64 matrix";
         return FGPU_ERR_INVALID;
     }
-    const int G = spmv_group(A);
+    const int G = mult_group(A);
     PendingEvent ev;
     prof_begin(ctx, "spmv", ev);
     launch_spmv_t<PolF64>(ctx->stream, A, (const double*)A->d_val, G, x, y, b ? 1 : 0, b, nullptr, nullptr, nullptr,
