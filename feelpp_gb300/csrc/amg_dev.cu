@@ -1026,8 +1026,9 @@ int level_dev(fgpu_ctx* ctx, AmgDevLevel& L, const AmgHostCfg& cfg, const AmgNns
     // the graph to aggregate: the symmetrised dof graph S + S^T, or (near null space) its node graph,
     // formed as N(S) + N(S)^T (the same sorted rows as N(S + S^T): a node pair is coupled when any of
     // their dofs are, in either direction), which symmetrises the node graph instead of the nine-times
-    // larger dof graph of a 3-component operator (vector P2 48^3 beam: graph phase 113 -> 54 ms, set-up
-    // 750 -> 705 ms; the Lanczos estimate on its own stream now overlaps the aggregation instead)
+    // larger dof graph of a 3-component operator (vector P2 48^3 beam, the set-up run alone: graph phase
+    // 113 -> 54 ms, set-up 750 -> 705 ms, the Lanczos estimate on its own stream now overlapping the
+    // aggregation; after the other solves of the elasticity workload 742 ms)
     int64_t ng = n;
     const uint32_t* gp = tp;
     const int32_t* gjs = tmpj;
