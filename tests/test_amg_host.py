@@ -191,3 +191,34 @@ def test_rigid_body_near_null_space(fgpu_lib, oracle):
             assert abs(A - G).max() <= 1e-12 * abs(G).max()
         prev = (A, P)
     assert H.nlevels() >= 2
+
+
+@pytest.mark.parametrize("seed,nodes,bs,density", [(0, 40, 3, 0.05), (1, 25, 2, 0.2), (2, 60, 3, 0.01)])
+def test_node_graph_of_symmetrised_graph(seed, nodes, bs, density):
+    """The device set-up of a level with a near null space symmetrises the node graph of the strength
+    graph, N(S) + N(S)^T, instead of taking the node graph of the symmetrised dof graph, N(S + S^T): the
+    two are the same sorted node rows (a node pair is coupled when some dof pair of theirs is, in
+    either direction). Checked on random non-symmetric dof graphs with bs dofs per node."""
+    rng = np.random.default_rng(seed)
+    n = nodes * bs
+    S = sp.random(n, n, density=density, random_state=rng, format="csr")
+    S.data[:] = 1.0
+    S.setdiag(0.0)
+    S.eliminate_zeros()
+    node = np.arange(n) // bs
+    inc = sp.csr_matrix((np.ones(n), (node, np.arange(n))), shape=(nodes, n))   # node x dof incidence
+
+    def node_graph(G):
+        N = (inc @ G @ inc.T).tocsr()
+        N.setdiag(0.0)
+        N.eliminate_zeros()
+        N.data[:] = 1.0
+        N.sort_indices()
+        return N
+
+    a = node_graph(S + S.T)
+    NS = node_graph(S)
+    b = (NS + NS.T).tocsr()
+    b.data[:] = 1.0
+    b.sort_indices()
+    assert np.array_equal(a.indptr, b.indptr) and np.array_equal(a.indices, b.indices)
